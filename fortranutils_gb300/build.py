@@ -1,0 +1,88 @@
+"""Build the GB300 library liblester_gpu.so in-tree with nvcc (sm_103a).
+
+The exact FP64 translation units are compiled with ``-fmad=false`` so that
+every product and sum is rounded separately, as in the reference's FP64
+Fortran; the fast multigrid unit keeps FMA contraction.  Objects go to
+``fortranutils_gb300/_build``; the shared library to
+``fortranutils_gb300/_lib``.  Sources compile in parallel.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIBDIR = PKG / "_lib"
+LIBNAME = "liblester_gpu.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+          "-I", str(PKG.parent / "include")]
+# translation unit -> extra flags
+UNITS = {
+    "lester_host.cu": [],
+    "k_exact.cu": ["-fmad=false"],
+    "k_metric.cu": ["-fmad=false"],
+    "k_sgs.cu": ["-fmad=false"],
+    "k_fast.cu": [],
+}
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc")
+    if exe:
+        return exe
+    cand = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(cand):
+        return cand
+    raise RuntimeError("nvcc not found")
+
+
+def lib_path() -> Path:
+    return LIBDIR / LIBNAME
+
+
+def _compile(src: str, extra: list[str], verbose: bool) -> Path:
+    obj = BUILD / (Path(src).stem + ".o")
+    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+    if verbose:
+        cmd.insert(1, "-Xptxas=-v")
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{res.stdout}\n{res.stderr}")
+    if verbose and res.stderr:
+        sys.stderr.write(res.stderr)
+    return obj
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile every CUDA unit for sm_103a and link the shared library."""
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    out = lib_path()
+    srcs = [CSRC / s for s in UNITS] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
+    srcs.append(PKG.parent / "include" / "lester_gpu.h")
+    if out.exists() and not force:
+        newest = max(p.stat().st_mtime for p in srcs)
+        if out.stat().st_mtime >= newest:
+            return out
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        futs = [ex.submit(_compile, s, f, verbose) for s, f in UNITS.items()]
+        objs = [f.result() for f in futs]
+    tmp = out.with_suffix(".so.tmp")
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, out)
+    return out
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,94 @@
+// k_common.cuh -- device-side descriptors and helpers shared by the kernels.
+//
+// Layout in HBM is the reference arena's: one FP64 array per field, blocks
+// back to back, each block in Fortran order (i fastest) including one ghost
+// layer per side; multigrid fields hold every level, level after level
+// (code/set_offset.F:166-234).  A kernel that works on every block of a
+// level takes the level's BlkDev table and runs a 2-D grid:
+// gridDim.y = block, gridDim.x covers that block's points.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define LES_BCT_WALL_D 1
+#define LES_BCT_ZERO_GRAD_D 2
+#define LES_BCT_TRACTION_D 6
+#define LES_BCT_PERIODIC_D 12
+#define LES_BCT_INTERFACE_D 13
+
+struct BlkDev {
+    int n[3];      // nip1, njp1, nkp1 (points incl. ghosts)
+    int bc[6];     // W E S N L R
+    int mult[3];   // coarsening factor to the next level (1 or 2)
+    long off3;     // 0-based start of this block in a 3-D field at this level
+    long off2;     // 0-based start in a 2-D (i,j) metric at this level
+    long off1k;    // 0-based start in a 1-D k metric at this level
+    long ncell;    // interior points (nip1-2)(njp1-2)(nkp1-2)
+};
+
+// One periodic/interface face of swap_sc (code/swap_sc0.F:92-133 and
+// 239-283).  Own pack plane = first interior plane of (block, side); own
+// ghost plane receives the partner face's pack plane.  Positions are 0-based
+// indices into the 3-D field, strides are the in-plane (j, k) strides.
+struct FaceDev {
+    long pk, gh, jo, ko;      // own pack plane, own ghost plane, strides
+    long ppk, pjo, pko;       // partner pack plane and its strides
+    int nj, nk;               // plane size (equal on both sides)
+    long woff, pwoff;         // own and partner slot in the pack buffer
+    int skip;                 // edge rows a later side of this block rewrites:
+                              // 1 = j first, 2 = j last, 4 = k first, 8 = k last
+};
+
+// true if in-plane element (j, k) (0-based) of face f is rewritten later by
+// another side of the same block, so this face must leave it alone
+__device__ __forceinline__ bool face_skips(const FaceDev &f, long j, long k)
+{
+    return ((f.skip & 1) && j == 0) || ((f.skip & 2) && j == f.nj - 1) ||
+           ((f.skip & 4) && k == 0) || ((f.skip & 8) && k == f.nk - 1);
+}
+
+__device__ __forceinline__ bool is_per_or_int(int bc)
+{
+    return bc == LES_BCT_PERIODIC_D || bc == LES_BCT_INTERFACE_D;
+}
+
+// interior point number q -> (i, j, k) 1-based and 0-based field index
+__device__ __forceinline__ long decode_interior(const BlkDev &b, long q, int &i,
+                                                int &j, int &k)
+{
+    int ni = b.n[0] - 2, nj = b.n[1] - 2;
+    long t = q / ni;
+    i = (int)(q - t * ni) + 2;
+    long t2 = t / nj;
+    j = (int)(t - t2 * nj) + 2;
+    k = (int)t2 + 2;
+    return b.off3 + (i - 1) + (long)b.n[0] * ((j - 1) + (long)b.n[1] * (k - 1));
+}
+
+// Deterministic block reduction of NV doubles: warp shuffles in a fixed
+// pattern, then warp 0 combines the per-warp sums in warp order.
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
+{
+    __shared__ double sm[32][NV];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+        double x = v[q];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        v[q] = x;
+    }
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) sm[wid][q] = v[q];
+    __syncthreads();
+    if (wid == 0) {
+        int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double x = lane < nw ? sm[lane][q] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) out[q] = x;
+        }
+    }
+}

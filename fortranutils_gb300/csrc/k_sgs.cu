@@ -1,0 +1,150 @@
+// k_sgs.cu -- eddy-viscosity kernels (FP64, -fmad=false), one thread per
+// interior point of every block.
+//
+// subgrid (code/subgrid.F:58-92) dispatches on the model:
+//   Smagorinsky  code/subgrid_smagorinsky.F:85-237
+//   WALE         code/subgrid_wale.F:73-239 (the reference's scalar Sd)
+//   none         code/subgrid_nosgs.F (gam = gamsc1 = 0)
+// The staggered-grid gradients are the reference's face/edge averages.  The
+// filter width uses the reference's literal exponent 0.33333333.  pow() is
+// CUDA's and may differ from a CPU libm in the last bit; everything else is
+// operation-for-operation.
+#include "k_common.cuh"
+#include "kernels.h"
+
+#define IDX2(b, i, j) ((b).off2 + ((i) - 1) + (long)(b).n[0] * ((j) - 1))
+
+__global__ void __launch_bounds__(128) k_subgrid(
+    const BlkDev *__restrict__ blk, int model, double csles, int gotrad,
+    double *__restrict__ gam, double *__restrict__ gamsc1, const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, const double *__restrict__ sc1,
+    double *__restrict__ sc1var, double *__restrict__ sc1dis, const double *__restrict__ vdd,
+    const double *__restrict__ dip, const double *__restrict__ diu, const double *__restrict__ djp,
+    const double *__restrict__ djv, const double *__restrict__ dkp, const double *__restrict__ dkw,
+    const double *__restrict__ hijp, const double *__restrict__ hjip,
+    const double *__restrict__ hkip, const double *__restrict__ hkjp, const double *__restrict__ rp)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    long ijk = decode_interior(b, q, i, j, k);
+    if (model == 0) {
+        gam[ijk] = 0.0;
+        gamsc1[ijk] = 0.0;
+        sc1var[ijk] = 0.0;
+        sc1dis[ijk] = 0.0;
+        return;
+    }
+    const double sct = 0.3, cfv = 0.1;
+    long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    long ijkw = ijk - 1, ijke = ijk + 1, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko,
+         ijkr = ijk + ko;
+    long ijkse = ijks + 1, ijknw = ijkn - 1, ijkne = ijkn + 1, ijkel = ijke - ko, ijknl = ijkn - ko,
+         ijkwr = ijkw + ko, ijker = ijke + ko, ijksr = ijks + ko, ijknr = ijkn + ko;
+    long ij = IDX2(b, i, j);
+    double dkwk = dkw[b.off1k + k - 1], dkpk = dkp[b.off1k + k - 1];
+
+    double fwf = 0.5 * (sc1[ijk] + sc1[ijkw]);
+    double fef = 0.5 * (sc1[ijk] + sc1[ijke]);
+    double fsf = 0.5 * (sc1[ijk] + sc1[ijks]);
+    double fnf = 0.5 * (sc1[ijk] + sc1[ijkn]);
+    double flf = 0.5 * (sc1[ijk] + sc1[ijkl]);
+    double frf = 0.5 * (sc1[ijk] + sc1[ijkr]);
+    double dfdip = (fef - fwf) / dip[ij];
+    double dfdjp = (fnf - fsf) / djp[ij];
+    double dfdkp = (frf - flf) / (rp[ij] * dkwk);
+
+    double up = 0.5 * (u[ijk] + u[ijke]);
+    double vp = 0.5 * (v[ijk] + v[ijkn]);
+    double di = dip[ij], dj = djp[ij], dk;
+    double vwf = 0.25 * (v[ijk] + v[ijkn] + v[ijkw] + v[ijknw]);
+    double vef = 0.25 * (v[ijk] + v[ijkn] + v[ijke] + v[ijkne]);
+    double usf = 0.25 * (u[ijk] + u[ijke] + u[ijks] + u[ijkse]);
+    double unf = 0.25 * (u[ijk] + u[ijke] + u[ijkn] + u[ijkne]);
+    double ulf = 0.25 * (u[ijk] + u[ijke] + u[ijkl] + u[ijkel]);
+    double urf = 0.25 * (u[ijk] + u[ijke] + u[ijkr] + u[ijker]);
+    double vlf = 0.25 * (v[ijk] + v[ijkn] + v[ijkl] + v[ijknl]);
+    double vrf = 0.25 * (v[ijk] + v[ijkn] + v[ijkr] + v[ijknr]);
+
+    double dudi = (u[ijke] - u[ijk]) / di + vp * hijp[ij];
+    double dvdi = (vef - vwf) / di - up * hijp[ij];
+    double dudj = (unf - usf) / dj - vp * hjip[ij];
+    double dvdj = (v[ijkn] - v[ijk]) / dj + up * hjip[ij];
+    double dwdi, dwdj, dudk, dvdk, dwdk;
+    if (gotrad) {
+        long jn = b.n[0];
+        double radp = rp[ij], radw = rp[ij - 1], rade = rp[ij + 1], rads = rp[ij - jn],
+               radn = rp[ij + jn];
+        dk = radp * dkpk;
+        double hki = hkip[ij], hkj = hkjp[ij];
+        double wdrw = 0.5 * (w[ijkw] + w[ijkwr]) / radw;
+        double wdre = 0.5 * (w[ijke] + w[ijker]) / rade;
+        double wdrs = 0.5 * (w[ijks] + w[ijksr]) / rads;
+        double wdrn = 0.5 * (w[ijkn] + w[ijknr]) / radn;
+        dwdi = radp * (wdre - wdrw) / (diu[ij] + diu[ij + 1]);
+        dwdj = radp * (wdrn - wdrs) / (djv[ij] + djv[ij + jn]);
+        double wp = 0.5 * (w[ijk] + w[ijkr]);
+        dudk = (urf - ulf) / dk - wp * hki;
+        dvdk = (vrf - vlf) / dk - wp * hkj;
+        dwdk = (w[ijkr] - w[ijk]) / dk + up * hki + vp * hkj;
+    } else {
+        dk = dkpk;
+        double wwf = 0.25 * (w[ijk] + w[ijkr] + w[ijkw] + w[ijkwr]);
+        double wef = 0.25 * (w[ijk] + w[ijkr] + w[ijke] + w[ijker]);
+        double wsf = 0.25 * (w[ijk] + w[ijkr] + w[ijks] + w[ijksr]);
+        double wnf = 0.25 * (w[ijk] + w[ijkr] + w[ijkn] + w[ijknr]);
+        dwdi = (wef - wwf) / di;
+        dwdj = (wnf - wsf) / dj;
+        dudk = (urf - ulf) / dk;
+        dvdk = (vrf - vlf) / dk;
+        dwdk = (w[ijkr] - w[ijk]) / dk;
+    }
+    double sijsij = dvdj * dvdj + dwdk * dwdk + dudi * dudi +
+                    0.5 * ((dudj + dvdi) * (dudj + dvdi) + (dvdk + dwdj) * (dvdk + dwdj) +
+                           (dudk + dwdi) * (dudk + dwdi));
+    double delta_xyz = pow(di * dj * dk, .33333333);
+    double g;
+    if (model == 1) {
+        double evisc = csles * delta_xyz * vdd[ijk];
+        g = evisc * evisc * sqrt(2.0 * sijsij);
+    } else {
+        double g11 = dudi * dudi + dudj * dvdi + dudk * dwdi;
+        double g22 = dvdi * dudj + dvdj * dvdj + dvdk * dwdj;
+        double g33 = dwdi * dudk + dwdj * dvdk + dwdk * dwdk;
+        double g12 = dudi * dudj + dudj * dvdj + dudk * dwdj;
+        double g13 = dudi * dudk + dudj * dvdk + dudk * dwdk;
+        double g21 = dvdi * dudi + dvdj * dvdi + dvdk * dwdi;
+        double g23 = dvdi * dudk + dvdj * dvdk + dvdk * dwdk;
+        double g31 = dwdi * dudi + dwdj * dvdi + dwdk * dwdi;
+        double g32 = dwdi * dudj + dwdj * dvdj + dwdk * dwdj;
+        double tracet = (1.0 / 3.0) * (g11 + g22 + g33);
+        double sdij = (g11 - tracet) + (g22 - tracet) + (g33 - tracet) + 0.5 * (g12 + g21) +
+                      0.5 * (g13 + g31) + 0.5 * (g23 + g32);
+        double sd2 = sdij * sdij;
+        double ev = (csles * delta_xyz) * (csles * delta_xyz);
+        g = ev * (pow(sd2, 1.5) / (pow(sijsij, 2.5) + pow(sd2, 1.25)));
+    }
+    gam[ijk] = g;
+    gamsc1[ijk] = (csles == 0.0) ? 0.0 : g / sct;
+    double dfdijk = dfdip * dfdip + dfdjp * dfdjp + dfdkp * dfdkp;
+    double sv = cfv * dfdijk * (delta_xyz * delta_xyz);
+    sc1var[ijk] = sv;
+    sc1dis[ijk] = sv * sqrt(2.0 * sijsij);
+}
+
+namespace les {
+
+void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,
+                    double *gam, double *gamsc1, const double *u, const double *v, const double *w,
+                    const double *sc1, double *sc1var, double *sc1dis, const double *vdd,
+                    const double *const *m, cudaStream_t st)
+{
+    // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
+    k_subgrid<<<dim3((unsigned)((maxcell + 127) / 128), nb), 128, 0, st>>>(
+        blk, model, csles, gotrad, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m[0], m[1], m[2],
+        m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10]);
+    count_launch(1);
+}
+
+} // namespace les

@@ -1,0 +1,90 @@
+// kernels.h -- host-side launchers of the device kernels (one namespace,
+// all asynchronous on the given stream).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include "k_common.cuh"
+
+namespace les {
+
+// running count of kernel launches made by this library
+void count_launch(long n);
+
+// k_exact.cu
+void launch_halo(const FaceDev *faces, int nface, long maxface, double *var, double *work,
+                 cudaStream_t st);
+void launch_coeff_p(const BlkDev *blk, int nb, long maxcell, const double *const *m,
+                    const double *dkp, const double *dkw, double *const *a, cudaStream_t st);
+void launch_sour_p(const BlkDev *blk, int nb, long maxcell, double dtime, const double *rdiv,
+                   const double *rdju, const double *didjp, const double *dkp,
+                   const double *rdidjp, const double *dkw, const double *u, const double *v,
+                   const double *w, const double *rho, const double *rhonp1, double *drhodt,
+                   double *s, double *srhot, double *srhoux, cudaStream_t st);
+long norms_parts(int nb, long maxcell);
+void launch_norms(const BlkDev *blk, int nb, long maxcell, const double *const *a, const double *x,
+                  const double *b, double *residu, double *partial, double rnpts, double *out,
+                  cudaStream_t st);
+void launch_lex_pass(const BlkDev *blk, int nb, int maxjk, int smin, int smax, int dir,
+                     double omega, const double *const *a, double *f, const double *src,
+                     double *nrm3, int want_norm, cudaStream_t st);
+void launch_lex_norm(const BlkDev *blk, int nb, long maxcell, const double *nrm3, double *partial,
+                     double rnpts, double *out, cudaStream_t st);
+void launch_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const double *ff,
+                     double *fc, cudaStream_t st);
+void launch_prolong(const BlkDev *bc, const BlkDev *bf, int nb, long maxfine, double *f,
+                    cudaStream_t st);
+void launch_extrap_p(const BlkDev *blk, int nb, double *p, cudaStream_t st);
+void launch_pref(const BlkDev *blk, double *p, long n, double *scratch, cudaStream_t st);
+void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dtime,
+                    const double *dg, const double *rp, const double *dkw, double *u,
+                    const double *u_int, const double *rho, const double *p, cudaStream_t st);
+void launch_swap_rhos(double *rho, const double *rhonp1, double *rhonm1, long n, cudaStream_t st);
+void launch_search_lib(double *sc1, double *rhonp1, const double *rho, double alpha, double rholo,
+                       double rhohi, long n, cudaStream_t st);
+void launch_slipbc(const BlkDev *blk, int nb, long maxik, double dtime, const double *djp,
+                   double *u, double *v, const double *v_int, double *w, double *sc1,
+                   double *rho, const double *p, cudaStream_t st);
+
+// k_metric.cu
+void launch_metric(const void *metblk, int nb, long maxij, long maxk, const double *x,
+                   const double *y, const double *z, double *const *m, double *dkp, double *dkw,
+                   int gotrad, cudaStream_t st);
+void launch_metric_swap(const void *faces, int nf, long maxlen, double *const *m, double *dkp,
+                        double *dkw, double *buf, long slot, int phase, cudaStream_t st);
+size_t metblk_size();
+size_t metface_size();
+void fill_metblk(void *dst, int idx, const int *n, long off2, long off1k, long offxy, long offz);
+void fill_metface(void *dst, int idx, long src2, long dst2, long stride, int len, long srck,
+                  long dstk);
+
+// k_sgs.cu
+void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,
+                    double *gam, double *gamsc1, const double *u, const double *v, const double *w,
+                    const double *sc1, double *sc1var, double *sc1dis, const double *vdd,
+                    const double *const *m, cudaStream_t st);
+
+// k_fast.cu (T = float or double)
+template <typename T>
+int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *const *a, T *E, T *N,
+                     T *R, T *D, double *E64, double *N64, double *R64, double *P64, int *bad,
+                     cudaStream_t st);
+template <typename T>
+void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
+               const T *N, const T *R, const T *D, T *x, const T *b, cudaStream_t st);
+template <typename T>
+void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
+                           const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
+                           cudaStream_t st);
+template <typename T>
+void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
+                         T *xf, cudaStream_t st);
+template <typename T>
+void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
+template <typename T>
+void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
+                        const double *R, const double *P, const double *x, const double *b, T *rT,
+                        double *partial, double *out2, cudaStream_t st);
+template <typename T>
+void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st);
+
+} // namespace les

@@ -1,0 +1,117 @@
+// lester_ctx.h -- host-side state of the library (what the reference keeps
+// in COMMON blocks) and helpers shared by the host translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include <vector>
+#include "../../include/lester_gpu.h"
+#include "k_common.cuh"
+
+namespace les {
+
+struct LevelGeom {
+    int n[LES_MAXBL + 1][3];
+    int mult[LES_MAXBL + 1][3];
+    long off3[LES_MAXBL + 1], off2[LES_MAXBL + 1], off1k[LES_MAXBL + 1];
+    long offxy[LES_MAXBL + 1], offz[LES_MAXBL + 1];
+    long maxcell, maxjk, maxhalf, maxfine, maxik, maxface, maxij, maxk;
+    long start3, len3;     // contiguous range of this level in a 3-D mg field
+    double npts_all;       // interior points, pressure loop bounds (set_loop_bound.F:364)
+    BlkDev *d_blk = nullptr;
+    FaceDev *d_face = nullptr;
+    int nface = 0;
+    long worklen = 0;
+    void *d_metblk = nullptr;
+    void *d_metface[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int nmetface[6] = {0, 0, 0, 0, 0, 0};
+    long maxmetlen = 0;
+};
+
+// device buffers of the fast solvers, precision T
+template <typename T> struct FastSet {
+    T *E = nullptr, *N = nullptr, *R = nullptr, *D = nullptr, *x = nullptr, *b = nullptr;
+};
+
+struct Ctx {
+    lester_geom g;
+    lester_ctrl c;
+    int nummgl = 0;
+    LevelGeom lv[LES_MAXMGL + 1];
+    long tot3 = 0, tot_sg3 = 0, tot2 = 0, tot1k = 0, totxy = 0, totz = 0, totki = 0, totjk = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int jumble = 0;
+    // scratch
+    double *d_work = nullptr;       // swap pack buffer
+    double *d_partial = nullptr;    // reduction partials
+    long npartial = 0;
+    double *d_small = nullptr;      // small results (norms, p_ref)
+    double *h_small = nullptr;      // pinned mirror
+    double *d_nrm3 = nullptr;       // per-point SOR norm terms (reference smoother)
+    double *d_metbuf = nullptr;
+    long metslot = 0;
+    long metmaxf = 0;
+    int *d_flag = nullptr;
+    // fast solvers
+    FastSet<float> f32;
+    FastSet<double> f64;
+    double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
+    const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
+    long coef_gen_seen = -1;
+    int coef_prec = -1;
+    long coef_gen = 0;
+    // staging buffers for host arguments
+    std::vector<void *> stage_buf;
+    std::vector<size_t> stage_cap;
+    // last solve statistics
+    double last_norms[4] = {0, 0, 0, 0};
+    int last_cycles = 0;
+    double last_relres = 0;
+};
+
+extern Ctx *g_ctx;
+extern std::string g_err;
+int set_err(int code, const char *fmt, ...);
+
+#define LES_CUDA(call)                                                                             \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return les::set_err(LES_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,          \
+                                cudaGetErrorString(e_));                                           \
+    } while (0)
+
+#define LES_NEED_CTX()                                                                             \
+    do {                                                                                           \
+        if (!les::g_ctx) return les::set_err(LES_ERR_NOT_INIT, "lester_gpu_init not called");      \
+    } while (0)
+
+// Maps the pointers of one entry-point call to device memory: device
+// pointers pass through, host arrays are copied to library-owned device
+// buffers and, for outputs, copied back by finish().
+class Staging {
+  public:
+    explicit Staging(Ctx *c) : c_(c) {}
+    ~Staging();
+    // in: read only; io: read and written
+    int in(const double *user, long n, const double **dev);
+    int io(double *user, long n, double **dev);
+    int finish();  // copies outputs back and synchronises if anything was staged
+    bool any_host() const { return any_host_; }
+
+  private:
+    int map(const double *user, long n, bool out, double **dev);
+    Ctx *c_;
+    struct Ent {
+        const double *user;
+        double *dev;
+        long n;
+        bool out;
+        bool host;
+    };
+    std::vector<Ent> ent_;
+    int slot_ = 0;
+    bool any_host_ = false;
+};
+
+} // namespace les

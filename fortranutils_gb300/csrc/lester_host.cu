@@ -1,0 +1,1197 @@
+// lester_host.cu -- C ABI entry points (include/lester_gpu.h): geometry
+// tables, argument staging, and the host control of every routine.
+//
+// The host side plays the role of the reference's driver-side bookkeeping:
+// set_offset (code/set_offset.F:8-263), set_interfaces
+// (code/set_interfaces.F:6-256) and set_loop_bound (code/set_loop_bound.F)
+// become device tables built once in lester_gpu_init; the multigrid state
+// machine of lmg_solve (code/lmg_solve.F:82-157) and the control of smooth
+// and sporlx run here and launch kernels.
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "kernels.h"
+#include "lester_ctx.h"
+
+namespace les {
+
+Ctx *g_ctx = nullptr;
+std::string g_err;
+static std::atomic<long> g_launches(0);
+
+void count_launch(long n) { g_launches += n; }
+
+int set_err(int code, const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+// ------------------------------------------------------------------ staging
+Staging::~Staging() {}
+
+int Staging::map(const double *user, long n, bool out, double **dev)
+{
+    if (!user) {
+        *dev = nullptr;
+        return 0;
+    }
+    for (auto &e : ent_)
+        if (e.user == user) {
+            if (e.n < n) return set_err(LES_ERR_ARG, "one array passed twice with different sizes");
+            e.out = e.out || out;
+            *dev = e.dev;
+            return 0;
+        }
+    cudaPointerAttributes at;
+    cudaError_t er = cudaPointerGetAttributes(&at, user);
+    if (er != cudaSuccess) {
+        cudaGetLastError();
+        at.type = cudaMemoryTypeUnregistered;
+    }
+    Ent e{user, nullptr, n, out, false};
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        e.dev = const_cast<double *>(user);
+    } else {
+        e.host = true;
+        any_host_ = true;
+        int s = slot_++;
+        if ((int)c_->stage_buf.size() <= s) {
+            c_->stage_buf.push_back(nullptr);
+            c_->stage_cap.push_back(0);
+        }
+        size_t bytes = (size_t)n * sizeof(double);
+        if (c_->stage_cap[s] < bytes) {
+            if (c_->stage_buf[s]) cudaFree(c_->stage_buf[s]);
+            c_->stage_buf[s] = nullptr;
+            c_->stage_cap[s] = 0;
+            if (cudaMalloc(&c_->stage_buf[s], bytes) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(LES_ERR_NOMEM, "staging allocation of %zu bytes failed", bytes);
+            }
+            c_->stage_cap[s] = bytes;
+        }
+        e.dev = (double *)c_->stage_buf[s];
+        LES_CUDA(cudaMemcpyAsync(e.dev, user, bytes, cudaMemcpyHostToDevice, c_->stream));
+    }
+    ent_.push_back(e);
+    *dev = e.dev;
+    return 0;
+}
+
+int Staging::in(const double *user, long n, const double **dev)
+{
+    double *d;
+    int r = map(user, n, false, &d);
+    *dev = d;
+    return r;
+}
+
+int Staging::io(double *user, long n, double **dev) { return map(user, n, true, dev); }
+
+int Staging::finish()
+{
+    if (!any_host_) {
+        LES_CUDA(cudaGetLastError());
+        return 0;
+    }
+    for (auto &e : ent_)
+        if (e.host && e.out)
+            LES_CUDA(cudaMemcpyAsync(const_cast<double *>(e.user), e.dev, (size_t)e.n * sizeof(double),
+                                     cudaMemcpyDeviceToHost, c_->stream));
+    LES_CUDA(cudaStreamSynchronize(c_->stream));
+    return 0;
+}
+
+// ------------------------------------------------------------- geometry
+static bool per_int(int bc) { return bc == LES_BCT_PERIODIC || bc == LES_BCT_INTERFACE; }
+
+// level search and offsets, code/set_offset.F:94-234
+static int build_levels(Ctx &c)
+{
+    const lester_geom &g = c.g;
+    int nb = g.numbl;
+    for (int b = 1; b <= nb; b++)
+        for (int d = 0; d < 3; d++) {
+            c.lv[1].n[b][d] = g.bl_nijkp1[b - 1][d];
+            if (c.lv[1].n[b][d] < 3)
+                return set_err(LES_ERR_GEOM, "block %d axis %d has fewer than 3 points", b, d + 1);
+        }
+    int found = 1;
+    int cap = g.maxmgl > 0 ? g.maxmgl : 3;
+    if (cap > LES_MAXMGL) cap = LES_MAXMGL;
+    for (int lev = 1; lev <= cap - 1; lev++) {
+        bool coarser = true;
+        for (int b = 1; b <= nb && coarser; b++) {
+            int *n = c.lv[lev].n[b];
+            if (n[0] % 2 == 0 && n[1] % 2 == 0 && n[2] % 2 == 0) {
+                int m0 = n[0] / 2 + 1, m1 = n[1] / 2 + 1, m2 = n[2] / 2 + 1;
+                if (m0 >= 4 && m1 >= 4 && m2 >= 4) {
+                    c.lv[lev + 1].n[b][0] = m0;
+                    c.lv[lev + 1].n[b][1] = m1;
+                    c.lv[lev + 1].n[b][2] = m2;
+                } else
+                    coarser = false;
+            } else
+                coarser = false;
+        }
+        if (!coarser) break;
+        found = lev + 1;
+    }
+    if (g.nummgl == 0)
+        c.nummgl = found;
+    else if (g.nummgl <= found && g.nummgl > 0)
+        c.nummgl = g.nummgl;
+    else
+        return set_err(LES_ERR_GEOM, "levels found %d but required %d", found, g.nummgl);
+    long o3 = 0, o2 = 0, o1 = 0, oxy = 0, oz = 0, oki = 0, ojk = 0;
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        LevelGeom &L = c.lv[lev];
+        L.start3 = o3;
+        L.maxcell = L.maxjk = L.maxhalf = L.maxfine = L.maxik = L.maxij = L.maxk = 0;
+        double npts = 0;
+        for (int b = 1; b <= nb; b++) {
+            int *n = L.n[b];
+            L.off3[b] = o3;
+            L.off2[b] = o2;
+            L.off1k[b] = o1;
+            L.offxy[b] = oxy;
+            L.offz[b] = oz;
+            o3 += (long)n[0] * n[1] * n[2];
+            o2 += (long)n[0] * n[1];
+            o1 += n[2];
+            oxy += (long)(n[0] + 1) * (n[1] + 1);
+            oz += n[2] + 1;
+            if (lev == 1) {
+                oki += (long)n[2] * n[0];
+                ojk += (long)n[1] * n[2];
+            }
+            long nc = (long)(n[0] - 2) * (n[1] - 2) * (n[2] - 2);
+            L.maxcell = std::max(L.maxcell, nc);
+            L.maxjk = std::max(L.maxjk, (long)(n[1] - 2) * (n[2] - 2));
+            L.maxhalf = std::max(L.maxhalf, (long)((n[0] - 1) / 2) * (n[1] - 2) * (n[2] - 2));
+            L.maxfine = std::max(L.maxfine, (long)n[0] * n[1] * n[2]);
+            L.maxik = std::max(L.maxik, (long)n[0] * (n[2] - 2));
+            L.maxij = std::max(L.maxij, (long)n[0] * n[1]);
+            L.maxk = std::max(L.maxk, (long)n[2]);
+            npts += (double)(n[0] - 2) * (double)(n[1] - 2) * (double)(n[2] - 2);
+        }
+        L.npts_all = npts;
+        L.len3 = o3 - L.start3;
+        if (lev == 1) {
+            c.tot_sg3 = o3;
+            c.totki = oki;
+            c.totjk = ojk;
+        }
+    }
+    c.tot3 = o3;
+    c.tot2 = o2;
+    c.tot1k = o1;
+    c.totxy = oxy;
+    c.totz = oz;
+    for (int lev = 1; lev < c.nummgl; lev++)
+        for (int b = 1; b <= nb; b++)
+            for (int d = 0; d < 3; d++)
+                c.lv[lev].mult[b][d] = (c.lv[lev].n[b][d] == c.lv[lev + 1].n[b][d]) ? 1 : 2;
+    for (int b = 1; b <= nb; b++)
+        for (int d = 0; d < 3; d++) c.lv[c.nummgl].mult[b][d] = 2;
+    return 0;
+}
+
+// cyclic of code/set_const.F:16-21: the in-plane axes of a face on axis d1
+static const int kCyc[2][4] = {{0, 2, 3, 1}, {0, 3, 1, 2}};
+
+// face tables of code/set_interfaces.F:415-500 for every level
+static int build_faces(Ctx &c)
+{
+    const lester_geom &g = c.g;
+    int nb = g.numbl;
+    long maxwork = 0;
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        LevelGeom &L = c.lv[lev];
+        std::vector<FaceDev> fv;
+        long slot[LES_MAXBL + 1][6];
+        long w = 0;
+        // own pack-plane descriptors first (one slot per face)
+        for (int b = 1; b <= nb; b++)
+            for (int s = 1; s <= 6; s++) {
+                slot[b][s - 1] = -1;
+                if (!per_int(g.bl_bc[b - 1][s - 1])) continue;
+                int bn = g.bl2bl[b - 1][s - 1], sn = g.bl2side[b - 1][s - 1];
+                if (bn < 1 || bn > nb || sn < 1 || sn > 6)
+                    return set_err(LES_ERR_GEOM, "block %d side %d: bad neighbour link", b, s);
+                if ((s % 2) == (sn % 2))
+                    return set_err(LES_ERR_GEOM, "interface coupling invalid: bl %d side %d with bl %d side %d",
+                                   b, s, bn, sn);
+                if (!per_int(g.bl_bc[bn - 1][sn - 1]))
+                    return set_err(LES_ERR_GEOM, "block %d side %d links to a side that is not periodic/interface", b, s);
+                int d1 = (s + 1) / 2, d2 = kCyc[0][d1], d3 = kCyc[1][d1];
+                int dn1 = (sn + 1) / 2, dn2 = kCyc[0][dn1], dn3 = kCyc[1][dn1];
+                int *n = L.n[b], *m = L.n[bn];
+                if (n[d2 - 1] != m[dn2 - 1] || n[d3 - 1] != m[dn3 - 1])
+                    return set_err(LES_ERR_GEOM, "block %d face %d to block %d face %d mismatch", b, s, bn, sn);
+                slot[b][s - 1] = w;
+                w += (long)n[d2 - 1] * n[d3 - 1] + 1;
+            }
+        for (int b = 1; b <= nb; b++)
+            for (int s = 1; s <= 6; s++) {
+                if (slot[b][s - 1] < 0) continue;
+                int bn = g.bl2bl[b - 1][s - 1], sn = g.bl2side[b - 1][s - 1];
+                int d1 = (s + 1) / 2, d2 = kCyc[0][d1], d3 = kCyc[1][d1];
+                int *n = L.n[b];
+                long st[4] = {0, 1, n[0], (long)n[0] * n[1]};
+                FaceDev f;
+                long ipk = (s % 2 == 0) ? n[d1 - 1] - 2 : 1;  // 0-based first interior plane
+                long igh = (s % 2 == 0) ? n[d1 - 1] - 1 : 0;  // 0-based ghost plane
+                f.pk = L.off3[b] + st[d1] * ipk;
+                f.gh = L.off3[b] + st[d1] * igh;
+                f.jo = st[d2];
+                f.ko = st[d3];
+                f.nj = n[d2 - 1];
+                f.nk = n[d3 - 1];
+                int dn1 = (sn + 1) / 2, dn2 = kCyc[0][dn1], dn3 = kCyc[1][dn1];
+                int *m = L.n[bn];
+                long sm[4] = {0, 1, m[0], (long)m[0] * m[1]};
+                long ipn = (sn % 2 == 0) ? m[dn1 - 1] - 2 : 1;
+                f.ppk = L.off3[bn] + sm[dn1] * ipn;
+                f.pjo = sm[dn2];
+                f.pko = sm[dn3];
+                f.woff = slot[b][s - 1];
+                f.pwoff = slot[bn][sn - 1];
+                // edges rewritten later by another side of this block
+                int skip = 0;
+                if (2 * d2 - 1 > s && per_int(g.bl_bc[b - 1][2 * d2 - 2])) skip |= 1;
+                if (2 * d2 > s && per_int(g.bl_bc[b - 1][2 * d2 - 1])) skip |= 2;
+                if (2 * d3 - 1 > s && per_int(g.bl_bc[b - 1][2 * d3 - 2])) skip |= 4;
+                if (2 * d3 > s && per_int(g.bl_bc[b - 1][2 * d3 - 1])) skip |= 8;
+                f.skip = skip;
+                fv.push_back(f);
+                L.maxface = std::max(L.maxface, (long)f.nj * f.nk);
+            }
+        L.nface = (int)fv.size();
+        L.worklen = w;
+        maxwork = std::max(maxwork, w);
+        if (L.nface) {
+            LES_CUDA(cudaMalloc(&L.d_face, sizeof(FaceDev) * fv.size()));
+            LES_CUDA(cudaMemcpy(L.d_face, fv.data(), sizeof(FaceDev) * fv.size(), cudaMemcpyHostToDevice));
+        }
+        // block descriptors
+        std::vector<BlkDev> bv(nb);
+        for (int b = 1; b <= nb; b++) {
+            BlkDev &d = bv[b - 1];
+            for (int a = 0; a < 3; a++) {
+                d.n[a] = L.n[b][a];
+                d.mult[a] = L.mult[b][a];
+            }
+            for (int s = 0; s < 6; s++) d.bc[s] = g.bl_bc[b - 1][s];
+            d.off3 = L.off3[b];
+            d.off2 = L.off2[b];
+            d.off1k = L.off1k[b];
+            d.ncell = (long)(L.n[b][0] - 2) * (L.n[b][1] - 2) * (L.n[b][2] - 2);
+        }
+        LES_CUDA(cudaMalloc(&L.d_blk, sizeof(BlkDev) * nb));
+        LES_CUDA(cudaMemcpy(L.d_blk, bv.data(), sizeof(BlkDev) * nb, cudaMemcpyHostToDevice));
+        // metric tables (code/comp_metric.F, metric_swap1/2.F)
+        std::vector<char> mb(metblk_size() * nb);
+        for (int b = 1; b <= nb; b++)
+            fill_metblk(mb.data(), b - 1, L.n[b], L.off2[b], L.off1k[b], L.offxy[b], L.offz[b]);
+        LES_CUDA(cudaMalloc(&L.d_metblk, mb.size()));
+        LES_CUDA(cudaMemcpy(L.d_metblk, mb.data(), mb.size(), cudaMemcpyHostToDevice));
+        for (int s = 1; s <= 6; s++) {
+            std::vector<char> mf;
+            int cnt = 0;
+            for (int b = 1; b <= nb; b++) {
+                if (!per_int(g.bl_bc[b - 1][s - 1])) continue;
+                int bn = g.bl2bl[b - 1][s - 1], sn = g.bl2side[b - 1][s - 1];
+                int *n = L.n[b], *m = L.n[bn];
+                mf.resize(metface_size() * (cnt + 1));
+                if (s >= 5) {
+                    long srck = L.off1k[bn] + ((sn == 5) ? 1 : m[2] - 2);
+                    long dstk = L.off1k[b] + ((s == 5) ? 0 : n[2] - 1);
+                    fill_metface(mf.data(), cnt, 0, 0, 0, 0, srck, dstk);
+                } else {
+                    // own ghost line and the partner's packed line
+                    long src2, dst2, stride;
+                    int len;
+                    if (s <= 2) {
+                        stride = n[0];
+                        len = n[1];
+                        dst2 = L.off2[b] + ((s == 1) ? 0 : n[0] - 1);
+                    } else {
+                        stride = 1;
+                        len = n[0];
+                        dst2 = L.off2[b] + (long)n[0] * ((s == 3) ? 0 : n[1] - 1);
+                    }
+                    if (sn <= 2)
+                        src2 = L.off2[bn] + ((sn == 1) ? 1 : m[0] - 2);
+                    else
+                        src2 = L.off2[bn] + (long)m[0] * ((sn == 3) ? 1 : m[1] - 2);
+                    int plen = (sn <= 2) ? m[1] : m[0];
+                    if (plen != len)
+                        return set_err(LES_ERR_GEOM, "metric exchange: block %d side %d length mismatch", b, s);
+                    fill_metface(mf.data(), cnt, src2, dst2, stride, len, -1, -1);
+                    L.maxmetlen = std::max(L.maxmetlen, (long)len);
+                }
+                cnt++;
+            }
+            L.nmetface[s - 1] = cnt;
+            if (cnt) {
+                LES_CUDA(cudaMalloc(&L.d_metface[s - 1], mf.size()));
+                LES_CUDA(cudaMemcpy(L.d_metface[s - 1], mf.data(), mf.size(), cudaMemcpyHostToDevice));
+            }
+        }
+    }
+    LES_CUDA(cudaMalloc(&c.d_work, sizeof(double) * (maxwork + 1)));
+    return 0;
+}
+
+static void free_ctx(Ctx *c)
+{
+    if (!c) return;
+    for (int lev = 1; lev <= LES_MAXMGL; lev++) {
+        LevelGeom &L = c->lv[lev];
+        cudaFree(L.d_blk);
+        cudaFree(L.d_face);
+        cudaFree(L.d_metblk);
+        for (int s = 0; s < 6; s++) cudaFree(L.d_metface[s]);
+    }
+    cudaFree(c->d_work);
+    cudaFree(c->d_partial);
+    cudaFree(c->d_small);
+    if (c->h_small) cudaFreeHost(c->h_small);
+    cudaFree(c->d_nrm3);
+    cudaFree(c->d_metbuf);
+    cudaFree(c->d_flag);
+    void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b,
+                  c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b,
+                  c->E64,   c->N64,   c->R64,   c->P64};
+    for (void *p : fp) cudaFree(p);
+    for (void *p : c->stage_buf) cudaFree(p);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+static int sync_small(Ctx &c, int n)
+{
+    LES_CUDA(cudaMemcpyAsync(c.h_small, c.d_small, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// ------------------------------------------------- reference multigrid
+struct Coef {
+    const double *a[7]; // ap aw ae as an al ar
+};
+
+// code/norms.F:5-127 at one level; result in c.h_small[0..3]
+static int norms_level(Ctx &c, int ilev, const Coef &A, const double *x, const double *b,
+                       double *residu, double *out4)
+{
+    LevelGeom &L = c.lv[ilev];
+    launch_norms(L.d_blk, c.g.numbl, L.maxcell, A.a, x, b, residu, c.d_partial, 1.0 / L.npts_all,
+                 c.d_small, c.stream);
+    int r = sync_small(c, 4);
+    if (r) return r;
+    for (int q = 0; q < 4; q++) out4[q] = c.h_small[q];
+    return 0;
+}
+
+static void halo(Ctx &c, int ilev, double *var)
+{
+    LevelGeom &L = c.lv[ilev];
+    launch_halo(L.d_face, L.nface, L.maxface, var, c.d_work, c.stream);
+}
+
+// code/sporlx.F:5-203 (niter = 1).  io4 = res, rhs, err, var norms.
+static int sporlx(Ctx &c, int ilev, const Coef &A, double *f, const double *b, double omega,
+                  double soltol, double *io4)
+{
+    LevelGeom &L = c.lv[ilev];
+    double rn = 1.0 / L.npts_all;
+    int jumfor = ((c.jumble % 16) >= 8) ? 1 : 2;
+    int jumst = (c.jumble % 24) / 8 + 1;
+    int d[3] = {jumst, kCyc[((jumfor + 1) % 2)][jumst], kCyc[(jumfor % 2)][jumst]};
+    if (io4[2] / io4[3] > soltol) {
+        int smin = 6, smax = 0;
+        for (int b = 1; b <= c.g.numbl; b++)
+            smax = std::max(smax, L.n[b][0] + L.n[b][1] + L.n[b][2] - 3);
+        for (int il = 0; il < 3; il++) {
+            launch_lex_pass(L.d_blk, c.g.numbl, (int)L.maxjk, smin, smax, d[il], omega, A.a, f, b,
+                            c.d_nrm3, il == 2, c.stream);
+            halo(c, ilev, f);
+        }
+        launch_lex_norm(L.d_blk, c.g.numbl, L.maxcell, c.d_nrm3, c.d_partial, rn, c.d_small, c.stream);
+        int r = sync_small(c, 3);
+        if (r) return r;
+        io4[0] = c.h_small[0];
+        io4[2] = c.h_small[1];
+        io4[3] = c.h_small[2];
+        if (!std::isfinite(io4[0]) || !std::isfinite(io4[2]))
+            return set_err(LES_ERR_NONFINITE, "non-finite smoother norm at level %d", ilev);
+    } else {
+        io4[0] = std::sqrt(io4[0] * rn);
+    }
+    c.jumble += 13;
+    if (c.jumble > 99999) c.jumble = c.jumble % 99999;
+    return 0;
+}
+
+// code/smooth.F:5-105
+static int smooth(Ctx &c, int ilev, const Coef &A, double *f, const double *b, double *residu,
+                  int nsmooth, double omega, double soltol, double *nrm)
+{
+    int r;
+    if (ilev == 1 || ilev == c.nummgl) {
+        if ((r = norms_level(c, ilev, A, f, b, residu, nrm))) return r;
+    } else {
+        nrm[2] = 1.;
+        nrm[3] = 1.;
+    }
+    int ismooth = 0;
+    while (nrm[2] / nrm[3] > soltol && ismooth < nsmooth) {
+        ismooth++;
+        if ((r = sporlx(c, ilev, A, f, b, omega, soltol, nrm))) return r;
+        if (ismooth == nsmooth)
+            if ((r = norms_level(c, ilev, A, f, b, residu, nrm))) return r;
+    }
+    return 0;
+}
+
+// code/lmg_solve.F:5-172
+static int lmg_reference(Ctx &c, const Coef &A, double *f, double *b, double *residu)
+{
+    const lester_ctrl &m = c.c;
+    int nummgl = c.nummgl;
+    int mg_gamma = (m.meth_cycle == 1) ? 1 : 2;
+    bool fcycle = (m.meth_cycle == 2);
+    double tolc = (nummgl == 1) ? m.tolf : 0.;
+    int nummg_l[LES_MAXMGL + 2];
+    double nrm[LES_MAXMGL + 2][4];
+    memset(nrm, 0, sizeof nrm);
+    if (!c.d_nrm3) LES_CUDA(cudaMalloc(&c.d_nrm3, sizeof(double) * 3 * c.tot3));
+    int r;
+    if ((r = norms_level(c, 1, A, f, b, residu, nrm[1]))) return r;
+    nummg_l[1] = m.nummgits;
+    int ilev = 1, cycles = 0;
+    while (nummg_l[1] > 0 && nrm[1][2] / nrm[1][3] > m.tolf) {
+        bool goto_fine = (ilev == nummgl) || (nummg_l[ilev] == 0);
+        if (goto_fine) {
+            if (ilev == nummgl) {
+                if ((r = smooth(c, ilev, A, f, b, residu, m.numcits, m.relax_pmgc, tolc, nrm[ilev]))) return r;
+                if (fcycle) mg_gamma = 1;
+            }
+            if (ilev > 1 && nummgl != 1) {
+                ilev--;
+                LevelGeom &Lc = c.lv[ilev + 1], &Lf = c.lv[ilev];
+                launch_prolong(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxfine, f, c.stream);
+                halo(c, ilev, f);
+                if ((r = smooth(c, ilev, A, f, b, residu, m.numpost, m.relax_pmg, tolc, nrm[ilev]))) return r;
+                if (ilev == 1 && fcycle) mg_gamma = 2;
+            }
+            if (ilev == 1) cycles++;
+            nummg_l[ilev]--;
+        } else {
+            if ((r = smooth(c, ilev, A, f, b, residu, m.numpre, m.relax_pmg, tolc, nrm[ilev]))) return r;
+            ilev++;
+            nummg_l[ilev] = mg_gamma;
+            LevelGeom &Lc = c.lv[ilev], &Lf = c.lv[ilev - 1];
+            LES_CUDA(cudaMemsetAsync(f + Lc.start3, 0, sizeof(double) * Lc.len3, c.stream));
+            launch_restrict(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxcell, residu, b, c.stream);
+        }
+    }
+    for (int q = 0; q < 4; q++) c.last_norms[q] = nrm[1][q];
+    c.last_cycles = cycles;
+    c.last_relres = nrm[1][1] > 0 ? nrm[1][0] / nrm[1][1] : 0.;
+    return 0;
+}
+
+// ----------------------------------------------------------- fast solvers
+template <typename T> static FastSet<T> &fset(Ctx &c);
+template <> FastSet<float> &fset<float>(Ctx &c) { return c.f32; }
+template <> FastSet<double> &fset<double>(Ctx &c) { return c.f64; }
+
+template <typename T> static int alloc_fast(Ctx &c)
+{
+    FastSet<T> &F = fset<T>(c);
+    if (F.E) return 0;
+    size_t nb = sizeof(T) * (size_t)c.tot3;
+    T **arr[6] = {&F.E, &F.N, &F.R, &F.D, &F.x, &F.b};
+    for (T **a : arr) {
+        if (cudaMalloc((void **)a, nb) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(LES_ERR_NOMEM, "fast-solver allocation failed");
+        }
+        LES_CUDA(cudaMemset(*a, 0, nb));
+    }
+    if (!c.E64) {
+        size_t n1 = sizeof(double) * (size_t)c.tot_sg3;
+        double **a64[4] = {&c.E64, &c.N64, &c.R64, &c.P64};
+        for (double **a : a64) {
+            if (cudaMalloc((void **)a, n1) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(LES_ERR_NOMEM, "fast-solver allocation failed");
+            }
+            LES_CUDA(cudaMemset(*a, 0, n1));
+        }
+    }
+    return 0;
+}
+
+template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
+{
+    bool same = (c.coef_prec == prec) && (c.coef_gen_seen == c.coef_gen);
+    for (int q = 0; q < 7; q++) same = same && (c.coef_key[q] == A.a[q]);
+    if (same) return 0;
+    int r = alloc_fast<T>(c);
+    if (r) return r;
+    FastSet<T> &F = fset<T>(c);
+    LES_CUDA(cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream));
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        LevelGeom &L = c.lv[lev];
+        launch_conv_coef<T>(L.d_blk, c.g.numbl, L.maxcell, A.a, F.E, F.N, F.R, F.D,
+                            lev == 1 ? c.E64 : nullptr, c.N64, c.R64, c.P64, c.d_flag, c.stream);
+    }
+    int bad = 0;
+    LES_CUDA(cudaMemcpyAsync(&bad, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    if (bad)
+        return set_err(LES_ERR_STRUCTURE,
+                       "coefficients lack the aw(i)=ae(i-1) pairing of coeff_p (mask %d); use LES_PSOLVE_REFERENCE", bad);
+    for (int q = 0; q < 7; q++) c.coef_key[q] = A.a[q];
+    c.coef_gen_seen = c.coef_gen;
+    c.coef_prec = prec;
+    return 0;
+}
+
+template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
+{
+    FastSet<T> &F = fset<T>(c);
+    LevelGeom &L = c.lv[lev];
+    for (int s = 0; s < nsweep; s++)
+        for (int color = 0; color < 2; color++) {
+            launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
+                         F.b, c.stream);
+            launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
+        }
+}
+
+// one V-cycle on the correction equation A e = r, e = 0 on entry; r is in
+// F.b at level 1
+template <typename T> static void fast_vcycle(Ctx &c)
+{
+    FastSet<T> &F = fset<T>(c);
+    int L = c.nummgl;
+    int pre = c.c.rb_sweeps > 0 ? c.c.rb_sweeps : 1;
+    int crs = c.c.rb_coarse > 0 ? c.c.rb_coarse : 20;
+    cudaMemsetAsync(F.x, 0, sizeof(T) * c.tot3, c.stream);
+    count_launch(1);
+    for (int lev = 1; lev < L; lev++) {
+        fast_smooth<T>(c, lev, pre);
+        LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
+        launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxcell, F.E, F.N, F.R, F.D, F.x,
+                                 F.b, F.b, c.stream);
+    }
+    fast_smooth<T>(c, L, L == 1 ? pre : crs);
+    for (int lev = L - 1; lev >= 1; lev--) {
+        LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
+        launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxcell, F.x, F.x, c.stream);
+        launch_halo_fast<T>(Lf.d_face, Lf.nface, Lf.maxface, F.x, c.stream);
+        fast_smooth<T>(c, lev, pre);
+    }
+}
+
+// defect correction: p <- p + V(b - A p) until ||b - A p|| <= rtol ||b||
+template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, double *b, double *residu,
+                                            int prec)
+{
+    int r = prepare_coef<T>(c, A, prec);
+    if (r) return r;
+    FastSet<T> &F = fset<T>(c);
+    LevelGeom &L1 = c.lv[1];
+    int nb = c.g.numbl;
+    double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
+    int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
+    launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b, c.d_partial,
+                          c.d_small, c.stream);
+    if ((r = sync_small(c, 2))) return r;
+    double r2 = c.h_small[0], b2 = c.h_small[1];
+    int it = 0;
+    double rel = b2 > 0 ? std::sqrt(r2 / b2) : 0.;
+    while (b2 > 0 && rel > rtol && it < maxit) {
+        fast_vcycle<T>(c);
+        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, c.stream);
+        launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b,
+                              c.d_partial, c.d_small, c.stream);
+        if ((r = sync_small(c, 2))) return r;
+        r2 = c.h_small[0];
+        rel = std::sqrt(r2 / b2);
+        it++;
+        if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+    }
+    c.last_cycles = it;
+    c.last_relres = rel;
+    // reference-style norms and level-1 residual for the caller
+    double n4[4];
+    if ((r = norms_level(c, 1, A, f, b, residu, n4))) return r;
+    for (int q = 0; q < 4; q++) c.last_norms[q] = n4[q];
+    if (rel > rtol && b2 > 0)
+        return set_err(LES_ERR_NOT_CONVERGED, "relative residual %.3e after %d cycles", rel, it);
+    return 0;
+}
+
+static int ensure_scratch(Ctx &c)
+{
+    long np = 0;
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        long t = norms_parts(c.g.numbl, c.lv[lev].maxcell) * 4;
+        np = std::max(np, t);
+    }
+    LES_CUDA(cudaMalloc(&c.d_partial, sizeof(double) * (np + 16)));
+    c.npartial = np;
+    LES_CUDA(cudaMalloc(&c.d_small, sizeof(double) * 64));
+    LES_CUDA(cudaMallocHost(&c.h_small, sizeof(double) * 64));
+    LES_CUDA(cudaMalloc(&c.d_flag, sizeof(int) * 4));
+    return 0;
+}
+
+} // namespace les
+
+using namespace les;
+
+// ================================================================ C ABI
+extern "C" {
+
+const char *lester_gpu_last_error(void) { return g_err.c_str(); }
+long lester_gpu_launch_count(void) { return g_launches.load(); }
+
+int lester_gpu_finalize(void)
+{
+    if (g_ctx) {
+        cudaStreamSynchronize(g_ctx->stream);
+        free_ctx(g_ctx);
+        g_ctx = nullptr;
+    }
+    return 0;
+}
+
+int lester_gpu_init(const lester_geom *g, const lester_ctrl *c)
+{
+    lester_gpu_finalize();
+    if (!g || !c) return set_err(LES_ERR_ARG, "null geometry or control");
+    if (g->numbl < 1 || g->numbl > LES_MAXBL) return set_err(LES_ERR_GEOM, "numbl %d out of 1..%d", g->numbl, LES_MAXBL);
+    Ctx *ctx = new Ctx();
+    ctx->g = *g;
+    ctx->c = *c;
+    int r = build_levels(*ctx);
+    if (!r) r = build_faces(*ctx);
+    if (!r) r = ensure_scratch(*ctx);
+    if (!r) {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+            r = set_err(LES_ERR_CUDA, "stream creation failed");
+        else
+            ctx->own_stream = true;
+    }
+    if (r) {
+        free_ctx(ctx);
+        return r;
+    }
+    g_ctx = ctx;
+    return 0;
+}
+
+int lester_gpu_set_ctrl(const lester_ctrl *c)
+{
+    LES_NEED_CTX();
+    if (!c) return set_err(LES_ERR_ARG, "null control");
+    g_ctx->c = *c;
+    return 0;
+}
+
+int lester_gpu_sizes(lester_sizes *o)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    o->nummgl = c.nummgl;
+    o->n3_sg = c.tot_sg3;
+    o->n3_mg = c.tot3;
+    o->n2 = c.tot2;
+    o->n1k = c.tot1k;
+    o->nxy = c.totxy;
+    o->nz = c.totz;
+    o->n2_ki = c.totki;
+    o->n2_jk = c.totjk;
+    return 0;
+}
+
+int lester_gpu_block_info(int ilev, int iblk, int *n, long *offs)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    if (ilev < 1 || ilev > c.nummgl || iblk < 1 || iblk > c.g.numbl) return set_err(LES_ERR_ARG, "bad level/block");
+    LevelGeom &L = c.lv[ilev];
+    for (int d = 0; d < 3; d++) n[d] = L.n[iblk][d];
+    offs[0] = L.off3[iblk];
+    offs[1] = L.off2[iblk];
+    offs[2] = L.off1k[iblk];
+    offs[3] = L.offxy[iblk];
+    offs[4] = L.offz[iblk];
+    return 0;
+}
+
+int lester_gpu_sync(void)
+{
+    LES_NEED_CTX();
+    LES_CUDA(cudaStreamSynchronize(g_ctx->stream));
+    LES_CUDA(cudaGetLastError());
+    return 0;
+}
+
+void *lester_gpu_get_stream(void) { return g_ctx ? (void *)g_ctx->stream : nullptr; }
+
+int lester_gpu_set_stream(void *s)
+{
+    LES_NEED_CTX();
+    if (g_ctx->own_stream && g_ctx->stream) cudaStreamDestroy(g_ctx->stream);
+    g_ctx->stream = (cudaStream_t)s;
+    g_ctx->own_stream = false;
+    return 0;
+}
+
+int lester_gpu_set_jumble(int j)
+{
+    LES_NEED_CTX();
+    g_ctx->jumble = j;
+    return 0;
+}
+
+int lester_gpu_get_jumble(void) { return g_ctx ? g_ctx->jumble : 0; }
+
+// solve statistics of the last lester_solvers / lester_lmg_solve call:
+// out[0..3] = rnorm, fnorm, enorm, vnorm of level 1 (code/norms.F:393-398),
+// out[4] = cycles, out[5] = ||b - A p|| / ||b||
+int lester_gpu_solve_stats(double *out)
+{
+    LES_NEED_CTX();
+    for (int q = 0; q < 4; q++) out[q] = g_ctx->last_norms[q];
+    out[4] = g_ctx->last_cycles;
+    out[5] = g_ctx->last_relres;
+    return 0;
+}
+
+int lester_swap_sc(const int *ivar1, const int *igrid, double *var, double *work, const int *mg_or_sg)
+{
+    (void)ivar1;
+    (void)work;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int ig = *igrid, mos = mg_or_sg ? *mg_or_sg : 1;
+    if (ig < 1 || ig > c.nummgl || (mos != 1 && ig != 1)) return set_err(LES_ERR_ARG, "bad igrid %d", ig);
+    Staging st(&c);
+    double *d;
+    int r = st.io(var, mos == 1 ? c.tot3 : c.tot_sg3, &d);
+    if (r) return r;
+    halo(c, ig, d);
+    return st.finish();
+}
+
+int lester_comp_metric(const double *x, const double *y, const double *t, double *dip, double *diu,
+                       double *div, double *dix, double *rdip, double *rdiv, double *rdix, double *djp,
+                       double *dju, double *djv, double *djx, double *rdjp, double *rdju, double *rdjx,
+                       double *hijp, double *hjip, double *hkip, double *hkjp, double *hiju, double *hjiu,
+                       double *hkiu, double *hkju, double *hijv, double *hjiv, double *hkiv, double *hkjv,
+                       double *rp, double *ru, double *rv, double *didjp, double *rdidjp, double *didju,
+                       double *rdidju, double *djdiv, double *rdjdiv, double *dkp, double *dkw,
+                       double *swap_geo, int *pnti)
+{
+    (void)swap_geo;
+    (void)pnti;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    double *user[35] = {dip,  diu,  div,  dix,  rdip, rdiv, rdix, djp,   dju, djv,
+                        djx,  rdjp, rdju, rdjx, hijp, hjip, hkip, hkjp,  hiju,  hjiu, hkiu,   hkju,
+                        hijv, hjiv, hkiv, hkjv, rp,   ru,   rv,   didjp, rdidjp, didju, rdidju, djdiv,
+                        rdjdiv};
+    Staging st(&c);
+    const double *dx, *dy, *dz;
+    int r;
+    if ((r = st.in(x, c.totxy, &dx)) || (r = st.in(y, c.totxy, &dy)) || (r = st.in(t, c.totz, &dz))) return r;
+    double *m[35];
+    for (int a = 0; a < 35; a++)
+        if ((r = st.io(user[a], c.tot2, &m[a]))) return r;
+    double *ddkp, *ddkw;
+    if ((r = st.io(dkp, c.tot1k, &ddkp)) || (r = st.io(dkw, c.tot1k, &ddkw))) return r;
+    if (!c.d_metbuf) {
+        long maxlen = 0;
+        int maxf = 0;
+        for (int lev = 1; lev <= c.nummgl; lev++) {
+            maxlen = std::max(maxlen, c.lv[lev].maxmetlen);
+            for (int s = 0; s < 6; s++) maxf = std::max(maxf, c.lv[lev].nmetface[s]);
+        }
+        c.metslot = 34 * maxlen + 2;
+        c.metmaxf = maxf + 1;
+        LES_CUDA(cudaMalloc(&c.d_metbuf, sizeof(double) * (c.metslot * 6 * c.metmaxf + 1)));
+    }
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        LevelGeom &L = c.lv[lev];
+        launch_metric(L.d_metblk, c.g.numbl, L.maxij, L.maxk, dx, dy, dz, m, ddkp, ddkw, c.g.gotrad, c.stream);
+        // every side is packed before any is unpacked; unpacking goes side
+        // by side so later sides overwrite shared corners, as in
+        // comp_metric.F:113-241
+        for (int phase = 0; phase < 2; phase++)
+            for (int s = 0; s < 6; s++)
+                launch_metric_swap(L.d_metface[s], L.nmetface[s], L.maxmetlen, m, ddkp, ddkw,
+                                   c.d_metbuf + (long)s * c.metmaxf * c.metslot, c.metslot, phase,
+                                   c.stream);
+    }
+    return st.finish();
+}
+
+int lester_coeff_p(const double *diu, const double *djv, const double *rdiv, const double *rdju,
+                   const double *didjp, const double *rp, const double *dkp, const double *dkw, double *ap,
+                   double *aw, double *ae, double *as, double *an, double *al, double *ar)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    const double *mu[6] = {diu, djv, rdiv, rdju, didjp, rp};
+    const double *m[6], *ddkp, *ddkw;
+    double *au[7] = {ap, aw, ae, as, an, al, ar}, *a[7];
+    int r;
+    for (int q = 0; q < 6; q++)
+        if ((r = st.in(mu[q], c.tot2, &m[q]))) return r;
+    if ((r = st.in(dkp, c.tot1k, &ddkp)) || (r = st.in(dkw, c.tot1k, &ddkw))) return r;
+    for (int q = 0; q < 7; q++)
+        if ((r = st.io(au[q], c.tot3, &a[q]))) return r;
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        LevelGeom &L = c.lv[lev];
+        launch_coeff_p(L.d_blk, c.g.numbl, L.maxcell, m, ddkp, ddkw, a, c.stream);
+    }
+    c.coef_gen++;
+    return st.finish();
+}
+
+int lester_sour_p(const double *diu, const double *djv, const double *rdiv, const double *rdju,
+                  const double *didjp, const double *dkp, const double *rdidjp, const double *dkw,
+                  const double *u, const double *v, const double *w, const double *rho, const double *rhonp1,
+                  double *drhonp1dt, double *s, double *srhot, double *srhoux, double *gia, double *gja)
+{
+    (void)diu;
+    (void)djv;
+    (void)gia;
+    (void)gja;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    const double *m[6], *f[5];
+    double *o[4];
+    int r;
+    const double *mu[6] = {rdiv, rdju, didjp, dkp, rdidjp, dkw};
+    long ml[6] = {c.tot2, c.tot2, c.tot2, c.tot1k, c.tot2, c.tot1k};
+    for (int q = 0; q < 6; q++)
+        if ((r = st.in(mu[q], ml[q], &m[q]))) return r;
+    const double *fu[5] = {u, v, w, rho, rhonp1};
+    for (int q = 0; q < 5; q++)
+        if ((r = st.in(fu[q], c.tot_sg3, &f[q]))) return r;
+    double *ou[4] = {drhonp1dt, s, srhot, srhoux};
+    for (int q = 0; q < 4; q++)
+        if ((r = st.io(ou[q], c.tot_sg3, &o[q]))) return r;
+    if (!(c.c.dtime > 0)) return set_err(LES_ERR_ARG, "dtime must be positive");
+    LevelGeom &L = c.lv[1];
+    launch_sour_p(L.d_blk, c.g.numbl, L.maxcell, c.c.dtime, m[0], m[1], m[2], m[3], m[4], m[5], f[0], f[1],
+                  f[2], f[3], f[4], o[0], o[1], o[2], o[3], c.stream);
+    return st.finish();
+}
+
+int lester_lmg_solve(const double *ap, const double *aw, const double *ae, const double *as,
+                     const double *an, const double *al, const double *ar, double *f, double *b,
+                     double *residu, int *ia, double *ra)
+{
+    (void)ia;
+    (void)ra;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    const double *au[7] = {ap, aw, ae, as, an, al, ar};
+    Coef A;
+    int r;
+    for (int q = 0; q < 7; q++)
+        if ((r = st.in(au[q], c.tot3, &A.a[q]))) return r;
+    double *df, *db, *dr;
+    if ((r = st.io(f, c.tot3, &df)) || (r = st.io(b, c.tot3, &db)) || (r = st.io(residu, c.tot3, &dr))) return r;
+    int ps = c.c.psolve;
+    if (ps == LES_PSOLVE_REFERENCE)
+        r = lmg_reference(c, A, df, db, dr);
+    else if (ps == LES_PSOLVE_FP64)
+        r = fast_solve<double>(c, A, df, db, dr, 64);
+    else if (ps == LES_PSOLVE_MIXED)
+        r = fast_solve<float>(c, A, df, db, dr, 32);
+    else
+        r = set_err(LES_ERR_ARG, "unknown psolve %d", ps);
+    int r2 = st.finish();
+    return r ? r : r2;
+}
+
+// code/solvers.F:5-41: psolver 101 is lmg_solve
+int lester_solvers(const double *ap, const double *aw, const double *ae, const double *as, const double *an,
+                   const double *al, const double *ar, double *f, double *b, double *residu, int *ia, double *ra)
+{
+    return lester_lmg_solve(ap, aw, ae, as, an, al, ar, f, b, residu, ia, ra);
+}
+
+int lester_norms(const int *ilev, const int *mg_or_sg, const double *ap, const double *aw, const double *ae,
+                 const double *as, const double *an, const double *al, const double *ar, const double *x,
+                 const double *b, double *residu, double *res_norm, double *rhs_norm, double *err_norm,
+                 double *var_norm)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int lev = *ilev;
+    if (lev < 1 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
+    if (mg_or_sg && *mg_or_sg != 1 && lev != 1) return set_err(LES_ERR_ARG, "single-grid x needs level 1");
+    Staging st(&c);
+    const double *au[7] = {ap, aw, ae, as, an, al, ar};
+    Coef A;
+    int r;
+    for (int q = 0; q < 7; q++)
+        if ((r = st.in(au[q], c.tot3, &A.a[q]))) return r;
+    const double *dx, *db;
+    double *dr;
+    if ((r = st.in(x, c.tot3, &dx)) || (r = st.in(b, c.tot3, &db)) || (r = st.io(residu, c.tot3, &dr))) return r;
+    double n4[4];
+    if ((r = norms_level(c, lev, A, dx, db, dr, n4))) return r;
+    *res_norm = n4[0];
+    *rhs_norm = n4[1];
+    *err_norm = n4[2];
+    *var_norm = n4[3];
+    return st.finish();
+}
+
+int lester_restriction(const int *ilev, const double *f, double *f1, double *work, int *offwork)
+{
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int lev = *ilev;
+    if (lev < 2 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
+    Staging st(&c);
+    const double *df;
+    double *d1;
+    int r;
+    if ((r = st.in(f, c.tot3, &df)) || (r = st.io(f1, c.tot3, &d1))) return r;
+    launch_restrict(c.lv[lev].d_blk, c.lv[lev - 1].d_blk, c.g.numbl, c.lv[lev].maxcell, df, d1, c.stream);
+    return st.finish();
+}
+
+int lester_prolongation(const int *ilev, double *f, double *work, int *offwork)
+{
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int lev = *ilev;
+    if (lev < 1 || lev >= c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
+    Staging st(&c);
+    double *df;
+    int r;
+    if ((r = st.io(f, c.tot3, &df))) return r;
+    launch_prolong(c.lv[lev + 1].d_blk, c.lv[lev].d_blk, c.g.numbl, c.lv[lev].maxfine, df, c.stream);
+    halo(c, lev, df);
+    return st.finish();
+}
+
+int lester_sporlx(const int *ilev, const double *ap, const double *aw, const double *ae, const double *as,
+                  const double *an, const double *al, const double *ar, double *f, const double *b,
+                  double *residu, const int *niter, const double *omega, const double *soltol, double *work,
+                  int *offwork, double *res_norm, double *rhs_norm, double *err_norm, double *var_norm)
+{
+    (void)residu;
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int lev = *ilev;
+    if (lev < 1 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
+    if (niter && *niter != 1) return set_err(LES_ERR_ARG, "sporlx is only called with niter = 1");
+    Staging st(&c);
+    const double *au[7] = {ap, aw, ae, as, an, al, ar};
+    Coef A;
+    int r;
+    for (int q = 0; q < 7; q++)
+        if ((r = st.in(au[q], c.tot3, &A.a[q]))) return r;
+    double *df;
+    const double *db;
+    if ((r = st.io(f, c.tot3, &df)) || (r = st.in(b, c.tot3, &db))) return r;
+    if (!c.d_nrm3) LES_CUDA(cudaMalloc(&c.d_nrm3, sizeof(double) * 3 * c.tot3));
+    double io4[4] = {*res_norm, *rhs_norm, *err_norm, *var_norm};
+    if ((r = sporlx(c, lev, A, df, db, *omega, *soltol, io4))) return r;
+    *res_norm = io4[0];
+    *err_norm = io4[2];
+    *var_norm = io4[3];
+    return st.finish();
+}
+
+int lester_extrap_p(double *p, double *work, int *offwork)
+{
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    double *dp;
+    int r;
+    if ((r = st.io(p, c.tot_sg3, &dp))) return r;
+    launch_extrap_p(c.lv[1].d_blk, c.g.numbl, dp, c.stream);
+    halo(c, 1, dp);
+    return st.finish();
+}
+
+int lester_p_ref_subtract(double *p)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    double *dp;
+    int r;
+    if ((r = st.io(p, c.tot_sg3, &dp))) return r;
+    launch_pref(c.lv[1].d_blk, dp, c.tot_sg3, c.d_small + 32, c.stream);
+    return st.finish();
+}
+
+int lester_uvw_adv(const int *ivar1, const double *diu, const double *rp, const double *dkw, double *u,
+                   const double *u_int, const double *rho, const double *p, double *wk, int *offwork,
+                   const int *step)
+{
+    (void)wk;
+    (void)offwork;
+    (void)step;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int iv = *ivar1;
+    if (iv < 1 || iv > 3) return set_err(LES_ERR_ARG, "uvw_adv: ivar1 %d", iv);
+    Staging st(&c);
+    const double *dd, *drp, *ddkw, *dui, *drho, *dpp;
+    double *du;
+    int r;
+    if ((r = st.in(diu, c.tot2, &dd)) || (r = st.in(rp, c.tot2, &drp)) || (r = st.in(dkw, c.tot1k, &ddkw)) ||
+        (r = st.io(u, c.tot_sg3, &du)) || (r = st.in(u_int, c.tot_sg3, &dui)) ||
+        (r = st.in(rho, c.tot_sg3, &drho)) || (r = st.in(p, c.tot_sg3, &dpp)))
+        return r;
+    LevelGeom &L = c.lv[1];
+    launch_uvw_adv(L.d_blk, c.g.numbl, L.maxcell, iv, c.c.dtime, dd, drp, ddkw, du, dui, drho, dpp, c.stream);
+    halo(c, 1, du);
+    return st.finish();
+}
+
+int lester_swap_rhos(double *rho, double *rhonp1, double *rhonm1)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    double *a, *b, *d;
+    int r;
+    if ((r = st.io(rho, c.tot_sg3, &a)) || (r = st.io(rhonp1, c.tot_sg3, &b)) || (r = st.io(rhonm1, c.tot_sg3, &d)))
+        return r;
+    launch_swap_rhos(a, b, d, c.tot_sg3, c.stream);
+    return st.finish();
+}
+
+int lester_search_lib(double *sc1, double *sc1var, double *rhonp1, double *temperature, double *work,
+                      int *offwork, const int *istep, const double *alpha, const double *rho,
+                      const double *rholo, const double *rhohi)
+{
+    (void)sc1var;
+    (void)work;
+    (void)offwork;
+    (void)istep;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    double *ds, *dr, *dt = nullptr;
+    const double *drho;
+    int r;
+    if ((r = st.io(sc1, c.tot_sg3, &ds)) || (r = st.io(rhonp1, c.tot_sg3, &dr)) || (r = st.in(rho, c.tot_sg3, &drho)))
+        return r;
+    if (temperature && (r = st.io(temperature, c.tot_sg3, &dt))) return r;
+    launch_search_lib(ds, dr, drho, *alpha, *rholo, *rhohi, c.tot_sg3, c.stream);
+    halo(c, 1, ds);
+    halo(c, 1, dr);
+    if (dt) halo(c, 1, dt);
+    return st.finish();
+}
+
+int lester_slipbc(const double *x, const double *y, const double *z, const double *dip, const double *diu,
+                  const double *djp, const double *djv, const double *dkp, double *u, double *v,
+                  const double *v_int, double *w, double *sc1, double *rho, const double *p, const int *step)
+{
+    (void)x;
+    (void)y;
+    (void)z;
+    (void)dip;
+    (void)diu;
+    (void)djv;
+    (void)dkp;
+    (void)step;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    const double *ddjp, *dvi, *dp;
+    double *du, *dv, *dw, *ds, *dr;
+    int r;
+    if ((r = st.in(djp, c.tot2, &ddjp)) || (r = st.io(u, c.tot_sg3, &du)) || (r = st.io(v, c.tot_sg3, &dv)) ||
+        (r = st.in(v_int, c.tot_sg3, &dvi)) || (r = st.io(w, c.tot_sg3, &dw)) || (r = st.io(sc1, c.tot_sg3, &ds)) ||
+        (r = st.io(rho, c.tot_sg3, &dr)) || (r = st.in(p, c.tot_sg3, &dp)))
+        return r;
+    LevelGeom &L = c.lv[1];
+    launch_slipbc(L.d_blk, c.g.numbl, L.maxik, c.c.dtime, ddjp, du, dv, dvi, dw, ds, dr, dp, c.stream);
+    return st.finish();
+}
+
+int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v, const double *w,
+                   const double *sc1, const double *rho, double *sc1var, double *sc1dis, const double *vd_damping,
+                   const double *dip, const double *diu, const double *djp, const double *djv, const double *dkp,
+                   const double *dkw, const double *hijp, const double *hjip, const double *hkip,
+                   const double *hkjp, const double *rp, double *work, int *offwork)
+{
+    (void)rho;
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    double *dg, *dgs, *dsv, *dsd;
+    const double *du, *dv, *dw, *dsc, *dvd = nullptr;
+    int r;
+    if ((r = st.io(gam, c.tot_sg3, &dg)) || (r = st.io(gamsc1, c.tot_sg3, &dgs)) || (r = st.in(u, c.tot_sg3, &du)) ||
+        (r = st.in(v, c.tot_sg3, &dv)) || (r = st.in(w, c.tot_sg3, &dw)) || (r = st.in(sc1, c.tot_sg3, &dsc)) ||
+        (r = st.io(sc1var, c.tot_sg3, &dsv)) || (r = st.io(sc1dis, c.tot_sg3, &dsd)))
+        return r;
+    if (c.c.model == 1) {
+        if (!vd_damping) return set_err(LES_ERR_ARG, "Smagorinsky needs vd_damping");
+        if ((r = st.in(vd_damping, c.tot_sg3, &dvd))) return r;
+    }
+    const double *mu[11] = {dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp};
+    long ml[11] = {c.tot2, c.tot2, c.tot2, c.tot2, c.tot1k, c.tot1k, c.tot2, c.tot2, c.tot2, c.tot2, c.tot2};
+    const double *m[11];
+    for (int q = 0; q < 11; q++)
+        if ((r = st.in(mu[q], ml[q], &m[q]))) return r;
+    LevelGeom &L = c.lv[1];
+    launch_subgrid(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, dg, dgs, du, dv, dw, dsc, dsv,
+                   dsd, dvd, m, c.stream);
+    halo(c, 1, dg);
+    halo(c, 1, dgs);
+    return st.finish();
+}
+
+} // extern "C"

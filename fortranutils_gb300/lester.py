@@ -1,0 +1,291 @@
+"""Python binding of liblester_gpu.so (include/lester_gpu.h).
+
+The functions keep the reference's subroutine names and argument order
+(code/step.F calls them); arrays may be torch CUDA tensors (used in place on
+the device) or numpy arrays (copied in and out by the library).  Scalars are
+passed by reference, as Fortran does.  Every call checks the returned status
+and raises ``LesterError`` with the library's message.
+
+There is no CPU fallback: if the shared library is missing this module
+raises at import time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+LES_MAXBL = 64
+LES_MAXMGL = 16
+
+BCT_WALL, BCT_ZERO_GRAD, BCT_CONVECTIVE, BCT_FIXED = 1, 2, 3, 4
+BCT_TRACTION, BCT_PERIODIC, BCT_INTERFACE = 6, 12, 13
+SV_U, SV_V, SV_W, SV_P, SV_SC1 = 1, 2, 3, 4, 5
+PSOLVE_REFERENCE, PSOLVE_FP64, PSOLVE_MIXED = 0, 1, 2
+
+ERRORS = {
+    -1: "LES_ERR_NOT_INIT", -2: "LES_ERR_GEOM", -3: "LES_ERR_ARG", -4: "LES_ERR_CUDA",
+    -5: "LES_ERR_NOMEM", -6: "LES_ERR_NONFINITE", -7: "LES_ERR_NOT_CONVERGED",
+    -8: "LES_ERR_STRUCTURE", -9: "LES_ERR_TIMEOUT", -10: "LES_ERR_SIZE",
+}
+
+
+class LesterError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Geom(C.Structure):
+    _fields_ = [
+        ("numbl", C.c_int), ("maxmgl", C.c_int), ("nummgl", C.c_int), ("gotrad", C.c_int),
+        ("bl_nijkp1", (C.c_int * 3) * LES_MAXBL), ("bl_bc", (C.c_int * 6) * LES_MAXBL),
+        ("bl2bl", (C.c_int * 6) * LES_MAXBL), ("bl2side", (C.c_int * 6) * LES_MAXBL),
+    ]
+
+
+class Ctrl(C.Structure):
+    _fields_ = [
+        ("dtime", C.c_double), ("visc", C.c_double), ("csles", C.c_double),
+        ("rholo", C.c_double), ("rhohi", C.c_double), ("alpha", C.c_double),
+        ("ylaminar", C.c_double), ("kappa", C.c_double), ("cwfun", C.c_double),
+        ("aplus", C.c_double), ("model", C.c_int),
+        ("nummgits", C.c_int), ("numpre", C.c_int), ("numpost", C.c_int),
+        ("numcits", C.c_int), ("meth_cycle", C.c_int),
+        ("tolf", C.c_double), ("relax_pmg", C.c_double), ("relax_pmgc", C.c_double),
+        ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
+        ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
+    ]
+
+
+class Sizes(C.Structure):
+    _fields_ = [("nummgl", C.c_int), ("n3_sg", C.c_long), ("n3_mg", C.c_long), ("n2", C.c_long),
+                ("n1k", C.c_long), ("nxy", C.c_long), ("nz", C.c_long), ("n2_ki", C.c_long),
+                ("n2_jk", C.c_long)]
+
+
+def default_ctrl(**kw) -> Ctrl:
+    """Controls with the reference defaults (code/defaults.F:59-71, const.inc)."""
+    c = Ctrl()
+    c.dtime = 1e-3
+    c.visc = 1.0 / 2800.0
+    c.csles = 0.1
+    c.rholo = 1.0
+    c.rhohi = 1.0
+    c.alpha = 0.0
+    c.ylaminar = 11.3
+    c.kappa = 0.41
+    c.cwfun = 5.2 * 0.41
+    c.aplus = 25.0
+    c.model = 1
+    c.nummgits = 5
+    c.numpre = 1
+    c.numpost = 1
+    c.numcits = 20
+    c.meth_cycle = 1
+    c.tolf = 5e-13
+    c.relax_pmg = 1.6
+    c.relax_pmgc = 1.6
+    c.psolve = PSOLVE_REFERENCE
+    c.rtol = 1e-8
+    c.max_outer = 200
+    c.rb_sweeps = 1
+    c.rb_coarse = 20
+    c.rb_omega = 1.15
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        path = _build.lib_path()
+        if not path.exists():
+            raise ImportError(f"{path} is missing: run fortranutils_gb300.build.build() first")
+        _lib = C.CDLL(str(path))
+        _lib.lester_gpu_last_error.restype = C.c_char_p
+        _lib.lester_gpu_get_stream.restype = C.c_void_p
+        _lib.lester_gpu_launch_count.restype = C.c_long
+        _lib.lester_gpu_set_stream.argtypes = [C.c_void_p]
+    return _lib
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        raise LesterError(code, lib().lester_gpu_last_error().decode())
+
+
+def _p(a):
+    """Raw pointer of a float64 contiguous torch tensor or numpy array."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+            raise TypeError("arrays must be contiguous float64")
+        return C.c_void_p(a.ctypes.data)
+    import torch  # noqa: F401  (tensor path)
+    if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
+        raise TypeError("tensors must be contiguous float64")
+    return C.c_void_p(a.data_ptr())
+
+
+def _i(v: int):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v: float):
+    return C.byref(C.c_double(float(v)))
+
+
+# ------------------------------------------------------------- lifecycle
+def gpu_init(geom: Geom, ctrl: Ctrl) -> None:
+    _check(lib().lester_gpu_init(C.byref(geom), C.byref(ctrl)))
+
+
+def gpu_set_ctrl(ctrl: Ctrl) -> None:
+    _check(lib().lester_gpu_set_ctrl(C.byref(ctrl)))
+
+
+def gpu_finalize() -> None:
+    _check(lib().lester_gpu_finalize())
+
+
+def gpu_sizes() -> Sizes:
+    s = Sizes()
+    _check(lib().lester_gpu_sizes(C.byref(s)))
+    return s
+
+
+def gpu_block_info(ilev: int, iblk: int):
+    n = (C.c_int * 3)()
+    o = (C.c_long * 5)()
+    _check(lib().lester_gpu_block_info(ilev, iblk, n, o))
+    return tuple(n), tuple(o)
+
+
+def gpu_sync() -> None:
+    _check(lib().lester_gpu_sync())
+
+
+def gpu_stream() -> int:
+    return lib().lester_gpu_get_stream()
+
+
+def gpu_set_jumble(j: int) -> None:
+    _check(lib().lester_gpu_set_jumble(int(j)))
+
+
+def gpu_get_jumble() -> int:
+    return lib().lester_gpu_get_jumble()
+
+
+def gpu_launch_count() -> int:
+    return lib().lester_gpu_launch_count()
+
+
+def gpu_solve_stats():
+    o = (C.c_double * 6)()
+    _check(lib().lester_gpu_solve_stats(o))
+    return {"rnorm": o[0], "fnorm": o[1], "enorm": o[2], "vnorm": o[3], "cycles": int(o[4]),
+            "relres": o[5]}
+
+
+# ----------------------------------------------------- reference routines
+METRIC_NAMES = ("dip diu div dix rdip rdiv rdix djp dju djv djx rdjp rdju rdjx hijp hjip hkip "
+                "hkjp hiju hjiu hkiu hkju hijv hjiv hkiv hkjv rp ru rv didjp rdidjp didju "
+                "rdidju djdiv rdjdiv").split()
+
+
+def swap_sc(ivar1, igrid, var, work=None, mg_or_sg=1):
+    _check(lib().lester_swap_sc(_i(ivar1), _i(igrid), _p(var), None, _i(mg_or_sg)))
+
+
+def comp_metric(x, y, t, metrics: dict, dkp, dkw):
+    args = [_p(metrics[n]) for n in METRIC_NAMES]
+    _check(lib().lester_comp_metric(_p(x), _p(y), _p(t), *args, _p(dkp), _p(dkw), None, None))
+
+
+def coeff_p(diu, djv, rdiv, rdju, didjp, rp, dkp, dkw, ap, aw, ae, as_, an, al, ar):
+    _check(lib().lester_coeff_p(*map(_p, (diu, djv, rdiv, rdju, didjp, rp, dkp, dkw, ap, aw, ae,
+                                          as_, an, al, ar))))
+
+
+def sour_p(diu, djv, rdiv, rdju, didjp, dkp, rdidjp, dkw, u, v, w, rho, rhonp1, drhonp1dt, s,
+           srhot, srhoux):
+    _check(lib().lester_sour_p(*map(_p, (diu, djv, rdiv, rdju, didjp, dkp, rdidjp, dkw, u, v, w,
+                                         rho, rhonp1, drhonp1dt, s, srhot, srhoux)), None, None))
+
+
+def lmg_solve(ap, aw, ae, as_, an, al, ar, f, b, residu):
+    _check(lib().lester_lmg_solve(*map(_p, (ap, aw, ae, as_, an, al, ar, f, b, residu)), None, None))
+
+
+def solvers(ap, aw, ae, as_, an, al, ar, f, b, residu):
+    _check(lib().lester_solvers(*map(_p, (ap, aw, ae, as_, an, al, ar, f, b, residu)), None, None))
+
+
+def norms(ilev, mg_or_sg, ap, aw, ae, as_, an, al, ar, x, b, residu):
+    o = [C.c_double() for _ in range(4)]
+    _check(lib().lester_norms(_i(ilev), _i(mg_or_sg), *map(_p, (ap, aw, ae, as_, an, al, ar, x, b,
+                                                                 residu)),
+                              *[C.byref(v) for v in o]))
+    return tuple(v.value for v in o)
+
+
+def restriction(ilev, f, f1):
+    _check(lib().lester_restriction(_i(ilev), _p(f), _p(f1), None, None))
+
+
+def prolongation(ilev, f):
+    _check(lib().lester_prolongation(_i(ilev), _p(f), None, None))
+
+
+def sporlx(ilev, ap, aw, ae, as_, an, al, ar, f, b, omega, soltol, norms4):
+    o = [C.c_double(v) for v in norms4]
+    _check(lib().lester_sporlx(_i(ilev), *map(_p, (ap, aw, ae, as_, an, al, ar, f, b)), None,
+                               _i(1), _d(omega), _d(soltol), None, None,
+                               *[C.byref(v) for v in o]))
+    return tuple(v.value for v in o)
+
+
+def extrap_p(p):
+    _check(lib().lester_extrap_p(_p(p), None, None))
+
+
+def p_ref_subtract(p):
+    _check(lib().lester_p_ref_subtract(_p(p)))
+
+
+def uvw_adv(ivar1, diu, rp, dkw, u, u_int, rho, p, step=1):
+    _check(lib().lester_uvw_adv(_i(ivar1), *map(_p, (diu, rp, dkw, u, u_int, rho, p)), None, None,
+                                _i(step)))
+
+
+def swap_rhos(rho, rhonp1, rhonm1):
+    _check(lib().lester_swap_rhos(_p(rho), _p(rhonp1), _p(rhonm1)))
+
+
+def search_lib(sc1, sc1var, rhonp1, temperature, istep, alpha, rho, rholo, rhohi):
+    _check(lib().lester_search_lib(_p(sc1), _p(sc1var), _p(rhonp1), _p(temperature), None, None,
+                                   _i(istep), _d(alpha), _p(rho), _d(rholo), _d(rhohi)))
+
+
+def slipbc(x, y, z, dip, diu, djp, djv, dkp, u, v, v_int, w, sc1, rho, p, step=1):
+    _check(lib().lester_slipbc(*map(_p, (x, y, z, dip, diu, djp, djv, dkp, u, v, v_int, w, sc1,
+                                         rho, p)), _i(step)))
+
+
+def subgrid(gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis, vd_damping, dip, diu, djp, djv, dkp,
+            dkw, hijp, hjip, hkip, hkjp, rp):
+    _check(lib().lester_subgrid(*map(_p, (gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis,
+                                          vd_damping, dip, diu, djp, djv, dkp, dkw, hijp, hjip,
+                                          hkip, hkjp, rp)), None, None))

@@ -1,0 +1,261 @@
+/*
+ * lester_gpu.h -- C ABI of the GB300 implementation of the LESter
+ * per-time-step hot path.
+ *
+ * Every routine that the reference's time-step driver (code/step.F) calls on
+ * the hot path has an entry point here with the reference's routine name
+ * prefixed by `lester_`, the same argument order and the same by-reference
+ * calling convention (scalars as pointers, arrays as FP64 arena slices in
+ * Fortran order), so a Fortran build binds them with
+ *     interface; subroutine ... bind(C, name="lester_<routine>") ...
+ * and keeps its own subroutine names.
+ *
+ * What the reference keeps in COMMON blocks (block sizes and links, boundary
+ * types, time step, model and multigrid controls) is passed once to
+ * lester_gpu_init / lester_gpu_set_ctrl.
+ *
+ * Pointers.  Every array argument may be a host pointer or a device pointer
+ * (cudaMalloc / torch).  Host arrays are copied in and the outputs copied
+ * back before the call returns ("strict drop-in" mode).  Device arrays are
+ * used in place and the work is queued on the library's stream
+ * (lester_gpu_get_stream); call lester_gpu_sync() before reading them on the
+ * host.  Workspace arguments of the reference (work, offwork, ia, ra, gia,
+ * gja, swap_geo, pnti) are accepted and ignored: the library owns its
+ * device workspace.
+ *
+ * Errors.  Every entry point returns 0 on success or a negative LES_ERR_*
+ * code; lester_gpu_last_error() gives a message.  No exception crosses the
+ * ABI.  The reference `stop`s on the same conditions (e.g. code/solvers.F:35,
+ * code/set_offset.F:149-151, code/set_interfaces.F:416-422).
+ */
+#ifndef LESTER_GPU_H
+#define LESTER_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LES_MAXBL 64  /* code/dim.inc:68 maxbl */
+#define LES_MAXMGL 16 /* level cap; code/dim.inc:65 has maxmgl = 3 */
+
+#define LES_OK 0
+#define LES_ERR_NOT_INIT -1
+#define LES_ERR_GEOM -2       /* bad block sizes, links or level request */
+#define LES_ERR_ARG -3        /* bad scalar argument */
+#define LES_ERR_CUDA -4       /* CUDA runtime error */
+#define LES_ERR_NOMEM -5      /* device allocation failed */
+#define LES_ERR_NONFINITE -6  /* NaN/Inf seen in a norm */
+#define LES_ERR_NOT_CONVERGED -7
+#define LES_ERR_STRUCTURE -8  /* coefficients lack the aw(i+1) = ae(i) pairing */
+#define LES_ERR_TIMEOUT -9    /* a bounded device wait gave up */
+#define LES_ERR_SIZE -10      /* request exceeds a stated maximum */
+
+/* boundary-condition types, code/bc_type.inc:17-27 */
+#define LES_BCT_WALL 1
+#define LES_BCT_ZERO_GRAD 2
+#define LES_BCT_CONVECTIVE 3
+#define LES_BCT_FIXED 4
+#define LES_BCT_TRACTION 6
+#define LES_BCT_PERIODIC 12
+#define LES_BCT_INTERFACE 13
+
+/* solution variables, code/les.inc:102-106 */
+#define LES_SV_U 1
+#define LES_SV_V 2
+#define LES_SV_W 3
+#define LES_SV_P 4
+#define LES_SV_SC1 5
+
+/* pressure-solver algorithm (lester_ctrl.psolve) */
+#define LES_PSOLVE_REFERENCE 0 /* lmg_solve exactly: lexicographic SOR order */
+#define LES_PSOLVE_FP64 1      /* red-black SOR V-cycles, all FP64 */
+#define LES_PSOLVE_MIXED 2     /* FP32 red-black V-cycles inside FP64 defect correction */
+
+/* Block layout, the content of block.dat and the cb.lgrid.inc tables.
+ * Blocks are 1-based in bl2bl; 0 = no neighbour. */
+typedef struct lester_geom {
+    int numbl;
+    int maxmgl;  /* level cap for the level search (reference: 3) */
+    int nummgl;  /* levels to use; 0 = as many as found */
+    int gotrad;  /* 1 = polar grid (cb.gridp.inc gotrad) */
+    int bl_nijkp1[LES_MAXBL][3]; /* points per axis incl. one ghost per side */
+    int bl_bc[LES_MAXBL][6];     /* boundary type per side W,E,S,N,L,R */
+    int bl2bl[LES_MAXBL][6];
+    int bl2side[LES_MAXBL][6];
+} lester_geom;
+
+/* Controls the reference reads from COMMON (cb.control.inc, defaults.F). */
+typedef struct lester_ctrl {
+    double dtime;      /* time step */
+    double visc;       /* molecular viscosity */
+    double csles;      /* Smagorinsky / WALE constant */
+    double rholo, rhohi;
+    double alpha;      /* density relaxation factor exp(-dt/t_relax) */
+    double ylaminar;   /* const.inc: 11.3 */
+    double kappa;      /* ck: von Karman constant */
+    double cwfun;      /* ca: log-law intercept term */
+    double aplus;      /* van Driest A+ */
+    int model;         /* 0 none, 1 Smagorinsky, 2 WALE */
+    /* multigrid, code/defaults.F:59-71 */
+    int nummgits, numpre, numpost, numcits, meth_cycle;
+    double tolf, relax_pmg, relax_pmgc;
+    /* GPU solver selection */
+    int psolve;        /* LES_PSOLVE_* */
+    double rtol;       /* fast solvers stop at ||b-Ap||/||b|| <= rtol */
+    int max_outer;     /* fast solvers: maximum V-cycles */
+    int rb_sweeps;     /* fast solvers: red-black sweeps per smoothing step */
+    int rb_coarse;     /* fast solvers: sweeps on the coarsest level */
+    double rb_omega;   /* fast solvers: SOR factor */
+} lester_ctrl;
+
+/* Arena slice lengths (elements) implied by the geometry. */
+typedef struct lester_sizes {
+    int nummgl;
+    long n3_sg;  /* one 3-D field, level 1 (sg_off layout) */
+    long n3_mg;  /* one 3-D field, all levels (mg_off layout) */
+    long n2;     /* one 2-D metric, all levels */
+    long n1k;    /* one 1-D k metric, all levels */
+    long nxy;    /* one x or y vertex array, all levels */
+    long nz;     /* z vertex array, all levels */
+    long n2_ki;  /* one 2-D (k,i) wall array, level 1 */
+    long n2_jk;  /* one 2-D (j,k) wall array, level 1 */
+} lester_sizes;
+
+/* ---- lifecycle -------------------------------------------------------- */
+/* Replaces the setup half of step.F:114-120 (set_offset, set_interfaces,
+ * set_loop_bound tables).  No reference counterpart of its own. */
+int lester_gpu_init(const lester_geom *g, const lester_ctrl *c);
+int lester_gpu_set_ctrl(const lester_ctrl *c);
+int lester_gpu_finalize(void);
+int lester_gpu_sizes(lester_sizes *out);
+int lester_gpu_block_info(int ilev, int iblk, int *nijkp1, long *offs);
+int lester_gpu_sync(void);
+void *lester_gpu_get_stream(void);
+int lester_gpu_set_stream(void *stream);
+const char *lester_gpu_last_error(void);
+/* smoother rotation counter, SAVEd in code/sporlx.F:58 */
+int lester_gpu_set_jumble(int jumble);
+int lester_gpu_get_jumble(void);
+/* launches of this library's kernels since the library was loaded */
+long lester_gpu_launch_count(void);
+/* statistics of the last lester_solvers / lester_lmg_solve call:
+ * out[0..3] = rnorm, fnorm, enorm, vnorm of level 1 (code/norms.F:393-398),
+ * out[4] = V-cycles, out[5] = ||b - A p|| / ||b|| */
+int lester_gpu_solve_stats(double *out);
+
+/* ---- halo exchange ---------------------------------------------------- */
+/* code/swap_sc0.F:6 swap_sc(ivar1, igrid, var, work, mg_or_sg) */
+int lester_swap_sc(const int *ivar1, const int *igrid, double *var,
+                   double *work, const int *mg_or_sg);
+
+/* ---- metrics ---------------------------------------------------------- */
+/* code/comp_metric.F:5 comp_metric(x, y, t, dip ... rdjdiv, dkp, dkw,
+ * swap_geo, pnti) */
+int lester_comp_metric(const double *x, const double *y, const double *t,
+                       double *dip, double *diu, double *div, double *dix,
+                       double *rdip, double *rdiv, double *rdix, double *djp,
+                       double *dju, double *djv, double *djx, double *rdjp,
+                       double *rdju, double *rdjx, double *hijp, double *hjip,
+                       double *hkip, double *hkjp, double *hiju, double *hjiu,
+                       double *hkiu, double *hkju, double *hijv, double *hjiv,
+                       double *hkiv, double *hkjv, double *rp, double *ru,
+                       double *rv, double *didjp, double *rdidjp,
+                       double *didju, double *rdidju, double *djdiv,
+                       double *rdjdiv, double *dkp, double *dkw,
+                       double *swap_geo, int *pnti);
+
+/* ---- pressure path ---------------------------------------------------- */
+/* code/coeff_p.F:5 coeff_p(diu, djv, rdiv, rdju, didjp, rp, dkp, dkw,
+ * ap, aw, ae, as, an, al, ar) */
+int lester_coeff_p(const double *diu, const double *djv, const double *rdiv,
+                   const double *rdju, const double *didjp, const double *rp,
+                   const double *dkp, const double *dkw, double *ap,
+                   double *aw, double *ae, double *as, double *an,
+                   double *al, double *ar);
+/* code/sour_p.F:6 sour_p(diu, djv, rdiv, rdju, didjp, dkp, rdidjp, dkw,
+ * u, v, w, rho, rhonp1, Drhonp1Dt, s, srhot, srhoux, gia, gja) */
+int lester_sour_p(const double *diu, const double *djv, const double *rdiv,
+                  const double *rdju, const double *didjp, const double *dkp,
+                  const double *rdidjp, const double *dkw, const double *u,
+                  const double *v, const double *w, const double *rho,
+                  const double *rhonp1, double *drhonp1dt, double *s,
+                  double *srhot, double *srhoux, double *gia, double *gja);
+/* code/solvers.F:5 solvers(ap, aw, ae, as, an, al, ar, f, b, residu, ia, ra)
+ * -> lmg_solve (code/lmg_solve.F:5) for psolver 101.  The algorithm follows
+ * lester_ctrl.psolve.  Coarse-level parts of b and residu are overwritten,
+ * as in the reference. */
+int lester_solvers(const double *ap, const double *aw, const double *ae,
+                   const double *as, const double *an, const double *al,
+                   const double *ar, double *f, double *b, double *residu,
+                   int *ia, double *ra);
+int lester_lmg_solve(const double *ap, const double *aw, const double *ae,
+                     const double *as, const double *an, const double *al,
+                     const double *ar, double *f, double *b, double *residu,
+                     int *ia, double *ra);
+/* code/norms.F:5 norms(ilev, mg_or_sg, ap..ar, x, b, residu,
+ * res_norm, rhs_norm, err_norm, var_norm) */
+int lester_norms(const int *ilev, const int *mg_or_sg, const double *ap,
+                 const double *aw, const double *ae, const double *as,
+                 const double *an, const double *al, const double *ar,
+                 const double *x, const double *b, double *residu,
+                 double *res_norm, double *rhs_norm, double *err_norm,
+                 double *var_norm);
+/* code/restriction.F:5 restriction(ilev, f, f1, work, offwork) */
+int lester_restriction(const int *ilev, const double *f, double *f1,
+                       double *work, int *offwork);
+/* code/prolongation.F:5 prolongation(ilev, f, work, offwork) */
+int lester_prolongation(const int *ilev, double *f, double *work,
+                        int *offwork);
+/* code/sporlx.F:5 sporlx(ilev, ap..ar, f, b, residu, niter, omega, soltol,
+ * work, offwork, res_norm, rhs_norm, err_norm, var_norm) */
+int lester_sporlx(const int *ilev, const double *ap, const double *aw,
+                  const double *ae, const double *as, const double *an,
+                  const double *al, const double *ar, double *f,
+                  const double *b, double *residu, const int *niter,
+                  const double *omega, const double *soltol, double *work,
+                  int *offwork, double *res_norm, double *rhs_norm,
+                  double *err_norm, double *var_norm);
+/* code/extrap_p.F:5 extrap_p(p, work, offwork) */
+int lester_extrap_p(double *p, double *work, int *offwork);
+/* code/p_ref_subtract.F:6 p_ref_subtract(p) */
+int lester_p_ref_subtract(double *p);
+/* code/uvw_adv.F:5 uvw_adv(ivar1, diu, rp, dkw, u, u_int, rho, p, wk,
+ * offwork, step) */
+int lester_uvw_adv(const int *ivar1, const double *diu, const double *rp,
+                   const double *dkw, double *u, const double *u_int,
+                   const double *rho, const double *p, double *wk,
+                   int *offwork, const int *step);
+/* code/swap_rhos.F:5 swap_rhos(rho, rhonp1, rhonm1) */
+int lester_swap_rhos(double *rho, double *rhonp1, double *rhonm1);
+/* code/search_lib.F:5 search_lib(sc1, sc1var, rhonp1, Temperature, work,
+ * offwork, istep, alpha, rho, rholo, rhohi) */
+int lester_search_lib(double *sc1, double *sc1var, double *rhonp1,
+                      double *temperature, double *work, int *offwork,
+                      const int *istep, const double *alpha,
+                      const double *rho, const double *rholo,
+                      const double *rhohi);
+/* code/slipbc.F:3 slipbc(x, y, z, dip, diu, djp, djv, dkp, u, v, v_int, w,
+ * sc1, rho, p, step) */
+int lester_slipbc(const double *x, const double *y, const double *z,
+                  const double *dip, const double *diu, const double *djp,
+                  const double *djv, const double *dkp, double *u, double *v,
+                  const double *v_int, double *w, double *sc1, double *rho,
+                  const double *p, const int *step);
+
+/* ---- eddy viscosity --------------------------------------------------- */
+/* code/subgrid.F:5 subgrid(gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis,
+ * vd_damping, dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp,
+ * work, offwork) */
+int lester_subgrid(double *gam, double *gamsc1, const double *u,
+                   const double *v, const double *w, const double *sc1,
+                   const double *rho, double *sc1var, double *sc1dis,
+                   const double *vd_damping, const double *dip,
+                   const double *diu, const double *djp, const double *djv,
+                   const double *dkp, const double *dkw, const double *hijp,
+                   const double *hjip, const double *hkip, const double *hkjp,
+                   const double *rp, double *work, int *offwork);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,173 @@
+"""ctypes access to the CPU parity oracle (oracle/_build/liblester_oracle.so).
+
+Test infrastructure only: the oracle is the checker, never the thing
+measured or shipped.  It is built from oracle/ by ``make -C oracle``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_SO = ORACLE_DIR / "_build" / "liblester_oracle.so"
+
+_lib = None
+
+
+def build_oracle() -> Path:
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+    return ORACLE_SO
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build_oracle()
+        _lib = C.CDLL(str(ORACLE_SO))
+        _lib.orc_create.restype = C.c_void_p
+        _lib.orc_npts_all.restype = C.c_double
+        for name in dir(_lib):
+            pass
+    return _lib
+
+
+def P(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return C.c_void_p(a.ctypes.data)
+
+
+class MgCtrl(C.Structure):
+    _fields_ = [("nummgits", C.c_int), ("numpre", C.c_int), ("numpost", C.c_int),
+                ("numcits", C.c_int), ("meth_cycle", C.c_int), ("meth_smooth", C.c_int),
+                ("meth_csolve", C.c_int), ("tolf", C.c_double), ("relax_pmg", C.c_double),
+                ("relax_pmgc", C.c_double)]
+
+
+class Oracle:
+    """One oracle context for a grid.Case (levels capped like the case)."""
+
+    def __init__(self, case):
+        self.case = case
+        nb, n, bc, l1, l2 = case.oracle_args()
+        st = C.c_int()
+        self._keep = (n, bc, l1, l2)
+        self.ctx = C.c_void_p(lib().orc_create(nb, n.ctypes.data_as(C.c_void_p),
+                                               bc.ctypes.data_as(C.c_void_p),
+                                               l1.ctypes.data_as(C.c_void_p),
+                                               l2.ctypes.data_as(C.c_void_p), case.maxmgl,
+                                               case.nummgl, C.byref(st)))
+        if st.value != 0:
+            raise RuntimeError(f"orc_create failed: {st.value}")
+
+    def __del__(self):
+        try:
+            lib().orc_destroy(self.ctx)
+        except Exception:
+            pass
+
+    def sizes(self):
+        out = (C.c_long * 9)()
+        lib().orc_sizes(self.ctx, out)
+        return list(out)
+
+    def block_info(self, ilev, iblk):
+        n = (C.c_int * 3)()
+        m = (C.c_int * 3)()
+        o = (C.c_long * 7)()
+        lib().orc_block_info(self.ctx, ilev, iblk, n, m, o)
+        return tuple(n), tuple(m), tuple(o)
+
+    def set_loop_bound(self, ivar):
+        lib().orc_set_loop_bound(self.ctx, ivar)
+
+    def npts_all(self, ilev):
+        return lib().orc_npts_all(self.ctx, ilev)
+
+    def set_jumble(self, j):
+        lib().orc_set_jumble(self.ctx, j)
+
+    def get_jumble(self):
+        return lib().orc_get_jumble(self.ctx)
+
+    def swap_sc(self, igrid, var, mg_or_sg=1):
+        lib().orc_swap_sc(self.ctx, igrid, P(var), mg_or_sg)
+
+    def comp_metric(self, x, y, z, gotrad=0):
+        c = self.case
+        metric = np.zeros(35 * c.n2)
+        dkp = np.zeros(c.n1k)
+        dkw = np.zeros(c.n1k)
+        lib().orc_comp_metric(self.ctx, P(x), P(y), P(z), P(metric), P(dkp), P(dkw), gotrad)
+        return metric.reshape(35, c.n2), dkp, dkw
+
+    def coeff_p(self, m, dkp, dkw, a):
+        lib().orc_coeff_p(self.ctx, *map(P, (m["diu"], m["djv"], m["rdiv"], m["rdju"],
+                                             m["didjp"], m["rp"], dkp, dkw)), *map(P, a))
+
+    def sour_p(self, dtime, m, dkp, dkw, u, v, w, rho, rhonp1, out4):
+        lib().orc_sour_p(self.ctx, C.c_double(dtime),
+                         *map(P, (m["diu"], m["djv"], m["rdiv"], m["rdju"], m["didjp"], dkp,
+                                  m["rdidjp"], dkw, u, v, w, rho, rhonp1)), *map(P, out4))
+
+    def norms(self, ilev, mg_or_sg, a, x, b, residu):
+        out = np.zeros(4)
+        lib().orc_norms(self.ctx, ilev, mg_or_sg, *map(P, a), P(x), P(b), P(residu), P(out))
+        return tuple(out)
+
+    def restriction(self, ilev, f, f1):
+        lib().orc_restriction(self.ctx, ilev, P(f), P(f1))
+
+    def prolongation(self, ilev, f):
+        lib().orc_prolongation(self.ctx, ilev, P(f))
+
+    def sporlx(self, ilev, a, f, b, omega, soltol, norms4):
+        io = np.array(norms4, dtype=np.float64)
+        lib().orc_sporlx(self.ctx, ilev, *map(P, a), P(f), P(b), C.c_double(omega),
+                         C.c_double(soltol), P(io))
+        return tuple(io)
+
+    def lmg_solve(self, ctrl: MgCtrl, a, f, b, residu):
+        out = np.zeros(5)
+        lib().orc_lmg_solve(self.ctx, C.byref(ctrl), *map(P, a), P(f), P(b), P(residu), P(out))
+        return out
+
+    def extrap_p(self, p):
+        lib().orc_extrap_p(self.ctx, P(p))
+
+    def p_ref_subtract(self, p):
+        lib().orc_p_ref_subtract(self.ctx, P(p))
+
+    def uvw_adv(self, ivar, dtime, dg, rp, dkw, u, u_int, rho, p):
+        lib().orc_uvw_adv(self.ctx, ivar, C.c_double(dtime), *map(P, (dg, rp, dkw, u, u_int, rho,
+                                                                       p)))
+
+    def swap_rhos(self, rho, rhonp1, rhonm1):
+        lib().orc_swap_rhos(self.ctx, P(rho), P(rhonp1), P(rhonm1))
+
+    def search_lib(self, sc1, rhonp1, alpha, rho, rholo, rhohi):
+        lib().orc_search_lib(self.ctx, P(sc1), P(rhonp1), C.c_double(alpha), P(rho),
+                             C.c_double(rholo), C.c_double(rhohi))
+
+    def slipbc(self, dtime, djp, u, v, v_int, w, sc1, rho, p):
+        lib().orc_slipbc(self.ctx, C.c_double(dtime), *map(P, (djp, u, v, v_int, w, sc1, rho, p)))
+
+    def subgrid(self, model, csles, gotrad, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m,
+                dkp, dkw):
+        lib().orc_subgrid(self.ctx, model, C.c_double(csles), gotrad,
+                          *map(P, (gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m["dip"],
+                                   m["diu"], m["djp"], m["djv"], dkp, dkw, m["hijp"], m["hjip"],
+                                   m["hkip"], m["hkjp"], m["rp"])))
+
+
+def mgctrl(nummgits=5, numpre=1, numpost=1, numcits=20, meth_cycle=1, tolf=5e-13, relax=1.6):
+    c = MgCtrl()
+    c.nummgits, c.numpre, c.numpost, c.numcits = nummgits, numpre, numpost, numcits
+    c.meth_cycle, c.meth_smooth, c.meth_csolve = meth_cycle, 1, 0
+    c.tolf, c.relax_pmg, c.relax_pmgc = tolf, relax, relax
+    return c
