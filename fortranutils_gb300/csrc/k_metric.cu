@@ -145,7 +145,8 @@ __global__ void k_metric_h(const MetBlk *__restrict__ mb, const double *__restri
 // column (io = 1, jo = nip1, length njp1), for j sides a row.
 struct MetFace {
     long src2, dst2;   // 0-based first element of the packed / ghost line
-    long stride;       // step along the line
+    long stride;       // step along the own (ghost) line
+    long sstride;      // step along the partner's (packed) line
     int len;           // line length
     long srck, dstk;   // 1-D (dkp, dkw) element for k sides, -1 otherwise
 };
@@ -168,7 +169,7 @@ __global__ void k_metric_swap(const MetFace *__restrict__ fc, int nf, MetricPtrs
         int a = (int)(q % 34);
         long jj = q / 34;
         int arr = c_swapped[a];
-        if (phase == 0) b[q] = P.m[arr][f.src2 + f.stride * jj];
+        if (phase == 0) b[q] = P.m[arr][f.src2 + f.sstride * jj];
         else P.m[arr][f.dst2 + f.stride * jj] = b[q];
     }
 }
@@ -215,13 +216,14 @@ void fill_metblk(void *dst, int idx, const int *n, long off2, long off1k, long o
     b->offz = offz;
 }
 
-void fill_metface(void *dst, int idx, long src2, long dst2, long stride, int len, long srck,
-                  long dstk)
+void fill_metface(void *dst, int idx, long src2, long dst2, long stride, long sstride, int len,
+                  long srck, long dstk)
 {
     MetFace *f = (MetFace *)dst + idx;
     f->src2 = src2;
     f->dst2 = dst2;
     f->stride = stride;
+    f->sstride = sstride;
     f->len = len;
     f->srck = srck;
     f->dstk = dstk;

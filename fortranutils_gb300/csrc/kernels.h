@@ -54,8 +54,8 @@ void launch_metric_swap(const void *faces, int nf, long maxlen, double *const *m
 size_t metblk_size();
 size_t metface_size();
 void fill_metblk(void *dst, int idx, const int *n, long off2, long off1k, long offxy, long offz);
-void fill_metface(void *dst, int idx, long src2, long dst2, long stride, int len, long srck,
-                  long dstk);
+void fill_metface(void *dst, int idx, long src2, long dst2, long stride, long sstride, int len,
+                  long srck, long dstk);
 
 // k_sgs.cu
 void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,

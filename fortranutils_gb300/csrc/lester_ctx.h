@@ -63,6 +63,14 @@ struct Ctx {
     // staging buffers for host arguments
     std::vector<void *> stage_buf;
     std::vector<size_t> stage_cap;
+    // kernel timing inside a timed region (lester_gpu_prof): CUDA events
+    // around every launch of the level-1 smoother of the fast solvers
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    long prof_launches = 0;
+    // bytes copied between host and device by staged (host-array) calls
+    long h2d_bytes = 0, d2h_bytes = 0;
     // last solve statistics
     double last_norms[4] = {0, 0, 0, 0};
     int last_cycles = 0;

@@ -82,6 +82,7 @@ int Staging::map(const double *user, long n, bool out, double **dev)
         }
         e.dev = (double *)c_->stage_buf[s];
         LES_CUDA(cudaMemcpyAsync(e.dev, user, bytes, cudaMemcpyHostToDevice, c_->stream));
+        c_->h2d_bytes += (long)bytes;
     }
     ent_.push_back(e);
     *dev = e.dev;
@@ -105,9 +106,11 @@ int Staging::finish()
         return 0;
     }
     for (auto &e : ent_)
-        if (e.host && e.out)
+        if (e.host && e.out) {
             LES_CUDA(cudaMemcpyAsync(const_cast<double *>(e.user), e.dev, (size_t)e.n * sizeof(double),
                                      cudaMemcpyDeviceToHost, c_->stream));
+            c_->d2h_bytes += e.n * (long)sizeof(double);
+        }
     LES_CUDA(cudaStreamSynchronize(c_->stream));
     return 0;
 }
@@ -317,7 +320,7 @@ static int build_faces(Ctx &c)
                 if (s >= 5) {
                     long srck = L.off1k[bn] + ((sn == 5) ? 1 : m[2] - 2);
                     long dstk = L.off1k[b] + ((s == 5) ? 0 : n[2] - 1);
-                    fill_metface(mf.data(), cnt, 0, 0, 0, 0, srck, dstk);
+                    fill_metface(mf.data(), cnt, 0, 0, 0, 0, 0, srck, dstk);
                 } else {
                     // own ghost line and the partner's packed line
                     long src2, dst2, stride;
@@ -336,9 +339,10 @@ static int build_faces(Ctx &c)
                     else
                         src2 = L.off2[bn] + (long)m[0] * ((sn == 3) ? 1 : m[1] - 2);
                     int plen = (sn <= 2) ? m[1] : m[0];
+                    long sstride = (sn <= 2) ? m[0] : 1;
                     if (plen != len)
                         return set_err(LES_ERR_GEOM, "metric exchange: block %d side %d length mismatch", b, s);
-                    fill_metface(mf.data(), cnt, src2, dst2, stride, len, -1, -1);
+                    fill_metface(mf.data(), cnt, src2, dst2, stride, sstride, len, -1, -1);
                     L.maxmetlen = std::max(L.maxmetlen, (long)len);
                 }
                 cnt++;
@@ -376,6 +380,7 @@ static void free_ctx(Ctx *c)
                   c->E64,   c->N64,   c->R64,   c->P64};
     for (void *p : fp) cudaFree(p);
     for (void *p : c->stage_buf) cudaFree(p);
+    for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -572,14 +577,30 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
     return 0;
 }
 
+static cudaEvent_t prof_event(Ctx &c)
+{
+    if (c.ev_used == c.ev_pool.size()) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c.ev_pool.push_back(e);
+    }
+    return c.ev_pool[c.ev_used++];
+}
+
 template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
 {
     FastSet<T> &F = fset<T>(c);
     LevelGeom &L = c.lv[lev];
+    bool prof = c.prof && lev == 1;
     for (int s = 0; s < nsweep; s++)
         for (int color = 0; color < 2; color++) {
+            if (prof) cudaEventRecord(prof_event(c), c.stream);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
                          F.b, c.stream);
+            if (prof) {
+                cudaEventRecord(prof_event(c), c.stream);
+                c.prof_launches++;
+            }
             launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
 }
@@ -765,6 +786,43 @@ int lester_gpu_set_stream(void *s)
     if (g_ctx->own_stream && g_ctx->stream) cudaStreamDestroy(g_ctx->stream);
     g_ctx->stream = (cudaStream_t)s;
     g_ctx->own_stream = false;
+    return 0;
+}
+
+// Kernel timing over a timed region: lester_gpu_prof(1) clears and starts,
+// lester_gpu_prof(0) stops; lester_gpu_prof_read sums the event pairs.
+int lester_gpu_prof(int enable)
+{
+    LES_NEED_CTX();
+    g_ctx->prof = enable != 0;
+    if (enable) {
+        g_ctx->ev_used = 0;
+        g_ctx->prof_launches = 0;
+    }
+    return 0;
+}
+
+int lester_gpu_prof_read(double *ms_total, long *launches)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    double tot = 0;
+    for (size_t q = 0; q + 1 < c.ev_used; q += 2) {
+        float ms = 0;
+        LES_CUDA(cudaEventElapsedTime(&ms, c.ev_pool[q], c.ev_pool[q + 1]));
+        tot += ms;
+    }
+    *ms_total = tot;
+    *launches = c.prof_launches;
+    return 0;
+}
+
+int lester_gpu_xfer_bytes(long *h2d, long *d2h)
+{
+    LES_NEED_CTX();
+    *h2d = g_ctx->h2d_bytes;
+    *d2h = g_ctx->d2h_bytes;
     return 0;
 }
 

@@ -132,8 +132,8 @@ def _p(a):
         if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
             raise TypeError("arrays must be contiguous float64")
         return C.c_void_p(a.ctypes.data)
-    import torch  # noqa: F401  (tensor path)
-    if a.dtype.__repr__() != "torch.float64" or not a.is_contiguous():
+    import torch
+    if a.dtype != torch.float64 or not a.is_contiguous():
         raise TypeError("tensors must be contiguous float64")
     return C.c_void_p(a.data_ptr())
 
@@ -289,3 +289,20 @@ def subgrid(gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis, vd_damping, dip, diu
     _check(lib().lester_subgrid(*map(_p, (gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis,
                                           vd_damping, dip, diu, djp, djv, dkp, dkw, hijp, hjip,
                                           hkip, hkjp, rp)), None, None))
+
+
+def gpu_prof(enable: bool) -> None:
+    _check(lib().lester_gpu_prof(1 if enable else 0))
+
+
+def gpu_prof_read():
+    ms = C.c_double()
+    n = C.c_long()
+    _check(lib().lester_gpu_prof_read(C.byref(ms), C.byref(n)))
+    return ms.value, n.value
+
+
+def gpu_xfer_bytes():
+    a, b = C.c_long(), C.c_long()
+    _check(lib().lester_gpu_xfer_bytes(C.byref(a), C.byref(b)))
+    return a.value, b.value

@@ -142,6 +142,14 @@ long lester_gpu_launch_count(void);
  * out[0..3] = rnorm, fnorm, enorm, vnorm of level 1 (code/norms.F:393-398),
  * out[4] = V-cycles, out[5] = ||b - A p|| / ||b|| */
 int lester_gpu_solve_stats(double *out);
+/* kernel timing inside a timed region: CUDA events around each launch of
+ * the level-1 red-black smoother of the fast solvers.  prof(1) clears and
+ * starts, prof(0) stops; prof_read returns the summed milliseconds and the
+ * number of timed launches. */
+int lester_gpu_prof(int enable);
+int lester_gpu_prof_read(double *ms_total, long *launches);
+/* bytes copied host->device and device->host by calls with host arrays */
+int lester_gpu_xfer_bytes(long *h2d, long *d2h);
 
 /* ---- halo exchange ---------------------------------------------------- */
 /* code/swap_sc0.F:6 swap_sc(ivar1, igrid, var, work, mg_or_sg) */
