@@ -143,8 +143,14 @@ class GpuStep:
         f = initial_fields(case)
         self.u0 = {k: dev(v) for k, v in f.items()}
         self.u, self.v, self.w = (self.u0[k].clone() for k in "uvw")
-        self.ui, self.vi, self.wi = (self.u0[k].clone() for k in "uvw")
         self.sc1, self.rho = self.u0["sc1"].clone(), self.u0["rho"].clone()
+        # slip faces first (v = 0 on the walls), so the pressure source is
+        # compatible with the all-Neumann/periodic pressure problem
+        L.slipbc(None, None, None, None, None, self.m["djp"], None, None, self.u, self.v,
+                 z3(), self.w, self.sc1, self.rho, z3())
+        for fld in (self.u, self.v, self.w, self.sc1, self.rho):
+            L.swap_sc(0, 1, fld, mg_or_sg=2)
+        self.ui, self.vi, self.wi = self.u.clone(), self.v.clone(), self.w.clone()
         self.rhonp1 = self.rho.clone()
         self.gam, self.gamsc1, self.sc1var, self.sc1dis = (z3() for _ in range(4))
         self.vdd = torch.ones(c.n3_sg, dtype=torch.float64, device="cuda")
@@ -191,7 +197,7 @@ def run_gpu(args, rank):
                               rtol=1e-8, max_outer=200)
         L.gpu_init(case.geom(), ctrl)
         st = GpuStep(case, dtime)
-        stream = torch.cuda.ExternalStream(L.gpu_stream())
+        stream = torch.cuda.current_stream()
         for _ in range(args.warmup):
             st.step()
         L.gpu_sync()

@@ -31,6 +31,9 @@ UNITS = {
     "k_metric.cu": ["-fmad=false"],
     "k_sgs.cu": ["-fmad=false"],
     "k_fast.cu": [],
+    "k_phys.cu": ["-fmad=false"],
+    "lester_phys_host.cu": [],
+    "k_virtbc.cu": ["-fmad=false"],
 }
 
 

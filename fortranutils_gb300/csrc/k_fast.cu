@@ -49,6 +49,10 @@ __global__ void k_conv_coef(const BlkDev *__restrict__ blk, const double *__rest
     else if (as[p] != an[p - jo]) atomicOr(bad, 2);
     if (k == 2) R[p - ko] = (T)al[p];
     else if (al[p] != ar[p - ko]) atomicOr(bad, 4);
+    // a row whose diagonal exceeds its off-diagonal sum makes the operator
+    // non-singular (bit 8); coeff_p's pure-Neumann/periodic rows never do
+    double off = aw[p] + ae[p] + as[p] + an[p] + al[p] + ar[p];
+    if (fabs(ap[p] - off) > 1e-12 * fabs(ap[p])) atomicOr(bad, 8);
     if (E64) {
         E64[p] = ae[p];
         N64[p] = an[p];
@@ -220,6 +224,37 @@ __global__ void k_sum2_final(const double *__restrict__ partial, long nparts, do
     }
 }
 
+// Coarsest level of a singular (pure Neumann / periodic) operator: remove
+// the mean of the right-hand side over all interior points so the coarse
+// problem is compatible and its smoothing cannot drift along the constant
+// null vector.  One CTA; the level has a few hundred points at most.
+template <typename T>
+__global__ void k_coarse_mean(const BlkDev *__restrict__ blk, int nb, T *__restrict__ bb)
+{
+    double v[2] = {0., 0.};
+    for (int ib = 0; ib < nb; ib++) {
+        const BlkDev b = blk[ib];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            long p = decode_interior(b, q, i, j, k);
+            v[0] += (double)bb[p];
+            v[1] += 1.0;
+        }
+    }
+    __shared__ double tot[2];
+    block_reduce_store<2>(v, tot);
+    __syncthreads();
+    T mean = (T)(tot[0] / tot[1]);
+    for (int ib = 0; ib < nb; ib++) {
+        const BlkDev b = blk[ib];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            long p = decode_interior(b, q, i, j, k);
+            bb[p] -= mean;
+        }
+    }
+}
+
 // p += e on the interior of level 1
 template <typename T>
 __global__ void k_update(const BlkDev *__restrict__ blk, double *__restrict__ p,
@@ -299,6 +334,13 @@ void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E
 }
 
 template <typename T>
+void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st)
+{
+    k_coarse_mean<T><<<1, 512, 0, st>>>(blk, nb, b);
+    count_launch(1);
+}
+
+template <typename T>
 void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st)
 {
     k_update<T><<<dim3(nb_(maxcell, 256), nb), 256, 0, st>>>(blk, p, e);
@@ -321,7 +363,8 @@ void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *
                                         const double *, const double *, const double *,           \
                                         const double *, const double *, T *, double *, double *,  \
                                         cudaStream_t);                                            \
-    template void launch_update<T>(const BlkDev *, int, long, double *, const T *, cudaStream_t);
+    template void launch_update<T>(const BlkDev *, int, long, double *, const T *, cudaStream_t); \
+    template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);
 INST(float)
 INST(double)
 #undef INST

@@ -1,0 +1,674 @@
+// k_phys.cu -- momentum predictor and scalar transport (FP64, -fmad=false).
+//
+//   set_u_int_block  code/set_u_int_block.F:103-462 (u, and v with the i/j
+//                    roles swapped exactly as set_uv_int passes them)
+//   set_w_int_block  code/set_w_int_block.F:95-458
+//   set_gamsc1_bc    code/set_gamsc1_bc.F
+//   set_sc1_block    code/set_sc1_block.F:66-505 -- sc1 is updated in place
+//                    in the loop order j, i, k, so every point reads new
+//                    values at its -1/-2 neighbours on each axis and old
+//                    values at +1/+2.  Points of one hyperplane i+j+k = s
+//                    are independent, so sweeping s upward reproduces the
+//                    reference's result exactly.
+//   set_sc1_bc       code/set_sc1_bc.F
+//   set_sc1var_block code/set_sc1var_block.F:26-66
+#include "k_common.cuh"
+#include "kernels.h"
+
+#define IDX2(b, i, j) ((b).off2 + ((i) - 1) + (long)(b).n[0] * ((j) - 1))
+
+// ------------------------------------------------------------- predictor
+// u (iva = 1): nip1, njp1 = n[0], n[1]; io = 1, jo = n[0].
+// v (iva = 2): nip1, njp1 = n[1], n[0]; io = n[0], jo = 1 (set_uv_int.F:119-142).
+__global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ blk, int iva,
+                                                   UIntArgs A_, double dtime, int iststep,
+                                                   double visc, double ylaminar, double kappa,
+                                                   double cwfun)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int ir, jr, k;
+    long ijk = decode_interior(b, q, ir, jr, k);
+    int i = iva == 1 ? ir : jr, j = iva == 1 ? jr : ir;
+    int nip1 = iva == 1 ? b.n[0] : b.n[1], njp1 = iva == 1 ? b.n[1] : b.n[0], nkp1 = b.n[2];
+    long io = iva == 1 ? 1 : b.n[0], jo = iva == 1 ? b.n[0] : 1, ko = (long)b.n[0] * b.n[1];
+    long io_ij = io, jo_ij = jo;
+    int d1 = iva == 1 ? 0 : 2, d2 = iva == 1 ? 2 : 0;  // first side of each axis
+    int s0 = b.bc[d1];
+    int istart = (s0 != LES_BCT_PERIODIC_D && s0 != LES_BCT_INTERFACE_D) ? 3 : 2;
+    if (i < istart) return;
+    bool wallsf = b.bc[d2] == LES_BCT_WALL_D, wallnf = b.bc[d2 + 1] == LES_BCT_WALL_D;
+    bool walllf = b.bc[4] == LES_BCT_WALL_D, wallrf = b.bc[5] == LES_BCT_WALL_D;
+    int nj = njp1 - 1, nk = nkp1 - 1;
+    double st1 = iststep - 1, st2 = iststep - 2, stden = 1.0 / iststep;
+    const double *u = A_.u, *v = A_.v, *w = A_.w, *rho = A_.rho, *gam = A_.gam;
+    long o2 = b.off2;
+    // 0-based 2-D positions of ij, ijw, ijs, ijn, ijnw
+    long ij = o2 + io_ij * (i - 1) + jo_ij * (j - 1);
+    long ijw = ij - io_ij, ijs = ij - jo_ij, ijn = ij + jo_ij, ijnw = ijw + jo_ij;
+    long ki = b.off1k * 0 + (k - 1) + (long)nkp1 * (i - 1);  // (k, i) of this block's wall array
+    const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
+    double di = A_.diu[ij], dj = A_.dju[ij];
+    long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
+    long ijksw = ijks - io, ijknw = ijkn - io, ijkwl = ijkw - ko, ijkwr = ijkw + ko;
+    double rdkp = A_.rp[ij] * dkp[k - 1];
+    double rdku = A_.ru[ij] * dkp[k - 1];
+    double va = 0.25 * (v[ijk] + v[ijkn] + v[ijkw] + v[ijknw]);
+    double wa = 0.25 * (w[ijk] + w[ijkr] + w[ijkw] + w[ijkwr]);
+    double rhoa = 0.5 * (rho[ijkw] + rho[ijk]);
+    double gama = 0.5 * (gam[ijkw] + gam[ijk]);
+    double rhowf = rho[ijkw], rhoef = rho[ijk];
+    double rhosf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijks] + rho[ijksw]);
+    double rhonf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijkn] + rho[ijknw]);
+    double rholf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijkl] + rho[ijkwl]);
+    double rhorf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijkr] + rho[ijkwr]);
+    double rhou = 0.5 * (rho[ijk] + rho[ijkw]);
+    double rhonp1u = 0.5 * (A_.rhonp1[ijk] + A_.rhonp1[ijkw]);
+    double gamwf = visc + gam[ijkw] * rhowf;
+    double gamef = visc + gam[ijk] * rhoef;
+    double gamsf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijks] + gam[ijksw]) * rhosf;
+    double gamnf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkn] + gam[ijknw]) * rhonf;
+    double gamlf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkl] + gam[ijkwl]) * rholf;
+    double gamrf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkr] + gam[ijkwr]) * rhorf;
+    double areawf = A_.rdjp[ijw] * dkp[k - 1];
+    double areaef = A_.rdjp[ij] * dkp[k - 1];
+    double areasf = A_.rdix[ij] * dkp[k - 1];
+    double areanf = A_.rdix[ijn] * dkp[k - 1];
+    double areak = A_.didju[ij];
+    double vol = A_.rdidju[ij] * dkp[k - 1];
+    double uwf = 0.5 * (u[ijk] + u[ijkw]);
+    double uef = 0.5 * (u[ijk] + u[ijke]);
+    double vsf = 0.5 * (v[ijk] + v[ijkw]);
+    double vnf = 0.5 * (v[ijkn] + v[ijknw]);
+    double wlf = 0.5 * (w[ijk] + w[ijkw]);
+    double wrf = 0.5 * (w[ijkr] + w[ijkwr]);
+    double gwf = uwf * uwf * rhowf * areawf;
+    double gef = uef * uef * rhoef * areaef;
+    double gsf = 0.5 * (u[ijk] + u[ijks]) * vsf * rhosf * areasf;
+    double gnf = 0.5 * (u[ijk] + u[ijkn]) * vnf * rhonf * areanf;
+    double glf = 0.5 * (u[ijk] + u[ijkl]) * wlf * rholf * areak;
+    double grf = 0.5 * (u[ijk] + u[ijkr]) * wrf * rhorf * areak;
+    double conf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
+    double cc1 = A_.hjiu[ij] * rhoa * (va * va) * vol;
+    double cc2 = A_.hkiu[ij] * rhoa * (wa * wa) * vol;
+    double cc3 = -A_.hiju[ij] * rhoa * va * u[ijk] * vol;
+    double conc = cc1 + cc2 + cc3;
+    double galwf = gamwf * areawf / A_.dip[ijw];
+    double galef = gamef * areaef / A_.dip[ij];
+    double galsf = gamsf * areasf / A_.djx[ij];
+    double galnf = gamnf * areanf / A_.djx[ijn];
+    double gallf = gamlf * areak / (A_.rp[ij] * dkw[k - 1]);
+    double galrf = gamrf * areak / (A_.rp[ij] * dkw[k]);
+    double vwf = 0.5 * (v[ijkw] + v[ijknw]);
+    double vef = 0.5 * (v[ijk] + v[ijkn]);
+    double twf = galwf * 2.0 * (u[ijk] - u[ijkw]);
+    double tef = galef * 2.0 * (u[ijke] - u[ijk]);
+    double tsf = galsf * A_.dix[ij] * (u[ijk] / A_.diu[ij] - u[ijks] / A_.diu[ijs]);
+    double tnf = galnf * A_.dix[ijn] * (u[ijkn] / A_.diu[ijn] - u[ijk] / A_.diu[ij]);
+    double tlf = gallf * (u[ijk] - u[ijkl]);
+    double trf = galrf * (u[ijkr] - u[ijk]);
+    double cwf = 2.0 * gamwf * areawf * vwf * A_.hijp[ijw];
+    double cef = 2.0 * gamef * areaef * vef * A_.hijp[ij];
+    double csf = gamsf * areasf * A_.djx[ij] * (v[ijk] / A_.djv[ij] - v[ijkw] / A_.djv[ijw]) / A_.dix[ij];
+    double cnf = gamnf * areanf * A_.djx[ijn] * (v[ijkn] / A_.djv[ijn] - v[ijknw] / A_.djv[ijnw]) /
+                 A_.dix[ijn];
+    double clf = gamlf * areak * A_.ru[ij] * (w[ijk] / A_.rp[ij] - w[ijkw] / A_.rp[ijw]) / A_.diu[ij];
+    double crf = gamrf * areak * A_.ru[ij] * (w[ijkr] / A_.rp[ij] - w[ijkwr] / A_.rp[ijw]) / A_.diu[ij];
+    double tiiwf = twf + cwf, tiief = tef + cef, tjisf = tsf + csf, tjinf = tnf + cnf;
+    double tkilf = tlf + clf, tkirf = trf + crf;
+    vsf = 0.5 * (v[ijk] + v[ijkw]);
+    vnf = 0.5 * (v[ijkn] + v[ijknw]);
+    double dc1 = -2.0 * gama * vol * A_.hjiu[ij] * ((vnf - vsf) / A_.dju[ij] + u[ijk] * A_.hjiu[ij]);
+    wlf = 0.5 * (w[ijk] + w[ijkw]);
+    wrf = 0.5 * (w[ijkr] + w[ijkwr]);
+    double dc2 = -2.0 * gama * vol * A_.hkiu[ij] * (u[ijk] * A_.hkiu[ij] + va * A_.hkju[ij] + (wrf - wlf) / rdkp);
+    double udisf = 0.5 * (u[ijk] + u[ijks]) / A_.dix[ij];
+    double udinf = 0.5 * (u[ijk] + u[ijkn]) / A_.dix[ijn];
+    double vdjwf = 0.5 * (v[ijkw] + v[ijknw]) / A_.djp[ijw];
+    double vdjef = 0.5 * (v[ijk] + v[ijkn]) / A_.djp[ij];
+    double dc3 = gama * vol * A_.hiju[ij] * (di * (udinf - udisf) / dj + dj * (vdjef - vdjwf) / di);
+    double diffc = dc1 + dc2 + dc3;
+    // log-law wall stress (set_u_int_block.F:353-439)
+    long kio = (iva == 1 ? A_.off_ki : A_.off_jk)[blockIdx.y];
+    long ijo = b.off2 - A_.off2_lev1_base;
+    double dist, tw_mean, ut_mean, yplus_mean, uloglaw, tw;
+    if (wallsf && j == 2) {
+        double *twa = A_.tw_s + kio;
+        dist = 0.5 * A_.dju[ij];
+        tw_mean = fabs(twa[ki]);
+        ut_mean = sqrt(tw_mean / rhosf);
+        yplus_mean = dist * ut_mean * rhosf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = u[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * u[ijk] / dist;
+        }
+        tjisf = areasf * tw;
+        twa[ki] = (st1 * (tw + twa[ki]) - st2 * tw) * stden;
+    }
+    if (wallnf && j == nj) {
+        double *twa = A_.tw_n + kio;
+        dist = 0.5 * A_.dju[ij];
+        tw_mean = fabs(twa[ki]);
+        ut_mean = sqrt(tw_mean / rhonf);
+        yplus_mean = dist * ut_mean * rhonf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = u[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * u[ijk] / dist;
+        }
+        tjinf = -areanf * tw;
+        twa[ki] = (st1 * (-tw + twa[ki]) - st2 * (-tw)) * stden;
+    }
+    long ijl = ijo + (ij - o2);  // this cell's entry of the (i, j) wall arrays
+    if (walllf && k == 2) {
+        double *twa = A_.tw_l;
+        dist = 0.5 * rdku;
+        tw_mean = fabs(twa[ijl]);
+        ut_mean = sqrt(tw_mean / rholf);
+        yplus_mean = dist * ut_mean * rholf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = u[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * u[ijk] / dist;
+        }
+        tkilf = areak * tw;
+        twa[ijl] = (st1 * (tw + twa[ijl]) - st2 * tw) * stden;
+    }
+    if (wallrf && k == nk) {
+        double *twa = A_.tw_r;
+        dist = 0.5 * rdku;
+        tw_mean = fabs(twa[ijl]);
+        ut_mean = sqrt(tw_mean / rhorf);
+        yplus_mean = dist * ut_mean * rhorf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = u[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * u[ijk] / dist;
+        }
+        tkirf = -areak * tw;
+        twa[ijl] = (st1 * (-tw + twa[ijl]) - st2 * (-tw)) * stden;
+    }
+    double h = conf + conc + diffc + tiief - tiiwf + tjinf - tjisf + tkirf - tkilf;
+    A_.u_int[ijk] = u[ijk] * (rhou / rhonp1u) +
+                    dtime / (rhonp1u * vol) * (1.5 * h - 0.5 * A_.hu[ijk] + 0.5 * (A_.p[ijk] - A_.p[ijkw]) * vol / A_.diu[ij]);
+    A_.hu[ijk] = h;
+    (void)nip1;
+}
+
+// code/set_w_int_block.F:95-458 (real i, j, k; k from kstart)
+__global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ blk, WIntArgs A_,
+                                                   double dtime, int iststep, double visc,
+                                                   double ylaminar, double kappa, double cwfun)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    long ijk = decode_interior(b, q, i, j, k);
+    int kstart = (b.bc[4] != LES_BCT_PERIODIC_D && b.bc[4] != LES_BCT_INTERFACE_D) ? 3 : 2;
+    if (k < kstart) return;
+    int nkp1 = b.n[2], ni = b.n[0] - 1, nj = b.n[1] - 1;
+    long io = 1, jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    double st1 = iststep - 1, st2 = iststep - 2, stden = 1.0 / iststep;
+    const double w_wall = 0.0;
+    const double *u = A_.u, *v = A_.v, *w = A_.w, *rho = A_.rho, *gam = A_.gam;
+    const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
+    const double *const *M = A_.m;
+#define G(a, ii, jj) M[a][IDX2(b, ii, jj)]
+    double radp = G(MW_RP, i, j), radw = G(MW_RP, i - 1, j), rade = G(MW_RP, i + 1, j);
+    double rads = G(MW_RP, i, j - 1), radn = G(MW_RP, i, j + 1);
+    long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
+    long ijkwl = ijkw - ko, ijksl = ijks - ko, ijkel = ijke - ko, ijknl = ijkn - ko;
+    double rhowf = 0.25 * (rho[ijk] + rho[ijkl] + rho[ijkw] + rho[ijkwl]);
+    double rhoef = 0.25 * (rho[ijk] + rho[ijkl] + rho[ijke] + rho[ijkel]);
+    double rhosf = 0.25 * (rho[ijk] + rho[ijkl] + rho[ijks] + rho[ijksl]);
+    double rhonf = 0.25 * (rho[ijk] + rho[ijkl] + rho[ijkn] + rho[ijknl]);
+    double rholf = rho[ijkl], rhorf = rho[ijk];
+    double rhow = 0.5 * (rho[ijk] + rho[ijkl]);
+    double rhonp1w = 0.5 * (A_.rhonp1[ijk] + A_.rhonp1[ijkl]);
+    double gamwf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijkw] + gam[ijkwl]) * rhowf;
+    double gamef = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijke] + gam[ijkel]) * rhoef;
+    double gamsf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijks] + gam[ijksl]) * rhosf;
+    double gamnf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijkn] + gam[ijknl]) * rhonf;
+    double gamlf = visc + gam[ijkl] * rholf;
+    double gamrf = visc + gam[ijk] * rhorf;
+    double areawf = G(MW_RDJU, i, j) * dkw[k - 1];
+    double areaef = G(MW_RDJU, i + 1, j) * dkw[k - 1];
+    double areasf = G(MW_RDIV, i, j) * dkw[k - 1];
+    double areanf = G(MW_RDIV, i, j + 1) * dkw[k - 1];
+    double areak = G(MW_DIDJP, i, j);
+    double vol = G(MW_RDIDJP, i, j) * dkw[k - 1];
+    double uwf = 0.5 * (u[ijk] + u[ijkl]);
+    double uef = 0.5 * (u[ijke] + u[ijkel]);
+    double vsf = 0.5 * (v[ijk] + v[ijkl]);
+    double vnf = 0.5 * (v[ijkn] + v[ijknl]);
+    double wlf = 0.5 * (w[ijk] + w[ijkl]);
+    double wrf = 0.5 * (w[ijkr] + w[ijk]);
+    double gwf = 0.5 * (w[ijk] + w[ijkw]) * uwf * rhowf * areawf;
+    double gef = 0.5 * (w[ijk] + w[ijke]) * uef * rhoef * areaef;
+    double gsf = 0.5 * (w[ijk] + w[ijks]) * vsf * rhosf * areasf;
+    double gnf = 0.5 * (w[ijk] + w[ijkn]) * vnf * rhonf * areanf;
+    double glf = wlf * wlf * rholf * areak;
+    double grf = wrf * wrf * rhorf * areak;
+    double conf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
+    double u_wc = 0.25 * (u[ijk] + u[ijke] + u[ijkl] + u[ijkel]);
+    double v_wc = 0.25 * (v[ijk] + v[ijkn] + v[ijkl] + v[ijknl]);
+    double conc = -vol * rhow * (w[ijk] * (u_wc * G(MW_HKIP, i, j) + v_wc * G(MW_HKJP, i, j)));
+    double galwf = gamwf * areawf / G(MW_DIU, i, j);
+    double galef = gamef * areaef / G(MW_DIU, i + 1, j);
+    double galsf = gamsf * areasf / G(MW_DJV, i, j);
+    double galnf = gamnf * areanf / G(MW_DJV, i, j + 1);
+    double gallf = gamlf * areak / (radp * dkp[k - 2]);
+    double galrf = gamrf * areak / (radp * dkp[k - 1]);
+    double radwf = 0.5 * (radp + radw), radef = 0.5 * (radp + rade);
+    double radsf = 0.5 * (radp + rads), radnf = 0.5 * (radp + radn);
+    double ulf = 0.5 * (u[ijkl] + u[ijkel]), urf = 0.5 * (u[ijk] + u[ijke]);
+    double vlf = 0.5 * (v[ijkl] + v[ijknl]), vrf = 0.5 * (v[ijk] + v[ijkn]);
+    double wwf = 0.5 * (w[ijk] + w[ijkw]), wef = 0.5 * (w[ijk] + w[ijke]);
+    double wsf = 0.5 * (w[ijk] + w[ijks]), wnf = 0.5 * (w[ijk] + w[ijkn]);
+    double twf = galwf * radwf * (w[ijk] / radp - w[ijkw] / radw);
+    double tef = galef * radef * (w[ijke] / rade - w[ijk] / radp);
+    double tsf = galsf * (w[ijk] - w[ijks]);
+    double tnf = galnf * (w[ijkn] - w[ijk]);
+    double tlf = 2.0 * gallf * (w[ijk] - w[ijkl]);
+    double trf = 2.0 * galrf * (w[ijkr] - w[ijk]);
+    double cwf = gamwf * areawf * ((u[ijk] - u[ijkl]) / dkw[k - 1] / radwf - wwf * G(MW_HKIU, i, j));
+    double cef = gamef * areaef * ((u[ijke] - u[ijkel]) / dkw[k - 1] / radef - wef * G(MW_HKIU, i + 1, j));
+    double csf = (j == 2) ? 0.0
+                          : gamsf * areasf * ((v[ijk] - v[ijkl]) / dkw[k - 1] / radsf - wsf * G(MW_HKJV, i, j));
+    double cnf = gamnf * areanf * ((v[ijkn] - v[ijknl]) / dkw[k - 1] / radnf - wnf * G(MW_HKJV, i, j + 1));
+    double clf = 2.0 * gamlf * areak * (ulf * G(MW_HKIP, i, j) + vlf * G(MW_HKJP, i, j));
+    double crf = 2.0 * gamrf * areak * (urf * G(MW_HKIP, i, j) + vrf * G(MW_HKJP, i, j));
+    double dwdy = (wnf - wsf) / G(MW_DJP, i, j);
+    double dvdz = (vrf - vlf) / (radp * dkw[k - 1]);
+    double dwdx = (wef - wwf) / G(MW_DIP, i, j);
+    double dudz = (urf - ulf) / (radp * dkw[k - 1]);
+    double diffc1 = G(MW_HKIP, i, j) * (dwdx + dudz - w[ijk] * G(MW_HKIP, i, j)) * vol * gamrf;
+    double diffc2 = G(MW_HKJP, i, j) * (dwdy + dvdz - w[ijk] * G(MW_HKJP, i, j)) * vol * gamrf;
+    double diffc = diffc1 + diffc2;
+    double tikwf = twf + cwf, tikef = tef + cef, tjksf = tsf + csf, tjknf = tnf + cnf;
+    double tkklf = tlf + clf, tkkrf = trf + crf;
+    double dist, tw_mean, ut_mean, yplus_mean, uloglaw, tw;
+    long kj = A_.off_jk[blockIdx.y] + (k - 1) + (long)nkp1 * (j - 1);
+    long kii = A_.off_ki[blockIdx.y] + (k - 1) + (long)nkp1 * (i - 1);
+    if (b.bc[0] == LES_BCT_WALL_D && i == 2) {
+        double *t_ = A_.tw_wfk;
+        dist = 0.5 * G(MW_DIP, i, j);
+        tw_mean = fabs(t_[kj]);
+        ut_mean = sqrt(tw_mean / rhowf);
+        yplus_mean = dist * ut_mean * rhowf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = w[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * w[ijk] / dist;
+        }
+        tikwf = areawf * tw;
+        t_[kj] = (st1 * (tw + t_[kj]) - st2 * tw) * stden;
+    }
+    if (b.bc[1] == LES_BCT_WALL_D && i == ni) {
+        double *t_ = A_.tw_efk;
+        dist = 0.5 * G(MW_DIP, i, j);
+        tw_mean = fabs(t_[kj]);
+        ut_mean = sqrt(tw_mean / rhoef);
+        yplus_mean = dist * ut_mean * rhoef / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = w[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * w[ijk] / dist;
+        }
+        tikef = -areaef * tw;
+        t_[kj] = (st1 * (-tw + t_[kj]) - st2 * (-tw)) * stden;
+    }
+    if (b.bc[2] == LES_BCT_WALL_D && j == 2) {
+        double *t_ = A_.tw_sfk;
+        dist = 0.5 * G(MW_DJP, i, j);
+        tw_mean = fabs(t_[kii]);
+        ut_mean = sqrt(tw_mean / rhosf);
+        yplus_mean = dist * ut_mean * rhosf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = w[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * (w[ijk] - w_wall) / dist;
+        }
+        tjksf = areasf * (tw - w_wall / 0.005 * visc);
+        t_[kii] = (st1 * (tw + t_[kii]) - st2 * tw) * stden;
+    }
+    if (b.bc[3] == LES_BCT_WALL_D && j == nj) {
+        double *t_ = A_.tw_nfk;
+        dist = 0.5 * G(MW_DJP, i, j);
+        tw_mean = fabs(t_[kii]);
+        ut_mean = sqrt(tw_mean / rhonf);
+        yplus_mean = dist * ut_mean * rhonf / visc;
+        if (yplus_mean > ylaminar) {
+            uloglaw = ut_mean / kappa * (log(yplus_mean) + cwfun);
+            tw = w[ijk] * tw_mean / uloglaw;
+        } else {
+            tw = visc * (w[ijk] - w_wall) / dist;
+        }
+        tjknf = -areanf * (tw + w_wall / 0.015 * visc);
+        t_[kii] = (st1 * (-tw + t_[kii]) - st2 * (-tw)) * stden;
+    }
+    double difff = tikef - tikwf + tjknf - tjksf + tkkrf - tkklf;
+    double h = conf + conc + difff + diffc;
+    A_.w_int[ijk] = w[ijk] * (rhow / rhonp1w) +
+                    dtime / (vol * rhonp1w) * (1.5 * h - 0.5 * A_.hw[ijk] + 0.5 * areak * (A_.p[ijk] - A_.p[ijkl]));
+    A_.hw[ijk] = h;
+#undef G
+}
+
+// ---------------------------------------------------------- scalar
+// gamlam := visc / 0.72 everywhere (set_gamsc1_bc.F first loop)
+__global__ void k_fill(double *__restrict__ a, double val, long n)
+{
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        a[q] = val;
+}
+
+// Face cells of set_gamsc1_bc / set_sc1_bc: segment 0 = i sides over
+// (j, k), 1 = j sides over (i, k), 2 = k sides over (i, j); interiors of
+// the faces only, so no two threads touch the same ghost.  mode 0 =
+// set_gamsc1_bc (gamsc1, gamlam and the interface gradients), mode 1 =
+// set_sc1_bc on `f`.
+__global__ void k_face_bc(const BlkDev *__restrict__ blk, int mode, double *__restrict__ f,
+                          double *__restrict__ gam, double *__restrict__ gaml,
+                          const double *__restrict__ sc1, const double *__restrict__ diu,
+                          const double *__restrict__ djv, const double *__restrict__ rp,
+                          const double *__restrict__ dkp, double *__restrict__ grad, long gstride,
+                          int gm)
+{
+    const BlkDev b = blk[blockIdx.z];
+    int seg = blockIdx.y;
+    int nip1 = b.n[0], njp1 = b.n[1], nkp1 = b.n[2];
+    int ni = nip1 - 1, nj = njp1 - 1, nk = nkp1 - 1;
+    long jo = nip1, ko = (long)nip1 * njp1;
+    int na, nb_;
+    if (seg == 0) { na = nj - 1; nb_ = nk - 1; }
+    else if (seg == 1) { na = ni - 1; nb_ = nk - 1; }
+    else { na = ni - 1; nb_ = nj - 1; }
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)na * nb_) return;
+    int a = (int)(q % na) + 2, c = (int)(q / na) + 2;
+    long base = b.off3 - 1;  // 1-based index -> 0-based position
+    double *G6 = grad + (long)blockIdx.z * 6 * gstride;
+    long st[2];
+    int sides[2];
+    long ghost[2], inner[2], per[2];
+    long gpos[2];
+    double gval[2] = {0., 0.};
+    if (seg == 0) {
+        int j = a, k = c;
+        long jk = jo * (j - 1) + ko * (k - 1);
+        sides[0] = 0; sides[1] = 1;
+        ghost[0] = 1 + jk; inner[0] = 2 + jk; per[0] = ni + jk;
+        ghost[1] = nip1 + jk; inner[1] = nip1 - 1 + jk; per[1] = 2 + jk;
+        if (mode == 0) {
+            long d2 = IDX2(b, 3, j), d2e = IDX2(b, ni, j);
+            gval[0] = (sc1[base + 3 + jk] - sc1[base + 2 + jk]) / diu[d2];
+            gval[1] = (sc1[base + nip1 - 1 + jk] - sc1[base + nip1 - 2 + jk]) / diu[d2e];
+            gpos[0] = 0 * gstride + (j - 1) + (long)gm * (k - 1);
+            gpos[1] = 1 * gstride + (j - 1) + (long)gm * (k - 1);
+        }
+    } else if (seg == 1) {
+        int i = a, k = c;
+        long ik = i + ko * (k - 1);
+        sides[0] = 2; sides[1] = 3;
+        ghost[0] = ik; inner[0] = ik + jo; per[0] = ik + jo * (nj - 1);
+        ghost[1] = ik + jo * (njp1 - 1); inner[1] = ik + jo * (njp1 - 2); per[1] = ik + jo;
+        if (mode == 0) {
+            gval[0] = (sc1[base + ik + 2 * jo] - sc1[base + ik + jo]) / djv[IDX2(b, i, 3)];
+            gval[1] = (sc1[base + ik + jo * (njp1 - 2)] - sc1[base + ik + jo * (njp1 - 3)]) / djv[IDX2(b, i, nj)];
+            gpos[0] = 2 * gstride + (i - 1) + (long)gm * (k - 1);
+            gpos[1] = 3 * gstride + (i - 1) + (long)gm * (k - 1);
+        }
+    } else {
+        int i = a, j = c;
+        long ij = i + jo * (j - 1);
+        sides[0] = 4; sides[1] = 5;
+        ghost[0] = ij; inner[0] = ij + ko; per[0] = ij + ko * (nk - 1);
+        ghost[1] = ij + ko * (nkp1 - 1); inner[1] = ij + ko * (nkp1 - 2); per[1] = ij + ko;
+        if (mode == 0) {
+            double r = rp[IDX2(b, i, j)];
+            gval[0] = (sc1[base + ij + 2 * ko] - sc1[base + ij + ko]) / (r * dkp[b.off1k + 1]);
+            gval[1] = (sc1[base + ij + ko * (nkp1 - 2)] - sc1[base + ij + ko * (nkp1 - 3)]) /
+                      (r * dkp[b.off1k + nk - 2]);
+            gpos[0] = 4 * gstride + (i - 1) + (long)gm * (j - 1);
+            gpos[1] = 5 * gstride + (i - 1) + (long)gm * (j - 1);
+        }
+    }
+    (void)st;
+    for (int e = 0; e < 2; e++) {
+        int t = b.bc[sides[e]];
+        long gh = base + ghost[e], in = base + inner[e], pe = base + per[e];
+        if (mode == 0) {
+            G6[gpos[e]] = gval[e];
+            if (t == LES_BCT_PERIODIC_D) gam[gh] = gam[pe];
+            else if (t == LES_BCT_WALL_D) { gam[gh] = -gam[in]; gaml[gh] = -gaml[in]; }
+            else if (t != LES_BCT_INTERFACE_D) gam[gh] = gam[in];
+        } else {
+            if (t == LES_BCT_PERIODIC_D) f[gh] = f[pe];
+            else if (t != LES_BCT_INTERFACE_D && t != 4 /* FIXED */) f[gh] = f[in];
+        }
+    }
+}
+
+// one hyperplane i + j + k = s of set_sc1_block (see the header comment)
+__global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk, int s,
+                                                  Sc1Args A_, double dtime)
+{
+    const BlkDev b = blk[blockIdx.y];
+    int nj_ = b.n[1] - 2, nk_ = b.n[2] - 2;
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)nj_ * nk_) return;
+    int k = (int)(q / nj_) + 2;
+    int j = (int)(q - (long)(k - 2) * nj_) + 2;
+    int i = s - j - k;
+    int nip1 = b.n[0];
+    if (i < 2 || i > nip1 - 1) return;
+    const double lambda = 4.0, small = 1.e-30;
+    int ni = nip1 - 1, nj = b.n[1] - 1, nk = b.n[2] - 1;
+    long io = 1, jo = nip1, ko = (long)nip1 * b.n[1];
+    long ijk = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
+    double *sc1 = A_.sc1;
+    const double *rho = A_.rho, *gs = A_.gamsc1, *gl = A_.gamlam;
+    const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
+#define G(a, ii, jj) A_.m[a][IDX2(b, ii, jj)]
+    double rhowf = 0.5 * (rho[ijk] + rho[ijkw]);
+    double rhoef = 0.5 * (rho[ijk] + rho[ijke]);
+    double rhosf = 0.5 * (rho[ijk] + rho[ijks]);
+    double rhonf = 0.5 * (rho[ijk] + rho[ijkn]);
+    double rholf = 0.5 * (rho[ijk] + rho[ijkl]);
+    double rhorf = 0.5 * (rho[ijk] + rho[ijkr]);
+    double rhop = rho[ijk];
+    double gamwf = 0.5 * (gs[ijk] + gs[ijkw]) * rhowf + 0.5 * (gl[ijk] + gl[ijkw]);
+    double gamef = 0.5 * (gs[ijk] + gs[ijke]) * rhoef + 0.5 * (gl[ijk] + gl[ijke]);
+    double gamsf = 0.5 * (gs[ijk] + gs[ijks]) * rhosf + 0.5 * (gl[ijk] + gl[ijks]);
+    double gamnf = 0.5 * (gs[ijk] + gs[ijkn]) * rhonf + 0.5 * (gl[ijk] + gl[ijkn]);
+    double gamlf = 0.5 * (gs[ijk] + gs[ijkl]) * rholf + 0.5 * (gl[ijk] + gl[ijkl]);
+    double gamrf = 0.5 * (gs[ijk] + gs[ijkr]) * rhorf + 0.5 * (gl[ijk] + gl[ijkr]);
+    double uwf = A_.u[ijk], uef = A_.u[ijke], vsf = A_.v[ijk], vnf = A_.v[ijkn];
+    double wlf = A_.w[ijk], wrf = A_.w[ijkr];
+    double dfdxwf = (sc1[ijk] - sc1[ijkw]) / G(MW_DIU, i, j);
+    double dfdxef = (sc1[ijke] - sc1[ijk]) / G(MW_DIU, i + 1, j);
+    const long gst = A_.gstride;
+    const double *GR = A_.grad;
+    int gm = A_.gm;
+    double dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
+    if (i == 2) dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D) ? dfdxwf
+                          : GR[(long)(A_.link[blockIdx.y * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
+    else dfdxwwf = (sc1[ijkw] - sc1[ijkw - io]) / G(MW_DIU, i - 1, j);
+    if (i == ni) dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D) ? dfdxef
+                           : GR[(long)(A_.link[blockIdx.y * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
+    else dfdxeef = (sc1[ijke + io] - sc1[ijke]) / G(MW_DIU, i + 2, j);
+    double dfdysf = (sc1[ijk] - sc1[ijks]) / G(MW_DJV, i, j);
+    double dfdynf = (sc1[ijkn] - sc1[ijk]) / G(MW_DJV, i, j + 1);
+    if (j == 2) dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D) ? dfdysf
+                          : GR[(long)(A_.link[blockIdx.y * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
+    else dfdyssf = (sc1[ijks] - sc1[ijks - jo]) / G(MW_DJV, i, j - 1);
+    if (j == nj) dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D) ? dfdynf
+                           : GR[(long)(A_.link[blockIdx.y * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
+    else dfdynnf = (sc1[ijkn + jo] - sc1[ijkn]) / G(MW_DJV, i, j + 2);
+    double rpij = G(MW_RP, i, j);
+    double dfdzlf = (sc1[ijk] - sc1[ijkl]) / (rpij * dkp[k - 2]);
+    double dfdzrf = (sc1[ijkr] - sc1[ijk]) / (rpij * dkp[k - 1]);
+    if (k == 2) dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D) ? dfdzlf
+                          : GR[(long)(A_.link[blockIdx.y * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
+    else dfdzllf = (sc1[ijkl] - sc1[ijkl - ko]) / (rpij * dkp[k - 3]);
+    if (k == nk) dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D) ? dfdzrf
+                           : GR[(long)(A_.link[blockIdx.y * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
+    else dfdzrrf = (sc1[ijkr + ko] - sc1[ijkr]) / (rpij * dkp[k]);
+    double rwst = (uwf >= 0.0) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
+    double rest = (uef > 0.0) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
+    double rsth = (vsf >= 0.0) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
+    double rnth = (vnf > 0.0) ? (dfdysf + small) / (dfdynf + small) : (dfdynnf + small) / (dfdynf + small);
+    double rlft = (wlf >= 0.0) ? (dfdzllf + small) / (dfdzlf + small) : (dfdzrf + small) / (dfdzlf + small);
+    double rrht = (wrf > 0.0) ? (dfdzlf + small) / (dfdzrf + small) : (dfdzrrf + small) / (dfdzrf + small);
+    double limw = fmax(0.0, fmin(lambda * rwst, 1.0));
+    double lime = fmax(0.0, fmin(lambda * rest, 1.0));
+    double lims = fmax(0.0, fmin(lambda * rsth, 1.0));
+    double limn = fmax(0.0, fmin(lambda * rnth, 1.0));
+    double liml = fmax(0.0, fmin(lambda * rlft, 1.0));
+    double limr = fmax(0.0, fmin(lambda * rrht, 1.0));
+    double s0 = sc1[ijk];
+    double fwf, fef, fsf, fnf, flf, frf;
+    if (uwf > 0.0) fwf = sc1[ijkw] + 0.5 * limw * (s0 - sc1[ijkw]);
+    else if (uwf < 0.0) fwf = s0 + 0.5 * limw * (sc1[ijkw] - s0);
+    else fwf = 0.5 * (s0 + sc1[ijkw]);
+    if (uef > 0.0) fef = s0 + 0.5 * lime * (sc1[ijke] - s0);
+    else if (uef < 0.0) fef = sc1[ijke] + 0.5 * lime * (s0 - sc1[ijke]);
+    else fef = 0.5 * (s0 + sc1[ijke]);
+    if (vsf > 0.0) fsf = sc1[ijks] + 0.5 * lims * (s0 - sc1[ijks]);
+    else if (vsf < 0.0) fsf = s0 + 0.5 * lims * (sc1[ijks] - s0);
+    else fsf = 0.5 * (s0 + sc1[ijks]);
+    if (vnf > 0.0) fnf = s0 + 0.5 * limn * (sc1[ijkn] - s0);
+    else if (vnf < 0.0) fnf = sc1[ijkn] + 0.5 * limn * (s0 - sc1[ijkn]);
+    else fnf = 0.5 * (s0 + sc1[ijkn]);
+    if (wlf > 0.0) flf = sc1[ijkl] + 0.5 * liml * (s0 - sc1[ijkl]);
+    else if (wlf < 0.0) flf = s0 + 0.5 * liml * (sc1[ijkl] - s0);
+    else flf = 0.5 * (s0 + sc1[ijkl]);
+    if (wrf > 0.0) frf = s0 + 0.5 * limr * (sc1[ijkr] - s0);
+    else if (wrf < 0.0) frf = sc1[ijkr] + 0.5 * limr * (s0 - sc1[ijkr]);
+    else frf = 0.5 * (s0 + sc1[ijkr]);
+    double areawf = G(MW_RDJU, i, j) * dkw[k - 1];
+    double areaef = G(MW_RDJU, i + 1, j) * dkw[k - 1];
+    double areasf = G(MW_RDIV, i, j) * dkw[k - 1];
+    double areanf = G(MW_RDIV, i, j + 1) * dkw[k - 1];
+    double areak = G(MW_DIDJP, i, j);
+    double vol = G(MW_RDIDJP, i, j) * dkw[k - 1];
+    double gwf = rhowf * uwf * fwf * areawf;
+    double gef = rhoef * uef * fef * areaef;
+    double gsf = rhosf * vsf * fsf * areasf;
+    double gnf = rhonf * vnf * fnf * areanf;
+    double glf = rholf * wlf * flf * areak;
+    double grf = rhorf * wrf * frf * areak;
+    double convf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
+    double twf = gamwf * areawf * dfdxwf;
+    double tef = gamef * areaef * dfdxef;
+    double tsf = gamsf * areasf * dfdysf;
+    double tnf = gamnf * areanf * dfdynf;
+    double tlf = gamlf * areak * dfdzlf;
+    double trf = gamrf * areak * dfdzrf;
+    double difff = (tef - twf) + (tnf - tsf) + (trf - tlf);
+    double h = convf + difff;
+    double tmp = s0 + dtime / (vol * rhop) * (1.5 * h - 0.5 * A_.hsc1[ijk]);
+    A_.hsc1[ijk] = h;
+    if (tmp < 0.0) tmp = 0.0;
+    if (tmp > 1.0) tmp = 1.0;
+    sc1[ijk] = tmp;
+#undef G
+}
+
+// code/set_sc1var_block.F:26-66
+__global__ void k_sc1var(const BlkDev *__restrict__ blk, const double *__restrict__ sc1,
+                         double *__restrict__ sc1var, const double *__restrict__ dip,
+                         const double *__restrict__ djp, const double *__restrict__ rp,
+                         const double *__restrict__ dkp, const double *__restrict__ dkw)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    long ijk = decode_interior(b, q, i, j, k);
+    long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const double cfv = 0.1;
+    long ij = IDX2(b, i, j);
+    double fwf = 0.5 * (sc1[ijk] + sc1[ijk - 1]);
+    double fef = 0.5 * (sc1[ijk] + sc1[ijk + 1]);
+    double fsf = 0.5 * (sc1[ijk] + sc1[ijk - jo]);
+    double fnf = 0.5 * (sc1[ijk] + sc1[ijk + jo]);
+    double flf = 0.5 * (sc1[ijk] + sc1[ijk - ko]);
+    double frf = 0.5 * (sc1[ijk] + sc1[ijk + ko]);
+    double dfdip = (fef - fwf) / dip[ij];
+    double dfdjp = (fnf - fsf) / djp[ij];
+    double dfdkp = (frf - flf) / (rp[ij] * dkw[b.off1k + k - 1]);
+    double dfdijk = dfdip * dfdip + dfdjp * dfdjp + dfdkp * dfdkp;
+    double dk = rp[ij] * dkp[b.off1k + k - 1];
+    double delta = pow(dip[ij] * djp[ij] * dk, .33333333);
+    sc1var[ijk] = cfv * dfdijk * (delta * delta);
+}
+
+namespace les {
+
+static inline unsigned nbk(long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+void launch_set_u_int(const BlkDev *blk, int nb, long maxcell, int iva, const UIntArgs &a,
+                      double dtime, int iststep, double visc, double ylaminar, double kappa,
+                      double cwfun, cudaStream_t st)
+{
+    k_set_u_int<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, iva, a, dtime, iststep, visc, ylaminar,
+                                                            kappa, cwfun);
+    count_launch(1);
+}
+
+void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a, double dtime,
+                      int iststep, double visc, double ylaminar, double kappa, double cwfun,
+                      cudaStream_t st)
+{
+    k_set_w_int<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, a, dtime, iststep, visc, ylaminar, kappa,
+                                                            cwfun);
+    count_launch(1);
+}
+
+void launch_fill(double *a, double val, long n, cudaStream_t st)
+{
+    unsigned g = nbk(n, 256);
+    k_fill<<<g > 4096 ? 4096 : g, 256, 0, st>>>(a, val, n);
+    count_launch(1);
+}
+
+void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f, double *gam,
+                    double *gaml, const double *sc1, const double *diu, const double *djv,
+                    const double *rp, const double *dkp, double *grad, long gstride, int gm,
+                    cudaStream_t st)
+{
+    k_face_bc<<<dim3(nbk(maxface, 128), 3, nb), 128, 0, st>>>(blk, mode, f, gam, gaml, sc1, diu, djv, rp, dkp,
+                                                             grad, gstride, gm);
+    count_launch(1);
+}
+
+void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax, const Sc1Args &a,
+                      double dtime, cudaStream_t st)
+{
+    unsigned gx = nbk(maxjk, 128);
+    for (int s = smin; s <= smax; s++) k_sc1_wave<<<dim3(gx, nb), 128, 0, st>>>(blk, s, a, dtime);
+    count_launch(smax - smin + 1);
+}
+
+void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,
+                   const double *dip, const double *djp, const double *rp, const double *dkp,
+                   const double *dkw, cudaStream_t st)
+{
+    k_sc1var<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, sc1, sc1var, dip, djp, rp, dkp, dkw);
+    count_launch(1);
+}
+
+} // namespace les

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include "k_common.cuh"
+#include "phys_args.h"
 
 namespace les {
 
@@ -86,5 +87,30 @@ void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E
                         double *partial, double *out2, cudaStream_t st);
 template <typename T>
 void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st);
+template <typename T>
+void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st);
+
+// k_phys.cu
+void launch_set_u_int(const BlkDev *blk, int nb, long maxcell, int iva, const UIntArgs &a,
+                      double dtime, int iststep, double visc, double ylaminar, double kappa,
+                      double cwfun, cudaStream_t st);
+void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a, double dtime,
+                      int iststep, double visc, double ylaminar, double kappa, double cwfun,
+                      cudaStream_t st);
+void launch_fill(double *a, double val, long n, cudaStream_t st);
+void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f, double *gam,
+                    double *gaml, const double *sc1, const double *diu, const double *djv,
+                    const double *rp, const double *dkp, double *grad, long gstride, int gm,
+                    cudaStream_t st);
+void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax, const Sc1Args &a,
+                      double dtime, cudaStream_t st);
+void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,
+                   const double *dip, const double *djp, const double *rp, const double *dkp,
+                   const double *dkw, cudaStream_t st);
+
+// k_virtbc.cu
+void launch_vbc_side(const BlkDev *blk, int nb, int iva, int side, unsigned long long wallmask,
+                     unsigned long long initmask, const VbcArgs &a, long maxpts, double visc,
+                     double kappa, double aplus, double ylam, double value, cudaStream_t st);
 
 } // namespace les

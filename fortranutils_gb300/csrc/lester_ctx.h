@@ -27,6 +27,18 @@ struct LevelGeom {
     long maxmetlen = 0;
 };
 
+// One defect-correction iteration of a fast solver (V-cycle, update, halo,
+// FP64 residual, read-back of two sums) captured as a CUDA graph.
+struct CycleGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void *f = nullptr, *b = nullptr;
+    int sweeps = 0, coarse = 0;
+    double omega = 0;
+    bool singular = false;
+    long launches = 0;              // kernels per replay
+    std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
+};
+
 // device buffers of the fast solvers, precision T
 template <typename T> struct FastSet {
     T *E = nullptr, *N = nullptr, *R = nullptr, *D = nullptr, *x = nullptr, *b = nullptr;
@@ -59,6 +71,7 @@ struct Ctx {
     const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long coef_gen_seen = -1;
     int coef_prec = -1;
+    bool singular = true;   // pure Neumann/periodic operator (constant null vector)
     long coef_gen = 0;
     // staging buffers for host arguments
     std::vector<void *> stage_buf;
@@ -69,8 +82,21 @@ struct Ctx {
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
     long prof_launches = 0;
+    double prof_ms_acc = 0;
+    // graphs of the fast solvers: [0] FP64, [1] mixed
+    CycleGraph cg[2];
+    cudaStream_t cap_stream = nullptr;
+    std::vector<cudaEvent_t> *cap_ev = nullptr;  // set while capturing
     // bytes copied between host and device by staged (host-array) calls
     long h2d_bytes = 0, d2h_bytes = 0;
+    // predictor / scalar tables (lester_phys_host.cu)
+    long *d_offki = nullptr, *d_offjk = nullptr;
+    int *d_link = nullptr;
+    double *d_grad = nullptr;
+    long gstride = 0, maxfacecell = 0, tot2_l1 = 0;
+    int gm = 0;
+    int iststep = 2;  // step.F:180 increments it once before the first step
+    int init_vdd[LES_MAXBL][6] = {};  // set_virt_bc's init_vdd (set by the u call)
     // last solve statistics
     double last_norms[4] = {0, 0, 0, 0};
     int last_cycles = 0;

@@ -380,7 +380,16 @@ static void free_ctx(Ctx *c)
                   c->E64,   c->N64,   c->R64,   c->P64};
     for (void *p : fp) cudaFree(p);
     for (void *p : c->stage_buf) cudaFree(p);
+    cudaFree(c->d_offki);
+    cudaFree(c->d_offjk);
+    cudaFree(c->d_link);
+    cudaFree(c->d_grad);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    for (CycleGraph &G : c->cg) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
+    }
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -568,9 +577,10 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
     int bad = 0;
     LES_CUDA(cudaMemcpyAsync(&bad, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     LES_CUDA(cudaStreamSynchronize(c.stream));
-    if (bad)
+    if (bad & 7)
         return set_err(LES_ERR_STRUCTURE,
                        "coefficients lack the aw(i)=ae(i-1) pairing of coeff_p (mask %d); use LES_PSOLVE_REFERENCE", bad);
+    c.singular = !(bad & 8);
     for (int q = 0; q < 7; q++) c.coef_key[q] = A.a[q];
     c.coef_gen_seen = c.coef_gen;
     c.coef_prec = prec;
@@ -591,16 +601,27 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
 {
     FastSet<T> &F = fset<T>(c);
     LevelGeom &L = c.lv[lev];
-    bool prof = c.prof && lev == 1;
+    // level-1 smoother launches are bracketed by events: recorded into the
+    // graph while capturing, or on the stream when timing eagerly
+    bool cap = c.cap_ev && lev == 1;
+    bool prof = !c.cap_ev && c.prof && lev == 1;
     for (int s = 0; s < nsweep; s++)
         for (int color = 0; color < 2; color++) {
-            if (prof) cudaEventRecord(prof_event(c), c.stream);
-            launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
-                         F.b, c.stream);
-            if (prof) {
-                cudaEventRecord(prof_event(c), c.stream);
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (cap) {
+                cudaEventCreate(&e0);
+                cudaEventCreate(&e1);
+                c.cap_ev->push_back(e0);
+                c.cap_ev->push_back(e1);
+            } else if (prof) {
+                e0 = prof_event(c);
+                e1 = prof_event(c);
                 c.prof_launches++;
             }
+            if (e0) cudaEventRecord(e0, c.stream);
+            launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
+                         F.b, c.stream);
+            if (e1) cudaEventRecord(e1, c.stream);
             launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
 }
@@ -621,6 +642,7 @@ template <typename T> static void fast_vcycle(Ctx &c)
         launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxcell, F.E, F.N, F.R, F.D, F.x,
                                  F.b, F.b, c.stream);
     }
+    if (c.singular) launch_coarse_mean<T>(c.lv[L].d_blk, c.g.numbl, F.b, c.stream);
     fast_smooth<T>(c, L, L == 1 ? pre : crs);
     for (int lev = L - 1; lev >= 1; lev--) {
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
@@ -630,41 +652,124 @@ template <typename T> static void fast_vcycle(Ctx &c)
     }
 }
 
+static void drop_graph(CycleGraph &G)
+{
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+    for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
+    G.ev.clear();
+}
+
+// Capture one defect-correction iteration -- V-cycle, p += e, halo of p,
+// FP64 residual and the read-back of its two sums -- as a CUDA graph, so
+// the ~10^2 small launches of the coarse levels cost one graph launch.
+// Re-captured when the arrays or the smoother settings change.
+template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b)
+{
+    const lester_ctrl &k = c.c;
+    if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
+        G.omega == k.rb_omega && G.singular == c.singular)
+        return 0;
+    drop_graph(G);
+    if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    FastSet<T> &F = fset<T>(c);
+    LevelGeom &L1 = c.lv[1];
+    int nb = c.g.numbl;
+    cudaStream_t saved = c.stream;
+    c.stream = c.cap_stream;
+    c.cap_ev = &G.ev;
+    long l0 = g_launches.load();
+    cudaGraph_t graph = nullptr;
+    cudaError_t pre = cudaGetLastError();
+    cudaError_t e = cudaStreamBeginCapture(c.cap_stream, cudaStreamCaptureModeThreadLocal);
+    cudaError_t mid = cudaSuccess;
+    if (e == cudaSuccess) {
+        fast_vcycle<T>(c);
+        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, c.stream);
+        launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b,
+                              c.d_partial, c.d_small, c.stream);
+        cudaMemcpyAsync(c.h_small, c.d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
+        mid = cudaGetLastError();
+        e = cudaStreamEndCapture(c.cap_stream, &graph);
+    }
+    c.stream = saved;
+    c.cap_ev = nullptr;
+    G.launches = g_launches.load() - l0;
+    g_launches -= G.launches;  // captured, not launched
+    if (pre != cudaSuccess) return set_err(LES_ERR_CUDA, "before graph capture: %s", cudaGetErrorString(pre));
+    if (mid != cudaSuccess) return set_err(LES_ERR_CUDA, "during graph capture: %s", cudaGetErrorString(mid));
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    G.f = f;
+    G.b = b;
+    G.sweeps = k.rb_sweeps;
+    G.coarse = k.rb_coarse;
+    G.omega = k.rb_omega;
+    G.singular = c.singular;
+    return 0;
+}
+
 // defect correction: p <- p + V(b - A p) until ||b - A p|| <= rtol ||b||
 template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, double *b, double *residu,
                                             int prec)
 {
+#define STAGE_CHECK(what)                                                                          \
+    do {                                                                                           \
+        cudaError_t se_ = cudaGetLastError();                                                      \
+        if (se_ != cudaSuccess) return set_err(LES_ERR_CUDA, "fast solve (%s): %s", what, cudaGetErrorString(se_)); \
+    } while (0)
+    STAGE_CHECK("entry");
     int r = prepare_coef<T>(c, A, prec);
     if (r) return r;
+    STAGE_CHECK("coefficients");
     FastSet<T> &F = fset<T>(c);
     LevelGeom &L1 = c.lv[1];
     int nb = c.g.numbl;
     double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
     int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
     launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+    STAGE_CHECK("initial halo");
     launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b, c.d_partial,
                           c.d_small, c.stream);
+    STAGE_CHECK("initial residual");
     if ((r = sync_small(c, 2))) return r;
     double r2 = c.h_small[0], b2 = c.h_small[1];
     int it = 0;
     double rel = b2 > 0 ? std::sqrt(r2 / b2) : 0.;
+    CycleGraph &G = c.cg[sizeof(T) == 4 ? 1 : 0];
+    if (b2 > 0 && rel > rtol && (r = ensure_cycle_graph<T>(c, G, f, b))) return r;
+    STAGE_CHECK("graph");
     while (b2 > 0 && rel > rtol && it < maxit) {
-        fast_vcycle<T>(c);
-        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, c.stream);
-        launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b,
-                              c.d_partial, c.d_small, c.stream);
-        if ((r = sync_small(c, 2))) return r;
+        LES_CUDA(cudaGraphLaunch(G.exec, c.stream));
+        count_launch(G.launches);
+        LES_CUDA(cudaStreamSynchronize(c.stream));
+        if (c.prof)
+            for (size_t q = 0; q + 1 < G.ev.size(); q += 2) {
+                float ms = 0;
+                LES_CUDA(cudaEventElapsedTime(&ms, G.ev[q], G.ev[q + 1]));
+                c.prof_ms_acc += ms;
+                c.prof_launches++;
+            }
         r2 = c.h_small[0];
         rel = std::sqrt(r2 / b2);
         it++;
         if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+    }
+    {
+        cudaError_t ee = cudaGetLastError();
+        if (ee != cudaSuccess) return set_err(LES_ERR_CUDA, "fast solve, %d cycles: %s", it, cudaGetErrorString(ee));
     }
     c.last_cycles = it;
     c.last_relres = rel;
     // reference-style norms and level-1 residual for the caller
     double n4[4];
     if ((r = norms_level(c, 1, A, f, b, residu, n4))) return r;
+    STAGE_CHECK("final norms");
+#undef STAGE_CHECK
     for (int q = 0; q < 4; q++) c.last_norms[q] = n4[q];
     if (rel > rtol && b2 > 0)
         return set_err(LES_ERR_NOT_CONVERGED, "relative residual %.3e after %d cycles", rel, it);
@@ -798,6 +903,7 @@ int lester_gpu_prof(int enable)
     if (enable) {
         g_ctx->ev_used = 0;
         g_ctx->prof_launches = 0;
+        g_ctx->prof_ms_acc = 0;
     }
     return 0;
 }
@@ -807,7 +913,7 @@ int lester_gpu_prof_read(double *ms_total, long *launches)
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
     LES_CUDA(cudaStreamSynchronize(c.stream));
-    double tot = 0;
+    double tot = c.prof_ms_acc;  // graph replays, summed after each replay
     for (size_t q = 0; q + 1 < c.ev_used; q += 2) {
         float ms = 0;
         LES_CUDA(cudaEventElapsedTime(&ms, c.ev_pool[q], c.ev_pool[q + 1]));

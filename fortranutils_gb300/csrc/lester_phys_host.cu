@@ -1,0 +1,354 @@
+// lester_phys_host.cu -- C ABI entry points of the momentum predictor and
+// the scalar transport (include/lester_gpu.h).
+#include <cstring>
+#include <vector>
+#include "kernels.h"
+#include "lester_ctx.h"
+
+namespace les {
+
+// per-block tables of the predictor / scalar kernels, built on first use
+static int ensure_phys_tables(Ctx &c)
+{
+    if (c.d_offki) return 0;
+    int nb = c.g.numbl;
+    std::vector<long> ki(nb), jk(nb);
+    std::vector<int> link(6 * nb);
+    long oki = 0, ojk = 0;
+    int gm = 0;
+    for (int b = 1; b <= nb; b++) {
+        int *n = c.lv[1].n[b];
+        ki[b - 1] = oki;
+        jk[b - 1] = ojk;
+        oki += (long)n[2] * n[0];
+        ojk += (long)n[1] * n[2];
+        for (int d = 0; d < 3; d++) gm = std::max(gm, n[d]);
+        for (int s = 0; s < 6; s++) link[6 * (b - 1) + s] = c.g.bl2bl[b - 1][s] - 1;
+    }
+    LES_CUDA(cudaMalloc(&c.d_offki, sizeof(long) * nb));
+    LES_CUDA(cudaMalloc(&c.d_offjk, sizeof(long) * nb));
+    LES_CUDA(cudaMalloc(&c.d_link, sizeof(int) * 6 * nb));
+    LES_CUDA(cudaMemcpy(c.d_offki, ki.data(), sizeof(long) * nb, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMemcpy(c.d_offjk, jk.data(), sizeof(long) * nb, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMemcpy(c.d_link, link.data(), sizeof(int) * 6 * nb, cudaMemcpyHostToDevice));
+    c.gm = gm;
+    c.gstride = (long)gm * gm;
+    LES_CUDA(cudaMalloc(&c.d_grad, sizeof(double) * 6 * c.gstride * nb));
+    LES_CUDA(cudaMemset(c.d_grad, 0, sizeof(double) * 6 * c.gstride * nb));
+    long mf = 0;
+    for (int b = 1; b <= nb; b++) {
+        int *n = c.lv[1].n[b];
+        long a = (long)(n[1] - 2) * (n[2] - 2), bq = (long)(n[0] - 2) * (n[2] - 2), cq = (long)(n[0] - 2) * (n[1] - 2);
+        mf = std::max(mf, std::max(a, std::max(bq, cq)));
+    }
+    c.maxfacecell = mf;
+    long l1 = 0;
+    for (int b = 1; b <= nb; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
+    c.tot2_l1 = l1;
+    return 0;
+}
+
+static int wave_range(Ctx &c, int &smin, int &smax)
+{
+    smin = 6;
+    smax = 0;
+    for (int b = 1; b <= c.g.numbl; b++) smax = std::max(smax, c.lv[1].n[b][0] + c.lv[1].n[b][1] + c.lv[1].n[b][2] - 3);
+    return 0;
+}
+
+} // namespace les
+
+using namespace les;
+
+extern "C" {
+
+int lester_gpu_set_iststep(int iststep)
+{
+    LES_NEED_CTX();
+    if (iststep < 1) return set_err(LES_ERR_ARG, "iststep must be >= 1");
+    g_ctx->iststep = iststep;
+    return 0;
+}
+
+// code/set_uv_int.F:5-164
+int lester_set_uv_int(const int *iva, const double *u, const double *v, const double *w, const double *p,
+                      const double *rho, const double *rhonp1, const double *gam, double *u_int, double *hu,
+                      const double *dip, const double *diu, const double *dix, const double *rdix,
+                      const double *djp, const double *dju, const double *djv, const double *djx,
+                      const double *rdjp, const double *rdju, const double *didjp, const double *didju,
+                      const double *rdidju, const double *hijp, const double *hiju, const double *hjiu,
+                      const double *hkiu, const double *hkju, const double *rp, const double *ru,
+                      const double *dkp, const double *dkw, double *tw_sfi, double *tw_nfi, double *tw_lfi,
+                      double *tw_rfi, double *work, int *offwork)
+{
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    int iv = *iva;
+    if (iv != 1 && iv != 2) return set_err(LES_ERR_ARG, "set_uv_int: iva %d", iv);
+    Staging st(&c);
+    UIntArgs A;
+    memset(&A, 0, sizeof A);
+    const double *mu[20] = {dip, diu, dix, rdix, djp, dju, djv, djx, rdjp, rdju,
+                            didjp, didju, rdidju, hijp, hiju, hjiu, hkiu, hkju, rp, ru};
+    const double **md[20] = {&A.dip, &A.diu, &A.dix, &A.rdix, &A.djp, &A.dju, &A.djv, &A.djx, &A.rdjp,
+                             &A.rdju, &A.didjp, &A.didju, &A.rdidju, &A.hijp, &A.hiju, &A.hjiu, &A.hkiu,
+                             &A.hkju, &A.rp, &A.ru};
+    for (int q = 0; q < 20; q++)
+        if ((r = st.in(mu[q], c.tot2, md[q]))) return r;
+    if ((r = st.in(dkp, c.tot1k, &A.dkp)) || (r = st.in(dkw, c.tot1k, &A.dkw))) return r;
+    const double *fu[7] = {u, v, w, p, rho, rhonp1, gam};
+    const double **fd[7] = {&A.u, &A.v, &A.w, &A.p, &A.rho, &A.rhonp1, &A.gam};
+    for (int q = 0; q < 7; q++)
+        if ((r = st.in(fu[q], c.tot_sg3, fd[q]))) return r;
+    if ((r = st.io(u_int, c.tot_sg3, &A.u_int)) || (r = st.io(hu, c.tot_sg3, &A.hu))) return r;
+    long nsn = (iv == 1) ? c.totki : c.totjk;
+    if ((r = st.io(tw_sfi, nsn, &A.tw_s)) || (r = st.io(tw_nfi, nsn, &A.tw_n)) ||
+        (r = st.io(tw_lfi, c.tot2_l1, &A.tw_l)) || (r = st.io(tw_rfi, c.tot2_l1, &A.tw_r)))
+        return r;
+    A.off_ki = c.d_offki;
+    A.off_jk = c.d_offjk;
+    A.off2_lev1_base = 0;
+    const lester_ctrl &k = c.c;
+    LevelGeom &L = c.lv[1];
+    launch_set_u_int(L.d_blk, c.g.numbl, L.maxcell, iv, A, k.dtime, c.iststep, k.visc, k.ylaminar, k.kappa,
+                     k.cwfun, c.stream);
+    launch_halo(L.d_face, L.nface, L.maxface, A.u_int, c.d_work, c.stream);
+    return st.finish();
+}
+
+// code/set_w_int.F:5-141
+int lester_set_w_int(const double *u, const double *v, const double *w, const double *p, const double *rho,
+                     const double *rhonp1, const double *gam, double *w_int, double *hw, const double *dip,
+                     const double *diu, const double *rdiv, const double *djp, const double *djv,
+                     const double *rdju, const double *didjp, const double *rdidjp, const double *hkip,
+                     const double *hkjp, const double *hkiu, const double *hkjv, const double *rp,
+                     const double *ru, const double *dkp, const double *dkw, double *tw_sfk, double *tw_nfk,
+                     double *tw_wfk, double *tw_efk, double *work, int *offwork)
+{
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    Staging st(&c);
+    WIntArgs A;
+    memset(&A, 0, sizeof A);
+    const double *mu[MW_N] = {dip, diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, ru};
+    for (int q = 0; q < MW_N; q++)
+        if ((r = st.in(mu[q], c.tot2, &A.m[q]))) return r;
+    if ((r = st.in(dkp, c.tot1k, &A.dkp)) || (r = st.in(dkw, c.tot1k, &A.dkw))) return r;
+    const double *fu[7] = {u, v, w, p, rho, rhonp1, gam};
+    const double **fd[7] = {&A.u, &A.v, &A.w, &A.p, &A.rho, &A.rhonp1, &A.gam};
+    for (int q = 0; q < 7; q++)
+        if ((r = st.in(fu[q], c.tot_sg3, fd[q]))) return r;
+    if ((r = st.io(w_int, c.tot_sg3, &A.w_int)) || (r = st.io(hw, c.tot_sg3, &A.hw))) return r;
+    if ((r = st.io(tw_sfk, c.totki, &A.tw_sfk)) || (r = st.io(tw_nfk, c.totki, &A.tw_nfk)) ||
+        (r = st.io(tw_wfk, c.totjk, &A.tw_wfk)) || (r = st.io(tw_efk, c.totjk, &A.tw_efk)))
+        return r;
+    A.off_ki = c.d_offki;
+    A.off_jk = c.d_offjk;
+    const lester_ctrl &k = c.c;
+    LevelGeom &L = c.lv[1];
+    launch_set_w_int(L.d_blk, c.g.numbl, L.maxcell, A, k.dtime, c.iststep, k.visc, k.ylaminar, k.kappa, k.cwfun,
+                     c.stream);
+    launch_halo(L.d_face, L.nface, L.maxface, A.w_int, c.d_work, c.stream);
+    return st.finish();
+}
+
+// code/set_virt_bc.F:8 set_virt_bc(iva, ilev, f, fm, rho, gam, vd_damping,
+// init_vdd, value, tw_sfi ... tw_nfk, dip, diu, div, dix, djp, dju, djv,
+// djx, ru, rv, dkp, dkw) at ilev = 1 for the velocities.  init_vdd is kept
+// by the library (set for every side by the u call); the argument is
+// accepted and ignored.
+int lester_set_virt_bc(const int *iva, const int *ilev, double *f, const double *fm, const double *rho,
+                       const double *gam, double *vd_damping, int *init_vdd, const double *value,
+                       double *tw_sfi, double *tw_nfi, double *tw_lfi, double *tw_rfi, double *tw_wfj,
+                       double *tw_efj, double *tw_lfj, double *tw_rfj, double *tw_wfk, double *tw_efk,
+                       double *tw_sfk, double *tw_nfk, const double *dip, const double *diu,
+                       const double *div, const double *dix, const double *djp, const double *dju,
+                       const double *djv, const double *djx, const double *ru, const double *rv,
+                       const double *dkp, const double *dkw)
+{
+    (void)fm;
+    (void)gam;
+    (void)init_vdd;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    int iv = *iva;
+    if (iv < 1 || iv > 3 || *ilev != 1) return set_err(LES_ERR_ARG, "set_virt_bc: velocities at level 1 only");
+    Staging st(&c);
+    VbcArgs A;
+    memset(&A, 0, sizeof A);
+    if ((r = st.io(f, c.tot_sg3, &A.f)) || (r = st.in(rho, c.tot_sg3, &A.rho)) ||
+        (r = st.io(vd_damping, c.tot_sg3, &A.vdd)))
+        return r;
+    const double *mu[10] = {dju, djx, ru, rv, div, dix, dip, diu, djp, djv};
+    const double **md[10] = {&A.dju, &A.djx, &A.ru, &A.rv, &A.div_, &A.dix, &A.dip, &A.diu, &A.djp, &A.djv};
+    for (int q = 0; q < 10; q++)
+        if ((r = st.in(mu[q], c.tot2, md[q]))) return r;
+    if ((r = st.in(dkp, c.tot1k, &A.dkp)) || (r = st.in(dkw, c.tot1k, &A.dkw))) return r;
+    // the four wall arrays of this component and their layouts
+    double *tws[4];
+    long twn[4];
+    if (iv == 1) {
+        double *t[4] = {tw_sfi, tw_nfi, tw_lfi, tw_rfi};
+        long n[4] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1};
+        for (int q = 0; q < 4; q++) { tws[q] = t[q]; twn[q] = n[q]; }
+    } else if (iv == 2) {
+        double *t[4] = {tw_wfj, tw_efj, tw_lfj, tw_rfj};
+        long n[4] = {c.totjk, c.totjk, c.tot2_l1, c.tot2_l1};
+        for (int q = 0; q < 4; q++) { tws[q] = t[q]; twn[q] = n[q]; }
+    } else {
+        double *t[4] = {tw_wfk, tw_efk, tw_sfk, tw_nfk};
+        long n[4] = {c.totjk, c.totjk, c.totki, c.totki};
+        for (int q = 0; q < 4; q++) { tws[q] = t[q]; twn[q] = n[q]; }
+    }
+    double *twd[4] = {nullptr, nullptr, nullptr, nullptr};
+    A.off_ki = c.d_offki;
+    A.off_jk = c.d_offjk;
+    int nb = c.g.numbl;
+    if (iv == 1)
+        for (int b = 0; b < nb; b++)
+            for (int s = 0; s < 6; s++) c.init_vdd[b][s] = 1;
+    launch_fill(A.vdd, 1.0, c.tot_sg3, c.stream);
+    // sides this component treats (set_virt_bc.F:77-135): not its own axis
+    const int sides[3][4] = {{3, 4, 5, 6}, {1, 2, 5, 6}, {1, 2, 3, 4}};
+    for (int q = 0; q < 4; q++) {
+        int s = sides[iv - 1][q];
+        unsigned long long wall = 0, init = 0;
+        long maxpts = 0;
+        for (int b = 1; b <= nb; b++) {
+            if (c.g.bl_bc[b - 1][s - 1] != LES_BCT_WALL) continue;
+            wall |= 1ull << (b - 1);
+            if (c.init_vdd[b - 1][s - 1]) init |= 1ull << (b - 1);
+            c.init_vdd[b - 1][s - 1] = 0;
+            int *n = c.lv[1].n[b];
+            long pts;
+            if (iv == 1 && (s == 3 || s == 4)) pts = (long)n[0] * n[2] * (n[1] / 2 + 1);
+            else if (s <= 2) pts = (long)n[1] * n[2];
+            else if (s <= 4) pts = (long)n[0] * n[2];
+            else pts = (long)n[0] * n[1];
+            maxpts = std::max(maxpts, pts);
+        }
+        if (!wall) continue;
+        if (!twd[q] && (r = st.io(tws[q], twn[q], &twd[q]))) return r;
+        A.tw = twd[q];
+        launch_vbc_side(c.lv[1].d_blk, nb, iv, s, wall, init, A, maxpts, c.c.visc, c.c.kappa, c.c.aplus,
+                        c.c.ylaminar, value ? *value : 0.0, c.stream);
+    }
+    return st.finish();
+}
+
+// code/set_gamsc1_bc.F
+int lester_set_gamsc1_bc(const double *sc1, double *gamsc1, double *gamlam, const double *diu,
+                         const double *djv, const double *dkp, const double *rp)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    Staging st(&c);
+    const double *ds, *ddiu, *ddjv, *ddkp, *drp;
+    double *dg, *dl;
+    if ((r = st.in(sc1, c.tot_sg3, &ds)) || (r = st.io(gamsc1, c.tot_sg3, &dg)) ||
+        (r = st.io(gamlam, c.tot_sg3, &dl)) || (r = st.in(diu, c.tot2, &ddiu)) || (r = st.in(djv, c.tot2, &ddjv)) ||
+        (r = st.in(dkp, c.tot1k, &ddkp)) || (r = st.in(rp, c.tot2, &drp)))
+        return r;
+    launch_fill(dl, c.c.visc / 0.72, c.tot_sg3, c.stream);
+    LevelGeom &L = c.lv[1];
+    launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 0, nullptr, dg, dl, ds, ddiu, ddjv, drp, ddkp, c.d_grad,
+                   c.gstride, c.gm, c.stream);
+    return st.finish();
+}
+
+// code/set_sc1.F:5-95
+int lester_set_sc1(const double *u, const double *v, const double *w, const double *p, double *sc1,
+                   const double *rho, const double *gamsc1, const double *gamlam, double *hsc1,
+                   const double *dip, const double *diu, const double *rdiv, const double *djp,
+                   const double *djv, const double *rdju, const double *didjp, const double *rdidjp,
+                   const double *hkip, const double *hkjp, const double *hkiu, const double *hkjv,
+                   const double *rp, const double *dkp, const double *dkw, double *work, int *offwork)
+{
+    (void)p;
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    Staging st(&c);
+    Sc1Args A;
+    memset(&A, 0, sizeof A);
+    const double *mu[MW_N] = {dip, diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, nullptr};
+    for (int q = 0; q < MW_N; q++)
+        if ((r = st.in(mu[q], c.tot2, &A.m[q]))) return r;
+    if ((r = st.in(dkp, c.tot1k, &A.dkp)) || (r = st.in(dkw, c.tot1k, &A.dkw))) return r;
+    const double *fu[6] = {u, v, w, rho, gamsc1, gamlam};
+    const double **fd[6] = {&A.u, &A.v, &A.w, &A.rho, &A.gamsc1, &A.gamlam};
+    for (int q = 0; q < 6; q++)
+        if ((r = st.in(fu[q], c.tot_sg3, fd[q]))) return r;
+    if ((r = st.io(sc1, c.tot_sg3, &A.sc1)) || (r = st.io(hsc1, c.tot_sg3, &A.hsc1))) return r;
+    A.grad = c.d_grad;
+    A.gstride = c.gstride;
+    A.gm = c.gm;
+    A.link = c.d_link;
+    LevelGeom &L = c.lv[1];
+    int smin, smax;
+    wave_range(c, smin, smax);
+    launch_sc1_waves(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
+    launch_halo(L.d_face, L.nface, L.maxface, A.sc1, c.d_work, c.stream);
+    return st.finish();
+}
+
+// code/set_sc1_bc.F
+int lester_set_sc1_bc(double *sc1)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    int r;
+    if ((r = ensure_phys_tables(c))) return r;
+    Staging st(&c);
+    double *d;
+    if ((r = st.io(sc1, c.tot_sg3, &d))) return r;
+    LevelGeom &L = c.lv[1];
+    launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 1, d, nullptr, nullptr, nullptr, nullptr, nullptr,
+                   nullptr, nullptr, nullptr, 0, 0, c.stream);
+    return st.finish();
+}
+
+// code/set_sc1var.F (sc1var only; the block routine does not write sc1dis)
+int lester_set_sc1var(const double *u, const double *v, const double *w, const double *sc1, const double *rho,
+                      double *sc1var, double *sc1dis, const double *dip, const double *djp, const double *dkp,
+                      const double *dkw, const double *rp, double *work, int *offwork)
+{
+    (void)u;
+    (void)v;
+    (void)w;
+    (void)rho;
+    (void)sc1dis;
+    (void)work;
+    (void)offwork;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c);
+    const double *ds, *ddip, *ddjp, *ddkp, *ddkw, *drp;
+    double *dv;
+    int r;
+    if ((r = st.in(sc1, c.tot_sg3, &ds)) || (r = st.io(sc1var, c.tot_sg3, &dv)) || (r = st.in(dip, c.tot2, &ddip)) ||
+        (r = st.in(djp, c.tot2, &ddjp)) || (r = st.in(dkp, c.tot1k, &ddkp)) || (r = st.in(dkw, c.tot1k, &ddkw)) ||
+        (r = st.in(rp, c.tot2, &drp)))
+        return r;
+    LevelGeom &L = c.lv[1];
+    launch_sc1var(L.d_blk, c.g.numbl, L.maxcell, ds, dv, ddip, ddjp, drp, ddkp, ddkw, c.stream);
+    launch_halo(L.d_face, L.nface, L.maxface, dv, c.d_work, c.stream);
+    return st.finish();
+}
+
+} // extern "C"

@@ -1,0 +1,49 @@
+// phys_args.h -- argument bundles of the predictor and scalar kernels
+// (passed by value; every pointer is a device pointer).
+#pragma once
+
+// metrics used by set_w_int / set_sc1 (their Fortran argument lists)
+enum { MW_DIP, MW_DIU, MW_RDIV, MW_DJP, MW_DJV, MW_RDJU, MW_DIDJP, MW_RDIDJP, MW_HKIP, MW_HKJP,
+       MW_HKIU, MW_HKJV, MW_RP, MW_RU, MW_N };
+
+// set_u_int_block arguments in the roles set_uv_int gives them (for the v
+// component the caller passes the swapped arrays, as code/step.F:319-326)
+struct UIntArgs {
+    const double *dip, *diu, *dix, *rdix, *djp, *dju, *djv, *djx, *rdjp, *rdju;
+    const double *didjp, *didju, *rdidju, *hijp, *hiju, *hjiu, *hkiu, *hkju, *rp, *ru;
+    const double *dkp, *dkw;
+    const double *u, *v, *w, *p, *rho, *rhonp1, *gam;
+    double *u_int, *hu;
+    double *tw_s, *tw_n, *tw_l, *tw_r;
+    const long *off_ki, *off_jk;  // per-block offsets of the (k,i) and (j,k) wall arrays
+    long off2_lev1_base;          // 0: level-1 (i,j) arrays start with block 1
+};
+
+struct WIntArgs {
+    const double *m[MW_N];
+    const double *dkp, *dkw;
+    const double *u, *v, *w, *p, *rho, *rhonp1, *gam;
+    double *w_int, *hw;
+    double *tw_sfk, *tw_nfk, *tw_wfk, *tw_efk;
+    const long *off_ki, *off_jk;
+};
+
+struct Sc1Args {
+    const double *m[MW_N];
+    const double *dkp, *dkw;
+    const double *u, *v, *w, *rho, *gamsc1, *gamlam;
+    double *sc1, *hsc1;
+    const double *grad;  // interface gradients: per block 6 planes of gm*gm
+    long gstride;
+    int gm;
+    const int *link;     // bl2bl, 0-based block numbers, 6 per block (-1 none)
+};
+
+// set_virt_bc arguments: the field, the wall array of the side being
+// processed and the metrics the velocity branches read
+struct VbcArgs {
+    double *f, *vdd;
+    const double *rho, *tw;
+    const double *dju, *djx, *ru, *rv, *div_, *dix, *dip, *diu, *djp, *djv, *dkp, *dkw;
+    const long *off_ki, *off_jk;
+};

@@ -93,9 +93,9 @@ def default_ctrl(**kw) -> Ctrl:
     c.psolve = PSOLVE_REFERENCE
     c.rtol = 1e-8
     c.max_outer = 200
-    c.rb_sweeps = 1
+    c.rb_sweeps = 3
     c.rb_coarse = 20
-    c.rb_omega = 1.15
+    c.rb_omega = 1.5
     for k, v in kw.items():
         setattr(c, k, v)
     return c
@@ -147,8 +147,19 @@ def _d(v: float):
 
 
 # ------------------------------------------------------------- lifecycle
-def gpu_init(geom: Geom, ctrl: Ctrl) -> None:
+def gpu_init(geom: Geom, ctrl: Ctrl, stream: int | None = None) -> None:
+    """Initialise; the library then queues its work on ``stream`` (default:
+    torch's current stream, so torch ops and library calls stay ordered)."""
     _check(lib().lester_gpu_init(C.byref(geom), C.byref(ctrl)))
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                stream = torch.cuda.current_stream().cuda_stream
+        except ImportError:
+            pass
+    if stream is not None:
+        _check(lib().lester_gpu_set_stream(C.c_void_p(stream)))
 
 
 def gpu_set_ctrl(ctrl: Ctrl) -> None:
@@ -306,3 +317,56 @@ def gpu_xfer_bytes():
     a, b = C.c_long(), C.c_long()
     _check(lib().lester_gpu_xfer_bytes(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def gpu_set_iststep(iststep: int) -> None:
+    _check(lib().lester_gpu_set_iststep(int(iststep)))
+
+
+# roles of set_uv_int's metric arguments (code/set_uv_int.F:5-11) and the
+# arrays step.F passes for u and for v (code/step.F:307-326)
+UV_ROLES = ("dip diu dix rdix djp dju djv djx rdjp rdju didjp didju rdidju hijp hiju hjiu hkiu "
+            "hkju rp ru").split()
+UV_FOR = {
+    1: UV_ROLES,
+    2: ("djp djv djx rdjx dip div diu dix rdip rdiv didjp djdiv rdjdiv hjip hjiv hijv hkjv hkiv "
+        "rp rv").split(),
+}
+W_ROLES = "dip diu rdiv djp djv rdju didjp rdidjp hkip hkjp hkiu hkjv rp ru".split()
+
+
+def set_uv_int(iva, u, v, w, p, rho, rhonp1, gam, u_int, hu, metrics: dict, dkp, dkw, tw_s, tw_n,
+               tw_l, tw_r):
+    """code/set_uv_int.F; for iva = 2 pass the v field as ``u`` and u as
+    ``v`` (step.F does), metrics is the comp_metric dict."""
+    mets = [_p(metrics[n]) for n in UV_FOR[iva]]
+    _check(lib().lester_set_uv_int(_i(iva), *map(_p, (u, v, w, p, rho, rhonp1, gam, u_int, hu)),
+                                   *mets, _p(dkp), _p(dkw), *map(_p, (tw_s, tw_n, tw_l, tw_r)),
+                                   None, None))
+
+
+def set_w_int(u, v, w, p, rho, rhonp1, gam, w_int, hw, metrics: dict, dkp, dkw, tw_sfk, tw_nfk,
+              tw_wfk, tw_efk):
+    mets = [_p(metrics[n]) for n in W_ROLES]
+    _check(lib().lester_set_w_int(*map(_p, (u, v, w, p, rho, rhonp1, gam, w_int, hw)), *mets,
+                                  _p(dkp), _p(dkw), *map(_p, (tw_sfk, tw_nfk, tw_wfk, tw_efk)),
+                                  None, None))
+
+
+def set_gamsc1_bc(sc1, gamsc1, gamlam, diu, djv, dkp, rp):
+    _check(lib().lester_set_gamsc1_bc(*map(_p, (sc1, gamsc1, gamlam, diu, djv, dkp, rp))))
+
+
+def set_sc1(u, v, w, p, sc1, rho, gamsc1, gamlam, hsc1, metrics: dict, dkp, dkw):
+    m = [_p(metrics[n]) for n in W_ROLES[:13]]
+    _check(lib().lester_set_sc1(*map(_p, (u, v, w, p, sc1, rho, gamsc1, gamlam, hsc1)), *m,
+                                _p(dkp), _p(dkw), None, None))
+
+
+def set_sc1_bc(f):
+    _check(lib().lester_set_sc1_bc(_p(f)))
+
+
+def set_sc1var(u, v, w, sc1, rho, sc1var, sc1dis, dip, djp, dkp, dkw, rp):
+    _check(lib().lester_set_sc1var(*map(_p, (u, v, w, sc1, rho, sc1var, sc1dis, dip, djp, dkp, dkw,
+                                             rp)), None, None))

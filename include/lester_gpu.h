@@ -250,6 +250,88 @@ int lester_slipbc(const double *x, const double *y, const double *z,
                   const double *v_int, double *w, double *sc1, double *rho,
                   const double *p, const int *step);
 
+/* ---- momentum predictor ----------------------------------------------- */
+/* the step counter iststep of code/step.F:180 (wall-stress running means) */
+int lester_gpu_set_iststep(int iststep);
+/* code/set_uv_int.F:5 set_uv_int(iva, u, v, w, p, rho, rhonp1, gam, u_int,
+ * hu, dip, diu, dix, rdix, djp, dju, djv, djx, rdjp, rdju, didjp, didju,
+ * rdidju, hijp, hiju, hjiu, hkiu, hkju, rp, ru, dkp, dkw, tw_sfi, tw_nfi,
+ * tw_lfi, tw_rfi, work, offwork).  For iva = 2 the caller passes the v
+ * arrays in the u roles, as code/step.F:319-326 does. */
+int lester_set_uv_int(const int *iva, const double *u, const double *v,
+                      const double *w, const double *p, const double *rho,
+                      const double *rhonp1, const double *gam, double *u_int,
+                      double *hu, const double *dip, const double *diu,
+                      const double *dix, const double *rdix, const double *djp,
+                      const double *dju, const double *djv, const double *djx,
+                      const double *rdjp, const double *rdju,
+                      const double *didjp, const double *didju,
+                      const double *rdidju, const double *hijp,
+                      const double *hiju, const double *hjiu,
+                      const double *hkiu, const double *hkju, const double *rp,
+                      const double *ru, const double *dkp, const double *dkw,
+                      double *tw_sfi, double *tw_nfi, double *tw_lfi,
+                      double *tw_rfi, double *work, int *offwork);
+/* code/set_w_int.F:5 set_w_int(u, v, w, p, rho, rhonp1, gam, w_int, hw, dip,
+ * diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, ru,
+ * dkp, dkw, tw_sfk, tw_nfk, tw_wfk, tw_efk, work, offwork) */
+int lester_set_w_int(const double *u, const double *v, const double *w,
+                     const double *p, const double *rho, const double *rhonp1,
+                     const double *gam, double *w_int, double *hw,
+                     const double *dip, const double *diu, const double *rdiv,
+                     const double *djp, const double *djv, const double *rdju,
+                     const double *didjp, const double *rdidjp,
+                     const double *hkip, const double *hkjp, const double *hkiu,
+                     const double *hkjv, const double *rp, const double *ru,
+                     const double *dkp, const double *dkw, double *tw_sfk,
+                     double *tw_nfk, double *tw_wfk, double *tw_efk,
+                     double *work, int *offwork);
+
+/* code/set_virt_bc.F:8 set_virt_bc(iva, ilev, f, fm, rho, gam, vd_damping,
+ * init_vdd, value, tw_sfi, tw_nfi, tw_lfi, tw_rfi, tw_wfj, tw_efj, tw_lfj,
+ * tw_rfj, tw_wfk, tw_efk, tw_sfk, tw_nfk, dip, diu, div, dix, djp, dju, djv,
+ * djx, ru, rv, dkp, dkw) for the velocities at ilev = 1: log-law / no-slip
+ * ghost values on wall sides and the van Driest damping field.  init_vdd is
+ * kept by the library. */
+int lester_set_virt_bc(const int *iva, const int *ilev, double *f,
+                       const double *fm, const double *rho, const double *gam,
+                       double *vd_damping, int *init_vdd, const double *value,
+                       double *tw_sfi, double *tw_nfi, double *tw_lfi,
+                       double *tw_rfi, double *tw_wfj, double *tw_efj,
+                       double *tw_lfj, double *tw_rfj, double *tw_wfk,
+                       double *tw_efk, double *tw_sfk, double *tw_nfk,
+                       const double *dip, const double *diu, const double *div,
+                       const double *dix, const double *djp, const double *dju,
+                       const double *djv, const double *djx, const double *ru,
+                       const double *rv, const double *dkp, const double *dkw);
+
+/* ---- scalar transport ------------------------------------------------- */
+/* code/set_gamsc1_bc.F set_gamsc1_bc(sc1, gamsc1, gamlam, diu, djv, dkp, rp) */
+int lester_set_gamsc1_bc(const double *sc1, double *gamsc1, double *gamlam,
+                         const double *diu, const double *djv,
+                         const double *dkp, const double *rp);
+/* code/set_sc1.F:5 set_sc1(u, v, w, p, sc1, rho, gamsc1, gamlam, hsc1, dip,
+ * diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, dkp,
+ * dkw, work, offwork) */
+int lester_set_sc1(const double *u, const double *v, const double *w,
+                   const double *p, double *sc1, const double *rho,
+                   const double *gamsc1, const double *gamlam, double *hsc1,
+                   const double *dip, const double *diu, const double *rdiv,
+                   const double *djp, const double *djv, const double *rdju,
+                   const double *didjp, const double *rdidjp,
+                   const double *hkip, const double *hkjp, const double *hkiu,
+                   const double *hkjv, const double *rp, const double *dkp,
+                   const double *dkw, double *work, int *offwork);
+/* code/set_sc1_bc.F set_sc1_bc(sc1) */
+int lester_set_sc1_bc(double *sc1);
+/* code/set_sc1var.F set_sc1var(u, v, w, sc1, rho, sc1var, sc1dis, dip, djp,
+ * dkp, dkw, rp, work, offwork) */
+int lester_set_sc1var(const double *u, const double *v, const double *w,
+                      const double *sc1, const double *rho, double *sc1var,
+                      double *sc1dis, const double *dip, const double *djp,
+                      const double *dkp, const double *dkw, const double *rp,
+                      double *work, int *offwork);
+
 /* ---- eddy viscosity --------------------------------------------------- */
 /* code/subgrid.F:5 subgrid(gam, gamsc1, u, v, w, sc1, rho, sc1var, sc1dis,
  * vd_damping, dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp,

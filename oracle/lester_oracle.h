@@ -134,6 +134,39 @@ void orc_slipbc(orc_ctx *c, double dtime, const double *djp, double *u,
                 double *v, const double *v_int, double *w, double *sc1,
                 double *rho, const double *p);
 
+/* ---- momentum predictor ------------------------------------------------ */
+/* iva = 1: u.  iva = 2: v, called as step.F:319-326 does -- pass the v field
+ * as `u` and the u field as `v`; tw_* are that component's wall arrays. */
+void orc_set_uv_int(orc_ctx *c, int iva, double dtime, int iststep, double visc,
+                    double ylaminar, double kappa, double cwfun, const double *u,
+                    const double *v, const double *w, const double *p, const double *rho,
+                    const double *rhonp1, const double *gam, double *u_int, double *hu,
+                    const double *metric, const double *dkp, const double *dkw, double *tw_s,
+                    double *tw_n, double *tw_l, double *tw_r);
+void orc_set_w_int(orc_ctx *c, double dtime, int iststep, double visc, double ylaminar,
+                   double kappa, double cwfun, const double *u, const double *v,
+                   const double *w, const double *p, const double *rho, const double *rhonp1,
+                   const double *gam, double *w_int, double *hw, const double *metric,
+                   const double *dkp, const double *dkw, double *tw_sfk, double *tw_nfk,
+                   double *tw_wfk, double *tw_efk);
+
+/* ---- wall ghost velocities --------------------------------------------- */
+void orc_set_virt_bc(orc_ctx *c, int iva, double visc, double kappa, double aplus,
+                     double ylaminar, double *f, const double *rho, double *vdd,
+                     const double *metric, const double *dkp, const double *dkw,
+                     double *const *tw);
+
+/* ---- scalar transport -------------------------------------------------- */
+void orc_set_gamsc1_bc(orc_ctx *c, double visc, const double *sc1, double *gamsc1,
+                       double *gamlam, const double *metric, const double *dkp);
+void orc_set_sc1(orc_ctx *c, double dtime, const double *metric, const double *dkp,
+                 const double *dkw, const double *u, const double *v, const double *w,
+                 double *sc1, double *hsc1, const double *rho, const double *gamsc1,
+                 const double *gamlam);
+void orc_set_sc1_bc(orc_ctx *c, double *f);
+void orc_set_sc1var(orc_ctx *c, const double *sc1, double *sc1var, const double *metric,
+                    const double *dkp, const double *dkw);
+
 /* ---- eddy viscosity ---------------------------------------------------- */
 void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
                  double *gam, double *gamsc1, const double *u,

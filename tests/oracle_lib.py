@@ -171,3 +171,51 @@ def mgctrl(nummgits=5, numpre=1, numpost=1, numcits=20, meth_cycle=1, tolf=5e-13
     c.meth_cycle, c.meth_smooth, c.meth_csolve = meth_cycle, 1, 0
     c.tolf, c.relax_pmg, c.relax_pmgc = tolf, relax, relax
     return c
+
+
+def _flat_metric(m: dict) -> np.ndarray:
+    from fortranutils_gb300 import lester as L
+    return np.ascontiguousarray(np.stack([m[n] for n in L.METRIC_NAMES]))
+
+
+def _orc_predictor_methods():
+    D = C.c_double
+
+    def set_uv_int(self, iva, dtime, iststep, k, u, v, w, p, rho, rhonp1, gam, u_int, hu, m, dkp,
+                   dkw, tw):
+        flat = _flat_metric(m)  # kept alive across the call
+        lib().orc_set_uv_int(self.ctx, iva, D(dtime), iststep, D(k["visc"]), D(k["ylaminar"]),
+                             D(k["kappa"]), D(k["cwfun"]),
+                             *map(P, (u, v, w, p, rho, rhonp1, gam, u_int, hu, flat, dkp,
+                                      dkw, *tw)))
+
+    def set_w_int(self, dtime, iststep, k, u, v, w, p, rho, rhonp1, gam, w_int, hw, m, dkp, dkw,
+                  tw):
+        flat = _flat_metric(m)
+        lib().orc_set_w_int(self.ctx, D(dtime), iststep, D(k["visc"]), D(k["ylaminar"]),
+                            D(k["kappa"]), D(k["cwfun"]),
+                            *map(P, (u, v, w, p, rho, rhonp1, gam, w_int, hw, flat, dkp,
+                                     dkw, *tw)))
+
+    def set_gamsc1_bc(self, visc, sc1, gamsc1, gamlam, m, dkp):
+        flat = _flat_metric(m)
+        lib().orc_set_gamsc1_bc(self.ctx, D(visc), P(sc1), P(gamsc1), P(gamlam), P(flat), P(dkp))
+
+    def set_sc1(self, dtime, m, dkp, dkw, u, v, w, sc1, hsc1, rho, gamsc1, gamlam):
+        flat = _flat_metric(m)
+        lib().orc_set_sc1(self.ctx, D(dtime), P(flat), *map(P, (dkp, dkw, u, v, w, sc1,
+                                                                           hsc1, rho, gamsc1,
+                                                                           gamlam)))
+
+    def set_sc1_bc(self, f):
+        lib().orc_set_sc1_bc(self.ctx, P(f))
+
+    def set_sc1var(self, sc1, sc1var, m, dkp, dkw):
+        flat = _flat_metric(m)
+        lib().orc_set_sc1var(self.ctx, P(sc1), P(sc1var), P(flat), P(dkp), P(dkw))
+
+    for f in (set_uv_int, set_w_int, set_gamsc1_bc, set_sc1, set_sc1_bc, set_sc1var):
+        setattr(Oracle, f.__name__, f)
+
+
+_orc_predictor_methods()
