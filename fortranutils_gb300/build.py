@@ -34,6 +34,7 @@ UNITS = {
     "k_phys.cu": ["-fmad=false"],
     "lester_phys_host.cu": [],
     "k_virtbc.cu": ["-fmad=false"],
+    "lester_step.cu": [],
 }
 
 

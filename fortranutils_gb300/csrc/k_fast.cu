@@ -184,26 +184,30 @@ __global__ void k_halo_fast(const FaceDev *__restrict__ fc, T *__restrict__ x)
 // ---- outer FP64 residual (defect correction) -------------------------------
 // r = b - A p with the exact FP64 coefficients; writes r (as T) as the
 // right-hand side of the next correction cycle and partial sums of r^2 and
-// b^2 for the stop test.
+// b^2 for the stop test.  `shift` (nullable, device scalar) is subtracted
+// from b first: the interior mean of b for a singular operator.
 template <typename T>
 __global__ void __launch_bounds__(256) k_resid_outer(
     const BlkDev *__restrict__ blk, const double *__restrict__ E, const double *__restrict__ N,
     const double *__restrict__ R, const double *__restrict__ P, const double *__restrict__ x,
-    const double *__restrict__ bb, T *__restrict__ rT, double *__restrict__ partial)
+    const double *__restrict__ bb, const double *__restrict__ shift, T *__restrict__ rT,
+    double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double v[2] = {0., 0.};
+    const double s0 = shift ? *shift : 0.;
     if (q < b.ncell) {
         int i, j, k;
         long p = decode_interior(b, q, i, j, k);
         long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-        double r = bb[p] - P[p] * x[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] +
+        const double bp = bb[p] - s0;
+        double r = bp - P[p] * x[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] +
                    N[p - jo] * x[p - jo] + N[p] * x[p + jo] + R[p - ko] * x[p - ko] +
                    R[p] * x[p + ko];
         rT[p] = (T)r;
         v[0] = r * r;
-        v[1] = bb[p] * bb[p];
+        v[1] = bp * bp;
     }
     block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
 }
@@ -222,6 +226,36 @@ __global__ void k_sum2_final(const double *__restrict__ partial, long nparts, do
         out[0] = r[0];
         out[1] = r[1];
     }
+}
+
+// Interior mean of a level-1 FP64 field over all blocks.  For a singular
+// operator (no Dirichlet side anywhere) the constant vector spans the null
+// space of the symmetric coeff_p matrix, so b minus this mean is the part
+// of the right-hand side that any p can match; the fast solvers drive the
+// residual of that compatible part.
+__global__ void __launch_bounds__(256) k_interior_sum(const BlkDev *__restrict__ blk,
+                                                      const double *__restrict__ bb,
+                                                      double *__restrict__ partial)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    double v[1] = {0.};
+    if (q < b.ncell) {
+        int i, j, k;
+        v[0] = bb[decode_interior(b, q, i, j, k)];
+    }
+    block_reduce_store<1>(v, partial + blockIdx.y * (long)gridDim.x + blockIdx.x);
+}
+
+__global__ void k_mean_final(const double *__restrict__ partial, long nparts, double ncell,
+                             double *__restrict__ out)
+{
+    double v[1] = {0.};
+    for (long t = threadIdx.x; t < nparts; t += blockDim.x) v[0] += partial[t];
+    __shared__ double r[1];
+    block_reduce_store<1>(v, r);
+    __syncthreads();
+    if (threadIdx.x == 0) out[0] = r[0] / ncell;
 }
 
 // Coarsest level of a singular (pure Neumann / periodic) operator: remove
@@ -324,12 +358,21 @@ void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaS
 
 template <typename T>
 void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
-                        const double *R, const double *P, const double *x, const double *b, T *rT,
-                        double *partial, double *out2, cudaStream_t st)
+                        const double *R, const double *P, const double *x, const double *b,
+                        const double *shift, T *rT, double *partial, double *out2, cudaStream_t st)
 {
     unsigned gx = nb_(maxcell, 256);
-    k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, rT, partial);
+    k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, partial);
     k_sum2_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out2);
+    count_launch(2);
+}
+
+void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
+                          double *partial, double *out, cudaStream_t st)
+{
+    unsigned gx = nb_(maxcell, 256);
+    k_interior_sum<<<dim3(gx, nb), 256, 0, st>>>(blk, b, partial);
+    k_mean_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, ncell, out);
     count_launch(2);
 }
 
@@ -361,8 +404,8 @@ void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *
     template void launch_halo_fast<T>(const FaceDev *, int, long, T *, cudaStream_t);             \
     template void launch_resid_outer<T>(const BlkDev *, int, long, const double *,                \
                                         const double *, const double *, const double *,           \
-                                        const double *, const double *, T *, double *, double *,  \
-                                        cudaStream_t);                                            \
+                                        const double *, const double *, const double *, T *,      \
+                                        double *, double *, cudaStream_t);                        \
     template void launch_update<T>(const BlkDev *, int, long, double *, const T *, cudaStream_t); \
     template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);
 INST(float)

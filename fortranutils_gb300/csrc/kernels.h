@@ -83,8 +83,10 @@ template <typename T>
 void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
 template <typename T>
 void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
-                        const double *R, const double *P, const double *x, const double *b, T *rT,
-                        double *partial, double *out2, cudaStream_t st);
+                        const double *R, const double *P, const double *x, const double *b,
+                        const double *shift, T *rT, double *partial, double *out2, cudaStream_t st);
+void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
+                          double *partial, double *out, cudaStream_t st);
 template <typename T>
 void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st);
 template <typename T>

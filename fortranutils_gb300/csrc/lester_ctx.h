@@ -96,7 +96,8 @@ struct Ctx {
     long gstride = 0, maxfacecell = 0, tot2_l1 = 0;
     int gm = 0;
     int iststep = 2;  // step.F:180 increments it once before the first step
-    int init_vdd[LES_MAXBL][6] = {};  // set_virt_bc's init_vdd (set by the u call)
+    int init_vdd[LES_MAXBL][6] = {};
+    std::vector<double *> scratch;  // step fields the caller left NULL  // set_virt_bc's init_vdd (set by the u call)
     // last solve statistics
     double last_norms[4] = {0, 0, 0, 0};
     int last_cycles = 0;

@@ -389,6 +389,7 @@ static void free_ctx(Ctx *c)
         if (G.exec) cudaGraphExecDestroy(G.exec);
         for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
     }
+    for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -688,8 +689,9 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
         fast_vcycle<T>(c);
         launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, c.stream);
         launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b,
-                              c.d_partial, c.d_small, c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                              c.singular ? c.d_small + 8 : nullptr, F.b, c.d_partial, c.d_small,
+                              c.stream);
         cudaMemcpyAsync(c.h_small, c.d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
         mid = cudaGetLastError();
         e = cudaStreamEndCapture(c.cap_stream, &graph);
@@ -733,8 +735,17 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
     launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
     STAGE_CHECK("initial halo");
-    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b, F.b, c.d_partial,
-                          c.d_small, c.stream);
+    // singular operator: drive the residual of the compatible part of b
+    // (b minus its interior mean, kept in d_small[8]); the constant part
+    // of p is fixed afterwards by p_ref_subtract, as in the reference
+    if (c.singular) {
+        double ncell = 0;
+        for (int ib = 1; ib <= nb; ib++)
+            ncell += (double)(L1.n[ib][0] - 2) * (L1.n[ib][1] - 2) * (L1.n[ib][2] - 2);
+        launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, ncell, c.d_partial, c.d_small + 8, c.stream);
+    }
+    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                          c.singular ? c.d_small + 8 : nullptr, F.b, c.d_partial, c.d_small, c.stream);
     STAGE_CHECK("initial residual");
     if ((r = sync_small(c, 2))) return r;
     double r2 = c.h_small[0], b2 = c.h_small[1];

@@ -146,7 +146,6 @@ int lester_step(lester_fields *F, const int *istep)
     double *const *m = D.metric;
     double **tw = D.tw;
     const lester_ctrl &k = c.c;
-    c.iststep += 1;  // code/step.F:180
     const int one = 1, iU = 1, iV = 2, iW = 3;
     double zero = 0.0;
     // ---- ivar = u: boundary ghosts, eddy viscosity, scalar, u predictor
@@ -206,6 +205,7 @@ int lester_step(lester_fields *F, const int *istep)
     RET(lester_slipbc(nullptr, nullptr, nullptr, m[M_DIP], m[M_DIU], m[M_DJP], m[M_DJV], D.dkp, D.u, D.v, D.v_int,
                       D.w, D.sc1, D.rho, D.p, istep));
     RET(lester_swap_rhos(D.rho, D.rhonp1, D.rhonm1));
+    c.iststep += 1;  // code/step.F:181, ready for the next step
     r = st.finish();
     if (r) return r;
     return rs;

@@ -101,7 +101,9 @@ typedef struct lester_ctrl {
     double tolf, relax_pmg, relax_pmgc;
     /* GPU solver selection */
     int psolve;        /* LES_PSOLVE_* */
-    double rtol;       /* fast solvers stop at ||b-Ap||/||b|| <= rtol */
+    double rtol;       /* fast solvers stop at ||b-Ap||/||b|| <= rtol; with no
+                          Dirichlet side (singular matrix) b is taken minus its
+                          interior mean, the only part any p can match */
     int max_outer;     /* fast solvers: maximum V-cycles */
     int rb_sweeps;     /* fast solvers: red-black sweeps per smoothing step */
     int rb_coarse;     /* fast solvers: sweeps on the coarsest level */
@@ -120,6 +122,23 @@ typedef struct lester_sizes {
     long n2_ki;  /* one 2-D (k,i) wall array, level 1 */
     long n2_jk;  /* one 2-D (j,k) wall array, level 1 */
 } lester_sizes;
+
+/* Every field of one time step, as the reference keeps them in its arena
+ * (code/step.F arguments).  3-D fields are level-1 (sg layout, n3_sg)
+ * except p, s, res and the seven coefficients, which span every multigrid
+ * level (n3_mg).  metric[] holds the 35 comp_metric arrays in its argument
+ * order.  tw[] holds the wall-stress arrays tw_sfi, tw_nfi, tw_lfi, tw_rfi,
+ * tw_wfj, tw_efj, tw_lfj, tw_rfj, tw_wfk, tw_efk, tw_sfk, tw_nfk.  Scratch
+ * fields (u_int, v_int, w_int, drhonp1dt, srhot, srhoux) may be NULL. */
+typedef struct lester_fields {
+    double *u, *v, *w, *sc1, *rho, *rhonp1, *rhonm1, *u_int, *v_int, *w_int;
+    double *hn_u, *hn_v, *hn_w, *hn_sc1, *gam, *gamsc1, *gamlam, *sc1var, *sc1dis;
+    double *vd_damping, *temperature, *drhonp1dt, *srhot, *srhoux;
+    double *p, *s, *res, *ap, *aw, *ae, *as, *an, *al, *ar;
+    double *metric[35];
+    double *dkp, *dkw;
+    double *tw[12];
+} lester_fields;
 
 /* ---- lifecycle -------------------------------------------------------- */
 /* Replaces the setup half of step.F:114-120 (set_offset, set_interfaces,
@@ -150,6 +169,14 @@ int lester_gpu_prof(int enable);
 int lester_gpu_prof_read(double *ms_total, long *launches);
 /* bytes copied host->device and device->host by calls with host arrays */
 int lester_gpu_xfer_bytes(long *h2d, long *d2h);
+
+/* One time step: the ivar loop of code/step.F:214-454 (set_virt_bc x3,
+ * subgrid, scalar transport and density, momentum predictor, coeff_p at
+ * istep 1, sour_p, solvers, extrap_p, p_ref_subtract, uvw_adv x3, slipbc,
+ * swap_rhos).  Host arrays are copied in once and back once per call.
+ * Returns LES_ERR_NOT_CONVERGED (after completing the step) if a fast
+ * pressure solver stopped at max_outer above rtol. */
+int lester_step(lester_fields *fields, const int *istep);
 
 /* ---- halo exchange ---------------------------------------------------- */
 /* code/swap_sc0.F:6 swap_sc(ivar1, igrid, var, work, mg_or_sg) */
@@ -251,7 +278,10 @@ int lester_slipbc(const double *x, const double *y, const double *z,
                   const double *p, const int *step);
 
 /* ---- momentum predictor ----------------------------------------------- */
-/* the step counter iststep of code/step.F:180 (wall-stress running means) */
+/* the step counter iststep of code/step.F:167,181 (wall-stress running
+ * means): the value the next predictor call and the next lester_step use.
+ * It starts at 2, the value of a run's first step; lester_step advances it
+ * by one after each step. */
 int lester_gpu_set_iststep(int iststep);
 /* code/set_uv_int.F:5 set_uv_int(iva, u, v, w, p, rho, rhonp1, gam, u_int,
  * hu, dip, diu, dix, rdix, djp, dju, djv, djx, rdjp, rdju, didjp, didju,

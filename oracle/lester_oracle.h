@@ -167,6 +167,27 @@ void orc_set_sc1_bc(orc_ctx *c, double *f);
 void orc_set_sc1var(orc_ctx *c, const double *sc1, double *sc1var, const double *metric,
                     const double *dkp, const double *dkw);
 
+/* ---- one time step ------------------------------------------------------ */
+typedef struct {
+    double dtime, visc, csles, rholo, rhohi, alpha, ylaminar, kappa, cwfun, aplus;
+    int model, gotrad;
+} orc_phys;
+
+/* the step's fields; metric is the flat 35 x tot2 comp_metric table, tw[]
+ * are tw_sfi tw_nfi tw_lfi tw_rfi tw_wfj tw_efj tw_lfj tw_rfj tw_wfk tw_efk
+ * tw_sfk tw_nfk */
+typedef struct {
+    double *u, *v, *w, *sc1, *rho, *rhonp1, *rhonm1, *u_int, *v_int, *w_int;
+    double *hn_u, *hn_v, *hn_w, *hn_sc1, *gam, *gamsc1, *gamlam, *sc1var, *sc1dis;
+    double *vd_damping, *temperature, *drhonp1dt, *srhot, *srhoux;
+    double *p, *s, *res, *ap, *aw, *ae, *as, *an, *al, *ar;
+    double *metric, *dkp, *dkw;
+    double *tw[12];
+} orc_fields;
+
+void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, int iststep,
+              orc_fields *F);
+
 /* ---- eddy viscosity ---------------------------------------------------- */
 void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
                  double *gam, double *gamsc1, const double *u,

@@ -219,3 +219,47 @@ def _orc_predictor_methods():
 
 
 _orc_predictor_methods()
+
+
+class OrcPhys(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dtime visc csles rholo rhohi alpha ylaminar kappa "
+                                           "cwfun aplus").split()] + [("model", C.c_int),
+                                                                      ("gotrad", C.c_int)]
+
+
+class OrcFields(C.Structure):
+    _fields_ = ([(n, C.c_void_p) for n in (
+        "u v w sc1 rho rhonp1 rhonm1 u_int v_int w_int hn_u hn_v hn_w hn_sc1 gam gamsc1 gamlam "
+        "sc1var sc1dis vd_damping temperature drhonp1dt srhot srhoux p s res ap aw ae as an al "
+        "ar metric dkp dkw").split()] + [("tw", C.c_void_p * 12)])
+
+
+def phys_from_ctrl(ctrl, gotrad=0) -> OrcPhys:
+    k = OrcPhys()
+    for n in "dtime visc csles rholo rhohi alpha ylaminar kappa cwfun aplus model".split():
+        setattr(k, n, getattr(ctrl, n))
+    k.gotrad = gotrad
+    return k
+
+
+def mgctrl_from_ctrl(ctrl) -> MgCtrl:
+    return mgctrl(ctrl.nummgits, ctrl.numpre, ctrl.numpost, ctrl.numcits, ctrl.meth_cycle,
+                  ctrl.tolf, ctrl.relax_pmg)
+
+
+def _orc_step(self, mg: MgCtrl, k: OrcPhys, istep: int, iststep: int, state) -> None:
+    """orc_step on a numpy State (fortranutils_gb300.state)."""
+    from fortranutils_gb300 import state as S
+    flat = _flat_metric(state["metric"])
+    f = OrcFields()
+    for n in S.FIELDS3 + S.FIELDSM:
+        setattr(f, n, P(state[n]).value)
+    f.metric = P(flat).value
+    f.dkp = P(state["dkp"]).value
+    f.dkw = P(state["dkw"]).value
+    for q, n in enumerate(S.TW):
+        f.tw[q] = P(state[n]).value
+    lib().orc_step(self.ctx, C.byref(mg), C.byref(k), istep, iststep, C.byref(f))
+
+
+Oracle.step = _orc_step
