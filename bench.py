@@ -1,22 +1,26 @@
-"""Benchmark of the LES-step hot path on one GB300.
+"""Benchmark of the LES time step on one GB300.
 
 Workload: the variable-density temporal mixing layer, 256 x 192 x 128
-cells, tanh stretching in y (beta = 2), periodic x/z, slip walls in y, WALE
-eddy viscosity, density ratio 2 carried by the scalar, seeded Gaussian noise
-(sigma = 0.02).  Inputs are synthetic (numpy default_rng, seed 2); the
-working set (~4 GB of FP64 fields) is far larger than the 129 MB L2, so no
-L2 flush is needed between steps.
+cells (one block), tanh stretching in y (beta = 2), periodic x/z, slip
+walls in y, WALE eddy viscosity (Cw = 0.5), density ratio 2 carried by the
+scalar through the mixing law, seeded Gaussian noise (sigma = 0.02, seed 2).
+Inputs are synthetic (numpy default_rng); the working set (~2 GB of FP64
+fields) is far larger than the 129 MB L2, so no L2 flush is needed between
+steps.
 
-A step is the per-time-step hot path run through the library: eddy
-viscosity (subgrid), pressure source (sour_p), the Poisson solve
-(lmg_solve) to ||b - A p|| / ||b|| <= 1e-8 from a zero initial guess,
-extrap_p, p_ref_subtract, the projection (uvw_adv for u, v, w, each with its
-halo swap) and the slip faces (slipbc).  The step is timed twice, with the
-mixed-precision solver (headline ``value``) and with the plain FP64 solver.
+A step is one call of lester_step: the ivar loop of code/step.F (wall ghost
+velocities, eddy viscosity, scalar transport and density, momentum
+predictor, pressure source, the Poisson solve to ||b - A p|| / ||b|| <= 1e-8,
+extrap_p, p_ref_subtract, projection, slip faces, density rotation).  The
+step is timed twice, with the mixed-precision solver (headline ``value``)
+and with the plain FP64 solver; the line carries both and their ratio.
 
-Output: one JSON line (rank 0).  ``--impl reference`` times the CPU oracle
-(the C restatement of the reference Fortran, one thread: the reference runs
-one MPI rank per block and this workload is one block) on the same workload.
+``value`` has every field resident in HBM.  ``e2e`` is the same step with
+every field in pinned host memory, copied in and back by each call (the
+strict drop-in a Fortran host sees).  ``cpu_baseline`` and ``--impl
+reference`` time the oracle (the C restatement of the reference Fortran,
+one thread: the reference runs one MPI rank per block and this workload is
+one block) on the same workload with the reference's own solver settings.
 """
 from __future__ import annotations
 
@@ -37,6 +41,8 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mcell-steps/s & Poisson V-cycle ms: mixed-prec vs FP64 on GB300 at 1e-8 resid"
 SHAPE = (256, 192, 128)
 DOMAIN = (30.0, 30.0, 15.0)
+WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
+            "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
 
 
 # ----------------------------------------------------------------- helpers
@@ -101,107 +107,72 @@ def make_case():
     return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
 
 
-def initial_fields(case, seed=2):
-    """u = 0.5 tanh(2y/delta), scalar 0.5(1 + tanh(2y)), noise sigma = 0.02."""
-    rng = np.random.default_rng(seed)
-    b = case.blocks[0]
-    nip1, njp1, nkp1 = b.n
-    yv = b.y.copy()
-    yv[0] = 2 * yv[1] - yv[2]
-    yv[-1] = 2 * yv[-2] - yv[-3]
-    yc = 0.5 * (yv[:-1] + yv[1:])[:njp1]  # cell centres j = 1..njp1
-    shape = (nkp1, njp1, nip1)
-    u = 0.5 * np.tanh(2.0 * yc)[None, :, None] + 0.02 * rng.standard_normal(shape)
-    v = 0.02 * rng.standard_normal(shape)
-    w = 0.02 * rng.standard_normal(shape)
-    sc1 = np.broadcast_to(0.5 * (1.0 + np.tanh(2.0 * yc))[None, :, None], shape).copy()
-    rholo, rhohi = 1.0, 2.0
-    rho = 1.0 / (sc1 / rhohi + (1.0 - sc1) / rholo)
-    return {k: np.ascontiguousarray(a.ravel()) for k, a in
-            dict(u=u, v=v, w=w, sc1=sc1, rho=rho).items()}
+def make_ctrl(psolve):
+    from fortranutils_gb300 import lester as L
+    return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
+                          rtol=1e-8, max_outer=200)
+
+
+def host_state(case, ctrl):
+    """Initial fields (numpy); metrics left zero for the caller to fill."""
+    from fortranutils_gb300 import lester as L, state as S
+    c = case
+    s = S.new_state(c, {n: np.zeros(c.n2) for n in L.METRIC_NAMES}, np.zeros(c.n1k),
+                    np.zeros(c.n1k))
+    return S.init_mixing_layer(s, seed=2, sigma=0.02, rholo=ctrl.rholo, rhohi=ctrl.rhohi)
+
+
+def device_state(case, ctrl):
+    """Device-resident state: metrics by comp_metric, halos exchanged."""
+    import torch
+    from fortranutils_gb300 import lester as L
+    g = host_state(case, ctrl).to("torch")
+    x, y, z = (torch.from_numpy(a).cuda() for a in case.coordinates())
+    L.comp_metric(x, y, z, g["metric"], g["dkp"], g["dkw"])
+    for n in ("u", "v", "w", "sc1", "rho", "rhonp1", "rhonm1"):
+        L.swap_sc(0, 1, g[n], mg_or_sg=2)
+    L.gpu_sync()
+    return g
+
+
+def step_bytes(mode: str, cycles: float, sweeps: int) -> float:
+    """Algorithmic bytes per interior cell of one step: distinct 3-D arrays
+    read plus written once per kernel (8 B FP64, 4 B FP32), metric tables and
+    matrix-free coefficients free.  Per V-cycle, levels sum with 8/7:
+      FP64: sweeps 24, residual 24, restriction 9, prolongation 17;
+      mixed: FP32 sweeps 12, restriction 4.5, prolongation 8.5, plus the
+      FP64 outer residual 24 and update p += e (8 + 4).
+    Per step: predictor 128, WALE 64, sour_p 72, projection 64, p_ref 16,
+    scalar predictor 80, search_lib 32."""
+    nsw = 2 * sweeps  # pre + post smoothing sweeps per level
+    if mode == "fp64":
+        bv = 8.0 / 7.0 * (nsw * 24 + 24 + 9 + 17)
+    else:
+        bv = 8.0 / 7.0 * (nsw * 12 + 4.5 + 8.5) + 24 + 12
+    return 128 + 64 + 72 + 64 + 16 + 80 + 32 + cycles * bv
 
 
 # ------------------------------------------------------------ GPU arm
-class GpuStep:
-    """Device-resident state and the step sequence (step.F:356-450 order)."""
-
-    def __init__(self, case, dtime):
-        import torch
-        from fortranutils_gb300 import lester as L
-        self.L, self.torch, self.case, self.dt = L, torch, case, dtime
-        c = case
-        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
-        z3 = lambda n=c.n3_sg: torch.zeros(n, dtype=torch.float64, device="cuda")  # noqa: E731
-        x, y, zc = c.coordinates()
-        self.m = {k: z3(c.n2) for k in L.METRIC_NAMES}
-        self.dkp, self.dkw = z3(c.n1k), z3(c.n1k)
-        L.comp_metric(dev(x), dev(y), dev(zc), self.m, self.dkp, self.dkw)
-        self.a = [z3(c.n3_mg) for _ in range(7)]
-        m = self.m
-        L.coeff_p(m["diu"], m["djv"], m["rdiv"], m["rdju"], m["didjp"], m["rp"], self.dkp,
-                  self.dkw, *self.a)
-        f = initial_fields(case)
-        self.u0 = {k: dev(v) for k, v in f.items()}
-        self.u, self.v, self.w = (self.u0[k].clone() for k in "uvw")
-        self.sc1, self.rho = self.u0["sc1"].clone(), self.u0["rho"].clone()
-        # slip faces first (v = 0 on the walls), so the pressure source is
-        # compatible with the all-Neumann/periodic pressure problem
-        L.slipbc(None, None, None, None, None, self.m["djp"], None, None, self.u, self.v,
-                 z3(), self.w, self.sc1, self.rho, z3())
-        for fld in (self.u, self.v, self.w, self.sc1, self.rho):
-            L.swap_sc(0, 1, fld, mg_or_sg=2)
-        self.ui, self.vi, self.wi = self.u.clone(), self.v.clone(), self.w.clone()
-        self.rhonp1 = self.rho.clone()
-        self.gam, self.gamsc1, self.sc1var, self.sc1dis = (z3() for _ in range(4))
-        self.vdd = torch.ones(c.n3_sg, dtype=torch.float64, device="cuda")
-        self.p = z3(c.n3_mg)
-        self.s = z3(c.n3_mg)
-        self.res = z3(c.n3_mg)
-        self.drho, self.srhot, self.srhoux = z3(), z3(), z3()
-        L.gpu_sync()
-
-    def step(self):
-        L, m, c = self.L, self.m, self.case
-        L.subgrid(self.gam, self.gamsc1, self.u, self.v, self.w, self.sc1, self.rho, self.sc1var,
-                  self.sc1dis, self.vdd, m["dip"], m["diu"], m["djp"], m["djv"], self.dkp,
-                  self.dkw, m["hijp"], m["hjip"], m["hkip"], m["hkjp"], m["rp"])
-        sl = self.s[: c.n3_sg]
-        L.sour_p(m["diu"], m["djv"], m["rdiv"], m["rdju"], m["didjp"], self.dkp, m["rdidjp"],
-                 self.dkw, self.ui, self.vi, self.wi, self.rho, self.rhonp1, self.drho, sl,
-                 self.srhot, self.srhoux)
-        self.p.zero_()
-        L.lmg_solve(*self.a, self.p, self.s, self.res)
-        p1 = self.p[: c.n3_sg]
-        L.extrap_p(p1)
-        L.p_ref_subtract(p1)
-        L.uvw_adv(1, m["diu"], m["rp"], self.dkw, self.u, self.ui, self.rhonp1, p1)
-        L.uvw_adv(2, m["djv"], m["rp"], self.dkw, self.v, self.vi, self.rhonp1, p1)
-        L.uvw_adv(3, m["diu"], m["rp"], self.dkw, self.w, self.wi, self.rhonp1, p1)
-        L.slipbc(None, None, None, None, None, m["djp"], None, None, self.u, self.v, self.vi,
-                 self.w, self.sc1, self.rho, p1)
-
-
-def run_gpu(args, rank):
+def run_gpu(args):
     import torch
-    from fortranutils_gb300 import build, lester as L
+    from fortranutils_gb300 import build, lester as L, state as S
     build.build()
     torch.cuda.set_device(0)
     case = make_case()
-    ncell = case.cells()
-    dtime = 0.01
     res = {}
     modes = [("fp64", L.PSOLVE_FP64), ("mixed", L.PSOLVE_MIXED)]
     modes = [m for m in modes if args.mode in ("both", m[0])]
     for mode, ps in modes:
-        ctrl = L.default_ctrl(dtime=dtime, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=ps,
-                              rtol=1e-8, max_outer=200)
+        ctrl = make_ctrl(ps)
         L.gpu_init(case.geom(), ctrl)
-        st = GpuStep(case, dtime)
+        g = device_state(case, ctrl)
         stream = torch.cuda.current_stream()
+        istep = 0
         for _ in range(args.warmup):
-            st.step()
+            istep += 1
+            S.step(g, istep)
         L.gpu_sync()
-        cyc = []
+        cyc, solve_ms, rel = [], [], []
         launches0 = L.gpu_launch_count()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -210,127 +181,106 @@ def run_gpu(args, rank):
             torch.cuda.synchronize()
             e0.record(stream)
             for _ in range(args.steps):
-                st.step()
-                cyc.append(L.gpu_solve_stats()["cycles"])
+                istep += 1
+                rc = S.step(g, istep)
+                st = L.gpu_solve_stats()
+                cyc.append(st["cycles"])
+                rel.append(st["relres"])
+                solve_ms.append(L.gpu_solve_time())
+                if rc != 0:
+                    raise RuntimeError(f"{mode} solver did not reach 1e-8: {st}")
             e1.record(stream)
             torch.cuda.synchronize()
         L.gpu_prof(False)
         ms = e0.elapsed_time(e1)
         kms, kl = L.gpu_prof_read()
-        stats = L.gpu_solve_stats()
         res[mode] = {"ms_per_step": ms / args.steps, "cycles": float(np.mean(cyc)),
-                     "relres": stats["relres"], "launches": L.gpu_launch_count() - launches0,
-                     "rb_ms": kms, "rb_launches": kl, "clocks": clk.summary()}
-        # e2e: the same step through the C ABI with host (pinned) buffers
+                     "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
+                     "launches": L.gpu_launch_count() - launches0, "rb_ms": kms,
+                     "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl}
+        del g
         if mode == "mixed" and not args.no_e2e:
-            res[mode]["e2e"] = run_e2e(args, st, case)
-        del st
+            res[mode]["e2e"] = run_e2e(args, case, ctrl)
         L.gpu_finalize()
         torch.cuda.empty_cache()
-    return case, ncell, res
+    return case, res
 
 
-def run_e2e(args, st, case):
-    """Projection step with every field on the host: each call copies its
-    inputs in and its outputs back (strict drop-in mode)."""
+def run_e2e(args, case, ctrl):
+    """lester_step with every field in pinned host memory: each call copies
+    all its arrays in and back once (strict drop-in)."""
     import torch
-    L = st.L
-    pin = lambda t: t.detach().cpu().pin_memory().numpy()  # noqa: E731
-    h = {k: pin(getattr(st, k)) for k in ("u", "v", "w", "ui", "vi", "wi", "sc1", "rho", "rhonp1",
-                                          "gam", "gamsc1", "sc1var", "sc1dis", "vdd", "p", "s",
-                                          "res", "drho", "srhot", "srhoux")}
-    # device-resident grid data (metrics, coefficients) stay on the device:
-    # they are computed once per run, as coeff_p is at istep == 1
-    m, dkp, dkw, a = st.m, st.dkp, st.dkw, st.a
-    c = case
-    bytes_in = bytes_out = 0
-
-    def one():
-        nonlocal bytes_in, bytes_out
-        L.subgrid(h["gam"], h["gamsc1"], h["u"], h["v"], h["w"], h["sc1"], h["rho"], h["sc1var"],
-                  h["sc1dis"], h["vdd"], m["dip"], m["diu"], m["djp"], m["djv"], dkp, dkw,
-                  m["hijp"], m["hjip"], m["hkip"], m["hkjp"], m["rp"])
-        sl = h["s"][: c.n3_sg]
-        L.sour_p(m["diu"], m["djv"], m["rdiv"], m["rdju"], m["didjp"], dkp, m["rdidjp"], dkw,
-                 h["ui"], h["vi"], h["wi"], h["rho"], h["rhonp1"], h["drho"], sl, h["srhot"],
-                 h["srhoux"])
-        h["p"][:] = 0.0
-        L.lmg_solve(*a, h["p"], h["s"], h["res"])
-        p1 = h["p"][: c.n3_sg]
-        L.extrap_p(p1)
-        L.p_ref_subtract(p1)
-        L.uvw_adv(1, m["diu"], m["rp"], dkw, h["u"], h["ui"], h["rhonp1"], p1)
-        L.uvw_adv(2, m["djv"], m["rp"], dkw, h["v"], h["vi"], h["rhonp1"], p1)
-        L.uvw_adv(3, m["diu"], m["rp"], dkw, h["w"], h["wi"], h["rhonp1"], p1)
-        L.slipbc(None, None, None, None, None, m["djp"], None, None, h["u"], h["v"], h["vi"],
-                 h["w"], h["sc1"], h["rho"], p1)
-
-    one()
+    from fortranutils_gb300 import lester as L, state as S
+    g = device_state(case, ctrl)
+    h = g.to("pinned")
+    del g
+    torch.cuda.empty_cache()
+    S.step(h, 1)  # coeff_p at istep 1, as the first step of a run
     L.gpu_sync()
     k = max(1, min(args.steps, 3))
     b0 = L.gpu_xfer_bytes()
     t0 = time.perf_counter()
-    for _ in range(k):
-        one()
+    for it in range(k):
+        S.step(h, 2 + it)
     L.gpu_sync()
     dt = (time.perf_counter() - t0) / k
     b1 = L.gpu_xfer_bytes()
-    return {"s_per_step": dt, "h2d_bytes_per_step": (b1[0] - b0[0]) // k,
+    return {"s_per_step": dt, "steps": k, "h2d_bytes_per_step": (b1[0] - b0[0]) // k,
             "d2h_bytes_per_step": (b1[1] - b0[1]) // k}
 
 
 # ------------------------------------------------------------- CPU arm
-def run_cpu_sample(case, budget_s=25.0):
-    """The oracle on the same workload: one projection step with the
-    reference algorithm (lexicographic SOR V(1,1) cycles, all levels) to
-    ||b - A p|| / ||b|| <= 1e-8.  One thread."""
+def run_cpu_steps(case, nsteps: int, warmup: int = 0):
+    """The oracle on the same workload: orc_step with the reference's own
+    solver settings (nummgits 5 V(1,1) cycles of lexicographic SOR).  One
+    thread.  Returns seconds per timed step."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
     from fortranutils_gb300 import lester as L
+    ctrl = make_ctrl(L.PSOLVE_REFERENCE)
     orc = O.Oracle(case)
     x, y, z = case.coordinates()
     met, dkp, dkw = orc.comp_metric(x, y, z)
-    m = {n: np.ascontiguousarray(met[i]) for i, n in enumerate(L.METRIC_NAMES)}
-    a = [np.zeros(case.n3_mg) for _ in range(7)]
-    orc.coeff_p(m, dkp, dkw, a)
-    f = initial_fields(case)
-    c = case
-    gam, gs1, sv, sd = (np.zeros(c.n3_sg) for _ in range(4))
-    vdd = np.ones(c.n3_sg)
+    s = host_state(case, ctrl)
+    for i, n in enumerate(L.METRIC_NAMES):
+        s["metric"][n][:] = met[i]
+    s["dkp"][:] = dkp
+    s["dkw"][:] = dkw
+    for n in ("u", "v", "w", "sc1", "rho", "rhonp1", "rhonm1"):
+        orc.swap_sc(1, s[n], 2)
+    orc.coeff_p(s["metric"], dkp, dkw, [s[n] for n in "ap aw ae as an al ar".split()])
+    mg, k = O.mgctrl_from_ctrl(ctrl), O.phys_from_ctrl(ctrl)
+    istep = 1  # coefficients exist: every oracle step runs as istep > 1
+    for _ in range(warmup):
+        istep += 1
+        orc.step(mg, k, istep, istep, s)
     t0 = time.perf_counter()
-    orc.subgrid(2, 0.5, 0, gam, gs1, f["u"], f["v"], f["w"], f["sc1"], sv, sd, vdd, m, dkp, dkw)
-    s = np.zeros(c.n3_mg)
-    outs = [np.zeros(c.n3_sg) for _ in range(4)]
-    orc.sour_p(0.01, m, dkp, dkw, f["u"], f["v"], f["w"], f["rho"], f["rho"], outs)
-    s[: c.n3_sg] = outs[1]
-    p = np.zeros(c.n3_mg)
-    r = np.zeros(c.n3_mg)
-    cycles, rel = 0, 1.0
-    tcyc = []
-    while rel > 1e-8 and cycles < 400:
-        t1 = time.perf_counter()
-        out = orc.lmg_solve(O.mgctrl(nummgits=1, tolf=0.0), a, p, s, r)
-        tcyc.append(time.perf_counter() - t1)
-        rel = out[0] / out[1] if out[1] > 0 else 0.0
-        cycles += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    converged = rel <= 1e-8
-    p1 = p[: c.n3_sg].copy()
-    orc.extrap_p(p1)
-    orc.p_ref_subtract(p1)
-    for iv, dg in ((1, m["diu"]), (2, m["djv"]), (3, m["diu"])):
-        uu = f["uvw"[iv - 1]].copy()
-        orc.uvw_adv(iv, 0.01, dg, m["rp"], dkw, uu, f["uvw"[iv - 1]], f["rho"], p1)
-    elapsed = time.perf_counter() - t0
-    if not converged:
-        # extrapolate the remaining cycles at the measured per-cycle cost
-        import math
-        fac = (rel ** (1.0 / max(cycles, 1)))
-        more = math.ceil(math.log(1e-8 / rel) / math.log(fac)) if 0 < fac < 1 else 0
-        elapsed += more * float(np.mean(tcyc))
-    return {"s_per_step": elapsed, "cycles": cycles, "converged": converged,
-            "vcycle_ms": 1e3 * float(np.mean(tcyc)) if tcyc else None}
+    for _ in range(nsteps):
+        istep += 1
+        orc.step(mg, k, istep, istep, s)
+    return (time.perf_counter() - t0) / nsteps, ctrl.nummgits
+
+
+def reference_line(args, rank):
+    """--impl reference: the oracle (the reference's algorithm on the CPU)."""
+    if rank != 0:
+        return
+    case = make_case()
+    n = max(1, min(args.steps, 2))
+    sps, nmg = run_cpu_steps(case, n, warmup=min(args.warmup, 1))
+    val = case.cells() / sps / 1e6
+    sample = (f"{n} full steps of the 256x192x128 workload after {min(args.warmup, 1)} warm-up, "
+              f"reference solver settings ({nmg} V-cycles per step)")
+    line = {"metric": METRIC, "value": val, "unit": "Mcell-steps/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
+            "ms_per_step": 1e3 * sps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy default_rng)",
+            "config": {"workload": WORKLOAD, "cells": case.cells()},
+            "cpu_baseline": {"value": val, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -348,82 +298,72 @@ def main():
     if world > 1:
         # the path runs on one GPU; extra ranks are independent replicas
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    ncores = 1
     if args.impl == "reference":
-        if rank != 0:
-            return
-        case = make_case()
-        cpu = run_cpu_sample(case)
-        val = case.cells() / cpu["s_per_step"] / 1e6
-        line = {"metric": METRIC, "value": val, "unit": "Mcell-steps/s", "impl": "reference",
-                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * cpu["s_per_step"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded numpy default_rng)",
-                "config": {"workload": "mixing layer 256x192x128, WALE, projection step "
-                                       "(sour_p, lmg_solve to 1e-8, extrap_p, p_ref_subtract, "
-                                       "uvw_adv x3)", "cells": case.cells()},
-                "cpu_baseline": {"value": val, "unit": "Mcell-steps/s", "cores": ncores,
-                                 "kind": "port", "sample": f"one step, {cpu['cycles']} V-cycles"
-                                 + ("" if cpu["converged"] else " measured, rest extrapolated")},
-                "e2e": {"value": val, "unit": "Mcell-steps/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        reference_line(args, rank)
         return
-    case, ncell, res = run_gpu(args, rank)
+    case, res = run_gpu(args)
+    ncell = case.cells()
     if args.mode != "both" or args.no_e2e:
-        print(json.dumps({k: {kk: vv for kk, vv in v.items() if kk != "clocks"}
-                          for k, v in res.items()}))
+        print(json.dumps({k: {kk: vv for kk, vv in v.items() if kk not in ("clocks", "ctrl")}
+                          for k, v in res.items()}), flush=True)
         return
     mx, fp = res["mixed"], res["fp64"]
     value = ncell / (mx["ms_per_step"] * 1e-3) / 1e6 * world
-    # roofline of the level-1 FP32 red-black half sweep (dominant kernel):
-    # algorithmic bytes per launch = 6 B x interior cells (12 B/cell/sweep,
-    # read f, b and write f in FP32, matrix-free coefficients, half per colour)
-    alg = 6.0 * ncell
-    rb_avg_ms = mx["rb_ms"] / max(mx["rb_launches"], 1)
     peaks = {}
     pf = ROOT / "MEASURED_PEAKS.json"
     if pf.exists():
         peaks = json.loads(pf.read_text())
-    peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = alg / (rb_avg_ms * 1e-3) / 1e9
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    # dominant kernel: the level-1 FP32 red-black smoother, one colour per
+    # launch: 12 B/cell per sweep (read f, b; write f) / 2 = 6 B x cells
+    rb_avg_ms = mx["rb_ms"] / max(mx["rb_launches"], 1)
+    achieved = 6.0 * ncell / (rb_avg_ms * 1e-3) / 1e9
+    sweeps = mx["ctrl"].rb_sweeps
+    step_gbs = {m: step_bytes(m, r["cycles"], sweeps) * ncell / (r["ms_per_step"] * 1e-3) / 1e9
+                for m, r in (("mixed", mx), ("fp64", fp))}
     cpu = None
     if not args.no_cpu and rank == 0:
-        cpu = run_cpu_sample(case)
+        sps, nmg = run_cpu_steps(case, 1)
+        cpu = {"value": ncell / sps / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
+               "sample": f"1 full step of the same workload, reference solver settings "
+                         f"({nmg} V-cycles, lexicographic SOR), {sps:.1f} s"}
     e2e = mx["e2e"]
-    e2e_val = ncell / e2e["s_per_step"] / 1e6
     line = {
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mx["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
         "data": "synthetic (seeded numpy default_rng, seed 2)",
-        "config": {"workload": "mixing layer 256x192x128, WALE, projection step (subgrid, sour_p, "
-                               "lmg_solve to 1e-8 from zero, extrap_p, p_ref_subtract, uvw_adv x3, "
-                               "slipbc)",
-                   "cells": ncell, "l2": "inputs larger than L2, no flush",
+        "config": {"workload": WORKLOAD, "cells": ncell,
+                   "l2": "inputs larger than L2 (~2 GB working set), no flush",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "mixed": {"vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"],
+                  "vcycle_ms": mx["solve_ms"] / max(mx["cycles"], 1),
+                  "relres_max": mx["relres_max"]},
         "fp64": {"value": ncell / (fp["ms_per_step"] * 1e-3) / 1e6 * world,
-                 "ms_per_step": fp["ms_per_step"], "vcycles": fp["cycles"],
-                 "vcycle_ms": None},
-        "mixed": {"vcycles": mx["cycles"], "relres": mx["relres"]},
+                 "ms_per_step": fp["ms_per_step"], "vcycles_per_step": fp["cycles"],
+                 "solve_ms": fp["solve_ms"], "vcycle_ms": fp["solve_ms"] / max(fp["cycles"], 1),
+                 "relres_max": fp["relres_max"]},
         "speedup_mixed_vs_fp64": fp["ms_per_step"] / mx["ms_per_step"],
+        "solve_speedup_mixed_vs_fp64": fp["solve_ms"] / mx["solve_ms"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "k_rb<float> level 1", "avg_launch_ms": rb_avg_ms},
-        "e2e": {"value": e2e_val, "unit": "Mcell-steps/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                     "kernel": "k_rb<float> level-1 red-black SOR half sweep",
+                     "avg_launch_ms": rb_avg_ms},
+        "step_roofline": {"mixed_gbs": step_gbs["mixed"], "fp64_gbs": step_gbs["fp64"],
+                          "mixed_frac": step_gbs["mixed"] / peak,
+                          "fp64_frac": step_gbs["fp64"] / peak},
+        "e2e": {"value": ncell / e2e["s_per_step"] / 1e6, "unit": "Mcell-steps/s",
                 "h2d_bytes_per_step": e2e["h2d_bytes_per_step"],
                 "d2h_bytes_per_step": e2e["d2h_bytes_per_step"]},
         "gpu_launches": mx["launches"],
         "clocks": mx["clocks"],
     }
     if cpu is not None:
-        cv = ncell / cpu["s_per_step"] / 1e6
-        line["cpu_baseline"] = {"value": cv, "unit": "Mcell-steps/s", "cores": ncores,
-                                "kind": "port",
-                                "sample": f"one projection step, {cpu['cycles']} V-cycles"
-                                + ("" if cpu["converged"] else " measured, rest extrapolated")}
+        line["cpu_baseline"] = cpu
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

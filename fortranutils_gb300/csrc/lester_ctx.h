@@ -102,6 +102,8 @@ struct Ctx {
     double last_norms[4] = {0, 0, 0, 0};
     int last_cycles = 0;
     double last_relres = 0;
+    double last_solve_ms = 0;              // device time of the last fast solve
+    cudaEvent_t ev_solve[2] = {nullptr, nullptr};
 };
 
 extern Ctx *g_ctx;

@@ -385,6 +385,8 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_link);
     cudaFree(c->d_grad);
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_solve)
+        if (e) cudaEventDestroy(e);
     for (CycleGraph &G : c->cg) {
         if (G.exec) cudaGraphExecDestroy(G.exec);
         for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
@@ -733,6 +735,9 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     int nb = c.g.numbl;
     double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
     int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
+    for (cudaEvent_t &e : c.ev_solve)
+        if (!e) LES_CUDA(cudaEventCreate(&e));
+    LES_CUDA(cudaEventRecord(c.ev_solve[0], c.stream));
     launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
     STAGE_CHECK("initial halo");
     // singular operator: drive the residual of the compatible part of b
@@ -776,6 +781,13 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     }
     c.last_cycles = it;
     c.last_relres = rel;
+    {
+        LES_CUDA(cudaEventRecord(c.ev_solve[1], c.stream));
+        LES_CUDA(cudaEventSynchronize(c.ev_solve[1]));
+        float ms = 0;
+        LES_CUDA(cudaEventElapsedTime(&ms, c.ev_solve[0], c.ev_solve[1]));
+        c.last_solve_ms = ms;
+    }
     // reference-style norms and level-1 residual for the caller
     double n4[4];
     if ((r = norms_level(c, 1, A, f, b, residu, n4))) return r;
@@ -961,6 +973,13 @@ int lester_gpu_solve_stats(double *out)
     for (int q = 0; q < 4; q++) out[q] = g_ctx->last_norms[q];
     out[4] = g_ctx->last_cycles;
     out[5] = g_ctx->last_relres;
+    return 0;
+}
+
+int lester_gpu_solve_time(double *ms)
+{
+    LES_NEED_CTX();
+    *ms = g_ctx->last_solve_ms;
     return 0;
 }
 

@@ -210,6 +210,13 @@ def gpu_solve_stats():
             "relres": o[5]}
 
 
+def gpu_solve_time() -> float:
+    """Device milliseconds of the last fast solve."""
+    ms = C.c_double()
+    _check(lib().lester_gpu_solve_time(C.byref(ms)))
+    return ms.value
+
+
 # ----------------------------------------------------- reference routines
 METRIC_NAMES = ("dip diu div dix rdip rdiv rdix djp dju djv djx rdjp rdju rdjx hijp hjip hkip "
                 "hkjp hiju hjiu hkiu hkju hijv hjiv hkiv hkjv rp ru rv didjp rdidjp didju "

@@ -161,6 +161,9 @@ long lester_gpu_launch_count(void);
  * out[0..3] = rnorm, fnorm, enorm, vnorm of level 1 (code/norms.F:393-398),
  * out[4] = V-cycles, out[5] = ||b - A p|| / ||b|| */
 int lester_gpu_solve_stats(double *out);
+/* device milliseconds of the last fast solve (LES_PSOLVE_FP64 / MIXED), from
+ * its first residual to its last, by CUDA events on the library stream */
+int lester_gpu_solve_time(double *ms);
 /* kernel timing inside a timed region: CUDA events around each launch of
  * the level-1 red-black smoother of the fast solvers.  prof(1) clears and
  * starts, prof(0) stops; prof_read returns the summed milliseconds and the
