@@ -113,9 +113,11 @@ int set_err(int code, const char *fmt, ...);
 #define LES_CUDA(call)                                                                             \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \
-        if (e_ != cudaSuccess)                                                                     \
+        if (e_ != cudaSuccess) {                                                                   \
+            cudaGetLastError(); /* reported here; not again by a later check */                    \
             return les::set_err(LES_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,          \
                                 cudaGetErrorString(e_));                                           \
+        }                                                                                          \
     } while (0)
 
 #define LES_NEED_CTX()                                                                             \
@@ -128,7 +130,9 @@ int set_err(int code, const char *fmt, ...);
 // buffers and, for outputs, copied back by finish().
 class Staging {
   public:
-    explicit Staging(Ctx *c) : c_(c) {}
+    // `who` names the entry point in error messages; an error already
+    // pending on entry is reported as such rather than blamed on this call
+    explicit Staging(Ctx *c, const char *who = "?") : c_(c), who_(who), pre_(cudaGetLastError()) {}
     ~Staging();
     // in: read only; io: read and written
     int in(const double *user, long n, const double **dev);
@@ -139,6 +143,8 @@ class Staging {
   private:
     int map(const double *user, long n, bool out, double **dev);
     Ctx *c_;
+    const char *who_;
+    cudaError_t pre_;
     struct Ent {
         const double *user;
         double *dev;

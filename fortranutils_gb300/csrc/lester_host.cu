@@ -101,8 +101,11 @@ int Staging::io(double *user, long n, double **dev) { return map(user, n, true, 
 
 int Staging::finish()
 {
+    if (pre_ != cudaSuccess)
+        return set_err(LES_ERR_CUDA, "CUDA error pending before %s: %s", who_, cudaGetErrorString(pre_));
     if (!any_host_) {
-        LES_CUDA(cudaGetLastError());
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "%s: %s", who_, cudaGetErrorString(e));
         return 0;
     }
     for (auto &e : ent_)
@@ -621,10 +624,13 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
                 e1 = prof_event(c);
                 c.prof_launches++;
             }
-            if (e0) cudaEventRecord(e0, c.stream);
+            // inside a capture only an external record becomes an event
+            // node whose timestamps can be read after each replay
+            unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
+            if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
                          F.b, c.stream);
-            if (e1) cudaEventRecord(e1, c.stream);
+            if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
 }
@@ -991,7 +997,7 @@ int lester_swap_sc(const int *ivar1, const int *igrid, double *var, double *work
     Ctx &c = *g_ctx;
     int ig = *igrid, mos = mg_or_sg ? *mg_or_sg : 1;
     if (ig < 1 || ig > c.nummgl || (mos != 1 && ig != 1)) return set_err(LES_ERR_ARG, "bad igrid %d", ig);
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *d;
     int r = st.io(var, mos == 1 ? c.tot3 : c.tot_sg3, &d);
     if (r) return r;
@@ -1016,7 +1022,7 @@ int lester_comp_metric(const double *x, const double *y, const double *t, double
                         djx,  rdjp, rdju, rdjx, hijp, hjip, hkip, hkjp,  hiju,  hjiu, hkiu,   hkju,
                         hijv, hjiv, hkiv, hkjv, rp,   ru,   rv,   didjp, rdidjp, didju, rdidju, djdiv,
                         rdjdiv};
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *dx, *dy, *dz;
     int r;
     if ((r = st.in(x, c.totxy, &dx)) || (r = st.in(y, c.totxy, &dy)) || (r = st.in(t, c.totz, &dz))) return r;
@@ -1057,7 +1063,7 @@ int lester_coeff_p(const double *diu, const double *djv, const double *rdiv, con
 {
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *mu[6] = {diu, djv, rdiv, rdju, didjp, rp};
     const double *m[6], *ddkp, *ddkw;
     double *au[7] = {ap, aw, ae, as, an, al, ar}, *a[7];
@@ -1086,7 +1092,7 @@ int lester_sour_p(const double *diu, const double *djv, const double *rdiv, cons
     (void)gja;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *m[6], *f[5];
     double *o[4];
     int r;
@@ -1115,7 +1121,7 @@ int lester_lmg_solve(const double *ap, const double *aw, const double *ae, const
     (void)ra;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *au[7] = {ap, aw, ae, as, an, al, ar};
     Coef A;
     int r;
@@ -1153,7 +1159,7 @@ int lester_norms(const int *ilev, const int *mg_or_sg, const double *ap, const d
     int lev = *ilev;
     if (lev < 1 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
     if (mg_or_sg && *mg_or_sg != 1 && lev != 1) return set_err(LES_ERR_ARG, "single-grid x needs level 1");
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *au[7] = {ap, aw, ae, as, an, al, ar};
     Coef A;
     int r;
@@ -1179,7 +1185,7 @@ int lester_restriction(const int *ilev, const double *f, double *f1, double *wor
     Ctx &c = *g_ctx;
     int lev = *ilev;
     if (lev < 2 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *df;
     double *d1;
     int r;
@@ -1196,7 +1202,7 @@ int lester_prolongation(const int *ilev, double *f, double *work, int *offwork)
     Ctx &c = *g_ctx;
     int lev = *ilev;
     if (lev < 1 || lev >= c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *df;
     int r;
     if ((r = st.io(f, c.tot3, &df))) return r;
@@ -1218,7 +1224,7 @@ int lester_sporlx(const int *ilev, const double *ap, const double *aw, const dou
     int lev = *ilev;
     if (lev < 1 || lev > c.nummgl) return set_err(LES_ERR_ARG, "bad level %d", lev);
     if (niter && *niter != 1) return set_err(LES_ERR_ARG, "sporlx is only called with niter = 1");
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *au[7] = {ap, aw, ae, as, an, al, ar};
     Coef A;
     int r;
@@ -1242,7 +1248,7 @@ int lester_extrap_p(double *p, double *work, int *offwork)
     (void)offwork;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *dp;
     int r;
     if ((r = st.io(p, c.tot_sg3, &dp))) return r;
@@ -1255,7 +1261,7 @@ int lester_p_ref_subtract(double *p)
 {
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *dp;
     int r;
     if ((r = st.io(p, c.tot_sg3, &dp))) return r;
@@ -1274,7 +1280,7 @@ int lester_uvw_adv(const int *ivar1, const double *diu, const double *rp, const 
     Ctx &c = *g_ctx;
     int iv = *ivar1;
     if (iv < 1 || iv > 3) return set_err(LES_ERR_ARG, "uvw_adv: ivar1 %d", iv);
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *dd, *drp, *ddkw, *dui, *drho, *dpp;
     double *du;
     int r;
@@ -1292,7 +1298,7 @@ int lester_swap_rhos(double *rho, double *rhonp1, double *rhonm1)
 {
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *a, *b, *d;
     int r;
     if ((r = st.io(rho, c.tot_sg3, &a)) || (r = st.io(rhonp1, c.tot_sg3, &b)) || (r = st.io(rhonm1, c.tot_sg3, &d)))
@@ -1311,7 +1317,7 @@ int lester_search_lib(double *sc1, double *sc1var, double *rhonp1, double *tempe
     (void)istep;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *ds, *dr, *dt = nullptr;
     const double *drho;
     int r;
@@ -1339,7 +1345,7 @@ int lester_slipbc(const double *x, const double *y, const double *z, const doubl
     (void)step;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *ddjp, *dvi, *dp;
     double *du, *dv, *dw, *ds, *dr;
     int r;
@@ -1363,7 +1369,7 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v
     (void)offwork;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *dg, *dgs, *dsv, *dsd;
     const double *du, *dv, *dw, *dsc, *dvd = nullptr;
     int r;

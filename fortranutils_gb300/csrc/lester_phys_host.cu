@@ -89,7 +89,7 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
     if ((r = ensure_phys_tables(c))) return r;
     int iv = *iva;
     if (iv != 1 && iv != 2) return set_err(LES_ERR_ARG, "set_uv_int: iva %d", iv);
-    Staging st(&c);
+    Staging st(&c, __func__);
     UIntArgs A;
     memset(&A, 0, sizeof A);
     const double *mu[20] = {dip, diu, dix, rdix, djp, dju, djv, djx, rdjp, rdju,
@@ -135,7 +135,7 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
     Ctx &c = *g_ctx;
     int r;
     if ((r = ensure_phys_tables(c))) return r;
-    Staging st(&c);
+    Staging st(&c, __func__);
     WIntArgs A;
     memset(&A, 0, sizeof A);
     const double *mu[MW_N] = {dip, diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, ru};
@@ -183,7 +183,7 @@ int lester_set_virt_bc(const int *iva, const int *ilev, double *f, const double 
     if ((r = ensure_phys_tables(c))) return r;
     int iv = *iva;
     if (iv < 1 || iv > 3 || *ilev != 1) return set_err(LES_ERR_ARG, "set_virt_bc: velocities at level 1 only");
-    Staging st(&c);
+    Staging st(&c, __func__);
     VbcArgs A;
     memset(&A, 0, sizeof A);
     if ((r = st.io(f, c.tot_sg3, &A.f)) || (r = st.in(rho, c.tot_sg3, &A.rho)) ||
@@ -254,7 +254,7 @@ int lester_set_gamsc1_bc(const double *sc1, double *gamsc1, double *gamlam, cons
     Ctx &c = *g_ctx;
     int r;
     if ((r = ensure_phys_tables(c))) return r;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *ds, *ddiu, *ddjv, *ddkp, *drp;
     double *dg, *dl;
     if ((r = st.in(sc1, c.tot_sg3, &ds)) || (r = st.io(gamsc1, c.tot_sg3, &dg)) ||
@@ -283,7 +283,7 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
     Ctx &c = *g_ctx;
     int r;
     if ((r = ensure_phys_tables(c))) return r;
-    Staging st(&c);
+    Staging st(&c, __func__);
     Sc1Args A;
     memset(&A, 0, sizeof A);
     const double *mu[MW_N] = {dip, diu, rdiv, djp, djv, rdju, didjp, rdidjp, hkip, hkjp, hkiu, hkjv, rp, nullptr};
@@ -314,7 +314,7 @@ int lester_set_sc1_bc(double *sc1)
     Ctx &c = *g_ctx;
     int r;
     if ((r = ensure_phys_tables(c))) return r;
-    Staging st(&c);
+    Staging st(&c, __func__);
     double *d;
     if ((r = st.io(sc1, c.tot_sg3, &d))) return r;
     LevelGeom &L = c.lv[1];
@@ -337,7 +337,7 @@ int lester_set_sc1var(const double *u, const double *v, const double *w, const d
     (void)offwork;
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
-    Staging st(&c);
+    Staging st(&c, __func__);
     const double *ds, *ddip, *ddjp, *ddkp, *ddkw, *drp;
     double *dv;
     int r;

@@ -94,7 +94,7 @@ int lester_step(lester_fields *F, const int *istep)
                                s + 1);
         }
     // whole-state staging: host arrays are mirrored once for the step
-    Staging st(&c);
+    Staging st(&c, __func__);
     lester_fields D = *F;
     long n3 = c.tot_sg3, nm = c.tot3;
     double **f3[] = {&D.u, &D.v, &D.w, &D.sc1, &D.rho, &D.rhonp1, &D.rhonm1, &D.u_int, &D.v_int, &D.w_int,

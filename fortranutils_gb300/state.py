@@ -114,6 +114,19 @@ def cell_centre_y(case, ib: int = 0) -> np.ndarray:
     return 0.5 * (yv[:-1] + yv[1:])[: b.n[1]]
 
 
+def _close_walls(s: State) -> None:
+    """No flow through solid or slip y sides: v = 0 on the south face of the
+    first interior cell and of the north ghost cell (the wall faces, which
+    no routine of the step writes)."""
+    c = s.case
+    for ib, b in enumerate(c.blocks):
+        v = c.block_view(s["v"], ib)
+        if b.bc[2] in (L.BCT_WALL, L.BCT_ZERO_GRAD):
+            v[:, 1, :] = 0.0
+        if b.bc[3] in (L.BCT_WALL, L.BCT_ZERO_GRAD):
+            v[:, -1, :] = 0.0
+
+
 def init_channel(s: State, seed: int = 1, sigma: float = 0.05) -> State:
     """u = 1 - y^2 + N(0, sigma^2), v, w = N(0, sigma^2), rho = 1."""
     rng = np.random.default_rng(seed)
@@ -125,6 +138,7 @@ def init_channel(s: State, seed: int = 1, sigma: float = 0.05) -> State:
         c.block_view(s["u"], ib)[...] = (1.0 - yc ** 2)[None, :, None] + sigma * rng.standard_normal(sh)
         c.block_view(s["v"], ib)[...] = sigma * rng.standard_normal(sh)
         c.block_view(s["w"], ib)[...] = sigma * rng.standard_normal(sh)
+    _close_walls(s)
     for n in ("rho", "rhonp1", "rhonm1"):
         s[n][:] = 1.0
     s["vd_damping"][:] = 1.0
@@ -144,6 +158,7 @@ def init_mixing_layer(s: State, seed: int = 2, sigma: float = 0.02, rholo: float
         c.block_view(s["v"], ib)[...] = sigma * rng.standard_normal(sh)
         c.block_view(s["w"], ib)[...] = sigma * rng.standard_normal(sh)
         c.block_view(s["sc1"], ib)[...] = np.broadcast_to(0.5 * (1.0 + np.tanh(2.0 * yc))[None, :, None], sh)
+    _close_walls(s)
     f = s["sc1"]
     rho = 1.0 / (f / rhohi + (1.0 - f) / rholo)
     for n in ("rho", "rhonp1", "rhonm1"):
