@@ -100,9 +100,9 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def make_case():
+def make_case(shape=SHAPE):
     from fortranutils_gb300 import grid, lester as L
-    ni, nj, nk = SHAPE
+    ni, nj, nk = shape
     lx, ly, lz = DOMAIN
     return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
 
@@ -158,7 +158,7 @@ def run_gpu(args):
     from fortranutils_gb300 import build, lester as L, state as S
     build.build()
     torch.cuda.set_device(0)
-    case = make_case()
+    case = make_case(tuple(args.shape))
     res = {}
     modes = [("fp64", L.PSOLVE_FP64), ("mixed", L.PSOLVE_MIXED)]
     modes = [m for m in modes if args.mode in ("both", m[0])]
@@ -293,6 +293,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
     ap.add_argument("--mode", default="both", choices=["both", "mixed", "fp64"],
                     help="solvers to time (the JSON line needs both)")
+    ap.add_argument("--shape", type=int, nargs=3, default=list(SHAPE),
+                    help="cells per axis (smaller shapes are for profiling only)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -303,7 +305,7 @@ def main():
         return
     case, res = run_gpu(args)
     ncell = case.cells()
-    if args.mode != "both" or args.no_e2e:
+    if args.mode != "both" or args.no_e2e or tuple(args.shape) != SHAPE:
         print(json.dumps({k: {kk: vv for kk, vv in v.items() if kk not in ("clocks", "ctrl")}
                           for k, v in res.items()}), flush=True)
         return
