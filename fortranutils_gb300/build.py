@@ -35,6 +35,7 @@ UNITS = {
     "lester_phys_host.cu": [],
     "k_virtbc.cu": ["-fmad=false"],
     "lester_step.cu": [],
+    "lester_noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -238,6 +238,26 @@ int lester_norms(const int *ilev, const int *mg_or_sg, const double *ap,
                  const double *x, const double *b, double *residu,
                  double *res_norm, double *rhs_norm, double *err_norm,
                  double *var_norm);
+/* No counterpart in the reference.  lester_norms for one block, for hosts
+ * that cannot allocate device memory at the call (inside a stream capture,
+ * under a fixed memory budget, or with their own device pool): it needs no
+ * lester_gpu_init and allocates nothing.  Its scratch is a static device
+ * array of 4 * LES_NOALLOC_MAX_POINTS / 256 + 8 doubles (512 KB); blocks
+ * with more than LES_NOALLOC_MAX_POINTS interior points are rejected with
+ * LES_ERR_SIZE.  nijkp1 = points per axis incl. ghosts; every array is
+ * device memory in the reference's Fortran order; the norms are written to
+ * host scalars after the work on `stream` (a cudaStream_t, NULL for the
+ * default stream) completes.  Nothing in the scratch has to start at
+ * zero.  Calls that overlap on the GPU race on the one scratch.  The first
+ * call on each device looks up the scratch address (cudaGetSymbolAddress)
+ * and should come before any stream capture. */
+#define LES_NOALLOC_MAX_POINTS 4194304L
+int lester_norms_noalloc(const int *nijkp1, const double *ap, const double *aw,
+                         const double *ae, const double *as, const double *an,
+                         const double *al, const double *ar, const double *x,
+                         const double *b, double *residu, double *res_norm,
+                         double *rhs_norm, double *err_norm, double *var_norm,
+                         void *stream);
 /* code/restriction.F:5 restriction(ilev, f, f1, work, offwork) */
 int lester_restriction(const int *ilev, const double *f, double *f1,
                        double *work, int *offwork);
