@@ -41,6 +41,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mcell-steps/s & Poisson V-cycle ms: mixed-prec vs FP64 on GB300 at 1e-8 resid"
 SHAPE = (256, 192, 128)
 DOMAIN = (30.0, 30.0, 15.0)
+# FP64 physics kernels: 0 = fast build (reciprocal metric tables, FMA), the
+# product default; the reference arm and the CPU baseline are unaffected
+EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
 
@@ -110,7 +113,7 @@ def make_case(shape=SHAPE):
 def make_ctrl(psolve):
     from fortranutils_gb300 import lester as L
     return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
-                          rtol=1e-8, max_outer=200)
+                          rtol=1e-8, max_outer=200, exact=EXACT)
 
 
 def host_state(case, ctrl):

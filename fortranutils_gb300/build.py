@@ -24,18 +24,22 @@ LIBNAME = "liblester_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           "-I", str(PKG.parent / "include")]
-# translation unit -> extra flags
+# object -> (translation unit, extra flags).  The FP64 physics units are
+# built twice: exact (-fmad=false, namespace les_exact) and fast
+# (-DLES_FAST_PHYS, namespace les_fast).
 UNITS = {
-    "lester_host.cu": [],
-    "k_exact.cu": ["-fmad=false"],
-    "k_metric.cu": ["-fmad=false"],
-    "k_sgs.cu": ["-fmad=false"],
-    "k_fast.cu": [],
-    "k_phys.cu": ["-fmad=false"],
-    "lester_phys_host.cu": [],
-    "k_virtbc.cu": ["-fmad=false"],
-    "lester_step.cu": [],
-    "lester_noalloc.cu": ["-fmad=false"],
+    "lester_host": ("lester_host.cu", []),
+    "k_exact": ("k_exact.cu", ["-fmad=false"]),
+    "k_metric": ("k_metric.cu", ["-fmad=false"]),
+    "k_sgs": ("k_sgs.cu", ["-fmad=false"]),
+    "k_sgs_fast": ("k_sgs.cu", ["-DLES_FAST_PHYS"]),
+    "k_fast": ("k_fast.cu", []),
+    "k_phys": ("k_phys.cu", ["-fmad=false"]),
+    "k_phys_fast": ("k_phys.cu", ["-DLES_FAST_PHYS"]),
+    "lester_phys_host": ("lester_phys_host.cu", []),
+    "k_virtbc": ("k_virtbc.cu", ["-fmad=false"]),
+    "lester_step": ("lester_step.cu", []),
+    "lester_noalloc": ("lester_noalloc.cu", ["-fmad=false"]),
 }
 
 
@@ -53,8 +57,8 @@ def lib_path() -> Path:
     return LIBDIR / LIBNAME
 
 
-def _compile(src: str, extra: list[str], verbose: bool) -> Path:
-    obj = BUILD / (Path(src).stem + ".o")
+def _compile(name: str, src: str, extra: list[str], verbose: bool) -> Path:
+    obj = BUILD / (name + ".o")
     cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
@@ -71,14 +75,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     out = lib_path()
-    srcs = [CSRC / s for s in UNITS] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
+    srcs = [CSRC / u[0] for u in UNITS.values()] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
     srcs.append(PKG.parent / "include" / "lester_gpu.h")
     if out.exists() and not force:
         newest = max(p.stat().st_mtime for p in srcs)
         if out.stat().st_mtime >= newest:
             return out
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        futs = [ex.submit(_compile, s, f, verbose) for s, f in UNITS.items()]
+        futs = [ex.submit(_compile, n, s, f, verbose) for n, (s, f) in UNITS.items()]
         objs = [f.result() for f in futs]
     tmp = out.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]

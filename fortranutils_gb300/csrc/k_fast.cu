@@ -64,6 +64,30 @@ __global__ void k_conv_coef(const BlkDev *__restrict__ blk, const double *__rest
     }
 }
 
+// ---- tables of the fast physics kernels -------------------------------------
+struct RecipJob {
+    const double *src[24];
+    double *dst[24];
+};
+
+__global__ void k_recip(RecipJob J, long n)
+{
+    const double *s = J.src[blockIdx.y];
+    double *d = J.dst[blockIdx.y];
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        d[e] = 1.0 / s[e];
+}
+
+__global__ void k_delta_tables(const double *__restrict__ dip, const double *__restrict__ djp,
+                               const double *__restrict__ rp, long n2, const double *__restrict__ dkp,
+                               long n1, double *__restrict__ d2, double *__restrict__ d1)
+{
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n2; e += (long)gridDim.x * blockDim.x) {
+        d2[e] = pow(dip[e] * djp[e] * rp[e], .33333333);
+        if (e < n1) d1[e] = pow(dkp[e], .33333333);
+    }
+}
+
 // ---- red-black SOR half sweep ---------------------------------------------
 // Points with (i + j + k) % 2 == color are updated; the others are read.
 template <typename T>
@@ -374,6 +398,32 @@ void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double 
     k_interior_sum<<<dim3(gx, nb), 256, 0, st>>>(blk, b, partial);
     k_mean_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, ncell, out);
     count_launch(2);
+}
+
+void launch_recip(const double *const *src, double *const *dst, int ntab, long n, cudaStream_t st)
+{
+    RecipJob J;
+    for (int b0 = 0; b0 < ntab; b0 += 24) {
+        int m = ntab - b0 < 24 ? ntab - b0 : 24;
+        for (int t = 0; t < m; t++) {
+            J.src[t] = src[b0 + t];
+            J.dst[t] = dst[b0 + t];
+        }
+        unsigned gx = nb_(n, 256);
+        if (gx > 256) gx = 256;
+        k_recip<<<dim3(gx, m), 256, 0, st>>>(J, n);
+        count_launch(1);
+    }
+}
+
+void launch_delta_tables(const double *dip, const double *djp, const double *rp, long n2,
+                         const double *dkp, long n1, double *d2, double *d1, cudaStream_t st)
+{
+    long n = n2 > n1 ? n2 : n1;
+    unsigned gx = nb_(n, 256);
+    if (gx > 1024) gx = 1024;
+    k_delta_tables<<<gx, 256, 0, st>>>(dip, djp, rp, n2, dkp, n1, d2, d1);
+    count_launch(1);
 }
 
 template <typename T>

@@ -1,4 +1,5 @@
-// k_phys.cu -- momentum predictor and scalar transport (FP64, -fmad=false).
+// k_phys.cu -- momentum predictor and scalar transport (FP64; exact and fast
+// builds, see phys_variant.h).
 //
 //   set_u_int_block  code/set_u_int_block.F:103-462 (u, and v with the i/j
 //                    roles swapped exactly as set_uv_int passes them)
@@ -14,6 +15,9 @@
 //   set_sc1var_block code/set_sc1var_block.F:26-66
 #include "k_common.cuh"
 #include "kernels.h"
+#include "phys_variant.h"
+
+namespace LES_PHYS_NS {
 
 #define IDX2(b, i, j) ((b).off2 + ((i) - 1) + (long)(b).n[0] * ((j) - 1))
 
@@ -49,6 +53,9 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
     long ijw = ij - io_ij, ijs = ij - jo_ij, ijn = ij + jo_ij, ijnw = ijw + jo_ij;
     long ki = b.off1k * 0 + (k - 1) + (long)nkp1 * (i - 1);  // (k, i) of this block's wall array
     const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
+#ifdef LES_FAST_PHYS
+    const double *rdkp_ = A_.r_dkp + b.off1k, *rdkw_ = A_.r_dkw + b.off1k;
+#endif
     double di = A_.diu[ij], dj = A_.dju[ij];
     long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
     long ijksw = ijks - io, ijknw = ijkn - io, ijkwl = ijkw - ko, ijkwr = ijkw + ko;
@@ -94,40 +101,52 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
     double cc2 = A_.hkiu[ij] * rhoa * (wa * wa) * vol;
     double cc3 = -A_.hiju[ij] * rhoa * va * u[ijk] * vol;
     double conc = cc1 + cc2 + cc3;
-    double galwf = gamwf * areawf / A_.dip[ijw];
-    double galef = gamef * areaef / A_.dip[ij];
-    double galsf = gamsf * areasf / A_.djx[ij];
-    double galnf = gamnf * areanf / A_.djx[ijn];
-    double gallf = gamlf * areak / (A_.rp[ij] * dkw[k - 1]);
-    double galrf = gamrf * areak / (A_.rp[ij] * dkw[k]);
+    double galwf = QDIV(gamwf * areawf, A_.dip[ijw], A_.r_dip[ijw]);
+    double galef = QDIV(gamef * areaef, A_.dip[ij], A_.r_dip[ij]);
+    double galsf = QDIV(gamsf * areasf, A_.djx[ij], A_.r_djx[ij]);
+    double galnf = QDIV(gamnf * areanf, A_.djx[ijn], A_.r_djx[ijn]);
+    double gallf = QDIV(gamlf * areak, (A_.rp[ij] * dkw[k - 1]), A_.r_rp[ij] * rdkw_[k - 1]);
+    double galrf = QDIV(gamrf * areak, (A_.rp[ij] * dkw[k]), A_.r_rp[ij] * rdkw_[k]);
     double vwf = 0.5 * (v[ijkw] + v[ijknw]);
     double vef = 0.5 * (v[ijk] + v[ijkn]);
     double twf = galwf * 2.0 * (u[ijk] - u[ijkw]);
     double tef = galef * 2.0 * (u[ijke] - u[ijk]);
-    double tsf = galsf * A_.dix[ij] * (u[ijk] / A_.diu[ij] - u[ijks] / A_.diu[ijs]);
-    double tnf = galnf * A_.dix[ijn] * (u[ijkn] / A_.diu[ijn] - u[ijk] / A_.diu[ij]);
+    double tsf = galsf * A_.dix[ij] *
+                 (QDIV(u[ijk], A_.diu[ij], A_.r_diu[ij]) - QDIV(u[ijks], A_.diu[ijs], A_.r_diu[ijs]));
+    double tnf = galnf * A_.dix[ijn] *
+                 (QDIV(u[ijkn], A_.diu[ijn], A_.r_diu[ijn]) - QDIV(u[ijk], A_.diu[ij], A_.r_diu[ij]));
     double tlf = gallf * (u[ijk] - u[ijkl]);
     double trf = galrf * (u[ijkr] - u[ijk]);
     double cwf = 2.0 * gamwf * areawf * vwf * A_.hijp[ijw];
     double cef = 2.0 * gamef * areaef * vef * A_.hijp[ij];
-    double csf = gamsf * areasf * A_.djx[ij] * (v[ijk] / A_.djv[ij] - v[ijkw] / A_.djv[ijw]) / A_.dix[ij];
-    double cnf = gamnf * areanf * A_.djx[ijn] * (v[ijkn] / A_.djv[ijn] - v[ijknw] / A_.djv[ijnw]) /
-                 A_.dix[ijn];
-    double clf = gamlf * areak * A_.ru[ij] * (w[ijk] / A_.rp[ij] - w[ijkw] / A_.rp[ijw]) / A_.diu[ij];
-    double crf = gamrf * areak * A_.ru[ij] * (w[ijkr] / A_.rp[ij] - w[ijkwr] / A_.rp[ijw]) / A_.diu[ij];
+    double csf = QDIV(gamsf * areasf * A_.djx[ij] *
+                          (QDIV(v[ijk], A_.djv[ij], A_.r_djv[ij]) - QDIV(v[ijkw], A_.djv[ijw], A_.r_djv[ijw])),
+                      A_.dix[ij], A_.r_dix[ij]);
+    double cnf = QDIV(gamnf * areanf * A_.djx[ijn] *
+                          (QDIV(v[ijkn], A_.djv[ijn], A_.r_djv[ijn]) -
+                           QDIV(v[ijknw], A_.djv[ijnw], A_.r_djv[ijnw])),
+                      A_.dix[ijn], A_.r_dix[ijn]);
+    double clf = QDIV(gamlf * areak * A_.ru[ij] *
+                          (QDIV(w[ijk], A_.rp[ij], A_.r_rp[ij]) - QDIV(w[ijkw], A_.rp[ijw], A_.r_rp[ijw])),
+                      A_.diu[ij], A_.r_diu[ij]);
+    double crf = QDIV(gamrf * areak * A_.ru[ij] *
+                          (QDIV(w[ijkr], A_.rp[ij], A_.r_rp[ij]) - QDIV(w[ijkwr], A_.rp[ijw], A_.r_rp[ijw])),
+                      A_.diu[ij], A_.r_diu[ij]);
     double tiiwf = twf + cwf, tiief = tef + cef, tjisf = tsf + csf, tjinf = tnf + cnf;
     double tkilf = tlf + clf, tkirf = trf + crf;
     vsf = 0.5 * (v[ijk] + v[ijkw]);
     vnf = 0.5 * (v[ijkn] + v[ijknw]);
-    double dc1 = -2.0 * gama * vol * A_.hjiu[ij] * ((vnf - vsf) / A_.dju[ij] + u[ijk] * A_.hjiu[ij]);
+    double dc1 = -2.0 * gama * vol * A_.hjiu[ij] * (QDIV(vnf - vsf, A_.dju[ij], A_.r_dju[ij]) + u[ijk] * A_.hjiu[ij]);
     wlf = 0.5 * (w[ijk] + w[ijkw]);
     wrf = 0.5 * (w[ijkr] + w[ijkwr]);
-    double dc2 = -2.0 * gama * vol * A_.hkiu[ij] * (u[ijk] * A_.hkiu[ij] + va * A_.hkju[ij] + (wrf - wlf) / rdkp);
-    double udisf = 0.5 * (u[ijk] + u[ijks]) / A_.dix[ij];
-    double udinf = 0.5 * (u[ijk] + u[ijkn]) / A_.dix[ijn];
-    double vdjwf = 0.5 * (v[ijkw] + v[ijknw]) / A_.djp[ijw];
-    double vdjef = 0.5 * (v[ijk] + v[ijkn]) / A_.djp[ij];
-    double dc3 = gama * vol * A_.hiju[ij] * (di * (udinf - udisf) / dj + dj * (vdjef - vdjwf) / di);
+    double dc2 = -2.0 * gama * vol * A_.hkiu[ij] *
+                 (u[ijk] * A_.hkiu[ij] + va * A_.hkju[ij] + QDIV(wrf - wlf, rdkp, A_.r_rp[ij] * rdkp_[k - 1]));
+    double udisf = QDIV(0.5 * (u[ijk] + u[ijks]), A_.dix[ij], A_.r_dix[ij]);
+    double udinf = QDIV(0.5 * (u[ijk] + u[ijkn]), A_.dix[ijn], A_.r_dix[ijn]);
+    double vdjwf = QDIV(0.5 * (v[ijkw] + v[ijknw]), A_.djp[ijw], A_.r_djp[ijw]);
+    double vdjef = QDIV(0.5 * (v[ijk] + v[ijkn]), A_.djp[ij], A_.r_djp[ij]);
+    double dc3 = gama * vol * A_.hiju[ij] *
+                 (QDIV(di * (udinf - udisf), dj, A_.r_dju[ij]) + QDIV(dj * (vdjef - vdjwf), di, A_.r_diu[ij]));
     double diffc = dc1 + dc2 + dc3;
     // log-law wall stress (set_u_int_block.F:353-439)
     long kio = (iva == 1 ? A_.off_ki : A_.off_jk)[blockIdx.y];
@@ -196,7 +215,9 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
     }
     double h = conf + conc + diffc + tiief - tiiwf + tjinf - tjisf + tkirf - tkilf;
     A_.u_int[ijk] = u[ijk] * (rhou / rhonp1u) +
-                    dtime / (rhonp1u * vol) * (1.5 * h - 0.5 * A_.hu[ijk] + 0.5 * (A_.p[ijk] - A_.p[ijkw]) * vol / A_.diu[ij]);
+                    dtime / (rhonp1u * vol) *
+                        (1.5 * h - 0.5 * A_.hu[ijk] +
+                         QDIV(0.5 * (A_.p[ijk] - A_.p[ijkw]) * vol, A_.diu[ij], A_.r_diu[ij]));
     A_.hu[ijk] = h;
     (void)nip1;
 }
@@ -221,6 +242,10 @@ __global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ bl
     const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
     const double *const *M = A_.m;
 #define G(a, ii, jj) M[a][IDX2(b, ii, jj)]
+#ifdef LES_FAST_PHYS
+#define GI(a, ii, jj) A_.r[a][IDX2(b, ii, jj)]
+    const double *rdkp_ = A_.rdkp + b.off1k, *rdkw_ = A_.rdkw + b.off1k;
+#endif
     double radp = G(MW_RP, i, j), radw = G(MW_RP, i - 1, j), rade = G(MW_RP, i + 1, j);
     double rads = G(MW_RP, i, j - 1), radn = G(MW_RP, i, j + 1);
     long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
@@ -260,35 +285,38 @@ __global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ bl
     double u_wc = 0.25 * (u[ijk] + u[ijke] + u[ijkl] + u[ijkel]);
     double v_wc = 0.25 * (v[ijk] + v[ijkn] + v[ijkl] + v[ijknl]);
     double conc = -vol * rhow * (w[ijk] * (u_wc * G(MW_HKIP, i, j) + v_wc * G(MW_HKJP, i, j)));
-    double galwf = gamwf * areawf / G(MW_DIU, i, j);
-    double galef = gamef * areaef / G(MW_DIU, i + 1, j);
-    double galsf = gamsf * areasf / G(MW_DJV, i, j);
-    double galnf = gamnf * areanf / G(MW_DJV, i, j + 1);
-    double gallf = gamlf * areak / (radp * dkp[k - 2]);
-    double galrf = gamrf * areak / (radp * dkp[k - 1]);
+    double galwf = QDIV(gamwf * areawf, G(MW_DIU, i, j), GI(MW_DIU, i, j));
+    double galef = QDIV(gamef * areaef, G(MW_DIU, i + 1, j), GI(MW_DIU, i + 1, j));
+    double galsf = QDIV(gamsf * areasf, G(MW_DJV, i, j), GI(MW_DJV, i, j));
+    double galnf = QDIV(gamnf * areanf, G(MW_DJV, i, j + 1), GI(MW_DJV, i, j + 1));
+    double gallf = QDIV(gamlf * areak, (radp * dkp[k - 2]), GI(MW_RP, i, j) * rdkp_[k - 2]);
+    double galrf = QDIV(gamrf * areak, (radp * dkp[k - 1]), GI(MW_RP, i, j) * rdkp_[k - 1]);
     double radwf = 0.5 * (radp + radw), radef = 0.5 * (radp + rade);
     double radsf = 0.5 * (radp + rads), radnf = 0.5 * (radp + radn);
     double ulf = 0.5 * (u[ijkl] + u[ijkel]), urf = 0.5 * (u[ijk] + u[ijke]);
     double vlf = 0.5 * (v[ijkl] + v[ijknl]), vrf = 0.5 * (v[ijk] + v[ijkn]);
     double wwf = 0.5 * (w[ijk] + w[ijkw]), wef = 0.5 * (w[ijk] + w[ijke]);
     double wsf = 0.5 * (w[ijk] + w[ijks]), wnf = 0.5 * (w[ijk] + w[ijkn]);
-    double twf = galwf * radwf * (w[ijk] / radp - w[ijkw] / radw);
-    double tef = galef * radef * (w[ijke] / rade - w[ijk] / radp);
+    double twf = galwf * radwf * (QDIV(w[ijk], radp, GI(MW_RP, i, j)) - QDIV(w[ijkw], radw, GI(MW_RP, i - 1, j)));
+    double tef = galef * radef * (QDIV(w[ijke], rade, GI(MW_RP, i + 1, j)) - QDIV(w[ijk], radp, GI(MW_RP, i, j)));
     double tsf = galsf * (w[ijk] - w[ijks]);
     double tnf = galnf * (w[ijkn] - w[ijk]);
     double tlf = 2.0 * gallf * (w[ijk] - w[ijkl]);
     double trf = 2.0 * galrf * (w[ijkr] - w[ijk]);
-    double cwf = gamwf * areawf * ((u[ijk] - u[ijkl]) / dkw[k - 1] / radwf - wwf * G(MW_HKIU, i, j));
-    double cef = gamef * areaef * ((u[ijke] - u[ijkel]) / dkw[k - 1] / radef - wef * G(MW_HKIU, i + 1, j));
+    double cwf = gamwf * areawf * (QDIV(u[ijk] - u[ijkl], dkw[k - 1], rdkw_[k - 1]) / radwf - wwf * G(MW_HKIU, i, j));
+    double cef = gamef * areaef *
+                 (QDIV(u[ijke] - u[ijkel], dkw[k - 1], rdkw_[k - 1]) / radef - wef * G(MW_HKIU, i + 1, j));
     double csf = (j == 2) ? 0.0
-                          : gamsf * areasf * ((v[ijk] - v[ijkl]) / dkw[k - 1] / radsf - wsf * G(MW_HKJV, i, j));
-    double cnf = gamnf * areanf * ((v[ijkn] - v[ijknl]) / dkw[k - 1] / radnf - wnf * G(MW_HKJV, i, j + 1));
+                          : gamsf * areasf *
+                                (QDIV(v[ijk] - v[ijkl], dkw[k - 1], rdkw_[k - 1]) / radsf - wsf * G(MW_HKJV, i, j));
+    double cnf = gamnf * areanf *
+                 (QDIV(v[ijkn] - v[ijknl], dkw[k - 1], rdkw_[k - 1]) / radnf - wnf * G(MW_HKJV, i, j + 1));
     double clf = 2.0 * gamlf * areak * (ulf * G(MW_HKIP, i, j) + vlf * G(MW_HKJP, i, j));
     double crf = 2.0 * gamrf * areak * (urf * G(MW_HKIP, i, j) + vrf * G(MW_HKJP, i, j));
-    double dwdy = (wnf - wsf) / G(MW_DJP, i, j);
-    double dvdz = (vrf - vlf) / (radp * dkw[k - 1]);
-    double dwdx = (wef - wwf) / G(MW_DIP, i, j);
-    double dudz = (urf - ulf) / (radp * dkw[k - 1]);
+    double dwdy = QDIV(wnf - wsf, G(MW_DJP, i, j), GI(MW_DJP, i, j));
+    double dvdz = QDIV(vrf - vlf, (radp * dkw[k - 1]), GI(MW_RP, i, j) * rdkw_[k - 1]);
+    double dwdx = QDIV(wef - wwf, G(MW_DIP, i, j), GI(MW_DIP, i, j));
+    double dudz = QDIV(urf - ulf, (radp * dkw[k - 1]), GI(MW_RP, i, j) * rdkw_[k - 1]);
     double diffc1 = G(MW_HKIP, i, j) * (dwdx + dudz - w[ijk] * G(MW_HKIP, i, j)) * vol * gamrf;
     double diffc2 = G(MW_HKJP, i, j) * (dwdy + dvdz - w[ijk] * G(MW_HKJP, i, j)) * vol * gamrf;
     double diffc = diffc1 + diffc2;
@@ -363,6 +391,9 @@ __global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ bl
                     dtime / (vol * rhonp1w) * (1.5 * h - 0.5 * A_.hw[ijk] + 0.5 * areak * (A_.p[ijk] - A_.p[ijkl]));
     A_.hw[ijk] = h;
 #undef G
+#ifdef GI
+#undef GI
+#endif
 }
 
 // ---------------------------------------------------------- scalar
@@ -497,35 +528,42 @@ __global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk
     double gamrf = 0.5 * (gs[ijk] + gs[ijkr]) * rhorf + 0.5 * (gl[ijk] + gl[ijkr]);
     double uwf = A_.u[ijk], uef = A_.u[ijke], vsf = A_.v[ijk], vnf = A_.v[ijkn];
     double wlf = A_.w[ijk], wrf = A_.w[ijkr];
-    double dfdxwf = (sc1[ijk] - sc1[ijkw]) / G(MW_DIU, i, j);
-    double dfdxef = (sc1[ijke] - sc1[ijk]) / G(MW_DIU, i + 1, j);
+#ifdef LES_FAST_PHYS
+#define GI(a, ii, jj) A_.r[a][IDX2(b, ii, jj)]
+    const double *rdkp_ = A_.rdkp + b.off1k;
+#endif
+    double dfdxwf = QDIV(sc1[ijk] - sc1[ijkw], G(MW_DIU, i, j), GI(MW_DIU, i, j));
+    double dfdxef = QDIV(sc1[ijke] - sc1[ijk], G(MW_DIU, i + 1, j), GI(MW_DIU, i + 1, j));
     const long gst = A_.gstride;
     const double *GR = A_.grad;
     int gm = A_.gm;
     double dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
     if (i == 2) dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D) ? dfdxwf
                           : GR[(long)(A_.link[blockIdx.y * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
-    else dfdxwwf = (sc1[ijkw] - sc1[ijkw - io]) / G(MW_DIU, i - 1, j);
+    else dfdxwwf = QDIV(sc1[ijkw] - sc1[ijkw - io], G(MW_DIU, i - 1, j), GI(MW_DIU, i - 1, j));
     if (i == ni) dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D) ? dfdxef
                            : GR[(long)(A_.link[blockIdx.y * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
-    else dfdxeef = (sc1[ijke + io] - sc1[ijke]) / G(MW_DIU, i + 2, j);
-    double dfdysf = (sc1[ijk] - sc1[ijks]) / G(MW_DJV, i, j);
-    double dfdynf = (sc1[ijkn] - sc1[ijk]) / G(MW_DJV, i, j + 1);
+    else dfdxeef = QDIV(sc1[ijke + io] - sc1[ijke], G(MW_DIU, i + 2, j), GI(MW_DIU, i + 2, j));
+    double dfdysf = QDIV(sc1[ijk] - sc1[ijks], G(MW_DJV, i, j), GI(MW_DJV, i, j));
+    double dfdynf = QDIV(sc1[ijkn] - sc1[ijk], G(MW_DJV, i, j + 1), GI(MW_DJV, i, j + 1));
     if (j == 2) dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D) ? dfdysf
                           : GR[(long)(A_.link[blockIdx.y * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
-    else dfdyssf = (sc1[ijks] - sc1[ijks - jo]) / G(MW_DJV, i, j - 1);
+    else dfdyssf = QDIV(sc1[ijks] - sc1[ijks - jo], G(MW_DJV, i, j - 1), GI(MW_DJV, i, j - 1));
     if (j == nj) dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D) ? dfdynf
                            : GR[(long)(A_.link[blockIdx.y * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
-    else dfdynnf = (sc1[ijkn + jo] - sc1[ijkn]) / G(MW_DJV, i, j + 2);
+    else dfdynnf = QDIV(sc1[ijkn + jo] - sc1[ijkn], G(MW_DJV, i, j + 2), GI(MW_DJV, i, j + 2));
     double rpij = G(MW_RP, i, j);
-    double dfdzlf = (sc1[ijk] - sc1[ijkl]) / (rpij * dkp[k - 2]);
-    double dfdzrf = (sc1[ijkr] - sc1[ijk]) / (rpij * dkp[k - 1]);
+#ifdef LES_FAST_PHYS
+    const double rrpij = GI(MW_RP, i, j);
+#endif
+    double dfdzlf = QDIV(sc1[ijk] - sc1[ijkl], (rpij * dkp[k - 2]), rrpij * rdkp_[k - 2]);
+    double dfdzrf = QDIV(sc1[ijkr] - sc1[ijk], (rpij * dkp[k - 1]), rrpij * rdkp_[k - 1]);
     if (k == 2) dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D) ? dfdzlf
                           : GR[(long)(A_.link[blockIdx.y * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
-    else dfdzllf = (sc1[ijkl] - sc1[ijkl - ko]) / (rpij * dkp[k - 3]);
+    else dfdzllf = QDIV(sc1[ijkl] - sc1[ijkl - ko], (rpij * dkp[k - 3]), rrpij * rdkp_[k - 3]);
     if (k == nk) dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D) ? dfdzrf
                            : GR[(long)(A_.link[blockIdx.y * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
-    else dfdzrrf = (sc1[ijkr + ko] - sc1[ijkr]) / (rpij * dkp[k]);
+    else dfdzrrf = QDIV(sc1[ijkr + ko] - sc1[ijkr], (rpij * dkp[k]), rrpij * rdkp_[k]);
     double rwst = (uwf >= 0.0) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
     double rest = (uef > 0.0) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
     double rsth = (vsf >= 0.0) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
@@ -585,14 +623,18 @@ __global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk
     if (tmp > 1.0) tmp = 1.0;
     sc1[ijk] = tmp;
 #undef G
+#ifdef GI
+#undef GI
+#endif
 }
 
 // code/set_sc1var_block.F:26-66
 __global__ void k_sc1var(const BlkDev *__restrict__ blk, const double *__restrict__ sc1,
                          double *__restrict__ sc1var, const double *__restrict__ dip,
                          const double *__restrict__ djp, const double *__restrict__ rp,
-                         const double *__restrict__ dkp, const double *__restrict__ dkw)
+                         const double *__restrict__ dkp, const double *__restrict__ dkw, SgsFast F)
 {
+    (void)F;
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
@@ -607,16 +649,18 @@ __global__ void k_sc1var(const BlkDev *__restrict__ blk, const double *__restric
     double fnf = 0.5 * (sc1[ijk] + sc1[ijk + jo]);
     double flf = 0.5 * (sc1[ijk] + sc1[ijk - ko]);
     double frf = 0.5 * (sc1[ijk] + sc1[ijk + ko]);
-    double dfdip = (fef - fwf) / dip[ij];
-    double dfdjp = (fnf - fsf) / djp[ij];
-    double dfdkp = (frf - flf) / (rp[ij] * dkw[b.off1k + k - 1]);
+    double dfdip = QDIV(fef - fwf, dip[ij], F.r_dip[ij]);
+    double dfdjp = QDIV(fnf - fsf, djp[ij], F.r_djp[ij]);
+    double dfdkp = QDIV(frf - flf, (rp[ij] * dkw[b.off1k + k - 1]), F.r_rp[ij] * F.r_dkw[b.off1k + k - 1]);
     double dfdijk = dfdip * dfdip + dfdjp * dfdjp + dfdkp * dfdkp;
+#ifdef LES_FAST_PHYS
+    double delta = F.delta2d[ij] * F.delta1d[b.off1k + k - 1];
+#else
     double dk = rp[ij] * dkp[b.off1k + k - 1];
     double delta = pow(dip[ij] * djp[ij] * dk, .33333333);
+#endif
     sc1var[ijk] = cfv * dfdijk * (delta * delta);
 }
-
-namespace les {
 
 static inline unsigned nbk(long n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -626,7 +670,7 @@ void launch_set_u_int(const BlkDev *blk, int nb, long maxcell, int iva, const UI
 {
     k_set_u_int<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, iva, a, dtime, iststep, visc, ylaminar,
                                                             kappa, cwfun);
-    count_launch(1);
+    les::count_launch(1);
 }
 
 void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a, double dtime,
@@ -635,14 +679,14 @@ void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a
 {
     k_set_w_int<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, a, dtime, iststep, visc, ylaminar, kappa,
                                                             cwfun);
-    count_launch(1);
+    les::count_launch(1);
 }
 
 void launch_fill(double *a, double val, long n, cudaStream_t st)
 {
     unsigned g = nbk(n, 256);
     k_fill<<<g > 4096 ? 4096 : g, 256, 0, st>>>(a, val, n);
-    count_launch(1);
+    les::count_launch(1);
 }
 
 void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f, double *gam,
@@ -652,7 +696,7 @@ void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f
 {
     k_face_bc<<<dim3(nbk(maxface, 128), 3, nb), 128, 0, st>>>(blk, mode, f, gam, gaml, sc1, diu, djv, rp, dkp,
                                                              grad, gstride, gm);
-    count_launch(1);
+    les::count_launch(1);
 }
 
 void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax, const Sc1Args &a,
@@ -660,15 +704,15 @@ void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax,
 {
     unsigned gx = nbk(maxjk, 128);
     for (int s = smin; s <= smax; s++) k_sc1_wave<<<dim3(gx, nb), 128, 0, st>>>(blk, s, a, dtime);
-    count_launch(smax - smin + 1);
+    les::count_launch(smax - smin + 1);
 }
 
 void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,
                    const double *dip, const double *djp, const double *rp, const double *dkp,
-                   const double *dkw, cudaStream_t st)
+                   const double *dkw, const SgsFast &f, cudaStream_t st)
 {
-    k_sc1var<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, sc1, sc1var, dip, djp, rp, dkp, dkw);
-    count_launch(1);
+    k_sc1var<<<dim3(nbk(maxcell, 128), nb), 128, 0, st>>>(blk, sc1, sc1var, dip, djp, rp, dkp, dkw, f);
+    les::count_launch(1);
 }
 
-} // namespace les
+} // namespace LES_PHYS_NS

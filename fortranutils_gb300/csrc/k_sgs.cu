@@ -1,5 +1,5 @@
-// k_sgs.cu -- eddy-viscosity kernels (FP64, -fmad=false), one thread per
-// interior point of every block.
+// k_sgs.cu -- eddy-viscosity kernels (FP64; exact and fast builds, see
+// phys_variant.h), one thread per interior point of every block.
 //
 // subgrid (code/subgrid.F:58-92) dispatches on the model:
 //   Smagorinsky  code/subgrid_smagorinsky.F:85-237
@@ -11,6 +11,9 @@
 // operation-for-operation.
 #include "k_common.cuh"
 #include "kernels.h"
+#include "phys_variant.h"
+
+namespace LES_PHYS_NS {
 
 #define IDX2(b, i, j) ((b).off2 + ((i) - 1) + (long)(b).n[0] * ((j) - 1))
 
@@ -22,8 +25,10 @@ __global__ void __launch_bounds__(128) k_subgrid(
     const double *__restrict__ dip, const double *__restrict__ diu, const double *__restrict__ djp,
     const double *__restrict__ djv, const double *__restrict__ dkp, const double *__restrict__ dkw,
     const double *__restrict__ hijp, const double *__restrict__ hjip,
-    const double *__restrict__ hkip, const double *__restrict__ hkjp, const double *__restrict__ rp)
+    const double *__restrict__ hkip, const double *__restrict__ hkjp, const double *__restrict__ rp,
+    SgsFast F)
 {
+    (void)F;
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
@@ -44,6 +49,9 @@ __global__ void __launch_bounds__(128) k_subgrid(
          ijkwr = ijkw + ko, ijker = ijke + ko, ijksr = ijks + ko, ijknr = ijkn + ko;
     long ij = IDX2(b, i, j);
     double dkwk = dkw[b.off1k + k - 1], dkpk = dkp[b.off1k + k - 1];
+#ifdef LES_FAST_PHYS
+    const double rdi = F.r_dip[ij], rdj = F.r_djp[ij], rdkp = F.r_dkp[b.off1k + k - 1];
+#endif
 
     double fwf = 0.5 * (sc1[ijk] + sc1[ijkw]);
     double fef = 0.5 * (sc1[ijk] + sc1[ijke]);
@@ -51,9 +59,9 @@ __global__ void __launch_bounds__(128) k_subgrid(
     double fnf = 0.5 * (sc1[ijk] + sc1[ijkn]);
     double flf = 0.5 * (sc1[ijk] + sc1[ijkl]);
     double frf = 0.5 * (sc1[ijk] + sc1[ijkr]);
-    double dfdip = (fef - fwf) / dip[ij];
-    double dfdjp = (fnf - fsf) / djp[ij];
-    double dfdkp = (frf - flf) / (rp[ij] * dkwk);
+    double dfdip = QDIV(fef - fwf, dip[ij], rdi);
+    double dfdjp = QDIV(fnf - fsf, djp[ij], rdj);
+    double dfdkp = QDIV(frf - flf, (rp[ij] * dkwk), F.r_rp[ij] * F.r_dkw[b.off1k + k - 1]);
 
     double up = 0.5 * (u[ijk] + u[ijke]);
     double vp = 0.5 * (v[ijk] + v[ijkn]);
@@ -67,10 +75,10 @@ __global__ void __launch_bounds__(128) k_subgrid(
     double vlf = 0.25 * (v[ijk] + v[ijkn] + v[ijkl] + v[ijknl]);
     double vrf = 0.25 * (v[ijk] + v[ijkn] + v[ijkr] + v[ijknr]);
 
-    double dudi = (u[ijke] - u[ijk]) / di + vp * hijp[ij];
-    double dvdi = (vef - vwf) / di - up * hijp[ij];
-    double dudj = (unf - usf) / dj - vp * hjip[ij];
-    double dvdj = (v[ijkn] - v[ijk]) / dj + up * hjip[ij];
+    double dudi = QDIV(u[ijke] - u[ijk], di, rdi) + vp * hijp[ij];
+    double dvdi = QDIV(vef - vwf, di, rdi) - up * hijp[ij];
+    double dudj = QDIV(unf - usf, dj, rdj) - vp * hjip[ij];
+    double dvdj = QDIV(v[ijkn] - v[ijk], dj, rdj) + up * hjip[ij];
     double dwdi, dwdj, dudk, dvdk, dwdk;
     if (gotrad) {
         long jn = b.n[0];
@@ -85,25 +93,33 @@ __global__ void __launch_bounds__(128) k_subgrid(
         dwdi = radp * (wdre - wdrw) / (diu[ij] + diu[ij + 1]);
         dwdj = radp * (wdrn - wdrs) / (djv[ij] + djv[ij + jn]);
         double wp = 0.5 * (w[ijk] + w[ijkr]);
-        dudk = (urf - ulf) / dk - wp * hki;
-        dvdk = (vrf - vlf) / dk - wp * hkj;
-        dwdk = (w[ijkr] - w[ijk]) / dk + up * hki + vp * hkj;
+#ifdef LES_FAST_PHYS
+        const double rdk = F.r_rp[ij] * rdkp;
+#endif
+        dudk = QDIV(urf - ulf, dk, rdk) - wp * hki;
+        dvdk = QDIV(vrf - vlf, dk, rdk) - wp * hkj;
+        dwdk = QDIV(w[ijkr] - w[ijk], dk, rdk) + up * hki + vp * hkj;
     } else {
         dk = dkpk;
         double wwf = 0.25 * (w[ijk] + w[ijkr] + w[ijkw] + w[ijkwr]);
         double wef = 0.25 * (w[ijk] + w[ijkr] + w[ijke] + w[ijker]);
         double wsf = 0.25 * (w[ijk] + w[ijkr] + w[ijks] + w[ijksr]);
         double wnf = 0.25 * (w[ijk] + w[ijkr] + w[ijkn] + w[ijknr]);
-        dwdi = (wef - wwf) / di;
-        dwdj = (wnf - wsf) / dj;
-        dudk = (urf - ulf) / dk;
-        dvdk = (vrf - vlf) / dk;
-        dwdk = (w[ijkr] - w[ijk]) / dk;
+        dwdi = QDIV(wef - wwf, di, rdi);
+        dwdj = QDIV(wnf - wsf, dj, rdj);
+        dudk = QDIV(urf - ulf, dk, rdkp);
+        dvdk = QDIV(vrf - vlf, dk, rdkp);
+        dwdk = QDIV(w[ijkr] - w[ijk], dk, rdkp);
     }
     double sijsij = dvdj * dvdj + dwdk * dwdk + dudi * dudi +
                     0.5 * ((dudj + dvdi) * (dudj + dvdi) + (dvdk + dwdj) * (dvdk + dwdj) +
                            (dudk + dwdi) * (dudk + dwdi));
+#ifdef LES_FAST_PHYS
+    // (di dj dk)^e = (dip djp rp)^e dkp^e: rp is 1 exactly off polar grids
+    double delta_xyz = F.delta2d[ij] * F.delta1d[b.off1k + k - 1];
+#else
     double delta_xyz = pow(di * dj * dk, .33333333);
+#endif
     double g;
     if (model == 1) {
         double evisc = csles * delta_xyz * vdd[ijk];
@@ -123,7 +139,13 @@ __global__ void __launch_bounds__(128) k_subgrid(
                       0.5 * (g13 + g31) + 0.5 * (g23 + g32);
         double sd2 = sdij * sdij;
         double ev = (csles * delta_xyz) * (csles * delta_xyz);
+#ifdef LES_FAST_PHYS
+        // x^1.5 = x sqrt(x), x^2.5 = x^2 sqrt(x), x^1.25 = x sqrt(sqrt(x)) for x >= 0
+        double rsd = sqrt(sd2), rss = sqrt(sijsij);
+        g = ev * ((sd2 * rsd) / (sijsij * sijsij * rss + sd2 * sqrt(rsd)));
+#else
         g = ev * (pow(sd2, 1.5) / (pow(sijsij, 2.5) + pow(sd2, 1.25)));
+#endif
     }
     gam[ijk] = g;
     gamsc1[ijk] = (csles == 0.0) ? 0.0 : g / sct;
@@ -133,18 +155,16 @@ __global__ void __launch_bounds__(128) k_subgrid(
     sc1dis[ijk] = sv * sqrt(2.0 * sijsij);
 }
 
-namespace les {
-
 void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,
                     double *gam, double *gamsc1, const double *u, const double *v, const double *w,
                     const double *sc1, double *sc1var, double *sc1dis, const double *vdd,
-                    const double *const *m, cudaStream_t st)
+                    const double *const *m, const SgsFast &f, cudaStream_t st)
 {
     // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
     k_subgrid<<<dim3((unsigned)((maxcell + 127) / 128), nb), 128, 0, st>>>(
         blk, model, csles, gotrad, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m[0], m[1], m[2],
-        m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10]);
-    count_launch(1);
+        m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], f);
+    les::count_launch(1);
 }
 
-} // namespace les
+} // namespace LES_PHYS_NS

@@ -58,11 +58,6 @@ void fill_metblk(void *dst, int idx, const int *n, long off2, long off1k, long o
 void fill_metface(void *dst, int idx, long src2, long dst2, long stride, long sstride, int len,
                   long srck, long dstk);
 
-// k_sgs.cu
-void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,
-                    double *gam, double *gamsc1, const double *u, const double *v, const double *w,
-                    const double *sc1, double *sc1var, double *sc1dis, const double *vdd,
-                    const double *const *m, cudaStream_t st);
 
 // k_fast.cu (T = float or double)
 template <typename T>
@@ -92,27 +87,48 @@ void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *
 template <typename T>
 void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st);
 
-// k_phys.cu
-void launch_set_u_int(const BlkDev *blk, int nb, long maxcell, int iva, const UIntArgs &a,
-                      double dtime, int iststep, double visc, double ylaminar, double kappa,
-                      double cwfun, cudaStream_t st);
-void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a, double dtime,
-                      int iststep, double visc, double ylaminar, double kappa, double cwfun,
-                      cudaStream_t st);
-void launch_fill(double *a, double val, long n, cudaStream_t st);
-void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f, double *gam,
-                    double *gaml, const double *sc1, const double *diu, const double *djv,
-                    const double *rp, const double *dkp, double *grad, long gstride, int gm,
-                    cudaStream_t st);
-void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax, const Sc1Args &a,
-                      double dtime, cudaStream_t st);
-void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,
-                   const double *dip, const double *djp, const double *rp, const double *dkp,
-                   const double *dkw, cudaStream_t st);
-
 // k_virtbc.cu
 void launch_vbc_side(const BlkDev *blk, int nb, int iva, int side, unsigned long long wallmask,
                      unsigned long long initmask, const VbcArgs &a, long maxpts, double visc,
                      double kappa, double aplus, double ylam, double value, cudaStream_t st);
 
+// k_fast.cu: tables of the fast physics kernels.  dst[t][e] = 1 / src[t][e]
+// for the first n entries of each table; and the split filter width
+// d2[e] = (dip djp rp)^0.33333333 over n2 entries, d1[e] = dkp^0.33333333
+// over n1 entries.
+void launch_recip(const double *const *src, double *const *dst, int ntab, long n, cudaStream_t st);
+void launch_delta_tables(const double *dip, const double *djp, const double *rp, long n2,
+                         const double *dkp, long n1, double *d2, double *d1, cudaStream_t st);
+
 } // namespace les
+
+// k_phys.cu and k_sgs.cu, built twice (phys_variant.h): les_exact and les_fast
+#define LES_PHYS_LAUNCHERS                                                                          \
+    void launch_set_u_int(const BlkDev *blk, int nb, long maxcell, int iva, const UIntArgs &a,      \
+                          double dtime, int iststep, double visc, double ylaminar, double kappa,   \
+                          double cwfun, cudaStream_t st);                                           \
+    void launch_set_w_int(const BlkDev *blk, int nb, long maxcell, const WIntArgs &a, double dtime, \
+                          int iststep, double visc, double ylaminar, double kappa, double cwfun,   \
+                          cudaStream_t st);                                                         \
+    void launch_fill(double *a, double val, long n, cudaStream_t st);                               \
+    void launch_face_bc(const BlkDev *blk, int nb, long maxface, int mode, double *f, double *gam,  \
+                        double *gaml, const double *sc1, const double *diu, const double *djv,      \
+                        const double *rp, const double *dkp, double *grad, long gstride, int gm,    \
+                        cudaStream_t st);                                                           \
+    void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax,                \
+                          const Sc1Args &a, double dtime, cudaStream_t st);                         \
+    void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,  \
+                       const double *dip, const double *djp, const double *rp, const double *dkp,   \
+                       const double *dkw, const SgsFast &f, cudaStream_t st);                       \
+    void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles,           \
+                        int gotrad, double *gam, double *gamsc1, const double *u, const double *v,  \
+                        const double *w, const double *sc1, double *sc1var, double *sc1dis,         \
+                        const double *vdd, const double *const *m, const SgsFast &f,               \
+                        cudaStream_t st);
+
+namespace les_exact {
+LES_PHYS_LAUNCHERS
+}
+namespace les_fast {
+LES_PHYS_LAUNCHERS
+}

@@ -6,6 +6,7 @@
 #include <vector>
 #include "../../include/lester_gpu.h"
 #include "k_common.cuh"
+#include "phys_args.h"
 
 namespace les {
 
@@ -103,12 +104,25 @@ struct Ctx {
     int last_cycles = 0;
     double last_relres = 0;
     double last_solve_ms = 0;              // device time of the last fast solve
+    double *d_tabpool = nullptr;  // tables of the fast physics kernels
+    long tabcap = 0, tab_next = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
 };
 
 extern Ctx *g_ctx;
 extern std::string g_err;
 int set_err(int code, const char *fmt, ...);
+// fast physics kernels: reciprocals of n device tables of length len, and
+// the split filter-width tables; slots are reused by the next call (same
+// stream).  tab_reset starts a call.
+void tab_reset(Ctx &c);
+int recip_tabs(Ctx &c, int n, const double *const *src, long len, const double **out);
+int delta_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, const double *dkp,
+               const double **d2, const double **d1);
+int fast_sgs_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, const double *dkp,
+                  const double *dkw, SgsFast &F);
+// the exact (bitwise) or fast build of the physics launchers
+#define LES_PHYS(c, fn) ((c).c.exact ? les_exact::fn : les_fast::fn)
 
 #define LES_CUDA(call)                                                                             \
     do {                                                                                           \

@@ -396,6 +396,7 @@ static void free_ctx(Ctx *c)
     }
     for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->d_tabpool) cudaFree(c->d_tabpool);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1387,8 +1388,12 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v
     for (int q = 0; q < 11; q++)
         if ((r = st.in(mu[q], ml[q], &m[q]))) return r;
     LevelGeom &L = c.lv[1];
-    launch_subgrid(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, dg, dgs, du, dv, dw, dsc, dsv,
-                   dsd, dvd, m, c.stream);
+    SgsFast F;
+    memset(&F, 0, sizeof F);
+    // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
+    if (!c.c.exact && (r = fast_sgs_tabs(c, m[0], m[2], m[10], m[4], m[5], F))) return r;
+    LES_PHYS(c, launch_subgrid)(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, dg, dgs, du, dv,
+                                dw, dsc, dsv, dsd, dvd, m, F, c.stream);
     halo(c, 1, dg);
     halo(c, 1, dgs);
     return st.finish();

@@ -58,6 +58,71 @@ static int wave_range(Ctx &c, int &smin, int &smax)
 
 } // namespace les
 
+namespace les {
+
+void tab_reset(Ctx &c) { c.tab_next = 0; }
+
+static int tab_take(Ctx &c, long len, double **p)
+{
+    if (!c.d_tabpool) {
+        long cap = 24 * c.tot2 + 12 * c.tot1k;
+        if (cudaMalloc(&c.d_tabpool, sizeof(double) * cap) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(LES_ERR_NOMEM, "fast physics tables: %ld doubles", cap);
+        }
+        c.tabcap = cap;
+    }
+    if (c.tab_next + len > c.tabcap) return set_err(LES_ERR_SIZE, "fast physics tables exhausted");
+    *p = c.d_tabpool + c.tab_next;
+    c.tab_next += len;
+    return 0;
+}
+
+int recip_tabs(Ctx &c, int n, const double *const *src, long len, const double **out)
+{
+    double *dst[32];
+    if (n > 32) return set_err(LES_ERR_ARG, "recip_tabs: %d tables", n);
+    int r;
+    for (int t = 0; t < n; t++) {
+        if ((r = tab_take(c, len, &dst[t]))) return r;
+        out[t] = dst[t];
+    }
+    launch_recip(src, dst, n, len, c.stream);
+    return 0;
+}
+
+int delta_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, const double *dkp,
+               const double **d2, const double **d1)
+{
+    double *a, *b;
+    int r;
+    if ((r = tab_take(c, c.tot2, &a)) || (r = tab_take(c, c.tot1k, &b))) return r;
+    launch_delta_tables(dip, djp, rp, c.tot2, dkp, c.tot1k, a, b, c.stream);
+    *d2 = a;
+    *d1 = b;
+    return 0;
+}
+
+int fast_sgs_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, const double *dkp,
+                  const double *dkw, SgsFast &F)
+{
+    tab_reset(c);
+    const double *src2[3] = {dip, djp, rp}, *o2[3], *o1[2];
+    const double *src1[2] = {dkp, dkw};
+    int r;
+    if ((r = recip_tabs(c, 3, src2, c.tot2, o2)) || (r = recip_tabs(c, 2, src1, c.tot1k, o1)) ||
+        (r = delta_tabs(c, dip, djp, rp, dkp, &F.delta2d, &F.delta1d)))
+        return r;
+    F.r_dip = o2[0];
+    F.r_djp = o2[1];
+    F.r_rp = o2[2];
+    F.r_dkp = o1[0];
+    F.r_dkw = o1[1];
+    return 0;
+}
+
+} // namespace les
+
 using namespace les;
 
 extern "C" {
@@ -114,8 +179,19 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
     A.off2_lev1_base = 0;
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
-    launch_set_u_int(L.d_blk, c.g.numbl, L.maxcell, iv, A, k.dtime, c.iststep, k.visc, k.ylaminar, k.kappa,
-                     k.cwfun, c.stream);
+    if (!k.exact) {
+        tab_reset(c);
+        const double *src2[8] = {A.dip, A.diu, A.dix, A.djp, A.dju, A.djv, A.djx, A.rp};
+        const double **dst2[8] = {&A.r_dip, &A.r_diu, &A.r_dix, &A.r_djp, &A.r_dju, &A.r_djv, &A.r_djx, &A.r_rp};
+        const double *src1[2] = {A.dkp, A.dkw};
+        const double *o2[8], *o1[2];
+        if ((r = recip_tabs(c, 8, src2, c.tot2, o2)) || (r = recip_tabs(c, 2, src1, c.tot1k, o1))) return r;
+        for (int q = 0; q < 8; q++) *dst2[q] = o2[q];
+        A.r_dkp = o1[0];
+        A.r_dkw = o1[1];
+    }
+    LES_PHYS(c, launch_set_u_int)(L.d_blk, c.g.numbl, L.maxcell, iv, A, k.dtime, c.iststep, k.visc, k.ylaminar,
+                                  k.kappa, k.cwfun, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, A.u_int, c.d_work, c.stream);
     return st.finish();
 }
@@ -154,8 +230,19 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
     A.off_jk = c.d_offjk;
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
-    launch_set_w_int(L.d_blk, c.g.numbl, L.maxcell, A, k.dtime, c.iststep, k.visc, k.ylaminar, k.kappa, k.cwfun,
-                     c.stream);
+    if (!k.exact) {
+        tab_reset(c);
+        const int qs[5] = {MW_DIU, MW_DJV, MW_RP, MW_DJP, MW_DIP};
+        const double *src2[5], *o2[5], *o1[2];
+        for (int t = 0; t < 5; t++) src2[t] = A.m[qs[t]];
+        const double *src1[2] = {A.dkp, A.dkw};
+        if ((r = recip_tabs(c, 5, src2, c.tot2, o2)) || (r = recip_tabs(c, 2, src1, c.tot1k, o1))) return r;
+        for (int t = 0; t < 5; t++) A.r[qs[t]] = o2[t];
+        A.rdkp = o1[0];
+        A.rdkw = o1[1];
+    }
+    LES_PHYS(c, launch_set_w_int)(L.d_blk, c.g.numbl, L.maxcell, A, k.dtime, c.iststep, k.visc, k.ylaminar,
+                                  k.kappa, k.cwfun, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, A.w_int, c.d_work, c.stream);
     return st.finish();
 }
@@ -217,7 +304,7 @@ int lester_set_virt_bc(const int *iva, const int *ilev, double *f, const double 
     if (iv == 1)
         for (int b = 0; b < nb; b++)
             for (int s = 0; s < 6; s++) c.init_vdd[b][s] = 1;
-    launch_fill(A.vdd, 1.0, c.tot_sg3, c.stream);
+    les_exact::launch_fill(A.vdd, 1.0, c.tot_sg3, c.stream);
     // sides this component treats (set_virt_bc.F:77-135): not its own axis
     const int sides[3][4] = {{3, 4, 5, 6}, {1, 2, 5, 6}, {1, 2, 3, 4}};
     for (int q = 0; q < 4; q++) {
@@ -261,9 +348,9 @@ int lester_set_gamsc1_bc(const double *sc1, double *gamsc1, double *gamlam, cons
         (r = st.io(gamlam, c.tot_sg3, &dl)) || (r = st.in(diu, c.tot2, &ddiu)) || (r = st.in(djv, c.tot2, &ddjv)) ||
         (r = st.in(dkp, c.tot1k, &ddkp)) || (r = st.in(rp, c.tot2, &drp)))
         return r;
-    launch_fill(dl, c.c.visc / 0.72, c.tot_sg3, c.stream);
+    les_exact::launch_fill(dl, c.c.visc / 0.72, c.tot_sg3, c.stream);
     LevelGeom &L = c.lv[1];
-    launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 0, nullptr, dg, dl, ds, ddiu, ddjv, drp, ddkp, c.d_grad,
+    les_exact::launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 0, nullptr, dg, dl, ds, ddiu, ddjv, drp, ddkp, c.d_grad,
                    c.gstride, c.gm, c.stream);
     return st.finish();
 }
@@ -302,7 +389,17 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
     LevelGeom &L = c.lv[1];
     int smin, smax;
     wave_range(c, smin, smax);
-    launch_sc1_waves(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
+    if (!c.c.exact) {
+        tab_reset(c);
+        const double *src2[3] = {A.m[MW_DIU], A.m[MW_DJV], A.m[MW_RP]}, *o2[3], *o1[1];
+        const double *src1[1] = {A.dkp};
+        if ((r = recip_tabs(c, 3, src2, c.tot2, o2)) || (r = recip_tabs(c, 1, src1, c.tot1k, o1))) return r;
+        A.r[MW_DIU] = o2[0];
+        A.r[MW_DJV] = o2[1];
+        A.r[MW_RP] = o2[2];
+        A.rdkp = o1[0];
+    }
+    LES_PHYS(c, launch_sc1_waves)(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, A.sc1, c.d_work, c.stream);
     return st.finish();
 }
@@ -318,7 +415,7 @@ int lester_set_sc1_bc(double *sc1)
     double *d;
     if ((r = st.io(sc1, c.tot_sg3, &d))) return r;
     LevelGeom &L = c.lv[1];
-    launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 1, d, nullptr, nullptr, nullptr, nullptr, nullptr,
+    les_exact::launch_face_bc(L.d_blk, c.g.numbl, c.maxfacecell, 1, d, nullptr, nullptr, nullptr, nullptr, nullptr,
                    nullptr, nullptr, nullptr, 0, 0, c.stream);
     return st.finish();
 }
@@ -346,7 +443,10 @@ int lester_set_sc1var(const double *u, const double *v, const double *w, const d
         (r = st.in(rp, c.tot2, &drp)))
         return r;
     LevelGeom &L = c.lv[1];
-    launch_sc1var(L.d_blk, c.g.numbl, L.maxcell, ds, dv, ddip, ddjp, drp, ddkp, ddkw, c.stream);
+    SgsFast F;
+    memset(&F, 0, sizeof F);
+    if (!c.c.exact && (r = fast_sgs_tabs(c, ddip, ddjp, drp, ddkp, ddkw, F))) return r;
+    LES_PHYS(c, launch_sc1var)(L.d_blk, c.g.numbl, L.maxcell, ds, dv, ddip, ddjp, drp, ddkp, ddkw, F, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, dv, c.d_work, c.stream);
     return st.finish();
 }

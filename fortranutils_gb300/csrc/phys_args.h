@@ -17,6 +17,8 @@ struct UIntArgs {
     double *tw_s, *tw_n, *tw_l, *tw_r;
     const long *off_ki, *off_jk;  // per-block offsets of the (k,i) and (j,k) wall arrays
     long off2_lev1_base;          // 0: level-1 (i,j) arrays start with block 1
+    // fast variant only: reciprocals of the divisor metrics (same layout)
+    const double *r_dip, *r_diu, *r_dix, *r_djp, *r_dju, *r_djv, *r_djx, *r_rp, *r_dkp, *r_dkw;
 };
 
 struct WIntArgs {
@@ -26,6 +28,8 @@ struct WIntArgs {
     double *w_int, *hw;
     double *tw_sfk, *tw_nfk, *tw_wfk, *tw_efk;
     const long *off_ki, *off_jk;
+    const double *r[MW_N];        // fast variant only: reciprocals of m[]
+    const double *rdkp, *rdkw;
 };
 
 struct Sc1Args {
@@ -37,6 +41,15 @@ struct Sc1Args {
     long gstride;
     int gm;
     const int *link;     // bl2bl, 0-based block numbers, 6 per block (-1 none)
+    const double *r[MW_N];  // fast variant only: reciprocals of m[]
+    const double *rdkp;
+};
+
+// eddy viscosity and scalar variance, fast variant only: reciprocals of
+// the divisor metrics and the filter width split as
+// delta2d(i,j) * delta1d(k) = (dip*djp*rp)^0.33333333 * dkp^0.33333333
+struct SgsFast {
+    const double *r_dip, *r_djp, *r_rp, *r_dkp, *r_dkw, *delta2d, *delta1d;
 };
 
 // set_virt_bc arguments: the field, the wall array of the side being

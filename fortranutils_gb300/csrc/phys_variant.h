@@ -1,0 +1,21 @@
+// phys_variant.h -- the two builds of the FP64 physics units.
+//
+// k_phys.cu and k_sgs.cu are compiled twice.  The exact build (namespace
+// les_exact, -fmad=false) keeps the reference's operation order, so every
+// product, sum and quotient rounds as the Fortran FP64 does.  The fast build
+// (namespace les_fast, -DLES_FAST_PHYS, FMA contraction on) multiplies by
+// reciprocal metric tables instead of dividing by the metrics, takes the
+// WALE powers 1.5, 2.5 and 1.25 through sqrt and the filter width from
+// separable tables: each of those changes a result by a few units in the
+// last place, not more, and GB300 issues FP64 slowly enough that the
+// divisions and powers are most of these kernels' time.
+#pragma once
+
+#ifdef LES_FAST_PHYS
+#define LES_PHYS_NS les_fast
+// x / d, with rd = 1 / d precomputed
+#define QDIV(x, d, rd) ((x) * (rd))
+#else
+#define LES_PHYS_NS les_exact
+#define QDIV(x, d, rd) ((x) / (d))
+#endif

@@ -108,6 +108,11 @@ typedef struct lester_ctrl {
     int rb_sweeps;     /* fast solvers: red-black sweeps per smoothing step */
     int rb_coarse;     /* fast solvers: sweeps on the coarsest level */
     double rb_omega;   /* fast solvers: SOR factor */
+    int exact;         /* FP64 physics kernels (predictor, eddy viscosity,
+                          scalar): 1 = the reference's operation order, no
+                          FMA, bitwise reproducible; 0 = fast build
+                          (reciprocal metric tables, FMA, sqrt-based WALE
+                          powers), a few units in the last place apart */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */

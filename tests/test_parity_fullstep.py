@@ -70,9 +70,11 @@ def gpu_steps(st, ctrl, s, nstep, kind="torch"):
         L.gpu_finalize()
 
 
+@pytest.mark.parametrize("exact", [1, 0])
 @pytest.mark.parametrize("name", list(SETUPS))
-def test_steps_reference_solver(name, gpulib):
-    st, ctrl, s = make(name)
+def test_steps_reference_solver(name, exact, gpulib):
+    """Both builds of the FP64 physics kernels against the oracle."""
+    st, ctrl, s = make(name, exact=exact)
     ref = oracle_steps(st, ctrl, s, NSTEP)
     got, rcs = gpu_steps(st, ctrl, s, NSTEP)
     assert rcs == [0] * NSTEP

@@ -30,10 +30,13 @@ def host(t):
     return t.cpu().numpy()
 
 
-@pytest.fixture(params=NAMES)
+@pytest.fixture(params=[(n, e) for e in (1, 0) for n in NAMES],
+                ids=[f"{n}-{'exact' if e else 'fast'}" for e in (1, 0) for n in NAMES])
 def env(request, gpulib):
-    s = cases.Setup(request.param, seed=11)
-    L.gpu_init(s.case.geom(), L.default_ctrl(dtime=0.01, **K))
+    name, exact = request.param
+    s = cases.Setup(name, seed=11)
+    s.exact = exact
+    L.gpu_init(s.case.geom(), L.default_ctrl(dtime=0.01, exact=exact, **K))
     L.gpu_set_iststep(5)
     yield s
     L.gpu_finalize()
@@ -66,8 +69,15 @@ def wall_arrays(s, kind):
             r.uniform(1e-6, 1e-2, n_jk), r.uniform(1e-6, 1e-2, n_jk)]
 
 
-def close(a, b):
-    np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-300)
+def close(a, b, exact=1):
+    """exact build: 1e-13 per element (log/pow may differ in the last bit);
+    fast build: relative L2 1e-12 and 1e-9 per element above a floor."""
+    if exact:
+        np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-300)
+        return
+    scale = np.abs(b).max()
+    assert np.linalg.norm(a - b) <= 1e-12 * max(np.linalg.norm(b), 1e-300)
+    np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-12 * scale)
 
 
 @pytest.mark.parametrize("iva", [1, 2])
@@ -85,10 +95,10 @@ def test_set_uv_int(env, iva):
     md = {k: dev(v) for k, v in s.m.items()}
     L.set_uv_int(iva, dev(a), dev(b), dev(f["w"]), dev(f["p"]), dev(f["rho"]), dev(f["rhonp1"]),
                  dev(f["gam"]), ui, hu, md, dev(s.dkp), dev(s.dkw), *twd)
-    close(host(ui), ui_ref)
-    close(host(hu), hu_ref)
+    close(host(ui), ui_ref, s.exact)
+    close(host(hu), hu_ref, s.exact)
     for q in range(4):
-        close(host(twd[q]), tw_ref[q])
+        close(host(twd[q]), tw_ref[q], s.exact)
 
 
 def test_set_w_int(env):
@@ -104,14 +114,15 @@ def test_set_w_int(env):
     md = {k: dev(v) for k, v in s.m.items()}
     L.set_w_int(dev(f["u"]), dev(f["v"]), dev(f["w"]), dev(f["p"]), dev(f["rho"]),
                 dev(f["rhonp1"]), dev(f["gam"]), wi, hw, md, dev(s.dkp), dev(s.dkw), *twd)
-    close(host(wi), wi_ref)
-    close(host(hw), hw_ref)
+    close(host(wi), wi_ref, s.exact)
+    close(host(hw), hw_ref, s.exact)
     for q in range(4):
-        close(host(twd[q]), tw_ref[q])
+        close(host(twd[q]), tw_ref[q], s.exact)
 
 
-def test_scalar_transport_bitwise(env):
-    """set_gamsc1_bc -> set_sc1 (in-place, hyperplane order) -> set_sc1_bc."""
+def test_scalar_transport(env):
+    """set_gamsc1_bc -> set_sc1 (in-place, hyperplane order) -> set_sc1_bc;
+    bitwise in the exact build."""
     s = env
     c = s.case
     r = s.rng
@@ -137,8 +148,12 @@ def test_scalar_transport_bitwise(env):
     L.set_sc1(dev(u), dev(v), dev(w), None, scd, dev(rho), gd, ld, hsd, md, dev(s.dkp),
               dev(s.dkw))
     L.set_sc1_bc(scd)
-    assert np.array_equal(host(scd), sc_ref)
-    assert np.array_equal(host(hsd), hs_ref)
+    if s.exact:
+        assert np.array_equal(host(scd), sc_ref)
+        assert np.array_equal(host(hsd), hs_ref)
+    else:
+        close(host(scd), sc_ref, 0)
+        close(host(hsd), hs_ref, 0)
 
 
 def test_set_sc1var(env):
@@ -151,4 +166,4 @@ def test_set_sc1var(env):
     md = {k: dev(val) for k, val in s.m.items()}
     L.set_sc1var(None, None, None, dev(sc1), None, d, None, md["dip"], md["djp"], dev(s.dkp),
                  dev(s.dkw), md["rp"])
-    close(host(d), ref)
+    close(host(d), ref, s.exact)
