@@ -39,6 +39,35 @@ struct FaceDev {
                               // 1 = j first, 2 = j last, 4 = k first, 8 = k last
 };
 
+// Push-style halo of the fast solvers: for side s of a block whose first
+// interior plane feeds a ghost plane (periodic or interface link), the
+// ghost cell mirroring a point of that plane with 0-based coordinates c[]
+// is gh + jo * c[a2] + ko * c[a3].  A kernel that updates a point on such a
+// plane writes the new value to its mirror as well, so no separate halo
+// launch is needed; face interiors only, as the 7-point operator reads.
+struct PushDev {
+    long gh, jo, ko;
+    int a2, a3, valid;
+};
+
+template <typename T>
+__device__ __forceinline__ void push_ghosts(const PushDev *__restrict__ pd, const BlkDev &b, int i,
+                                            int j, int k, T val, T *__restrict__ x)
+{
+    const int c[3] = {i - 1, j - 1, k - 1};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (c[d] == 1) {
+            const PushDev &P = pd[2 * d];
+            if (P.valid) x[P.gh + P.jo * c[P.a2] + P.ko * c[P.a3]] = val;
+        }
+        if (c[d] == b.n[d] - 2) {
+            const PushDev &P = pd[2 * d + 1];
+            if (P.valid) x[P.gh + P.jo * c[P.a2] + P.ko * c[P.a3]] = val;
+        }
+    }
+}
+
 // true if in-plane element (j, k) (0-based) of face f is rewritten later by
 // another side of the same block, so this face must leave it alone
 __device__ __forceinline__ bool face_skips(const FaceDev &f, long j, long k)

@@ -94,7 +94,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
                                             const T *__restrict__ R, const T *__restrict__ D,
-                                            T *__restrict__ x, const T *__restrict__ bb)
+                                            T *__restrict__ x, const T *__restrict__ bb,
+                                            const PushDev *__restrict__ push)
 {
     const BlkDev b = blk[blockIdx.y];
     int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
@@ -112,7 +113,9 @@ __global__ void __launch_bounds__(256) k_rb(const BlkDev *__restrict__ blk, int 
     T s = bb[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] + N[p - jo] * x[p - jo] +
           N[p] * x[p + jo] + R[p - ko] * x[p - ko] + R[p] * x[p + ko];
     T xo = x[p];
-    x[p] = xo + omega * (s * D[p] - xo);
+    T xn = xo + omega * (s * D[p] - xo);
+    x[p] = xn;
+    if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, xn, x);
 }
 
 // ---- residual + restriction ------------------------------------------------
@@ -158,7 +161,8 @@ __device__ __forceinline__ int clamp_c(int ic, int n, int lo_int, int hi_int)
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
                                                  const BlkDev *__restrict__ bf_,
-                                                 const T *__restrict__ xc, T *__restrict__ xf)
+                                                 const T *__restrict__ xc, T *__restrict__ xf,
+                                                 const PushDev *__restrict__ push)
 {
     const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -186,7 +190,9 @@ __global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
                 int kk = clamp_c<T>(kc + sz, c.n[2], kl, kr);
                 cr += w[h] * xc[c.off3 + (ii - 1) + joc * (jj - 1) + koc * (kk - 1)];
             }
-    xf[pf] += cr;
+    T v = xf[pf] + cr;
+    xf[pf] = v;
+    if (push) push_ghosts(push + 6 * blockIdx.y, f, i, j, k, v, xf);
 }
 
 // ---- halo for the fast solvers ---------------------------------------------
@@ -221,7 +227,7 @@ __global__ void __launch_bounds__(256) k_resid_outer(
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double v[2] = {0., 0.};
     const double s0 = shift ? *shift : 0.;
-    if (q < b.ncell) {
+    for (; q < b.ncell; q += (long)gridDim.x * blockDim.x) {
         int i, j, k;
         long p = decode_interior(b, q, i, j, k);
         long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
@@ -230,8 +236,8 @@ __global__ void __launch_bounds__(256) k_resid_outer(
                    N[p - jo] * x[p - jo] + N[p] * x[p + jo] + R[p - ko] * x[p - ko] +
                    R[p] * x[p + ko];
         rT[p] = (T)r;
-        v[0] = r * r;
-        v[1] = bp * bp;
+        v[0] += r * r;
+        v[1] += bp * bp;
     }
     block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
 }
@@ -264,9 +270,9 @@ __global__ void __launch_bounds__(256) k_interior_sum(const BlkDev *__restrict__
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double v[1] = {0.};
-    if (q < b.ncell) {
+    for (; q < b.ncell; q += (long)gridDim.x * blockDim.x) {
         int i, j, k;
-        v[0] = bb[decode_interior(b, q, i, j, k)];
+        v[0] += bb[decode_interior(b, q, i, j, k)];
     }
     block_reduce_store<1>(v, partial + blockIdx.y * (long)gridDim.x + blockIdx.x);
 }
@@ -316,14 +322,16 @@ __global__ void k_coarse_mean(const BlkDev *__restrict__ blk, int nb, T *__restr
 // p += e on the interior of level 1
 template <typename T>
 __global__ void k_update(const BlkDev *__restrict__ blk, double *__restrict__ p,
-                         const T *__restrict__ e)
+                         const T *__restrict__ e, const PushDev *__restrict__ push)
 {
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
     int i, j, k;
     long pp = decode_interior(b, q, i, j, k);
-    p[pp] += (double)e[pp];
+    double v = p[pp] + (double)e[pp];
+    p[pp] = v;
+    if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, v, p);
 }
 
 // ================================================================ launchers
@@ -346,9 +354,10 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 // maxhalf = max over blocks of ((ni + 1) / 2) * nj * nk
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
-               const T *N, const T *R, const T *D, T *x, const T *b, cudaStream_t st)
+               const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
+               cudaStream_t st)
 {
-    k_rb<T><<<dim3(nb_(maxhalf, 256), nb), 256, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b);
+    k_rb<T><<<dim3(nb_(maxhalf, 256), nb), 256, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push);
     count_launch(1);
 }
 
@@ -364,9 +373,9 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxc
 
 template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
-                         T *xf, cudaStream_t st)
+                         T *xf, const PushDev *push, cudaStream_t st)
 {
-    k_prolong<T><<<dim3(nb_(maxcell_f, 256), nb), 256, 0, st>>>(bc, bf, xc, xf);
+    k_prolong<T><<<dim3(nb_(maxcell_f, 256), nb), 256, 0, st>>>(bc, bf, xc, xf, push);
     count_launch(1);
 }
 
@@ -385,7 +394,10 @@ void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E
                         const double *R, const double *P, const double *x, const double *b,
                         const double *shift, T *rT, double *partial, double *out2, cudaStream_t st)
 {
+    // grid-stride: a few CTAs per SM, so the final sum reads few partials
     unsigned gx = nb_(maxcell, 256);
+    unsigned cap = (unsigned)((1216 + nb - 1) / nb);
+    if (gx > cap) gx = cap;
     k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, partial);
     k_sum2_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out2);
     count_launch(2);
@@ -395,6 +407,8 @@ void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double 
                           double *partial, double *out, cudaStream_t st)
 {
     unsigned gx = nb_(maxcell, 256);
+    unsigned cap = (unsigned)((1216 + nb - 1) / nb);
+    if (gx > cap) gx = cap;
     k_interior_sum<<<dim3(gx, nb), 256, 0, st>>>(blk, b, partial);
     k_mean_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, ncell, out);
     count_launch(2);
@@ -434,9 +448,10 @@ void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st)
 }
 
 template <typename T>
-void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st)
+void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, const PushDev *push,
+                   cudaStream_t st)
 {
-    k_update<T><<<dim3(nb_(maxcell, 256), nb), 256, 0, st>>>(blk, p, e);
+    k_update<T><<<dim3(nb_(maxcell, 256), nb), 256, 0, st>>>(blk, p, e, push);
     count_launch(1);
 }
 
@@ -445,18 +460,20 @@ void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *
                                      T *, T *, double *, double *, double *, double *, int *,     \
                                      cudaStream_t);                                                \
     template void launch_rb<T>(const BlkDev *, int, long, int, double, const T *, const T *,      \
-                               const T *, const T *, T *, const T *, cudaStream_t);               \
+                               const T *, const T *, T *, const T *, const PushDev *,             \
+                               cudaStream_t);                                                     \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
                                            const T *, const T *, const T *, const T *, const T *, \
                                            T *, cudaStream_t);                                    \
     template void launch_prolong_fast<T>(const BlkDev *, const BlkDev *, int, long, const T *,    \
-                                         T *, cudaStream_t);                                      \
+                                         T *, const PushDev *, cudaStream_t);                     \
     template void launch_halo_fast<T>(const FaceDev *, int, long, T *, cudaStream_t);             \
     template void launch_resid_outer<T>(const BlkDev *, int, long, const double *,                \
                                         const double *, const double *, const double *,           \
                                         const double *, const double *, const double *, T *,      \
                                         double *, double *, cudaStream_t);                        \
-    template void launch_update<T>(const BlkDev *, int, long, double *, const T *, cudaStream_t); \
+    template void launch_update<T>(const BlkDev *, int, long, double *, const T *, const PushDev *, \
+                                   cudaStream_t);                                                \
     template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);
 INST(float)
 INST(double)

@@ -492,24 +492,19 @@ __global__ void k_face_bc(const BlkDev *__restrict__ blk, int mode, double *__re
 }
 
 // one hyperplane i + j + k = s of set_sc1_block (see the header comment)
-__global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk, int s,
-                                                  Sc1Args A_, double dtime)
+// One point of set_sc1_block.F:66-505.  sc1 is read through L2 (__ldcg):
+// in the persistent sweep other CTAs update it between planes.
+#define LDS(x) __ldcg(sc1r + (x))
+__device__ __forceinline__ void sc1_cell(const BlkDev &b, int bi, int i, int j, int k,
+                                         const Sc1Args &A_, double dtime)
 {
-    const BlkDev b = blk[blockIdx.y];
-    int nj_ = b.n[1] - 2, nk_ = b.n[2] - 2;
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= (long)nj_ * nk_) return;
-    int k = (int)(q / nj_) + 2;
-    int j = (int)(q - (long)(k - 2) * nj_) + 2;
-    int i = s - j - k;
-    int nip1 = b.n[0];
-    if (i < 2 || i > nip1 - 1) return;
     const double lambda = 4.0, small = 1.e-30;
+    int nip1 = b.n[0];
     int ni = nip1 - 1, nj = b.n[1] - 1, nk = b.n[2] - 1;
     long io = 1, jo = nip1, ko = (long)nip1 * b.n[1];
     long ijk = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
     long ijkw = ijk - io, ijke = ijk + io, ijks = ijk - jo, ijkn = ijk + jo, ijkl = ijk - ko, ijkr = ijk + ko;
-    double *sc1 = A_.sc1;
+    const double *sc1r = A_.sc1;
     const double *rho = A_.rho, *gs = A_.gamsc1, *gl = A_.gamlam;
     const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
 #define G(a, ii, jj) A_.m[a][IDX2(b, ii, jj)]
@@ -532,38 +527,38 @@ __global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk
 #define GI(a, ii, jj) A_.r[a][IDX2(b, ii, jj)]
     const double *rdkp_ = A_.rdkp + b.off1k;
 #endif
-    double dfdxwf = QDIV(sc1[ijk] - sc1[ijkw], G(MW_DIU, i, j), GI(MW_DIU, i, j));
-    double dfdxef = QDIV(sc1[ijke] - sc1[ijk], G(MW_DIU, i + 1, j), GI(MW_DIU, i + 1, j));
+    double dfdxwf = QDIV(LDS(ijk) - LDS(ijkw), G(MW_DIU, i, j), GI(MW_DIU, i, j));
+    double dfdxef = QDIV(LDS(ijke) - LDS(ijk), G(MW_DIU, i + 1, j), GI(MW_DIU, i + 1, j));
     const long gst = A_.gstride;
     const double *GR = A_.grad;
     int gm = A_.gm;
     double dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
     if (i == 2) dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D) ? dfdxwf
-                          : GR[(long)(A_.link[blockIdx.y * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
-    else dfdxwwf = QDIV(sc1[ijkw] - sc1[ijkw - io], G(MW_DIU, i - 1, j), GI(MW_DIU, i - 1, j));
+                          : GR[(long)(A_.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
+    else dfdxwwf = QDIV(LDS(ijkw) - LDS(ijkw - io), G(MW_DIU, i - 1, j), GI(MW_DIU, i - 1, j));
     if (i == ni) dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D) ? dfdxef
-                           : GR[(long)(A_.link[blockIdx.y * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
-    else dfdxeef = QDIV(sc1[ijke + io] - sc1[ijke], G(MW_DIU, i + 2, j), GI(MW_DIU, i + 2, j));
-    double dfdysf = QDIV(sc1[ijk] - sc1[ijks], G(MW_DJV, i, j), GI(MW_DJV, i, j));
-    double dfdynf = QDIV(sc1[ijkn] - sc1[ijk], G(MW_DJV, i, j + 1), GI(MW_DJV, i, j + 1));
+                           : GR[(long)(A_.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
+    else dfdxeef = QDIV(LDS(ijke + io) - LDS(ijke), G(MW_DIU, i + 2, j), GI(MW_DIU, i + 2, j));
+    double dfdysf = QDIV(LDS(ijk) - LDS(ijks), G(MW_DJV, i, j), GI(MW_DJV, i, j));
+    double dfdynf = QDIV(LDS(ijkn) - LDS(ijk), G(MW_DJV, i, j + 1), GI(MW_DJV, i, j + 1));
     if (j == 2) dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D) ? dfdysf
-                          : GR[(long)(A_.link[blockIdx.y * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
-    else dfdyssf = QDIV(sc1[ijks] - sc1[ijks - jo], G(MW_DJV, i, j - 1), GI(MW_DJV, i, j - 1));
+                          : GR[(long)(A_.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
+    else dfdyssf = QDIV(LDS(ijks) - LDS(ijks - jo), G(MW_DJV, i, j - 1), GI(MW_DJV, i, j - 1));
     if (j == nj) dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D) ? dfdynf
-                           : GR[(long)(A_.link[blockIdx.y * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
-    else dfdynnf = QDIV(sc1[ijkn + jo] - sc1[ijkn], G(MW_DJV, i, j + 2), GI(MW_DJV, i, j + 2));
+                           : GR[(long)(A_.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
+    else dfdynnf = QDIV(LDS(ijkn + jo) - LDS(ijkn), G(MW_DJV, i, j + 2), GI(MW_DJV, i, j + 2));
     double rpij = G(MW_RP, i, j);
 #ifdef LES_FAST_PHYS
     const double rrpij = GI(MW_RP, i, j);
 #endif
-    double dfdzlf = QDIV(sc1[ijk] - sc1[ijkl], (rpij * dkp[k - 2]), rrpij * rdkp_[k - 2]);
-    double dfdzrf = QDIV(sc1[ijkr] - sc1[ijk], (rpij * dkp[k - 1]), rrpij * rdkp_[k - 1]);
+    double dfdzlf = QDIV(LDS(ijk) - LDS(ijkl), (rpij * dkp[k - 2]), rrpij * rdkp_[k - 2]);
+    double dfdzrf = QDIV(LDS(ijkr) - LDS(ijk), (rpij * dkp[k - 1]), rrpij * rdkp_[k - 1]);
     if (k == 2) dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D) ? dfdzlf
-                          : GR[(long)(A_.link[blockIdx.y * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
-    else dfdzllf = QDIV(sc1[ijkl] - sc1[ijkl - ko], (rpij * dkp[k - 3]), rrpij * rdkp_[k - 3]);
+                          : GR[(long)(A_.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
+    else dfdzllf = QDIV(LDS(ijkl) - LDS(ijkl - ko), (rpij * dkp[k - 3]), rrpij * rdkp_[k - 3]);
     if (k == nk) dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D) ? dfdzrf
-                           : GR[(long)(A_.link[blockIdx.y * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
-    else dfdzrrf = QDIV(sc1[ijkr + ko] - sc1[ijkr], (rpij * dkp[k]), rrpij * rdkp_[k]);
+                           : GR[(long)(A_.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
+    else dfdzrrf = QDIV(LDS(ijkr + ko) - LDS(ijkr), (rpij * dkp[k]), rrpij * rdkp_[k]);
     double rwst = (uwf >= 0.0) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
     double rest = (uef > 0.0) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
     double rsth = (vsf >= 0.0) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
@@ -576,26 +571,26 @@ __global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk
     double limn = fmax(0.0, fmin(lambda * rnth, 1.0));
     double liml = fmax(0.0, fmin(lambda * rlft, 1.0));
     double limr = fmax(0.0, fmin(lambda * rrht, 1.0));
-    double s0 = sc1[ijk];
+    double s0 = LDS(ijk);
     double fwf, fef, fsf, fnf, flf, frf;
-    if (uwf > 0.0) fwf = sc1[ijkw] + 0.5 * limw * (s0 - sc1[ijkw]);
-    else if (uwf < 0.0) fwf = s0 + 0.5 * limw * (sc1[ijkw] - s0);
-    else fwf = 0.5 * (s0 + sc1[ijkw]);
-    if (uef > 0.0) fef = s0 + 0.5 * lime * (sc1[ijke] - s0);
-    else if (uef < 0.0) fef = sc1[ijke] + 0.5 * lime * (s0 - sc1[ijke]);
-    else fef = 0.5 * (s0 + sc1[ijke]);
-    if (vsf > 0.0) fsf = sc1[ijks] + 0.5 * lims * (s0 - sc1[ijks]);
-    else if (vsf < 0.0) fsf = s0 + 0.5 * lims * (sc1[ijks] - s0);
-    else fsf = 0.5 * (s0 + sc1[ijks]);
-    if (vnf > 0.0) fnf = s0 + 0.5 * limn * (sc1[ijkn] - s0);
-    else if (vnf < 0.0) fnf = sc1[ijkn] + 0.5 * limn * (s0 - sc1[ijkn]);
-    else fnf = 0.5 * (s0 + sc1[ijkn]);
-    if (wlf > 0.0) flf = sc1[ijkl] + 0.5 * liml * (s0 - sc1[ijkl]);
-    else if (wlf < 0.0) flf = s0 + 0.5 * liml * (sc1[ijkl] - s0);
-    else flf = 0.5 * (s0 + sc1[ijkl]);
-    if (wrf > 0.0) frf = s0 + 0.5 * limr * (sc1[ijkr] - s0);
-    else if (wrf < 0.0) frf = sc1[ijkr] + 0.5 * limr * (s0 - sc1[ijkr]);
-    else frf = 0.5 * (s0 + sc1[ijkr]);
+    if (uwf > 0.0) fwf = LDS(ijkw) + 0.5 * limw * (s0 - LDS(ijkw));
+    else if (uwf < 0.0) fwf = s0 + 0.5 * limw * (LDS(ijkw) - s0);
+    else fwf = 0.5 * (s0 + LDS(ijkw));
+    if (uef > 0.0) fef = s0 + 0.5 * lime * (LDS(ijke) - s0);
+    else if (uef < 0.0) fef = LDS(ijke) + 0.5 * lime * (s0 - LDS(ijke));
+    else fef = 0.5 * (s0 + LDS(ijke));
+    if (vsf > 0.0) fsf = LDS(ijks) + 0.5 * lims * (s0 - LDS(ijks));
+    else if (vsf < 0.0) fsf = s0 + 0.5 * lims * (LDS(ijks) - s0);
+    else fsf = 0.5 * (s0 + LDS(ijks));
+    if (vnf > 0.0) fnf = s0 + 0.5 * limn * (LDS(ijkn) - s0);
+    else if (vnf < 0.0) fnf = LDS(ijkn) + 0.5 * limn * (s0 - LDS(ijkn));
+    else fnf = 0.5 * (s0 + LDS(ijkn));
+    if (wlf > 0.0) flf = LDS(ijkl) + 0.5 * liml * (s0 - LDS(ijkl));
+    else if (wlf < 0.0) flf = s0 + 0.5 * liml * (LDS(ijkl) - s0);
+    else flf = 0.5 * (s0 + LDS(ijkl));
+    if (wrf > 0.0) frf = s0 + 0.5 * limr * (LDS(ijkr) - s0);
+    else if (wrf < 0.0) frf = LDS(ijkr) + 0.5 * limr * (s0 - LDS(ijkr));
+    else frf = 0.5 * (s0 + LDS(ijkr));
     double areawf = G(MW_RDJU, i, j) * dkw[k - 1];
     double areaef = G(MW_RDJU, i + 1, j) * dkw[k - 1];
     double areasf = G(MW_RDIV, i, j) * dkw[k - 1];
@@ -621,11 +616,207 @@ __global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk
     A_.hsc1[ijk] = h;
     if (tmp < 0.0) tmp = 0.0;
     if (tmp > 1.0) tmp = 1.0;
-    sc1[ijk] = tmp;
+    A_.sc1[ijk] = tmp;
 #undef G
 #ifdef GI
 #undef GI
 #endif
+}
+#undef LDS
+
+__global__ void __launch_bounds__(128) k_sc1_wave(const BlkDev *__restrict__ blk, int s,
+                                                  Sc1Args A_, double dtime)
+{
+    const BlkDev b = blk[blockIdx.y];
+    int nj_ = b.n[1] - 2, nk_ = b.n[2] - 2;
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= (long)nj_ * nk_) return;
+    int k = (int)(q / nj_) + 2;
+    int j = (int)(q - (long)(k - 2) * nj_) + 2;
+    int i = s - j - k;
+    if (i < 2 || i > b.n[0] - 1) return;
+    sc1_cell(b, blockIdx.y, i, j, k, A_, dtime);
+}
+
+// Bounded grid barrier of the persistent sweep.  All CTAs of a cooperative
+// launch are resident, so every arrival happens; the wait is still capped
+// (limit polls, then err = 1 and every CTA leaves at its next barrier).
+__device__ __forceinline__ bool wave_barrier(WaveSync *ws, unsigned nblk, unsigned target, long limit)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        __threadfence();
+        unsigned arrived = atomicAdd(&ws->count, 1u) + 1u;
+        if (arrived == nblk * target) {
+            __threadfence();
+            atomicExch(&ws->gen, target);
+        } else {
+            long it = 0;
+            while (true) {
+                unsigned g = *(volatile unsigned *)&ws->gen;
+                if (g >= target) break;
+                if (*(volatile int *)&ws->err) {
+                    ok = 0;
+                    break;
+                }
+                if (++it > limit) {
+                    atomicExch(&ws->err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// One face of point (i, j, k) in set_sc1_block.F:66-505: axis d (0 x, 1 y,
+// 2 z), hi = 0 for the low (W, S, L) face, 1 for the high (E, N, R) face.
+// Every face runs the same code with axis-dependent indices, so the six
+// faces of a point can go to six lanes without divergence.  Returns the
+// convective flux g (rho u f area) and the diffusive flux t (gam area
+// grad), with the reference's operands and order for each.
+__device__ __forceinline__ void sc1_face(const BlkDev &b, int bi, int i, int j, int k, int d, int hi,
+                                         const Sc1Args &A_, double &gout, double &tout)
+{
+    const double lambda = 4.0, small = 1.e-30;
+    const double *sc1r = A_.sc1;
+    const double *rho = A_.rho, *gs = A_.gamsc1, *gl = A_.gamlam;
+    const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
+#ifdef LES_FAST_PHYS
+    const double *rdkp_ = A_.rdkp + b.off1k;
+#endif
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long ijk = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    const long sd = d == 0 ? 1 : d == 1 ? jo : ko;
+    const int h = (d == 0 ? i : d == 1 ? j : k) + hi;  // high-side point of this face along d
+    const int nd = d == 0 ? b.n[0] : d == 1 ? b.n[1] : b.n[2];
+    const long ph = ijk + (hi ? sd : 0);
+    const long pl = ph - sd;
+    const long pn = hi ? ph : pl;          // the neighbour across the face
+    // gradient across the face whose high-side point is hh (index phh)
+    auto grad = [&](int hh, long phh) -> double {
+        double df = __ldcg(sc1r + phh) - __ldcg(sc1r + phh - sd);
+        if (d == 0) return QDIV(df, A_.m[MW_DIU][IDX2(b, hh, j)], A_.r[MW_DIU][IDX2(b, hh, j)]);
+        if (d == 1) return QDIV(df, A_.m[MW_DJV][IDX2(b, i, hh)], A_.r[MW_DJV][IDX2(b, i, hh)]);
+        return QDIV(df, (A_.m[MW_RP][IDX2(b, i, j)] * dkp[hh - 2]),
+                    A_.r[MW_RP][IDX2(b, i, j)] * rdkp_[hh - 2]);
+    };
+    // interface gradient of the linked block (set_gamsc1_bc planes)
+    auto igrad = [&](int side) -> double {
+        long t = (d == 0) ? (j - 1) + (long)A_.gm * (k - 1)
+                          : (d == 1) ? (i - 1) + (long)A_.gm * (k - 1) : (i - 1) + (long)A_.gm * (j - 1);
+        return A_.grad[(long)A_.link[bi * 6 + side] * 6 * A_.gstride + (side ^ 1) * A_.gstride + t];
+    };
+    const double g0 = grad(h, ph);
+    double gm, gp;
+    if (h == 2) gm = (b.bc[2 * d] != LES_BCT_INTERFACE_D) ? g0 : igrad(2 * d);
+    else gm = grad(h - 1, ph - sd);
+    if (h == nd) gp = (b.bc[2 * d + 1] != LES_BCT_INTERFACE_D) ? g0 : igrad(2 * d + 1);
+    else gp = grad(h + 1, ph + sd);
+    const double *vel = d == 0 ? A_.u : d == 1 ? A_.v : A_.w;
+    const double vf = vel[ph];
+    // low faces test vel >= 0, high faces vel > 0 (the reference's rwst/rest)
+    const bool up = hi ? (vf > 0.0) : (vf >= 0.0);
+    const double r = up ? (gm + small) / (g0 + small) : (gp + small) / (g0 + small);
+    const double lim = fmax(0.0, fmin(lambda * r, 1.0));
+    const double s0 = __ldcg(sc1r + ijk), pa = __ldcg(sc1r + pl), pc = __ldcg(sc1r + ph);
+    const double other = __ldcg(sc1r + pn);
+    double f;
+    if (vf > 0.0) f = pa + 0.5 * lim * (pc - pa);
+    else if (vf < 0.0) f = pc + 0.5 * lim * (pa - pc);
+    else f = 0.5 * (s0 + other);
+    const double rhof = 0.5 * (rho[ijk] + rho[pn]);
+    const double gamf = 0.5 * (gs[ijk] + gs[pn]) * rhof + 0.5 * (gl[ijk] + gl[pn]);
+    double area;
+    if (d == 0) area = A_.m[MW_RDJU][IDX2(b, h, j)] * dkw[k - 1];
+    else if (d == 1) area = A_.m[MW_RDIV][IDX2(b, i, h)] * dkw[k - 1];
+    else area = A_.m[MW_DIDJP][IDX2(b, i, j)];
+    gout = rhof * vf * f * area;
+    tout = gamf * area * g0;
+}
+
+// The whole in-place sweep in one cooperative launch.  Plane s holds the
+// points with i + j + k = s; cum[s - smin][q] counts them over the (block,
+// k) slices before q, so the points of a plane are enumerated densely.  A
+// CTA takes 32 points at a time: warp w < 6 computes face w (W E S N L R) of
+// all 32, warp 6 loads the point data, then combines the six faces in the
+// reference's order and updates the points.  Every FP64 instruction thus
+// runs with full warps (the FP64 pipe costs the same per warp instruction
+// whatever the active mask).  A bounded grid barrier separates the planes.
+// Results equal k_sc1_wave's.
+__global__ void __launch_bounds__(256) k_sc1_sweep(const BlkDev *__restrict__ blk,
+                                                   const int *__restrict__ cum,
+                                                   const int2 *__restrict__ slice, int nslice,
+                                                   int smin, int smax, Sc1Args A_, double dtime,
+                                                   WaveSync *ws, long limit)
+{
+    extern __shared__ int scum[];
+    __shared__ double fg[6][32], ft[6][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int s = smin; s <= smax; s++) {
+        const int *row = cum + (long)(s - smin) * (nslice + 1);
+        for (int q = threadIdx.x; q <= nslice; q += blockDim.x) scum[q] = row[q];
+        __syncthreads();
+        const int ncell = scum[nslice];
+        for (long tb = (long)blockIdx.x * 32; tb < ncell; tb += (long)gridDim.x * 32) {
+            const long t = tb + lane;
+            const bool valid = t < ncell;
+            int bi = 0, i = 0, j = 0, k = 0;
+            if (valid) {
+                int lo = 0, hi = nslice;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (scum[mid] <= t) lo = mid;
+                    else hi = mid;
+                }
+                const int2 sl = slice[lo];
+                bi = sl.x;
+                k = sl.y;
+                int jlo = s - k - (blk[bi].n[0] - 1);
+                if (jlo < 2) jlo = 2;
+                j = jlo + (int)(t - scum[lo]);
+                i = s - j - k;
+            }
+            double s0 = 0., hold = 0., vr = 0.;
+            long ijk = 0;
+            if (w < 6) {
+                if (valid) {
+                    double gf, tf;
+                    sc1_face(blk[bi], bi, i, j, k, w >> 1, w & 1, A_, gf, tf);
+                    fg[w][lane] = gf;
+                    ft[w][lane] = tf;
+                }
+            } else if (w == 6 && valid) {
+                const BlkDev &b = blk[bi];
+                ijk = b.off3 + (i - 1) + (long)b.n[0] * (j - 1) + (long)b.n[0] * b.n[1] * (k - 1);
+                double vol = A_.m[MW_RDIDJP][IDX2(b, i, j)] * A_.dkw[b.off1k + k - 1];
+                vr = dtime / (vol * A_.rho[ijk]);
+                s0 = __ldcg(A_.sc1 + ijk);
+                hold = A_.hsc1[ijk];
+            }
+            __syncthreads();
+            if (w == 6 && valid) {
+                double convf = -(fg[1][lane] - fg[0][lane]) - (fg[3][lane] - fg[2][lane]) -
+                               (fg[5][lane] - fg[4][lane]);
+                double difff = (ft[1][lane] - ft[0][lane]) + (ft[3][lane] - ft[2][lane]) +
+                               (ft[5][lane] - ft[4][lane]);
+                double hh = convf + difff;
+                double tmp = s0 + vr * (1.5 * hh - 0.5 * hold);
+                A_.hsc1[ijk] = hh;
+                if (tmp < 0.0) tmp = 0.0;
+                if (tmp > 1.0) tmp = 1.0;
+                A_.sc1[ijk] = tmp;
+            }
+            __syncthreads();
+        }
+        if (!wave_barrier(ws, gridDim.x, (unsigned)(s - smin + 1), limit)) return;
+    }
 }
 
 // code/set_sc1var_block.F:26-66
@@ -705,6 +896,30 @@ void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax,
     unsigned gx = nbk(maxjk, 128);
     for (int s = smin; s <= smax; s++) k_sc1_wave<<<dim3(gx, nb), 128, 0, st>>>(blk, s, a, dtime);
     les::count_launch(smax - smin + 1);
+}
+
+int sc1_sweep_max_ctas(int smem)
+{
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sc1_sweep, 256, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nsm * per;
+}
+
+cudaError_t launch_sc1_sweep(const BlkDev *blk, const int *cum, const int2 *slice, int nslice, int nctas,
+                             int smin, int smax, const Sc1Args &a, double dtime, WaveSync *ws, long limit,
+                             cudaStream_t st)
+{
+    Sc1Args A = a;
+    void *args[] = {(void *)&blk, (void *)&cum, (void *)&slice, (void *)&nslice, (void *)&smin,
+                    (void *)&smax, (void *)&A, (void *)&dtime, (void *)&ws, (void *)&limit};
+    size_t smem = sizeof(int) * (nslice + 1);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_sc1_sweep, dim3(nctas), dim3(256), args, smem, st);
+    les::count_launch(1);
+    return e;
 }
 
 void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,

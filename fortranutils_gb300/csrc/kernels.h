@@ -66,14 +66,15 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
                      cudaStream_t st);
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
-               const T *N, const T *R, const T *D, T *x, const T *b, cudaStream_t st);
+               const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
+               cudaStream_t st);
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
                            cudaStream_t st);
 template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
-                         T *xf, cudaStream_t st);
+                         T *xf, const PushDev *push, cudaStream_t st);
 template <typename T>
 void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
 template <typename T>
@@ -83,7 +84,8 @@ void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E
 void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
                           double *partial, double *out, cudaStream_t st);
 template <typename T>
-void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, cudaStream_t st);
+void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, const PushDev *push,
+                   cudaStream_t st);
 template <typename T>
 void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st);
 
@@ -117,6 +119,10 @@ void launch_delta_tables(const double *dip, const double *djp, const double *rp,
                         cudaStream_t st);                                                           \
     void launch_sc1_waves(const BlkDev *blk, int nb, long maxjk, int smin, int smax,                \
                           const Sc1Args &a, double dtime, cudaStream_t st);                         \
+    int sc1_sweep_max_ctas(int smem);                                                               \
+    cudaError_t launch_sc1_sweep(const BlkDev *blk, const int *cum, const int2 *slice, int nslice,  \
+                                 int nctas, int smin, int smax, const Sc1Args &a, double dtime,     \
+                                 WaveSync *ws, long limit, cudaStream_t st);                        \
     void launch_sc1var(const BlkDev *blk, int nb, long maxcell, const double *sc1, double *sc1var,  \
                        const double *dip, const double *djp, const double *rp, const double *dkp,   \
                        const double *dkw, const SgsFast &f, cudaStream_t st);                       \

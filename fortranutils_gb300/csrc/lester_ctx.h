@@ -20,6 +20,10 @@ struct LevelGeom {
     double npts_all;       // interior points, pressure loop bounds (set_loop_bound.F:364)
     BlkDev *d_blk = nullptr;
     FaceDev *d_face = nullptr;
+    PushDev *d_push = nullptr;  // 6 per block: ghost mirrors of the interior planes
+    // red-black sweeps may push: on every face the point a ghost mirrors and
+    // the point that reads that ghost have different colours
+    bool rb_push = true;
     int nface = 0;
     long worklen = 0;
     void *d_metblk = nullptr;
@@ -104,7 +108,14 @@ struct Ctx {
     int last_cycles = 0;
     double last_relres = 0;
     double last_solve_ms = 0;              // device time of the last fast solve
+    bool want_norms = true;  // fast solves end with the reference-style norms and residu
     double *d_tabpool = nullptr;  // tables of the fast physics kernels
+    // persistent scalar sweep: per plane, cumulative point counts over the
+    // (block, k) slices; the slices; the grid barrier
+    int *d_wcum = nullptr;
+    int2 *d_wslice = nullptr;
+    int nslice = 0;
+    WaveSync *d_wave = nullptr;
     long tabcap = 0, tab_next = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
 };

@@ -225,6 +225,8 @@ static int build_faces(Ctx &c)
     for (int lev = 1; lev <= c.nummgl; lev++) {
         LevelGeom &L = c.lv[lev];
         std::vector<FaceDev> fv;
+        std::vector<PushDev> pv((size_t)nb * 6);
+        for (auto &P : pv) P = PushDev{0, 0, 0, 0, 0, 0};
         long slot[LES_MAXBL + 1][6];
         long w = 0;
         // own pack-plane descriptors first (one slot per face)
@@ -281,9 +283,27 @@ static int build_faces(Ctx &c)
                 if (2 * d3 > s && per_int(g.bl_bc[b - 1][2 * d3 - 1])) skip |= 8;
                 f.skip = skip;
                 fv.push_back(f);
+                // the partner's plane (bn, sn) feeds this ghost plane; the
+                // reader of a ghost (1-based normal coordinate 2 or n-1) and
+                // the point it mirrors must differ in colour for a push
+                // from a red-black sweep to equal a halo copy after it
+                {
+                    int rn = (s % 2 == 0) ? n[d1 - 1] - 1 : 2;
+                    int mn = (sn % 2 == 0) ? m[dn1 - 1] - 1 : 2;
+                    if ((rn + mn) % 2 == 0) L.rb_push = false;
+                }
+                PushDev &P = pv[(bn - 1) * 6 + (sn - 1)];
+                P.gh = f.gh;
+                P.jo = f.jo;
+                P.ko = f.ko;
+                P.a2 = dn2 - 1;
+                P.a3 = dn3 - 1;
+                P.valid = 1;
                 L.maxface = std::max(L.maxface, (long)f.nj * f.nk);
             }
         L.nface = (int)fv.size();
+        LES_CUDA(cudaMalloc(&L.d_push, sizeof(PushDev) * pv.size()));
+        LES_CUDA(cudaMemcpy(L.d_push, pv.data(), sizeof(PushDev) * pv.size(), cudaMemcpyHostToDevice));
         L.worklen = w;
         maxwork = std::max(maxwork, w);
         if (L.nface) {
@@ -368,6 +388,7 @@ static void free_ctx(Ctx *c)
         LevelGeom &L = c->lv[lev];
         cudaFree(L.d_blk);
         cudaFree(L.d_face);
+        cudaFree(L.d_push);
         cudaFree(L.d_metblk);
         for (int s = 0; s < 6; s++) cudaFree(L.d_metface[s]);
     }
@@ -397,6 +418,9 @@ static void free_ctx(Ctx *c)
     for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->d_tabpool) cudaFree(c->d_tabpool);
+    cudaFree(c->d_wcum);
+    cudaFree(c->d_wslice);
+    cudaFree(c->d_wave);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -630,9 +654,9 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
-                         F.b, c.stream);
+                         F.b, L.rb_push ? L.d_push : nullptr, c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
-            launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
+            if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
 }
 
@@ -656,8 +680,7 @@ template <typename T> static void fast_vcycle(Ctx &c)
     fast_smooth<T>(c, L, L == 1 ? pre : crs);
     for (int lev = L - 1; lev >= 1; lev--) {
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
-        launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxcell, F.x, F.x, c.stream);
-        launch_halo_fast<T>(Lf.d_face, Lf.nface, Lf.maxface, F.x, c.stream);
+        launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxcell, F.x, F.x, Lf.d_push, c.stream);
         fast_smooth<T>(c, lev, pre);
     }
 }
@@ -696,8 +719,7 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
     cudaError_t mid = cudaSuccess;
     if (e == cudaSuccess) {
         fast_vcycle<T>(c);
-        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, c.stream);
-        launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
         launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
                               c.singular ? c.d_small + 8 : nullptr, F.b, c.d_partial, c.d_small,
                               c.stream);
@@ -795,12 +817,20 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
         LES_CUDA(cudaEventElapsedTime(&ms, c.ev_solve[0], c.ev_solve[1]));
         c.last_solve_ms = ms;
     }
-    // reference-style norms and level-1 residual for the caller
-    double n4[4];
-    if ((r = norms_level(c, 1, A, f, b, residu, n4))) return r;
-    STAGE_CHECK("final norms");
+    // reference-style norms and level-1 residual for the caller (lester_step,
+    // which reads neither, skips them)
+    if (c.want_norms) {
+        double n4[4];
+        if ((r = norms_level(c, 1, A, f, b, residu, n4))) return r;
+        STAGE_CHECK("final norms");
+        for (int q = 0; q < 4; q++) c.last_norms[q] = n4[q];
+    } else {
+        double rn = 1.0 / c.lv[1].npts_all;
+        c.last_norms[0] = std::sqrt(r2 * rn);
+        c.last_norms[1] = std::sqrt(b2 * rn);
+        c.last_norms[2] = c.last_norms[3] = 0.;
+    }
 #undef STAGE_CHECK
-    for (int q = 0; q < 4; q++) c.last_norms[q] = n4[q];
     if (rel > rtol && b2 > 0)
         return set_err(LES_ERR_NOT_CONVERGED, "relative residual %.3e after %d cycles", rel, it);
     return 0;

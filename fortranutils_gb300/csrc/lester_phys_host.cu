@@ -45,6 +45,30 @@ static int ensure_phys_tables(Ctx &c)
     long l1 = 0;
     for (int b = 1; b <= nb; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
     c.tot2_l1 = l1;
+    // planes i + j + k = s of the in-place scalar sweep
+    std::vector<int2> sl;
+    for (int b = 1; b <= nb; b++)
+        for (int k = 2; k <= c.lv[1].n[b][2] - 1; k++) sl.push_back(make_int2(b - 1, k));
+    int smin = 6, smax = 0;
+    for (int b = 1; b <= nb; b++) smax = std::max(smax, c.lv[1].n[b][0] + c.lv[1].n[b][1] + c.lv[1].n[b][2] - 3);
+    int ns = (int)sl.size();
+    std::vector<int> cum((size_t)(smax - smin + 1) * (ns + 1));
+    for (int sp = smin; sp <= smax; sp++) {
+        int *row = &cum[(size_t)(sp - smin) * (ns + 1)];
+        row[0] = 0;
+        for (int q = 0; q < ns; q++) {
+            const int *n = c.lv[1].n[sl[q].x + 1];
+            int k = sl[q].y, ni = n[0] - 1, nj = n[1] - 1;
+            int jlo = std::max(2, sp - k - ni), jhi = std::min(nj, sp - k - 2);
+            row[q + 1] = row[q] + std::max(0, jhi - jlo + 1);
+        }
+    }
+    c.nslice = ns;
+    LES_CUDA(cudaMalloc(&c.d_wslice, sizeof(int2) * ns));
+    LES_CUDA(cudaMemcpy(c.d_wslice, sl.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMalloc(&c.d_wcum, sizeof(int) * cum.size()));
+    LES_CUDA(cudaMemcpy(c.d_wcum, cum.data(), sizeof(int) * cum.size(), cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMalloc(&c.d_wave, sizeof(WaveSync)));
     return 0;
 }
 
@@ -399,7 +423,21 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
         A.r[MW_RP] = o2[2];
         A.rdkp = o1[0];
     }
-    LES_PHYS(c, launch_sc1_waves)(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
+    // the whole sweep as one cooperative launch with a grid barrier per
+    // plane; per-plane launches where the device cannot co-schedule it
+    int smem = (int)sizeof(int) * (c.nslice + 1);
+    int maxctas = smem <= 48 * 1024 ? LES_PHYS(c, sc1_sweep_max_ctas)(smem) : 0;
+    if (maxctas > 0) {
+        LES_CUDA(cudaMemsetAsync(c.d_wave, 0, sizeof(WaveSync), c.stream));
+        LES_CUDA(LES_PHYS(c, launch_sc1_sweep)(L.d_blk, c.d_wcum, c.d_wslice, c.nslice, maxctas, smin, smax, A,
+                                               c.c.dtime, c.d_wave, 1L << 24, c.stream));
+        int err = 0;
+        LES_CUDA(cudaMemcpyAsync(&err, &c.d_wave->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        LES_CUDA(cudaStreamSynchronize(c.stream));
+        if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: grid barrier of the scalar sweep timed out");
+    } else {
+        LES_PHYS(c, launch_sc1_waves)(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
+    }
     launch_halo(L.d_face, L.nface, L.maxface, A.sc1, c.d_work, c.stream);
     return st.finish();
 }

@@ -193,7 +193,9 @@ int lester_step(lester_fields *F, const int *istep)
                            D.ae, D.as, D.an, D.al, D.ar));
     RET(lester_sour_p(m[M_DIU], m[M_DJV], m[M_RDIV], m[M_RDJU], m[M_DIDJP], D.dkp, m[M_RDIDJP], D.dkw, D.u_int,
                       D.v_int, D.w_int, D.rho, D.rhonp1, D.drhonp1dt, D.s, D.srhot, D.srhoux, nullptr, nullptr));
+    c.want_norms = false;
     int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
+    c.want_norms = true;
     // the reference carries on after nummgits cycles whatever the residual;
     // a fast solver that stops short reports it and the step continues
     if (rs && rs != LES_ERR_NOT_CONVERGED) return rs;

@@ -45,6 +45,13 @@ struct Sc1Args {
     const double *rdkp;
 };
 
+// grid barrier state of the persistent scalar sweep (zeroed before each
+// launch): arrivals, the last completed barrier, and the timeout flag
+struct WaveSync {
+    unsigned count, gen;
+    int err, pad;
+};
+
 // eddy viscosity and scalar variance, fast variant only: reciprocals of
 // the divisor metrics and the filter width split as
 // delta2d(i,j) * delta1d(k) = (dip*djp*rp)^0.33333333 * dkp^0.33333333
