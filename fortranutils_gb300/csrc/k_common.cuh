@@ -39,6 +39,13 @@ struct FaceDev {
                               // 1 = j first, 2 = j last, 4 = k first, 8 = k last
 };
 
+// separable factors of the fast-solver coefficients (k_fast.cu): coupling
+// E(i,j,k) = E2(i,j) Ez(k), likewise N and R; 2-D tables in the metric
+// layout (b.off2), 1-D in the k layout (b.off1k).  E2 == nullptr: unused.
+template <typename T> struct MfTab {
+    T *E2 = nullptr, *N2 = nullptr, *R2 = nullptr, *Ez = nullptr, *Nz = nullptr, *Rz = nullptr;
+};
+
 // Push-style halo of the fast solvers: for side s of a block whose first
 // interior plane feeds a ghost plane (periodic or interface link), the
 // ghost cell mirroring a point of that plane with 0-based coordinates c[]
@@ -68,6 +75,15 @@ __device__ __forceinline__ void push_ghosts(const PushDev *__restrict__ pd, cons
     }
 }
 
+// one multigrid level of the fast solvers, for kernels that walk levels
+struct VLev {
+    const BlkDev *blk;     // block table of the level (device)
+    const PushDev *push;   // ghost mirrors, 6 per block
+    const FaceDev *face;   // periodic / interface face copies
+    int nface;
+    int rb_push;           // red-black sweeps push (else copy the faces after each)
+};
+
 // true if in-plane element (j, k) (0-based) of face f is rewritten later by
 // another side of the same block, so this face must leave it alone
 __device__ __forceinline__ bool face_skips(const FaceDev &f, long j, long k)
@@ -82,13 +98,15 @@ __device__ __forceinline__ bool is_per_or_int(int bc)
 }
 
 // interior point number q -> (i, j, k) 1-based and 0-based field index
+// (a block's interior count is below 2^31, checked at init, so the decode
+// uses 32-bit divisions: a 64-bit division is a long emulated sequence)
 __device__ __forceinline__ long decode_interior(const BlkDev &b, long q, int &i,
                                                 int &j, int &k)
 {
-    int ni = b.n[0] - 2, nj = b.n[1] - 2;
-    long t = q / ni;
-    i = (int)(q - t * ni) + 2;
-    long t2 = t / nj;
+    const unsigned ni = (unsigned)(b.n[0] - 2), nj = (unsigned)(b.n[1] - 2), uq = (unsigned)q;
+    const unsigned t = uq / ni;
+    i = (int)(uq - t * ni) + 2;
+    const unsigned t2 = t / nj;
     j = (int)(t - t2 * nj) + 2;
     k = (int)t2 + 2;
     return b.off3 + (i - 1) + (long)b.n[0] * ((j - 1) + (long)b.n[1] * (k - 1));

@@ -24,6 +24,7 @@ template <typename T> struct Lvl {
     T *E, *N, *R, *D;
 };
 
+
 // ---- coefficient conversion (once per coefficient set) --------------------
 template <typename T>
 __global__ void k_conv_coef(const BlkDev *__restrict__ blk, const double *__restrict__ ap,
@@ -88,50 +89,152 @@ __global__ void k_delta_tables(const double *__restrict__ dip, const double *__r
     }
 }
 
+// ---- separable (matrix-free) coefficients ---------------------------------
+// coeff_p's couplings factor into a 2-D (i, j) part and a 1-D k part
+// (code/coeff_p_block.F: ae = rdju/diu * dkp(k), an = rdiv/djv * dkp(k),
+// ar = didjp/rp / dkw(k+1), with the boundary rows zeroed or recomputed per
+// (i, j) or per k).  The FP32 solver then needs no coefficient arrays: the
+// factors are taken from the converted coefficients at a reference column
+// and point of each block, checked against every coefficient
+// (k_mf_check), and the six couplings and 1/ap are formed on the fly.
+template <typename T>
+__device__ __forceinline__ void coefs_mf(const BlkDev &b, const MfTab<T> &t, int i, int j, int k,
+                                         T c[6], T &dinv)
+{
+    const long n0 = b.n[0];
+    const long ij = b.off2 + (i - 1) + n0 * (j - 1), kk = b.off1k + (k - 1);
+    const T ez = t.Ez[kk], nz = t.Nz[kk], r2 = t.R2[ij];
+    c[0] = t.E2[ij - 1] * ez;
+    c[1] = t.E2[ij] * ez;
+    c[2] = t.N2[ij - n0] * nz;
+    c[3] = t.N2[ij] * nz;
+    c[4] = r2 * t.Rz[kk - 1];
+    c[5] = r2 * t.Rz[kk];
+    dinv = (T)1 / (((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5]));
+}
+
+// 2-D factors at k = kr, 1-D factors along the reference column (i0, j0)
+template <typename T>
+__global__ void k_mf_extract(const BlkDev *__restrict__ blk, const T *__restrict__ E,
+                             const T *__restrict__ N, const T *__restrict__ R, MfTab<T> t,
+                             int *__restrict__ bad)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+    const long jo = n0, ko = (long)n0 * n1;
+    const int i0 = (n0 + 1) / 2, j0 = (n1 + 1) / 2, kr = (n2 + 1) / 2;
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q < (long)n0 * n1) {
+        long p = b.off3 + q + ko * (kr - 1);
+        t.E2[b.off2 + q] = E[p];
+        t.N2[b.off2 + q] = N[p];
+        t.R2[b.off2 + q] = R[p];
+    }
+    if (q < n2) {
+        long pc = b.off3 + (i0 - 1) + jo * (j0 - 1);
+        T e0 = E[pc + ko * (kr - 1)], nn0 = N[pc + ko * (kr - 1)], r0 = R[pc + ko * (kr - 1)];
+        if (e0 == (T)0 || nn0 == (T)0 || r0 == (T)0) {
+            atomicOr(bad, 16);
+            return;
+        }
+        t.Ez[b.off1k + q] = E[pc + ko * q] / e0;
+        t.Nz[b.off1k + q] = N[pc + ko * q] / nn0;
+        t.Rz[b.off1k + q] = R[pc + ko * q] / r0;
+    }
+}
+
+// every coupling and ap of every interior point within tol * ap
+template <typename T>
+__global__ void k_mf_check(const BlkDev *__restrict__ blk, const T *__restrict__ E,
+                           const T *__restrict__ N, const T *__restrict__ R,
+                           const T *__restrict__ D, MfTab<T> t, T tol, int *__restrict__ bad)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    long p = decode_interior(b, q, i, j, k);
+    long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    T c[6], dinv;
+    coefs_mf(b, t, i, j, k, c, dinv);
+    const T ref[6] = {E[p - 1], E[p], N[p - jo], N[p], R[p - ko], R[p]};
+    const T ap = (T)1 / D[p];
+    bool ok = fabs((double)(1 / dinv) - (double)ap) <= (double)tol * fabs((double)ap);
+    for (int m = 0; m < 6; m++) ok = ok && fabs((double)(c[m] - ref[m])) <= (double)tol * fabs((double)ap);
+    if (!ok) atomicOr(bad, 32);
+}
+
 // ---- red-black SOR half sweep ---------------------------------------------
 // Points with (i + j + k) % 2 == color are updated; the others are read.
+// one red-black update of interior point (i, j, k) of block bi
+template <typename T>
+__device__ __forceinline__ void rb_point(const BlkDev &b, int bi, int i, int j, int k, T omega,
+                                         const T *__restrict__ E, const T *__restrict__ N,
+                                         const T *__restrict__ R, const T *__restrict__ D,
+                                         T *__restrict__ x, const T *__restrict__ bb,
+                                         const PushDev *__restrict__ push, const MfTab<T> &mf)
+{
+    long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    long p = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    T c[6], dinv;
+    if (mf.E2) {
+        coefs_mf(b, mf, i, j, k, c, dinv);
+    } else {
+        c[0] = E[p - 1];
+        c[1] = E[p];
+        c[2] = N[p - jo];
+        c[3] = N[p];
+        c[4] = R[p - ko];
+        c[5] = R[p];
+        dinv = D[p];
+    }
+    T s = bb[p] + c[0] * x[p - 1] + c[1] * x[p + 1] + c[2] * x[p - jo] + c[3] * x[p + jo] +
+          c[4] * x[p - ko] + c[5] * x[p + ko];
+    T xo = x[p];
+    T xn = xo + omega * (s * dinv - xo);
+    x[p] = xn;
+    if (push) push_ghosts(push + 6 * bi, b, i, j, k, xn, x);
+}
+
+// thread q of a half sweep of colour `color` -> point (i, j, k); false if none
+__device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color, int &i, int &j, int &k)
+{
+    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
+    const unsigned nh = (unsigned)(ni + 1) >> 1;
+    if (q >= nh * (unsigned)nj * (unsigned)nk) return false;
+    const unsigned t = q / nh;
+    const int ii = (int)(q - t * nh);
+    const unsigned tk = t / (unsigned)nj;
+    k = (int)tk + 2;
+    j = (int)(t - tk * (unsigned)nj) + 2;
+    i = 2 + 2 * ii + ((2 + j + k + color) & 1);
+    return i <= ni + 1;
+}
+
+// ---- red-black SOR half sweep, all blocks of a level ----------------------
 template <typename T>
 __global__ void __launch_bounds__(256) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
                                             const T *__restrict__ R, const T *__restrict__ D,
                                             T *__restrict__ x, const T *__restrict__ bb,
-                                            const PushDev *__restrict__ push)
+                                            const PushDev *__restrict__ push, MfTab<T> mf)
 {
     const BlkDev b = blk[blockIdx.y];
-    int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
-    int nh = (ni + 1) >> 1;
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= (long)nh * nj * nk) return;
-    long t = q / nh;
-    int ii = (int)(q - t * nh);
-    int k = (int)(t / nj) + 2;
-    int j = (int)(t - (long)(k - 2) * nj) + 2;
-    int i = 2 + 2 * ii + ((2 + j + k + color) & 1);
-    if (i > ni + 1) return;
-    long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    long p = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
-    T s = bb[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] + N[p - jo] * x[p - jo] +
-          N[p] * x[p + jo] + R[p - ko] * x[p - ko] + R[p] * x[p + ko];
-    T xo = x[p];
-    T xn = xo + omega * (s * D[p] - xo);
-    x[p] = xn;
-    if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, xn, x);
+    int i, j, k;
+    if (!rb_decode(b, blockIdx.x * blockDim.x + threadIdx.x, color, i, j, k)) return;
+    rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
 }
 
 // ---- residual + restriction ------------------------------------------------
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
 // children are summed into the coarse right-hand side.
+// residual of the 8 fine children of coarse point (i, j, k), summed
 template <typename T>
-__global__ void __launch_bounds__(256) k_resid_restrict(
-    const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_, const T *__restrict__ E,
-    const T *__restrict__ N, const T *__restrict__ R, const T *__restrict__ D,
-    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse)
+__device__ __forceinline__ T rr_point(const BlkDev &f, int i, int j, int k, const T *__restrict__ E,
+                                      const T *__restrict__ N, const T *__restrict__ R,
+                                      const T *__restrict__ D, const T *__restrict__ x,
+                                      const T *__restrict__ bb, const MfTab<T> &mf)
 {
-    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= c.ncell) return;
-    int i, j, k;
-    long pc = decode_interior(c, q, i, j, k);
     long jo = f.n[0], ko = (long)f.n[0] * f.n[1];
     long p0 = f.off3 + (2 * i - 3) + jo * (2 * j - 3) + ko * (2 * k - 3);
     T sum = 0;
@@ -142,11 +245,39 @@ __global__ void __launch_bounds__(256) k_resid_restrict(
 #pragma unroll
             for (int dx = 0; dx < 2; dx++) {
                 long p = p0 + dx + jo * dy + ko * dz;
-                T ax = E[p - 1] * x[p - 1] + E[p] * x[p + 1] + N[p - jo] * x[p - jo] +
-                       N[p] * x[p + jo] + R[p - ko] * x[p - ko] + R[p] * x[p + ko];
-                sum += bb[p] - x[p] / D[p] + ax;
+                T cf[6], dinv;
+                if (mf.E2) {
+                    coefs_mf(f, mf, 2 * i - 2 + dx, 2 * j - 2 + dy, 2 * k - 2 + dz, cf, dinv);
+                } else {
+                    cf[0] = E[p - 1];
+                    cf[1] = E[p];
+                    cf[2] = N[p - jo];
+                    cf[3] = N[p];
+                    cf[4] = R[p - ko];
+                    cf[5] = R[p];
+                    dinv = D[p];
+                }
+                T ax = cf[0] * x[p - 1] + cf[1] * x[p + 1] + cf[2] * x[p - jo] + cf[3] * x[p + jo] +
+                       cf[4] * x[p - ko] + cf[5] * x[p + ko];
+                sum += bb[p] - x[p] / dinv + ax;
             }
-    bcoarse[pc] = sum;
+    return sum;
+}
+
+// One coarse interior point per thread: the residuals of its 2x2x2 fine
+// children are summed into the coarse right-hand side.
+template <typename T>
+__global__ void __launch_bounds__(256) k_resid_restrict(
+    const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_, const T *__restrict__ E,
+    const T *__restrict__ N, const T *__restrict__ R, const T *__restrict__ D,
+    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse, MfTab<T> mf)
+{
+    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= c.ncell) return;
+    int i, j, k;
+    long pc = decode_interior(c, q, i, j, k);
+    bcoarse[pc] = rr_point(f, i, j, k, E, N, R, D, x, bb, mf);
 }
 
 // ---- prolongation + correction --------------------------------------------
@@ -158,17 +289,12 @@ __device__ __forceinline__ int clamp_c(int ic, int n, int lo_int, int hi_int)
     return ic;
 }
 
+// trilinear correction of fine interior point (i, j, k) at pf
 template <typename T>
-__global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
-                                                 const BlkDev *__restrict__ bf_,
-                                                 const T *__restrict__ xc, T *__restrict__ xf,
-                                                 const PushDev *__restrict__ push)
+__device__ __forceinline__ void prolong_point(const BlkDev &c, const BlkDev &f, int bi, int i, int j,
+                                              int k, long pf, const T *__restrict__ xc,
+                                              T *__restrict__ xf, const PushDev *__restrict__ push)
 {
-    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= f.ncell) return;
-    int i, j, k;
-    long pf = decode_interior(f, q, i, j, k);
     int ic = (i + 1) >> 1, a = (i + 1) & 1;
     int jc = (j + 1) >> 1, bq = (j + 1) & 1;
     int kc = (k + 1) >> 1, cq = (k + 1) & 1;
@@ -192,7 +318,21 @@ __global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
             }
     T v = xf[pf] + cr;
     xf[pf] = v;
-    if (push) push_ghosts(push + 6 * blockIdx.y, f, i, j, k, v, xf);
+    if (push) push_ghosts(push + 6 * bi, f, i, j, k, v, xf);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
+                                                 const BlkDev *__restrict__ bf_,
+                                                 const T *__restrict__ xc, T *__restrict__ xf,
+                                                 const PushDev *__restrict__ push)
+{
+    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= f.ncell) return;
+    int i, j, k;
+    long pf = decode_interior(f, q, i, j, k);
+    prolong_point(c, f, blockIdx.y, i, j, k, pf, xc, xf, push);
 }
 
 // ---- halo for the fast solvers ---------------------------------------------
@@ -208,6 +348,101 @@ __global__ void k_halo_fast(const FaceDev *__restrict__ fc, T *__restrict__ x)
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         long k = q / nj + 1, j = q - (k - 1) * nj + 1;
         x[f.gh + f.jo * j + f.ko * k] = x[f.ppk + f.pjo * j + f.pko * k];
+    }
+}
+
+// ---- the coarse tail of a V-cycle in one CTA --------------------------------
+// Below a few tens of thousands of points a level's kernels are launch- and
+// drain-bound (a few microseconds each for little work).  k_vtail runs the
+// V-cycle from level l0 down to the coarsest level L and back -- smoothing,
+// residual + restriction, coarsest-level mean removal and sweeps,
+// prolongation -- as phases of one CTA separated by __syncthreads, the same
+// operations in the same order as the per-level launches.
+template <typename T>
+__device__ void tail_smooth(const VLev &L, int nb, int nsweep, T omega, const T *E, const T *N,
+                            const T *R, const T *D, T *x, const T *bb, const MfTab<T> &mf)
+{
+    for (int sw = 0; sw < nsweep; sw++)
+        for (int color = 0; color < 2; color++) {
+            for (int bi = 0; bi < nb; bi++) {
+                const BlkDev b = L.blk[bi];
+                const unsigned nh = (unsigned)(b.n[0] - 1) >> 1;
+                const unsigned tot = nh * (unsigned)(b.n[1] - 2) * (unsigned)(b.n[2] - 2);
+                for (unsigned q = threadIdx.x; q < tot; q += blockDim.x) {
+                    int i, j, k;
+                    if (rb_decode(b, q, color, i, j, k))
+                        rb_point(b, bi, i, j, k, omega, E, N, R, D, x, bb, L.rb_push ? L.push : nullptr, mf);
+                }
+            }
+            __syncthreads();
+            if (!L.rb_push && L.nface) {
+                for (int fi = 0; fi < L.nface; fi++) {
+                    const FaceDev f = L.face[fi];
+                    const long nj = f.nj - 2, n = nj * (f.nk - 2);
+                    for (long q = threadIdx.x; q < n; q += blockDim.x) {
+                        long kk = q / nj + 1, jj = q - (kk - 1) * nj + 1;
+                        x[f.gh + f.jo * jj + f.ko * kk] = x[f.ppk + f.pjo * jj + f.pko * kk];
+                    }
+                }
+                __syncthreads();
+            }
+        }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int l0, int L, int nb,
+                                                int pre, int crs, T omega, int singular,
+                                                const T *__restrict__ E, const T *__restrict__ N,
+                                                const T *__restrict__ R, const T *__restrict__ D,
+                                                T *__restrict__ x, T *__restrict__ bb, MfTab<T> mf)
+{
+    for (int lev = l0; lev < L; lev++) {
+        tail_smooth(lv[lev], nb, pre, omega, E, N, R, D, x, bb, mf);
+        for (int bi = 0; bi < nb; bi++) {
+            const BlkDev c = lv[lev + 1].blk[bi], f = lv[lev].blk[bi];
+            for (long q = threadIdx.x; q < c.ncell; q += blockDim.x) {
+                int i, j, k;
+                long pc = decode_interior(c, q, i, j, k);
+                bb[pc] = rr_point(f, i, j, k, E, N, R, D, x, bb, mf);
+            }
+        }
+        __syncthreads();
+    }
+    if (singular) {
+        double v[2] = {0., 0.};
+        for (int bi = 0; bi < nb; bi++) {
+            const BlkDev b = lv[L].blk[bi];
+            for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+                int i, j, k;
+                v[0] += (double)bb[decode_interior(b, q, i, j, k)];
+                v[1] += 1.0;
+            }
+        }
+        __shared__ double tot[2];
+        block_reduce_store<2>(v, tot);
+        __syncthreads();
+        const T mean = (T)(tot[0] / tot[1]);
+        for (int bi = 0; bi < nb; bi++) {
+            const BlkDev b = lv[L].blk[bi];
+            for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+                int i, j, k;
+                bb[decode_interior(b, q, i, j, k)] -= mean;
+            }
+        }
+        __syncthreads();
+    }
+    tail_smooth(lv[L], nb, L == 1 ? pre : crs, omega, E, N, R, D, x, bb, mf);
+    for (int lev = L - 1; lev >= l0; lev--) {
+        for (int bi = 0; bi < nb; bi++) {
+            const BlkDev c = lv[lev + 1].blk[bi], f = lv[lev].blk[bi];
+            for (long q = threadIdx.x; q < f.ncell; q += blockDim.x) {
+                int i, j, k;
+                long pf = decode_interior(f, q, i, j, k);
+                prolong_point(c, f, bi, i, j, k, pf, x, x, lv[lev].push);
+            }
+        }
+        __syncthreads();
+        tail_smooth(lv[lev], nb, pre, omega, E, N, R, D, x, bb, mf);
     }
 }
 
@@ -355,19 +590,19 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               cudaStream_t st)
+               const MfTab<T> &mf, cudaStream_t st)
 {
-    k_rb<T><<<dim3(nb_(maxhalf, 256), nb), 256, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push);
+    k_rb<T><<<dim3(nb_(maxhalf, 256), nb), 256, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
     count_launch(1);
 }
 
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           cudaStream_t st)
+                           const MfTab<T> &mf, cudaStream_t st)
 {
     k_resid_restrict<T><<<dim3(nb_(maxcell_c, 256), nb), 256, 0, st>>>(bc, bf, E, N, R, D, x, b,
-                                                                     bcoarse);
+                                                                     bcoarse, mf);
     count_launch(1);
 }
 
@@ -455,16 +690,42 @@ void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *
     count_launch(1);
 }
 
+template <typename T>
+void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const T *E,
+                      const T *N, const T *R, const T *D, const MfTab<T> &t, double tol, int *bad,
+                      cudaStream_t st)
+{
+    long n = max2d > maxn2 ? max2d : maxn2;
+    k_mf_extract<T><<<dim3(nb_(n, 256), nb), 256, 0, st>>>(blk, E, N, R, t, bad);
+    k_mf_check<T><<<dim3(nb_(maxcell, 256), nb), 256, 0, st>>>(blk, E, N, R, D, t, (T)tol, bad);
+    count_launch(2);
+}
+
+template <typename T>
+void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
+                  const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
+                  cudaStream_t st)
+{
+    k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf);
+    count_launch(1);
+}
+
 #define INST(T)                                                                                    \
     template int launch_conv_coef<T>(const BlkDev *, int, long, const double *const *, T *, T *,   \
                                      T *, T *, double *, double *, double *, double *, int *,     \
                                      cudaStream_t);                                                \
     template void launch_rb<T>(const BlkDev *, int, long, int, double, const T *, const T *,      \
                                const T *, const T *, T *, const T *, const PushDev *,             \
-                               cudaStream_t);                                                     \
+                               const MfTab<T> &, cudaStream_t);                                   \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
                                            const T *, const T *, const T *, const T *, const T *, \
-                                           T *, cudaStream_t);                                    \
+                                           T *, const MfTab<T> &, cudaStream_t);                  \
+    template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
+                                  const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
+                                  cudaStream_t);                                                  \
+    template void launch_mf_tables<T>(const BlkDev *, int, long, long, int, const T *, const T *, \
+                                      const T *, const T *, const MfTab<T> &, double, int *,      \
+                                      cudaStream_t);                                              \
     template void launch_prolong_fast<T>(const BlkDev *, const BlkDev *, int, long, const T *,    \
                                          T *, const PushDev *, cudaStream_t);                     \
     template void launch_halo_fast<T>(const FaceDev *, int, long, T *, cudaStream_t);             \

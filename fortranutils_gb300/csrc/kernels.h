@@ -67,11 +67,19 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               cudaStream_t st);
+               const MfTab<T> &mf, cudaStream_t st);
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           cudaStream_t st);
+                           const MfTab<T> &mf, cudaStream_t st);
+template <typename T>
+void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
+                  const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
+                  cudaStream_t st);
+template <typename T>
+void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const T *E,
+                      const T *N, const T *R, const T *D, const MfTab<T> &t, double tol, int *bad,
+                      cudaStream_t st);
 template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
                          T *xf, const PushDev *push, cudaStream_t st);

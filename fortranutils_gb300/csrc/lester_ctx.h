@@ -7,6 +7,7 @@
 #include "../../include/lester_gpu.h"
 #include "k_common.cuh"
 #include "phys_args.h"
+#include "kernels.h"
 
 namespace les {
 
@@ -40,6 +41,8 @@ struct CycleGraph {
     int sweeps = 0, coarse = 0;
     double omega = 0;
     bool singular = false;
+    bool mf = false;
+    int tail = 0;
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };
@@ -47,6 +50,8 @@ struct CycleGraph {
 // device buffers of the fast solvers, precision T
 template <typename T> struct FastSet {
     T *E = nullptr, *N = nullptr, *R = nullptr, *D = nullptr, *x = nullptr, *b = nullptr;
+    MfTab<T> tab;       // separable factors (FP32 solver)
+    bool mf = false;    // tab checked against every coefficient: used
 };
 
 struct Ctx {
@@ -116,6 +121,7 @@ struct Ctx {
     int2 *d_wslice = nullptr;
     int nslice = 0;
     WaveSync *d_wave = nullptr;
+    VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     long tabcap = 0, tab_next = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
 };

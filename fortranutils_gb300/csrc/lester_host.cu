@@ -126,6 +126,10 @@ static int build_levels(Ctx &c)
 {
     const lester_geom &g = c.g;
     int nb = g.numbl;
+    for (int b = 1; b <= nb; b++) {
+        long np = (long)g.bl_nijkp1[b - 1][0] * g.bl_nijkp1[b - 1][1] * g.bl_nijkp1[b - 1][2];
+        if (np >= (1L << 31)) return set_err(LES_ERR_SIZE, "block %d: %ld points exceed 2^31", b, np);
+    }
     for (int b = 1; b <= nb; b++)
         for (int d = 0; d < 3; d++) {
             c.lv[1].n[b][d] = g.bl_nijkp1[b - 1][d];
@@ -378,6 +382,16 @@ static int build_faces(Ctx &c)
         }
     }
     LES_CUDA(cudaMalloc(&c.d_work, sizeof(double) * (maxwork + 1)));
+    // per-level descriptors of the single-CTA V-cycle tail
+    {
+        std::vector<VLev> hv(c.nummgl + 1);
+        for (int lev = 1; lev <= c.nummgl; lev++) {
+            LevelGeom &L = c.lv[lev];
+            hv[lev] = VLev{L.d_blk, L.d_push, L.d_face, L.nface, L.rb_push ? 1 : 0};
+        }
+        LES_CUDA(cudaMalloc(&c.d_vlev, sizeof(VLev) * hv.size()));
+        LES_CUDA(cudaMemcpy(c.d_vlev, hv.data(), sizeof(VLev) * hv.size(), cudaMemcpyHostToDevice));
+    }
     return 0;
 }
 
@@ -418,7 +432,11 @@ static void free_ctx(Ctx *c)
     for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->d_tabpool) cudaFree(c->d_tabpool);
+    for (void *p : {(void *)c->f32.tab.E2, (void *)c->f32.tab.N2, (void *)c->f32.tab.R2, (void *)c->f32.tab.Ez,
+                    (void *)c->f32.tab.Nz, (void *)c->f32.tab.Rz})
+        cudaFree(p);
     cudaFree(c->d_wcum);
+    cudaFree(c->d_vlev);
     cudaFree(c->d_wslice);
     cudaFree(c->d_wave);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -612,6 +630,31 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
         return set_err(LES_ERR_STRUCTURE,
                        "coefficients lack the aw(i)=ae(i-1) pairing of coeff_p (mask %d); use LES_PSOLVE_REFERENCE", bad);
     c.singular = !(bad & 8);
+    // FP32 solver: separable factors instead of the coefficient arrays
+    F.mf = false;
+    if (sizeof(T) == 4 && c.c.rb_matfree) {
+        if (!F.tab.E2) {
+            T **t2[3] = {&F.tab.E2, &F.tab.N2, &F.tab.R2}, **t1[3] = {&F.tab.Ez, &F.tab.Nz, &F.tab.Rz};
+            for (T **a : t2) LES_CUDA(cudaMalloc((void **)a, sizeof(T) * c.tot2));
+            for (T **a : t1) LES_CUDA(cudaMalloc((void **)a, sizeof(T) * c.tot1k));
+        }
+        LES_CUDA(cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream));
+        for (int lev = 1; lev <= c.nummgl; lev++) {
+            LevelGeom &L = c.lv[lev];
+            long max2d = 0;
+            int maxn2 = 0;
+            for (int b = 1; b <= c.g.numbl; b++) {
+                max2d = std::max(max2d, (long)L.n[b][0] * L.n[b][1]);
+                maxn2 = std::max(maxn2, L.n[b][2]);
+            }
+            launch_mf_tables<T>(L.d_blk, c.g.numbl, L.maxcell, max2d, maxn2, F.E, F.N, F.R, F.D, F.tab, 1e-5,
+                                c.d_flag, c.stream);
+        }
+        int mbad = 0;
+        LES_CUDA(cudaMemcpyAsync(&mbad, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        LES_CUDA(cudaStreamSynchronize(c.stream));
+        F.mf = (mbad == 0);
+    }
     for (int q = 0; q < 7; q++) c.coef_key[q] = A.a[q];
     c.coef_gen_seen = c.coef_gen;
     c.coef_prec = prec;
@@ -654,7 +697,7 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
-                         F.b, L.rb_push ? L.d_push : nullptr, c.stream);
+                         F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
@@ -662,23 +705,45 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
 
 // one V-cycle on the correction equation A e = r, e = 0 on entry; r is in
 // F.b at level 1
+// levels from the first one with at most mg_tail interior points down to
+// the coarsest run as one single-CTA launch (k_vtail); 0 = none
+static int tail_level(const Ctx &c)
+{
+    if (c.c.mg_tail <= 0 || !c.d_vlev) return 0;
+    for (int lev = 1; lev <= c.nummgl; lev++) {
+        long n = 0;
+        for (int b = 1; b <= c.g.numbl; b++)
+            n += (long)(c.lv[lev].n[b][0] - 2) * (c.lv[lev].n[b][1] - 2) * (c.lv[lev].n[b][2] - 2);
+        if (n <= c.c.mg_tail) return lev;
+    }
+    return 0;
+}
+
 template <typename T> static void fast_vcycle(Ctx &c)
 {
     FastSet<T> &F = fset<T>(c);
     int L = c.nummgl;
     int pre = c.c.rb_sweeps > 0 ? c.c.rb_sweeps : 1;
     int crs = c.c.rb_coarse > 0 ? c.c.rb_coarse : 20;
+    const MfTab<T> mf = F.mf ? F.tab : MfTab<T>();
+    const int l0 = tail_level(c);
+    const int Lr = l0 ? l0 : L;  // levels below Lr run as per-level launches
     cudaMemsetAsync(F.x, 0, sizeof(T) * c.tot3, c.stream);
     count_launch(1);
-    for (int lev = 1; lev < L; lev++) {
+    for (int lev = 1; lev < Lr; lev++) {
         fast_smooth<T>(c, lev, pre);
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
         launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxcell, F.E, F.N, F.R, F.D, F.x,
-                                 F.b, F.b, c.stream);
+                                 F.b, F.b, mf, c.stream);
     }
-    if (c.singular) launch_coarse_mean<T>(c.lv[L].d_blk, c.g.numbl, F.b, c.stream);
-    fast_smooth<T>(c, L, L == 1 ? pre : crs);
-    for (int lev = L - 1; lev >= 1; lev--) {
+    if (l0) {
+        launch_vtail<T>(c.d_vlev, l0, L, c.g.numbl, pre, crs, c.c.rb_omega, c.singular ? 1 : 0, F.E, F.N,
+                        F.R, F.D, F.x, F.b, mf, c.stream);
+    } else {
+        if (c.singular) launch_coarse_mean<T>(c.lv[L].d_blk, c.g.numbl, F.b, c.stream);
+        fast_smooth<T>(c, L, L == 1 ? pre : crs);
+    }
+    for (int lev = Lr - 1; lev >= 1; lev--) {
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
         launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxcell, F.x, F.x, Lf.d_push, c.stream);
         fast_smooth<T>(c, lev, pre);
@@ -701,7 +766,7 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
 {
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
-        G.omega == k.rb_omega && G.singular == c.singular)
+        G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -743,6 +808,8 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
     G.coarse = k.rb_coarse;
     G.omega = k.rb_omega;
     G.singular = c.singular;
+    G.mf = fset<T>(c).mf;
+    G.tail = k.mg_tail;
     return 0;
 }
 

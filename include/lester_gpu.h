@@ -113,6 +113,13 @@ typedef struct lester_ctrl {
                           FMA, bitwise reproducible; 0 = fast build
                           (reciprocal metric tables, FMA, sqrt-based WALE
                           powers), a few units in the last place apart */
+    int rb_matfree;    /* FP32 solver: 1 = form the couplings from their
+                          separable (i,j) x k factors instead of reading the
+                          coefficient arrays, when every coefficient matches
+                          them to 1e-5 of ap; 0 = always read the arrays */
+    int mg_tail;       /* fast solvers: levels with at most this many
+                          interior points (all blocks) run as one single-CTA
+                          launch per V-cycle; 0 = one launch per operation */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */

@@ -179,8 +179,12 @@ def test_lmg_solve_reference_bitwise(env, cycle):
                                rtol=1e-12)
 
 
+@pytest.mark.parametrize("layout", ["tail", "per-level", "stored-coef"])
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
-def test_fast_solvers_converge_to_reference(env, psolve):
+def test_fast_solvers_converge_to_reference(env, psolve, layout):
+    """The fast solvers reach the converged reference solution, with the
+    coarse levels in one single-CTA launch (default on these small grids),
+    with one launch per operation, and with stored FP32 coefficients."""
     s = env
     c = s.case
     b = s.interior_random(mg=True, zero_mean=True)
@@ -189,7 +193,9 @@ def test_fast_solvers_converge_to_reference(env, psolve):
     s.orc.set_jumble(0)
     s.orc.lmg_solve(O.mgctrl(nummgits=400, tolf=1e-15), s.a, fr, br, rr)
     s.orc.p_ref_subtract(fr)
-    ctrl = L.default_ctrl(psolve=psolve, rtol=1e-9, max_outer=400)
+    ctrl = L.default_ctrl(psolve=psolve, rtol=1e-9, max_outer=400,
+                          mg_tail=0 if layout != "tail" else 32768,
+                          rb_matfree=0 if layout == "stored-coef" else 1)
     L.gpu_set_ctrl(ctrl)
     fd, bd, rd = dev(np.zeros(c.n3_mg)), dev(b), dev(np.zeros(c.n3_mg))
     L.lmg_solve(*[dev(a) for a in s.a], fd, bd, rd)
