@@ -40,6 +40,8 @@ UNITS = {
     "k_virtbc": ("k_virtbc.cu", ["-fmad=false"]),
     "lester_step": ("lester_step.cu", []),
     "lester_noalloc": ("lester_noalloc.cu", ["-fmad=false"]),
+    "k_adjoint": ("k_adjoint.cu", ["-fmad=false"]),
+    "lester_adjoint": ("lester_adjoint.cu", []),
 }
 
 

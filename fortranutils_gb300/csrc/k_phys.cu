@@ -214,6 +214,7 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
         twa[ijl] = (st1 * (-tw + twa[ijl]) - st2 * (-tw)) * stden;
     }
     double h = conf + conc + diffc + tiief - tiiwf + tjinf - tjisf + tkirf - tkilf;
+    if (A_.fb) h += A_.fb[ijk] * vol;  // body force per unit volume (off unless set)
     A_.u_int[ijk] = u[ijk] * (rhou / rhonp1u) +
                     dtime / (rhonp1u * vol) *
                         (1.5 * h - 0.5 * A_.hu[ijk] +
@@ -387,6 +388,7 @@ __global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ bl
     }
     double difff = tikef - tikwf + tjknf - tjksf + tkkrf - tkklf;
     double h = conf + conc + difff + diffc;
+    if (A_.fb) h += A_.fb[ijk] * vol;  // body force per unit volume (off unless set)
     A_.w_int[ijk] = w[ijk] * (rhow / rhonp1w) +
                     dtime / (vol * rhonp1w) * (1.5 * h - 0.5 * A_.hw[ijk] + 0.5 * areak * (A_.p[ijk] - A_.p[ijkl]));
     A_.hw[ijk] = h;

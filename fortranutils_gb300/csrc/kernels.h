@@ -110,6 +110,31 @@ void launch_recip(const double *const *src, double *const *dst, int ntab, long n
 void launch_delta_tables(const double *dip, const double *djp, const double *rp, long n2,
                          const double *dkp, long n1, double *d2, double *d1, cudaStream_t st);
 
+// k_adjoint.cu: linearised predictors (mode 0 tangent, 1 adjoint pass for
+// slot q0, 2 forward value) and the transposes of the linear step operators
+void launch_upred_lin(const BlkDev *blk, int nb, long maxcell, int iva, int mode, int q0, const UIntArgs &a,
+                      const PredRefs &base, const PredRefs &tan, const PredBars &bar, const double *lam_u,
+                      const double *lam_h, double *out_u, double *out_h, double dtime, double visc,
+                      double ylaminar, double kappa, double cwfun, cudaStream_t st);
+void launch_wpred_lin(const BlkDev *blk, int nb, long maxcell, int mode, int q0, const WIntArgs &a,
+                      const PredRefs &base, const PredRefs &tan, const PredBars &bar, const double *lam_u,
+                      const double *lam_h, double *out_u, double *out_h, double dtime, double visc,
+                      double ylaminar, double kappa, double cwfun, cudaStream_t st);
+void launch_take(const BlkDev *blk, int nb, long maxcell, int which, const double *src, double *dst,
+                 double *zero_src, cudaStream_t st);
+void launch_halo_t(const FaceDev *faces, int nface, long maxface, double *bar, double *wbar, cudaStream_t st);
+void launch_extrap_p_t(const BlkDev *blk, int nb, double *bar, cudaStream_t st);
+void launch_pref_t(const BlkDev *blk, double *bar, long n, cudaStream_t st);
+void launch_sour_p_t(const BlkDev *blk, int nb, long maxcell, double dtime, const double *rdiv,
+                     const double *rdju, const double *didjp, const double *dkp, const double *rhonp1,
+                     const double *sbar, double *ubar, double *vbar, double *wbar, cudaStream_t st);
+void launch_uvw_adv_t(const BlkDev *blk, int nb, long maxcell, int ivar, double dtime, const double *dg,
+                      const double *rp, const double *dkw, double *ubar, double *uibar, const double *rho,
+                      double *pbar, cudaStream_t st);
+void launch_wall_shear(const BlkDev *blk, int nb, long maxik, const double *dju, double visc, const double *u,
+                       double coef, double *ubar, double *sum, cudaStream_t st);
+void launch_fill_d(double *a, double v, long n, cudaStream_t st);
+
 } // namespace les
 
 // k_phys.cu and k_sgs.cu, built twice (phys_variant.h): les_exact and les_fast

@@ -122,6 +122,7 @@ struct Ctx {
     int nslice = 0;
     WaveSync *d_wave = nullptr;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
+    const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)
     long tabcap = 0, tab_next = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
 };

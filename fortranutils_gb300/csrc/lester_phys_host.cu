@@ -151,6 +151,23 @@ using namespace les;
 
 extern "C" {
 
+int lester_gpu_set_body_force(const double *fu, const double *fv, const double *fw)
+{
+    LES_NEED_CTX();
+    const double *f[3] = {fu, fv, fw};
+    for (int q = 0; q < 3; q++) {
+        if (!f[q]) continue;
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, f[q]) != cudaSuccess ||
+            (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+            cudaGetLastError();
+            return set_err(LES_ERR_ARG, "body force %d must be device memory", q);
+        }
+    }
+    for (int q = 0; q < 3; q++) g_ctx->fb[q] = f[q];
+    return 0;
+}
+
 int lester_gpu_set_iststep(int iststep)
 {
     LES_NEED_CTX();
@@ -201,6 +218,7 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
     A.off_ki = c.d_offki;
     A.off_jk = c.d_offjk;
     A.off2_lev1_base = 0;
+    A.fb = c.fb[iv - 1];
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
     if (!k.exact) {
@@ -252,6 +270,7 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
         return r;
     A.off_ki = c.d_offki;
     A.off_jk = c.d_offjk;
+    A.fb = c.fb[2];
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
     if (!k.exact) {

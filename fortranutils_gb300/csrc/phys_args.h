@@ -19,6 +19,7 @@ struct UIntArgs {
     long off2_lev1_base;          // 0: level-1 (i,j) arrays start with block 1
     // fast variant only: reciprocals of the divisor metrics (same layout)
     const double *r_dip, *r_diu, *r_dix, *r_djp, *r_dju, *r_djv, *r_djx, *r_rp, *r_dkp, *r_dkw;
+    const double *fb;  // body force of this component per unit volume, or null
 };
 
 struct WIntArgs {
@@ -30,6 +31,7 @@ struct WIntArgs {
     const long *off_ki, *off_jk;
     const double *r[MW_N];        // fast variant only: reciprocals of m[]
     const double *rdkp, *rdkw;
+    const double *fb;             // body force of w per unit volume, or null
 };
 
 struct Sc1Args {
@@ -57,6 +59,15 @@ struct WaveSync {
 // delta2d(i,j) * delta1d(k) = (dip*djp*rp)^0.33333333 * dkp^0.33333333
 struct SgsFast {
     const double *r_dip, *r_djp, *r_rp, *r_dkp, *r_dkw, *delta2d, *delta1d;
+};
+
+// base, tangent and adjoint arrays of the linearised predictor inputs, in
+// slot-field order: role-u, role-v, w, p, old h, body force (may be null)
+struct PredRefs {
+    const double *f[6];
+};
+struct PredBars {
+    double *f[6];
 };
 
 // set_virt_bc arguments: the field, the wall array of the side being

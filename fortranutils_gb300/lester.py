@@ -334,6 +334,17 @@ def gpu_set_iststep(iststep: int) -> None:
     _check(lib().lester_gpu_set_iststep(int(iststep)))
 
 
+def gpu_set_body_force(fu=None, fv=None, fw=None) -> None:
+    """Body force per unit volume added to the u, v, w predictors (device
+    tensors in the level-1 layout, kept alive by the caller; None = none)."""
+    _check(lib().lester_gpu_set_body_force(_p(fu), _p(fv), _p(fw)))
+
+
+class AdjCfg(C.Structure):
+    """include/lester_gpu.h lester_adj_cfg"""
+    _fields_ = [("nsteps", C.c_int), ("j_first", C.c_int), ("j_last", C.c_int), ("checkpoint", C.c_int)]
+
+
 # roles of set_uv_int's metric arguments (code/set_uv_int.F:5-11) and the
 # arrays step.F passes for u and for v (code/step.F:307-326)
 UV_ROLES = ("dip diu dix rdix djp dju djv djx rdjp rdju didjp didju rdidju hijp hiju hjiu hkiu "

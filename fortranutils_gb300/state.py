@@ -176,3 +176,33 @@ def step(state: State, istep: int) -> int:
     if rc not in (0, -7):
         L._check(rc)
     return rc
+
+
+def _adj_cfg(nsteps, j_first, j_last, checkpoint):
+    return L.AdjCfg(int(nsteps), int(j_first), int(j_last if j_last is not None else nsteps),
+                    int(checkpoint if checkpoint is not None else nsteps))
+
+
+def adjoint_run(state: State, nsteps: int, gfu, gfv, gfw, j_first: int = 1, j_last: int | None = None,
+                checkpoint: int | None = None) -> float:
+    """lester_adjoint_run: the objective J (mean wall shear stress over
+    steps j_first..j_last of an nsteps run from ``state``, which is left
+    unchanged) and its gradient with respect to the body force, written to
+    the device tensors gfu, gfv, gfw."""
+    f = state.fields()
+    cfg = _adj_cfg(nsteps, j_first, j_last, checkpoint)
+    J = C.c_double()
+    L._check(L.lib().lester_adjoint_run(C.byref(cfg), C.byref(f), C.byref(J), L._p(gfu), L._p(gfv),
+                                        L._p(gfw)))
+    return J.value
+
+
+def tangent_run(state: State, nsteps: int, dfu, dfv, dfw, j_first: int = 1, j_last: int | None = None):
+    """lester_tangent_run: (J, dJ), dJ the derivative of J along the body
+    force direction (dfu, dfv, dfw); ``state`` is left unchanged."""
+    f = state.fields()
+    cfg = _adj_cfg(nsteps, j_first, j_last, None)
+    J, dJ = C.c_double(), C.c_double()
+    L._check(L.lib().lester_tangent_run(C.byref(cfg), C.byref(f), L._p(dfu), L._p(dfv), L._p(dfw), C.byref(J),
+                                        C.byref(dJ)))
+    return J.value, dJ.value

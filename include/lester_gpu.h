@@ -318,6 +318,11 @@ int lester_slipbc(const double *x, const double *y, const double *z,
  * It starts at 2, the value of a run's first step; lester_step advances it
  * by one after each step. */
 int lester_gpu_set_iststep(int iststep);
+/* No counterpart in the reference: a body force per unit volume for the u,
+ * v and w predictors (device arrays in the level-1 layout, NULL = none),
+ * added to each component's explicit term h.  It is the control of the
+ * adjoint (lester_adjoint_run); the reference has no forcing term. */
+int lester_gpu_set_body_force(const double *fu, const double *fv, const double *fw);
 /* code/set_uv_int.F:5 set_uv_int(iva, u, v, w, p, rho, rhonp1, gam, u_int,
  * hu, dip, diu, dix, rdix, djp, dju, djv, djx, rdjp, rdju, didjp, didju,
  * rdidju, hijp, hiju, hjiu, hkiu, hkju, rp, ru, dkp, dkw, tw_sfi, tw_nfi,
@@ -409,6 +414,34 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u,
                    const double *dkp, const double *dkw, const double *hijp,
                    const double *hjip, const double *hkip, const double *hkjp,
                    const double *rp, double *work, int *offwork);
+
+/* ---- adjoint and tangent-linear runs ---------------------------------- */
+/* No counterpart in the reference.  A run of nsteps lester_step calls from
+ * the state in `fields` (device arrays; the caller's arrays are not
+ * changed) and the objective
+ *   J = mean over steps j_first..j_last (1-based) of the mean wall shear
+ *       stress visc * u / (0.5 * dju) over the first interior u points of
+ *       the WALL y sides (S, N),
+ * differentiated with respect to the body force of lester_gpu_set_body_force
+ * (per unit volume; the current one is the linearisation point).
+ * lester_adjoint_run returns J and dJ/dfu, dJ/dfv, dJ/dfw (device arrays in
+ * the level-1 layout, overwritten) by the transposed step, with the state
+ * checkpointed every `checkpoint` steps and each segment recomputed.
+ * lester_tangent_run returns J and the directional derivative dJ along
+ * (dfu, dfv, dfw) by the linearised step.  Scope: psolve FP64 or MIXED
+ * (converged: the linearisation of an iterative solve is the exact solve),
+ * rholo == rhohi, model 0, no ZERO_GRAD sides, wall points in the laminar
+ * branch of the wall function (y+ below ylaminar).  Errors as lester_step;
+ * LES_ERR_ARG outside that scope. */
+typedef struct lester_adj_cfg {
+    int nsteps;
+    int j_first, j_last;  /* objective window, 1 <= j_first <= j_last <= nsteps */
+    int checkpoint;       /* steps per checkpoint segment (>= 1) */
+} lester_adj_cfg;
+int lester_adjoint_run(const lester_adj_cfg *cfg, const lester_fields *fields, double *J, double *gfu,
+                       double *gfv, double *gfw);
+int lester_tangent_run(const lester_adj_cfg *cfg, const lester_fields *fields, const double *dfu,
+                       const double *dfv, const double *dfw, double *J, double *dJ);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,163 @@
+"""Adjoint and tangent-linear runs of the time step (lester_adjoint_run,
+lester_tangent_run) on small channels, through the C ABI.
+
+Objective: the mean wall shear stress over a window of steps; control: the
+body force of the u, v, w predictors.  Checks:
+  * the tangent against central finite differences of the forward run
+    (relative 1e-6: the O(eps^2) truncation of a quadratic map);
+  * the adjoint gradient against the tangent along random directions
+    (<grad J, d> = dJ(d), relative 1e-9: the two runs differ only by the
+    rounding and the 1e-12 residuals of their pressure solves);
+  * the gradient does not depend on the checkpoint interval;
+  * the caller's state is left unchanged, and runs outside the scope the
+    transposition covers are refused.
+"""
+import numpy as np
+import pytest
+
+from fortranutils_gb300 import lester as L
+from fortranutils_gb300 import state as S
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+NSTEP = 4
+
+
+def start(name, psolve=L.PSOLVE_FP64, **kw):
+    """A channel state after one ordinary step (which forms the pressure
+    coefficients and the wall-stress running means), laminar at the walls."""
+    import torch
+    st = cases.Setup(name)
+    ctrl = dict(dtime=2e-3, model=0, psolve=psolve, rtol=1e-12, max_outer=400, visc=1.0 / 500.0)
+    ctrl.update(kw)
+    s = S.new_state(st.case, st.m, st.dkp, st.dkw)
+    S.init_channel(s, seed=7)
+    g = s.to("torch")
+    L.gpu_init(st.case.geom(), L.default_ctrl(**ctrl))
+    assert S.step(g, 1) == 0
+    torch.cuda.synchronize()
+    return st, g
+
+
+def direction(st, seed):
+    """A body-force direction: a uniform streamwise part plus noise."""
+    import torch
+    rng = np.random.default_rng(seed)
+    st.rng = rng
+    du = st.interior_random(scale=0.3)
+    for ib in range(len(st.case.blocks)):
+        st.case.block_view(du, ib, 0)[1:-1, 1:-1, 1:-1] += 1.0
+    dv = st.interior_random(scale=0.3)
+    dw = st.interior_random(scale=0.3)
+    return [torch.from_numpy(a).cuda() for a in (du, dv, dw)]
+
+
+def dot(a, b):
+    return float(sum((x * y).sum().item() for x, y in zip(a, b)))
+
+
+@pytest.fixture
+def finalize():
+    yield
+    L.gpu_finalize()
+
+
+@pytest.mark.parametrize("name", ["box_wall", "two_block"])
+def test_tangent_matches_finite_differences(name, finalize):
+    import torch
+    st, g = start(name)
+    d = direction(st, 11)
+    J0, dJ = S.tangent_run(g, NSTEP, *d, j_first=2)
+    assert J0 > 0 and dJ != 0
+    eps = 1e-3
+    Js = []
+    for sgn in (1.0, -1.0):
+        f = [sgn * eps * x for x in d]
+        L.gpu_set_body_force(*f)
+        zero = [torch.zeros_like(x) for x in d]
+        Js.append(S.tangent_run(g, NSTEP, *zero, j_first=2)[0])
+        L.gpu_set_body_force()
+    fd = (Js[0] - Js[1]) / (2 * eps)
+    assert abs(fd - dJ) <= 1e-6 * abs(dJ), (fd, dJ)
+
+
+@pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
+@pytest.mark.parametrize("name", ["box_wall", "two_block"])
+def test_adjoint_matches_tangent(name, psolve, finalize):
+    """The adjoint is the transpose of the tangent: for two directions,
+    <grad J, d> equals the tangent's dJ(d)."""
+    import torch
+    st, g = start(name, psolve=psolve)
+    grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+    J = S.adjoint_run(g, NSTEP, *grad, j_first=2, checkpoint=2)
+    for seed in (3, 4):
+        d = direction(st, seed)
+        Jt, dJ = S.tangent_run(g, NSTEP, *d, j_first=2)
+        assert abs(Jt - J) <= 1e-12 * abs(J)
+        adj = dot(grad, d)
+        assert abs(adj - dJ) <= 1e-9 * abs(dJ), (adj, dJ)
+
+
+def test_gradient_independent_of_checkpoints(finalize):
+    import torch
+    st, g = start("box_wall")
+    out = []
+    for K in (1, 3, NSTEP):
+        grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+        J = S.adjoint_run(g, NSTEP, *grad, checkpoint=K)
+        out.append((J, [x.cpu().numpy() for x in grad]))
+    J0, g0 = out[0]
+    scale = max(np.abs(x).max() for x in g0)
+    assert scale > 0
+    for J, gk in out[1:]:
+        assert abs(J - J0) <= 1e-14 * abs(J0)
+        for a, b in zip(gk, g0):
+            assert np.abs(a - b).max() <= 1e-12 * scale
+
+
+def test_window_and_state_unchanged(finalize):
+    """A window of one step; the caller's arrays are not touched."""
+    import torch
+    st, g = start("box_wall")
+    before = {n: g[n].clone() for n in S.STATE}
+    grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+    J_last = S.adjoint_run(g, NSTEP, *grad, j_first=NSTEP, j_last=NSTEP)
+    d = direction(st, 5)
+    Jt, dJ = S.tangent_run(g, NSTEP, *d, j_first=NSTEP, j_last=NSTEP)
+    assert abs(Jt - J_last) <= 1e-12 * abs(J_last)
+    assert abs(dot(grad, d) - dJ) <= 1e-9 * abs(dJ)
+    for n in S.STATE:
+        assert torch.equal(g[n], before[n]), n
+    # the gradient vanishes where the predictors write nothing: the first
+    # interior v plane on each wall
+    gv = grad[1].cpu().numpy()
+    for ib in range(len(st.case.blocks)):
+        assert np.all(st.case.block_view(gv, ib, 0)[:, 1, :] == 0.0)
+
+
+@pytest.mark.parametrize("name,bad", [("box_wall", dict(model=1)), ("box_wall", dict(rholo=1.0, rhohi=2.0)),
+                                      ("box_wall", dict(psolve=L.PSOLVE_REFERENCE)),
+                                      ("box_slip_stretched", {})])
+def test_scope_refused(name, bad, finalize):
+    """Eddy viscosity, variable density, the reference solver (not
+    converged) and slip sides are outside the transposed step."""
+    import torch
+    st, g = start(name, **bad)
+    grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+    with pytest.raises(L.LesterError):
+        S.adjoint_run(g, 2, *grad)
+    with pytest.raises(L.LesterError):
+        S.tangent_run(g, 2, *grad)
+
+
+def test_bad_configuration_refused(finalize):
+    import torch
+    st, g = start("box_wall")
+    grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+    for kw in (dict(j_first=0), dict(j_first=3, j_last=2), dict(j_last=5), dict(checkpoint=0)):
+        with pytest.raises(L.LesterError):
+            S.adjoint_run(g, 4, *grad, **kw)
+    with pytest.raises(L.LesterError):
+        S.adjoint_run(g.to("numpy"), 2, *grad)
