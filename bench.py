@@ -110,10 +110,10 @@ def make_case(shape=SHAPE):
     return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
 
 
-def make_ctrl(psolve):
+def make_ctrl(psolve, krylov=2):
     from fortranutils_gb300 import lester as L
     return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
-                          rtol=1e-8, max_outer=200, exact=EXACT)
+                          rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
 
 
 def host_state(case, ctrl):
@@ -138,20 +138,25 @@ def device_state(case, ctrl):
     return g
 
 
-def step_bytes(mode: str, cycles: float, sweeps: int) -> float:
+def step_bytes(mode: str, cycles: float, sweeps: int, krylov: int = 1) -> float:
     """Algorithmic bytes per interior cell of one step: distinct 3-D arrays
     read plus written once per kernel (8 B FP64, 4 B FP32), metric tables and
     matrix-free coefficients free.  Per V-cycle, levels sum with 8/7:
       FP64: sweeps 24, residual 24, restriction 9, prolongation 17;
-      mixed: FP32 sweeps 12, restriction 4.5, prolongation 8.5, plus the
-      FP64 outer residual 24 and update p += e (8 + 4).
+      mixed: FP32 sweeps 12, restriction 4.5, prolongation 8.5.
+    Per outer iteration (level 1, FP64 vectors; z the cycle's correction):
+      defect correction: residual 24 + update p += z (16 + |z|);
+      flexible CG: z.q and z.r (16 + |z|), direction p, q (40 + |z|),
+      step x, r (48 + |z|).
     Per step: predictor 128, WALE 64, sour_p 72, projection 64, p_ref 16,
     scalar predictor 80, search_lib 32."""
     nsw = 2 * sweeps  # pre + post smoothing sweeps per level
+    zb = 8 if mode == "fp64" else 4
+    outer = (104 + 3 * zb) if krylov else (40 + zb)
     if mode == "fp64":
-        bv = 8.0 / 7.0 * (nsw * 24 + 24 + 9 + 17)
+        bv = 8.0 / 7.0 * (nsw * 24 + 24 + 9 + 17) + outer
     else:
-        bv = 8.0 / 7.0 * (nsw * 12 + 4.5 + 8.5) + 24 + 12
+        bv = 8.0 / 7.0 * (nsw * 12 + 4.5 + 8.5) + outer
     return 128 + 64 + 72 + 64 + 16 + 80 + 32 + cycles * bv
 
 
@@ -166,7 +171,7 @@ def run_gpu(args):
     modes = [("fp64", L.PSOLVE_FP64), ("mixed", L.PSOLVE_MIXED)]
     modes = [m for m in modes if args.mode in ("both", m[0])]
     for mode, ps in modes:
-        ctrl = make_ctrl(ps)
+        ctrl = make_ctrl(ps, {"dc": 0, "fcg": 1, "auto": 2}[args.outer])
         L.gpu_init(case.geom(), ctrl)
         g = device_state(case, ctrl)
         stream = torch.cuda.current_stream()
@@ -289,13 +294,16 @@ def reference_line(args, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
     ap.add_argument("--mode", default="both", choices=["both", "mixed", "fp64"],
                     help="solvers to time (the JSON line needs both)")
+    ap.add_argument("--outer", default="auto", choices=["auto", "fcg", "dc"],
+                    help="fast solvers' outer loop: defect correction switching to flexible CG "
+                         "when a cycle stalls (auto), flexible CG, or defect correction")
     ap.add_argument("--shape", type=int, nargs=3, default=list(SHAPE),
                     help="cells per axis (smaller shapes are for profiling only)")
     args = ap.parse_args()
@@ -326,7 +334,9 @@ def main():
     rb_avg_ms = mx["rb_ms"] / max(mx["rb_launches"], 1)
     achieved = 6.0 * ncell / (rb_avg_ms * 1e-3) / 1e9
     sweeps = mx["ctrl"].rb_sweeps
-    step_gbs = {m: step_bytes(m, r["cycles"], sweeps) * ncell / (r["ms_per_step"] * 1e-3) / 1e9
+    # outer iterations counted as defect correction unless flexible CG ran
+    kry = 1 if args.outer == "fcg" else 0
+    step_gbs = {m: step_bytes(m, r["cycles"], sweeps, kry) * ncell / (r["ms_per_step"] * 1e-3) / 1e9
                 for m, r in (("mixed", mx), ("fp64", fp))}
     cpu = None
     if not args.no_cpu and rank == 0:
@@ -342,7 +352,9 @@ def main():
         "data": "synthetic (seeded numpy default_rng, seed 2)",
         "config": {"workload": WORKLOAD, "cells": ncell,
                    "l2": "inputs larger than L2 (~2 GB working set), no flush",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+                   "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "outer_loop": {"auto": "defect correction, flexible CG when a cycle stalls",
+                                  "fcg": "flexible CG", "dc": "defect correction"}[args.outer]},
         "mixed": {"vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"],
                   "vcycle_ms": mx["solve_ms"] / max(mx["cycles"], 1),
                   "relres_max": mx["relres_max"]},

@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(256) k_resid_outer(
     const BlkDev *__restrict__ blk, const double *__restrict__ E, const double *__restrict__ N,
     const double *__restrict__ R, const double *__restrict__ P, const double *__restrict__ x,
     const double *__restrict__ bb, const double *__restrict__ shift, T *__restrict__ rT,
-    double *__restrict__ partial)
+    double *__restrict__ r64, double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -471,6 +471,7 @@ __global__ void __launch_bounds__(256) k_resid_outer(
                    N[p - jo] * x[p - jo] + N[p] * x[p + jo] + R[p - ko] * x[p - ko] +
                    R[p] * x[p + ko];
         rT[p] = (T)r;
+        if (r64) r64[p] = r;
         v[0] += r * r;
         v[1] += bp * bp;
     }
@@ -569,6 +570,88 @@ __global__ void k_update(const BlkDev *__restrict__ blk, double *__restrict__ p,
     if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, v, p);
 }
 
+// ---- flexible conjugate gradients around the V-cycle ----------------------
+// FCG(1): with z = V(r) the cycle's correction for the residual r,
+//   beta = (z.q) / (p.q),  p <- z - beta p,  q <- A z - beta q   (q = A p)
+//   alpha = (p.r) / (p.q), x <- x + alpha p,  r <- r - alpha q
+// The scalars stay on the device: sc[0] = z.q, sc[2] = p.q, sc[3] = p.r
+// (sc[2] = 0 restarts with beta = 0).  Interior points of level 1; the
+// reductions are per-CTA partials summed by k_sum2_final.
+
+// partial sums of z.q (and z.r)
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_dot(const BlkDev *__restrict__ blk, const T *__restrict__ z,
+                                                 const double *__restrict__ q, const double *__restrict__ r,
+                                                 double *__restrict__ partial)
+{
+    const BlkDev b = blk[blockIdx.y];
+    double v[2] = {0., 0.};
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < b.ncell; t += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        long p = decode_interior(b, t, i, j, k);
+        const double zp = (double)z[p];
+        v[0] += zp * q[p];
+        v[1] += zp * r[p];
+    }
+    block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
+}
+
+// new direction p and q = A p (FP64 coefficients, z's ghosts current);
+// partial sums of p.q and p.r
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_dir(
+    const BlkDev *__restrict__ blk, const double *__restrict__ E, const double *__restrict__ N,
+    const double *__restrict__ R, const double *__restrict__ P, const T *__restrict__ z,
+    double *__restrict__ pd, double *__restrict__ q, const double *__restrict__ r,
+    const double *__restrict__ sc, double *__restrict__ partial)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const double pq = sc[2];
+    const double beta = pq != 0. ? sc[0] / pq : 0.;
+    double v[2] = {0., 0.};
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < b.ncell; t += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        long p = decode_interior(b, t, i, j, k);
+        long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+        double az = P[p] * (double)z[p] - E[p - 1] * (double)z[p - 1] - E[p] * (double)z[p + 1] -
+                    N[p - jo] * (double)z[p - jo] - N[p] * (double)z[p + jo] -
+                    R[p - ko] * (double)z[p - ko] - R[p] * (double)z[p + ko];
+        double pn = (double)z[p] - beta * pd[p];
+        double qn = az - beta * q[p];
+        pd[p] = pn;
+        q[p] = qn;
+        v[0] += pn * qn;
+        v[1] += pn * r[p];
+    }
+    block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
+}
+
+// x += alpha p (with the ghost mirrors), r -= alpha q, rT = r; partial r.r
+template <typename T>
+__global__ void __launch_bounds__(256) k_fcg_step(const BlkDev *__restrict__ blk, double *__restrict__ x,
+                                                  const double *__restrict__ pd, const double *__restrict__ q,
+                                                  double *__restrict__ r, T *__restrict__ rT,
+                                                  const double *__restrict__ sc, const PushDev *__restrict__ push,
+                                                  double *__restrict__ partial)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const double pq = sc[2];
+    const double alpha = pq != 0. ? sc[3] / pq : 0.;
+    double v[2] = {0., 0.};
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < b.ncell; t += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        long p = decode_interior(b, t, i, j, k);
+        double xn = x[p] + alpha * pd[p];
+        x[p] = xn;
+        if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, xn, x);
+        double rn = r[p] - alpha * q[p];
+        r[p] = rn;
+        rT[p] = (T)rn;
+        v[0] += rn * rn;
+    }
+    block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
+}
+
 // ================================================================ launchers
 namespace les {
 
@@ -627,15 +710,39 @@ void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaS
 template <typename T>
 void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
                         const double *R, const double *P, const double *x, const double *b,
-                        const double *shift, T *rT, double *partial, double *out2, cudaStream_t st)
+                        const double *shift, T *rT, double *r64, double *partial, double *out2,
+                        cudaStream_t st)
 {
     // grid-stride: a few CTAs per SM, so the final sum reads few partials
     unsigned gx = nb_(maxcell, 256);
     unsigned cap = (unsigned)((1216 + nb - 1) / nb);
     if (gx > cap) gx = cap;
-    k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, partial);
+    k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, r64, partial);
     k_sum2_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out2);
     count_launch(2);
+}
+
+static unsigned reduce_grid(long maxcell, int nb)
+{
+    unsigned gx = nb_(maxcell, 256);
+    unsigned cap = (unsigned)((1216 + nb - 1) / nb);
+    return gx > cap ? cap : gx;
+}
+
+template <typename T>
+void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N, const double *R,
+                const double *P, const T *z, double *x, double *pd, double *q, double *r, T *rT,
+                const PushDev *push, double *partial, double *sc, double *out_rr, cudaStream_t st)
+{
+    unsigned gx = reduce_grid(maxcell, nb);
+    long np = (long)gx * nb;
+    k_fcg_dot<T><<<dim3(gx, nb), 256, 0, st>>>(blk, z, q, r, partial);
+    k_sum2_final<<<1, 256, 0, st>>>(partial, np, sc);
+    k_fcg_dir<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, z, pd, q, r, sc, partial);
+    k_sum2_final<<<1, 256, 0, st>>>(partial, np, sc + 2);
+    k_fcg_step<T><<<dim3(gx, nb), 256, 0, st>>>(blk, x, pd, q, r, rT, sc, push, partial);
+    k_sum2_final<<<1, 256, 0, st>>>(partial, np, out_rr);
+    count_launch(6);
 }
 
 void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
@@ -732,7 +839,11 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
     template void launch_resid_outer<T>(const BlkDev *, int, long, const double *,                \
                                         const double *, const double *, const double *,           \
                                         const double *, const double *, const double *, T *,      \
-                                        double *, double *, cudaStream_t);                        \
+                                        double *, double *, double *, cudaStream_t);              \
+    template void launch_fcg<T>(const BlkDev *, int, long, const double *, const double *,        \
+                                const double *, const double *, const T *, double *, double *,   \
+                                double *, double *, T *, const PushDev *, double *, double *,    \
+                                double *, cudaStream_t);                                         \
     template void launch_update<T>(const BlkDev *, int, long, double *, const T *, const PushDev *, \
                                    cudaStream_t);                                                \
     template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);

@@ -88,7 +88,15 @@ void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaS
 template <typename T>
 void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
                         const double *R, const double *P, const double *x, const double *b,
-                        const double *shift, T *rT, double *partial, double *out2, cudaStream_t st);
+                        const double *shift, T *rT, double *r64, double *partial, double *out2,
+                        cudaStream_t st);
+// one flexible-CG update around a V-cycle whose correction is z: new
+// direction p, q = A p, then x += alpha p, r -= alpha q, rT = r; sc[0..3]
+// device scalars (sc[2] = 0 restarts), out_rr[0] = r.r
+template <typename T>
+void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N, const double *R,
+                const double *P, const T *z, double *x, double *pd, double *q, double *r, T *rT,
+                const PushDev *push, double *partial, double *sc, double *out_rr, cudaStream_t st);
 void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
                           double *partial, double *out, cudaStream_t st);
 template <typename T>

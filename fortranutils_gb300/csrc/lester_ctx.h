@@ -43,6 +43,7 @@ struct CycleGraph {
     bool singular = false;
     bool mf = false;
     int tail = 0;
+    int krylov = 0;
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };
@@ -78,6 +79,7 @@ struct Ctx {
     FastSet<float> f32;
     FastSet<double> f64;
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
+    double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
     const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long coef_gen_seen = -1;
     int coef_prec = -1;
@@ -93,8 +95,8 @@ struct Ctx {
     size_t ev_used = 0;
     long prof_launches = 0;
     double prof_ms_acc = 0;
-    // graphs of the fast solvers: [0] FP64, [1] mixed
-    CycleGraph cg[2];
+    // graphs of the fast solvers: [FP64, mixed][defect correction, flexible CG]
+    CycleGraph cg[2][2];
     cudaStream_t cap_stream = nullptr;
     std::vector<cudaEvent_t> *cap_ev = nullptr;  // set while capturing
     // bytes copied between host and device by staged (host-array) calls

@@ -415,7 +415,7 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_flag);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b,
-                  c->E64,   c->N64,   c->R64,   c->P64};
+                  c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq};
     for (void *p : fp) cudaFree(p);
     for (void *p : c->stage_buf) cudaFree(p);
     cudaFree(c->d_offki);
@@ -425,10 +425,11 @@ static void free_ctx(Ctx *c)
     for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : c->ev_solve)
         if (e) cudaEventDestroy(e);
-    for (CycleGraph &G : c->cg) {
-        if (G.exec) cudaGraphExecDestroy(G.exec);
-        for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
-    }
+    for (auto &row : c->cg)
+        for (CycleGraph &G : row) {
+            if (G.exec) cudaGraphExecDestroy(G.exec);
+            for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
+        }
     for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->d_tabpool) cudaFree(c->d_tabpool);
@@ -758,15 +759,18 @@ static void drop_graph(CycleGraph &G)
     G.ev.clear();
 }
 
-// Capture one defect-correction iteration -- V-cycle, p += e, halo of p,
-// FP64 residual and the read-back of its two sums -- as a CUDA graph, so
-// the ~10^2 small launches of the coarse levels cost one graph launch.
-// Re-captured when the arrays or the smoother settings change.
-template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b)
+// Capture one outer iteration as a CUDA graph, so the ~10^2 small launches
+// of the coarse levels cost one graph launch: defect correction (V-cycle,
+// p += e, FP64 residual) or flexible CG (V-cycle, direction and step),
+// then the read-back of the residual sums.  Re-captured when the arrays or
+// the solver settings change.
+template <typename T>
+static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b, bool kry)
 {
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
-        G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail)
+        G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
+        G.krylov == (int)kry)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -784,10 +788,15 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
     cudaError_t mid = cudaSuccess;
     if (e == cudaSuccess) {
         fast_vcycle<T>(c);
-        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                              c.singular ? c.d_small + 8 : nullptr, F.b, c.d_partial, c.d_small,
-                              c.stream);
+        if (kry) {
+            launch_fcg<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, F.x, f, c.d_fp, c.d_fq,
+                          c.d_fr, F.b, L1.d_push, c.d_partial, c.d_small + 16, c.d_small, c.stream);
+        } else {
+            launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                                  c.singular ? c.d_small + 8 : nullptr, F.b, nullptr, c.d_partial,
+                                  c.d_small, c.stream);
+        }
         cudaMemcpyAsync(c.h_small, c.d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
         mid = cudaGetLastError();
         e = cudaStreamEndCapture(c.cap_stream, &graph);
@@ -810,10 +819,26 @@ template <typename T> static int ensure_cycle_graph(Ctx &c, CycleGraph &G, doubl
     G.singular = c.singular;
     G.mf = fset<T>(c).mf;
     G.tail = k.mg_tail;
+    G.krylov = (int)kry;
     return 0;
 }
 
-// defect correction: p <- p + V(b - A p) until ||b - A p|| <= rtol ||b||
+// flexible CG: the vectors r, p, q, zero, and the scalars restarted
+static int fcg_reset(Ctx &c)
+{
+    double **v[3] = {&c.d_fr, &c.d_fp, &c.d_fq};
+    for (double **a : v) {
+        if (!*a) LES_CUDA(cudaMalloc(a, sizeof(double) * c.tot_sg3));
+        LES_CUDA(cudaMemsetAsync(*a, 0, sizeof(double) * c.tot_sg3, c.stream));
+    }
+    LES_CUDA(cudaMemsetAsync(c.d_small + 16, 0, 4 * sizeof(double), c.stream));
+    return 0;
+}
+
+// p <- p + V(b - A p) (defect correction), or flexible CG with the V-cycle
+// as preconditioner, until ||b - A p|| <= rtol ||b||.  krylov 2 starts with
+// defect correction and moves to flexible CG (from the current p) at the
+// first cycle that fails to halve the residual.
 template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, double *b, double *residu,
                                             int prec)
 {
@@ -845,17 +870,23 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
             ncell += (double)(L1.n[ib][0] - 2) * (L1.n[ib][1] - 2) * (L1.n[ib][2] - 2);
         launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, ncell, c.d_partial, c.d_small + 8, c.stream);
     }
+    bool kry = c.c.krylov == 1;
+    const bool may_switch = c.c.krylov == 2;
+    if (kry && (r = fcg_reset(c))) return r;
     launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                          c.singular ? c.d_small + 8 : nullptr, F.b, c.d_partial, c.d_small, c.stream);
+                          c.singular ? c.d_small + 8 : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial,
+                          c.d_small, c.stream);
     STAGE_CHECK("initial residual");
     if ((r = sync_small(c, 2))) return r;
     double r2 = c.h_small[0], b2 = c.h_small[1];
     int it = 0;
     double rel = b2 > 0 ? std::sqrt(r2 / b2) : 0.;
-    CycleGraph &G = c.cg[sizeof(T) == 4 ? 1 : 0];
-    if (b2 > 0 && rel > rtol && (r = ensure_cycle_graph<T>(c, G, f, b))) return r;
-    STAGE_CHECK("graph");
+    CycleGraph *Gs = c.cg[sizeof(T) == 4 ? 1 : 0];
     while (b2 > 0 && rel > rtol && it < maxit) {
+        CycleGraph &G = Gs[kry ? 1 : 0];
+        if ((r = ensure_cycle_graph<T>(c, G, f, b, kry))) return r;
+        STAGE_CHECK("graph");
+        const double rel_prev = rel;
         LES_CUDA(cudaGraphLaunch(G.exec, c.stream));
         count_launch(G.launches);
         LES_CUDA(cudaStreamSynchronize(c.stream));
@@ -870,6 +901,28 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
         rel = std::sqrt(r2 / b2);
         it++;
         if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+        if (may_switch && !kry && rel > rtol && rel > 0.5 * rel_prev) {
+            // the plain cycle has stalled or diverges: flexible CG from here
+            kry = true;
+            if ((r = fcg_reset(c))) return r;
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                                  c.singular ? c.d_small + 8 : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
+                                  c.stream);
+            if ((r = sync_small(c, 2))) return r;
+            rel = std::sqrt(c.h_small[0] / b2);
+            if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+        }
+        if (kry && rel <= rtol) {
+            // the CG residual is updated recursively: confirm with b - A p,
+            // and restart from it (beta = 0) if rounding has drifted
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                                  c.singular ? c.d_small + 8 : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
+                                  c.stream);
+            if ((r = sync_small(c, 2))) return r;
+            r2 = c.h_small[0];
+            rel = std::sqrt(r2 / b2);
+            if (rel > rtol) LES_CUDA(cudaMemsetAsync(c.d_small + 18, 0, sizeof(double), c.stream));
+        }
     }
     {
         cudaError_t ee = cudaGetLastError();

@@ -59,7 +59,7 @@ class Ctrl(C.Structure):
         ("tolf", C.c_double), ("relax_pmg", C.c_double), ("relax_pmgc", C.c_double),
         ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
-        ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int),
+        ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
     ]
 
 
@@ -100,6 +100,7 @@ def default_ctrl(**kw) -> Ctrl:
     c.exact = 1
     c.rb_matfree = 1
     c.mg_tail = 4096
+    c.krylov = 2
     for k, v in kw.items():
         setattr(c, k, v)
     return c

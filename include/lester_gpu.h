@@ -120,6 +120,14 @@ typedef struct lester_ctrl {
     int mg_tail;       /* fast solvers: levels with at most this many
                           interior points (all blocks) run as one single-CTA
                           launch per V-cycle; 0 = one launch per operation */
+    int krylov;        /* fast solvers' outer loop: 0 = defect correction
+                          p += V(b - A p); 1 = flexible conjugate gradients
+                          with the V-cycle as preconditioner (FP64 vectors
+                          and sums; converges where the plain cycle's
+                          coarse-grid correction overshoots, e.g. on
+                          strongly stretched grids); 2 = defect correction
+                          until a cycle fails to halve the residual, then
+                          flexible CG from the current p */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */

@@ -161,3 +161,92 @@ def test_bad_configuration_refused(finalize):
             S.adjoint_run(g, 4, *grad, **kw)
     with pytest.raises(L.LesterError):
         S.adjoint_run(g.to("numpy"), 2, *grad)
+
+
+def channel_state(shape=(128, 96, 64), beta=2.2, re_tau=180.0, sigma=0.1, seed=4, cfl=0.3):
+    """Stretched channel: laminar profile u = 1 - y^2 (laminar friction
+    Reynolds number sqrt(2 / visc) = re_tau) plus N(0, sigma^2) noise on
+    u, v, w; dt from the initial CFL number (cflest-style: max over cells
+    of |u|/dx + |v|/dy + |w|/dz).  Returns (case, ctrl, device state
+    after one ordinary step)."""
+    import torch
+    from fortranutils_gb300 import grid
+    case = grid.box_case(*shape, ybc=L.BCT_WALL, beta=beta)
+    s = S.new_state(case, {n: np.zeros(case.n2) for n in L.METRIC_NAMES}, np.zeros(case.n1k),
+                    np.zeros(case.n1k))
+    S.init_channel(s, seed=seed, sigma=sigma)
+    x, y, z = case.coordinates()
+    b = case.blocks[0]
+    dx = np.diff(b.x[1:b.n[0]]).min()
+    dy = np.diff(b.y[1:b.n[1]])
+    dz = np.diff(b.z[1:b.n[2]]).min()
+    u, v, w = (case.block_view(s[n], 0)[1:-1, 1:-1, 1:-1] for n in "uvw")
+    c = np.abs(u) / dx + np.abs(v) / dy[None, :, None] + np.abs(w) / dz
+    ctrl = L.default_ctrl(dtime=cfl / c.max(), model=0, psolve=L.PSOLVE_FP64, rtol=1e-12, max_outer=400,
+                          visc=2.0 / re_tau ** 2)
+    L.gpu_init(case.geom(), ctrl)
+    g = s.to("torch")
+    xt, yt, zt = (torch.from_numpy(a).cuda() for a in (x, y, z))
+    L.comp_metric(xt, yt, zt, g["metric"], g["dkp"], g["dkw"])
+    for n in ("u", "v", "w"):
+        L.swap_sc(0, 1, g[n], mg_or_sg=2)
+    assert S.step(g, 1) == 0
+    return case, ctrl, g
+
+
+def test_channel_gradient_against_fd_and_tangent(finalize):
+    """128x96x64 stretched channel (tanh beta 2.2, periodic x/z), 40 steps,
+    J over steps 21-40, FP64 solve, checkpoints every 10 steps: the adjoint
+    gradient against the tangent and against central differences along 16
+    seeded directions (seeds 400-415); the finite-difference step is picked
+    by a sweep on the first direction."""
+    import time
+    import torch
+    case, ctrl, g = channel_state()
+    nst, j0, j1 = 40, 21, 40
+    grad = [torch.zeros_like(g["u"]) for _ in range(3)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = S.adjoint_run(g, nst, *grad, j_first=j0, j_last=j1, checkpoint=10)
+    t_adj = time.perf_counter() - t0
+    zero = [torch.zeros_like(g["u"]) for _ in range(3)]
+
+    def J_at(f):
+        L.gpu_set_body_force(*f)
+        try:
+            return S.tangent_run(g, nst, *zero, j_first=j0, j_last=j1)[0]
+        finally:
+            L.gpu_set_body_force()
+
+    def dirn(seed):
+        rng = np.random.default_rng(seed)
+        out = []
+        for _ in range(3):
+            a = np.zeros(case.n3_sg)
+            v = case.block_view(a, 0)
+            v[1:-1, 1:-1, 1:-1] = rng.standard_normal(v[1:-1, 1:-1, 1:-1].shape)
+            out.append(torch.from_numpy(a).cuda())
+        return out
+
+    worst_tlm = worst_fd = 0.0
+    eps_best = None
+    for seed in range(400, 416):
+        d = dirn(seed)
+        Jt, dJ = S.tangent_run(g, nst, *d, j_first=j0, j_last=j1)
+        assert abs(Jt - J) <= 1e-12 * abs(J)
+        adj = dot(grad, d)
+        worst_tlm = max(worst_tlm, abs(adj - dJ) / abs(dJ))
+        if eps_best is None:
+            errs = {}
+            for eps in (1e-1, 1e-2, 1e-3, 1e-4, 1e-5):
+                fd = (J_at([eps * x for x in d]) - J_at([-eps * x for x in d])) / (2 * eps)
+                errs[eps] = abs(fd - dJ) / abs(dJ)
+            eps_best = min(errs, key=errs.get)
+            print(f"\nFD step sweep (relative error vs tangent): {errs}")
+        fd = (J_at([eps_best * x for x in d]) - J_at([-eps_best * x for x in d])) / (2 * eps_best)
+        worst_fd = max(worst_fd, abs(fd - dJ) / abs(dJ))
+    print(f"channel 128x96x64, 40 steps, dt {ctrl.dtime:.3e}: J = {J:.10e}, adjoint run {t_adj:.2f} s; "
+          f"16 directions: max rel |<grad,d> - dJ_tlm| = {worst_tlm:.2e}, max rel |FD - dJ_tlm| = "
+          f"{worst_fd:.2e} (eps {eps_best:g})")
+    assert worst_tlm <= 1e-9
+    assert worst_fd <= 1e-4
