@@ -46,6 +46,24 @@ DOMAIN = (30.0, 30.0, 15.0)
 EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
+# other workloads (--workload): the plain channel of the reference's own
+# CPU-runnable case, and the large stretched channel
+WORKLOADS = {
+    "mixing": dict(shape=SHAPE, desc=WORKLOAD),
+    "channel64": dict(shape=(64, 64, 64), beta=None, nummgl=4, seed=1,
+                      desc="plane channel 64^3 cells, 2pi x 2 x pi, walls in y, periodic x/z, uniform "
+                           "grid, Re_b 2800, Smagorinsky Cs 0.1, constant density, dt from CFL 0.3 and "
+                           "diffusion number 0.2, "
+                           "4 multigrid levels, full lester_step, Poisson to 1e-8"),
+    "poisson32": dict(shape=(0, 0, 0), seed=5,
+                      desc="32 independent Poisson boxes in one solve, sides drawn from 32,40,...,128 "
+                           "cells per axis (seed 5), cubic cells, periodic x/z and Neumann y, sources "
+                           "N(0,1) minus their mean, to 1e-8"),
+    "channel512": dict(shape=(512, 384, 256), beta=2.2, nummgl=0, seed=5,
+                       desc="stretched plane channel 512x384x256 cells, 2pi x 2 x pi, tanh walls "
+                            "beta 2.2, periodic x/z, Re_b 2800, Smagorinsky Cs 0.1, constant "
+                            "density, dt from CFL 0.3 and diffusion number 0.2, full lester_step, Poisson to 1e-8"),
+}
 
 
 # ----------------------------------------------------------------- helpers
@@ -103,33 +121,55 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def make_case(shape=SHAPE):
+def make_case(shape=SHAPE, wl="mixing"):
     from fortranutils_gb300 import grid, lester as L
     ni, nj, nk = shape
-    lx, ly, lz = DOMAIN
-    return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
+    if wl == "mixing":
+        lx, ly, lz = DOMAIN
+        return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
+    w = WORKLOADS[wl]
+    return grid.box_case(ni, nj, nk, ybc=L.BCT_WALL, beta=w["beta"], nummgl=w["nummgl"])
 
 
-def make_ctrl(psolve, krylov=2):
+def cfl_dt(case, s, cfl=0.3, dfs=0.2, visc=1.0 / 2800.0):
+    """dt from the initial field (cflest-style): the smaller of cfl / max
+    over cells of |u|/dx + |v|/dy + |w|/dz and, since the predictor's
+    diffusion is explicit, dfs / max of visc (1/dx^2 + 1/dy^2 + 1/dz^2)."""
+    b = case.blocks[0]
+    dx = np.diff(b.x[1:b.n[0]]).min()
+    dy = np.diff(b.y[1:b.n[1]])
+    dz = np.diff(b.z[1:b.n[2]]).min()
+    u, v, w = (case.block_view(s[n], 0)[1:-1, 1:-1, 1:-1] for n in "uvw")
+    c = np.abs(u) / dx + np.abs(v) / dy[None, :, None] + np.abs(w) / dz
+    d = visc * (1.0 / dx ** 2 + 1.0 / dy.min() ** 2 + 1.0 / dz ** 2)
+    return min(cfl / float(c.max()), dfs / d)
+
+
+def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     from fortranutils_gb300 import lester as L
-    return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
-                          rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
+    if wl == "mixing":
+        return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
+                              rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
+    return L.default_ctrl(dtime=dtime, model=1, csles=0.1, rholo=1.0, rhohi=1.0, visc=1.0 / 2800.0,
+                          psolve=psolve, rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
 
 
-def host_state(case, ctrl):
+def host_state(case, ctrl, wl="mixing"):
     """Initial fields (numpy); metrics left zero for the caller to fill."""
     from fortranutils_gb300 import lester as L, state as S
     c = case
     s = S.new_state(c, {n: np.zeros(c.n2) for n in L.METRIC_NAMES}, np.zeros(c.n1k),
                     np.zeros(c.n1k))
-    return S.init_mixing_layer(s, seed=2, sigma=0.02, rholo=ctrl.rholo, rhohi=ctrl.rhohi)
+    if wl == "mixing":
+        return S.init_mixing_layer(s, seed=2, sigma=0.02, rholo=ctrl.rholo, rhohi=ctrl.rhohi)
+    return S.init_channel(s, seed=WORKLOADS[wl]["seed"], sigma=0.05)
 
 
-def device_state(case, ctrl):
+def device_state(case, ctrl, wl="mixing"):
     """Device-resident state: metrics by comp_metric, halos exchanged."""
     import torch
     from fortranutils_gb300 import lester as L
-    g = host_state(case, ctrl).to("torch")
+    g = host_state(case, ctrl, wl).to("torch")
     x, y, z = (torch.from_numpy(a).cuda() for a in case.coordinates())
     L.comp_metric(x, y, z, g["metric"], g["dkp"], g["dkw"])
     for n in ("u", "v", "w", "sc1", "rho", "rhonp1", "rhonm1"):
@@ -166,14 +206,16 @@ def run_gpu(args):
     from fortranutils_gb300 import build, lester as L, state as S
     build.build()
     torch.cuda.set_device(0)
-    case = make_case(tuple(args.shape))
+    wl = args.workload
+    case = make_case(tuple(args.shape), wl)
+    dtime = None if wl == "mixing" else cfl_dt(case, host_state(case, make_ctrl(0, wl=wl, dtime=1.0), wl))
     res = {}
     modes = [("fp64", L.PSOLVE_FP64), ("mixed", L.PSOLVE_MIXED)]
     modes = [m for m in modes if args.mode in ("both", m[0])]
     for mode, ps in modes:
-        ctrl = make_ctrl(ps, {"dc": 0, "fcg": 1, "auto": 2}[args.outer])
+        ctrl = make_ctrl(ps, {"dc": 0, "fcg": 1, "auto": 2}[args.outer], wl, dtime)
         L.gpu_init(case.geom(), ctrl)
-        g = device_state(case, ctrl)
+        g = device_state(case, ctrl, wl)
         stream = torch.cuda.current_stream()
         istep = 0
         for _ in range(args.warmup):
@@ -208,18 +250,18 @@ def run_gpu(args):
                      "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl}
         del g
         if mode == "mixed" and not args.no_e2e:
-            res[mode]["e2e"] = run_e2e(args, case, ctrl)
+            res[mode]["e2e"] = run_e2e(args, case, ctrl, wl)
         L.gpu_finalize()
         torch.cuda.empty_cache()
     return case, res
 
 
-def run_e2e(args, case, ctrl):
+def run_e2e(args, case, ctrl, wl="mixing"):
     """lester_step with every field in pinned host memory: each call copies
     all its arrays in and back once (strict drop-in)."""
     import torch
     from fortranutils_gb300 import lester as L, state as S
-    g = device_state(case, ctrl)
+    g = device_state(case, ctrl, wl)
     h = g.to("pinned")
     del g
     torch.cuda.empty_cache()
@@ -238,18 +280,18 @@ def run_e2e(args, case, ctrl):
 
 
 # ------------------------------------------------------------- CPU arm
-def run_cpu_steps(case, nsteps: int, warmup: int = 0):
+def run_cpu_steps(case, nsteps: int, warmup: int = 0, wl: str = "mixing", dtime=None):
     """The oracle on the same workload: orc_step with the reference's own
     solver settings (nummgits 5 V(1,1) cycles of lexicographic SOR).  One
     thread.  Returns seconds per timed step."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
     from fortranutils_gb300 import lester as L
-    ctrl = make_ctrl(L.PSOLVE_REFERENCE)
+    ctrl = make_ctrl(L.PSOLVE_REFERENCE, wl=wl, dtime=dtime)
     orc = O.Oracle(case)
     x, y, z = case.coordinates()
     met, dkp, dkw = orc.comp_metric(x, y, z)
-    s = host_state(case, ctrl)
+    s = host_state(case, ctrl, wl)
     for i, n in enumerate(L.METRIC_NAMES):
         s["metric"][n][:] = met[i]
     s["dkp"][:] = dkp
@@ -267,6 +309,65 @@ def run_cpu_steps(case, nsteps: int, warmup: int = 0):
         istep += 1
         orc.step(mg, k, istep, istep, s)
     return (time.perf_counter() - t0) / nsteps, ctrl.nummgits
+
+
+def run_poisson(args):
+    """Batched Poisson solves: 32 unlinked boxes of uneven sizes as one
+    multiblock grid, every multigrid operation one launch over all boxes."""
+    import torch
+    from fortranutils_gb300 import build, grid, lester as L
+    build.build()
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(WORKLOADS["poisson32"]["seed"])
+    sizes = [tuple(int(v) for v in rng.choice(np.arange(32, 129, 8), 3)) for _ in range(32)]
+    case = grid.boxes_case(sizes, h=1.0 / 64.0)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    b = np.zeros(case.n3_mg)
+    for ib in range(len(case.blocks)):
+        v = case.block_view(b, ib, 0)[1:-1, 1:-1, 1:-1]
+        v[...] = rng.standard_normal(v.shape)
+        v -= v.mean()
+    out = {}
+    for mode, ps in (("fp64", L.PSOLVE_FP64), ("mixed", L.PSOLVE_MIXED)):
+        ctrl = L.default_ctrl(psolve=ps, rtol=1e-8, max_outer=200)
+        L.gpu_init(case.geom(), ctrl)
+        met = {n: torch.zeros(case.n2, dtype=torch.float64, device="cuda") for n in L.METRIC_NAMES}
+        dkp = torch.zeros(case.n1k, dtype=torch.float64, device="cuda")
+        dkw = torch.zeros_like(dkp)
+        L.comp_metric(*(dev(a) for a in case.coordinates()), met, dkp, dkw)
+        a = [torch.zeros(case.n3_mg, dtype=torch.float64, device="cuda") for _ in range(7)]
+        L.coeff_p(met["diu"], met["djv"], met["rdiv"], met["rdju"], met["didjp"], met["rp"], dkp, dkw, *a)
+        bd, rd = dev(b), torch.zeros_like(a[0])
+        fd = torch.zeros_like(a[0])
+        for _ in range(args.warmup):
+            fd.zero_()
+            L.lmg_solve(*a, fd, bd.clone(), rd)
+        ms, cyc, rel = [], [], []
+        for _ in range(args.steps):
+            fd.zero_()
+            bc = bd.clone()
+            L.lmg_solve(*a, fd, bc, rd)
+            st = L.gpu_solve_stats()
+            ms.append(L.gpu_solve_time())
+            cyc.append(st["cycles"])
+            rel.append(st["relres"])
+        out[mode] = {"solve_ms": float(np.mean(ms)), "cycles": float(np.mean(cyc)),
+                     "relres_max": float(np.max(rel)),
+                     "vcycle_ms": float(np.mean(ms)) / max(float(np.mean(cyc)), 1.0)}
+        L.gpu_finalize()
+        del a, bd, rd, fd, met
+        torch.cuda.empty_cache()
+    ncell = case.cells()
+    line = {"metric": "Poisson solve ms to 1e-8, 32 independent boxes (mixed; FP64 beside)",
+            "value": out["mixed"]["solve_ms"], "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "dtype": "f32/f64",
+            "data": "synthetic (seeded numpy default_rng, seed 5)",
+            "config": {"workload": WORKLOADS["poisson32"]["desc"], "cells": ncell,
+                       "levels": case.levels and len(case.levels), "sizes": sizes},
+            "mixed": out["mixed"], "fp64": out["fp64"],
+            "solve_speedup_mixed_vs_fp64": out["fp64"]["solve_ms"] / out["mixed"]["solve_ms"],
+            "mcells_per_s_mixed": ncell / (out["mixed"]["solve_ms"] * 1e-3) / 1e6}
+    print(json.dumps(line), flush=True)
 
 
 def reference_line(args, rank):
@@ -304,9 +405,14 @@ def main():
     ap.add_argument("--outer", default="auto", choices=["auto", "fcg", "dc"],
                     help="fast solvers' outer loop: defect correction switching to flexible CG "
                          "when a cycle stalls (auto), flexible CG, or defect correction")
-    ap.add_argument("--shape", type=int, nargs=3, default=list(SHAPE),
-                    help="cells per axis (smaller shapes are for profiling only)")
+    ap.add_argument("--workload", default="mixing", choices=list(WORKLOADS),
+                    help="mixing: the headline mixing layer; channel64: the 64^3 plain channel; "
+                         "channel512: the 512x384x256 stretched channel")
+    ap.add_argument("--shape", type=int, nargs=3, default=None,
+                    help="cells per axis (other shapes than the workload's are for profiling only)")
     args = ap.parse_args()
+    if args.shape is None:
+        args.shape = list(WORKLOADS[args.workload]["shape"])
     rank, world, local = dist_env()
     if world > 1:
         # the path runs on one GPU; extra ranks are independent replicas
@@ -314,9 +420,14 @@ def main():
     if args.impl == "reference":
         reference_line(args, rank)
         return
+    if args.workload == "poisson32":
+        if rank == 0:
+            run_poisson(args)
+        return
     case, res = run_gpu(args)
     ncell = case.cells()
-    if args.mode != "both" or args.no_e2e or tuple(args.shape) != SHAPE:
+    wl = args.workload
+    if args.mode != "both" or args.no_e2e or tuple(args.shape) != WORKLOADS[wl]["shape"]:
         print(json.dumps({k: {kk: vv for kk, vv in v.items() if kk not in ("clocks", "ctrl")}
                           for k, v in res.items()}), flush=True)
         return
@@ -339,8 +450,8 @@ def main():
     step_gbs = {m: step_bytes(m, r["cycles"], sweeps, kry) * ncell / (r["ms_per_step"] * 1e-3) / 1e9
                 for m, r in (("mixed", mx), ("fp64", fp))}
     cpu = None
-    if not args.no_cpu and rank == 0:
-        sps, nmg = run_cpu_steps(case, 1)
+    if not args.no_cpu and rank == 0 and ncell <= 10_000_000:
+        sps, nmg = run_cpu_steps(case, 1, wl=wl, dtime=mx["ctrl"].dtime)
         cpu = {"value": ncell / sps / 1e6, "unit": "Mcell-steps/s", "cores": 1, "kind": "port",
                "sample": f"1 full step of the same workload, reference solver settings "
                          f"({nmg} V-cycles, lexicographic SOR), {sps:.1f} s"}
@@ -349,9 +460,10 @@ def main():
         "metric": METRIC, "value": value, "unit": "Mcell-steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": mx["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64",
-        "data": "synthetic (seeded numpy default_rng, seed 2)",
-        "config": {"workload": WORKLOAD, "cells": ncell,
-                   "l2": "inputs larger than L2 (~2 GB working set), no flush",
+        "data": f"synthetic (seeded numpy default_rng, seed {WORKLOADS[wl].get('seed', 2)})",
+        "config": {"workload": WORKLOADS[wl]["desc"], "cells": ncell,
+                   "l2": ("inputs larger than L2, no flush" if ncell * 8 * 20 > 129e6 else
+                          "working set smaller than the 129 MB L2 (not flushed): a small-case figure"),
                    "parallelism": "replicas" if world > 1 else "1 GPU",
                    "outer_loop": {"auto": "defect correction, flexible CG when a cycle stalls",
                                   "fcg": "flexible CG", "dc": "defect correction"}[args.outer]},

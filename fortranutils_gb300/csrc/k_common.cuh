@@ -16,6 +16,8 @@
 #define LES_BCT_PERIODIC_D 12
 #define LES_BCT_INTERFACE_D 13
 
+constexpr int kMaxBlk = 64;  // blocks per grid (code/dim.inc maxbl, LES_MAXBL)
+
 struct BlkDev {
     int n[3];      // nip1, njp1, nkp1 (points incl. ghosts)
     int bc[6];     // W E S N L R
@@ -24,6 +26,8 @@ struct BlkDev {
     long off2;     // 0-based start in a 2-D (i,j) metric at this level
     long off1k;    // 0-based start in a 1-D k metric at this level
     long ncell;    // interior points (nip1-2)(njp1-2)(nkp1-2)
+    int comp;      // connected component (blocks joined by periodic/interface links)
+    int pad_;
 };
 
 // One periodic/interface face of swap_sc (code/swap_sc0.F:92-133 and

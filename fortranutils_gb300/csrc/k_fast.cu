@@ -358,6 +358,74 @@ __global__ void k_halo_fast(const FaceDev *__restrict__ fc, T *__restrict__ x)
 // residual + restriction, coarsest-level mean removal and sweeps,
 // prolongation -- as phases of one CTA separated by __syncthreads, the same
 // operations in the same order as the per-level launches.
+// per-block sums sb[] (block order) -> mean[b] = the interior mean over the
+// connected component of block b; single thread, fixed order
+__device__ __forceinline__ void comp_means_from_sums(const BlkDev *__restrict__ blk, int nb,
+                                                     const double *sb, double *mean)
+{
+    double cs[kMaxBlk], cn[kMaxBlk];
+    for (int q = 0; q < nb; q++) cs[q] = cn[q] = 0.;
+    for (int b = 0; b < nb; b++) {
+        const int cp = blk[b].comp;
+        cs[cp] += sb[b];
+        cn[cp] += (double)blk[b].ncell;
+    }
+    for (int b = 0; b < nb; b++) {
+        const int cp = blk[b].comp;
+        mean[b] = cn[cp] > 0. ? cs[cp] / cn[cp] : 0.;
+    }
+}
+
+// per-block partial sums of k_interior_sum (gx per block) -> out[b], the
+// interior mean over block b's component.  One CTA.
+__global__ void k_comp_mean_final(const double *__restrict__ partial, int gx, int nb,
+                                  const BlkDev *__restrict__ blk, double *__restrict__ out)
+{
+    __shared__ double sb[kMaxBlk];
+    __shared__ double r[1];
+    for (int b = 0; b < nb; b++) {
+        double v[1] = {0.};
+        for (int t = threadIdx.x; t < gx; t += blockDim.x) v[0] += partial[(long)b * gx + t];
+        block_reduce_store<1>(v, r);
+        __syncthreads();
+        if (threadIdx.x == 0) sb[b] = r[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) comp_means_from_sums(blk, nb, sb, out);
+}
+
+// subtract from b, on every interior point, the mean of b over the point's
+// component (all threads of the CTA take part)
+template <typename T>
+__device__ void remove_comp_means(const BlkDev *__restrict__ blk, int nb, T *__restrict__ bb)
+{
+    __shared__ double sb[kMaxBlk], mean[kMaxBlk];
+    __shared__ double r[1];
+    for (int ib = 0; ib < nb; ib++) {
+        const BlkDev b = blk[ib];
+        double v[1] = {0.};
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            v[0] += (double)bb[decode_interior(b, q, i, j, k)];
+        }
+        block_reduce_store<1>(v, r);
+        __syncthreads();
+        if (threadIdx.x == 0) sb[ib] = r[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) comp_means_from_sums(blk, nb, sb, mean);
+    __syncthreads();
+    for (int ib = 0; ib < nb; ib++) {
+        const BlkDev b = blk[ib];
+        const T m = (T)mean[ib];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            bb[decode_interior(b, q, i, j, k)] -= m;
+        }
+    }
+    __syncthreads();
+}
+
 template <typename T>
 __device__ void tail_smooth(const VLev &L, int nb, int nsweep, T omega, const T *E, const T *N,
                             const T *R, const T *D, T *x, const T *bb, const MfTab<T> &mf)
@@ -408,29 +476,7 @@ __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int 
         }
         __syncthreads();
     }
-    if (singular) {
-        double v[2] = {0., 0.};
-        for (int bi = 0; bi < nb; bi++) {
-            const BlkDev b = lv[L].blk[bi];
-            for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
-                int i, j, k;
-                v[0] += (double)bb[decode_interior(b, q, i, j, k)];
-                v[1] += 1.0;
-            }
-        }
-        __shared__ double tot[2];
-        block_reduce_store<2>(v, tot);
-        __syncthreads();
-        const T mean = (T)(tot[0] / tot[1]);
-        for (int bi = 0; bi < nb; bi++) {
-            const BlkDev b = lv[L].blk[bi];
-            for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
-                int i, j, k;
-                bb[decode_interior(b, q, i, j, k)] -= mean;
-            }
-        }
-        __syncthreads();
-    }
+    if (singular) remove_comp_means<T>(lv[L].blk, nb, bb);
     tail_smooth(lv[L], nb, L == 1 ? pre : crs, omega, E, N, R, D, x, bb, mf);
     for (int lev = L - 1; lev >= l0; lev--) {
         for (int bi = 0; bi < nb; bi++) {
@@ -461,7 +507,7 @@ __global__ void __launch_bounds__(256) k_resid_outer(
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double v[2] = {0., 0.};
-    const double s0 = shift ? *shift : 0.;
+    const double s0 = shift ? shift[blockIdx.y] : 0.;
     for (; q < b.ncell; q += (long)gridDim.x * blockDim.x) {
         int i, j, k;
         long p = decode_interior(b, q, i, j, k);
@@ -513,46 +559,14 @@ __global__ void __launch_bounds__(256) k_interior_sum(const BlkDev *__restrict__
     block_reduce_store<1>(v, partial + blockIdx.y * (long)gridDim.x + blockIdx.x);
 }
 
-__global__ void k_mean_final(const double *__restrict__ partial, long nparts, double ncell,
-                             double *__restrict__ out)
-{
-    double v[1] = {0.};
-    for (long t = threadIdx.x; t < nparts; t += blockDim.x) v[0] += partial[t];
-    __shared__ double r[1];
-    block_reduce_store<1>(v, r);
-    __syncthreads();
-    if (threadIdx.x == 0) out[0] = r[0] / ncell;
-}
-
 // Coarsest level of a singular (pure Neumann / periodic) operator: remove
-// the mean of the right-hand side over all interior points so the coarse
-// problem is compatible and its smoothing cannot drift along the constant
-// null vector.  One CTA; the level has a few hundred points at most.
+// the mean of the right-hand side over each component's interior points so
+// the coarse problem is compatible and its smoothing cannot drift along the
+// constant null vectors.  One CTA; the level has a few hundred points at most.
 template <typename T>
 __global__ void k_coarse_mean(const BlkDev *__restrict__ blk, int nb, T *__restrict__ bb)
 {
-    double v[2] = {0., 0.};
-    for (int ib = 0; ib < nb; ib++) {
-        const BlkDev b = blk[ib];
-        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
-            int i, j, k;
-            long p = decode_interior(b, q, i, j, k);
-            v[0] += (double)bb[p];
-            v[1] += 1.0;
-        }
-    }
-    __shared__ double tot[2];
-    block_reduce_store<2>(v, tot);
-    __syncthreads();
-    T mean = (T)(tot[0] / tot[1]);
-    for (int ib = 0; ib < nb; ib++) {
-        const BlkDev b = blk[ib];
-        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
-            int i, j, k;
-            long p = decode_interior(b, q, i, j, k);
-            bb[p] -= mean;
-        }
-    }
+    remove_comp_means<T>(blk, nb, bb);
 }
 
 // p += e on the interior of level 1
@@ -745,14 +759,14 @@ void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const 
     count_launch(6);
 }
 
-void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
-                          double *partial, double *out, cudaStream_t st)
+void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double *partial,
+                          double *out, cudaStream_t st)
 {
     unsigned gx = nb_(maxcell, 256);
     unsigned cap = (unsigned)((1216 + nb - 1) / nb);
     if (gx > cap) gx = cap;
     k_interior_sum<<<dim3(gx, nb), 256, 0, st>>>(blk, b, partial);
-    k_mean_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, ncell, out);
+    k_comp_mean_final<<<1, 256, 0, st>>>(partial, (int)gx, nb, blk, out);
     count_launch(2);
 }
 

@@ -97,8 +97,9 @@ template <typename T>
 void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N, const double *R,
                 const double *P, const T *z, double *x, double *pd, double *q, double *r, T *rT,
                 const PushDev *push, double *partial, double *sc, double *out_rr, cudaStream_t st);
-void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double ncell,
-                          double *partial, double *out, cudaStream_t st);
+// out[b] = interior mean of the level-1 field over block b's component
+void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double *partial,
+                          double *out, cudaStream_t st);
 template <typename T>
 void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, const PushDev *push,
                    cudaStream_t st);

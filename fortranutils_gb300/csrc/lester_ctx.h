@@ -80,6 +80,8 @@ struct Ctx {
     FastSet<double> f64;
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
+    int ncomp = 1;                  // connected components of the block graph
+    double *d_bmean = nullptr;      // per block: interior mean of b over its component
     const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long coef_gen_seen = -1;
     int coef_prec = -1;

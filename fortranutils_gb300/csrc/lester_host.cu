@@ -314,10 +314,34 @@ static int build_faces(Ctx &c)
             LES_CUDA(cudaMalloc(&L.d_face, sizeof(FaceDev) * fv.size()));
             LES_CUDA(cudaMemcpy(L.d_face, fv.data(), sizeof(FaceDev) * fv.size(), cudaMemcpyHostToDevice));
         }
-        // block descriptors
+        // block descriptors; components: blocks joined by periodic or
+        // interface links (independent boxes each have their own
+        // constant null vector when the operator is singular)
+        std::vector<int> root(nb + 1);
+        for (int b = 1; b <= nb; b++) root[b] = b;
+        auto find = [&](int b) {
+            while (root[b] != b) b = root[b] = root[root[b]];
+            return b;
+        };
+        for (int b = 1; b <= nb; b++)
+            for (int s2 = 0; s2 < 6; s2++)
+                if (per_int(g.bl_bc[b - 1][s2])) {
+                    int bn = g.bl2bl[b - 1][s2];
+                    if (bn >= 1 && bn <= nb) root[find(b)] = find(bn);
+                }
+        std::vector<int> compid(nb + 1, -1);
+        int ncomp = 0;
+        for (int b = 1; b <= nb; b++) {
+            int r = find(b);
+            if (compid[r] < 0) compid[r] = ncomp++;
+            compid[b] = compid[r];
+        }
+        c.ncomp = ncomp;
         std::vector<BlkDev> bv(nb);
         for (int b = 1; b <= nb; b++) {
             BlkDev &d = bv[b - 1];
+            d.comp = compid[b];
+            d.pad_ = 0;
             for (int a = 0; a < 3; a++) {
                 d.n[a] = L.n[b][a];
                 d.mult[a] = L.mult[b][a];
@@ -415,7 +439,7 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_flag);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b,
-                  c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq};
+                  c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean};
     for (void *p : fp) cudaFree(p);
     for (void *p : c->stage_buf) cudaFree(p);
     cudaFree(c->d_offki);
@@ -726,6 +750,10 @@ template <typename T> static void fast_vcycle(Ctx &c)
     int L = c.nummgl;
     int pre = c.c.rb_sweeps > 0 ? c.c.rb_sweeps : 1;
     int crs = c.c.rb_coarse > 0 ? c.c.rb_coarse : 20;
+    // the coarsest level needs O(n) SOR sweeps for its n points per axis:
+    // at least four per point of its largest interior extent
+    for (int b = 1; b <= c.g.numbl; b++)
+        for (int a = 0; a < 3; a++) crs = std::max(crs, 4 * (c.lv[L].n[b][a] - 2));
     const MfTab<T> mf = F.mf ? F.tab : MfTab<T>();
     const int l0 = tail_level(c);
     const int Lr = l0 ? l0 : L;  // levels below Lr run as per-level launches
@@ -794,7 +822,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
         } else {
             launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                                  c.singular ? c.d_small + 8 : nullptr, F.b, nullptr, c.d_partial,
+                                  c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial,
                                   c.d_small, c.stream);
         }
         cudaMemcpyAsync(c.h_small, c.d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream);
@@ -862,19 +890,18 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
     STAGE_CHECK("initial halo");
     // singular operator: drive the residual of the compatible part of b
-    // (b minus its interior mean, kept in d_small[8]); the constant part
+    // (b minus its interior mean over each connected component of blocks,
+    // per block in d_bmean); the constant part
     // of p is fixed afterwards by p_ref_subtract, as in the reference
     if (c.singular) {
-        double ncell = 0;
-        for (int ib = 1; ib <= nb; ib++)
-            ncell += (double)(L1.n[ib][0] - 2) * (L1.n[ib][1] - 2) * (L1.n[ib][2] - 2);
-        launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, ncell, c.d_partial, c.d_small + 8, c.stream);
+        if (!c.d_bmean) LES_CUDA(cudaMalloc(&c.d_bmean, sizeof(double) * LES_MAXBL));
+        launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, c.d_partial, c.d_bmean, c.stream);
     }
     bool kry = c.c.krylov == 1;
     const bool may_switch = c.c.krylov == 2;
     if (kry && (r = fcg_reset(c))) return r;
     launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                          c.singular ? c.d_small + 8 : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial,
+                          c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial,
                           c.d_small, c.stream);
     STAGE_CHECK("initial residual");
     if ((r = sync_small(c, 2))) return r;
@@ -906,7 +933,7 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
             kry = true;
             if ((r = fcg_reset(c))) return r;
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                                  c.singular ? c.d_small + 8 : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
+                                  c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
                                   c.stream);
             if ((r = sync_small(c, 2))) return r;
             rel = std::sqrt(c.h_small[0] / b2);
@@ -916,7 +943,7 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
             // the CG residual is updated recursively: confirm with b - A p,
             // and restart from it (beta = 0) if rounding has drifted
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                                  c.singular ? c.d_small + 8 : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
+                                  c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
                                   c.stream);
             if ((r = sync_small(c, 2))) return r;
             r2 = c.h_small[0];

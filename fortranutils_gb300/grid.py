@@ -224,3 +224,21 @@ def two_block_case(ni1: int, ni2: int, nj: int, nk: int, ybc: int = L.BCT_WALL,
     b2 = Block(n=(ni2 + 2, nj + 2, nk + 2), bc=[I, I, ybc, ybc, P, P],
                link=[(1, 2), (1, 1), (0, 0), (0, 0), (2, 6), (2, 5)], x=x2, y=yv, z=zv)
     return Case(blocks=[b1, b2], maxmgl=maxmgl, nummgl=nummgl).setup()
+
+
+def boxes_case(sizes, ybc: int = L.BCT_WALL, h: float | None = None, maxmgl: int = 16,
+               nummgl: int = 0) -> Case:
+    """Independent boxes, one block each: (ni, nj, nk) cells, each periodic
+    in x and z onto itself and bounded in y by `ybc` sides, on
+    [0, 2 pi] x [-1, 1] x [0, pi], or with cubic cells of side h on
+    [0, ni h] x [-nj h / 2, nj h / 2] x [0, nk h].  No block links to
+    another, so a singular pressure operator has one constant null vector
+    per box."""
+    blocks = []
+    for ib, (ni, nj, nk) in enumerate(sizes, start=1):
+        link = [(ib, 2), (ib, 1), (0, 0), (0, 0), (ib, 6), (ib, 5)]
+        P = L.BCT_PERIODIC
+        lx, ly, lz = (2 * np.pi, 2.0, np.pi) if h is None else (ni * h, nj * h, nk * h)
+        blocks.append(Block(n=(ni + 2, nj + 2, nk + 2), bc=[P, P, ybc, ybc, P, P], link=link,
+                            x=_axis(ni, 0.0, lx), y=_axis(nj, -ly / 2, ly / 2), z=_axis(nk, 0.0, lz)))
+    return Case(blocks=blocks, maxmgl=maxmgl, nummgl=nummgl).setup()

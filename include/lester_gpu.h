@@ -106,7 +106,8 @@ typedef struct lester_ctrl {
                           interior mean, the only part any p can match */
     int max_outer;     /* fast solvers: maximum V-cycles */
     int rb_sweeps;     /* fast solvers: red-black sweeps per smoothing step */
-    int rb_coarse;     /* fast solvers: sweeps on the coarsest level */
+    int rb_coarse;     /* fast solvers: sweeps on the coarsest level (at
+                          least 4 per point of its largest extent) */
     double rb_omega;   /* fast solvers: SOR factor */
     int exact;         /* FP64 physics kernels (predictor, eddy viscosity,
                           scalar): 1 = the reference's operation order, no
