@@ -42,6 +42,8 @@ UNITS = {
     "lester_noalloc": ("lester_noalloc.cu", ["-fmad=false"]),
     "k_adjoint": ("k_adjoint.cu", ["-fmad=false"]),
     "lester_adjoint": ("lester_adjoint.cu", []),
+    "k_outflow": ("k_outflow.cu", ["-fmad=false"]),
+    "lester_outflow": ("lester_outflow.cu", []),
 }
 
 

@@ -30,6 +30,27 @@ struct BlkDev {
     int pad_;
 };
 
+// One convective-outflow or fixed-inflow side at level 1: its exit plane
+// along axis d1 (conv_exitbc.F:141-143) and, per variable 1..3, the
+// set_loop_bound ranges (1-based, inclusive; index 0 unused)
+struct SideJob {
+    int blk, side, d1, conv;  // 0-based block, side 1..6, axis 1..3, 1 = convective
+    int n[3];
+    int plane;
+    long off3, off2, off1k;
+    int bnd[4][6];
+};
+
+// per exit axis d1 = 1..3 (index 0 unused): the metric conv_exitbc passes
+// as dip / rp / dkp to conv_exitbc1_block for the variable being updated
+struct ExitMetrics {
+    const double *dm[4], *rm[4], *km[4];
+};
+
+// slots of the SAVEd outflow values (conv_exitbc.F:78): per-side totals
+// (index side 1..6), inflow and outflow sums, mass change
+enum { EX_TTL = 0, EX_ARHO = 7, EX_IN = 14, EX_OUT = 15, EX_MCHG = 16, EX_N = 17 };
+
 // One periodic/interface face of swap_sc (code/swap_sc0.F:92-133 and
 // 239-283).  Own pack plane = first interior plane of (block, side); own
 // ghost plane receives the partner face's pack plane.  Positions are 0-based

@@ -144,6 +144,24 @@ void launch_wall_shear(const BlkDev *blk, int nb, long maxik, const double *dju,
                        double coef, double *ubar, double *sum, cudaStream_t st);
 void launch_fill_d(double *a, double v, long n, cudaStream_t st);
 
+// k_outflow.cu: convective outflow / fixed inflow sides
+void launch_side_flux(const SideJob *jobs, int njobs, int iva, int which, const double *u, const double *v,
+                      const double *w, const double *rho, const double *rdju, const double *rdiv,
+                      const double *didjp, const double *dkp, double *out, cudaStream_t st);
+void launch_side_combine(const SideJob *jobs, int njobs, const double *out, int mode, double *ex,
+                         cudaStream_t st);
+void launch_exit_update(const SideJob *jobs, int njobs, int task, int iva, const ExitMetrics &M, double *u,
+                        double *u_int, const double *rho, const double *rhonp1, double *hn, double dtime,
+                        const double *ex, cudaStream_t st);
+void launch_exit_scale(const SideJob *jobs, int njobs, int iva, double *f, const double *ex, cudaStream_t st);
+void launch_mass_change(const BlkDev *blk, int nb, long maxcell, double dtime, const double *rho,
+                        const double *rhonp1, const double *rdidjp, const double *dkw, double *partial,
+                        double *out, cudaStream_t st);
+void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, const double *uprof,
+                        const double *vprof, unsigned long long seed, int step, double rholo, double rhohi,
+                        double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
+                        double *v_int, double *w_int, cudaStream_t st);
+
 } // namespace les
 
 // k_phys.cu and k_sgs.cu, built twice (phys_variant.h): les_exact and les_fast

@@ -80,6 +80,16 @@ struct Ctx {
     FastSet<double> f64;
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
+    // convective outflow / fixed inflow sides (lester_outflow.cu)
+    bool sides_built = false;
+    std::vector<SideJob> sides;     // (block, side) order
+    SideJob *d_sides = nullptr;
+    double *d_exit = nullptr;       // EX_N SAVEd values
+    double *d_sideout = nullptr;    // 3 sums per side
+    int inlet[4] = {0, 0, 0, 0};    // inlet blocks (1-based; 0 none)
+    double *d_uprof = nullptr, *d_vprof = nullptr;
+    int nprof = 0;
+    unsigned long long inlet_seed = 0;
     int ncomp = 1;                  // connected components of the block graph
     double *d_bmean = nullptr;      // per block: interior mean of b over its component
     const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -155,6 +165,17 @@ int fast_sgs_tabs(Ctx &c, const double *dip, const double *djp, const double *rp
                                 cudaGetErrorString(e_));                                           \
         }                                                                                          \
     } while (0)
+
+// lester_outflow.cu: convective outflow / fixed inflow on device arrays;
+// m[] = dip, diu, dix, djp, djv, djx, rdiv, rdju, didjp, rp, ru, rv
+int ensure_sides(Ctx &c);
+bool has_convective(const Ctx &c);
+bool has_inlet(const Ctx &c);
+int exit_task(Ctx &c, int task, int iva, const double *rho, const double *rhonp1, double *u, double *v,
+              double *w, double *u_int, double *v_int, double *w_int, double *hu, double *hv, double *hw,
+              const double *const *m, const double *dkp, const double *dkw, const double *rdidjp);
+int inlet_task(Ctx &c, const double *uprof, const double *vprof, unsigned long long seed, int step, double *u,
+               double *v, double *w, double *sc1, double *rho, double *u_int, double *v_int, double *w_int);
 
 #define LES_NEED_CTX()                                                                             \
     do {                                                                                           \

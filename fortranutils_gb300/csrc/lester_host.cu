@@ -439,8 +439,10 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_flag);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b,
-                  c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean};
+                  c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
+                  c->d_exit, c->d_sideout, c->d_uprof, c->d_vprof};
     for (void *p : fp) cudaFree(p);
+    cudaFree(c->d_sides);
     for (void *p : c->stage_buf) cudaFree(p);
     cudaFree(c->d_offki);
     cudaFree(c->d_offjk);

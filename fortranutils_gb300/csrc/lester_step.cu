@@ -86,13 +86,10 @@ int lester_step(lester_fields *F, const int *istep)
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
     if (!F || !istep) return set_err(LES_ERR_ARG, "null fields / istep");
-    for (int b = 0; b < c.g.numbl; b++)
-        for (int s = 0; s < 6; s++) {
-            int t = c.g.bl_bc[b][s];
-            if (t == LES_BCT_FIXED || t == LES_BCT_CONVECTIVE)
-                return set_err(LES_ERR_GEOM, "block %d side %d: FIXED/CONVECTIVE sides are not supported", b + 1,
-                               s + 1);
-        }
+    int r0;
+    if ((r0 = ensure_sides(c))) return r0;
+    if (has_inlet(c) && (!c.d_uprof || !c.d_vprof))
+        return set_err(LES_ERR_ARG, "inlet blocks set without profiles (lester_gpu_set_inlet)");
     // whole-state staging: host arrays are mirrored once for the step
     Staging st(&c, __func__);
     lester_fields D = *F;
@@ -148,6 +145,17 @@ int lester_step(lester_fields *F, const int *istep)
     const lester_ctrl &k = c.c;
     const int one = 1, iU = 1, iV = 2, iW = 3;
     double zero = 0.0;
+    const double *mx[12] = {m[M_DIP], m[M_DIU], m[M_DIX], m[M_DJP], m[M_DJV], m[M_DJX],
+                            m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], m[M_RU], m[M_RV]};
+    // conv_exitbc(task, iva) of step.F:344 and 435
+    auto exitbc = [&](int task, int iva) {
+        return exit_task(c, task, iva, D.rho, D.rhonp1, D.u, D.v, D.w, D.u_int, D.v_int, D.w_int, D.hn_u, D.hn_v,
+                         D.hn_w, mx, D.dkp, D.dkw, m[M_RDIDJP]);
+    };
+    // ---- ivar = u: the inlet planes (step.F:226)
+    if (has_inlet(c))
+        RET(inlet_task(c, c.d_uprof, c.d_vprof, c.inlet_seed, *istep, D.u, D.v, D.w, D.sc1, D.rho, D.u_int,
+                       D.v_int, D.w_int));
     // ---- ivar = u: boundary ghosts, eddy viscosity, scalar, u predictor
     for (int iv = 1; iv <= 3; iv++) {
         double *fld = iv == 1 ? D.u : iv == 2 ? D.v : D.w;
@@ -176,17 +184,20 @@ int lester_step(lester_fields *F, const int *istep)
                           m[M_DIDJP], m[M_DIDJU], m[M_RDIDJU], m[M_HIJP], m[M_HIJU], m[M_HJIU], m[M_HKIU],
                           m[M_HKJU], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[0], tw[1], tw[2], tw[3], nullptr,
                           nullptr));
+    RET(exitbc(1, 1));
     // ---- ivar = v (step.F:319-326: the v arrays in the u roles)
     RET(lester_set_uv_int(&iV, D.v, D.u, D.w, D.p, D.rho, D.rhonp1, D.gam, D.v_int, D.hn_v, m[M_DJP], m[M_DJV],
                           m[M_DJX], m[M_RDJX], m[M_DIP], m[M_DIV], m[M_DIU], m[M_DIX], m[M_RDIP], m[M_RDIV],
                           m[M_DIDJP], m[M_DJDIV], m[M_RDJDIV], m[M_HJIP], m[M_HJIV], m[M_HIJV], m[M_HKJV],
                           m[M_HKIV], m[M_RP], m[M_RV], D.dkp, D.dkw, tw[4], tw[5], tw[6], tw[7], nullptr,
                           nullptr));
+    RET(exitbc(1, 2));
     // ---- ivar = w
     RET(lester_set_w_int(D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.w_int, D.hn_w, m[M_DIP], m[M_DIU],
                          m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
                          m[M_HKIU], m[M_HKJV], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[10], tw[11], tw[8], tw[9],
                          nullptr, nullptr));
+    RET(exitbc(1, 3));
     // ---- ivar = p
     if (*istep == 1)
         RET(lester_coeff_p(m[M_DIU], m[M_DJV], m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], D.dkp, D.dkw, D.ap, D.aw,
@@ -206,6 +217,7 @@ int lester_step(lester_fields *F, const int *istep)
     RET(lester_uvw_adv(&iW, m[M_DIU], m[M_RP], D.dkw, D.w, D.w_int, D.rhonp1, D.p, nullptr, nullptr, istep));
     RET(lester_slipbc(nullptr, nullptr, nullptr, m[M_DIP], m[M_DIU], m[M_DJP], m[M_DJV], D.dkp, D.u, D.v, D.v_int,
                       D.w, D.sc1, D.rho, D.p, istep));
+    for (int iva = 1; iva <= 3; iva++) RET(exitbc(2, iva));
     RET(lester_swap_rhos(D.rho, D.rhonp1, D.rhonm1));
     c.iststep += 1;  // code/step.F:181, ready for the next step
     r = st.finish();

@@ -242,3 +242,25 @@ def boxes_case(sizes, ybc: int = L.BCT_WALL, h: float | None = None, maxmgl: int
         blocks.append(Block(n=(ni + 2, nj + 2, nk + 2), bc=[P, P, ybc, ybc, P, P], link=link,
                             x=_axis(ni, 0.0, lx), y=_axis(nj, -ly / 2, ly / 2), z=_axis(nk, 0.0, lz)))
     return Case(blocks=blocks, maxmgl=maxmgl, nummgl=nummgl).setup()
+
+
+def inflow_case(ni1: int, ni2: int, nj: int, nk: int, ybc: int = L.BCT_WALL, beta: float | None = None,
+                maxmgl: int = 16, nummgl: int = 0) -> Case:
+    """A spatially developing channel of two blocks in x joined by an
+    interface: block 1's west side a fixed inflow (BCT_FIXED), block 2's
+    east side a convective outflow (BCT_CONVECTIVE), `ybc` sides in y,
+    periodic in z."""
+    lx = 4.0 * np.pi
+    xs = _axis(ni1 + ni2, 0.0, lx)
+    x1 = np.zeros(ni1 + 3)
+    x1[1:ni1 + 2] = xs[1:ni1 + 2]
+    x2 = np.zeros(ni2 + 3)
+    x2[1:ni2 + 2] = xs[ni1 + 1:ni1 + ni2 + 2]
+    yv = _axis(nj, -1.0, 1.0, beta)
+    zv = _axis(nk, 0.0, np.pi)
+    I, P, F, Cv = L.BCT_INTERFACE, L.BCT_PERIODIC, L.BCT_FIXED, L.BCT_CONVECTIVE
+    b1 = Block(n=(ni1 + 2, nj + 2, nk + 2), bc=[F, I, ybc, ybc, P, P],
+               link=[(0, 0), (2, 1), (0, 0), (0, 0), (1, 6), (1, 5)], x=x1, y=yv, z=zv)
+    b2 = Block(n=(ni2 + 2, nj + 2, nk + 2), bc=[I, Cv, ybc, ybc, P, P],
+               link=[(1, 2), (0, 0), (0, 0), (0, 0), (2, 6), (2, 5)], x=x2, y=yv, z=zv)
+    return Case(blocks=[b1, b2], maxmgl=maxmgl, nummgl=nummgl).setup()

@@ -393,3 +393,36 @@ def set_sc1_bc(f):
 def set_sc1var(u, v, w, sc1, rho, sc1var, sc1dis, dip, djp, dkp, dkw, rp):
     _check(lib().lester_set_sc1var(*map(_p, (u, v, w, sc1, rho, sc1var, sc1dis, dip, djp, dkp, dkw,
                                              rp)), None, None))
+
+
+# ------------------------------------- convective outflow / fixed inflow
+def conv_exitbc(task, iva, rho, rhonp1, u, v, w, u_int, v_int, w_int, hu, hv, hw, metrics: dict, dkp,
+                dkw):
+    """code/conv_exitbc.F:21 (metrics: the 2-D metric dict)."""
+    m = metrics
+    _check(lib().lester_conv_exitbc(_i(task), _i(iva), _p(rho), _p(rhonp1), _p(u), _p(v), _p(w),
+                                    _p(u_int), _p(v_int), _p(w_int), _p(hu), _p(hv), _p(hw),
+                                    *[_p(m[n]) for n in ("dip", "diu", "dix", "djp", "djv", "djx", "rdiv",
+                                                         "rdju", "didjp", "rp", "ru", "rv")],
+                                    _p(dkp), _p(dkw), _p(m["rdidjp"])))
+
+
+def mass_change(rho, rhonp1, rdidjp, dkw) -> float:
+    out = C.c_double()
+    _check(lib().lester_mass_change(_p(rho), _p(rhonp1), C.byref(out), _p(rdidjp), _p(dkw)))
+    return out.value
+
+
+def gpu_set_inlet(inlet, uprof=None, vprof=None, seed: int = 0) -> None:
+    """Inlet blocks (four 1-based block numbers, 0 = none) and the u, v
+    inflow profiles (equal-length float64 arrays)."""
+    ib = (C.c_int * 4)(*[int(b) for b in inlet])
+    n = 0 if uprof is None else len(uprof)
+    _check(lib().lester_gpu_set_inlet(ib, _p(uprof), _p(vprof), n, C.c_ulonglong(seed)))
+
+
+def fixed_inlet(u_int, v_int, w_int, u, v, w, sc1, rho, iseed, uprof, vprof, step):
+    """code/fixed_inlet.F:5 (the arguments it reads; the rest are passed as NULL)."""
+    _check(lib().lester_fixed_inlet(None, None, None, _p(u_int), _p(v_int), _p(w_int), _p(u), _p(v), _p(w),
+                                    None, _p(sc1), _p(rho), None, _i(iseed), None, _p(uprof), _p(vprof),
+                                    None, None, None, None, None, None, None, None, None, None, _i(step)))

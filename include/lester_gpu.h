@@ -194,10 +194,11 @@ int lester_gpu_prof_read(double *ms_total, long *launches);
 /* bytes copied host->device and device->host by calls with host arrays */
 int lester_gpu_xfer_bytes(long *h2d, long *d2h);
 
-/* One time step: the ivar loop of code/step.F:214-454 (set_virt_bc x3,
- * subgrid, scalar transport and density, momentum predictor, coeff_p at
- * istep 1, sour_p, solvers, extrap_p, p_ref_subtract, uvw_adv x3, slipbc,
- * swap_rhos).  Host arrays are copied in once and back once per call.
+/* One time step: the ivar loop of code/step.F:214-454 (fixed_inlet on the
+ * inlet blocks of lester_gpu_set_inlet, set_virt_bc x3, subgrid, scalar
+ * transport and density, momentum predictor with conv_exitbc task 1 after
+ * each component, coeff_p at istep 1, sour_p, solvers, extrap_p,
+ * p_ref_subtract, uvw_adv x3, slipbc, conv_exitbc task 2, swap_rhos).  Host arrays are copied in once and back once per call.
  * Returns LES_ERR_NOT_CONVERGED (after completing the step) if a fast
  * pressure solver stopped at max_outer above rtol. */
 int lester_step(lester_fields *fields, const int *istep);
@@ -423,6 +424,50 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u,
                    const double *dkp, const double *dkw, const double *hijp,
                    const double *hjip, const double *hkip, const double *hkjp,
                    const double *rp, double *work, int *offwork);
+
+/* ---- convective outflow and fixed inflow sides ------------------------ */
+/* code/conv_exitbc.F:21 conv_exitbc(task, iva, rho, rhonp1, u, v, w,
+ * u_int, v_int, w_int, hu, hv, hw, dip, diu, dix, djp, djv, djx, rdiv,
+ * rdju, didjp, rp, ru, rv, dkp, dkw, rdidjp).  Task 1 (after the predictor
+ * of variable iva, step.F:344): the exit planes of BCT_CONVECTIVE sides get
+ * u_int from the convective condition with the side's mean outflow
+ * velocity of step n, and at iva = 3 the exit velocities are scaled so the
+ * outflow matches the inflow of the BCT_FIXED sides minus the mass change.
+ * Task 2 (after the projection, step.F:433-441): the exit planes take
+ * u_int.  The SAVEd values between calls live on the device.  No-op
+ * without convective sides; a convective low-z side is refused
+ * (LES_ERR_GEOM: the reference reads below the block there). */
+int lester_conv_exitbc(const int *task, const int *iva, const double *rho, const double *rhonp1, double *u,
+                       double *v, double *w, double *u_int, double *v_int, double *w_int, double *hu, double *hv,
+                       double *hw, const double *dip, const double *diu, const double *dix, const double *djp,
+                       const double *djv, const double *djx, const double *rdiv, const double *rdju,
+                       const double *didjp, const double *rp, const double *ru, const double *rv,
+                       const double *dkp, const double *dkw, const double *rdidjp);
+/* code/mass_change.F:6 mass_change(rho, rhonp1, mass_chg, rdidjp, dkw):
+ * sum over interior cells of (rhonp1 - rho) rdidjp dkw / dtime. */
+int lester_mass_change(const double *rho, const double *rhonp1, double *mass_chg, const double *rdidjp,
+                       const double *dkw);
+/* The inlet configuration fixed_inlet reads from COMMON (inlet1..inlet4:
+ * 1-based block numbers, 0 = none) and the profiles read_profile reads
+ * from inflowbc.3d (fixed_inlet.F:187-227): nprof values of u and v, host
+ * or device arrays, copied.  `seed` keys the inlet perturbations that
+ * lester_step draws. */
+int lester_gpu_set_inlet(const int *inlet, const double *uprof, const double *vprof, int nprof,
+                         unsigned long long seed);
+/* code/fixed_inlet.F:5 fixed_inlet(hu, hv, hw, u_int, v_int, w_int, u, v,
+ * w, p, sc1, rho, gam, iseed, y, uprof, vprof, wprof, uuprof, vvprof,
+ * wwprof, umean, vmean, wmean, uumean, vvmean, wwmean, step): the inflow
+ * plane (i = 2 faces, i = 1 ghosts) of each inlet block from the profiles
+ * plus a perturbation 0.005 a (2 U - 1), U uniform in [0, 1).  The
+ * reference draws U with the Fortran random_number; here U is a
+ * counter-based function of (iseed, step, block, j, k).  Only uprof and
+ * vprof (length nprof of lester_gpu_set_inlet) are read. */
+int lester_fixed_inlet(double *hu, double *hv, double *hw, double *u_int, double *v_int, double *w_int, double *u,
+                       double *v, double *w, const double *p, double *sc1, double *rho, const double *gam,
+                       const int *iseed, const double *y, const double *uprof, const double *vprof,
+                       const double *wprof, const double *uuprof, const double *vvprof, const double *wwprof,
+                       const double *umean, const double *vmean, const double *wmean, const double *uumean,
+                       const double *vvmean, const double *wwmean, const int *step);
 
 /* ---- adjoint and tangent-linear runs ---------------------------------- */
 /* No counterpart in the reference.  A run of nsteps lester_step calls from

@@ -188,6 +188,28 @@ typedef struct {
 void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, int iststep,
               orc_fields *F);
 
+/* ---- convective outflow and fixed inflow (orc_outflow.c) ---------------- */
+int orc_has_convective(const orc_ctx *c);
+/* code/conv_exitbc.F:21: task 1 after each predictor (iva = ivar), task 2
+   after the projection; metric = the 35 packed 2-D metrics */
+void orc_conv_exitbc(orc_ctx *c, int task, int iva, double dtime, const double *rho,
+                     const double *rhonp1, double *u, double *v, double *w, double *u_int,
+                     double *v_int, double *w_int, double *hu, double *hv, double *hw,
+                     const double *metric, const double *dkp, const double *dkw);
+/* code/mass_change.F:6: sum over cells of (rhonp1 - rho) vol / dt */
+double orc_mass_change(orc_ctx *c, double dtime, const double *rho, const double *rhonp1,
+                       const double *rdidjp, const double *dkw);
+/* counter-based uniform [0, 1) of the inlet perturbations */
+double orc_inlet_uniform(unsigned long long seed, int step, int block, int j, int k);
+/* code/fixed_inlet.F:5 on the blocks inlet[0..3] (1-based, 0 = none) */
+void orc_fixed_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const double *vprof,
+                     unsigned long long seed, int step, double rholo, double rhohi, double *u,
+                     double *v, double *w, double *sc1, double *rho, double *u_int, double *v_int,
+                     double *w_int);
+/* inlet configuration used by orc_step (profiles copied, nprof values each) */
+void orc_set_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const double *vprof,
+                   int nprof, unsigned long long seed);
+
 /* ---- eddy viscosity ---------------------------------------------------- */
 void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
                  double *gam, double *gamsc1, const double *u,

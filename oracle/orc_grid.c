@@ -190,6 +190,8 @@ void orc_destroy(orc_ctx *c)
 {
     if (!c) return;
     free(c->work);
+    free(c->uprof);
+    free(c->vprof);
     free(c);
 }
 

@@ -49,6 +49,13 @@ struct orc_ctx {
     int jumble;
     double rnorm[ORC_MAXMGL + 1], fnorm[ORC_MAXMGL + 1], enorm[ORC_MAXMGL + 1], vnorm[ORC_MAXMGL + 1];
     double tolc;
+    /* conv_exitbc's SAVEd values (code/conv_exitbc.F:78): per-side outflow
+       mass flux and rho-weighted area at step n, inflow and outflow sums */
+    double exit_mflux_ttl[7], exit_arho_ttl[7], exit_mflux_in, exit_mflux_out;
+    /* fixed_inlet: inlet block numbers (COMMON inlet1..inlet4), profiles */
+    int inlet[4];
+    double *uprof, *vprof;
+    unsigned long long inlet_seed;
 };
 
 #endif

@@ -2,15 +2,18 @@
  * orc_step.c -- oracle: one time step in the order of code/step.F:214-454.
  * TEST INFRASTRUCTURE ONLY.
  *
- * ivar = u: set_virt_bc for u, v, w (step.F:236-255), subgrid (258),
+ * ivar = u: fixed_inlet on the inlet blocks (step.F:226), set_virt_bc for
+ *   u, v, w (236-255), subgrid (258),
  *   set_gamsc1_bc, set_sc1, set_sc1_bc, set_sc1var, search_lib, set_sc1_bc
- *   x3 (268-298), set_uv_int(u) (307)
- * ivar = v: set_uv_int with the v arrays in the u roles (319-326)
- * ivar = w: set_w_int (331)
+ *   x3 (268-298), set_uv_int(u) (307), conv_exitbc(1, u) (344)
+ * ivar = v: set_uv_int with the v arrays in the u roles (319-326),
+ *   conv_exitbc(1, v)
+ * ivar = w: set_w_int (331), conv_exitbc(1, w)
  * ivar = p: coeff_p at istep 1 (359-362), sour_p (366), lmg_solve (372),
  *   extrap_p (376), p_ref_subtract (380), uvw_adv x3 (418-425), slipbc
- *   (428), swap_rhos (450)
- * conv_exitbc is a no-op without convective sides and cflest only prints.
+ *   (428), conv_exitbc(2, u..w) (433-441), swap_rhos (450)
+ * conv_exitbc is a no-op without convective sides; conv_exitbc(1, p) and
+ * (1, sc1) change nothing; cflest only prints.
  */
 #include <stdlib.h>
 #include "orc_internal.h"
@@ -34,6 +37,9 @@ void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, in
     double *twu[4] = {F->tw[0], F->tw[1], F->tw[2], F->tw[3]};
     double *twv[4] = {F->tw[4], F->tw[5], F->tw[6], F->tw[7]};
     double *tww[4] = {F->tw[8], F->tw[9], F->tw[10], F->tw[11]};
+    if (c->inlet[0] || c->inlet[1] || c->inlet[2] || c->inlet[3])
+        orc_fixed_inlet(c, c->inlet, c->uprof, c->vprof, c->inlet_seed, istep, k->rholo, k->rhohi,
+                        F->u, F->v, F->w, F->sc1, F->rho, F->u_int, F->v_int, F->w_int);
     orc_set_virt_bc(c, ORC_SV_U, k->visc, k->kappa, k->aplus, k->ylaminar, F->u, F->rho,
                     F->vd_damping, metric, F->dkp, F->dkw, twu);
     orc_set_virt_bc(c, ORC_SV_V, k->visc, k->kappa, k->aplus, k->ylaminar, F->v, F->rho,
@@ -57,12 +63,18 @@ void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, in
     orc_set_uv_int(c, ORC_SV_U, k->dtime, iststep, k->visc, k->ylaminar, k->kappa, k->cwfun,
                    F->u, F->v, F->w, F->p, F->rho, F->rhonp1, F->gam, F->u_int, F->hn_u, metric,
                    F->dkp, F->dkw, F->tw[0], F->tw[1], F->tw[2], F->tw[3]);
+    orc_conv_exitbc(c, 1, ORC_SV_U, k->dtime, F->rho, F->rhonp1, F->u, F->v, F->w, F->u_int,
+                    F->v_int, F->w_int, F->hn_u, F->hn_v, F->hn_w, metric, F->dkp, F->dkw);
     orc_set_uv_int(c, ORC_SV_V, k->dtime, iststep, k->visc, k->ylaminar, k->kappa, k->cwfun,
                    F->v, F->u, F->w, F->p, F->rho, F->rhonp1, F->gam, F->v_int, F->hn_v, metric,
                    F->dkp, F->dkw, F->tw[4], F->tw[5], F->tw[6], F->tw[7]);
+    orc_conv_exitbc(c, 1, ORC_SV_V, k->dtime, F->rho, F->rhonp1, F->u, F->v, F->w, F->u_int,
+                    F->v_int, F->w_int, F->hn_u, F->hn_v, F->hn_w, metric, F->dkp, F->dkw);
     orc_set_w_int(c, k->dtime, iststep, k->visc, k->ylaminar, k->kappa, k->cwfun, F->u, F->v,
                   F->w, F->p, F->rho, F->rhonp1, F->gam, F->w_int, F->hn_w, metric, F->dkp,
                   F->dkw, F->tw[10], F->tw[11], F->tw[8], F->tw[9]);
+    orc_conv_exitbc(c, 1, ORC_SV_W, k->dtime, F->rho, F->rhonp1, F->u, F->v, F->w, F->u_int,
+                    F->v_int, F->w_int, F->hn_u, F->hn_v, F->hn_w, metric, F->dkp, F->dkw);
     if (istep == 1)
         orc_coeff_p(c, MET(M_DIU), MET(M_DJV), MET(M_RDIV), MET(M_RDJU), MET(M_DIDJP), MET(M_RP),
                     F->dkp, F->dkw, F->ap, F->aw, F->ae, F->as, F->an, F->al, F->ar);
@@ -78,6 +90,9 @@ void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, in
     orc_uvw_adv(c, ORC_SV_V, k->dtime, MET(M_DJV), MET(M_RP), F->dkw, F->v, F->v_int, F->rhonp1, F->p);
     orc_uvw_adv(c, ORC_SV_W, k->dtime, MET(M_DIU), MET(M_RP), F->dkw, F->w, F->w_int, F->rhonp1, F->p);
     orc_slipbc(c, k->dtime, MET(M_DJP), F->u, F->v, F->v_int, F->w, F->sc1, F->rho, F->p);
+    for (int iva = ORC_SV_U; iva <= ORC_SV_W; iva++)
+        orc_conv_exitbc(c, 2, iva, k->dtime, F->rho, F->rhonp1, F->u, F->v, F->w, F->u_int,
+                        F->v_int, F->w_int, F->hn_u, F->hn_v, F->hn_w, metric, F->dkp, F->dkw);
     orc_swap_rhos(c, F->rho, F->rhonp1, F->rhonm1);
 #undef MET
 }

@@ -263,3 +263,35 @@ def _orc_step(self, mg: MgCtrl, k: OrcPhys, istep: int, iststep: int, state) -> 
 
 
 Oracle.step = _orc_step
+
+
+# ---- convective outflow / fixed inflow (oracle/orc_outflow.c) ------------
+def _orc_conv_exitbc(self, task, iva, dtime, rho, rhonp1, u, v, w, u_int, v_int, w_int, hu, hv, hw,
+                     metric: dict, dkp, dkw) -> None:
+    flat = _flat_metric(metric)
+    lib().orc_conv_exitbc(self.ctx, int(task), int(iva), C.c_double(dtime),
+                          *map(P, (rho, rhonp1, u, v, w, u_int, v_int, w_int, hu, hv, hw, flat, dkp, dkw)))
+
+
+def _orc_mass_change(self, dtime, rho, rhonp1, rdidjp, dkw) -> float:
+    lib().orc_mass_change.restype = C.c_double
+    return lib().orc_mass_change(self.ctx, C.c_double(dtime), P(rho), P(rhonp1), P(rdidjp), P(dkw))
+
+
+def _orc_fixed_inlet(self, inlet, uprof, vprof, seed, step, rholo, rhohi, u, v, w, sc1, rho, u_int,
+                     v_int, w_int) -> None:
+    ib = (C.c_int * 4)(*inlet)
+    lib().orc_fixed_inlet(self.ctx, ib, P(uprof), P(vprof), C.c_ulonglong(seed), int(step),
+                          C.c_double(rholo), C.c_double(rhohi),
+                          *map(P, (u, v, w, sc1, rho, u_int, v_int, w_int)))
+
+
+def _orc_set_inlet(self, inlet, uprof, vprof, seed) -> None:
+    ib = (C.c_int * 4)(*inlet)
+    lib().orc_set_inlet(self.ctx, ib, P(uprof), P(vprof), len(uprof), C.c_ulonglong(seed))
+
+
+Oracle.conv_exitbc = _orc_conv_exitbc
+Oracle.mass_change = _orc_mass_change
+Oracle.fixed_inlet = _orc_fixed_inlet
+Oracle.set_inlet = _orc_set_inlet
