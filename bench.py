@@ -59,6 +59,15 @@ WORKLOADS = {
                       desc="32 independent Poisson boxes in one solve, sides drawn from 32,40,...,128 "
                            "cells per axis (seed 5), cubic cells, periodic x/z and Neumann y, sources "
                            "N(0,1) minus their mean, to 1e-8"),
+    "bl6": dict(shape=(384, 144, 64), seed=3,
+                desc="multiblock spatially developing boundary layer: 6 uneven blocks (160,96,64) "
+                     "(128,96,64) (96,96,64) below (160,48,64) (128,48,64) (96,48,64), interfaces in x "
+                     "and y, fixed inflow u = tanh(y/0.5) + noise (fixed plane, no recycling), convective "
+                     "outflow, wall below, slip above, periodic z, a passive scalar layer at y = 2 at "
+                     "constant density (with density ratio 1.5 the reference scheme itself diverges in "
+                     "its first steps at this resolution), "
+                     "Smagorinsky Cs 0.1, dt from CFL 0.3 and diffusion number 0.2, full lester_step, "
+                     "Poisson to 1e-8"),
     "channel512": dict(shape=(512, 384, 256), beta=2.2, nummgl=0, seed=5,
                        desc="stretched plane channel 512x384x256 cells, 2pi x 2 x pi, tanh walls "
                             "beta 2.2, periodic x/z, Re_b 2800, Smagorinsky Cs 0.1, constant "
@@ -127,6 +136,8 @@ def make_case(shape=SHAPE, wl="mixing"):
     if wl == "mixing":
         lx, ly, lz = DOMAIN
         return grid.box_case(ni, nj, nk, lx=lx, ly=ly, lz=lz, ybc=L.BCT_ZERO_GRAD, beta=2.0)
+    if wl == "bl6":
+        return grid.bl6_case(1)
     w = WORKLOADS[wl]
     return grid.box_case(ni, nj, nk, ybc=L.BCT_WALL, beta=w["beta"], nummgl=w["nummgl"])
 
@@ -135,14 +146,16 @@ def cfl_dt(case, s, cfl=0.3, dfs=0.2, visc=1.0 / 2800.0):
     """dt from the initial field (cflest-style): the smaller of cfl / max
     over cells of |u|/dx + |v|/dy + |w|/dz and, since the predictor's
     diffusion is explicit, dfs / max of visc (1/dx^2 + 1/dy^2 + 1/dz^2)."""
-    b = case.blocks[0]
-    dx = np.diff(b.x[1:b.n[0]]).min()
-    dy = np.diff(b.y[1:b.n[1]])
-    dz = np.diff(b.z[1:b.n[2]]).min()
-    u, v, w = (case.block_view(s[n], 0)[1:-1, 1:-1, 1:-1] for n in "uvw")
-    c = np.abs(u) / dx + np.abs(v) / dy[None, :, None] + np.abs(w) / dz
-    d = visc * (1.0 / dx ** 2 + 1.0 / dy.min() ** 2 + 1.0 / dz ** 2)
-    return min(cfl / float(c.max()), dfs / d)
+    cmax = dmax = 0.0
+    for ib, b in enumerate(case.blocks):
+        dx = np.diff(b.x[1:b.n[0]]).min()
+        dy = np.diff(b.y[1:b.n[1]])
+        dz = np.diff(b.z[1:b.n[2]]).min()
+        u, v, w = (case.block_view(s[n], ib)[1:-1, 1:-1, 1:-1] for n in "uvw")
+        c = np.abs(u) / dx + np.abs(v) / dy[None, :, None] + np.abs(w) / dz
+        cmax = max(cmax, float(c.max()))
+        dmax = max(dmax, visc * (1.0 / dx ** 2 + 1.0 / dy.min() ** 2 + 1.0 / dz ** 2))
+    return min(cfl / cmax, dfs / dmax)
 
 
 def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
@@ -150,8 +163,9 @@ def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     if wl == "mixing":
         return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
                               rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
-    return L.default_ctrl(dtime=dtime, model=1, csles=0.1, rholo=1.0, rhohi=1.0, visc=1.0 / 2800.0,
-                          psolve=psolve, rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
+    return L.default_ctrl(dtime=dtime, model=1, csles=0.1, rholo=1.0, rhohi=1.0,
+                          visc=1.0 / 2800.0, psolve=psolve, rtol=1e-8, max_outer=200, exact=EXACT,
+                          krylov=krylov)
 
 
 def host_state(case, ctrl, wl="mixing"):
@@ -162,7 +176,22 @@ def host_state(case, ctrl, wl="mixing"):
                     np.zeros(c.n1k))
     if wl == "mixing":
         return S.init_mixing_layer(s, seed=2, sigma=0.02, rholo=ctrl.rholo, rhohi=ctrl.rhohi)
+    if wl == "bl6":
+        return S.init_bl6(s, seed=3, sigma=0.03, rholo=1.0, rhohi=1.0, width=0.25)
     return S.init_channel(s, seed=WORKLOADS[wl]["seed"], sigma=0.05)
+
+
+def set_inlet(case, wl, orc=None):
+    """The bl6 workload's inflow planes (fixed, no recycling): blocks 1 and
+    4 in fixed_inlet's slots 1 and 4."""
+    if wl != "bl6":
+        return
+    from fortranutils_gb300 import grid, lester as L
+    up, vp = grid.bl6_inflow(case)
+    if orc is not None:
+        orc.set_inlet([1, 0, 0, 4], up, vp, 3)
+    else:
+        L.gpu_set_inlet([1, 0, 0, 4], up, vp, 3)
 
 
 def device_state(case, ctrl, wl="mixing"):
@@ -215,6 +244,7 @@ def run_gpu(args):
     for mode, ps in modes:
         ctrl = make_ctrl(ps, {"dc": 0, "fcg": 1, "auto": 2}[args.outer], wl, dtime)
         L.gpu_init(case.geom(), ctrl)
+        set_inlet(case, wl)
         g = device_state(case, ctrl, wl)
         stream = torch.cuda.current_stream()
         istep = 0
@@ -289,6 +319,7 @@ def run_cpu_steps(case, nsteps: int, warmup: int = 0, wl: str = "mixing", dtime=
     from fortranutils_gb300 import lester as L
     ctrl = make_ctrl(L.PSOLVE_REFERENCE, wl=wl, dtime=dtime)
     orc = O.Oracle(case)
+    set_inlet(case, wl, orc)
     x, y, z = case.coordinates()
     met, dkp, dkw = orc.comp_metric(x, y, z)
     s = host_state(case, ctrl, wl)

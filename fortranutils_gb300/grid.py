@@ -264,3 +264,50 @@ def inflow_case(ni1: int, ni2: int, nj: int, nk: int, ybc: int = L.BCT_WALL, bet
     b2 = Block(n=(ni2 + 2, nj + 2, nk + 2), bc=[I, Cv, ybc, ybc, P, P],
                link=[(1, 2), (0, 0), (0, 0), (0, 0), (2, 6), (2, 5)], x=x2, y=yv, z=zv)
     return Case(blocks=[b1, b2], maxmgl=maxmgl, nummgl=nummgl).setup()
+
+
+BL6_LOWER = ((160, 96, 64), (128, 96, 64), (96, 96, 64))
+BL6_UPPER = ((160, 48, 64), (128, 48, 64), (96, 48, 64))
+
+
+def bl6_case(div: int = 1, maxmgl: int = 16, nummgl: int = 0) -> Case:
+    """Multiblock boundary layer: two rows of three blocks of uneven sizes
+    (cells, divided by `div`): lower (160,96,64) (128,96,64) (96,96,64) on
+    y in [0, 2], upper (160,48,64) (128,48,64) (96,48,64) on y in [2, 3],
+    joined by interfaces in x and y; x = 0 a fixed inflow (blocks 1 and 4),
+    the east end a convective outflow (blocks 3 and 6), a wall at y = 0, a
+    slip side at y = 3, periodic in z (depth 2).  Cubic cells of side
+    1/32 (times div)."""
+    lo = [tuple(v // div for v in s) for s in BL6_LOWER]
+    up = [tuple(v // div for v in s) for s in BL6_UPPER]
+    h = div / 32.0
+    I, P, F, Cv, W, Z = (L.BCT_INTERFACE, L.BCT_PERIODIC, L.BCT_FIXED, L.BCT_CONVECTIVE, L.BCT_WALL,
+                         L.BCT_ZERO_GRAD)
+    nx = [s[0] for s in lo]
+    x0 = np.cumsum([0] + nx) * h
+    blocks = []
+    for row, sizes in enumerate((lo, up)):
+        for col, (ni, nj, nk) in enumerate(sizes):
+            b = 3 * row + col + 1
+            bc = [F if col == 0 else I, Cv if col == 2 else I, W if row == 0 else I, Z if row == 1 else I, P, P]
+            link = [(0, 0) if col == 0 else (b - 1, 2), (0, 0) if col == 2 else (b + 1, 1),
+                    (0, 0) if row == 0 else (b - 3, 4), (0, 0) if row == 1 else (b + 3, 3), (b, 6), (b, 5)]
+            y0, y1 = (0.0, 2.0) if row == 0 else (2.0, 3.0)
+            blocks.append(Block(n=(ni + 2, nj + 2, nk + 2), bc=bc, link=link, x=_axis(ni, x0[col], x0[col + 1]),
+                                y=_axis(nj, y0, y1), z=_axis(nk, 0.0, nk * h)))
+    return Case(blocks=blocks, maxmgl=maxmgl, nummgl=nummgl).setup()
+
+
+def bl6_inflow(case, delta: float = 0.5, uinf: float = 1.0):
+    """u, v inflow profiles of the bl6 case for inlet slots 1 (block 1) and
+    4 (block 4) of fixed_inlet: u = uinf tanh(y / delta) at the cell
+    centres (ghosts included) of each inlet block, v = 0."""
+    b1, b4 = case.blocks[0], case.blocks[3]
+    nj4 = b4.n[1] - 1
+    off4 = 3 * (nj4 - 1)
+    n = max(b1.n[1], off4 + b4.n[1], 4 * (nj4 - 2)) + 1
+    up, vp = np.zeros(n), np.zeros(n)
+    for b, off in ((b1, 0), (b4, off4)):
+        yc = 0.5 * (b.y[:-1] + b.y[1:])[: b.n[1]]
+        up[off:off + b.n[1]] = uinf * np.tanh(np.maximum(yc, 0.0) / delta)
+    return np.ascontiguousarray(up), np.ascontiguousarray(vp)

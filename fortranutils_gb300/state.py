@@ -167,6 +167,38 @@ def init_mixing_layer(s: State, seed: int = 2, sigma: float = 0.02, rholo: float
     return s
 
 
+def init_bl6(s: State, seed: int = 3, sigma: float = 0.03, delta: float = 0.5, rholo: float = 1.0,
+             rhohi: float = 1.5, width: float = 0.0) -> State:
+    """Boundary layer of grid.bl6_case: u = tanh(y / delta) + N(0, sigma^2),
+    v, w = N(0, sigma^2); the scalar 0 below y = 2 (the lower row of blocks)
+    and 1 above it, as a step (width 0) or 0.5 (1 + tanh((y - 2) / width)),
+    rho from the mixing law.  (A step in density leaving through the
+    convective outflow makes the reference scheme's first steps blow up at
+    full resolution; the smooth form does not.)"""
+    rng = np.random.default_rng(seed)
+    c = s.case
+    for ib, b in enumerate(c.blocks):
+        nip1, njp1, nkp1 = b.n
+        yc = 0.5 * (b.y[:-1] + b.y[1:])[:njp1]
+        sh = (nkp1, njp1, nip1)
+        c.block_view(s["u"], ib)[...] = np.tanh(np.maximum(yc, 0.0) / delta)[None, :, None] + \
+            sigma * rng.standard_normal(sh)
+        c.block_view(s["v"], ib)[...] = sigma * rng.standard_normal(sh)
+        c.block_view(s["w"], ib)[...] = sigma * rng.standard_normal(sh)
+        if width > 0.0:
+            f = 0.5 * (1.0 + np.tanh((yc - 2.0) / width))
+            c.block_view(s["sc1"], ib)[...] = np.broadcast_to(f[None, :, None], sh)
+        else:
+            c.block_view(s["sc1"], ib)[...] = 0.0 if ib < 3 else 1.0
+    _close_walls(s)
+    f = s["sc1"]
+    rho = 1.0 / (f / rhohi + (1.0 - f) / rholo)
+    for n in ("rho", "rhonp1", "rhonm1"):
+        s[n][:] = rho
+    s["vd_damping"][:] = 1.0
+    return s
+
+
 def step(state: State, istep: int) -> int:
     """lester_step on the state's arrays; returns the status (0, or
     LES_ERR_NOT_CONVERGED when a fast solver stopped short) and raises on

@@ -138,3 +138,41 @@ def test_steps_inflow_outflow(exact, gpulib):
     bad = {n: rel(got[n], ref[n]) for n in S.STATE if rel(got[n], ref[n]) > 1e-10}
     assert not bad, bad
     assert rel(got["u"], s["u"]) > 1e-6
+
+
+@pytest.mark.parametrize("psolve", [L.PSOLVE_REFERENCE, L.PSOLVE_FP64])
+def test_steps_six_blocks(psolve, gpulib):
+    """The six-block boundary layer (two rows of uneven blocks joined by
+    interfaces in x and y, two inlet blocks, two outlet blocks, a wall and
+    a slip side), one eighth of its size: whole steps against the oracle,
+    density ratio 1.5 carried by the scalar, Smagorinsky."""
+    case = grid.bl6_case(8)
+    cases.CASES["bl6"] = lambda: case
+    try:
+        st = cases.Setup("bl6", seed=3)
+    finally:
+        del cases.CASES["bl6"]
+    ctrl = L.default_ctrl(dtime=2e-3, model=1, rholo=1.0, rhohi=1.5, psolve=psolve, rtol=1e-11, max_outer=100)
+    s = S.new_state(case, st.m, st.dkp, st.dkw)
+    S.init_bl6(s, rholo=1.0, rhohi=1.5)
+    up, vp = grid.bl6_inflow(case)
+    inlet = [1, 0, 0, 4]
+    ref = s.to("numpy")
+    st.orc.set_inlet(inlet, up, vp, SEED)
+    mg = O.mgctrl_from_ctrl(ctrl) if psolve == L.PSOLVE_REFERENCE else O.mgctrl(nummgits=300, tolf=1e-15)
+    k = O.phys_from_ctrl(ctrl)
+    for it in range(1, 4):
+        st.orc.step(mg, k, it, it + 1, ref)
+    L.gpu_init(case.geom(), ctrl)
+    try:
+        L.gpu_set_inlet(inlet, up, vp, SEED)
+        g = s.to("torch")
+        rcs = [S.step(g, it) for it in range(1, 4)]
+        got = g.to("numpy")
+    finally:
+        L.gpu_finalize()
+    assert all(rc == 0 for rc in rcs), rcs
+    tol = 1e-10 if psolve == L.PSOLVE_REFERENCE else 1e-7
+    bad = {n: rel(got[n], ref[n]) for n in ("u", "v", "w", "sc1", "rho", "rhonp1") if rel(got[n], ref[n]) > tol}
+    assert not bad, bad
+    assert rel(got["u"], s["u"]) > 1e-6
