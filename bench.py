@@ -46,6 +46,9 @@ DOMAIN = (30.0, 30.0, 15.0)
 EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
+# DRAM bytes of one level-1 k_rb<float> launch of the mixing-layer workload
+# (ncu: 52.0 MB read + 0.27 MB written), against 37.7 MB algorithmic
+RB_TRAFFIC = 52.28e6
 # other workloads (--workload): the plain channel of the reference's own
 # CPU-runnable case, and the large stretched channel
 WORKLOADS = {
@@ -508,7 +511,10 @@ def main():
         "speedup_mixed_vs_fp64": fp["ms_per_step"] / mx["ms_per_step"],
         "solve_speedup_mixed_vs_fp64": fp["solve_ms"] / mx["solve_ms"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                     "frac": achieved / peak, "traffic": RB_TRAFFIC if wl == "mixing" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one level-1 "
+                                       "launch, profiles/k_rb_float_level1_256x192x128.md",
+                     "peak_source": peak_src,
                      "kernel": "k_rb<float> level-1 red-black SOR half sweep",
                      "avg_launch_ms": rb_avg_ms},
         "step_roofline": {"mixed_gbs": step_gbs["mixed"], "fp64_gbs": step_gbs["fp64"],
