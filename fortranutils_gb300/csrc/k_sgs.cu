@@ -4,6 +4,14 @@
 // subgrid (code/subgrid.F:58-92) dispatches on the model:
 //   Smagorinsky  code/subgrid_smagorinsky.F:85-237
 //   WALE         code/subgrid_wale.F:73-239 (the reference's scalar Sd)
+//   Sigma        edge/subgrid_sigma.F:66-300 (model 3 of the reference's edge
+//                variant): singular values of the gradient tensor from the
+//                invariants of g = grad(u)^T grad(u) by the trigonometric
+//                cubic solution.  As written there, the square root in the
+//                eigenvalue formula is taken of the COMMON `alpha` (the density
+//                relaxation factor of cb.control.inc), not of alpha1; that is
+//                reproduced: with alpha = 0 the three values coincide and gam
+//                is 0.
 //   none         code/subgrid_nosgs.F (gam = gamsc1 = 0)
 // The staggered-grid gradients are the reference's face/edge averages.  The
 // filter width uses the reference's literal exponent 0.33333333.  pow() is
@@ -18,7 +26,7 @@ namespace LES_PHYS_NS {
 #define IDX2(b, i, j) ((b).off2 + ((i) - 1) + (long)(b).n[0] * ((j) - 1))
 
 __global__ void __launch_bounds__(128) k_subgrid(
-    const BlkDev *__restrict__ blk, int model, double csles, int gotrad,
+    const BlkDev *__restrict__ blk, int model, double csles, int gotrad, double alpha,
     double *__restrict__ gam, double *__restrict__ gamsc1, const double *__restrict__ u,
     const double *__restrict__ v, const double *__restrict__ w, const double *__restrict__ sc1,
     double *__restrict__ sc1var, double *__restrict__ sc1dis, const double *__restrict__ vdd,
@@ -124,6 +132,35 @@ __global__ void __launch_bounds__(128) k_subgrid(
     if (model == 1) {
         double evisc = csles * delta_xyz * vdd[ijk];
         g = evisc * evisc * sqrt(2.0 * sijsij);
+    } else if (model == 3) {
+        const double onethird = 1.0 / 3.0, pi = 3.1415927;
+        double g11 = dudi * dudi + dvdi * dvdi + dwdi * dwdi;
+        double g12 = dudi * dudj + dvdi * dvdj + dwdi * dwdj;
+        double g13 = dudi * dudk + dvdi * dvdk + dwdi * dwdk;
+        double g21 = dudj * dudi + dvdj * dvdi + dwdj * dwdi;
+        double g22 = dudj * dudj + dvdj * dvdj + dwdj * dwdj;
+        double g23 = dudj * dudk + dvdj * dvdk + dwdj * dwdk;
+        double g31 = dudk * dudi + dvdk * dvdi + dwdk * dwdi;
+        double g32 = dudk * dudj + dvdk * dvdj + dwdk * dwdj;
+        double g33 = dudk * dudk + dvdk * dvdk + dwdk * dwdk;
+        double gg11 = g11 * g11 + g12 * g21 + g13 * g31;
+        double gg22 = g21 * g12 + g22 * g22 + g23 * g32;
+        double gg33 = g31 * g13 + g32 * g23 + g33 * g33;
+        double tracegg = gg11 + gg22 + gg33;
+        double inv1 = g11 + g22 + g33;
+        double inv2 = 0.5 * (inv1 * inv1 - tracegg);
+        double inv3 = g11 * (g22 * g33 - g23 * g32) - g12 * (g21 * g33 - g23 * g31) + g13 * (g21 * g32 - g22 * g31);
+        double alpha1 = (inv1 * inv1 * 0.11111111) - (inv2 * onethird);
+        double alpha2 = (inv1 * inv1 * inv1 * 0.03703703703) - (inv1 * inv2 * 0.16666666666) + (inv3 * 0.5);
+        double alpha3 = onethird * acos(alpha2 / pow(alpha1, 1.5));
+        double inv13 = inv1 * onethird;
+        double sqrtalpha = sqrt(alpha);
+        double sigma1 = pow(inv13 + 2.0 * sqrtalpha * cos(alpha3), 0.5);
+        double sigma2 = pow(inv13 - 2.0 * sqrtalpha * cos(pi * onethird + alpha3), 0.5);
+        double sigma3 = pow(inv13 - 2.0 * sqrtalpha * cos(pi * onethird - alpha3), 0.5);
+        double sigmafinal = (sigma3 * (sigma1 - sigma2) * (sigma2 - sigma3)) / pow(sigma1, 2.0);
+        double evisc = (csles * delta_xyz) * (csles * delta_xyz);
+        g = evisc * sigmafinal;
     } else {
         double g11 = dudi * dudi + dudj * dvdi + dudk * dwdi;
         double g22 = dvdi * dudj + dvdj * dvdj + dvdk * dwdj;
@@ -156,13 +193,13 @@ __global__ void __launch_bounds__(128) k_subgrid(
 }
 
 void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles, int gotrad,
-                    double *gam, double *gamsc1, const double *u, const double *v, const double *w,
+                    double alpha, double *gam, double *gamsc1, const double *u, const double *v, const double *w,
                     const double *sc1, double *sc1var, double *sc1dis, const double *vdd,
                     const double *const *m, const SgsFast &f, cudaStream_t st)
 {
     // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
     k_subgrid<<<dim3((unsigned)((maxcell + 127) / 128), nb), 128, 0, st>>>(
-        blk, model, csles, gotrad, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m[0], m[1], m[2],
+        blk, model, csles, gotrad, alpha, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m[0], m[1], m[2],
         m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], f);
     les::count_launch(1);
 }

@@ -187,7 +187,7 @@ void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, cons
                        const double *dip, const double *djp, const double *rp, const double *dkp,   \
                        const double *dkw, const SgsFast &f, cudaStream_t st);                       \
     void launch_subgrid(const BlkDev *blk, int nb, long maxcell, int model, double csles,           \
-                        int gotrad, double *gam, double *gamsc1, const double *u, const double *v,  \
+                        int gotrad, double alpha, double *gam, double *gamsc1, const double *u, const double *v,  \
                         const double *w, const double *sc1, double *sc1var, double *sc1dis,         \
                         const double *vdd, const double *const *m, const SgsFast &f,               \
                         cudaStream_t st);

@@ -1571,7 +1571,8 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v
     memset(&F, 0, sizeof F);
     // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
     if (!c.c.exact && (r = fast_sgs_tabs(c, m[0], m[2], m[10], m[4], m[5], F))) return r;
-    LES_PHYS(c, launch_subgrid)(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, dg, dgs, du, dv,
+    LES_PHYS(c, launch_subgrid)(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, c.c.alpha, dg,
+                                dgs, du, dv,
                                 dw, dsc, dsv, dsd, dvd, m, F, c.stream);
     halo(c, 1, dg);
     halo(c, 1, dgs);

@@ -95,7 +95,7 @@ typedef struct lester_ctrl {
     double kappa;      /* ck: von Karman constant */
     double cwfun;      /* ca: log-law intercept term */
     double aplus;      /* van Driest A+ */
-    int model;         /* 0 none, 1 Smagorinsky, 2 WALE */
+    int model;         /* 0 none, 1 Smagorinsky, 2 WALE, 3 Sigma (edge/subgrid_sigma.F) */
     /* multigrid, code/defaults.F:59-71 */
     int nummgits, numpre, numpost, numcits, meth_cycle;
     double tolf, relax_pmg, relax_pmgc;

@@ -211,7 +211,7 @@ void orc_set_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const do
                    int nprof, unsigned long long seed);
 
 /* ---- eddy viscosity ---------------------------------------------------- */
-void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
+void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad, double alpha,
                  double *gam, double *gamsc1, const double *u,
                  const double *v, const double *w, const double *sc1,
                  double *sc1var, double *sc1dis, const double *vd_damping,

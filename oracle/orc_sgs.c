@@ -10,7 +10,7 @@
 #include <math.h>
 #include "orc_internal.h"
 
-static void sgs_block(int model, double csles, int gotrad, int nip1, int njp1,
+static void sgs_block(int model, double csles, int gotrad, double alpha, int nip1, int njp1,
                       int nkp1, double *gam, double *gamsc1, const double *u,
                       const double *v, const double *w, const double *sc1,
                       double *sc1var, double *sc1dis, const double *vdd,
@@ -100,6 +100,39 @@ static void sgs_block(int model, double csles, int gotrad, int nip1, int njp1,
                     double evisc = csles * delta_xyz * A(vdd, ijk);
                     evisc = evisc * evisc * sqrt(2.0 * sijsij);
                     g = evisc;
+                } else if (model == 3) {
+                    /* edge/subgrid_sigma.F:202-269; sqrt of the COMMON alpha
+                       (cb.control.inc) as written there */
+                    const double pi = 3.1415927;
+                    double g11 = dudi * dudi + dvdi * dvdi + dwdi * dwdi;
+                    double g12 = dudi * dudj + dvdi * dvdj + dwdi * dwdj;
+                    double g13 = dudi * dudk + dvdi * dvdk + dwdi * dwdk;
+                    double g21 = dudj * dudi + dvdj * dvdi + dwdj * dwdi;
+                    double g22 = dudj * dudj + dvdj * dvdj + dwdj * dwdj;
+                    double g23 = dudj * dudk + dvdj * dvdk + dwdj * dwdk;
+                    double g31 = dudk * dudi + dvdk * dvdi + dwdk * dwdi;
+                    double g32 = dudk * dudj + dvdk * dvdj + dwdk * dwdj;
+                    double g33 = dudk * dudk + dvdk * dvdk + dwdk * dwdk;
+                    double gg11 = g11 * g11 + g12 * g21 + g13 * g31;
+                    double gg22 = g21 * g12 + g22 * g22 + g23 * g32;
+                    double gg33 = g31 * g13 + g32 * g23 + g33 * g33;
+                    double tracegg = gg11 + gg22 + gg33;
+                    double invari1 = g11 + g22 + g33;
+                    double invari2 = 0.5 * (invari1 * invari1 - tracegg);
+                    double invari3 = g11 * (g22 * g33 - g23 * g32) - g12 * (g21 * g33 - g23 * g31) +
+                                     g13 * (g21 * g32 - g22 * g31);
+                    double alpha1 = (invari1 * invari1 * 0.11111111) - (invari2 * onethird);
+                    double alpha2 = (invari1 * invari1 * invari1 * 0.03703703703) -
+                                    (invari1 * invari2 * 0.16666666666) + (invari3 * 0.5);
+                    double alpha3 = onethird * acos(alpha2 / pow(alpha1, 1.5));
+                    double invari13rd = invari1 * onethird;
+                    double sqrtalpha = sqrt(alpha);
+                    double sigma1 = pow(invari13rd + 2.0 * sqrtalpha * cos(alpha3), 0.5);
+                    double sigma2 = pow(invari13rd - 2.0 * sqrtalpha * cos(pi * onethird + alpha3), 0.5);
+                    double sigma3 = pow(invari13rd - 2.0 * sqrtalpha * cos(pi * onethird - alpha3), 0.5);
+                    double sigmafinal = (sigma3 * (sigma1 - sigma2) * (sigma2 - sigma3)) / pow(sigma1, 2.0);
+                    double evisc = (csles * delta_xyz) * (csles * delta_xyz);
+                    g = evisc * sigmafinal;
                 } else {
                     /* subgrid_wale.F:200-227 */
                     double g11 = dudi * dudi + dudj * dvdi + dudk * dwdi;
@@ -132,7 +165,7 @@ static void sgs_block(int model, double csles, int gotrad, int nip1, int njp1,
 #undef G
 }
 
-void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
+void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad, double alpha,
                  double *gam, double *gamsc1, const double *u,
                  const double *v, const double *w, const double *sc1,
                  double *sc1var, double *sc1dis, const double *vd_damping,
@@ -158,8 +191,8 @@ void orc_subgrid(orc_ctx *c, int model, double csles, int gotrad,
                         A(sc1var, q) = 0.0;
                         A(sc1dis, q) = 0.0;
                     }
-        } else if (model == 1 || model == 2)
-            sgs_block(model, csles, gotrad, n[0], n[1], n[2], gam + p3, gamsc1 + p3,
+        } else if (model >= 1 && model <= 3)
+            sgs_block(model, csles, gotrad, alpha, n[0], n[1], n[2], gam + p3, gamsc1 + p3,
                       u + p3, v + p3, w + p3, sc1 + p3, sc1var + p3, sc1dis + p3,
                       vd_damping + p3, dip + p2, diu + p2, djp + p2, djv + p2,
                       dkp + p1, dkw + p1, hijp + p2, hjip + p2, hkip + p2,

@@ -46,7 +46,7 @@ void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, in
                     F->vd_damping, metric, F->dkp, F->dkw, twv);
     orc_set_virt_bc(c, ORC_SV_W, k->visc, k->kappa, k->aplus, k->ylaminar, F->w, F->rho,
                     F->vd_damping, metric, F->dkp, F->dkw, tww);
-    orc_subgrid(c, k->model, k->csles, k->gotrad, F->gam, F->gamsc1, F->u, F->v, F->w, F->sc1,
+    orc_subgrid(c, k->model, k->csles, k->gotrad, k->alpha, F->gam, F->gamsc1, F->u, F->v, F->w, F->sc1,
                 F->sc1var, F->sc1dis, F->vd_damping, MET(M_DIP), MET(M_DIU), MET(M_DJP),
                 MET(M_DJV), F->dkp, F->dkw, MET(M_HIJP), MET(M_HJIP), MET(M_HKIP), MET(M_HKJP),
                 MET(M_RP));

@@ -158,8 +158,8 @@ class Oracle:
         lib().orc_slipbc(self.ctx, C.c_double(dtime), *map(P, (djp, u, v, v_int, w, sc1, rho, p)))
 
     def subgrid(self, model, csles, gotrad, gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m,
-                dkp, dkw):
-        lib().orc_subgrid(self.ctx, model, C.c_double(csles), gotrad,
+                dkp, dkw, alpha=0.0):
+        lib().orc_subgrid(self.ctx, model, C.c_double(csles), gotrad, C.c_double(alpha),
                           *map(P, (gam, gamsc1, u, v, w, sc1, sc1var, sc1dis, vdd, m["dip"],
                                    m["diu"], m["djp"], m["djv"], dkp, dkw, m["hijp"], m["hjip"],
                                    m["hkip"], m["hkjp"], m["rp"])))

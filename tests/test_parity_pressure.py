@@ -286,7 +286,7 @@ def test_slipbc_bitwise(env):
 
 
 @pytest.mark.parametrize("exact", [1, 0])
-@pytest.mark.parametrize("model", [0, 1, 2])
+@pytest.mark.parametrize("model", [0, 1, 2, 3])
 def test_subgrid(env, model, exact):
     """exact build: 1e-13 per element (pow may differ in the last bit);
     fast build (reciprocal tables, sqrt-based WALE powers, split filter
@@ -297,9 +297,12 @@ def test_subgrid(env, model, exact):
     sc1 = s.rng.uniform(0, 1, c.n3_sg)
     vdd = s.rng.uniform(0.5, 1.0, c.n3_sg)
     outs = [np.zeros(c.n3_sg) for _ in range(4)]
+    # Sigma (model 3) takes the square root of the density relaxation
+    # factor alpha; 0.3 gives non-zero viscosities
+    alpha = 0.3 if model == 3 else 0.0
     s.orc.subgrid(model, 0.1, 0, outs[0], outs[1], u, v, w, sc1, outs[2], outs[3], vdd, s.m,
-                  s.dkp, s.dkw)
-    L.gpu_set_ctrl(L.default_ctrl(model=model, csles=0.1, exact=exact))
+                  s.dkp, s.dkw, alpha)
+    L.gpu_set_ctrl(L.default_ctrl(model=model, csles=0.1, exact=exact, alpha=alpha))
     od = [dev(np.zeros(c.n3_sg)) for _ in range(4)]
     md = {k: dev(val) for k, val in s.m.items()}
     L.subgrid(od[0], od[1], dev(u), dev(v), dev(w), dev(sc1), None, od[2], od[3], dev(vdd),
@@ -307,13 +310,19 @@ def test_subgrid(env, model, exact):
               md["hjip"], md["hkip"], md["hkjp"], md["rp"])
     for q in range(4):
         got = host(od[q])
-        if exact:
+        if exact and model != 3:
             np.testing.assert_allclose(got, outs[q], rtol=1e-13, atol=1e-300)
         else:
+            # Sigma: acos, cos and fractional powers (CUDA's against the
+            # C library's) in a formula that cancels where two singular
+            # values are close: relative L2 1e-10 over the finite values
             fin = np.isfinite(outs[q])
             assert np.array_equal(fin, np.isfinite(got)), q
             ref = outs[q][fin]
-            assert np.linalg.norm(got[fin] - ref) <= 1e-12 * max(np.linalg.norm(ref), 1e-300), q
+            tol = 1e-10 if model == 3 else 1e-12
+            assert np.linalg.norm(got[fin] - ref) <= tol * max(np.linalg.norm(ref), 1e-300), q
+    if model == 3:
+        assert np.nanmax(np.abs(outs[0])) > 0
 
 
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
