@@ -28,6 +28,10 @@ class Block:
     x: np.ndarray | None = None  # vertex coordinates along i (length nip1 + 1)
     y: np.ndarray | None = None
     z: np.ndarray | None = None
+    # general 2-D interior vertices x(i, j), y(i, j), i = 2..nip1, j = 2..njp1,
+    # stored (j, i) (an x.bin / y.bin block); used instead of x, y when set
+    xv: np.ndarray | None = None
+    yv: np.ndarray | None = None
 
 
 @dataclass
@@ -113,8 +117,12 @@ class Case:
             nip2, njp2, nkp2 = nip1 + 1, njp1 + 1, nkp1 + 1
             X = np.zeros((njp2, nip2))
             Y = np.zeros((njp2, nip2))
-            X[1:njp1, 1:nip1] = b.x[None, 1:nip1]
-            Y[1:njp1, 1:nip1] = b.y[1:njp1, None]
+            if b.xv is not None:
+                X[1:njp1, 1:nip1] = b.xv
+                Y[1:njp1, 1:nip1] = b.yv
+            else:
+                X[1:njp1, 1:nip1] = b.x[None, 1:nip1]
+                Y[1:njp1, 1:nip1] = b.y[1:njp1, None]
             Z = np.zeros(nkp2)
             Z[1:nkp1] = b.z[1:nkp1]
             _extrap2(X)
