@@ -46,6 +46,9 @@ DOMAIN = (30.0, 30.0, 15.0)
 EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
+# fast solvers tune their red-black launch shape, sweeps/omega and tail
+# threshold on the first solve (inside the warm-up steps)
+AUTOTUNE = 1
 # DRAM bytes of one level-1 k_rb<float> launch of the mixing-layer workload
 # (ncu: 52.0 MB read + 0.27 MB written), against 37.7 MB algorithmic
 RB_TRAFFIC = 52.28e6
@@ -165,10 +168,10 @@ def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     from fortranutils_gb300 import lester as L
     if wl == "mixing":
         return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
-                              rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov)
+                              rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov, autotune=AUTOTUNE)
     return L.default_ctrl(dtime=dtime, model=1, csles=0.1, rholo=1.0, rhohi=1.0,
                           visc=1.0 / 2800.0, psolve=psolve, rtol=1e-8, max_outer=200, exact=EXACT,
-                          krylov=krylov)
+                          krylov=krylov, autotune=AUTOTUNE)
 
 
 def host_state(case, ctrl, wl="mixing"):
@@ -275,12 +278,13 @@ def run_gpu(args):
             e1.record(stream)
             torch.cuda.synchronize()
         L.gpu_prof(False)
+        tuned = L.gpu_tuned(32 if mode == "mixed" else 64)
         ms = e0.elapsed_time(e1)
         kms, kl = L.gpu_prof_read()
         res[mode] = {"ms_per_step": ms / args.steps, "cycles": float(np.mean(cyc)),
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
                      "launches": L.gpu_launch_count() - launches0, "rb_ms": kms,
-                     "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl}
+                     "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
         del g
         if mode == "mixed" and not args.no_e2e:
             res[mode]["e2e"] = run_e2e(args, case, ctrl, wl)
@@ -478,7 +482,7 @@ def main():
     # launch: 12 B/cell per sweep (read f, b; write f) / 2 = 6 B x cells
     rb_avg_ms = mx["rb_ms"] / max(mx["rb_launches"], 1)
     achieved = 6.0 * ncell / (rb_avg_ms * 1e-3) / 1e9
-    sweeps = mx["ctrl"].rb_sweeps
+    sweeps = mx["tuned"]["rb_sweeps"] if mx["tuned"]["done"] else mx["ctrl"].rb_sweeps
     # outer iterations counted as defect correction unless flexible CG ran
     kry = 1 if args.outer == "fcg" else 0
     step_gbs = {m: step_bytes(m, r["cycles"], sweeps, kry) * ncell / (r["ms_per_step"] * 1e-3) / 1e9
@@ -501,12 +505,13 @@ def main():
                    "parallelism": "replicas" if world > 1 else "1 GPU",
                    "outer_loop": {"auto": "defect correction, flexible CG when a cycle stalls",
                                   "fcg": "flexible CG", "dc": "defect correction"}[args.outer]},
-        "mixed": {"vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"],
+        "mixed": {"vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"], "tuned": mx["tuned"],
                   "vcycle_ms": mx["solve_ms"] / max(mx["cycles"], 1),
                   "relres_max": mx["relres_max"]},
         "fp64": {"value": ncell / (fp["ms_per_step"] * 1e-3) / 1e6 * world,
                  "ms_per_step": fp["ms_per_step"], "vcycles_per_step": fp["cycles"],
                  "solve_ms": fp["solve_ms"], "vcycle_ms": fp["solve_ms"] / max(fp["cycles"], 1),
+                 "tuned": fp["tuned"],
                  "relres_max": fp["relres_max"]},
         "speedup_mixed_vs_fp64": fp["ms_per_step"] / mx["ms_per_step"],
         "solve_speedup_mixed_vs_fp64": fp["solve_ms"] / mx["solve_ms"],

@@ -213,7 +213,7 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 
 // ---- red-black SOR half sweep, all blocks of a level ----------------------
 template <typename T>
-__global__ void __launch_bounds__(256) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
+__global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
                                             const T *__restrict__ R, const T *__restrict__ D,
                                             T *__restrict__ x, const T *__restrict__ bb,
@@ -687,9 +687,10 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, cudaStream_t st)
+               const MfTab<T> &mf, int threads, cudaStream_t st)
 {
-    k_rb<T><<<dim3(nb_(maxhalf, 256), nb), 256, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
+    const int t = (threads == 128 || threads == 512) ? threads : 256;
+    k_rb<T><<<dim3(nb_(maxhalf, t), nb), t, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
     count_launch(1);
 }
 
@@ -837,7 +838,7 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
                                      cudaStream_t);                                                \
     template void launch_rb<T>(const BlkDev *, int, long, int, double, const T *, const T *,      \
                                const T *, const T *, T *, const T *, const PushDev *,             \
-                               const MfTab<T> &, cudaStream_t);                                   \
+                               const MfTab<T> &, int, cudaStream_t);                              \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
                                            const T *, const T *, const T *, const T *, const T *, \
                                            T *, const MfTab<T> &, cudaStream_t);                  \

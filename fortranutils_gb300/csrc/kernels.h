@@ -67,7 +67,7 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, cudaStream_t st);
+               const MfTab<T> &mf, int threads, cudaStream_t st);
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,

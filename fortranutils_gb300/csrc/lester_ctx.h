@@ -35,6 +35,12 @@ struct LevelGeom {
 
 // One defect-correction iteration of a fast solver (V-cycle, update, halo,
 // FP64 residual, read-back of two sums) captured as a CUDA graph.
+struct Tuned {
+    bool done = false;
+    int threads = 256, sweeps = 3, tail = 4096;
+    double omega = 1.5;
+};
+
 struct CycleGraph {
     cudaGraphExec_t exec = nullptr;
     const void *f = nullptr, *b = nullptr;
@@ -44,6 +50,7 @@ struct CycleGraph {
     bool mf = false;
     int tail = 0;
     int krylov = 0;
+    int threads = 0;                // red-black CTA size
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };
@@ -91,6 +98,8 @@ struct Ctx {
     int nprof = 0;
     unsigned long long inlet_seed = 0;
     int ncomp = 1;                  // connected components of the block graph
+    int rb_threads = 256;           // red-black launch shape (autotuned)
+    Tuned tuned[2];                 // autotuned solver settings [FP64, mixed]
     double *d_bmean = nullptr;      // per block: interior mean of b over its component
     const void *coef_key[7] = {0, 0, 0, 0, 0, 0, 0};
     long coef_gen_seen = -1;

@@ -724,7 +724,8 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
-                         F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.stream);
+                         F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.rb_threads,
+                         c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
@@ -800,7 +801,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
-        G.krylov == (int)kry)
+        G.krylov == (int)kry && G.threads == c.rb_threads)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -850,6 +851,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.mf = fset<T>(c).mf;
     G.tail = k.mg_tail;
     G.krylov = (int)kry;
+    G.threads = c.rb_threads;
     return 0;
 }
 
@@ -869,8 +871,8 @@ static int fcg_reset(Ctx &c)
 // as preconditioner, until ||b - A p|| <= rtol ||b||.  krylov 2 starts with
 // defect correction and moves to flexible CG (from the current p) at the
 // first cycle that fails to halve the residual.
-template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, double *b, double *residu,
-                                            int prec)
+template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f, double *b, double *residu,
+                                                int prec)
 {
 #define STAGE_CHECK(what)                                                                          \
     do {                                                                                           \
@@ -983,6 +985,86 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     if (rel > rtol && b2 > 0)
         return set_err(LES_ERR_NOT_CONVERGED, "relative residual %.3e after %d cycles", rel, it);
     return 0;
+}
+
+// Autotuner.  With ctrl.autotune set, the first fast solve of each
+// precision after init times candidate settings on the caller's own system
+// (the initial p restored before each trial) and keeps the fastest that
+// converges: the red-black launch shape (threads per CTA), then sweeps and
+// omega, then the single-CTA tail threshold, each stage starting from the
+// best so far.  The settings found (lester_gpu_tuned) replace the
+// controls' for the rest of the run; the call returns the solution of the
+// final setting.
+template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, double *b, double *residu, int prec)
+{
+    const int pi = sizeof(T) == 4 ? 1 : 0;
+    Tuned &tu = c.tuned[pi];
+    if (!c.c.autotune || tu.done) {
+        if (tu.done) {
+            c.c.rb_sweeps = tu.sweeps;
+            c.c.rb_omega = tu.omega;
+            c.c.mg_tail = tu.tail;
+            c.rb_threads = tu.threads;
+        }
+        return fast_solve_run<T>(c, A, f, b, residu, prec);
+    }
+    int r;
+    double *f0 = nullptr;
+    if (cudaMalloc(&f0, sizeof(double) * c.tot3) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(LES_ERR_NOMEM, "autotune: copy of p");
+    }
+    LES_CUDA(cudaMemcpyAsync(f0, f, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
+    struct Cand {
+        int threads, sweeps, tail;
+        double omega;
+    };
+    Cand best = {c.rb_threads, c.c.rb_sweeps, c.c.mg_tail, c.c.rb_omega};
+    double best_ms = 1e300;
+    auto trial = [&](const Cand &q) -> int {
+        c.rb_threads = q.threads;
+        c.c.rb_sweeps = q.sweeps;
+        c.c.rb_omega = q.omega;
+        c.c.mg_tail = q.tail;
+        LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
+        int rr = fast_solve_run<T>(c, A, f, b, residu, prec);
+        if (rr && rr != LES_ERR_NOT_CONVERGED && rr != LES_ERR_NONFINITE) return rr;
+        cudaGetLastError();
+        if (rr == 0) {
+            // a second run: the first one includes the graph capture
+            LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
+            if ((rr = fast_solve_run<T>(c, A, f, b, residu, prec))) return rr == LES_ERR_NOT_CONVERGED ? 0 : rr;
+            if (c.last_solve_ms < best_ms) {
+                best_ms = c.last_solve_ms;
+                best = q;
+            }
+        }
+        return 0;
+    };
+    const int thr[3] = {128, 256, 512};
+    for (int t : thr)
+        if ((r = trial({t, best.sweeps, best.tail, best.omega}))) break;
+    const int sw[5] = {2, 3, 4, 3, 2};
+    const double om[5] = {1.5, 1.5, 1.5, 1.3, 1.3};
+    const Cand s0 = best;
+    for (int q = 0; q < 5 && !r; q++)
+        if (!(sw[q] == s0.sweeps && om[q] == s0.omega)) r = trial({s0.threads, sw[q], s0.tail, om[q]});
+    const int tl[4] = {0, 1024, 4096, 16384};
+    const Cand s1 = best;
+    for (int q = 0; q < 4 && !r; q++)
+        if (tl[q] != s1.tail) r = trial({s1.threads, s1.sweeps, tl[q], s1.omega});
+    if (!r) {
+        tu = {true, best.threads, best.sweeps, best.tail, best.omega};
+        c.rb_threads = best.threads;
+        c.c.rb_sweeps = best.sweeps;
+        c.c.rb_omega = best.omega;
+        c.c.mg_tail = best.tail;
+        LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
+        r = fast_solve_run<T>(c, A, f, b, residu, prec);
+    }
+    cudaStreamSynchronize(c.stream);
+    cudaFree(f0);
+    return r;
 }
 
 static int ensure_scratch(Ctx &c)
@@ -1159,6 +1241,19 @@ int lester_gpu_solve_stats(double *out)
     for (int q = 0; q < 4; q++) out[q] = g_ctx->last_norms[q];
     out[4] = g_ctx->last_cycles;
     out[5] = g_ctx->last_relres;
+    return 0;
+}
+
+int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail)
+{
+    LES_NEED_CTX();
+    if (prec != 32 && prec != 64) return set_err(LES_ERR_ARG, "tuned: prec must be 32 or 64");
+    const Tuned &t = g_ctx->tuned[prec == 32 ? 1 : 0];
+    if (done) *done = t.done ? 1 : 0;
+    if (threads) *threads = t.threads;
+    if (sweeps) *sweeps = t.sweeps;
+    if (omega) *omega = t.omega;
+    if (tail) *tail = t.tail;
     return 0;
 }
 

@@ -60,6 +60,7 @@ class Ctrl(C.Structure):
         ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
+        ("autotune", C.c_int),
     ]
 
 
@@ -213,6 +214,15 @@ def gpu_solve_stats():
     _check(lib().lester_gpu_solve_stats(o))
     return {"rnorm": o[0], "fnorm": o[1], "enorm": o[2], "vnorm": o[3], "cycles": int(o[4]),
             "relres": o[5]}
+
+
+def gpu_tuned(prec: int) -> dict:
+    """Settings the autotuner chose for prec 64 (FP64) or 32 (mixed)."""
+    d, t, s, tl = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    om = C.c_double()
+    _check(lib().lester_gpu_tuned(int(prec), C.byref(d), C.byref(t), C.byref(s), C.byref(om), C.byref(tl)))
+    return {"done": bool(d.value), "rb_threads": t.value, "rb_sweeps": s.value, "rb_omega": om.value,
+            "mg_tail": tl.value}
 
 
 def gpu_solve_time() -> float:

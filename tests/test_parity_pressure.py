@@ -398,3 +398,31 @@ def test_fast_solvers_independent_boxes(psolve, gpulib):
         r = case.block_view(fr, ib, 0)[1:-1, 1:-1, 1:-1]
         g, r = g - g.mean(), r - r.mean()
         assert np.linalg.norm(g - r) <= 1e-7 * np.linalg.norm(r), ib
+
+
+@pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
+def test_autotune(psolve, gpulib):
+    """The first solve with autotune tries the candidate settings on the
+    system itself, keeps the fastest converged one and still returns the
+    converged solution; later solves use the chosen settings."""
+    s = cases.Setup("box_wall", seed=5)
+    c = s.case
+    b = s.interior_random(mg=True, zero_mean=True)
+    L.gpu_init(c.geom(), L.default_ctrl(psolve=psolve, rtol=1e-10, max_outer=200, autotune=1))
+    try:
+        prec = 64 if psolve == L.PSOLVE_FP64 else 32
+        assert not L.gpu_tuned(prec)["done"]
+        sols = []
+        for _ in range(2):
+            fd = dev(np.zeros(c.n3_mg))
+            L.lmg_solve(*[dev(a) for a in s.a], fd, dev(b), dev(np.zeros(c.n3_mg)))
+            assert L.gpu_solve_stats()["relres"] <= 1e-10
+            L.p_ref_subtract(fd)
+            sols.append(host(fd))
+        t = L.gpu_tuned(prec)
+    finally:
+        L.gpu_finalize()
+    assert t["done"]
+    assert t["rb_threads"] in (128, 256, 512) and t["rb_sweeps"] in (2, 3, 4)
+    assert t["rb_omega"] in (1.3, 1.5) and t["mg_tail"] in (0, 1024, 4096, 16384)
+    assert np.linalg.norm(sols[0] - sols[1]) <= 1e-8 * np.linalg.norm(sols[1])
