@@ -107,8 +107,15 @@ def new_state(case, metrics: dict, dkp, dkw) -> State:
 
 
 def cell_centre_y(case, ib: int = 0) -> np.ndarray:
+    """y at the cell centres j = 1..njp1 of block ib (ghosts by linear
+    extrapolation); for a block with 2-D vertices (a deck), along its first
+    interior i line."""
     b = case.blocks[ib]
-    yv = b.y.copy()
+    if b.xv is not None:
+        yv = np.zeros(b.n[1] + 1)
+        yv[1:b.n[1]] = 0.5 * (b.yv[:, 0] + b.yv[:, 1])
+    else:
+        yv = b.y.copy()
     yv[0] = 2 * yv[1] - yv[2]
     yv[-1] = 2 * yv[-2] - yv[-3]
     return 0.5 * (yv[:-1] + yv[1:])[: b.n[1]]
