@@ -47,6 +47,12 @@ struct ExitMetrics {
     const double *dm[4], *rm[4], *km[4];
 };
 
+// recycling: the running means and rms (read and written) and the target
+// mean and rms profiles of u, v, w, indexed by j (1-D device arrays)
+struct RecycProf {
+    const double *mean[3], *rms[3], *prof[3], *rprof[3];
+};
+
 // slots of the SAVEd outflow values (conv_exitbc.F:78): per-side totals
 // (index side 1..6), inflow and outflow sums, mass change
 enum { EX_TTL = 0, EX_ARHO = 7, EX_IN = 14, EX_OUT = 15, EX_MCHG = 16, EX_N = 17 };

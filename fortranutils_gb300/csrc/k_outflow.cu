@@ -281,6 +281,107 @@ __global__ void k_fixed_inlet(const BlkDev *__restrict__ blk, int iblk, int whic
     }
 }
 
+// ---- recycling (mas-recyc/recycling.F) ----------------------------------
+// plane averages over i = 2..nip1 of one block for every (j, k), j, k =
+// 2..njp1 / nkp1 (pass 0: u, v, w; pass 1: their squared deviations from
+// the running means), summed in the reference's order, one thread each
+__global__ void k_recyc_work(const BlkDev *__restrict__ blk, int ib, int pass, const double *__restrict__ u,
+                             const double *__restrict__ v, const double *__restrict__ w, const double *__restrict__ mu,
+                             const double *__restrict__ mv, const double *__restrict__ mw, double *__restrict__ work)
+{
+    const BlkDev b = blk[ib];
+    const int nip1 = b.n[0], njp1 = b.n[1], nkp1 = b.n[2];
+    const long jo = nip1, ko = (long)nip1 * njp1;
+    const int nj = njp1 - 1, nk = nkp1 - 1;
+    const long plane = (long)(njp1 + 1) * (nkp1 + 1);
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nj * nk; q += gridDim.x * blockDim.x) {
+        const int j = 2 + q % nj, k = 2 + q / nj;
+        const long base = b.off3 + jo * (j - 1) + ko * (k - 1);
+        const double *f[3] = {u, v, w};
+        const double *m[3] = {mu, mv, mw};
+        for (int c = 0; c < 3; c++) {
+            double s = 0.0;
+            for (int i = 2; i <= nip1; i++) {
+                double d = f[c][base + i - 1];
+                if (pass == 1) {
+                    d = d - m[c][j - 1];
+                    d = d * d;
+                }
+                s = s + d;
+            }
+            work[c * plane + (long)k * (njp1 + 1) + j] = s / (double)(nip1 - 1);
+        }
+    }
+}
+
+// the running means (pass 0) or rms (pass 1) per j from the plane averages
+__global__ void k_recyc_means(const BlkDev *__restrict__ blk, int ib, int pass, const double *__restrict__ work,
+                              double *__restrict__ mu, double *__restrict__ mv, double *__restrict__ mw,
+                              double *__restrict__ ru, double *__restrict__ rv, double *__restrict__ rw)
+{
+    const BlkDev b = blk[ib];
+    const int njp1 = b.n[1], nkp1 = b.n[2];
+    const long plane = (long)(njp1 + 1) * (nkp1 + 1);
+    const double cpfilt = 0.144;
+    double *m[3] = {mu, mv, mw}, *r[3] = {ru, rv, rw};
+    for (int j = 2 + blockIdx.x * blockDim.x + threadIdx.x; j <= njp1; j += gridDim.x * blockDim.x)
+        for (int c = 0; c < 3; c++) {
+            double s = 0.0;
+            for (int k = 2; k <= nkp1; k++) s = s + work[c * plane + (long)k * (njp1 + 1) + j];
+            s = s / (double)(nkp1 - 1);
+            if (pass == 0)
+                m[c][j - 1] = cpfilt * s + (1. - cpfilt) * m[c][j - 1];
+            else
+                r[c][j - 1] = sqrt(cpfilt * s + (1. - cpfilt) * (r[c][j - 1] * r[c][j - 1]));
+        }
+}
+
+// rescaling to the target mean and rms profiles (recycling.F:180-206)
+__global__ void k_recyc_rescale(const BlkDev *__restrict__ blk, int ib, int i0, int jmult, RecycProf P,
+                                double *__restrict__ u, double *__restrict__ v, double *__restrict__ w)
+{
+    const BlkDev b = blk[ib];
+    const int nip1 = b.n[0], njp1 = b.n[1], nkp1 = b.n[2];
+    const long jo = nip1, ko = (long)nip1 * njp1;
+    const int ni = nip1 - i0 + 1, nj = njp1 - 1, nk = nkp1 - 1;
+    const double small = 0.0000001;
+    double *f[3] = {u, v, w};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (long)ni * nj * nk; q += (long)gridDim.x * blockDim.x) {
+        const int i = i0 + (int)(q % ni), j = 2 + (int)((q / ni) % nj), k = 2 + (int)(q / ((long)ni * nj));
+        const long ijk = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+        for (int c = 0; c < 3; c++)
+            f[c][ijk] = (P.rprof[c][j + jmult - 1] / (P.rms[c][j - 1] + small)) * (f[c][ijk] - P.mean[c][j - 1]) +
+                        P.prof[c][j + jmult - 1];
+    }
+}
+
+// the recycling plane (i = 3 for u, i = 2 for v, w) of block src, in (k, j)
+// order, into the inflow plane of block dst (recycling.F:212-300)
+__global__ void k_recyc_copy(const BlkDev *__restrict__ blk, int src, int dst, double rhohi, double *__restrict__ u,
+                             double *__restrict__ v, double *__restrict__ w, double *__restrict__ sc1,
+                             double *__restrict__ rho, double *__restrict__ u_int, double *__restrict__ v_int,
+                             double *__restrict__ w_int)
+{
+    const BlkDev bs = blk[src], bd = blk[dst];
+    const long ns = (long)(bs.n[1] - 1) * (bs.n[2] - 1), nd = (long)(bd.n[1] - 1) * (bd.n[2] - 1);
+    const long n = ns < nd ? ns : nd;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const int js = 2 + (int)(q % (bs.n[1] - 1)), ks = 2 + (int)(q / (bs.n[1] - 1));
+        const int jd = 2 + (int)(q % (bd.n[1] - 1)), kd = 2 + (int)(q / (bd.n[1] - 1));
+        const long is = bs.off3 + 2 + (long)bs.n[0] * (js - 1) + (long)bs.n[0] * bs.n[1] * (ks - 1);
+        const long id = bd.off3 + 1 + (long)bd.n[0] * (jd - 1) + (long)bd.n[0] * bd.n[1] * (kd - 1);
+        const double us = u[is], vs = v[is - 1], ws = w[is - 1];
+        u[id] = us;
+        v[id - 1] = vs;
+        w[id - 1] = ws;
+        sc1[id - 1] = 1.0;
+        rho[id - 1] = rhohi;
+        u_int[id] = us;
+        v_int[id - 1] = vs;
+        w_int[id - 1] = ws;
+    }
+}
+
 // ================================================================ launchers
 namespace les {
 
@@ -337,6 +438,38 @@ void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, cons
     k_fixed_inlet<<<g, 256, 0, st>>>(blk, iblk, which, uprof, vprof, seed, step, rholo, rhohi, u, v, w, sc1, rho,
                                      u_int, v_int, w_int);
     count_launch(1);
+}
+
+void launch_recycling(const BlkDev *blk, const int *nijk, int nb, int step, int inblock, int jmult, double rhohi,
+                      const RecycProf &P, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
+                      double *v_int, double *w_int, double *work, cudaStream_t st)
+{
+    for (int b = inblock; b <= inblock + 7 && b <= nb; b++) {
+        const int *n = nijk + 3 * (b - 1);
+        unsigned g = (unsigned)(((long)(n[1] - 1) * (n[2] - 1) + 255) / 256);
+        for (int pass = 0; pass < 2; pass++) {
+            k_recyc_work<<<g, 256, 0, st>>>(blk, b - 1, pass, u, v, w, P.mean[0], P.mean[1], P.mean[2], work);
+            k_recyc_means<<<(unsigned)((n[1] + 127) / 128), 128, 0, st>>>(
+                blk, b - 1, pass, work, (double *)P.mean[0], (double *)P.mean[1], (double *)P.mean[2],
+                (double *)P.rms[0], (double *)P.rms[1], (double *)P.rms[2]);
+            count_launch(2);
+        }
+    }
+    for (int b = inblock; b <= inblock + 7 && b <= nb; b++) {
+        if (!(step % 100 == 0 && step >= 200)) break;
+        const int *n = nijk + 3 * (b - 1);
+        int i0 = b != inblock ? 1 : 2;
+        long cnt = (long)(n[0] - i0 + 1) * (n[1] - 1) * (n[2] - 1);
+        unsigned g = (unsigned)((cnt + 255) / 256);
+        k_recyc_rescale<<<g > 4096 ? 4096 : g, 256, 0, st>>>(blk, b - 1, i0, jmult, P, u, v, w);
+        count_launch(1);
+    }
+    if (inblock + 7 <= nb) {
+        const int *n = nijk + 3 * (inblock - 1);
+        unsigned g = (unsigned)(((long)(n[1] - 1) * (n[2] - 1) + 255) / 256);
+        k_recyc_copy<<<g, 256, 0, st>>>(blk, inblock + 6, inblock - 1, rhohi, u, v, w, sc1, rho, u_int, v_int, w_int);
+        count_launch(1);
+    }
 }
 
 } // namespace les

@@ -162,6 +162,10 @@ void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, cons
                         double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                         double *v_int, double *w_int, cudaStream_t st);
 
+void launch_recycling(const BlkDev *blk, const int *nijk, int nb, int step, int inblock, int jmult, double rhohi,
+                      const RecycProf &P, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
+                      double *v_int, double *w_int, double *work, cudaStream_t st);
+
 } // namespace les
 
 // k_phys.cu and k_sgs.cu, built twice (phys_variant.h): les_exact and les_fast

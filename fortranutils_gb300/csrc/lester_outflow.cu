@@ -279,4 +279,66 @@ int lester_fixed_inlet(double *hu, double *hv, double *hw, double *u_int, double
     return st.finish();
 }
 
+int lester_recycling(double *hu, double *hv, double *hw, double *u_int, double *v_int, double *w_int, double *u,
+                     double *v, double *w, const double *p, double *sc1, double *rho, const double *gam, const int *iseed,
+                     const double *y, const double *uprof, const double *vprof, const double *wprof,
+                     const double *uuprof, const double *vvprof, const double *wwprof, double *umean, double *vmean,
+                     double *wmean, double *uumean, double *vvmean, double *wwmean, const int *step,
+                     const int *inblock)
+{
+    (void)hu, (void)hv, (void)hw, (void)p, (void)gam, (void)iseed, (void)y;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    if (!step || !inblock) return set_err(LES_ERR_ARG, "recycling: NULL step / inblock");
+    if (*inblock < 1 || *inblock > c.g.numbl) return set_err(LES_ERR_ARG, "recycling: inblock %d", *inblock);
+    if (*inblock + 7 > c.g.numbl)
+        return set_err(LES_ERR_ARG, "recycling: the chain %d..%d needs %d blocks", *inblock, *inblock + 7,
+                       *inblock + 7);
+    if (c.nprof <= 0) return set_err(LES_ERR_ARG, "recycling: profile length not set (lester_gpu_set_inlet)");
+    Staging st(&c, __func__);
+    int r;
+    const double *pin[6] = {uprof, vprof, wprof, uuprof, vvprof, wwprof};
+    const double *dpro[6];
+    for (int q = 0; q < 6; q++)
+        if ((r = st.in(pin[q], c.nprof, &dpro[q]))) return r;
+    double *pio[6] = {umean, vmean, wmean, uumean, vvmean, wwmean};
+    double *dm[6];
+    for (int q = 0; q < 6; q++)
+        if ((r = st.io(pio[q], c.nprof, &dm[q]))) return r;
+    double *d3[8];
+    double *io3[8] = {u, v, w, sc1, rho, u_int, v_int, w_int};
+    for (int q = 0; q < 8; q++)
+        if ((r = st.io(io3[q], c.tot_sg3, &d3[q]))) return r;
+    std::vector<int> nijk(3 * c.g.numbl);
+    long wl = 0;
+    int njmax = 0;
+    for (int b = 1; b <= c.g.numbl; b++) {
+        for (int a = 0; a < 3; a++) nijk[3 * (b - 1) + a] = c.lv[1].n[b][a];
+        wl = std::max(wl, 3L * (c.lv[1].n[b][1] + 1) * (c.lv[1].n[b][2] + 1));
+        njmax = std::max(njmax, c.lv[1].n[b][1]);
+    }
+    int jmult = 0;
+    if (*inblock == c.inlet[2]) jmult = 0;
+    if (*inblock == c.inlet[1]) jmult = c.lv[1].n[*inblock][1] - 2;
+    if (njmax + jmult > c.nprof) return set_err(LES_ERR_ARG, "recycling: profiles shorter than %d", njmax + jmult);
+    double *work = nullptr;
+    if (cudaMalloc(&work, sizeof(double) * wl) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(LES_ERR_NOMEM, "recycling: work");
+    }
+    RecycProf P;
+    for (int q = 0; q < 3; q++) {
+        P.mean[q] = dm[q];
+        P.rms[q] = dm[3 + q];
+        P.prof[q] = dpro[q];
+        P.rprof[q] = dpro[3 + q];
+    }
+    launch_recycling(c.lv[1].d_blk, nijk.data(), c.g.numbl, *step, *inblock, jmult, c.c.rhohi, P, d3[0], d3[1],
+                     d3[2], d3[3], d3[4], d3[5], d3[6], d3[7], work, c.stream);
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    cudaFree(work);
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "recycling: %s", cudaGetErrorString(e));
+    return st.finish();
+}
+
 } // extern "C"

@@ -319,3 +319,22 @@ def bl6_inflow(case, delta: float = 0.5, uinf: float = 1.0):
         yc = 0.5 * (b.y[:-1] + b.y[1:])[: b.n[1]]
         up[off:off + b.n[1]] = uinf * np.tanh(np.maximum(yc, 0.0) / delta)
     return np.ascontiguousarray(up), np.ascontiguousarray(vp)
+
+
+def chain_case(nblocks: int, ni: int, nj: int, nk: int, ybc: int = L.BCT_WALL) -> Case:
+    """`nblocks` equal blocks in a row along x joined by interfaces: a fixed
+    inflow on block 1's west side, a convective outflow on the last block's
+    east side, `ybc` sides in y, periodic in z (a recycling chain)."""
+    I, P, F, Cv = L.BCT_INTERFACE, L.BCT_PERIODIC, L.BCT_FIXED, L.BCT_CONVECTIVE
+    lx = 0.5 * nblocks
+    xs = _axis(ni * nblocks, 0.0, lx)
+    blocks = []
+    for b in range(1, nblocks + 1):
+        x = np.zeros(ni + 3)
+        x[1:ni + 2] = xs[(b - 1) * ni + 1:b * ni + 2]
+        bc = [F if b == 1 else I, Cv if b == nblocks else I, ybc, ybc, P, P]
+        link = [(0, 0) if b == 1 else (b - 1, 2), (0, 0) if b == nblocks else (b + 1, 1), (0, 0), (0, 0),
+                (b, 6), (b, 5)]
+        blocks.append(Block(n=(ni + 2, nj + 2, nk + 2), bc=bc, link=link, x=x, y=_axis(nj, -1.0, 1.0),
+                            z=_axis(nk, 0.0, 1.0)))
+    return Case(blocks=blocks).setup()

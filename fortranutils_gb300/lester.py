@@ -436,3 +436,11 @@ def fixed_inlet(u_int, v_int, w_int, u, v, w, sc1, rho, iseed, uprof, vprof, ste
     _check(lib().lester_fixed_inlet(None, None, None, _p(u_int), _p(v_int), _p(w_int), _p(u), _p(v), _p(w),
                                     None, _p(sc1), _p(rho), None, _i(iseed), None, _p(uprof), _p(vprof),
                                     None, None, None, None, None, None, None, None, None, None, _i(step)))
+
+
+def recycling(u_int, v_int, w_int, u, v, w, sc1, rho, prof, means, step, inblock):
+    """mas-recyc/recycling.F:5: prof = (uprof, vprof, wprof, uuprof, vvprof,
+    wwprof), means = (umean, vmean, wmean, uumean, vvmean, wwmean)."""
+    _check(lib().lester_recycling(None, None, None, _p(u_int), _p(v_int), _p(w_int), _p(u), _p(v), _p(w), None,
+                                  _p(sc1), _p(rho), None, _i(0), None, *[_p(a) for a in prof],
+                                  *[_p(a) for a in means], _i(step), _i(inblock)))

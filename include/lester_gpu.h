@@ -478,6 +478,24 @@ int lester_fixed_inlet(double *hu, double *hv, double *hw, double *u_int, double
                        const double *umean, const double *vmean, const double *wmean, const double *uumean,
                        const double *vvmean, const double *wwmean, const int *step);
 
+/* mas-recyc/recycling.F:5 recycling(hu, hv, hw, u_int, v_int, w_int, u, v,
+ * w, p, sc1, rho, gam, iseed, y, uprof, vprof, wprof, uuprof, vvprof,
+ * wwprof, umean, vmean, wmean, uumean, vvmean, wwmean, step, inblock):
+ * recycling-rescaling inflow on the chain of blocks inblock..inblock+7 --
+ * running plane means and rms of u, v, w per j (relaxation 0.144), every
+ * 100th step from step 200 the chain rescaled to the target profiles, and
+ * the plane i = 3 of block inblock+7 copied into the inflow plane of block
+ * inblock (scalar 1, density rhohi).  The 1-D arrays have the length nprof
+ * of lester_gpu_set_inlet; the reference's file reads and writes of the
+ * running means are the caller's.  Call it immediately before lester_step,
+ * the position of its call in that program's step.F. */
+int lester_recycling(double *hu, double *hv, double *hw, double *u_int, double *v_int, double *w_int, double *u,
+                     double *v, double *w, const double *p, double *sc1, double *rho, const double *gam, const int *iseed,
+                     const double *y, const double *uprof, const double *vprof, const double *wprof,
+                     const double *uuprof, const double *vvprof, const double *wwprof, double *umean, double *vmean,
+                     double *wmean, double *uumean, double *vvmean, double *wwmean, const int *step,
+                     const int *inblock);
+
 /* ---- adjoint and tangent-linear runs ---------------------------------- */
 /* No counterpart in the reference.  A run of nsteps lester_step calls from
  * the state in `fields` (device arrays; the caller's arrays are not

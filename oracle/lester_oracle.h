@@ -206,6 +206,12 @@ void orc_fixed_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const 
                      unsigned long long seed, int step, double rholo, double rhohi, double *u,
                      double *v, double *w, double *sc1, double *rho, double *u_int, double *v_int,
                      double *w_int);
+/* mas-recyc/recycling.F:5 on blocks inblock..inblock+7 (1-based) */
+void orc_recycling(orc_ctx *c, int step, int inblock, const int inlet[4], double rhohi, double *u, double *v,
+                   double *w, double *sc1, double *rho, double *u_int, double *v_int, double *w_int,
+                   const double *uprof, const double *vprof, const double *wprof, const double *uuprof,
+                   const double *vvprof, const double *wwprof, double *umean, double *vmean, double *wmean,
+                   double *uumean, double *vvmean, double *wwmean);
 /* inlet configuration used by orc_step (profiles copied, nprof values each) */
 void orc_set_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const double *vprof,
                    int nprof, unsigned long long seed);

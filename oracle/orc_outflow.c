@@ -410,3 +410,128 @@ void orc_set_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const do
         }
     }
 }
+
+/* ---- recycling --------------------------------------------------------- */
+/* mas-recyc/recycling.F:5-366 on the chain of blocks inblock..inblock+7
+ * (1-based; those that exist), level 1.  The running means (umean ..
+ * wwmean, indexed by j) and the target profiles (uprof .. wwprof) are
+ * caller arrays; the reference's reads and writes of the means from and to
+ * files (recycling.F:55-66, 148-156) are left to the caller.  jmult: 0 for
+ * the inlet3 chain, njp1 - 2 for inlet2 (recycling.F:177-178), else 0.
+ * rhohi is the density the recycled inflow plane takes. */
+void orc_recycling(orc_ctx *c, int step, int inblock, const int inlet[4], double rhohi, double *u, double *v,
+                   double *w, double *sc1, double *rho, double *u_int, double *v_int, double *w_int,
+                   const double *uprof, const double *vprof, const double *wprof, const double *uuprof,
+                   const double *vvprof, const double *wwprof, double *umean, double *vmean, double *wmean,
+                   double *uumean, double *vvmean, double *wwmean)
+{
+    const double small = 0.0000001, cpfilt = 0.144;
+    double *vel[3] = {u, v, w};
+    double *mean[3] = {umean, vmean, wmean}, *rms[3] = {uumean, vvmean, wwmean};
+    const double *prof[3] = {uprof, vprof, wprof}, *rprof[3] = {uuprof, vvprof, wwprof};
+    for (int b = 1; b <= c->numbl; b++) {
+        if (b < inblock || b > inblock + 7) continue;
+        const int *n = c->mg_nijkp1[1][b];
+        int nip1 = n[0], njp1 = n[1], nkp1 = n[2];
+        long jo = nip1, ko = (long)nip1 * njp1, boff3 = c->off3[1][b];
+        double *work = (double *)calloc((size_t)3 * (njp1 + 1) * (nkp1 + 1), sizeof(double));
+#define WK(q, j, k) work[((size_t)(q) * (nkp1 + 1) + (k)) * (njp1 + 1) + (j)]
+        for (int pass = 0; pass < 2; pass++) {
+            for (int k = 2; k <= nkp1; k++) {
+                long koff = (k - 1) * ko + boff3;
+                for (int j = 2; j <= njp1; j++) {
+                    long jkoff = (j - 1) * jo + koff;
+                    for (int q = 0; q < 3; q++) {
+                        double s = 0.0;
+                        for (int i = 2; i <= nip1; i++) {
+                            double d = A(vel[q], i + jkoff);
+                            if (pass == 1) {
+                                d = d - A(mean[q], j);
+                                d = d * d;
+                            }
+                            s = s + d;
+                        }
+                        WK(q, j, k) = s / (double)(nip1 - 1);
+                    }
+                }
+            }
+            for (int j = 2; j <= njp1; j++)
+                for (int q = 0; q < 3; q++) {
+                    double s = 0.0;
+                    for (int k = 2; k <= nkp1; k++) s = s + WK(q, j, k);
+                    s = s / (double)(nkp1 - 1);
+                    if (pass == 0)
+                        A(mean[q], j) = cpfilt * s + (1. - cpfilt) * A(mean[q], j);
+                    else
+                        A(rms[q], j) = sqrt(cpfilt * s + (1. - cpfilt) * (A(rms[q], j) * A(rms[q], j)));
+                }
+        }
+#undef WK
+        free(work);
+    }
+    double *utemp = 0, *vtemp = 0, *wtemp = 0;
+    long ntemp = 0;
+    for (int b = 1; b <= c->numbl; b++) {
+        const int *n = c->mg_nijkp1[1][b];
+        int nip1 = n[0], njp1 = n[1], nkp1 = n[2];
+        long jo = nip1, ko = (long)nip1 * njp1, boff3 = c->off3[1][b];
+        if (step % 100 == 0 && step >= 200 && b >= inblock && b <= inblock + 7) {
+            int jmult = 0;
+            if (inblock == inlet[2]) jmult = 0;
+            if (inblock == inlet[1]) jmult = njp1 - 2;
+            for (int k = 2; k <= nkp1; k++) {
+                long koff = (k - 1) * ko + boff3;
+                for (int j = 2; j <= njp1; j++) {
+                    long jkoff = (j - 1) * jo + koff;
+                    for (int i = (b != inblock) ? 1 : 2; i <= nip1; i++) {
+                        long ijk = i + jkoff;
+                        for (int q = 0; q < 3; q++)
+                            A(vel[q], ijk) = (A(rprof[q], j + jmult) / (A(rms[q], j) + small)) *
+                                                 (A(vel[q], ijk) - A(mean[q], j)) +
+                                             A(prof[q], j + jmult);
+                    }
+                }
+            }
+        }
+        if (b == inblock + 7) {
+            ntemp = (long)(njp1 - 1) * (nkp1 - 1);
+            utemp = (double *)malloc(sizeof(double) * ntemp);
+            vtemp = (double *)malloc(sizeof(double) * ntemp);
+            wtemp = (double *)malloc(sizeof(double) * ntemp);
+            long jk = 0;
+            for (int k = 2; k <= nkp1; k++)
+                for (int j = 2; j <= njp1; j++) {
+                    long ijk = 3 + (j - 1) * jo + (k - 1) * ko + boff3, ijkw = ijk - 1;
+                    utemp[jk] = A(u, ijk);
+                    vtemp[jk] = A(v, ijkw);
+                    wtemp[jk] = A(w, ijkw);
+                    jk++;
+                }
+        }
+    }
+    if (utemp) {
+        for (int b = 1; b <= c->numbl; b++) {
+            if (b != inblock) continue;
+            const int *n = c->mg_nijkp1[1][b];
+            int nip1 = n[0], njp1 = n[1], nkp1 = n[2];
+            long jo = nip1, ko = (long)nip1 * njp1, boff3 = c->off3[1][b];
+            long jk = 0;
+            for (int k = 2; k <= nkp1; k++)
+                for (int j = 2; j <= njp1 && jk < ntemp; j++) {
+                    long ijk = 2 + (j - 1) * jo + (k - 1) * ko + boff3, ijkw = ijk - 1;
+                    A(u, ijk) = utemp[jk];
+                    A(v, ijkw) = vtemp[jk];
+                    A(w, ijkw) = wtemp[jk];
+                    A(sc1, ijkw) = 1.0;
+                    A(rho, ijkw) = rhohi;
+                    A(u_int, ijk) = A(u, ijk);
+                    A(v_int, ijkw) = A(v, ijkw);
+                    A(w_int, ijkw) = A(w, ijkw);
+                    jk++;
+                }
+        }
+        free(utemp);
+        free(vtemp);
+        free(wtemp);
+    }
+}

@@ -295,3 +295,12 @@ Oracle.conv_exitbc = _orc_conv_exitbc
 Oracle.mass_change = _orc_mass_change
 Oracle.fixed_inlet = _orc_fixed_inlet
 Oracle.set_inlet = _orc_set_inlet
+
+
+def _orc_recycling(self, step, inblock, inlet, rhohi, u, v, w, sc1, rho, u_int, v_int, w_int, prof, means):
+    ib = (C.c_int * 4)(*inlet)
+    lib().orc_recycling(self.ctx, int(step), int(inblock), ib, C.c_double(rhohi),
+                        *map(P, (u, v, w, sc1, rho, u_int, v_int, w_int)), *map(P, prof), *map(P, means))
+
+
+Oracle.recycling = _orc_recycling

@@ -176,3 +176,44 @@ def test_steps_six_blocks(psolve, gpulib):
     bad = {n: rel(got[n], ref[n]) for n in ("u", "v", "w", "sc1", "rho", "rhonp1") if rel(got[n], ref[n]) > tol}
     assert not bad, bad
     assert rel(got["u"], s["u"]) > 1e-6
+
+
+def test_recycling_bitwise(gpulib):
+    """The recycling-rescaling inflow on an eight-block chain: running
+    means every step, rescaling at step 200, the plane copy; every array
+    bitwise (the sums run in the reference's order on both sides)."""
+    case = grid.chain_case(8, 6, 8, 4)
+    cases.CASES["chain"] = lambda: case
+    try:
+        st = cases.Setup("chain", seed=3)
+    finally:
+        del cases.CASES["chain"]
+    rng = np.random.default_rng(21)
+    nprof = 32
+    prof = [np.ascontiguousarray(1.0 + 0.1 * rng.random(nprof)) for _ in range(6)]
+    means0 = [np.ascontiguousarray(0.5 + 0.1 * rng.random(nprof)) for _ in range(6)]
+    s = state(st, 12)
+    inlet = [0, 0, 1, 0]
+    names = ("u", "v", "w", "sc1", "rho", "u_int", "v_int", "w_int")
+    ref = s.to("numpy")
+    rmeans = [m.copy() for m in means0]
+    L.gpu_init(case.geom(), L.default_ctrl(rholo=1.0, rhohi=1.5))
+    try:
+        L.gpu_set_inlet(inlet, prof[0], prof[1], 0)
+        g = s.to("torch")
+        import torch
+        gmeans = [torch.from_numpy(m.copy()).cuda() for m in means0]
+        gprof = [torch.from_numpy(p).cuda() for p in prof]
+        for step in (199, 200):
+            st.orc.recycling(step, 1, inlet, 1.5, *[ref[n] for n in names], prof, rmeans)
+            L.recycling(g["u_int"], g["v_int"], g["w_int"], g["u"], g["v"], g["w"], g["sc1"], g["rho"], gprof,
+                        gmeans, step, 1)
+        got = g.to("numpy")
+        gm = [m.cpu().numpy() for m in gmeans]
+    finally:
+        L.gpu_finalize()
+    for n in names:
+        np.testing.assert_array_equal(got[n], ref[n], err_msg=n)
+    for a, b in zip(gm, rmeans):
+        np.testing.assert_array_equal(a, b)
+    assert not np.array_equal(ref["u"], s["u"])
