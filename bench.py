@@ -46,9 +46,6 @@ DOMAIN = (30.0, 30.0, 15.0)
 EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
-# fast solvers tune their red-black launch shape, sweeps/omega and tail
-# threshold on the first solve (inside the warm-up steps)
-AUTOTUNE = 1
 # DRAM bytes of one level-1 k_rb<float> launch of the mixing-layer workload
 # (ncu: 52.0 MB read + 0.27 MB written), against 37.7 MB algorithmic
 RB_TRAFFIC = 52.28e6
@@ -164,14 +161,20 @@ def cfl_dt(case, s, cfl=0.3, dfs=0.2, visc=1.0 / 2800.0):
     return min(cfl / cmax, dfs / dmax)
 
 
+SMOOTHER = "auto"
+
+
 def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     from fortranutils_gb300 import lester as L
+    sm = dict(autotune=3) if SMOOTHER == "auto" else dict(autotune=0)
+    if SMOOTHER == "line":
+        sm.update(rb_line=1, rb_omega=1.2, rb_sweeps=2)
     if wl == "mixing":
         return L.default_ctrl(dtime=0.01, model=2, csles=0.5, rholo=1.0, rhohi=2.0, psolve=psolve,
-                              rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov, autotune=AUTOTUNE)
+                              rtol=1e-8, max_outer=200, exact=EXACT, krylov=krylov, **sm)
     return L.default_ctrl(dtime=dtime, model=1, csles=0.1, rholo=1.0, rhohi=1.0,
                           visc=1.0 / 2800.0, psolve=psolve, rtol=1e-8, max_outer=200, exact=EXACT,
-                          krylov=krylov, autotune=AUTOTUNE)
+                          krylov=krylov, **sm)
 
 
 def host_state(case, ctrl, wl="mixing"):
@@ -443,12 +446,17 @@ def main():
     ap.add_argument("--outer", default="auto", choices=["auto", "fcg", "dc"],
                     help="fast solvers' outer loop: defect correction switching to flexible CG "
                          "when a cycle stalls (auto), flexible CG, or defect correction")
+    ap.add_argument("--smoother", default="auto", choices=["auto", "point", "line"],
+                    help="fast solvers' smoother: autotuned on the third solve (inside the warm-up "
+                         "steps), point red-black, or y-line zebra relaxation")
     ap.add_argument("--workload", default="mixing", choices=list(WORKLOADS),
                     help="mixing: the headline mixing layer; channel64: the 64^3 plain channel; "
                          "channel512: the 512x384x256 stretched channel")
     ap.add_argument("--shape", type=int, nargs=3, default=None,
                     help="cells per axis (other shapes than the workload's are for profiling only)")
     args = ap.parse_args()
+    global SMOOTHER
+    SMOOTHER = args.smoother
     if args.shape is None:
         args.shape = list(WORKLOADS[args.workload]["shape"])
     rank, world, local = dist_env()

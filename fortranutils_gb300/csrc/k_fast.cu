@@ -225,6 +225,74 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
     rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
 }
 
+// ---- y-line zebra relaxation ---------------------------------------------
+// One thread per (i, k) column with (i + k) % 2 == color: the column's
+// tridiagonal system in j (couplings N to j -/+ 1, the i and k neighbours
+// at their current values, the ghost rows j = 1 and nj + 2 known) solved by
+// the Thomas algorithm through the scratch arrays cp, dp (same layout as
+// x), then x += omega (x_line - x).  Strong coupling in y -- cells much
+// thinner than they are long, as at stretched walls -- is what point
+// smoothing cannot damp and line relaxation removes.
+template <typename T>
+__global__ void __launch_bounds__(256) k_yline(const BlkDev *__restrict__ blk, int color, T omega,
+                                               const T *__restrict__ E, const T *__restrict__ N,
+                                               const T *__restrict__ R, const T *__restrict__ D,
+                                               T *__restrict__ x, const T *__restrict__ bb, MfTab<T> mf,
+                                               T *__restrict__ cp, T *__restrict__ dp)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
+    const unsigned nh = (unsigned)(ni + 1) >> 1;
+    const unsigned q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nh * (unsigned)nk) return;
+    const unsigned kq = q / nh;
+    const int k = (int)kq + 2;
+    const int i = 2 + 2 * (int)(q - kq * nh) + ((2 + k + color) & 1);
+    if (i > ni + 1) return;
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long p0 = b.off3 + (i - 1) + ko * (k - 1);
+    T cprev = 0, dprev = 0;
+    for (int j = 2; j <= nj + 1; j++) {
+        const long p = p0 + jo * (j - 1);
+        T c[6], dinv;
+        if (mf.E2) {
+            coefs_mf(b, mf, i, j, k, c, dinv);
+        } else {
+            c[0] = E[p - 1];
+            c[1] = E[p];
+            c[2] = N[p - jo];
+            c[3] = N[p];
+            c[4] = R[p - ko];
+            c[5] = R[p];
+            dinv = D[p];
+        }
+        T rhs = bb[p] + c[0] * x[p - 1] + c[1] * x[p + 1] + c[4] * x[p - ko] + c[5] * x[p + ko];
+        T lo = c[2], up = c[3];
+        if (j == 2) {
+            rhs += lo * x[p - jo];
+            lo = 0;
+        }
+        if (j == nj + 1) {
+            rhs += up * x[p + jo];
+            up = 0;
+        }
+        const T m = (T)1 / dinv - lo * cprev;
+        const T cj = up / m, dj = (rhs + lo * dprev) / m;
+        cp[p] = cj;
+        dp[p] = dj;
+        cprev = cj;
+        dprev = dj;
+    }
+    T xnext = 0;
+    for (int j = nj + 1; j >= 2; j--) {
+        const long p = p0 + jo * (j - 1);
+        const T xl = dp[p] + cp[p] * xnext;
+        xnext = xl;
+        const T xo = x[p];
+        x[p] = xo + omega * (xl - xo);
+    }
+}
+
 // ---- residual + restriction ------------------------------------------------
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
 // children are summed into the coarse right-hand side.
@@ -695,6 +763,14 @@ void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega,
 }
 
 template <typename T>
+void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double omega, const T *E, const T *N,
+                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, cudaStream_t st)
+{
+    k_yline<T><<<dim3(nb_(maxik_half, 128), nb), 128, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, mf, cp, dp);
+    count_launch(1);
+}
+
+template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
                            const MfTab<T> &mf, cudaStream_t st)
@@ -839,6 +915,9 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
     template void launch_rb<T>(const BlkDev *, int, long, int, double, const T *, const T *,      \
                                const T *, const T *, T *, const T *, const PushDev *,             \
                                const MfTab<T> &, int, cudaStream_t);                              \
+    template void launch_yline<T>(const BlkDev *, int, long, int, double, const T *, const T *,   \
+                                  const T *, const T *, T *, const T *, const MfTab<T> &, T *, T *, \
+                                  cudaStream_t);                                                  \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
                                            const T *, const T *, const T *, const T *, const T *, \
                                            T *, const MfTab<T> &, cudaStream_t);                  \

@@ -68,6 +68,11 @@ template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
                const MfTab<T> &mf, int threads, cudaStream_t st);
+// y-line zebra relaxation of one colour of (i, k) columns (maxik_half: the
+// most columns of one colour in a block)
+template <typename T>
+void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double omega, const T *E, const T *N,
+                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, cudaStream_t st);
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,

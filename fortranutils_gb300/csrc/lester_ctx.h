@@ -37,7 +37,8 @@ struct LevelGeom {
 // FP64 residual, read-back of two sums) captured as a CUDA graph.
 struct Tuned {
     bool done = false;
-    int threads = 256, sweeps = 3, tail = 4096;
+    int threads = 256, sweeps = 3, tail = 4096, line = 0;
+    int seen = 0;  // solves before tuning
     double omega = 1.5;
 };
 
@@ -51,6 +52,7 @@ struct CycleGraph {
     int tail = 0;
     int krylov = 0;
     int threads = 0;                // red-black CTA size
+    int line = 0;                   // y-line relaxation
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };
@@ -58,6 +60,7 @@ struct CycleGraph {
 // device buffers of the fast solvers, precision T
 template <typename T> struct FastSet {
     T *E = nullptr, *N = nullptr, *R = nullptr, *D = nullptr, *x = nullptr, *b = nullptr;
+    T *cp = nullptr, *dp = nullptr;  // y-line Thomas scratch (all levels), at first use
     MfTab<T> tab;       // separable factors (FP32 solver)
     bool mf = false;    // tab checked against every coefficient: used
 };

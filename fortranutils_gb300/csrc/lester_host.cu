@@ -437,8 +437,8 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_nrm3);
     cudaFree(c->d_metbuf);
     cudaFree(c->d_flag);
-    void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b,
-                  c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b,
+    void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b, c->f32.cp, c->f32.dp,
+                  c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b, c->f64.cp, c->f64.dp,
                   c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
                   c->d_exit, c->d_sideout, c->d_uprof, c->d_vprof};
     for (void *p : fp) cudaFree(p);
@@ -702,6 +702,16 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
 {
     FastSet<T> &F = fset<T>(c);
     LevelGeom &L = c.lv[lev];
+    if (c.c.rb_line && F.cp) {
+        // y-line zebra relaxation; halos exchanged after each colour
+        for (int s = 0; s < nsweep; s++)
+            for (int color = 0; color < 2; color++) {
+                launch_yline<T>(L.d_blk, c.g.numbl, L.maxik, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x, F.b,
+                                F.mf ? F.tab : MfTab<T>(), F.cp, F.dp, c.stream);
+                launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
+            }
+        return;
+    }
     // level-1 smoother launches are bracketed by events: recorded into the
     // graph while capturing, or on the stream when timing eagerly
     bool cap = c.cap_ev && lev == 1;
@@ -801,7 +811,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
-        G.krylov == (int)kry && G.threads == c.rb_threads)
+        G.krylov == (int)kry && G.threads == c.rb_threads && G.line == k.rb_line)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -852,6 +862,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.tail = k.mg_tail;
     G.krylov = (int)kry;
     G.threads = c.rb_threads;
+    G.line = k.rb_line;
     return 0;
 }
 
@@ -884,6 +895,12 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
     if (r) return r;
     STAGE_CHECK("coefficients");
     FastSet<T> &F = fset<T>(c);
+    if (c.c.rb_line && !F.cp) {
+        if (cudaMalloc(&F.cp, sizeof(T) * c.tot3) != cudaSuccess || cudaMalloc(&F.dp, sizeof(T) * c.tot3) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(LES_ERR_NOMEM, "y-line scratch");
+        }
+    }
     LevelGeom &L1 = c.lv[1];
     int nb = c.g.numbl;
     double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
@@ -999,11 +1016,15 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
 {
     const int pi = sizeof(T) == 4 ? 1 : 0;
     Tuned &tu = c.tuned[pi];
-    if (!c.c.autotune || tu.done) {
+    // autotune 1: tune on the first solve; 2: on the second (the first
+    // solve of a run usually starts from p = 0 and is not representative)
+    const bool skip = c.c.autotune >= 2 && ++tu.seen < c.c.autotune;
+    if (!c.c.autotune || tu.done || skip) {
         if (tu.done) {
             c.c.rb_sweeps = tu.sweeps;
             c.c.rb_omega = tu.omega;
             c.c.mg_tail = tu.tail;
+            c.c.rb_line = tu.line;
             c.rb_threads = tu.threads;
         }
         return fast_solve_run<T>(c, A, f, b, residu, prec);
@@ -1018,14 +1039,16 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
     struct Cand {
         int threads, sweeps, tail;
         double omega;
+        int line;
     };
-    Cand best = {c.rb_threads, c.c.rb_sweeps, c.c.mg_tail, c.c.rb_omega};
+    Cand best = {c.rb_threads, c.c.rb_sweeps, c.c.mg_tail, c.c.rb_omega, c.c.rb_line};
     double best_ms = 1e300;
     auto trial = [&](const Cand &q) -> int {
         c.rb_threads = q.threads;
         c.c.rb_sweeps = q.sweeps;
         c.c.rb_omega = q.omega;
         c.c.mg_tail = q.tail;
+        c.c.rb_line = q.line;
         LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
         int rr = fast_solve_run<T>(c, A, f, b, residu, prec);
         if (rr && rr != LES_ERR_NOT_CONVERGED && rr != LES_ERR_NONFINITE) return rr;
@@ -1034,31 +1057,44 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
             // a second run: the first one includes the graph capture
             LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
             if ((rr = fast_solve_run<T>(c, A, f, b, residu, prec))) return rr == LES_ERR_NOT_CONVERGED ? 0 : rr;
-            if (c.last_solve_ms < best_ms) {
+            // a challenger has to beat the incumbent by 3%: one solve is a
+            // small sample of the solves to come
+            if (c.last_solve_ms < (best_ms < 1e300 ? 0.97 : 1.0) * best_ms) {
                 best_ms = c.last_solve_ms;
                 best = q;
             }
         }
         return 0;
     };
+    // the controls as given first: the incumbent
+    r = trial(best);
     const int thr[3] = {128, 256, 512};
     for (int t : thr)
-        if ((r = trial({t, best.sweeps, best.tail, best.omega}))) break;
-    const int sw[5] = {2, 3, 4, 3, 2};
-    const double om[5] = {1.5, 1.5, 1.5, 1.3, 1.3};
+        if (!r && t != best.threads) r = trial({t, best.sweeps, best.tail, best.omega, best.line});
+    // point red-black (sweeps, omega), then y-line zebra relaxation
+    const int sw[9] = {2, 3, 4, 3, 2, 1, 2, 2, 3};
+    const double om[9] = {1.5, 1.5, 1.5, 1.3, 1.3, 1.0, 1.0, 1.2, 1.0};
+    const int ln[9] = {0, 0, 0, 0, 0, 1, 1, 1, 1};
     const Cand s0 = best;
-    for (int q = 0; q < 5 && !r; q++)
-        if (!(sw[q] == s0.sweeps && om[q] == s0.omega)) r = trial({s0.threads, sw[q], s0.tail, om[q]});
+    for (int q = 0; q < 9 && !r; q++)
+        if (!(sw[q] == s0.sweeps && om[q] == s0.omega && ln[q] == s0.line))
+            r = trial({s0.threads, sw[q], s0.tail, om[q], ln[q]});
     const int tl[4] = {0, 1024, 4096, 16384};
     const Cand s1 = best;
     for (int q = 0; q < 4 && !r; q++)
-        if (tl[q] != s1.tail) r = trial({s1.threads, s1.sweeps, tl[q], s1.omega});
+        if (tl[q] != s1.tail) r = trial({s1.threads, s1.sweeps, tl[q], s1.omega, s1.line});
     if (!r) {
-        tu = {true, best.threads, best.sweeps, best.tail, best.omega};
+        tu.done = true;
+        tu.threads = best.threads;
+        tu.sweeps = best.sweeps;
+        tu.tail = best.tail;
+        tu.omega = best.omega;
+        tu.line = best.line;
         c.rb_threads = best.threads;
         c.c.rb_sweeps = best.sweeps;
         c.c.rb_omega = best.omega;
         c.c.mg_tail = best.tail;
+        c.c.rb_line = best.line;
         LES_CUDA(cudaMemcpyAsync(f, f0, sizeof(double) * c.tot3, cudaMemcpyDeviceToDevice, c.stream));
         r = fast_solve_run<T>(c, A, f, b, residu, prec);
     }
@@ -1244,7 +1280,7 @@ int lester_gpu_solve_stats(double *out)
     return 0;
 }
 
-int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail)
+int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail, int *line)
 {
     LES_NEED_CTX();
     if (prec != 32 && prec != 64) return set_err(LES_ERR_ARG, "tuned: prec must be 32 or 64");
@@ -1254,6 +1290,7 @@ int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *ome
     if (sweeps) *sweeps = t.sweeps;
     if (omega) *omega = t.omega;
     if (tail) *tail = t.tail;
+    if (line) *line = t.line;
     return 0;
 }
 

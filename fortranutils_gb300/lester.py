@@ -60,7 +60,7 @@ class Ctrl(C.Structure):
         ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
-        ("autotune", C.c_int),
+        ("rb_line", C.c_int), ("autotune", C.c_int),
     ]
 
 
@@ -218,11 +218,12 @@ def gpu_solve_stats():
 
 def gpu_tuned(prec: int) -> dict:
     """Settings the autotuner chose for prec 64 (FP64) or 32 (mixed)."""
-    d, t, s, tl = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    d, t, s, tl, ln = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
     om = C.c_double()
-    _check(lib().lester_gpu_tuned(int(prec), C.byref(d), C.byref(t), C.byref(s), C.byref(om), C.byref(tl)))
+    _check(lib().lester_gpu_tuned(int(prec), C.byref(d), C.byref(t), C.byref(s), C.byref(om), C.byref(tl),
+                                  C.byref(ln)))
     return {"done": bool(d.value), "rb_threads": t.value, "rb_sweeps": s.value, "rb_omega": om.value,
-            "mg_tail": tl.value}
+            "mg_tail": tl.value, "rb_line": ln.value}
 
 
 def gpu_solve_time() -> float:

@@ -129,10 +129,16 @@ typedef struct lester_ctrl {
                           strongly stretched grids); 2 = defect correction
                           until a cycle fails to halve the residual, then
                           flexible CG from the current p */
-    int autotune;      /* fast solvers: 1 = the first solve of each precision
-                          times candidate settings (red-black CTA size,
-                          sweeps and omega, tail threshold) on its own system
-                          and keeps the fastest for the rest of the run
+    int rb_line;       /* fast solvers: 1 = y-line zebra relaxation (a
+                          tridiagonal solve along j per (i, k) column,
+                          checkerboard in i + k) instead of point red-black
+                          on the levels above the single-CTA tail; for
+                          cells much thinner in y than in x and z */
+    int autotune;      /* fast solvers: n >= 1 = the n-th solve of each
+                          precision times candidate settings (red-black CTA
+                          size, sweeps and omega, point or y-line smoothing,
+                          tail threshold) on its own system and keeps the
+                          fastest for the rest of the run
                           (lester_gpu_tuned); 0 = the controls as given */
 } lester_ctrl;
 
@@ -191,9 +197,9 @@ int lester_gpu_solve_stats(double *out);
  * its first residual to its last, by CUDA events on the library stream */
 int lester_gpu_solve_time(double *ms);
 /* the settings the autotuner chose for precision prec (64 FP64, 32 mixed):
- * red-black threads per CTA, sweeps, omega and tail threshold; *done = 0
- * while it has not run */
-int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail);
+ * red-black threads per CTA, sweeps, omega, tail threshold and whether
+ * y-line relaxation won; *done = 0 while it has not run */
+int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail, int *line);
 /* kernel timing inside a timed region: CUDA events around each launch of
  * the level-1 red-black smoother of the fast solvers.  prof(1) clears and
  * starts, prof(0) stops; prof_read returns the summed milliseconds and the

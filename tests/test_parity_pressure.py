@@ -326,8 +326,8 @@ def test_subgrid(env, model, exact):
 
 
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
-@pytest.mark.parametrize("krylov", [1, 2])
-def test_fast_solvers_stretched_channel(psolve, krylov, gpulib):
+@pytest.mark.parametrize("krylov,line", [(1, 0), (2, 0), (2, 1)])
+def test_fast_solvers_stretched_channel(psolve, krylov, line, gpulib):
     """A wall-stretched channel (tanh beta 2.2, 64x48x32): with a random
     right-hand side the plain defect-correction cycle converges slowly or
     not at all here (the coarse-grid correction overshoots near the
@@ -345,7 +345,10 @@ def test_fast_solvers_stretched_channel(psolve, krylov, gpulib):
     s.orc.set_jumble(0)
     s.orc.lmg_solve(O.mgctrl(nummgits=120, tolf=1e-15), s.a, fr, b.copy(), rr)
     s.orc.p_ref_subtract(fr)
-    L.gpu_init(case.geom(), L.default_ctrl(psolve=psolve, rtol=1e-10, max_outer=60, krylov=krylov))
+    ctrl = L.default_ctrl(psolve=psolve, rtol=1e-10, max_outer=60, krylov=krylov, rb_line=line)
+    if line:
+        ctrl.rb_omega, ctrl.rb_sweeps = 1.0, 2
+    L.gpu_init(case.geom(), ctrl)
     try:
         fd = dev(np.zeros(case.n3_mg))
         L.lmg_solve(*[dev(a) for a in s.a], fd, dev(b), dev(np.zeros(case.n3_mg)))
@@ -423,6 +426,7 @@ def test_autotune(psolve, gpulib):
     finally:
         L.gpu_finalize()
     assert t["done"]
-    assert t["rb_threads"] in (128, 256, 512) and t["rb_sweeps"] in (2, 3, 4)
-    assert t["rb_omega"] in (1.3, 1.5) and t["mg_tail"] in (0, 1024, 4096, 16384)
+    assert t["rb_threads"] in (128, 256, 512) and t["rb_sweeps"] in (1, 2, 3, 4)
+    assert t["rb_omega"] in (1.0, 1.2, 1.3, 1.5) and t["mg_tail"] in (0, 1024, 4096, 16384)
+    assert t["rb_line"] in (0, 1)
     assert np.linalg.norm(sols[0] - sols[1]) <= 1e-8 * np.linalg.norm(sols[1])
