@@ -53,6 +53,12 @@ struct RecycProf {
     const double *mean[3], *rms[3], *prof[3], *rprof[3];
 };
 
+// the 16 running span averages of statistics.F (2-D, level-1 metric
+// layout): um vm wm pm rhom ruv rvw rwu ruu rvv rww rrh fm rff sc1varm T_m
+struct StatOut {
+    double *f[16];
+};
+
 // slots of the SAVEd outflow values (conv_exitbc.F:78): per-side totals
 // (index side 1..6), inflow and outflow sums, mass change
 enum { EX_TTL = 0, EX_ARHO = 7, EX_IN = 14, EX_OUT = 15, EX_MCHG = 16, EX_N = 17 };

@@ -382,6 +382,102 @@ __global__ void k_recyc_copy(const BlkDev *__restrict__ blk, int src, int dst, d
     }
 }
 
+// ---- span-averaged statistics (code/statistics.F) ------------------------
+// cell-centred velocities of one block as statistics.F's centre makes them:
+// the interior, then the i, k and j boundary planes; edge cells stay 0
+__global__ void k_centre(const BlkDev *__restrict__ blk, const double *__restrict__ u, const double *__restrict__ v,
+                         const double *__restrict__ w, double *__restrict__ ut, double *__restrict__ vt,
+                         double *__restrict__ wt)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int nip1 = b.n[0], njp1 = b.n[1], nkp1 = b.n[2];
+    const long jo = nip1, ko = (long)nip1 * njp1, np = (long)nip1 * njp1 * nkp1;
+    const double *U = u + b.off3, *V = v + b.off3, *W = w + b.off3;
+    double *Ut = ut + b.off3, *Vt = vt + b.off3, *Wt = wt + b.off3;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < np; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % nip1) + 1, j = (int)((q / nip1) % njp1) + 1, k = (int)(q / ko) + 1;
+        const long p = q;  // 0-based ijk - 1
+        const bool ii = i >= 2 && i <= nip1 - 1, jj = j >= 2 && j <= njp1 - 1, kk = k >= 2 && k <= nkp1 - 1;
+        double a = 0., bv = 0., cw = 0.;
+        if (ii && jj && kk) {
+            a = 0.5 * (U[p] + U[p + 1]);
+            bv = 0.5 * (V[p] + V[p + jo]);
+            cw = 0.5 * (W[p] + W[p + ko]);
+        } else if (jj && kk && i == 1) {
+            a = U[p + 1];
+            bv = 0.25 * (V[p] + V[p + 1] + V[p + jo] + V[p + jo + 1]);
+            cw = 0.25 * (W[p] + W[p + 1] + W[p + ko] + W[p + ko + 1]);
+        } else if (jj && kk && i == nip1) {
+            a = U[p];
+            bv = 0.25 * (V[p] + V[p - 1] + V[p + jo] + V[p + jo - 1]);
+            cw = 0.25 * (W[p] + W[p - 1] + W[p + ko] + W[p + ko - 1]);
+        } else if (ii && jj && k == 1) {
+            cw = W[p + ko];
+            bv = 0.25 * (V[p] + V[p + ko] + V[p + jo] + V[p + jo + ko]);
+            a = 0.25 * (U[p] + U[p + ko] + U[p + 1] + U[p + ko + 1]);
+        } else if (ii && jj && k == nkp1) {
+            cw = W[p];
+            bv = 0.25 * (V[p] + V[p - ko] + V[p + jo] + V[p + jo - ko]);
+            a = 0.25 * (U[p] + U[p - ko] + U[p + 1] + U[p - ko + 1]);
+        } else if (ii && kk && j == 1) {
+            bv = V[p + jo];
+            cw = 0.25 * (W[p] + W[p + jo] + W[p + ko] + W[p + ko + jo]);
+            a = 0.25 * (U[p] + U[p + jo] + U[p + 1] + U[p + jo + 1]);
+        } else if (ii && kk && j == njp1) {
+            bv = V[p];
+            cw = 0.25 * (W[p] + W[p - jo] + W[p + ko] + W[p + ko - jo]);
+            a = 0.25 * (U[p] + U[p - jo] + U[p + 1] + U[p - jo + 1]);
+        }
+        Ut[p] = a;
+        Vt[p] = bv;
+        Wt[p] = cw;
+    }
+}
+
+// the 16 span means (k = 2..nkp1-1, in order) of one (i, j) column folded
+// into the running averages over no_sam samples
+__global__ void k_span_stats(const BlkDev *__restrict__ blk, int no_sam, const double *__restrict__ ut,
+                             const double *__restrict__ vt, const double *__restrict__ wt,
+                             const double *__restrict__ p, const double *__restrict__ rho,
+                             const double *__restrict__ sc1, const double *__restrict__ sc1var,
+                             const double *__restrict__ gam, StatOut O)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int nip1 = b.n[0], njp1 = b.n[1], nkp1 = b.n[2];
+    const long jo = nip1, ko = (long)nip1 * njp1;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (long)nip1 * njp1;
+         q += (long)gridDim.x * blockDim.x) {
+        double s[16];
+        for (int m = 0; m < 16; m++) s[m] = 0.0;
+        for (int k = 2; k <= nkp1 - 1; k++) {
+            const long ijk = b.off3 + q + ko * (k - 1);
+            const double rr = rho[ijk], uu = ut[ijk], vv = vt[ijk], ww = wt[ijk];
+            s[0] = s[0] + rr * uu;
+            s[1] = s[1] + rr * vv;
+            s[2] = s[2] + rr * ww;
+            s[3] = s[3] + p[ijk];
+            s[4] = s[4] + rr;
+            s[5] = s[5] + rr * uu * vv;
+            s[6] = s[6] + rr * vv * ww;
+            s[7] = s[7] + rr * uu * ww;
+            s[8] = s[8] + rr * uu * uu;
+            s[9] = s[9] + rr * vv * vv;
+            s[10] = s[10] + rr * ww * ww;
+            s[11] = s[11] + rr * rr;
+            s[12] = s[12] + sc1[ijk];
+            s[13] = s[13] + sc1[ijk] * sc1[ijk];
+            s[14] = s[14] + sc1var[ijk];
+            s[15] = s[15] + gam[ijk];
+        }
+        (void)jo;
+        const long ij = b.off2 + q;
+        for (int m = 0; m < 16; m++) {
+            const double avg = s[m] / (double)(nkp1 - 2);
+            O.f[m][ij] = (O.f[m][ij] * (double)(no_sam - 1) + avg) / (double)no_sam;
+        }
+    }
+}
+
 // ================================================================ launchers
 namespace les {
 
@@ -438,6 +534,17 @@ void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, cons
     k_fixed_inlet<<<g, 256, 0, st>>>(blk, iblk, which, uprof, vprof, seed, step, rholo, rhohi, u, v, w, sc1, rho,
                                      u_int, v_int, w_int);
     count_launch(1);
+}
+
+void launch_statistics(const BlkDev *blk, int nb, long maxpts, long maxij, int no_sam, const double *u,
+                       const double *v, const double *w, const double *p, const double *rho, const double *sc1,
+                       const double *sc1var, const double *gam, double *ut, double *vt, double *wt,
+                       const StatOut &O, cudaStream_t st)
+{
+    unsigned g1 = (unsigned)((maxpts + 255) / 256), g2 = (unsigned)((maxij + 127) / 128);
+    k_centre<<<dim3(g1 > 2048 ? 2048 : g1, nb), 256, 0, st>>>(blk, u, v, w, ut, vt, wt);
+    k_span_stats<<<dim3(g2, nb), 128, 0, st>>>(blk, no_sam, ut, vt, wt, p, rho, sc1, sc1var, gam, O);
+    count_launch(2);
 }
 
 void launch_recycling(const BlkDev *blk, const int *nijk, int nb, int step, int inblock, int jmult, double rhohi,

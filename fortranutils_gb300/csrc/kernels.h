@@ -167,6 +167,10 @@ void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, cons
                         double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                         double *v_int, double *w_int, cudaStream_t st);
 
+void launch_statistics(const BlkDev *blk, int nb, long maxpts, long maxij, int no_sam, const double *u,
+                       const double *v, const double *w, const double *p, const double *rho, const double *sc1,
+                       const double *sc1var, const double *gam, double *ut, double *vt, double *wt,
+                       const StatOut &O, cudaStream_t st);
 void launch_recycling(const BlkDev *blk, const int *nijk, int nb, int step, int inblock, int jmult, double rhohi,
                       const RecycProf &P, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                       double *v_int, double *w_int, double *work, cudaStream_t st);

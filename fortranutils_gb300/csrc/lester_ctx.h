@@ -100,6 +100,7 @@ struct Ctx {
     double *d_uprof = nullptr, *d_vprof = nullptr;
     int nprof = 0;
     unsigned long long inlet_seed = 0;
+    int no_sam = 1;                 // statistics: samples so far (COMMON no_sam)
     int ncomp = 1;                  // connected components of the block graph
     int rb_threads = 256;           // red-black launch shape (autotuned)
     Tuned tuned[2];                 // autotuned solver settings [FP64, mixed]

@@ -341,4 +341,56 @@ int lester_recycling(double *hu, double *hv, double *hw, double *u_int, double *
     return st.finish();
 }
 
+int lester_gpu_set_stat_samples(int no_sam)
+{
+    LES_NEED_CTX();
+    if (no_sam < 1) return set_err(LES_ERR_ARG, "statistics: no_sam must be >= 1");
+    g_ctx->no_sam = no_sam;
+    return 0;
+}
+
+int lester_statistics(const double *u, const double *v, const double *w, const double *p, const double *rho,
+                      double *um, double *vm, double *wm, double *pm, double *rhom, double *ruv, double *rvw,
+                      double *rwu, double *ruu, double *rvv, double *rww, double *rrh, const double *gam,
+                      const double *gamsc1, const double *sc1, double *fm, double *rff, const double *sc1var,
+                      const double *sc1dis, double *sc1varm, double *sc1dism, const double *temperature, double *t_m,
+                      const double *dip, const double *djp, const double *rp, const double *dkp, const double *dkw,
+                      const double *x, const double *y, const double *z, const int *step)
+{
+    (void)gamsc1, (void)sc1dis, (void)sc1dism, (void)temperature, (void)dip, (void)djp, (void)rp, (void)dkp;
+    (void)dkw, (void)x, (void)y, (void)z, (void)step;
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    Staging st(&c, __func__);
+    int r;
+    const double *in[8] = {u, v, w, p, rho, sc1, sc1var, gam};
+    const double *d[8];
+    for (int q = 0; q < 8; q++)
+        if ((r = st.in(in[q], c.tot_sg3, &d[q]))) return r;
+    double *outs[16] = {um, vm, wm, pm, rhom, ruv, rvw, rwu, ruu, rvv, rww, rrh, fm, rff, sc1varm, t_m};
+    StatOut O;
+    long n2 = 0;
+    for (int b = 1; b <= c.g.numbl; b++) n2 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
+    for (int q = 0; q < 16; q++)
+        if ((r = st.io(outs[q], n2, &O.f[q]))) return r;
+    double *tmp = nullptr;
+    if (cudaMalloc(&tmp, sizeof(double) * 3 * c.tot_sg3) != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(LES_ERR_NOMEM, "statistics: centred velocities");
+    }
+    cudaMemsetAsync(tmp, 0, sizeof(double) * 3 * c.tot_sg3, c.stream);
+    long maxpts = 0, maxij = 0;
+    for (int b = 1; b <= c.g.numbl; b++) {
+        const int *n = c.lv[1].n[b];
+        maxpts = std::max(maxpts, (long)n[0] * n[1] * n[2]);
+        maxij = std::max(maxij, (long)n[0] * n[1]);
+    }
+    launch_statistics(c.lv[1].d_blk, c.g.numbl, maxpts, maxij, c.no_sam, d[0], d[1], d[2], d[3], d[4], d[5], d[6],
+                      d[7], tmp, tmp + c.tot_sg3, tmp + 2 * c.tot_sg3, O, c.stream);
+    cudaError_t e = cudaStreamSynchronize(c.stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "statistics: %s", cudaGetErrorString(e));
+    return st.finish();
+}
+
 } // extern "C"

@@ -445,3 +445,19 @@ def recycling(u_int, v_int, w_int, u, v, w, sc1, rho, prof, means, step, inblock
     _check(lib().lester_recycling(None, None, None, _p(u_int), _p(v_int), _p(w_int), _p(u), _p(v), _p(w), None,
                                   _p(sc1), _p(rho), None, _i(0), None, *[_p(a) for a in prof],
                                   *[_p(a) for a in means], _i(step), _i(inblock)))
+
+
+STAT_NAMES = "um vm wm pm rhom ruv rvw rwu ruu rvv rww rrh fm rff sc1varm T_m".split()
+
+
+def statistics(u, v, w, p, rho, sc1, sc1var, gam, outs: dict, no_sam: int):
+    """code/statistics.F:1 (the averaging): outs maps STAT_NAMES to 2-D
+    arrays (level-1 metric layout), updated in place; no_sam the sample
+    count including this one."""
+    _check(lib().lester_gpu_set_stat_samples(int(no_sam)))
+    o = outs
+    _check(lib().lester_statistics(_p(u), _p(v), _p(w), _p(p), _p(rho), _p(o["um"]), _p(o["vm"]), _p(o["wm"]),
+                                   _p(o["pm"]), _p(o["rhom"]), _p(o["ruv"]), _p(o["rvw"]), _p(o["rwu"]),
+                                   _p(o["ruu"]), _p(o["rvv"]), _p(o["rww"]), _p(o["rrh"]), _p(gam), None,
+                                   _p(sc1), _p(o["fm"]), _p(o["rff"]), _p(sc1var), None, _p(o["sc1varm"]), None,
+                                   None, _p(o["T_m"]), None, None, None, None, None, None, None, None, _i(0)))

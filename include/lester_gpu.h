@@ -502,6 +502,26 @@ int lester_recycling(double *hu, double *hv, double *hw, double *u_int, double *
                      double *wmean, double *uumean, double *vvmean, double *wwmean, const int *step,
                      const int *inblock);
 
+/* ---- statistics ------------------------------------------------------- */
+/* code/statistics.F:1 statistics(u, v, w, p, rho, um, vm, wm, pm, rhom, ruv,
+ * rvw, rwu, ruu, rvv, rww, rrh, gam, gamsc1, sc1, fm, rff, sc1var, sc1dis,
+ * sc1varm, sc1dism, Temperature, T_m, dip, djp, rp, dkp, dkw, x, y, z,
+ * step): span (k) averages of rho u, rho v, rho w, p, rho and the second
+ * moments, the scalar, its square and variance, and gam (into T_m, as the
+ * reference stores it), folded into running means over no_sam samples
+ * (lester_gpu_set_stat_samples; the COMMON no_sam).  The 2-D outputs use
+ * the level-1 layout of the 2-D metrics.  Velocities are cell-centred as
+ * statistics.F's centre does; its unset edge cells are 0 here.  The file
+ * outputs are not part of this call. */
+int lester_gpu_set_stat_samples(int no_sam);
+int lester_statistics(const double *u, const double *v, const double *w, const double *p, const double *rho,
+                      double *um, double *vm, double *wm, double *pm, double *rhom, double *ruv, double *rvw,
+                      double *rwu, double *ruu, double *rvv, double *rww, double *rrh, const double *gam,
+                      const double *gamsc1, const double *sc1, double *fm, double *rff, const double *sc1var,
+                      const double *sc1dis, double *sc1varm, double *sc1dism, const double *temperature, double *t_m,
+                      const double *dip, const double *djp, const double *rp, const double *dkp, const double *dkw,
+                      const double *x, const double *y, const double *z, const int *step);
+
 /* ---- adjoint and tangent-linear runs ---------------------------------- */
 /* No counterpart in the reference.  A run of nsteps lester_step calls from
  * the state in `fields` (device arrays; the caller's arrays are not

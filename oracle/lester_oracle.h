@@ -212,6 +212,11 @@ void orc_recycling(orc_ctx *c, int step, int inblock, const int inlet[4], double
                    const double *uprof, const double *vprof, const double *wprof, const double *uuprof,
                    const double *vvprof, const double *wwprof, double *umean, double *vmean, double *wmean,
                    double *uumean, double *vvmean, double *wwmean);
+/* code/statistics.F:1-200: span-averaged running statistics, outs = the 2-D
+   arrays um vm wm pm rhom ruv rvw rwu ruu rvv rww rrh fm rff sc1varm T_m */
+void orc_statistics(orc_ctx *c, int no_sam, const double *u, const double *v, const double *w, const double *p,
+                    const double *rho, const double *sc1, const double *sc1var, const double *gam,
+                    double *const *outs);
 /* inlet configuration used by orc_step (profiles copied, nprof values each) */
 void orc_set_inlet(orc_ctx *c, const int inlet[4], const double *uprof, const double *vprof,
                    int nprof, unsigned long long seed);

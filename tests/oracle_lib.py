@@ -304,3 +304,12 @@ def _orc_recycling(self, step, inblock, inlet, rhohi, u, v, w, sc1, rho, u_int, 
 
 
 Oracle.recycling = _orc_recycling
+
+
+def _orc_statistics(self, no_sam, u, v, w, p, rho, sc1, sc1var, gam, outs: dict) -> None:
+    from fortranutils_gb300 import lester as L
+    arr = (C.c_void_p * 16)(*[P(outs[n]).value for n in L.STAT_NAMES])
+    lib().orc_statistics(self.ctx, int(no_sam), *map(P, (u, v, w, p, rho, sc1, sc1var, gam)), arr)
+
+
+Oracle.statistics = _orc_statistics

@@ -217,3 +217,31 @@ def test_recycling_bitwise(gpulib):
     for a, b in zip(gm, rmeans):
         np.testing.assert_array_equal(a, b)
     assert not np.array_equal(ref["u"], s["u"])
+
+
+def test_statistics_bitwise(gpulib):
+    """Span-averaged running statistics over two samples on the two-block
+    inflow/outflow case: every 2-D output bitwise (same summation order)."""
+    import torch
+    st = setup()
+    c = st.case
+    s = state(st, 13)
+    rng = np.random.default_rng(5)
+    extra = {n: rng.standard_normal(c.n3_sg) for n in ("sc1var", "gam")}
+    p = rng.standard_normal(c.n3_mg)
+    outs0 = {n: 0.1 * rng.standard_normal(c.n2) for n in L.STAT_NAMES}
+    ref = {n: a.copy() for n, a in outs0.items()}
+    L.gpu_init(c.geom(), L.default_ctrl())
+    try:
+        dev = {n: torch.from_numpy(a.copy()).cuda() for n, a in outs0.items()}
+        for no_sam in (1, 2):
+            args = [s["u"], s["v"], s["w"], p, s["rho"], s["sc1"], extra["sc1var"], extra["gam"]]
+            st.orc.statistics(no_sam, *args, ref)
+            L.statistics(*[torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in args], dev, no_sam)
+            s["u"] = s["u"] * 1.1
+        got = {n: a.cpu().numpy() for n, a in dev.items()}
+    finally:
+        L.gpu_finalize()
+    for n in L.STAT_NAMES:
+        np.testing.assert_array_equal(got[n], ref[n], err_msg=n)
+    assert not np.array_equal(ref["um"], outs0["um"])
