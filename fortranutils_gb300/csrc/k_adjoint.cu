@@ -22,13 +22,13 @@
 
 // slots of the u/v predictor inputs, in the roles set_uv_int gives them
 enum { SU_P, SU_W, SU_E, SU_S, SU_N, SU_L, SU_R, SV_P, SV_N, SV_W, SV_NW, SW_P, SW_R, SW_W, SW_WR,
-       SP_P, SP_W, SH_P, SF_P, NSU };
+       SP_P, SP_W, SH_P, SF_P, SG_P, SG_W, SG_S, SG_SW, SG_N, SG_NW, SG_L, SG_WL, SG_R, SG_WR, NSU };
 // slots of the w predictor inputs
 enum { TU_P, TU_L, TU_E, TU_EL, TV_P, TV_L, TV_N, TV_NL, TW_P, TW_L, TW_R, TW_W, TW_E, TW_S, TW_N,
-       TP_P, TP_L, TH_P, TF_P, NSW };
+       TP_P, TP_L, TH_P, TF_P, TG_P, TG_L, TG_W, TG_WL, TG_E, TG_EL, TG_S, TG_SL, TG_N, TG_NL, NSW };
 
 struct UPoint {
-    long ijk, ijkw, ijke, ijks, ijkn, ijkl, ijkr, ijknw, ijkwr;
+    long ijk, ijkw, ijke, ijks, ijkn, ijkl, ijkr, ijknw, ijkwr, ijksw, ijkwl;
     long ij, ijw, ijn, ijs, ijnw;
     int i, j, k;  // role coordinates
 };
@@ -55,6 +55,8 @@ __device__ __forceinline__ bool upoint(const BlkDev &b, int iva, long ijk, int i
     P.ijkr = ijk + ko;
     P.ijknw = P.ijkn - io;
     P.ijkwr = P.ijkw + ko;
+    P.ijksw = P.ijks - io;
+    P.ijkwl = P.ijkw - ko;
     P.ij = b.off2 + io * (i - 1) + jo * (j - 1);
     P.ijw = P.ij - io;
     P.ijs = P.ij - jo;
@@ -74,12 +76,12 @@ __device__ void upred_cell(const BlkDev &b, int bi, int iva, const UPoint &P, co
     const long ijknw = P.ijknw, ijkwr = P.ijkwr;
     const long ij = P.ij, ijw = P.ijw, ijn = P.ijn, ijs = P.ijs, ijnw = P.ijnw;
     const long io = P.ijke - ijk, jo = ijkn - ijk, ko = ijkr - ijk;
-    const long ijksw = ijks - io, ijkwl = ijkw - ko;
+    const long ijksw = P.ijksw, ijkwl = P.ijkwl;
     const int nkp1 = b.n[2], nj = (iva == 1 ? b.n[1] : b.n[0]) - 1, nk = nkp1 - 1;
     const bool wallsf = b.bc[iva == 1 ? 2 : 0] == LES_BCT_WALL_D;
     const bool wallnf = b.bc[iva == 1 ? 3 : 1] == LES_BCT_WALL_D;
     const bool walllf = b.bc[4] == LES_BCT_WALL_D, wallrf = b.bc[5] == LES_BCT_WALL_D;
-    const double *rho = A_.rho, *gam = A_.gam;
+    const double *rho = A_.rho;
     const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
     const double di = A_.diu[ij], dj = A_.dju[ij];
     const double rdkp = A_.rp[ij] * dkp[k - 1];
@@ -91,7 +93,11 @@ __device__ void upred_cell(const BlkDev &b, int bi, int iva, const UPoint &P, co
     R va = 0.25 * (vP + vN + vW + vNW);
     R wa = 0.25 * (wP + wR + wW + wWR);
     double rhoa = 0.5 * (rho[ijkw] + rho[ijk]);
-    double gama = 0.5 * (gam[ijkw] + gam[ijk]);
+    // the eddy viscosity is an input slot (differentiated through the
+    // subgrid model); the densities are not
+    const R gP = in[SG_P], gW = in[SG_W], gS = in[SG_S], gSW = in[SG_SW], gN = in[SG_N], gNW = in[SG_NW],
+            gL = in[SG_L], gWL = in[SG_WL], gR = in[SG_R], gWR = in[SG_WR];
+    R gama = 0.5 * (gW + gP);
     double rhowf = rho[ijkw], rhoef = rho[ijk];
     double rhosf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijks] + rho[ijksw]);
     double rhonf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijkn] + rho[ijknw]);
@@ -99,12 +105,12 @@ __device__ void upred_cell(const BlkDev &b, int bi, int iva, const UPoint &P, co
     double rhorf = 0.25 * (rho[ijk] + rho[ijkw] + rho[ijkr] + rho[ijkwr]);
     double rhou = 0.5 * (rho[ijk] + rho[ijkw]);
     double rhonp1u = 0.5 * (A_.rhonp1[ijk] + A_.rhonp1[ijkw]);
-    double gamwf = visc + gam[ijkw] * rhowf;
-    double gamef = visc + gam[ijk] * rhoef;
-    double gamsf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijks] + gam[ijksw]) * rhosf;
-    double gamnf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkn] + gam[ijknw]) * rhonf;
-    double gamlf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkl] + gam[ijkwl]) * rholf;
-    double gamrf = visc + .25 * (gam[ijk] + gam[ijkw] + gam[ijkr] + gam[ijkwr]) * rhorf;
+    R gamwf = visc + gW * rhowf;
+    R gamef = visc + gP * rhoef;
+    R gamsf = visc + .25 * (gP + gW + gS + gSW) * rhosf;
+    R gamnf = visc + .25 * (gP + gW + gN + gNW) * rhonf;
+    R gamlf = visc + .25 * (gP + gW + gL + gWL) * rholf;
+    R gamrf = visc + .25 * (gP + gW + gR + gWR) * rhorf;
     double areawf = A_.rdjp[ijw] * dkp[k - 1];
     double areaef = A_.rdjp[ij] * dkp[k - 1];
     double areasf = A_.rdix[ij] * dkp[k - 1];
@@ -128,12 +134,12 @@ __device__ void upred_cell(const BlkDev &b, int bi, int iva, const UPoint &P, co
     R cc2 = A_.hkiu[ij] * rhoa * (wa * wa) * vol;
     R cc3 = -A_.hiju[ij] * rhoa * va * uP * vol;
     R conc = cc1 + cc2 + cc3;
-    double galwf = gamwf * areawf / A_.dip[ijw];
-    double galef = gamef * areaef / A_.dip[ij];
-    double galsf = gamsf * areasf / A_.djx[ij];
-    double galnf = gamnf * areanf / A_.djx[ijn];
-    double gallf = gamlf * areak / (A_.rp[ij] * dkw[k - 1]);
-    double galrf = gamrf * areak / (A_.rp[ij] * dkw[k]);
+    R galwf = gamwf * areawf / A_.dip[ijw];
+    R galef = gamef * areaef / A_.dip[ij];
+    R galsf = gamsf * areasf / A_.djx[ij];
+    R galnf = gamnf * areanf / A_.djx[ijn];
+    R gallf = gamlf * areak / (A_.rp[ij] * dkw[k - 1]);
+    R galrf = gamrf * areak / (A_.rp[ij] * dkw[k]);
     R vwf = 0.5 * (vW + vNW);
     R vef = 0.5 * (vP + vN);
     R twf = galwf * 2.0 * (uP - uW);
@@ -187,10 +193,11 @@ __device__ void upred_cell(const BlkDev &b, int bi, int iva, const UPoint &P, co
 // the absolute positions of the u/v predictor slots
 __device__ __forceinline__ void uslots(const UPoint &P, long *at, int *fld)
 {
-    // fld: 0 role-u, 1 role-v, 2 w, 3 p, 4 h, 5 body force
-    const long a[NSU] = {P.ijk, P.ijkw, P.ijke, P.ijks, P.ijkn, P.ijkl, P.ijkr, P.ijk, P.ijkn, P.ijkw,
-                         P.ijknw, P.ijk, P.ijkr, P.ijkw, P.ijkwr, P.ijk, P.ijkw, P.ijk, P.ijk};
-    const int f[NSU] = {0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 4, 5};
+    // fld: 0 role-u, 1 role-v, 2 w, 3 p, 4 h, 5 body force, 6 eddy viscosity
+    const long a[NSU] = {P.ijk,  P.ijkw, P.ijke, P.ijks, P.ijkn, P.ijkl,  P.ijkr, P.ijk,  P.ijkn, P.ijkw,
+                         P.ijknw, P.ijk, P.ijkr, P.ijkw, P.ijkwr, P.ijk,  P.ijkw, P.ijk,  P.ijk,  P.ijk,
+                         P.ijkw, P.ijks, P.ijksw, P.ijkn, P.ijknw, P.ijkl, P.ijkwl, P.ijkr, P.ijkwr};
+    const int f[NSU] = {0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 4, 5, 6, 6, 6, 6, 6, 6, 6, 6, 6, 6};
 #pragma unroll
     for (int q = 0; q < NSU; q++) {
         at[q] = a[q];
@@ -214,7 +221,7 @@ __device__ void wpred_cell(const BlkDev &b, int bi, const WPoint &P, const WIntA
     const long ijk = P.ijk, ijkw = P.ijkw, ijke = P.ijke, ijks = P.ijks, ijkn = P.ijkn, ijkl = P.ijkl;
     const long ijkwl = P.ijkwl, ijksl = P.ijksl, ijkel = P.ijkel, ijknl = P.ijknl;
     const int nkp1 = b.n[2], ni = b.n[0] - 1, nj = b.n[1] - 1;
-    const double *rho = A_.rho, *gam = A_.gam;
+    const double *rho = A_.rho;
     const double *dkp = A_.dkp + b.off1k, *dkw = A_.dkw + b.off1k;
     const double *const *M = A_.m;
 #define G(a, ii, jj) M[a][IDX2(b, ii, jj)]
@@ -227,12 +234,14 @@ __device__ void wpred_cell(const BlkDev &b, int bi, const WPoint &P, const WIntA
     double rholf = rho[ijkl], rhorf = rho[ijk];
     double rhow = 0.5 * (rho[ijk] + rho[ijkl]);
     double rhonp1w = 0.5 * (A_.rhonp1[ijk] + A_.rhonp1[ijkl]);
-    double gamwf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijkw] + gam[ijkwl]) * rhowf;
-    double gamef = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijke] + gam[ijkel]) * rhoef;
-    double gamsf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijks] + gam[ijksl]) * rhosf;
-    double gamnf = visc + .25 * (gam[ijk] + gam[ijkl] + gam[ijkn] + gam[ijknl]) * rhonf;
-    double gamlf = visc + gam[ijkl] * rholf;
-    double gamrf = visc + gam[ijk] * rhorf;
+    const R gP = in[TG_P], gL = in[TG_L], gW = in[TG_W], gWL = in[TG_WL], gE = in[TG_E], gEL = in[TG_EL],
+            gS = in[TG_S], gSL = in[TG_SL], gN = in[TG_N], gNL = in[TG_NL];
+    R gamwf = visc + .25 * (gP + gL + gW + gWL) * rhowf;
+    R gamef = visc + .25 * (gP + gL + gE + gEL) * rhoef;
+    R gamsf = visc + .25 * (gP + gL + gS + gSL) * rhosf;
+    R gamnf = visc + .25 * (gP + gL + gN + gNL) * rhonf;
+    R gamlf = visc + gL * rholf;
+    R gamrf = visc + gP * rhorf;
     double areawf = G(MW_RDJU, i, j) * dkw[k - 1];
     double areaef = G(MW_RDJU, i + 1, j) * dkw[k - 1];
     double areasf = G(MW_RDIV, i, j) * dkw[k - 1];
@@ -259,12 +268,12 @@ __device__ void wpred_cell(const BlkDev &b, int bi, const WPoint &P, const WIntA
     R u_wc = 0.25 * (uP + uE + uL + uEL);
     R v_wc = 0.25 * (vP + vN + vL + vNL);
     R conc = -vol * rhow * (wP * (u_wc * G(MW_HKIP, i, j) + v_wc * G(MW_HKJP, i, j)));
-    double galwf = gamwf * areawf / G(MW_DIU, i, j);
-    double galef = gamef * areaef / G(MW_DIU, i + 1, j);
-    double galsf = gamsf * areasf / G(MW_DJV, i, j);
-    double galnf = gamnf * areanf / G(MW_DJV, i, j + 1);
-    double gallf = gamlf * areak / (radp * dkp[k - 2]);
-    double galrf = gamrf * areak / (radp * dkp[k - 1]);
+    R galwf = gamwf * areawf / G(MW_DIU, i, j);
+    R galef = gamef * areaef / G(MW_DIU, i + 1, j);
+    R galsf = gamsf * areasf / G(MW_DJV, i, j);
+    R galnf = gamnf * areanf / G(MW_DJV, i, j + 1);
+    R gallf = gamlf * areak / (radp * dkp[k - 2]);
+    R galrf = gamrf * areak / (radp * dkp[k - 1]);
     double radwf = 0.5 * (radp + radw), radef = 0.5 * (radp + rade);
     double radsf = 0.5 * (radp + rads), radnf = 0.5 * (radp + radn);
     R ulf = 0.5 * (uL + uEL), urf = 0.5 * (uP + uE);
@@ -327,9 +336,10 @@ __device__ void wpred_cell(const BlkDev &b, int bi, const WPoint &P, const WIntA
 __device__ __forceinline__ void wslots(const WPoint &P, long *at, int *fld)
 {
     // fld: 0 u, 1 v, 2 w, 3 p, 4 h, 5 body force
-    const long a[NSW] = {P.ijk, P.ijkl, P.ijke, P.ijkel, P.ijk, P.ijkl, P.ijkn, P.ijknl, P.ijk, P.ijkl,
-                         P.ijkr, P.ijkw, P.ijke, P.ijks, P.ijkn, P.ijk, P.ijkl, P.ijk, P.ijk};
-    const int f[NSW] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 3, 3, 4, 5};
+    const long a[NSW] = {P.ijk,  P.ijkl,  P.ijke, P.ijkel, P.ijk,  P.ijkl, P.ijkn, P.ijknl, P.ijk,  P.ijkl,
+                         P.ijkr, P.ijkw,  P.ijke, P.ijks,  P.ijkn, P.ijk,  P.ijkl, P.ijk,   P.ijk,  P.ijk,
+                         P.ijkl, P.ijkw, P.ijkwl, P.ijke, P.ijkel, P.ijks, P.ijksl, P.ijkn, P.ijknl};
+    const int f[NSW] = {0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 3, 3, 4, 5, 6, 6, 6, 6, 6, 6, 6, 6, 6, 6};
 #pragma unroll
     for (int q = 0; q < NSW; q++) {
         at[q] = a[q];
@@ -465,6 +475,130 @@ __global__ void k_take(const BlkDev *__restrict__ blk, int iva_or_w, const doubl
     if (c < start) return;
     dst[ijk] = src[ijk];
     if (zero_src) zero_src[ijk] = 0.;
+}
+
+// ------------------------------------------------- linearised Smagorinsky
+// subgrid_smagorinsky.F:85-222 (as k_sgs.cu computes it off polar grids) for
+// one interior point: gam from 30 velocity slots (fields 0-2: u, v, w).
+// The damping is a constant: set_virt_bc resets it to 1 on each of the
+// step's three calls (set_virt_bc.F:72-74) and the w call's wall planes keep
+// the larger of 1 and the van Driest value, so the step's gam sees 1.
+enum { GU_P, GU_E, GU_S, GU_SE, GU_N, GU_NE, GU_L, GU_EL, GU_R, GU_ER,
+       GV_P, GV_N, GV_W, GV_NW, GV_E, GV_NE, GV_L, GV_NL, GV_R, GV_NR,
+       GW_P, GW_R, GW_W, GW_WR, GW_E, GW_ER, GW_S, GW_SR, GW_N, GW_NR, NSG };
+
+template <typename R>
+__device__ R smag_cell(const R *in, double di, double dj, double dk, double hijp, double hjip, double csles,
+                       double vdd)
+{
+    R up = 0.5 * (in[GU_P] + in[GU_E]);
+    R vp = 0.5 * (in[GV_P] + in[GV_N]);
+    R vwf = 0.25 * (in[GV_P] + in[GV_N] + in[GV_W] + in[GV_NW]);
+    R vef = 0.25 * (in[GV_P] + in[GV_N] + in[GV_E] + in[GV_NE]);
+    R usf = 0.25 * (in[GU_P] + in[GU_E] + in[GU_S] + in[GU_SE]);
+    R unf = 0.25 * (in[GU_P] + in[GU_E] + in[GU_N] + in[GU_NE]);
+    R ulf = 0.25 * (in[GU_P] + in[GU_E] + in[GU_L] + in[GU_EL]);
+    R urf = 0.25 * (in[GU_P] + in[GU_E] + in[GU_R] + in[GU_ER]);
+    R vlf = 0.25 * (in[GV_P] + in[GV_N] + in[GV_L] + in[GV_NL]);
+    R vrf = 0.25 * (in[GV_P] + in[GV_N] + in[GV_R] + in[GV_NR]);
+    R dudi = (in[GU_E] - in[GU_P]) / di + vp * hijp;
+    R dvdi = (vef - vwf) / di - up * hijp;
+    R dudj = (unf - usf) / dj - vp * hjip;
+    R dvdj = (in[GV_N] - in[GV_P]) / dj + up * hjip;
+    R wwf = 0.25 * (in[GW_P] + in[GW_R] + in[GW_W] + in[GW_WR]);
+    R wef = 0.25 * (in[GW_P] + in[GW_R] + in[GW_E] + in[GW_ER]);
+    R wsf = 0.25 * (in[GW_P] + in[GW_R] + in[GW_S] + in[GW_SR]);
+    R wnf = 0.25 * (in[GW_P] + in[GW_R] + in[GW_N] + in[GW_NR]);
+    R dwdi = (wef - wwf) / di;
+    R dwdj = (wnf - wsf) / dj;
+    R dudk = (urf - ulf) / dk;
+    R dvdk = (vrf - vlf) / dk;
+    R dwdk = (in[GW_R] - in[GW_P]) / dk;
+    R sijsij = dvdj * dvdj + dwdk * dwdk + dudi * dudi +
+               0.5 * ((dudj + dvdi) * (dudj + dvdi) + (dvdk + dwdj) * (dvdk + dwdj) + (dudk + dwdi) * (dudk + dwdi));
+    const double delta_xyz = pow(di * dj * dk, .33333333);
+    const double evisc = csles * delta_xyz * vdd;
+    return evisc * evisc * sqrt(2.0 * sijsij);
+}
+
+// mode 0: gam tangent from the velocity tangents into out; mode 1: pass for
+// slot q0, lam (adjoint of gam) times the derivative added to the slot's
+// velocity adjoint
+__global__ void __launch_bounds__(128) k_sgs_lin(const BlkDev *__restrict__ blk, int mode, int q0, PredRefs base,
+                                                 PredRefs tan, PredBars bar, const double *__restrict__ lam,
+                                                 double *__restrict__ out, const double *__restrict__ dip,
+                                                 const double *__restrict__ djp, const double *__restrict__ dkp,
+                                                 const double *__restrict__ hijp, const double *__restrict__ hjip,
+                                                 const double *__restrict__ vdd, double csles)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    const long ijk = decode_interior(b, q, i, j, k);
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long at[NSG] = {ijk, ijk + 1, ijk - jo, ijk - jo + 1, ijk + jo, ijk + jo + 1, ijk - ko, ijk + 1 - ko,
+                          ijk + ko, ijk + 1 + ko,
+                          ijk, ijk + jo, ijk - 1, ijk + jo - 1, ijk + 1, ijk + jo + 1, ijk - ko, ijk + jo - ko,
+                          ijk + ko, ijk + jo + ko,
+                          ijk, ijk + ko, ijk - 1, ijk - 1 + ko, ijk + 1, ijk + 1 + ko, ijk - jo, ijk - jo + ko,
+                          ijk + jo, ijk + jo + ko};
+    Dual<1> in[NSG];
+#pragma unroll
+    for (int m = 0; m < NSG; m++) {
+        const int f = m / 10;
+        in[m].v = base.f[f][at[m]];
+        in[m].d[0] = mode == 0 ? tan.f[f][at[m]] : (m == q0 ? 1.0 : 0.0);
+    }
+    const long ij = IDX2(b, i, j);
+    Dual<1> g = smag_cell(in, dip[ij], djp[ij], dkp[b.off1k + k - 1], hijp[ij], hjip[ij], csles, vdd[ijk]);
+    if (mode == 0) {
+        out[ijk] = g.d[0];
+    } else {
+        const double c = lam[ijk] * g.d[0];
+        if (c != 0.) atomicAdd(bar.f[q0 / 10] + at[q0], c);
+    }
+}
+
+// wall ghosts written by set_virt_bc (set_virt_bc_block.F), linearised:
+// ghost = +/- interior (the log-law branch shifts by a constant of the
+// running means; the laminar one reflects), for u and w on the WALL y
+// sides.  mode 0: tangent ghost = s * tangent interior; mode 1: adjoint
+// interior += s * adjoint ghost, adjoint ghost = 0.  blockIdx.z: 0 u, 1 w.
+__global__ void k_vbc_lin(const BlkDev *__restrict__ blk, int mode, double *__restrict__ fu, double *__restrict__ fw,
+                          const double *__restrict__ tws_u, const double *__restrict__ twn_u,
+                          const double *__restrict__ tws_w, const double *__restrict__ twn_w,
+                          const long *__restrict__ off_ki, const double *__restrict__ dju,
+                          const double *__restrict__ djp, const double *__restrict__ rho, double visc, double ylam)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+    const long jo = n0, ko = (long)n0 * n1;
+    const int comp = blockIdx.z >> 1, side = 3 + (blockIdx.z & 1);
+    if (b.bc[side - 1] != LES_BCT_WALL_D) return;
+    double *f = comp == 0 ? fu : fw;
+    const double *tw = comp == 0 ? (side == 3 ? tws_u : twn_u) : (side == 3 ? tws_w : twn_w);
+    const double *dj = comp == 0 ? dju : djp;
+    const int jg = side == 3 ? 1 : n1, jn = side == 3 ? 2 : n1 - 1, k1 = side == 3 ? 2 : n1;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < (long)n0 * n2; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % n0) + 1, k = (int)(q / n0) + 1;
+        const long g = b.off3 + (i - 1) + jo * (jg - 1) + ko * (k - 1), nx = g + (jn - jg) * jo;
+        const double twv = tw[off_ki[blockIdx.y] + (k - 1) + (long)n2 * (i - 1)];
+        // the face density of the forward kernels (interior i, k: the i-1
+        // neighbours for u, the k-1 ones for w)
+        const long o = comp == 0 ? 1 : ko;
+        const bool in = comp == 0 ? i > 1 : k > 1;
+        const double r = in ? 0.25 * (rho[g] + rho[nx] + rho[g - o] + rho[nx - o]) : 0.5 * (rho[g] + rho[nx]);
+        const double dist = 0.5 * dj[b.off2 + (i - 1) + (long)n0 * (k1 - 1)];
+        const double yp = dist * sqrt(fabs(twv) / r) * r / visc;
+        const double sgn = yp > ylam ? 1.0 : -1.0;
+        if (mode == 0) {
+            f[g] = sgn * f[nx];
+        } else {
+            atomicAdd(f + nx, sgn * f[g]);  // nx is shared by both sides when n1 == 3
+            f[g] = 0.0;
+        }
+    }
 }
 
 // ---------------------------------------------------- linear transposes
@@ -718,6 +852,27 @@ void launch_wall_shear(const BlkDev *blk, int nb, long maxik, const double *dju,
                        double coef, double *ubar, double *sum, cudaStream_t st)
 {
     k_wall_shear<<<dim3(nbk_(2 * maxik, 256), nb), 256, 0, st>>>(blk, dju, visc, u, coef, ubar, sum);
+    count_launch(1);
+}
+
+void launch_sgs_lin(const BlkDev *blk, int nb, long maxcell, int mode, int q0, const PredRefs &base,
+                    const PredRefs &tan, const PredBars &bar, const double *lam, double *out, const double *dip,
+                    const double *djp, const double *dkp, const double *hijp, const double *hjip, const double *vdd,
+                    double csles, cudaStream_t st)
+{
+    k_sgs_lin<<<dim3(nbk_(maxcell, 128), nb), 128, 0, st>>>(blk, mode, q0, base, tan, bar, lam, out, dip, djp, dkp,
+                                                            hijp, hjip, vdd, csles);
+    count_launch(1);
+}
+
+void launch_vbc_lin(const BlkDev *blk, int nb, long maxik, int mode, double *fu, double *fw, const double *tws_u,
+                    const double *twn_u, const double *tws_w, const double *twn_w, const long *off_ki,
+                    const double *dju, const double *djp, const double *rho, double visc, double ylam,
+                    cudaStream_t st)
+{
+    unsigned g = nbk_(maxik, 128);
+    k_vbc_lin<<<dim3(g > 1024 ? 1024 : g, nb, 4), 128, 0, st>>>(blk, mode, fu, fw, tws_u, twn_u, tws_w, twn_w,
+                                                                off_ki, dju, djp, rho, visc, ylam);
     count_launch(1);
 }
 

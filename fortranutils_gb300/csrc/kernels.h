@@ -148,6 +148,17 @@ void launch_uvw_adv_t(const BlkDev *blk, int nb, long maxcell, int ivar, double 
 void launch_wall_shear(const BlkDev *blk, int nb, long maxik, const double *dju, double visc, const double *u,
                        double coef, double *ubar, double *sum, cudaStream_t st);
 void launch_fill_d(double *a, double v, long n, cudaStream_t st);
+// linearised Smagorinsky (mode 0 tangent into out, mode 1 pass q0 of 30;
+// base/tan/bar fields: u, v, w) and the wall ghosts of set_virt_bc for u and
+// w on WALL y sides (mode 0 tangent, 1 transpose)
+void launch_sgs_lin(const BlkDev *blk, int nb, long maxcell, int mode, int q0, const PredRefs &base,
+                    const PredRefs &tan, const PredBars &bar, const double *lam, double *out, const double *dip,
+                    const double *djp, const double *dkp, const double *hijp, const double *hjip, const double *vdd,
+                    double csles, cudaStream_t st);
+void launch_vbc_lin(const BlkDev *blk, int nb, long maxik, int mode, double *fu, double *fw, const double *tws_u,
+                    const double *twn_u, const double *tws_w, const double *twn_w, const long *off_ki,
+                    const double *dju, const double *djp, const double *rho, double visc, double ylam,
+                    cudaStream_t st);
 
 // k_outflow.cu: convective outflow / fixed inflow sides
 void launch_side_flux(const SideJob *jobs, int njobs, int iva, int which, const double *u, const double *v,

@@ -8,16 +8,24 @@
 //
 // The adjoint is the exact transpose of the discrete step as lester_step
 // computes it, for the flows where that step is smooth in the velocities:
-// constant density, no eddy-viscosity model, no slip sides, wall points in
-// the laminar branch of the wall function, and a converged fast pressure
+// constant density, no eddy viscosity or the Smagorinsky model (model 1,
+// walls on the y sides only, Cartesian), no slip sides, wall points in the
+// laminar branch of the wall function, and a converged fast pressure
 // solve.  Per step, in reverse order of the forward operations:
 //   face copies of u, v, w  ->  uvw_adv  ->  p_ref_subtract, face copies
 //   and extrap_p of p  ->  Poisson solve (the matrix is symmetric: the same
 //   solver)  ->  sour_p  ->  face copies of u_int, v_int, w_int  ->  the
-//   three predictors (local Jacobian rows by forward-mode duals, scattered).
-// Ghost values of u, v, w on the wall sides are rewritten by set_virt_bc at
-// the start of every step and enter the predictors only multiplied by the
-// zero wall-normal velocity, so their adjoints are dropped.
+//   three predictors (local Jacobian rows by forward-mode duals, scattered)
+//   ->  with model 1: face copies of gam  ->  Smagorinsky gam (duals)  ->
+//   set_virt_bc's wall ghosts of u and w.
+// With model 1 the van Driest damping is a constant of the step:
+// set_virt_bc resets it to 1 on each of its three calls and the w call's
+// wall planes keep the larger of 1 and the van Driest value.  The running
+// means of the wall stress then enter only through the branch choices of
+// the wall function and the wall ghosts (laminar here).
+// Without a model, ghost values of u, v, w on the wall sides enter the
+// predictors only multiplied by the zero wall-normal velocity, so their
+// adjoints are dropped.
 //
 // Memory: the state is checkpointed every cfg->checkpoint steps and each
 // segment is recomputed forward, keeping its per-step states, before its
@@ -168,7 +176,18 @@ int check_scope(const Ctx &c, const lester_adj_cfg &cfg)
     if (k.psolve == LES_PSOLVE_REFERENCE)
         return set_err(LES_ERR_ARG, "adjoint: needs a converged fast pressure solve (psolve FP64 or MIXED)");
     if (k.rholo != k.rhohi) return set_err(LES_ERR_ARG, "adjoint: constant density only (rholo == rhohi)");
-    if (k.model != 0) return set_err(LES_ERR_ARG, "adjoint: no eddy-viscosity model (model 0) only");
+    if (k.model != 0 && k.model != 1)
+        return set_err(LES_ERR_ARG, "adjoint: no eddy viscosity (model 0) or Smagorinsky (model 1) only");
+    if (k.model == 1) {
+        if (c.g.gotrad) return set_err(LES_ERR_ARG, "adjoint: Smagorinsky on Cartesian grids only");
+        for (int b = 0; b < c.g.numbl; b++)
+            for (int s = 0; s < 6; s++) {
+                const int bc = c.g.bl_bc[b][s];
+                const bool open = bc == LES_BCT_PERIODIC || bc == LES_BCT_INTERFACE;
+                if (!open && !(bc == LES_BCT_WALL && (s == 2 || s == 3)))
+                    return set_err(LES_ERR_ARG, "adjoint: Smagorinsky with walls on the y sides only");
+            }
+    }
     for (int b = 0; b < c.g.numbl; b++)
         for (int s = 0; s < 6; s++)
             if (c.g.bl_bc[b][s] == LES_BCT_ZERO_GRAD)
@@ -298,13 +317,69 @@ __global__ void k_zero_wall_ghosts(const BlkDev *__restrict__ blk, double *__res
     }
 }
 
+// the linearisation point of a step with the Smagorinsky model: the
+// velocities after set_virt_bc, the damping and eddy viscosity of the step
+// (and subgrid's other outputs, unused)
+struct Lin {
+    double *u, *v, *w, *vdd, *gam, *gsc, *svar, *sdis;
+};
+
+// zero the interior points of every block
+__global__ void k_zero_interior(const BlkDev *__restrict__ blk, double *__restrict__ a)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    a[decode_interior(b, q, i, j, k)] = 0.;
+}
+
 struct Adj {
     double *ub, *vb, *wb, *pb, *hub, *hvb, *hwb;   // adjoint of the carried state
     double *uib, *vib, *wib;                       // adjoint of u_int, v_int, w_int
     double *lam_h[3];                              // adjoint of the new h (taken)
     double *bsolve, *xsolve, *res;                 // adjoint Poisson solve (all levels)
     double *wbar;                                  // face-copy buffer
+    double *gamb;                                  // model 1: adjoint of gam (carried)
+    Lin S;
 };
+
+bool smagorinsky(const Ctx &c) { return c.c.model == 1; }
+
+// the step's wall ghosts, damping and eddy viscosity from the state B, as
+// lester_step computes them, into S
+int base_physics(Ctx &c, const lester_fields &B, Lin &S)
+{
+    const size_t nb = sizeof(double) * c.tot_sg3;
+    LES_CUDA(cudaMemcpyAsync(S.u, B.u, nb, cudaMemcpyDeviceToDevice, c.stream));
+    LES_CUDA(cudaMemcpyAsync(S.v, B.v, nb, cudaMemcpyDeviceToDevice, c.stream));
+    LES_CUDA(cudaMemcpyAsync(S.w, B.w, nb, cudaMemcpyDeviceToDevice, c.stream));
+    LES_CUDA(cudaMemcpyAsync(S.gam, B.gam, nb, cudaMemcpyDeviceToDevice, c.stream));
+    double *const *m = B.metric;
+    double *const *tw = B.tw;
+    const int one = 1;
+    double zero = 0.0;
+    int r;
+    for (int iv = 1; iv <= 3; iv++) {
+        double *fld = iv == 1 ? S.u : iv == 2 ? S.v : S.w;
+        if ((r = lester_set_virt_bc(&iv, &one, fld, nullptr, B.rho, S.gam, S.vdd, nullptr, &zero, tw[0], tw[1],
+                                    tw[2], tw[3], tw[4], tw[5], tw[6], tw[7], tw[8], tw[9], tw[10], tw[11], m[M_DIP],
+                                    m[M_DIU], m[M_DIV], m[M_DIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RU],
+                                    m[M_RV], B.dkp, B.dkw)))
+            return r;
+    }
+    return lester_subgrid(S.gam, S.gsc, S.u, S.v, S.w, B.sc1, B.rho, S.svar, S.sdis, S.vdd, m[M_DIP], m[M_DIU],
+                          m[M_DJP], m[M_DJV], B.dkp, B.dkw, m[M_HIJP], m[M_HJIP], m[M_HKIP], m[M_HKJP], m[M_RP],
+                          nullptr, nullptr);
+}
+
+void vbc_lin(Ctx &c, const lester_fields &B, int mode, double *fu, double *fw)
+{
+    LevelGeom &L = c.lv[1];
+    double *const *m = B.metric;
+    launch_vbc_lin(L.d_blk, c.g.numbl, max_ik(c), mode, fu, fw, B.tw[0], B.tw[1], B.tw[10], B.tw[11], c.d_offki,
+                   m[M_DJU], m[M_DJP], B.rho, c.c.visc, c.c.ylaminar, c.stream);
+}
 
 int halo_t(Ctx &c, double *bar, double *wbar)
 {
@@ -376,29 +451,64 @@ int adjoint_step(Ctx &c, const lester_fields &W, const lester_fields &B, Adj &A,
     PredRefs none;
     memset(&none, 0, sizeof none);
     const double *fbase[3] = {c.fb[0], c.fb[1], c.fb[2]};
+    // the linearisation point: the state, or with model 1 the velocities
+    // after set_virt_bc and the step's eddy viscosity
+    const bool sgs = smagorinsky(c);
+    const double *bu = B.u, *bv = B.v, *bw = B.w, *bg = nullptr;
+    double *gb = nullptr;
+    int nsu = kSlotsU, nsw = kSlotsW;
+    if (sgs) {
+        if ((r = base_physics(c, B, A.S))) return r;
+        bu = A.S.u;
+        bv = A.S.v;
+        bw = A.S.w;
+        bg = A.S.gam;
+        gb = A.gamb;
+        nsu = kSlotsU + 10;
+        nsw = kSlotsW + 10;
+    }
     {
         UIntArgs a1 = uargs(c, B, 1);
-        PredRefs base = {{B.u, B.v, B.w, B.p, B.hn_u, fbase[0]}};
-        PredBars bar = {{A.ub, A.vb, A.wb, A.pb, A.hub, gf[0]}};
-        for (int q = 0; q < kSlotsU; q++)
+        PredRefs base = {{bu, bv, bw, B.p, B.hn_u, fbase[0], bg}};
+        PredBars bar = {{A.ub, A.vb, A.wb, A.pb, A.hub, gf[0], gb}};
+        for (int q = 0; q < nsu; q++)
             launch_upred_lin(L.d_blk, nb, L.maxcell, 1, 1, q, a1, base, none, bar, A.uib, A.lam_h[0], nullptr,
                              nullptr, k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
     }
     {
         UIntArgs a2 = uargs(c, B, 2);
-        PredRefs base = {{B.v, B.u, B.w, B.p, B.hn_v, fbase[1]}};
-        PredBars bar = {{A.vb, A.ub, A.wb, A.pb, A.hvb, gf[1]}};
-        for (int q = 0; q < kSlotsU; q++)
+        PredRefs base = {{bv, bu, bw, B.p, B.hn_v, fbase[1], bg}};
+        PredBars bar = {{A.vb, A.ub, A.wb, A.pb, A.hvb, gf[1], gb}};
+        for (int q = 0; q < nsu; q++)
             launch_upred_lin(L.d_blk, nb, L.maxcell, 2, 1, q, a2, base, none, bar, A.vib, A.lam_h[1], nullptr,
                              nullptr, k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
     }
     {
         WIntArgs aw = wargs(c, B);
-        PredRefs base = {{B.u, B.v, B.w, B.p, B.hn_w, fbase[2]}};
-        PredBars bar = {{A.ub, A.vb, A.wb, A.pb, A.hwb, gf[2]}};
-        for (int q = 0; q < kSlotsW; q++)
+        PredRefs base = {{bu, bv, bw, B.p, B.hn_w, fbase[2], bg}};
+        PredBars bar = {{A.ub, A.vb, A.wb, A.pb, A.hwb, gf[2], gb}};
+        for (int q = 0; q < nsw; q++)
             launch_wpred_lin(L.d_blk, nb, L.maxcell, 1, q, aw, base, none, bar, A.wib, A.lam_h[2], nullptr,
                              nullptr, k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
+    }
+    if (sgs) {
+        // gam after its face copies, then the wall ghosts of u and w.  The
+        // copies gather every partner plane before writing any ghost plane,
+        // so a corner ghost takes the previous step's value at an edge
+        // ghost: what the transposed copies leave on ghost points is the
+        // adjoint of the previous step's gam there and is carried; the
+        // interior (rewritten by subgrid) and the wall ghosts (never
+        // written) are cleared.
+        halo_t(c, A.gamb, A.wbar);
+        PredRefs base = {{bu, bv, bw}};
+        PredBars bar = {{A.ub, A.vb, A.wb}};
+        for (int q = 0; q < 30; q++)
+            launch_sgs_lin(L.d_blk, nb, L.maxcell, 1, q, base, none, bar, A.gamb, nullptr, m[M_DIP], m[M_DJP],
+                           W.dkp, m[M_HIJP], m[M_HJIP], A.S.vdd, k.csles, c.stream);
+        k_zero_interior<<<dim3((unsigned)((L.maxcell + 255) / 256), nb), 256, 0, c.stream>>>(L.d_blk, A.gamb);
+        c.prof_launches++;
+        zero_wall_ghosts(c, A.gamb);
+        vbc_lin(c, B, 1, A.ub, A.wb);
     }
     // wall ghosts of the state before the step are rewritten (set_virt_bc)
     zero_wall_ghosts(c, A.ub);
@@ -408,10 +518,23 @@ int adjoint_step(Ctx &c, const lester_fields &W, const lester_fields &B, Adj &A,
     return 0;
 }
 
+int alloc_lin(Run &R, Lin &S)
+{
+    int r;
+    double **sg[] = {&S.u, &S.v, &S.w, &S.vdd, &S.gam, &S.gsc, &S.svar, &S.sdis};
+    for (double **p : sg)
+        if ((r = R.alloc(R.c.tot_sg3, p))) return r;
+    return 0;
+}
+
 int alloc_adj(Run &R, Adj &A)
 {
     Ctx &c = R.c;
     int r;
+    memset(&A, 0, sizeof A);
+    if (smagorinsky(c)) {
+        if ((r = alloc_lin(R, A.S)) || (r = R.alloc(c.tot_sg3, &A.gamb))) return r;
+    }
     double **sg[] = {&A.ub, &A.vb, &A.wb, &A.pb, &A.hub, &A.hvb, &A.hwb, &A.uib, &A.vib, &A.wib,
                      &A.lam_h[0], &A.lam_h[1], &A.lam_h[2]};
     for (double **p : sg)
@@ -516,6 +639,12 @@ int lester_tangent_run(const lester_adj_cfg *cfg, const lester_fields *fields, c
     double **mg[] = {&dp, &dpn, &ds, &dres};
     for (double **p : mg)
         if ((r = R.alloc(c.tot3, p))) return r;
+    // model 1: the linearisation point and the tangent of gam (kept from
+    // step to step: its edge ghosts feed the next step's corner ghosts)
+    const bool sgs = smagorinsky(c);
+    Lin S{};
+    double *dgam = nullptr;
+    if (sgs && ((r = alloc_lin(R, S)) || (r = R.alloc(c.tot_sg3, &dgam)))) return r;
     const long nw = wall_points(c);
     if (nw == 0) return set_err(LES_ERR_ARG, "tangent: no wall points on the y sides");
     const double coef = 1.0 / ((double)nw * (cfg->j_last - cfg->j_first + 1));
@@ -527,18 +656,32 @@ int lester_tangent_run(const lester_adj_cfg *cfg, const lester_fields *fields, c
     for (int n = 1; n <= N && !r; n++) {
         lester_fields &W = R.W;
         const double *fbase[3] = {c.fb[0], c.fb[1], c.fb[2]};
+        const double *bu = W.u, *bv = W.v, *bw = W.w, *bg = nullptr;
+        if (sgs) {
+            // wall ghosts and gam of the step, with their tangents
+            if ((r = base_physics(c, W, S))) break;
+            bu = S.u;
+            bv = S.v;
+            bw = S.w;
+            bg = S.gam;
+            vbc_lin(c, W, 0, du, dw);
+            PredRefs base = {{bu, bv, bw}}, tan = {{du, dv, dw}};
+            launch_sgs_lin(L.d_blk, nb, L.maxcell, 0, 0, base, tan, nob, nullptr, dgam, m[M_DIP], m[M_DJP], W.dkp,
+                           m[M_HIJP], m[M_HJIP], S.vdd, k.csles, c.stream);
+            if ((r = lester_swap_sc(&iv0, &one, dgam, nullptr, &two))) break;
+        }
         // tangent predictors at the state before the step
         {
             UIntArgs a1 = uargs(c, W, 1);
-            PredRefs base = {{W.u, W.v, W.w, W.p, W.hn_u, fbase[0]}}, tan = {{du, dv, dw, dp, dhu, dfu}};
+            PredRefs base = {{bu, bv, bw, W.p, W.hn_u, fbase[0], bg}}, tan = {{du, dv, dw, dp, dhu, dfu, dgam}};
             launch_upred_lin(L.d_blk, nb, L.maxcell, 1, 0, 0, a1, base, tan, nob, nullptr, nullptr, dui, dhu,
                              k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
             UIntArgs a2 = uargs(c, W, 2);
-            PredRefs base2 = {{W.v, W.u, W.w, W.p, W.hn_v, fbase[1]}}, tan2 = {{dv, du, dw, dp, dhv, dfv}};
+            PredRefs base2 = {{bv, bu, bw, W.p, W.hn_v, fbase[1], bg}}, tan2 = {{dv, du, dw, dp, dhv, dfv, dgam}};
             launch_upred_lin(L.d_blk, nb, L.maxcell, 2, 0, 0, a2, base2, tan2, nob, nullptr, nullptr, dvi, dhv,
                              k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
             WIntArgs aw = wargs(c, W);
-            PredRefs base3 = {{W.u, W.v, W.w, W.p, W.hn_w, fbase[2]}}, tan3 = {{du, dv, dw, dp, dhw, dfw}};
+            PredRefs base3 = {{bu, bv, bw, W.p, W.hn_w, fbase[2], bg}}, tan3 = {{du, dv, dw, dp, dhw, dfw, dgam}};
             launch_wpred_lin(L.d_blk, nb, L.maxcell, 0, 0, aw, base3, tan3, nob, nullptr, nullptr, dwi, dhw,
                              k.dtime, k.visc, k.ylaminar, k.kappa, k.cwfun, c.stream);
         }

@@ -62,12 +62,13 @@ struct SgsFast {
 };
 
 // base, tangent and adjoint arrays of the linearised predictor inputs, in
-// slot-field order: role-u, role-v, w, p, old h, body force (may be null)
+// slot-field order: role-u, role-v, w, p, old h, body force, eddy
+// viscosity (any may be null: zero)
 struct PredRefs {
-    const double *f[6];
+    const double *f[7];
 };
 struct PredBars {
-    double *f[6];
+    double *f[7];
 };
 
 // set_virt_bc arguments: the field, the wall array of the side being

@@ -2,7 +2,9 @@
 lester_tangent_run) on small channels, through the C ABI.
 
 Objective: the mean wall shear stress over a window of steps; control: the
-body force of the u, v, w predictors.  Checks:
+body force of the u, v, w predictors.  Runs without an eddy-viscosity model
+and with the Smagorinsky model (model 1: gam, its van Driest damping in the
+wall-stress running means and the wall ghosts are differentiated).  Checks:
   * the tangent against central finite differences of the forward run
     (relative 1e-6: the O(eps^2) truncation of a quadratic map);
   * the adjoint gradient against the tangent along random directions
@@ -64,10 +66,13 @@ def finalize():
     L.gpu_finalize()
 
 
+@pytest.mark.parametrize("model", [0, 1])
 @pytest.mark.parametrize("name", ["box_wall", "two_block"])
-def test_tangent_matches_finite_differences(name, finalize):
+def test_tangent_matches_finite_differences(name, model, finalize):
     import torch
-    st, g = start(name)
+    st, g = start(name, model=model)
+    if model == 1:  # the eddy viscosity is comparable to the molecular one
+        assert g["gam"].abs().max().item() > 0.5 / 500.0
     d = direction(st, 11)
     J0, dJ = S.tangent_run(g, NSTEP, *d, j_first=2)
     assert J0 > 0 and dJ != 0
@@ -83,13 +88,14 @@ def test_tangent_matches_finite_differences(name, finalize):
     assert abs(fd - dJ) <= 1e-6 * abs(dJ), (fd, dJ)
 
 
+@pytest.mark.parametrize("model", [0, 1])
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
 @pytest.mark.parametrize("name", ["box_wall", "two_block"])
-def test_adjoint_matches_tangent(name, psolve, finalize):
+def test_adjoint_matches_tangent(name, psolve, model, finalize):
     """The adjoint is the transpose of the tangent: for two directions,
     <grad J, d> equals the tangent's dJ(d)."""
     import torch
-    st, g = start(name, psolve=psolve)
+    st, g = start(name, psolve=psolve, model=model)
     grad = [torch.zeros_like(g["u"]) for _ in range(3)]
     J = S.adjoint_run(g, NSTEP, *grad, j_first=2, checkpoint=2)
     for seed in (3, 4):
@@ -100,9 +106,10 @@ def test_adjoint_matches_tangent(name, psolve, finalize):
         assert abs(adj - dJ) <= 1e-9 * abs(dJ), (adj, dJ)
 
 
-def test_gradient_independent_of_checkpoints(finalize):
+@pytest.mark.parametrize("model", [0, 1])
+def test_gradient_independent_of_checkpoints(model, finalize):
     import torch
-    st, g = start("box_wall")
+    st, g = start("box_wall", model=model)
     out = []
     for K in (1, 3, NSTEP):
         grad = [torch.zeros_like(g["u"]) for _ in range(3)]
@@ -137,12 +144,13 @@ def test_window_and_state_unchanged(finalize):
         assert np.all(st.case.block_view(gv, ib, 0)[:, 1, :] == 0.0)
 
 
-@pytest.mark.parametrize("name,bad", [("box_wall", dict(model=1)), ("box_wall", dict(rholo=1.0, rhohi=2.0)),
+@pytest.mark.parametrize("name,bad", [("box_wall", dict(model=2)), ("box_wall", dict(model=3)),
+                                      ("box_wall", dict(rholo=1.0, rhohi=2.0)),
                                       ("box_wall", dict(psolve=L.PSOLVE_REFERENCE)),
                                       ("box_slip_stretched", {})])
 def test_scope_refused(name, bad, finalize):
-    """Eddy viscosity, variable density, the reference solver (not
-    converged) and slip sides are outside the transposed step."""
+    """WALE and Sigma eddy viscosity, variable density, the reference
+    solver (not converged) and slip sides are outside the transposed step."""
     import torch
     st, g = start(name, **bad)
     grad = [torch.zeros_like(g["u"]) for _ in range(3)]
@@ -163,7 +171,7 @@ def test_bad_configuration_refused(finalize):
         S.adjoint_run(g.to("numpy"), 2, *grad)
 
 
-def channel_state(shape=(128, 96, 64), beta=2.2, re_tau=180.0, sigma=0.1, seed=4, cfl=0.3):
+def channel_state(shape=(128, 96, 64), beta=2.2, re_tau=180.0, sigma=0.1, seed=4, cfl=0.3, model=0):
     """Stretched channel: laminar profile u = 1 - y^2 (laminar friction
     Reynolds number sqrt(2 / visc) = re_tau) plus N(0, sigma^2) noise on
     u, v, w; dt from the initial CFL number (cflest-style: max over cells
@@ -182,7 +190,7 @@ def channel_state(shape=(128, 96, 64), beta=2.2, re_tau=180.0, sigma=0.1, seed=4
     dz = np.diff(b.z[1:b.n[2]]).min()
     u, v, w = (case.block_view(s[n], 0)[1:-1, 1:-1, 1:-1] for n in "uvw")
     c = np.abs(u) / dx + np.abs(v) / dy[None, :, None] + np.abs(w) / dz
-    ctrl = L.default_ctrl(dtime=cfl / c.max(), model=0, psolve=L.PSOLVE_FP64, rtol=1e-12, max_outer=400,
+    ctrl = L.default_ctrl(dtime=cfl / c.max(), model=model, psolve=L.PSOLVE_FP64, rtol=1e-12, max_outer=400,
                           visc=2.0 / re_tau ** 2)
     L.gpu_init(case.geom(), ctrl)
     g = s.to("torch")
@@ -194,15 +202,19 @@ def channel_state(shape=(128, 96, 64), beta=2.2, re_tau=180.0, sigma=0.1, seed=4
     return case, ctrl, g
 
 
-def test_channel_gradient_against_fd_and_tangent(finalize):
+@pytest.mark.parametrize("model,ndir", [(0, 16), (1, 8)])
+def test_channel_gradient_against_fd_and_tangent(model, ndir, finalize):
     """128x96x64 stretched channel (tanh beta 2.2, periodic x/z), 40 steps,
-    J over steps 21-40, FP64 solve, checkpoints every 10 steps: the adjoint
-    gradient against the tangent and against central differences along 16
-    seeded directions (seeds 400-415); the finite-difference step is picked
-    by a sweep on the first direction."""
+    J over steps 21-40, FP64 solve, checkpoints every 10 steps, without an
+    eddy-viscosity model and with Smagorinsky: the adjoint gradient against
+    the tangent and against central differences along 16 (8) seeded
+    directions from seed 400; the finite-difference step is picked by a
+    sweep on the first direction."""
     import time
     import torch
-    case, ctrl, g = channel_state()
+    case, ctrl, g = channel_state(model=model)
+    if model == 1:  # Smagorinsky's gam reaches a fifth of the molecular viscosity
+        assert g["gam"].abs().max().item() > 0.2 * ctrl.visc
     nst, j0, j1 = 40, 21, 40
     grad = [torch.zeros_like(g["u"]) for _ in range(3)]
     torch.cuda.synchronize()
@@ -230,7 +242,7 @@ def test_channel_gradient_against_fd_and_tangent(finalize):
 
     worst_tlm = worst_fd = 0.0
     eps_best = None
-    for seed in range(400, 416):
+    for seed in range(400, 400 + ndir):
         d = dirn(seed)
         Jt, dJ = S.tangent_run(g, nst, *d, j_first=j0, j_last=j1)
         assert abs(Jt - J) <= 1e-12 * abs(J)
@@ -245,8 +257,8 @@ def test_channel_gradient_against_fd_and_tangent(finalize):
             print(f"\nFD step sweep (relative error vs tangent): {errs}")
         fd = (J_at([eps_best * x for x in d]) - J_at([-eps_best * x for x in d])) / (2 * eps_best)
         worst_fd = max(worst_fd, abs(fd - dJ) / abs(dJ))
-    print(f"channel 128x96x64, 40 steps, dt {ctrl.dtime:.3e}: J = {J:.10e}, adjoint run {t_adj:.2f} s; "
-          f"16 directions: max rel |<grad,d> - dJ_tlm| = {worst_tlm:.2e}, max rel |FD - dJ_tlm| = "
-          f"{worst_fd:.2e} (eps {eps_best:g})")
+    print(f"channel 128x96x64, model {model}, 40 steps, dt {ctrl.dtime:.3e}: J = {J:.10e}, adjoint run "
+          f"{t_adj:.2f} s; {ndir} directions: max rel |<grad,d> - dJ_tlm| = {worst_tlm:.2e}, max rel |FD - "
+          f"dJ_tlm| = {worst_fd:.2e} (eps {eps_best:g})")
     assert worst_tlm <= 1e-9
     assert worst_fd <= 1e-4
