@@ -537,9 +537,10 @@ int lester_statistics(const double *u, const double *v, const double *w, const d
  * lester_tangent_run returns J and the directional derivative dJ along
  * (dfu, dfv, dfw) by the linearised step.  Scope: psolve FP64 or MIXED
  * (converged: the linearisation of an iterative solve is the exact solve),
- * rholo == rhohi, model 0, no ZERO_GRAD sides, wall points in the laminar
- * branch of the wall function (y+ below ylaminar).  Errors as lester_step;
- * LES_ERR_ARG outside that scope. */
+ * rholo == rhohi, model 0 or 1 (Smagorinsky, Cartesian, walls only on the
+ * y sides), no ZERO_GRAD sides, wall points in the laminar branch of the
+ * wall function (y+ below ylaminar).  Errors as lester_step; LES_ERR_ARG
+ * outside that scope. */
 typedef struct lester_adj_cfg {
     int nsteps;
     int j_first, j_last;  /* objective window, 1 <= j_first <= j_last <= nsteps */
