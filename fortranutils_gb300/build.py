@@ -44,6 +44,7 @@ UNITS = {
     "lester_adjoint": ("lester_adjoint.cu", []),
     "k_outflow": ("k_outflow.cu", ["-fmad=false"]),
     "lester_outflow": ("lester_outflow.cu", []),
+    "k_graph": ("k_graph.cu", []),
 }
 
 

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
                                                    double visc, double ylaminar, double kappa,
                                                    double cwfun)
 {
+    if (A_.iststep) iststep = *A_.iststep;
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
@@ -228,6 +229,7 @@ __global__ void __launch_bounds__(128) k_set_w_int(const BlkDev *__restrict__ bl
                                                    double dtime, int iststep, double visc,
                                                    double ylaminar, double kappa, double cwfun)
 {
+    if (A_.iststep) iststep = *A_.iststep;
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;

@@ -10,6 +10,7 @@ namespace les {
 
 // running count of kernel launches made by this library
 void count_launch(long n);
+long launch_count();  // kernels launched so far (count_launch's total)
 
 // k_exact.cu
 void launch_halo(const FaceDev *faces, int nface, long maxface, double *var, double *work,
@@ -185,6 +186,16 @@ void launch_statistics(const BlkDev *blk, int nb, long maxpts, long maxij, int n
 void launch_recycling(const BlkDev *blk, const int *nijk, int nb, int step, int inblock, int jmult, double rhohi,
                       const RecycProf &P, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                       double *v_int, double *w_int, double *work, cudaStream_t st);
+
+// whole-step graph: the fast solve's cycle loop controlled on the device
+// (k_graph.cu; d_loop layout there)
+void launch_loop_init(cudaGraphConditionalHandle h, const double *small, double *loop, double rtol,
+                      cudaStream_t st);
+void launch_loop_step(cudaGraphConditionalHandle h, const double *small, double *loop, double rtol, int maxit,
+                      int may_switch, cudaStream_t st);
+void launch_loop_gate(cudaGraphConditionalHandle h, const double *small, double *loop, double rtol, int confirm,
+                      cudaStream_t st);
+void launch_copy_flag(const int *src, double *dst, cudaStream_t st);
 
 } // namespace les
 

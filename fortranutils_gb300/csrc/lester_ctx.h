@@ -152,7 +152,37 @@ struct Ctx {
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)
     long tabcap = 0, tab_next = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
+    // whole-step graph (ctrl.step_graph, lester_step.cu)
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        lester_fields key{};  // the fields it was captured with
+        lester_ctrl ctrl{};   // and the controls
+        long coef_gen = -1;
+        long launches = 0;    // kernels captured (the cycle loop's body once)
+        long body_launches = 0;  // kernels of one cycle
+        bool kry = false;     // its cycles are flexible CG
+        bool failed = false;  // capture failed for this key: run as launched
+        long replays = 0;     // steps run by replaying it
+        long handovers = 0;   // of those, solves the host loop finished
+        std::string why;      // the capture failure's message
+    } sg;
+    bool capturing = false;     // lester_step is being captured
+    cudaStream_t graph_stream = nullptr;  // the capture's stream (the caller's may be the legacy one)
+    cudaGraphConditionalHandle sg_post = 0;  // gate of the step after the solve
+    int *d_step = nullptr;      // iststep of the replayed step (device copy)
+    int *h_step = nullptr;      // its pinned host source
+    double *d_loop = nullptr;   // cycle-loop state of the captured solve
+    double *h_loop = nullptr;   // pinned copy of it, read after the step
+    bool force_krylov = false;  // the next fast solve starts in flexible CG
+    int cycle_budget = -1;      // and runs at most this many cycles (-1: max_outer)
 };
+
+// whole-step graph: conditional nodes inside the capture on c.stream
+// (lester_host.cu)
+int graph_cond_handle(Ctx &c, cudaGraphConditionalHandle *h);
+int graph_add_conditional(Ctx &c, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t *body);
+int graph_begin_body(Ctx &c, cudaGraph_t body, cudaStream_t *saved);
+int graph_end_body(Ctx &c, cudaStream_t saved);
 
 extern Ctx *g_ctx;
 extern std::string g_err;

@@ -24,6 +24,7 @@ std::string g_err;
 static std::atomic<long> g_launches(0);
 
 void count_launch(long n) { g_launches += n; }
+long launch_count() { return g_launches.load(); }
 
 int set_err(int code, const char *fmt, ...)
 {
@@ -458,6 +459,12 @@ static void free_ctx(Ctx *c)
         }
     for (double *p : c->scratch) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
+    if (c->sg.exec) cudaGraphExecDestroy(c->sg.exec);
+    if (c->graph_stream) cudaStreamDestroy(c->graph_stream);
+    if (c->h_step) cudaFreeHost(c->h_step);
+    if (c->h_loop) cudaFreeHost(c->h_loop);
+    cudaFree(c->d_step);
+    cudaFree(c->d_loop);
     if (c->d_tabpool) cudaFree(c->d_tabpool);
     for (void *p : {(void *)c->f32.tab.E2, (void *)c->f32.tab.N2, (void *)c->f32.tab.R2, (void *)c->f32.tab.Ez,
                     (void *)c->f32.tab.Nz, (void *)c->f32.tab.Rz})
@@ -878,6 +885,116 @@ static int fcg_reset(Ctx &c)
     return 0;
 }
 
+// ---- whole-step graph: conditional nodes inside a stream capture --------
+// A conditional handle of the graph being captured on c.stream, reset to 0
+// at each launch of the graph.
+int graph_cond_handle(Ctx &c, cudaGraphConditionalHandle *h)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    LES_CUDA(cudaStreamGetCaptureInfo(c.stream, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive || !g) return set_err(LES_ERR_CUDA, "step graph: no capture in progress");
+    LES_CUDA(cudaGraphConditionalHandleCreate(h, g, 0, cudaGraphCondAssignDefault));
+    return 0;
+}
+
+// A conditional node (WHILE or IF) at the current point of the capture on
+// c.stream; the capture continues after it.  *body is its empty body graph.
+int graph_add_conditional(Ctx &c, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t *body)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t nd = 0;
+    LES_CUDA(cudaStreamGetCaptureInfo(c.stream, &cs, nullptr, &g, &deps, &edges, &nd));
+    if (cs != cudaStreamCaptureStatusActive || !g) return set_err(LES_ERR_CUDA, "step graph: no capture in progress");
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    LES_CUDA(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
+    *body = p.conditional.phGraph_out[0];
+    LES_CUDA(cudaStreamUpdateCaptureDependencies(c.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return 0;
+}
+
+// Work issued on c.stream goes into `body` (on the capture stream) until
+// graph_end_body.
+int graph_begin_body(Ctx &c, cudaGraph_t body, cudaStream_t *saved)
+{
+    *saved = c.stream;
+    LES_CUDA(cudaStreamBeginCaptureToGraph(c.cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    c.stream = c.cap_stream;
+    return 0;
+}
+
+int graph_end_body(Ctx &c, cudaStream_t saved)
+{
+    cudaGraph_t g = nullptr;
+    c.stream = saved;
+    cudaError_t pre = cudaGetLastError();
+    cudaError_t e = cudaStreamEndCapture(c.cap_stream, &g);
+    if (pre != cudaSuccess) return set_err(LES_ERR_CUDA, "step graph: in a conditional body: %s", cudaGetErrorString(pre));
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "step graph: conditional body: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+// The fast solve as captured into the whole-step graph: the initial
+// residual, then a WHILE node whose body is one cycle (the same launches
+// as the per-cycle graph) and k_loop_step's decision, then the gate of the
+// rest of the step (c.sg_post, set by k_loop_gate).  The loop ends on
+// convergence, max_outer cycles, a non-finite residual, or -- with krylov 2
+// -- a defect-correction cycle that fails to halve the residual; the host
+// reads the outcome after the step (d_loop).
+template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double *f, double *b, int prec)
+{
+    int r = prepare_coef<T>(c, A, prec);  // cached: no work while capturing
+    if (r) return r;
+    FastSet<T> &F = fset<T>(c);
+    if (c.c.rb_line && !F.cp) return set_err(LES_ERR_ARG, "step graph: y-line scratch not allocated");
+    LevelGeom &L1 = c.lv[1];
+    const int nb = c.g.numbl;
+    const double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
+    const int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
+    const bool kry = c.c.krylov == 1;
+    launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
+    if (c.singular) launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, c.d_partial, c.d_bmean, c.stream);
+    if (kry && (r = fcg_reset(c))) return r;
+    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                          c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial, c.d_small,
+                          c.stream);
+    cudaGraphConditionalHandle hw;
+    if ((r = graph_cond_handle(c, &hw)) || (r = graph_cond_handle(c, &c.sg_post))) return r;
+    launch_loop_init(hw, c.d_small, c.d_loop, rtol, c.stream);
+    cudaGraph_t body;
+    cudaStream_t saved;
+    if ((r = graph_add_conditional(c, hw, cudaGraphCondTypeWhile, &body)) || (r = graph_begin_body(c, body, &saved)))
+        return r;
+    const long l0 = launch_count();
+    fast_vcycle<T>(c);
+    if (kry) {
+        launch_fcg<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, F.x, f, c.d_fp, c.d_fq, c.d_fr, F.b,
+                      L1.d_push, c.d_partial, c.d_small + 16, c.d_small, c.stream);
+    } else {
+        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                              c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial, c.d_small, c.stream);
+    }
+    launch_loop_step(hw, c.d_small, c.d_loop, rtol, maxit, c.c.krylov == 2 && !kry, c.stream);
+    c.sg.body_launches = launch_count() - l0;
+    if ((r = graph_end_body(c, saved))) return r;
+    // flexible CG: its recursive residual confirmed against b - A p
+    if (kry)
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                              c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small, c.stream);
+    launch_loop_gate(c.sg_post, c.d_small, c.d_loop, rtol, kry, c.stream);
+    c.sg.kry = kry;
+    return 0;
+}
+
 // p <- p + V(b - A p) (defect correction), or flexible CG with the V-cycle
 // as preconditioner, until ||b - A p|| <= rtol ||b||.  krylov 2 starts with
 // defect correction and moves to flexible CG (from the current p) at the
@@ -905,6 +1022,11 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
     int nb = c.g.numbl;
     double rtol = c.c.rtol > 0 ? c.c.rtol : 1e-8;
     int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
+    // a solve handed back by a replayed step: flexible CG, the cycles left
+    if (c.cycle_budget >= 0) maxit = c.cycle_budget;
+    const bool forced = c.force_krylov;
+    c.cycle_budget = -1;
+    c.force_krylov = false;
     for (cudaEvent_t &e : c.ev_solve)
         if (!e) LES_CUDA(cudaEventCreate(&e));
     LES_CUDA(cudaEventRecord(c.ev_solve[0], c.stream));
@@ -918,7 +1040,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
         if (!c.d_bmean) LES_CUDA(cudaMalloc(&c.d_bmean, sizeof(double) * LES_MAXBL));
         launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, c.d_partial, c.d_bmean, c.stream);
     }
-    bool kry = c.c.krylov == 1;
+    bool kry = c.c.krylov == 1 || forced;
     const bool may_switch = c.c.krylov == 2;
     if (kry && (r = fcg_reset(c))) return r;
     launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
@@ -1027,6 +1149,7 @@ template <typename T> static int fast_solve(Ctx &c, const Coef &A, double *f, do
             c.c.rb_line = tu.line;
             c.rb_threads = tu.threads;
         }
+        if (c.capturing) return fast_solve_graph<T>(c, A, f, b, prec);
         return fast_solve_run<T>(c, A, f, b, residu, prec);
     }
     int r;

@@ -219,6 +219,7 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
     A.off_jk = c.d_offjk;
     A.off2_lev1_base = 0;
     A.fb = c.fb[iv - 1];
+    A.iststep = c.capturing ? c.d_step : nullptr;
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
     if (!k.exact) {
@@ -271,6 +272,7 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
     A.off_ki = c.d_offki;
     A.off_jk = c.d_offjk;
     A.fb = c.fb[2];
+    A.iststep = c.capturing ? c.d_step : nullptr;
     const lester_ctrl &k = c.c;
     LevelGeom &L = c.lv[1];
     if (!k.exact) {
@@ -450,10 +452,15 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
         LES_CUDA(cudaMemsetAsync(c.d_wave, 0, sizeof(WaveSync), c.stream));
         LES_CUDA(LES_PHYS(c, launch_sc1_sweep)(L.d_blk, c.d_wcum, c.d_wslice, c.nslice, maxctas, smin, smax, A,
                                                c.c.dtime, c.d_wave, 1L << 24, c.stream));
-        int err = 0;
-        LES_CUDA(cudaMemcpyAsync(&err, &c.d_wave->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-        LES_CUDA(cudaStreamSynchronize(c.stream));
-        if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: grid barrier of the scalar sweep timed out");
+        if (c.capturing) {
+            // a replayed step reads the barrier's flag with its other status
+            launch_copy_flag(&c.d_wave->err, c.d_loop + 6, c.stream);
+        } else {
+            int err = 0;
+            LES_CUDA(cudaMemcpyAsync(&err, &c.d_wave->err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            LES_CUDA(cudaStreamSynchronize(c.stream));
+            if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: grid barrier of the scalar sweep timed out");
+        }
     } else {
         LES_PHYS(c, launch_sc1_waves)(L.d_blk, c.g.numbl, L.maxjk, smin, smax, A, c.c.dtime, c.stream);
     }

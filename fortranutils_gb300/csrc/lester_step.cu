@@ -10,7 +10,10 @@
 // device mirrors before the step and back after it (one copy each way per
 // call).  Scratch fields passed as NULL are kept on the device by the
 // library.
+#include <algorithm>
+#include <cstdio>
 #include <cstring>
+
 #include "kernels.h"
 #include "lester_ctx.h"
 
@@ -81,69 +84,15 @@ enum { M_DIP, M_DIU, M_DIV, M_DIX, M_RDIP, M_RDIV, M_RDIX, M_DJP, M_DJU, M_DJV, 
        M_RDJX, M_HIJP, M_HJIP, M_HKIP, M_HKJP, M_HIJU, M_HJIU, M_HKIU, M_HKJU, M_HIJV, M_HJIV, M_HKIV,
        M_HKJV, M_RP, M_RU, M_RV, M_DIDJP, M_RDIDJP, M_DIDJU, M_RDIDJU, M_DJDIV, M_RDJDIV };
 
-int lester_step(lester_fields *F, const int *istep)
+// step.F:214-420 up to the Poisson right-hand side: inlet planes, wall
+// ghosts, eddy viscosity, scalar, the three predictors, coeff_p (first
+// step), sour_p
+static int step_pre(Ctx &c, lester_fields &D, const int *istep)
 {
-    LES_NEED_CTX();
-    Ctx &c = *g_ctx;
-    if (!F || !istep) return set_err(LES_ERR_ARG, "null fields / istep");
-    int r0;
-    if ((r0 = ensure_sides(c))) return r0;
-    if (has_inlet(c) && (!c.d_uprof || !c.d_vprof))
-        return set_err(LES_ERR_ARG, "inlet blocks set without profiles (lester_gpu_set_inlet)");
-    // whole-state staging: host arrays are mirrored once for the step
-    Staging st(&c, __func__);
-    lester_fields D = *F;
-    long n3 = c.tot_sg3, nm = c.tot3;
-    double **f3[] = {&D.u, &D.v, &D.w, &D.sc1, &D.rho, &D.rhonp1, &D.rhonm1, &D.u_int, &D.v_int, &D.w_int,
-                     &D.hn_u, &D.hn_v, &D.hn_w, &D.hn_sc1, &D.gam, &D.gamsc1, &D.gamlam, &D.sc1var, &D.sc1dis,
-                     &D.vd_damping, &D.temperature, &D.drhonp1dt, &D.srhot, &D.srhoux};
-    int r;
-    int nscr = 0;
-    for (double **pp : f3) {
-        if (*pp) RET(st.io(*pp, n3, pp));
-        else {
-            // library-held scratch field
-            if ((int)c.scratch.size() <= nscr) {
-                double *d = nullptr;
-                if (cudaMalloc(&d, sizeof(double) * n3) != cudaSuccess) {
-                    cudaGetLastError();
-                    return set_err(LES_ERR_NOMEM, "step scratch allocation failed");
-                }
-                cudaMemsetAsync(d, 0, sizeof(double) * n3, c.stream);
-                c.scratch.push_back(d);
-            }
-            *pp = c.scratch[nscr++];
-        }
-    }
-    double **fm[] = {&D.p, &D.s, &D.res, &D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
-    for (double **pp : fm) {
-        if (!*pp) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
-        RET(st.io(*pp, nm, pp));
-    }
-    for (int q = 0; q < 35; q++) {
-        if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
-        RET(st.io(D.metric[q], c.tot2, &D.metric[q]));
-    }
-    RET(st.io(D.dkp, c.tot1k, &D.dkp));
-    RET(st.io(D.dkw, c.tot1k, &D.dkw));
-    {
-        long tl[12] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1, c.totjk, c.totjk, c.tot2_l1, c.tot2_l1,
-                       c.totjk, c.totjk, c.totki, c.totki};
-        // tot2_l1 is known once the tables exist
-        if (!c.d_offki) {
-            long l1 = 0;
-            for (int b = 1; b <= c.g.numbl; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
-            for (int q : {2, 3, 6, 7}) tl[q] = l1;
-        }
-        for (int q = 0; q < 12; q++) {
-            if (!D.tw[q]) return set_err(LES_ERR_ARG, "wall array %d missing", q);
-            RET(st.io(D.tw[q], tl[q], &D.tw[q]));
-        }
-    }
     double *const *m = D.metric;
     double **tw = D.tw;
     const lester_ctrl &k = c.c;
-    const int one = 1, iU = 1, iV = 2, iW = 3;
+    const int one = 1, iU = 1, iV = 2;
     double zero = 0.0;
     const double *mx[12] = {m[M_DIP], m[M_DIU], m[M_DIX], m[M_DJP], m[M_DJV], m[M_DJX],
                             m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], m[M_RU], m[M_RV]};
@@ -204,12 +153,22 @@ int lester_step(lester_fields *F, const int *istep)
                            D.ae, D.as, D.an, D.al, D.ar));
     RET(lester_sour_p(m[M_DIU], m[M_DJV], m[M_RDIV], m[M_RDJU], m[M_DIDJP], D.dkp, m[M_RDIDJP], D.dkw, D.u_int,
                       D.v_int, D.w_int, D.rho, D.rhonp1, D.drhonp1dt, D.s, D.srhot, D.srhoux, nullptr, nullptr));
-    c.want_norms = false;
-    int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
-    c.want_norms = true;
-    // the reference carries on after nummgits cycles whatever the residual;
-    // a fast solver that stops short reports it and the step continues
-    if (rs && rs != LES_ERR_NOT_CONVERGED) return rs;
+    return 0;
+}
+
+// step.F:420-454 after the Poisson solve: extrap_p, p_ref_subtract, the
+// projection, slip sides, outflow updates, the density rotation
+static int step_post(Ctx &c, lester_fields &D, const int *istep)
+{
+    double *const *m = D.metric;
+    const double *mx[12] = {m[M_DIP], m[M_DIU], m[M_DIX], m[M_DJP], m[M_DJV], m[M_DJX],
+                            m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], m[M_RU], m[M_RV]};
+    // conv_exitbc(task, iva) of step.F:344 and 435
+    auto exitbc = [&](int task, int iva) {
+        return exit_task(c, task, iva, D.rho, D.rhonp1, D.u, D.v, D.w, D.u_int, D.v_int, D.w_int, D.hn_u, D.hn_v,
+                         D.hn_w, mx, D.dkp, D.dkw, m[M_RDIDJP]);
+    };
+    const int iU = 1, iV = 2, iW = 3;
     RET(lester_extrap_p(D.p, nullptr, nullptr));
     RET(lester_p_ref_subtract(D.p));
     RET(lester_uvw_adv(&iU, m[M_DIU], m[M_RP], D.dkw, D.u, D.u_int, D.rhonp1, D.p, nullptr, nullptr, istep));
@@ -219,10 +178,247 @@ int lester_step(lester_fields *F, const int *istep)
                       D.w, D.sc1, D.rho, D.p, istep));
     for (int iva = 1; iva <= 3; iva++) RET(exitbc(2, iva));
     RET(lester_swap_rhos(D.rho, D.rhonp1, D.rhonm1));
+    return 0;
+}
+
+// ---- the whole step as one CUDA graph (ctrl.step_graph) -----------------
+// Capture: step_pre, the fast solve as a device-controlled loop (a WHILE
+// node, fast_solve_graph), then step_post inside an IF node that runs when
+// the solve converged or used its cycles -- the cases in which the step
+// as launched carries on.  The loop state is copied to pinned memory at
+// the end; the step counter of the predictors' running means is copied in
+// at the start.  Nothing runs while capturing, so a capture that fails
+// leaves the state as it was and the step runs as launched.
+static int step_capture(Ctx &c, lester_fields &D, const int *istep)
+{
+    if (c.sg.exec) cudaGraphExecDestroy(c.sg.exec);
+    c.sg.exec = nullptr;
+    if (!c.h_step) LES_CUDA(cudaMallocHost(&c.h_step, sizeof(int)));
+    if (!c.h_loop) LES_CUDA(cudaMallocHost(&c.h_loop, 8 * sizeof(double)));
+    if (!c.d_step) LES_CUDA(cudaMalloc(&c.d_step, sizeof(int)));
+    if (!c.d_loop) LES_CUDA(cudaMalloc(&c.d_loop, 8 * sizeof(double)));
+    if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
+    if (!c.graph_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.graph_stream, cudaStreamNonBlocking));
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    cudaGetLastError();
+    const long l0 = launch_count();
+    // captured on a stream of our own; the graph is launched on c.stream
+    const cudaStream_t user = c.stream;
+    c.stream = c.graph_stream;
+    if (cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        c.stream = user;
+        cudaGetLastError();
+        return set_err(LES_ERR_CUDA, "step graph: cannot begin the capture");
+    }
+    c.capturing = true;
+    int r = 0;
+    if (cudaMemcpyAsync(c.d_step, c.h_step, sizeof(int), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
+        cudaMemsetAsync(c.d_loop, 0, 8 * sizeof(double), c.stream) != cudaSuccess)
+        r = set_err(LES_ERR_CUDA, "step graph: status copies");
+    if (!r) r = step_pre(c, D, istep);
+    if (!r) {
+        c.want_norms = false;
+        r = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
+        c.want_norms = true;
+    }
+    if (!r) {
+        cudaGraph_t body;
+        cudaStream_t saved;
+        r = graph_add_conditional(c, c.sg_post, cudaGraphCondTypeIf, &body);
+        if (!r) r = graph_begin_body(c, body, &saved);
+        if (!r) {
+            r = step_post(c, D, istep);
+            const int r2 = graph_end_body(c, saved);
+            if (!r) r = r2;
+        }
+    }
+    if (!r && cudaMemcpyAsync(c.h_loop, c.d_loop, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+        r = set_err(LES_ERR_CUDA, "step graph: status copy");
+    c.capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+    c.stream = user;
+    const long captured = launch_count() - l0;
+    count_launch(-captured);  // captured, not launched
+    if (r || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return r ? r : set_err(LES_ERR_CUDA, "step graph capture: %s", cudaGetErrorString(e));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&c.sg.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        cudaGetLastError();
+        c.sg.exec = nullptr;
+        return set_err(LES_ERR_CUDA, "step graph instantiate: %s", cudaGetErrorString(ei));
+    }
+    c.sg.launches = captured;
+    return 0;
+}
+
+// The step by its graph.  *done is false when it is not eligible or
+// cannot be captured (the caller runs it as launched); otherwise the return
+// value is the step's.
+static int step_graph_run(Ctx &c, lester_fields &D, const int *istep);
+
+static int step_graph(Ctx &c, lester_fields &D, const int *istep, bool *done)
+{
+    *done = false;
+    const int ps = c.c.psolve;
+    if (*istep == 1 || (ps != LES_PSOLVE_FP64 && ps != LES_PSOLVE_MIXED) || c.prof || has_inlet(c) ||
+        has_convective(c))
+        return 0;
+    const int prec = ps == LES_PSOLVE_MIXED ? 32 : 64;
+    if (c.c.autotune && !c.tuned[prec == 32 ? 1 : 0].done) return 0;
+    // the coefficients converted by an earlier solve of this precision
+    const double *coef[7] = {D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar};
+    bool ready = c.coef_prec == prec && c.coef_gen_seen == c.coef_gen;
+    for (int q = 0; q < 7; q++) ready = ready && c.coef_key[q] == coef[q];
+    if (!ready || (c.c.krylov == 1 && !c.d_fr) || (c.singular && !c.d_bmean)) return 0;
+    const bool same = !memcmp(&c.sg.key, &D, sizeof D) && !memcmp(&c.sg.ctrl, &c.c, sizeof c.c) &&
+                      c.sg.coef_gen == c.coef_gen;
+    if (same && c.sg.failed) return 0;
+    if (!same || !c.sg.exec) {
+        c.sg.key = D;
+        c.sg.ctrl = c.c;
+        c.sg.coef_gen = c.coef_gen;
+        c.sg.failed = step_capture(c, D, istep) != 0;
+        if (c.sg.failed) {
+            c.sg.why = g_err;
+            g_err.clear();
+            return 0;
+        }
+    }
+    *done = true;
+    return step_graph_run(c, D, istep);
+}
+
+static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
+{
+    *c.h_step = c.iststep;
+    LES_CUDA(cudaGraphLaunch(c.sg.exec, c.stream));
+    c.sg.replays++;
+    LES_CUDA(cudaStreamSynchronize(c.stream));
+    const double *h = c.h_loop;
+    const int status = (int)h[4], cycles = (int)h[3];
+    count_launch(c.sg.launches + (long)(cycles - 1) * c.sg.body_launches);
+    c.last_cycles = cycles;
+    c.last_relres = h[1];
+    c.last_solve_ms = -1;  // not timed inside the graph
+    if (h[6] != 0) return set_err(LES_ERR_TIMEOUT, "set_sc1: grid barrier of the scalar sweep timed out");
+    if (status == 4) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", cycles);
+    if (status == 3 || status == 5) {
+        // the host loop takes over: flexible CG from the current p with the
+        // cycles left, then the rest of the step
+        const int maxit = c.c.max_outer > 0 ? c.c.max_outer : 100;
+        c.sg.handovers++;
+        c.force_krylov = true;
+        c.cycle_budget = std::max(0, maxit - cycles);
+        c.want_norms = false;
+        int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
+        c.want_norms = true;
+        c.last_cycles += cycles;
+        if (rs && rs != LES_ERR_NOT_CONVERGED) return rs;
+        RET(step_post(c, D, istep));
+        c.iststep += 1;
+        return rs;
+    }
+    c.iststep += 1;
+    if (status == 2)
+        return set_err(LES_ERR_NOT_CONVERGED, "relative residual %.3e after %d cycles", h[1], cycles);
+    return 0;
+}
+
+int lester_step(lester_fields *F, const int *istep)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    if (!F || !istep) return set_err(LES_ERR_ARG, "null fields / istep");
+    int r0;
+    if ((r0 = ensure_sides(c))) return r0;
+    if (has_inlet(c) && (!c.d_uprof || !c.d_vprof))
+        return set_err(LES_ERR_ARG, "inlet blocks set without profiles (lester_gpu_set_inlet)");
+    // whole-state staging: host arrays are mirrored once for the step
+    Staging st(&c, __func__);
+    lester_fields D = *F;
+    long n3 = c.tot_sg3, nm = c.tot3;
+    double **f3[] = {&D.u, &D.v, &D.w, &D.sc1, &D.rho, &D.rhonp1, &D.rhonm1, &D.u_int, &D.v_int, &D.w_int,
+                     &D.hn_u, &D.hn_v, &D.hn_w, &D.hn_sc1, &D.gam, &D.gamsc1, &D.gamlam, &D.sc1var, &D.sc1dis,
+                     &D.vd_damping, &D.temperature, &D.drhonp1dt, &D.srhot, &D.srhoux};
+    int r;
+    int nscr = 0;
+    for (double **pp : f3) {
+        if (*pp) RET(st.io(*pp, n3, pp));
+        else {
+            // library-held scratch field
+            if ((int)c.scratch.size() <= nscr) {
+                double *d = nullptr;
+                if (cudaMalloc(&d, sizeof(double) * n3) != cudaSuccess) {
+                    cudaGetLastError();
+                    return set_err(LES_ERR_NOMEM, "step scratch allocation failed");
+                }
+                cudaMemsetAsync(d, 0, sizeof(double) * n3, c.stream);
+                c.scratch.push_back(d);
+            }
+            *pp = c.scratch[nscr++];
+        }
+    }
+    double **fm[] = {&D.p, &D.s, &D.res, &D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
+    for (double **pp : fm) {
+        if (!*pp) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
+        RET(st.io(*pp, nm, pp));
+    }
+    for (int q = 0; q < 35; q++) {
+        if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
+        RET(st.io(D.metric[q], c.tot2, &D.metric[q]));
+    }
+    RET(st.io(D.dkp, c.tot1k, &D.dkp));
+    RET(st.io(D.dkw, c.tot1k, &D.dkw));
+    {
+        long tl[12] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1, c.totjk, c.totjk, c.tot2_l1, c.tot2_l1,
+                       c.totjk, c.totjk, c.totki, c.totki};
+        // tot2_l1 is known once the tables exist
+        if (!c.d_offki) {
+            long l1 = 0;
+            for (int b = 1; b <= c.g.numbl; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
+            for (int q : {2, 3, 6, 7}) tl[q] = l1;
+        }
+        for (int q = 0; q < 12; q++) {
+            if (!D.tw[q]) return set_err(LES_ERR_ARG, "wall array %d missing", q);
+            RET(st.io(D.tw[q], tl[q], &D.tw[q]));
+        }
+    }
+    if (c.c.step_graph && !st.any_host()) {
+        bool done = false;
+        const int rg = step_graph(c, D, istep, &done);
+        if (done) return rg;
+    }
+    RET(step_pre(c, D, istep));
+    c.want_norms = false;
+    int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
+    c.want_norms = true;
+    // the reference carries on after nummgits cycles whatever the residual;
+    // a fast solver that stops short reports it and the step continues
+    if (rs && rs != LES_ERR_NOT_CONVERGED) return rs;
+    RET(step_post(c, D, istep));
     c.iststep += 1;  // code/step.F:181, ready for the next step
     r = st.finish();
     if (r) return r;
     return rs;
+}
+
+// steps run by replaying the whole-step graph since lester_gpu_init, and
+// whether the graph for the current fields failed to capture
+int lester_gpu_step_graph_info(long *replays, long *handovers, int *failed, char *why, int why_len)
+{
+    LES_NEED_CTX();
+    if (replays) *replays = g_ctx->sg.replays;
+    if (handovers) *handovers = g_ctx->sg.handovers;
+    if (failed) *failed = g_ctx->sg.failed ? 1 : 0;
+    if (why && why_len > 0) {
+        snprintf(why, (size_t)why_len, "%s", g_ctx->sg.failed ? g_ctx->sg.why.c_str() : "");
+    }
+    return 0;
 }
 
 } // extern "C"

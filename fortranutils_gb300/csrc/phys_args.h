@@ -20,6 +20,7 @@ struct UIntArgs {
     // fast variant only: reciprocals of the divisor metrics (same layout)
     const double *r_dip, *r_diu, *r_dix, *r_djp, *r_dju, *r_djv, *r_djx, *r_rp, *r_dkp, *r_dkw;
     const double *fb;  // body force of this component per unit volume, or null
+    const int *iststep;  // replayed graphs: the step counter on the device, or null
 };
 
 struct WIntArgs {
@@ -32,6 +33,7 @@ struct WIntArgs {
     const double *r[MW_N];        // fast variant only: reciprocals of m[]
     const double *rdkp, *rdkw;
     const double *fb;             // body force of w per unit volume, or null
+    const int *iststep;           // replayed graphs: the step counter on the device, or null
 };
 
 struct Sc1Args {

@@ -60,7 +60,7 @@ class Ctrl(C.Structure):
         ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
-        ("rb_line", C.c_int), ("autotune", C.c_int),
+        ("rb_line", C.c_int), ("autotune", C.c_int), ("step_graph", C.c_int),
     ]
 
 
@@ -214,6 +214,16 @@ def gpu_solve_stats():
     _check(lib().lester_gpu_solve_stats(o))
     return {"rnorm": o[0], "fnorm": o[1], "enorm": o[2], "vnorm": o[3], "cycles": int(o[4]),
             "relres": o[5]}
+
+
+def gpu_step_graph_info() -> dict:
+    """Steps replayed from the whole-step graph since gpu_init, the solves
+    among them the host loop finished, and whether the current fields'
+    graph failed to capture (with the reason)."""
+    n, h, f = C.c_long(), C.c_long(), C.c_int()
+    why = C.create_string_buffer(512)
+    _check(lib().lester_gpu_step_graph_info(C.byref(n), C.byref(h), C.byref(f), why, 512))
+    return {"replays": n.value, "handovers": h.value, "failed": bool(f.value), "why": why.value.decode()}
 
 
 def gpu_tuned(prec: int) -> dict:

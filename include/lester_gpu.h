@@ -140,6 +140,12 @@ typedef struct lester_ctrl {
                           tail threshold) on its own system and keeps the
                           fastest for the rest of the run
                           (lester_gpu_tuned); 0 = the controls as given */
+    int step_graph;    /* 1 = lester_step replays the whole step as one CUDA
+                          graph, the fast solve's cycle loop a device-side
+                          conditional (WHILE) node; captured once per field
+                          set and controls (istep > 1, fast psolve, device
+                          fields, no inflow/outflow sides, autotuning
+                          finished); otherwise the step runs as launched */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */
@@ -521,6 +527,16 @@ int lester_statistics(const double *u, const double *v, const double *w, const d
                       const double *sc1dis, double *sc1varm, double *sc1dism, const double *temperature, double *t_m,
                       const double *dip, const double *djp, const double *rp, const double *dkp, const double *dkw,
                       const double *x, const double *y, const double *z, const int *step);
+
+/* Steps run by replaying the whole-step graph (ctrl.step_graph) since
+ * lester_gpu_init; of those, the steps whose pressure solve the host loop
+ * finished (krylov 2: a defect-correction cycle failed to halve the
+ * residual, so the solve continues in flexible CG; krylov 1: the CG
+ * residual missed the tolerance once recomputed); 1 in *failed if the graph
+ * for the current fields and controls could not be captured (those steps
+ * run as launched), with the reason in why (why_len bytes, NUL-terminated;
+ * may be NULL).  No counterpart in the reference. */
+int lester_gpu_step_graph_info(long *replays, long *handovers, int *failed, char *why, int why_len);
 
 /* ---- adjoint and tangent-linear runs ---------------------------------- */
 /* No counterpart in the reference.  A run of nsteps lester_step calls from

@@ -131,3 +131,50 @@ def test_variable_density_fast_solver_converges(psolve, gpulib):
     assert rcs == [0, 0, 0]
     for n in S.STATE:
         assert np.all(np.isfinite(got[n])), n
+
+
+GRAPH_VARIANTS = {
+    "converged": dict(rtol=1e-9, max_outer=60),
+    # every solve stops at max_outer: the step carries on (NOT_CONVERGED)
+    "max_outer": dict(rtol=1e-12, max_outer=2),
+    # a poor smoother: defect-correction cycles stall, the auto mode hands
+    # the solve to flexible CG (on the host, after the replayed part)
+    "stall": dict(rtol=1e-9, max_outer=60, rb_sweeps=1, rb_omega=1.95),
+}
+
+
+GRAPH_CASES = [(v, k) for v in GRAPH_VARIANTS for k in (0, 1, 2) if not (v == "stall" and k == 0)]
+
+
+# (the stall variant diverges with plain defect correction, krylov 0)
+@pytest.mark.parametrize("variant,krylov", GRAPH_CASES)
+@pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
+@pytest.mark.parametrize("name", list(SETUPS))
+def test_step_graph_replays_bitwise(name, psolve, krylov, variant, gpulib):
+    """ctrl.step_graph: steps 2..5 replayed from one captured graph (the
+    solve's cycle loop a device-side WHILE node, the rest of the step behind
+    an IF node) give the fields of the steps launched call by call, bit for
+    bit, and the same return codes."""
+    n = 5
+    st, ctrl, s = make(name, psolve=psolve, krylov=krylov, **GRAPH_VARIANTS[variant])
+    plain, rc0 = gpu_steps(st, ctrl, s, n)
+    ctrl.step_graph = 1
+    g = s.to("torch")
+    L.gpu_init(st.case.geom(), ctrl)
+    try:
+        rcs = [S.step(g, it) for it in range(1, n + 1)]
+        info = L.gpu_step_graph_info()
+        L.gpu_sync()
+        got = g.to("numpy")
+    finally:
+        L.gpu_finalize()
+    assert rcs == rc0
+    if variant == "max_outer":
+        assert rcs[1:] == [-7] * (n - 1)  # LES_ERR_NOT_CONVERGED
+    assert not info["failed"], info["why"]
+    assert info["replays"] == n - 1
+    if variant == "stall" and krylov == 2:  # the handover to the host loop ran
+        assert info["handovers"] > 0
+    for f in S.STATE:
+        assert np.all(np.isfinite(plain[f])), f
+        assert np.array_equal(got[f], plain[f]), f
