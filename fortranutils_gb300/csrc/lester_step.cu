@@ -280,9 +280,9 @@ static int step_graph(Ctx &c, lester_fields &D, const int *istep, bool *done)
     if (same && c.sg.failed) return 0;
     if (!same || !c.sg.exec) {
         c.sg.key = D;
-        c.sg.ctrl = c.c;
         c.sg.coef_gen = c.coef_gen;
         c.sg.failed = step_capture(c, D, istep) != 0;
+        c.sg.ctrl = c.c;  // as the capture left it (with any autotuned settings)
         if (c.sg.failed) {
             c.sg.why = g_err;
             g_err.clear();
