@@ -62,7 +62,7 @@ WORKLOADS = {
                       desc="32 independent Poisson boxes in one solve, sides drawn from 32,40,...,128 "
                            "cells per axis (seed 5), cubic cells, periodic x/z and Neumann y, sources "
                            "N(0,1) minus their mean, to 1e-8"),
-    "bl6": dict(shape=(384, 144, 64), seed=3,
+    "bl6": dict(shape=(384, 144, 64), seed=3, inflow=True,
                 desc="multiblock spatially developing boundary layer: 6 uneven blocks (160,96,64) "
                      "(128,96,64) (96,96,64) below (160,48,64) (128,48,64) (96,48,64), interfaces in x "
                      "and y, fixed inflow u = tanh(y/0.5) + noise (fixed plane, no recycling), convective "
@@ -288,9 +288,9 @@ def run_gpu(args):
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
                      "launches": L.gpu_launch_count() - launches0, "rb_ms": kms,
                      "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
-        if args.step_graph:
-            res[mode]["graph"] = run_graph_leg(args, ctrl, g, istep)
         del g
+        if args.step_graph and not WORKLOADS[wl].get("inflow"):
+            res[mode]["graph"] = run_graph_leg(args, case, ctrl, wl)
         if mode == "mixed" and not args.no_e2e:
             res[mode]["e2e"] = run_e2e(args, case, ctrl, wl)
         L.gpu_finalize()
@@ -298,16 +298,20 @@ def run_gpu(args):
     return case, res
 
 
-def run_graph_leg(args, ctrl, g, istep):
-    """The same steps replayed from the whole-step CUDA graph
-    (ctrl.step_graph): two untimed steps (capture, first replay), then
-    `steps` timed ones, continuing the run."""
+def run_graph_leg(args, case, ctrl, wl):
+    """The same run again from the same initial state and step counter, the
+    steps replayed from the whole-step CUDA graph (ctrl.step_graph; the
+    autotuned settings kept): step 1 as launched (coeff_p), the graph
+    captured at step 2, the same timed step indices as the launched leg."""
     import torch
     from fortranutils_gb300 import lester as L, state as S
+    g = device_state(case, ctrl, wl)
+    L.gpu_set_iststep(2)
     ctrl.step_graph = 1
     L.gpu_set_ctrl(ctrl)
     stream = torch.cuda.current_stream()
-    for _ in range(2):
+    istep = 0
+    for _ in range(args.warmup):
         istep += 1
         S.step(g, istep)
     L.gpu_sync()
@@ -331,6 +335,7 @@ def run_graph_leg(args, ctrl, g, istep):
     info = L.gpu_step_graph_info()
     ctrl.step_graph = 0
     L.gpu_set_ctrl(ctrl)
+    del g
     if info["failed"] or info["replays"] - info0["replays"] != args.steps:
         raise RuntimeError(f"whole-step graph not replayed: {info}")
     return {"ms_per_step": e0.elapsed_time(e1) / args.steps, "cycles": float(np.mean(cyc)),
@@ -571,6 +576,7 @@ def main():
         "step_launch": mx_how,
         "mixed": {"launched_ms_per_step": mx["ms_per_step"],
                   "graph_ms_per_step": mx["graph"]["ms_per_step"] if "graph" in mx else None,
+                  "graph_vcycles_per_step": mx["graph"]["cycles"] if "graph" in mx else None,
                   "vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"], "tuned": mx["tuned"],
                   "vcycle_ms": mx["solve_ms"] / max(mx["cycles"], 1),
                   "relres_max": mx["relres_max"]},
