@@ -162,11 +162,14 @@ def cfl_dt(case, s, cfl=0.3, dfs=0.2, visc=1.0 / 2800.0):
 
 
 SMOOTHER = "auto"
+PHYS32 = 1
 
 
 def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     from fortranutils_gb300 import lester as L
     sm = dict(autotune=3) if SMOOTHER == "auto" else dict(autotune=0)
+    # the mixed path's physics in FP32 arithmetic (FP64 fields)
+    sm["phys32"] = PHYS32 if psolve == L.PSOLVE_MIXED else 0
     if SMOOTHER == "line":
         sm.update(rb_line=1, rb_omega=1.2, rb_sweeps=2)
     if wl == "mixing":
@@ -488,6 +491,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) leg")
+    ap.add_argument("--phys32", type=int, default=1, choices=[0, 1],
+                    help="mixed path: predictors, scalar and eddy viscosity in FP32 arithmetic on the FP64 "
+                         "fields (0: the FP64 physics of the FP64 path)")
     ap.add_argument("--step-graph", type=int, default=1, choices=[0, 1],
                     help="also time the steps replayed from the whole-step CUDA graph; the headline is "
                          "the faster of the two ways of running the same step")
@@ -505,8 +511,9 @@ def main():
     ap.add_argument("--shape", type=int, nargs=3, default=None,
                     help="cells per axis (other shapes than the workload's are for profiling only)")
     args = ap.parse_args()
-    global SMOOTHER
+    global SMOOTHER, PHYS32
     SMOOTHER = args.smoother
+    PHYS32 = args.phys32
     if args.shape is None:
         args.shape = list(WORKLOADS[args.workload]["shape"])
     rank, world, local = dist_env()
@@ -571,6 +578,9 @@ def main():
                    "l2": ("inputs larger than L2, no flush" if ncell * 8 * 20 > 129e6 else
                           "working set smaller than the 129 MB L2 (not flushed): a small-case figure"),
                    "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "precision": ("mixed: FP32 arithmetic in the predictors, scalar, eddy viscosity and multigrid "
+                                 "cycles; FP64 fields, fine-grid residual, global sums, metrics" if args.phys32 else
+                                 "mixed: FP32 multigrid cycles, FP64 physics") + "; fp64: all FP64",
                    "outer_loop": {"auto": "defect correction, flexible CG when a cycle stalls",
                                   "fcg": "flexible CG", "dc": "defect correction"}[args.outer]},
         "step_launch": mx_how,

@@ -15,6 +15,11 @@ import subprocess
 import sys
 from pathlib import Path
 
+try:
+    from . import gen_f32
+except ImportError:  # run as a script
+    import gen_f32
+
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
@@ -45,6 +50,10 @@ UNITS = {
     "k_outflow": ("k_outflow.cu", ["-fmad=false"]),
     "lester_outflow": ("lester_outflow.cu", []),
     "k_graph": ("k_graph.cu", []),
+    # the FP32-arithmetic physics build (namespace les_f32), generated from
+    # k_phys.cu and k_sgs.cu by gen_f32.py into the build directory
+    "k_phys_f32": ("@k_phys_f32.cu", []),
+    "k_sgs_f32": ("@k_sgs_f32.cu", []),
 }
 
 
@@ -64,7 +73,9 @@ def lib_path() -> Path:
 
 def _compile(name: str, src: str, extra: list[str], verbose: bool) -> Path:
     obj = BUILD / (name + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(CSRC / src), "-o", str(obj)]
+    # "@name": a source generated into the build directory
+    path = BUILD / src[1:] if src.startswith("@") else CSRC / src
+    cmd = [nvcc(), *ARCH, *COMMON, "-I", str(CSRC), *extra, "-c", str(path), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     res = subprocess.run(cmd, capture_output=True, text=True)
@@ -80,7 +91,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
     out = lib_path()
-    srcs = [CSRC / u[0] for u in UNITS.values()] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh"))
+    gen_f32.generate(CSRC, BUILD)
+    srcs = [BUILD / u[0][1:] if u[0].startswith("@") else CSRC / u[0] for u in UNITS.values()]
+    srcs += list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [PKG / "gen_f32.py"]
     srcs.append(PKG.parent / "include" / "lester_gpu.h")
     if out.exists() and not force:
         newest = max(p.stat().st_mtime for p in srcs)

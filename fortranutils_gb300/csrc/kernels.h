@@ -233,3 +233,6 @@ LES_PHYS_LAUNCHERS
 namespace les_fast {
 LES_PHYS_LAUNCHERS
 }
+namespace les_f32 {
+LES_PHYS_LAUNCHERS
+}

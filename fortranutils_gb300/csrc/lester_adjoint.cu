@@ -176,6 +176,8 @@ int check_scope(const Ctx &c, const lester_adj_cfg &cfg)
     if (k.psolve == LES_PSOLVE_REFERENCE)
         return set_err(LES_ERR_ARG, "adjoint: needs a converged fast pressure solve (psolve FP64 or MIXED)");
     if (k.rholo != k.rhohi) return set_err(LES_ERR_ARG, "adjoint: constant density only (rholo == rhohi)");
+    if (k.phys32 && !k.exact)
+        return set_err(LES_ERR_ARG, "adjoint: the linearised step is FP64; phys32 must be 0");
     if (k.model != 0 && k.model != 1)
         return set_err(LES_ERR_ARG, "adjoint: no eddy viscosity (model 0) or Smagorinsky (model 1) only");
     if (k.model == 1) {

@@ -197,7 +197,7 @@ int delta_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, c
 int fast_sgs_tabs(Ctx &c, const double *dip, const double *djp, const double *rp, const double *dkp,
                   const double *dkw, SgsFast &F);
 // the exact (bitwise) or fast build of the physics launchers
-#define LES_PHYS(c, fn) ((c).c.exact ? les_exact::fn : les_fast::fn)
+#define LES_PHYS(c, fn) ((c).c.exact ? les_exact::fn : (c).c.phys32 ? les_f32::fn : les_fast::fn)
 
 #define LES_CUDA(call)                                                                             \
     do {                                                                                           \

@@ -11,7 +11,19 @@
 // divisions and powers are most of these kernels' time.
 #pragma once
 
-#ifdef LES_FAST_PHYS
+#if defined(LES_F32_PHYS)
+// the FP32-arithmetic build (gen_f32.py): FP64 fields read through LdF
+#define LES_PHYS_NS les_f32
+#define QDIV(x, d, rd) ((x) * (rd))
+typedef float real;
+struct LdF {
+    const double *p;
+    __host__ __device__ __forceinline__ LdF(const double *q) : p(q) {}
+    __device__ __forceinline__ float operator[](long i) const { return (float)p[i]; }
+    __device__ __forceinline__ LdF operator+(long o) const { return LdF(p + o); }
+    __device__ __forceinline__ operator const double *() const { return p; }
+};
+#elif defined(LES_FAST_PHYS)
 #define LES_PHYS_NS les_fast
 // x / d, with rd = 1 / d precomputed
 #define QDIV(x, d, rd) ((x) * (rd))

@@ -1,0 +1,136 @@
+"""Generate the FP32-arithmetic build of the physics kernels.
+
+k_phys.cu and k_sgs.cu (momentum predictors, scalar transport, eddy
+viscosity) are written once, in FP64.  This module derives a third build
+from them, namespace les_f32, in which every kernel and device function
+computes in FP32 while the fields stay FP64 in HBM: each load from an FP64
+array is converted on the way in (``LdF``), stores convert back, locals and
+by-value parameters are ``float``, and floating literals carry an ``f``
+suffix so that no expression is promoted back to FP64.  Host code (the
+launchers) is left as written, so the les_f32 launchers have the same FP64
+signatures as les_exact's and les_fast's.  The reciprocal metric tables of
+the fast build are used (LES_FAST_PHYS).
+
+The transformation is textual and confined to the bodies of ``__global__``
+and ``__device__`` functions; the FP64 builds compile the sources as they
+are.  Called by build.py; the output goes to the build directory.
+"""
+from __future__ import annotations
+
+import re
+from pathlib import Path
+
+HEADER = """// Generated by fortranutils_gb300/gen_f32.py from {src}: the FP32-arithmetic
+// build (namespace les_f32).  Do not edit; edit {src}.
+#define LES_F32_PHYS 1
+#define LES_FAST_PHYS 1
+"""
+
+# struct members that are not FP64 arrays, or are arrays of pointers
+_NOT_FP64 = {"n", "bc", "link", "m", "r", "iststep", "off_ki", "off_jk"}
+_STRUCTS = r"(?:A_|F)"
+
+_LITERAL = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])")
+
+
+def _match_close(text: str, i: int, open_c: str, close_c: str) -> int:
+    """Index of the bracket closing the one at text[i]."""
+    depth = 0
+    for j in range(i, len(text)):
+        c = text[j]
+        if c == open_c:
+            depth += 1
+        elif c == close_c:
+            depth -= 1
+            if depth == 0:
+                return j
+    raise ValueError(f"unbalanced {open_c} at {i}")
+
+
+def _function_spans(text: str):
+    """(start, brace, end) of every __global__ / __device__ function
+    definition: start of the qualifier, its body's opening brace, closing
+    brace."""
+    spans = []
+    for m in re.finditer(r"__(?:global|device)__", text):
+        start = m.start()
+        if spans and start < spans[-1][2]:
+            continue  # a qualifier inside an earlier function
+        p = text.index("(", m.end())
+        q = _match_close(text, p, "(", ")")
+        rest = text[q + 1:]
+        k = re.match(r"[^;{]*", rest).end()
+        if q + 1 + k >= len(text) or text[q + 1 + k] != "{":
+            continue  # a declaration
+        brace = q + 1 + k
+        spans.append((start, brace, _match_close(text, brace, "{", "}")))
+    return spans
+
+
+def _params(sig: str) -> str:
+    """FP64 pointer parameters become converting views (one pointer, the
+    same layout); FP64 scalars become float in device functions but stay
+    double in kernels, whose arguments a cooperative launch passes by
+    address (an FP64 value read as an FP32 parameter would be garbage)."""
+    sig = re.sub(r"const\s+double\s*\*\s*(?:__restrict__\s*)?(?=\w)", "LdF ", sig)
+    if sig.lstrip().startswith("__global__"):
+        return sig
+    return re.sub(r"\bdouble\b(?!\s*\*)", "real", sig)
+
+
+def _member_reads(body: str) -> str:
+    """A_.x[...] / F.x[...] reads of FP64 arrays through LdF (not writes)."""
+    out, pos = [], 0
+    for m in re.finditer(_STRUCTS + r"\.(\w+)\[", body):
+        if m.group(1) in _NOT_FP64 or m.start() < pos:
+            continue
+        close = _match_close(body, m.end() - 1, "[", "]")
+        if re.match(r"\s*=(?!=)", body[close + 1:]):
+            continue  # a store
+        out.append(body[pos:m.start()])
+        out.append("LdF(" + body[m.start():m.end() - 1] + ")" + body[m.end() - 1:close + 1])
+        pos = close + 1
+    out.append(body[pos:])
+    return "".join(out)
+
+
+def _local_pointers(body: str) -> str:
+    """`const double *a = ..., *b = ...;` -> `const LdF a = ..., b = ...;`"""
+    def fix(m):
+        stmt = m.group(0)
+        stmt = re.sub(r"^const\s+double\s*\*", "const LdF ", stmt)
+        return re.sub(r",\s*\*(\w+)\s*=", r", \1 =", stmt)
+    return re.sub(r"const\s+double\s*\*(?!\s*const)\s*\w+\s*=[^;]*;", fix, body)
+
+
+def _body(body: str) -> str:
+    body = re.sub(r"M\[a\]\[", "LdF(M[a])[", body)
+    body = re.sub(r"A_\.(m|r)\[a\]\[", r"LdF(A_.\1[a])[", body)
+    body = _local_pointers(body)
+    body = _member_reads(body)
+    body = re.sub(r"\bdouble\b(?!\s*\*)", "real", body)
+    return _LITERAL.sub(lambda m: m.group(1) + "f", body)
+
+
+def transform(text: str, src: str) -> str:
+    spans = _function_spans(text)
+    out, pos = [HEADER.format(src=src)], 0
+    for start, brace, end in spans:
+        out.append(text[pos:start])
+        out.append(_params(text[start:brace]))
+        out.append(_body(text[brace:end + 1]))
+        pos = end + 1
+    out.append(text[pos:])
+    return "".join(out)
+
+
+def generate(csrc: Path, outdir: Path) -> list[Path]:
+    """Write k_phys_f32.cu and k_sgs_f32.cu into outdir (only when changed)."""
+    outs = []
+    for name in ("k_phys.cu", "k_sgs.cu"):
+        text = transform((csrc / name).read_text(), name)
+        dst = outdir / name.replace(".cu", "_f32.cu")
+        if not dst.exists() or dst.read_text() != text:
+            dst.write_text(text)
+        outs.append(dst)
+    return outs

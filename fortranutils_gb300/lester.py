@@ -60,7 +60,7 @@ class Ctrl(C.Structure):
         ("psolve", C.c_int), ("rtol", C.c_double), ("max_outer", C.c_int),
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
-        ("rb_line", C.c_int), ("autotune", C.c_int), ("step_graph", C.c_int),
+        ("rb_line", C.c_int), ("autotune", C.c_int), ("phys32", C.c_int), ("step_graph", C.c_int),
     ]
 
 

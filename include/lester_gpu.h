@@ -140,6 +140,11 @@ typedef struct lester_ctrl {
                           tail threshold) on its own system and keeps the
                           fastest for the rest of the run
                           (lester_gpu_tuned); 0 = the controls as given */
+    int phys32;        /* 1 = the predictors, scalar transport and eddy
+                          viscosity compute in FP32 on the FP64 fields (the
+                          les_f32 build; exact must be 0): the mixed path's
+                          physics, its error against the FP64 path stated
+                          per field by the tests */
     int step_graph;    /* 1 = lester_step replays the whole step as one CUDA
                           graph, the fast solve's cycle loop a device-side
                           conditional (WHILE) node; captured once per field

@@ -178,3 +178,33 @@ def test_step_graph_replays_bitwise(name, psolve, krylov, variant, gpulib):
     for f in S.STATE:
         assert np.all(np.isfinite(plain[f])), f
         assert np.array_equal(got[f], plain[f]), f
+
+
+# ctrl.phys32: the mixed path with FP32 arithmetic in the predictors, the
+# scalar transport and the eddy viscosity (FP64 fields, FP64 fine-grid
+# residual and sums).  Its error against the FP64 oracle, per field, after
+# two steps at constant density (so that the reference's SOR converges to
+# the solution the fast solvers find), relative L2:
+# (measured on the three cases: u 2.3e-8 to 2.8e-8, v 1.6e-7 to 2.6e-7,
+# w 1.2e-7 to 1.5e-7, sc1 3.2e-8, p 3.4e-7 to 1.1e-6)
+PHYS32_TOL = {"u": 2e-7, "v": 2e-6, "w": 2e-6, "sc1": 2e-7, "rho": 1e-12, "p": 1e-5}
+
+
+@pytest.mark.parametrize("name", list(SETUPS))
+def test_phys32_error_per_field(name, gpulib):
+    """The FP32-arithmetic physics build with the mixed solver against a
+    converged FP64 oracle: every field within its stated tolerance, and
+    the FP64 physics build an order of magnitude or more closer."""
+    st, ctrl, s = make(name, psolve=L.PSOLVE_MIXED, rtol=1e-10, rholo=1.0, rhohi=1.0, exact=0)
+    ref = oracle_steps(st, ctrl, s, 2, O.mgctrl(nummgits=400, tolf=1e-14))
+    fp64, _ = gpu_steps(st, ctrl, s, 2)
+    ctrl.phys32 = 1
+    got, rcs = gpu_steps(st, ctrl, s, 2)
+    assert rcs == [0, 0]
+    errs = {n: rel(got[n], ref[n]) for n in PHYS32_TOL}
+    errs64 = {n: rel(fp64[n], ref[n]) for n in PHYS32_TOL}
+    print(f"\n{name} phys32 rel L2: " + ", ".join(f"{n} {e:.1e}" for n, e in errs.items()) +
+          "; FP64 physics: " + ", ".join(f"{n} {e:.1e}" for n, e in errs64.items()))
+    for n, tol in PHYS32_TOL.items():
+        assert errs[n] <= tol, (n, errs[n], tol)
+    assert rel(got["u"], s["u"]) > 1e-6  # the step did work
