@@ -23,6 +23,8 @@ struct LdF {
     __device__ __forceinline__ LdF operator+(long o) const { return LdF(p + o); }
     __device__ __forceinline__ operator const double *() const { return p; }
 };
+// an L2 load (__ldcg) of an FP64 value, converted
+__device__ __forceinline__ float ldcg_f(const double *q) { return (float)__ldcg(q); }
 #elif defined(LES_FAST_PHYS)
 #define LES_PHYS_NS les_fast
 // x / d, with rd = 1 / d precomputed

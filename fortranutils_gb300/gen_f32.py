@@ -4,7 +4,8 @@ k_phys.cu and k_sgs.cu (momentum predictors, scalar transport, eddy
 viscosity) are written once, in FP64.  This module derives a third build
 from them, namespace les_f32, in which every kernel and device function
 computes in FP32 while the fields stay FP64 in HBM: each load from an FP64
-array is converted on the way in (``LdF``), stores convert back, locals and
+array is converted on the way in (``LdF``, and ``ldcg_f`` for the L2 loads
+of the in-place scalar sweep), stores convert back, locals and
 by-value parameters are ``float``, and floating literals carry an ``f``
 suffix so that no expression is promoted back to FP64.  Host code (the
 launchers) is left as written, so the les_f32 launchers have the same FP64
@@ -67,15 +68,19 @@ def _function_spans(text: str):
     return spans
 
 
-def _params(sig: str) -> str:
+def _params(sig: str):
     """FP64 pointer parameters become converting views (one pointer, the
-    same layout); FP64 scalars become float in device functions but stay
-    double in kernels, whose arguments a cooperative launch passes by
-    address (an FP64 value read as an FP32 parameter would be garbage)."""
+    same layout).  FP64 scalars become float in device functions; in
+    kernels they stay double -- a cooperative launch passes arguments by
+    address, and an FP64 value read as an FP32 parameter is garbage -- under
+    a new name, and the body opens with a float copy under the old one.
+    Returns the signature and that opening."""
     sig = re.sub(r"const\s+double\s*\*\s*(?:__restrict__\s*)?(?=\w)", "LdF ", sig)
-    if sig.lstrip().startswith("__global__"):
-        return sig
-    return re.sub(r"\bdouble\b(?!\s*\*)", "real", sig)
+    if not sig.lstrip().startswith("__global__"):
+        return re.sub(r"\bdouble\b(?!\s*\*)", "real", sig), ""
+    names = re.findall(r"\bdouble\s+(\w+)\s*(?=[,)])", sig)
+    sig = re.sub(r"\bdouble\s+(\w+)\s*(?=[,)])", r"double \1_fp64", sig)
+    return sig, "".join(f" const real {n} = (real){n}_fp64;" for n in names)
 
 
 def _member_reads(body: str) -> str:
@@ -105,7 +110,8 @@ def _local_pointers(body: str) -> str:
 
 def _body(body: str) -> str:
     body = re.sub(r"M\[a\]\[", "LdF(M[a])[", body)
-    body = re.sub(r"A_\.(m|r)\[a\]\[", r"LdF(A_.\1[a])[", body)
+    body = re.sub(r"A_\.(m|r)\[(\w+)\]\[", r"LdF(A_.\1[\2])[", body)
+    body = body.replace("__ldcg(", "ldcg_f(")
     body = _local_pointers(body)
     body = _member_reads(body)
     body = re.sub(r"\bdouble\b(?!\s*\*)", "real", body)
@@ -117,8 +123,10 @@ def transform(text: str, src: str) -> str:
     out, pos = [HEADER.format(src=src)], 0
     for start, brace, end in spans:
         out.append(text[pos:start])
-        out.append(_params(text[start:brace]))
-        out.append(_body(text[brace:end + 1]))
+        sig, opening = _params(text[start:brace])
+        body = _body(text[brace:end + 1])
+        out.append(sig)
+        out.append(body[0] + opening + body[1:])
         pos = end + 1
     out.append(text[pos:])
     return "".join(out)
