@@ -129,7 +129,9 @@ def transform(text: str, src: str) -> str:
         out.append(body[0] + opening + body[1:])
         pos = end + 1
     out.append(text[pos:])
-    return "".join(out)
+    # macros defined between functions and expanded inside them
+    return re.sub(r"^(#define .*)$", lambda m: m.group(1).replace("__ldcg(", "ldcg_f("), "".join(out),
+                  flags=re.M)
 
 
 def generate(csrc: Path, outdir: Path) -> list[Path]:
