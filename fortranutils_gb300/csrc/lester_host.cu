@@ -1265,6 +1265,7 @@ int lester_gpu_init(const lester_geom *g, const lester_ctrl *c)
 {
     lester_gpu_finalize();
     if (!g || !c) return set_err(LES_ERR_ARG, "null geometry or control");
+    if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
     if (g->numbl < 1 || g->numbl > LES_MAXBL) return set_err(LES_ERR_GEOM, "numbl %d out of 1..%d", g->numbl, LES_MAXBL);
     Ctx *ctx = new Ctx();
     ctx->g = *g;
@@ -1290,6 +1291,7 @@ int lester_gpu_set_ctrl(const lester_ctrl *c)
 {
     LES_NEED_CTX();
     if (!c) return set_err(LES_ERR_ARG, "null control");
+    if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
     g_ctx->c = *c;
     return 0;
 }

@@ -142,7 +142,8 @@ typedef struct lester_ctrl {
                           (lester_gpu_tuned); 0 = the controls as given */
     int phys32;        /* 1 = the predictors, scalar transport and eddy
                           viscosity compute in FP32 on the FP64 fields (the
-                          les_f32 build; exact must be 0): the mixed path's
+                          les_f32 build; with exact = 1 lester_gpu_init and
+                          lester_gpu_set_ctrl refuse it): the mixed path's
                           physics, its error against the FP64 path stated
                           per field by the tests */
     int step_graph;    /* 1 = lester_step replays the whole step as one CUDA

@@ -46,3 +46,13 @@ def test_geometry_errors_are_reported(gpulib):
     rc = L.lib().lester_gpu_init(ctypes.byref(g), ctypes.byref(L.default_ctrl()))
     # with no GPU the call may fail on CUDA instead; it must never succeed
     assert rc != 0
+
+
+def test_contradictory_controls_refused(gpulib):
+    """FP32 physics (phys32) with the exact FP64 build is refused, before any
+    device work, by lester_gpu_init and lester_gpu_set_ctrl."""
+    from fortranutils_gb300 import grid, lester as L
+    case = grid.box_case(8, 8, 8)
+    rc = L.lib().lester_gpu_init(ctypes.byref(case.geom()), ctypes.byref(L.default_ctrl(exact=1, phys32=1)))
+    assert rc == -3  # LES_ERR_ARG
+    assert b"phys32" in L.lib().lester_gpu_last_error()
