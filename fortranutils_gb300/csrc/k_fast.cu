@@ -79,6 +79,20 @@ __global__ void k_recip(RecipJob J, long n)
         d[e] = 1.0 / s[e];
 }
 
+// FP32 copies of FP64 tables (the FP32 physics build's metrics)
+struct F32Job {
+    const double *src[24];
+    float *dst[24];
+};
+
+__global__ void k_to_f32(F32Job J, long n)
+{
+    const double *s = J.src[blockIdx.y];
+    float *d = J.dst[blockIdx.y];
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        d[e] = (float)s[e];
+}
+
 __global__ void k_delta_tables(const double *__restrict__ dip, const double *__restrict__ djp,
                                const double *__restrict__ rp, long n2, const double *__restrict__ dkp,
                                long n1, double *__restrict__ d2, double *__restrict__ d1)
@@ -859,6 +873,22 @@ void launch_recip(const double *const *src, double *const *dst, int ntab, long n
         unsigned gx = nb_(n, 256);
         if (gx > 256) gx = 256;
         k_recip<<<dim3(gx, m), 256, 0, st>>>(J, n);
+        count_launch(1);
+    }
+}
+
+void launch_to_f32(const double *const *src, float *const *dst, int ntab, long n, cudaStream_t st)
+{
+    F32Job J;
+    for (int b0 = 0; b0 < ntab; b0 += 24) {
+        int m = ntab - b0 < 24 ? ntab - b0 : 24;
+        for (int t = 0; t < m; t++) {
+            J.src[t] = src[b0 + t];
+            J.dst[t] = dst[b0 + t];
+        }
+        unsigned gx = nb_(n, 256);
+        if (gx > 256) gx = 256;
+        k_to_f32<<<dim3(gx, m), 256, 0, st>>>(J, n);
         count_launch(1);
     }
 }

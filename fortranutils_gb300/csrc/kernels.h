@@ -122,6 +122,7 @@ void launch_vbc_side(const BlkDev *blk, int nb, int iva, int side, unsigned long
 // d2[e] = (dip djp rp)^0.33333333 over n2 entries, d1[e] = dkp^0.33333333
 // over n1 entries.
 void launch_recip(const double *const *src, double *const *dst, int ntab, long n, cudaStream_t st);
+void launch_to_f32(const double *const *src, float *const *dst, int ntab, long n, cudaStream_t st);
 void launch_delta_tables(const double *dip, const double *djp, const double *rp, long n2,
                          const double *dkp, long n1, double *d2, double *d1, cudaStream_t st);
 

@@ -151,6 +151,8 @@ struct Ctx {
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)
     long tabcap = 0, tab_next = 0;
+    float *d_pool32 = nullptr;      // FP32 copies of the tables (phys32), reset per call
+    long cap32 = 0, next32 = 0;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
     // whole-step graph (ctrl.step_graph, lester_step.cu)
     struct StepGraph {
@@ -183,6 +185,14 @@ int graph_cond_handle(Ctx &c, cudaGraphConditionalHandle *h);
 int graph_add_conditional(Ctx &c, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t *body);
 int graph_begin_body(Ctx &c, cudaGraph_t body, cudaStream_t *saved);
 int graph_end_body(Ctx &c, cudaStream_t saved);
+
+// phys32 (the les_f32 build): its read-only tables as FP32 copies, passed
+// as pointers tagged in bit 0 (LdF in phys_variant.h reads them directly).
+// phys32_tables replaces each *pp[t] (length len) by such a copy, refreshed
+// on every call from a pool that phys32_reset rewinds (lester_phys_host.cu)
+inline bool phys32_on(const Ctx &c) { return c.c.phys32 && !c.c.exact; }
+void phys32_reset(Ctx &c);
+int phys32_tables(Ctx &c, int n, const double **const *pp, long len);
 
 extern Ctx *g_ctx;
 extern std::string g_err;

@@ -464,6 +464,7 @@ static void free_ctx(Ctx *c)
     if (c->h_step) cudaFreeHost(c->h_step);
     if (c->h_loop) cudaFreeHost(c->h_loop);
     cudaFree(c->d_step);
+    cudaFree(c->d_pool32);
     cudaFree(c->d_loop);
     if (c->d_tabpool) cudaFree(c->d_tabpool);
     for (void *p : {(void *)c->f32.tab.E2, (void *)c->f32.tab.N2, (void *)c->f32.tab.R2, (void *)c->f32.tab.Ez,
@@ -1828,6 +1829,16 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v
     memset(&F, 0, sizeof F);
     // m: dip, diu, djp, djv, dkp, dkw, hijp, hjip, hkip, hkjp, rp
     if (!c.c.exact && (r = fast_sgs_tabs(c, m[0], m[2], m[10], m[4], m[5], F))) return r;
+    if (phys32_on(c)) {
+        phys32_reset(c);
+        const double **const t2[12] = {&m[0], &m[1], &m[2], &m[3], &m[6], &m[7], &m[8], &m[9], &m[10],
+                                       &F.r_dip, &F.r_djp, &F.r_rp};
+        const double **const t2b[1] = {&F.delta2d};
+        const double **const t1[5] = {&m[4], &m[5], &F.r_dkp, &F.r_dkw, &F.delta1d};
+        if ((r = phys32_tables(c, 12, t2, c.tot2)) || (r = phys32_tables(c, 1, t2b, c.tot2)) ||
+            (r = phys32_tables(c, 5, t1, c.tot1k)))
+            return r;
+    }
     LES_PHYS(c, launch_subgrid)(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, c.c.alpha, dg,
                                 dgs, du, dv,
                                 dw, dsc, dsv, dsd, dvd, m, F, c.stream);

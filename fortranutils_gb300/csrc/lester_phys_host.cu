@@ -86,6 +86,38 @@ namespace les {
 
 void tab_reset(Ctx &c) { c.tab_next = 0; }
 
+void phys32_reset(Ctx &c) { c.next32 = 0; }
+
+int phys32_tables(Ctx &c, int n, const double **const *pp, long len)
+{
+    if (!c.d_pool32) {
+        const long cap = 48 * c.tot2 + 24 * c.tot1k + 256;
+        if (cudaMalloc(&c.d_pool32, sizeof(float) * cap) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(LES_ERR_NOMEM, "FP32 physics tables: %ld floats", cap);
+        }
+        c.cap32 = cap;
+    }
+    const double *src[64];
+    float *dst[64];
+    int m = 0;
+    if (n > 64) return set_err(LES_ERR_ARG, "phys32_tables: %d tables", n);
+    for (int t = 0; t < n; t++) {
+        const double *q = *pp[t];
+        if (!q || ((unsigned long long)q & 1ull)) continue;  // absent, or already a copy
+        const long step = (len + 3) & ~3L;                   // 16-byte aligned copies
+        if (c.next32 + step > c.cap32) return set_err(LES_ERR_SIZE, "FP32 physics tables exhausted");
+        float *d = c.d_pool32 + c.next32;
+        c.next32 += step;
+        src[m] = q;
+        dst[m] = d;
+        m++;
+        *pp[t] = (const double *)((unsigned long long)d | 1ull);
+    }
+    if (m) launch_to_f32(src, dst, m, len, c.stream);
+    return 0;
+}
+
 static int tab_take(Ctx &c, long len, double **p)
 {
     if (!c.d_tabpool) {
@@ -233,6 +265,15 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
         A.r_dkp = o1[0];
         A.r_dkw = o1[1];
     }
+    if (phys32_on(c)) {
+        phys32_reset(c);
+        const double **const t2[28] = {&A.dip, &A.diu, &A.dix, &A.rdix, &A.djp, &A.dju, &A.djv, &A.djx, &A.rdjp,
+                                       &A.rdju, &A.didjp, &A.didju, &A.rdidju, &A.hijp, &A.hiju, &A.hjiu, &A.hkiu,
+                                       &A.hkju, &A.rp, &A.ru, &A.r_dip, &A.r_diu, &A.r_dix, &A.r_djp, &A.r_dju,
+                                       &A.r_djv, &A.r_djx, &A.r_rp};
+        const double **const t1[4] = {&A.dkp, &A.dkw, &A.r_dkp, &A.r_dkw};
+        if ((r = phys32_tables(c, 28, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k))) return r;
+    }
     LES_PHYS(c, launch_set_u_int)(L.d_blk, c.g.numbl, L.maxcell, iv, A, k.dtime, c.iststep, k.visc, k.ylaminar,
                                   k.kappa, k.cwfun, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, A.u_int, c.d_work, c.stream);
@@ -285,6 +326,16 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
         for (int t = 0; t < 5; t++) A.r[qs[t]] = o2[t];
         A.rdkp = o1[0];
         A.rdkw = o1[1];
+    }
+    if (phys32_on(c)) {
+        phys32_reset(c);
+        const double **t2[2 * MW_N];
+        for (int q = 0; q < MW_N; q++) {
+            t2[q] = &A.m[q];
+            t2[MW_N + q] = &A.r[q];
+        }
+        const double **const t1[4] = {&A.dkp, &A.dkw, &A.rdkp, &A.rdkw};
+        if ((r = phys32_tables(c, 2 * MW_N, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k))) return r;
     }
     LES_PHYS(c, launch_set_w_int)(L.d_blk, c.g.numbl, L.maxcell, A, k.dtime, c.iststep, k.visc, k.ylaminar,
                                   k.kappa, k.cwfun, c.stream);
@@ -444,6 +495,16 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
         A.r[MW_RP] = o2[2];
         A.rdkp = o1[0];
     }
+    if (phys32_on(c)) {
+        phys32_reset(c);
+        const double **t2[2 * MW_N];
+        for (int q = 0; q < MW_N; q++) {
+            t2[q] = &A.m[q];
+            t2[MW_N + q] = &A.r[q];
+        }
+        const double **const t1[3] = {&A.dkp, &A.dkw, &A.rdkp};
+        if ((r = phys32_tables(c, 2 * MW_N, t2, c.tot2)) || (r = phys32_tables(c, 3, t1, c.tot1k))) return r;
+    }
     // the whole sweep as one cooperative launch with a grid barrier per
     // plane; per-plane launches where the device cannot co-schedule it
     int smem = (int)sizeof(int) * (c.nslice + 1);
@@ -510,6 +571,15 @@ int lester_set_sc1var(const double *u, const double *v, const double *w, const d
     SgsFast F;
     memset(&F, 0, sizeof F);
     if (!c.c.exact && (r = fast_sgs_tabs(c, ddip, ddjp, drp, ddkp, ddkw, F))) return r;
+    if (phys32_on(c)) {
+        phys32_reset(c);
+        const double **const t2[6] = {&ddip, &ddjp, &drp, &F.r_dip, &F.r_djp, &F.r_rp};
+        const double **const t2b[1] = {&F.delta2d};
+        const double **const t1[5] = {&ddkp, &ddkw, &F.r_dkp, &F.r_dkw, &F.delta1d};
+        if ((r = phys32_tables(c, 6, t2, c.tot2)) || (r = phys32_tables(c, 1, t2b, c.tot2)) ||
+            (r = phys32_tables(c, 5, t1, c.tot1k)))
+            return r;
+    }
     LES_PHYS(c, launch_sc1var)(L.d_blk, c.g.numbl, L.maxcell, ds, dv, ddip, ddjp, drp, ddkp, ddkw, F, c.stream);
     launch_halo(L.d_face, L.nface, L.maxface, dv, c.d_work, c.stream);
     return st.finish();

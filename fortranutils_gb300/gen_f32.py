@@ -30,6 +30,20 @@ HEADER = """// Generated by fortranutils_gb300/gen_f32.py from {src}: the FP32-a
 # struct members that are not FP64 arrays, or are arrays of pointers
 _NOT_FP64 = {"n", "bc", "link", "m", "r", "iststep", "off_ki", "off_jk"}
 _STRUCTS = r"(?:A_|F)"
+# read-only FP64 arrays the kernels offset before indexing (the 1-D z
+# metrics by a block's offset; the scalar in the sweep's L2 loads)
+_OFFSET_READ = ("dkp", "dkw", "r_dkp", "r_dkw", "rdkp", "rdkw", "sc1")
+# metric tables (struct members and kernel parameters): read through LdM,
+# the host passing FP32 copies (phys32_tables); everything else through LdF
+_METRICS = {"dip", "diu", "div", "dix", "djp", "dju", "djv", "djx", "rdip", "rdiv", "rdix", "rdjp", "rdju",
+            "rdjx", "hijp", "hjip", "hkip", "hkjp", "hiju", "hjiu", "hkiu", "hkju", "hijv", "hjiv", "hkiv",
+            "hkjv", "rp", "ru", "rv", "didjp", "rdidjp", "didju", "rdidju", "djdiv", "rdjdiv", "dkp", "dkw",
+            "rdkp", "rdkw", "r_dip", "r_diu", "r_dix", "r_djp", "r_dju", "r_djv", "r_djx", "r_rp", "r_dkp",
+            "r_dkw", "delta2d", "delta1d"}
+
+
+def _view(name: str) -> str:
+    return "LdM" if name in _METRICS else "LdF"
 
 _LITERAL = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])")
 
@@ -75,7 +89,8 @@ def _params(sig: str):
     address, and an FP64 value read as an FP32 parameter is garbage -- under
     a new name, and the body opens with a float copy under the old one.
     Returns the signature and that opening."""
-    sig = re.sub(r"const\s+double\s*\*\s*(?:__restrict__\s*)?(?=\w)", "LdF ", sig)
+    sig = re.sub(r"const\s+double\s*\*\s*(?:__restrict__\s*)?(\w+)", lambda m: _view(m.group(1)) + " " + m.group(1),
+                 sig)
     if not sig.lstrip().startswith("__global__"):
         return re.sub(r"\bdouble\b(?!\s*\*)", "real", sig), ""
     names = re.findall(r"\bdouble\s+(\w+)\s*(?=[,)])", sig)
@@ -93,7 +108,7 @@ def _member_reads(body: str) -> str:
         if re.match(r"\s*=(?!=)", body[close + 1:]):
             continue  # a store
         out.append(body[pos:m.start()])
-        out.append("LdF(" + body[m.start():m.end() - 1] + ")" + body[m.end() - 1:close + 1])
+        out.append(_view(m.group(1)) + "(" + body[m.start():m.end() - 1] + ")" + body[m.end() - 1:close + 1])
         pos = close + 1
     out.append(body[pos:])
     return "".join(out)
@@ -103,14 +118,26 @@ def _local_pointers(body: str) -> str:
     """`const double *a = ..., *b = ...;` -> `const LdF a = ..., b = ...;`"""
     def fix(m):
         stmt = m.group(0)
-        stmt = re.sub(r"^const\s+double\s*\*", "const LdF ", stmt)
-        return re.sub(r",\s*\*(\w+)\s*=", r", \1 =", stmt)
+        # one declarator per initializer: `*name = A_.member ...`
+        parts = re.split(r"(?:^const\s+double\s*\*|,\s*\*)(?=\s*\w+\s*=)", stmt)
+        decls = [p.strip() for p in parts if p.strip()]
+        views = []
+        for d in decls:
+            mm = re.search(r"=\s*(?:Ld[FM]\()?(?:A_|F)\.(\w+)", d)
+            views.append(_view(mm.group(1)) if mm else "LdF")
+        if len(set(views)) == 1:
+            return "const " + views[0] + " " + ", ".join(decls)
+        return " ".join(f"const {v} {d.rstrip(';')};" for v, d in zip(views, decls))
     return re.sub(r"const\s+double\s*\*(?!\s*const)\s*\w+\s*=[^;]*;", fix, body)
 
 
 def _body(body: str) -> str:
-    body = re.sub(r"M\[a\]\[", "LdF(M[a])[", body)
-    body = re.sub(r"A_\.(m|r)\[(\w+)\]\[", r"LdF(A_.\1[\2])[", body)
+    # pointer arithmetic on a member goes through the view (which scales
+    # the offset for an FP32 copy)
+    body = re.sub(_STRUCTS + r"\.(" + "|".join(_OFFSET_READ) + r")(?=\s*\+)",
+                  lambda m: _view(m.group(1)) + "(" + m.group(0) + ")", body)
+    body = re.sub(r"M\[a\]\[", "LdM(M[a])[", body)
+    body = re.sub(r"A_\.(m|r)\[(\w+)\]\[", r"LdM(A_.\1[\2])[", body)
     body = body.replace("__ldcg(", "ldcg_f(")
     body = _local_pointers(body)
     body = _member_reads(body)

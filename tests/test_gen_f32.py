@@ -56,3 +56,20 @@ void host(double d) { double e = d * 0.5; }
     assert "A_.z[n] = t;" in out and "1.e-30f + 2.0f * t" in out
     # host code as written
     assert "void host(double d) { double e = d * 0.5; }" in out
+
+
+def test_metric_tables_read_as_fp32_copies():
+    """Metric tables (the host passes FP32 copies) are read through LdM,
+    fields through LdF -- in members, parameters and local views."""
+    src = """namespace LES_PHYS_NS {
+__global__ void k(const double *__restrict__ u, const double *__restrict__ dip, double s)
+{
+    const double *dkp = A_.dkp + b.off1k, *w = A_.w;
+    double t = u[0] * dip[1] + A_.diu[2] + A_.rho[3] + dkp[4] + w[5] + A_.m[q][6];
+}
+}
+"""
+    out = gen_f32.transform(src, "t.cu")
+    assert "LdF u" in out and "LdM dip" in out
+    assert "const LdM dkp = LdM(A_.dkp) + b.off1k; const LdF w = A_.w;" in out
+    assert "LdM(A_.diu)[2]" in out and "LdF(A_.rho)[3]" in out and "LdM(A_.m[q])[6]" in out
