@@ -357,7 +357,7 @@ def run_e2e(args, case, ctrl, wl="mixing"):
     torch.cuda.empty_cache()
     S.step(h, 1)  # coeff_p at istep 1, as the first step of a run
     L.gpu_sync()
-    k = max(1, min(args.steps, 3))
+    k = max(1, min(args.steps, 10))
     b0 = L.gpu_xfer_bytes()
     t0 = time.perf_counter()
     for it in range(k):
