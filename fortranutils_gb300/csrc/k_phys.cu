@@ -911,10 +911,10 @@ int sc1_sweep_max_ctas(int smem)
         cudaGetLastError();
         return 0;
     }
-    // two CTAs per SM: fewer arrivals per barrier against work per plane
-    // (measured on the 256x192x128 mixing layer: 1, 2, 4 per SM gave 25.8,
-    // 23.7, 24.6 ms per step)
-    return nsm * (per < 2 ? per : 2);
+    // three CTAs per SM: fewer arrivals per barrier against work per plane
+    // (measured on the 256x192x128 mixing layer, FP32 physics: 1, 2, 3 per
+    // SM gave 20.8, 18.7, 18.2 ms per step)
+    return nsm * (per < 3 ? per : 3);
 }
 
 cudaError_t launch_sc1_sweep(const BlkDev *blk, const int *cum, const int2 *slice, int nslice, int nctas,
