@@ -364,9 +364,13 @@ int lester_step(lester_fields *F, const int *istep)
         }
     }
     double **fm[] = {&D.p, &D.s, &D.res, &D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
-    for (double **pp : fm) {
+    for (int q = 0; q < 10; q++) {
+        double **pp = fm[q];
         if (!*pp) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
-        RET(st.io(*pp, nm, pp));
+        // the coefficients are written only by coeff_p at the first step:
+        // host arrays are not copied back after the others
+        if (q >= 3 && *istep != 1) RET(st.in(*pp, nm, (const double **)pp));
+        else RET(st.io(*pp, nm, pp));
     }
     for (int q = 0; q < 35; q++) {
         if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
