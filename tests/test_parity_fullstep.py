@@ -144,19 +144,25 @@ GRAPH_VARIANTS = {
 
 
 GRAPH_CASES = [(v, k) for v in GRAPH_VARIANTS for k in (0, 1, 2) if not (v == "stall" and k == 0)]
+# the benchmarked path: FP32 physics (les_f32) replayed from the graph
+GRAPH_F32 = dict(exact=0, phys32=1)
 
 
 # (the stall variant diverges with plain defect correction, krylov 0)
+@pytest.mark.parametrize("physics", ["fp64", "f32"])
 @pytest.mark.parametrize("variant,krylov", GRAPH_CASES)
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
 @pytest.mark.parametrize("name", list(SETUPS))
-def test_step_graph_replays_bitwise(name, psolve, krylov, variant, gpulib):
+def test_step_graph_replays_bitwise(name, psolve, krylov, variant, physics, gpulib):
     """ctrl.step_graph: steps 2..5 replayed from one captured graph (the
     solve's cycle loop a device-side WHILE node, the rest of the step behind
     an IF node) give the fields of the steps launched call by call, bit for
     bit, and the same return codes."""
+    if physics == "f32" and (psolve != L.PSOLVE_MIXED or variant == "max_outer"):
+        pytest.skip("FP32 physics: with the mixed solver, converged and stalling solves")
     n = 5
-    st, ctrl, s = make(name, psolve=psolve, krylov=krylov, **GRAPH_VARIANTS[variant])
+    extra = GRAPH_F32 if physics == "f32" else {}
+    st, ctrl, s = make(name, psolve=psolve, krylov=krylov, **GRAPH_VARIANTS[variant], **extra)
     plain, rc0 = gpu_steps(st, ctrl, s, n)
     ctrl.step_graph = 1
     g = s.to("torch")
