@@ -214,3 +214,37 @@ def test_phys32_error_per_field(name, gpulib):
     for n, tol in PHYS32_TOL.items():
         assert errs[n] <= tol, (n, errs[n], tol)
     assert rel(got["u"], s["u"]) > 1e-6  # the step did work
+
+
+def test_step_graph_recaptures_on_new_fields_and_controls(gpulib):
+    """The graph is captured per field set and controls: moving the state to
+    new device arrays, then changing dtime, gives new captures, and the run
+    stays bit for bit the launched one."""
+    def run(graph):
+        st, ctrl, s = make("box_wall", psolve=L.PSOLVE_MIXED, rtol=1e-9, exact=0, phys32=1)
+        ctrl.step_graph = graph
+        g = s.to("torch")
+        L.gpu_init(st.case.geom(), ctrl)
+        try:
+            for it in (1, 2, 3):
+                assert S.step(g, it) == 0
+            g = g.to("numpy").to("torch")  # the same state in new arrays
+            for it in (4, 5):
+                assert S.step(g, it) == 0
+            ctrl.dtime = 1.5e-3
+            L.gpu_set_ctrl(ctrl)
+            for it in (6, 7):
+                assert S.step(g, it) == 0
+            info = L.gpu_step_graph_info()
+            L.gpu_sync()
+            return g.to("numpy"), info
+        finally:
+            L.gpu_finalize()
+
+    plain, _ = run(0)
+    got, info = run(1)
+    # step 4, the first on the new arrays, runs as launched (it converts the
+    # new coefficient arrays for the fast solver); captures at 2, 5 and 6
+    assert not info["failed"] and info["replays"] == 5, info
+    for f in S.STATE:
+        assert np.array_equal(got[f], plain[f]), f
