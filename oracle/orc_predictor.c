@@ -203,7 +203,7 @@ static void set_u_int_block(int nip1, int njp1, int nkp1, long io, long jo, long
 
 /* code/set_uv_int.F:63-160.  iva = 1 (u) or 2 (v).  metric[] holds the 35
  * comp_metric arrays (each tot2 long) in comp_metric order.  tw[4] are the
- * wall-stress arrays the driver passes for this component: for u
+ * wall-stress arrays the calling routine passes for this component: for u
  * tw_sfi, tw_nfi (ki layout), tw_lfi, tw_rfi (ij layout); for v tw_wfj,
  * tw_efj (jk layout), tw_lfj, tw_rfj. */
 void orc_set_uv_int(orc_ctx *c, int iva, double dtime, int iststep, double visc,
