@@ -91,7 +91,7 @@ void phys32_reset(Ctx &c) { c.next32 = 0; }
 int phys32_tables(Ctx &c, int n, const double **const *pp, long len)
 {
     if (!c.d_pool32) {
-        const long cap = 48 * c.tot2 + 24 * c.tot1k + 256;
+        const long cap = 48 * c.tot2 + 24 * c.tot1k + 7 * (c.tot_sg3 + 4) + 256;
         if (cudaMalloc(&c.d_pool32, sizeof(float) * cap) != cudaSuccess) {
             cudaGetLastError();
             return set_err(LES_ERR_NOMEM, "FP32 physics tables: %ld floats", cap);
@@ -272,7 +272,10 @@ int lester_set_uv_int(const int *iva, const double *u, const double *v, const do
                                        &A.hkju, &A.rp, &A.ru, &A.r_dip, &A.r_diu, &A.r_dix, &A.r_djp, &A.r_dju,
                                        &A.r_djv, &A.r_djx, &A.r_rp};
         const double **const t1[4] = {&A.dkp, &A.dkw, &A.r_dkp, &A.r_dkw};
-        if ((r = phys32_tables(c, 28, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k))) return r;
+        const double **const t3[7] = {&A.u, &A.v, &A.w, &A.p, &A.rho, &A.rhonp1, &A.gam};
+        if ((r = phys32_tables(c, 28, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k)) ||
+            (r = phys32_tables(c, 7, t3, c.tot_sg3)))
+            return r;
     }
     LES_PHYS(c, launch_set_u_int)(L.d_blk, c.g.numbl, L.maxcell, iv, A, k.dtime, c.iststep, k.visc, k.ylaminar,
                                   k.kappa, k.cwfun, c.stream);
@@ -335,7 +338,10 @@ int lester_set_w_int(const double *u, const double *v, const double *w, const do
             t2[MW_N + q] = &A.r[q];
         }
         const double **const t1[4] = {&A.dkp, &A.dkw, &A.rdkp, &A.rdkw};
-        if ((r = phys32_tables(c, 2 * MW_N, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k))) return r;
+        const double **const t3[7] = {&A.u, &A.v, &A.w, &A.p, &A.rho, &A.rhonp1, &A.gam};
+        if ((r = phys32_tables(c, 2 * MW_N, t2, c.tot2)) || (r = phys32_tables(c, 4, t1, c.tot1k)) ||
+            (r = phys32_tables(c, 7, t3, c.tot_sg3)))
+            return r;
     }
     LES_PHYS(c, launch_set_w_int)(L.d_blk, c.g.numbl, L.maxcell, A, k.dtime, c.iststep, k.visc, k.ylaminar,
                                   k.kappa, k.cwfun, c.stream);

@@ -42,8 +42,15 @@ _METRICS = {"dip", "diu", "div", "dix", "djp", "dju", "djv", "djx", "rdip", "rdi
             "r_dkw", "delta2d", "delta1d"}
 
 
+# fields that particular kernels read as FP32 copies too (the host converts
+# them once per call: each is read by ~7 neighbouring points)
+_FIELDS32 = {"k_set_u_int": {"u", "v", "w", "p", "rho", "rhonp1", "gam"},
+             "k_set_w_int": {"u", "v", "w", "p", "rho", "rhonp1", "gam"}}
+_func = ""
+
+
 def _view(name: str) -> str:
-    return "LdM" if name in _METRICS else "LdF"
+    return "LdM" if name in _METRICS or name in _FIELDS32.get(_func, ()) else "LdF"
 
 _LITERAL = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])")
 
@@ -148,13 +155,16 @@ def _body(body: str) -> str:
 def transform(text: str, src: str) -> str:
     spans = _function_spans(text)
     out, pos = [HEADER.format(src=src)], 0
+    global _func
     for start, brace, end in spans:
         out.append(text[pos:start])
+        _func = [n for n in re.findall(r"(\w+)\s*\(", text[start:brace]) if not n.startswith("__")][0]
         sig, opening = _params(text[start:brace])
         body = _body(text[brace:end + 1])
         out.append(sig)
         out.append(body[0] + opening + body[1:])
         pos = end + 1
+    _func = ""
     out.append(text[pos:])
     # macros defined between functions and expanded inside them
     return re.sub(r"^(#define .*)$", lambda m: m.group(1).replace("__ldcg(", "ldcg_f("), "".join(out),
