@@ -86,6 +86,48 @@ def dist_env():
     return rank, world, local
 
 
+class Ranks:
+    """The processes of a torchrun launch, one replica of the step per GPU
+    with no exchange on the data path: a host-side gloo group that starts and
+    ends every timed region together (barrier) and takes the slowest rank's
+    time (max).  One process: every call is a no-op."""
+
+    def __init__(self):
+        self.rank, self.world, self.local = dist_env()
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+RANKS = None  # set by main(); run_gpu's callers outside main get one process
+
+
+def _ranks() -> Ranks:
+    global RANKS
+    if RANKS is None:
+        RANKS = Ranks()
+    return RANKS
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -271,6 +313,7 @@ def run_gpu(args):
         L.gpu_prof(True)
         with ClockSampler(0) as clk:
             torch.cuda.synchronize()
+            _ranks().barrier()
             e0.record(stream)
             for _ in range(args.steps):
                 istep += 1
@@ -283,9 +326,10 @@ def run_gpu(args):
                     raise RuntimeError(f"{mode} solver did not reach 1e-8: {st}")
             e1.record(stream)
             torch.cuda.synchronize()
+            _ranks().barrier()
         L.gpu_prof(False)
         tuned = L.gpu_tuned(32 if mode == "mixed" else 64)
-        ms = e0.elapsed_time(e1)
+        ms = _ranks().max(e0.elapsed_time(e1))
         kms, kl = L.gpu_prof_read()
         res[mode] = {"ms_per_step": ms / args.steps, "cycles": float(np.mean(cyc)),
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
@@ -325,6 +369,7 @@ def run_graph_leg(args, case, ctrl, wl):
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
+        _ranks().barrier()
         e0.record(stream)
         for _ in range(args.steps):
             istep += 1
@@ -335,13 +380,14 @@ def run_graph_leg(args, case, ctrl, wl):
                 raise RuntimeError(f"graph step: solver did not reach 1e-8: {st}")
         e1.record(stream)
         torch.cuda.synchronize()
+        _ranks().barrier()
     info = L.gpu_step_graph_info()
     ctrl.step_graph = 0
     L.gpu_set_ctrl(ctrl)
     del g
     if info["failed"] or info["replays"] - info0["replays"] != args.steps:
         raise RuntimeError(f"whole-step graph not replayed: {info}")
-    return {"ms_per_step": e0.elapsed_time(e1) / args.steps, "cycles": float(np.mean(cyc)),
+    return {"ms_per_step": _ranks().max(e0.elapsed_time(e1)) / args.steps, "cycles": float(np.mean(cyc)),
             "launches": L.gpu_launch_count() - launches0, "clocks": clk.summary(),
             "handovers": info["handovers"] - info0["handovers"]}
 
@@ -359,11 +405,13 @@ def run_e2e(args, case, ctrl, wl="mixing"):
     L.gpu_sync()
     k = max(1, min(args.steps, 10))
     b0 = L.gpu_xfer_bytes()
+    _ranks().barrier()
     t0 = time.perf_counter()
     for it in range(k):
         S.step(h, 2 + it)
     L.gpu_sync()
-    dt = (time.perf_counter() - t0) / k
+    dt = _ranks().max(time.perf_counter() - t0) / k
+    _ranks().barrier()
     b1 = L.gpu_xfer_bytes()
     return {"s_per_step": dt, "steps": k, "h2d_bytes_per_step": (b1[0] - b0[0]) // k,
             "d2h_bytes_per_step": (b1[1] - b0[1]) // k}
@@ -527,6 +575,8 @@ def main():
         if rank == 0:
             run_poisson(args)
         return
+    global RANKS
+    RANKS = Ranks()
     case, res = run_gpu(args)
     ncell = case.cells()
     wl = args.workload
@@ -619,6 +669,7 @@ def main():
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
+    RANKS.close()
 
 
 if __name__ == "__main__":
