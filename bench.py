@@ -46,9 +46,18 @@ DOMAIN = (30.0, 30.0, 15.0)
 EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
-# DRAM bytes of one level-1 k_rb<float> launch of the mixing-layer workload
-# (ncu: 52.0 MB read + 0.27 MB written), against 37.7 MB algorithmic
-RB_TRAFFIC = 52.28e6
+# DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per launch
+# of the timed kernels on the mixing-layer workload, from one capture each:
+# the level-1 k_rb<float> half sweep (52.0 MB read + 0.27 MB written,
+# against 37.7 MB algorithmic) and the scalar sweep (not captured: None)
+TRAFFIC = {"rb": 52.28e6, "sweep": None}
+# algorithmic bytes per interior cell of one launch: the red-black half
+# sweep reads x and b and writes x in FP32, one colour per launch (12 / 2);
+# the scalar sweep reads sc1, hsc1, u, v, w, rho, gamsc1, gamlam and writes
+# sc1, hsc1 (10 FP64 arrays)
+ALG_BYTES = {"rb": 6.0, "sweep": 80.0}
+KERNEL_NAMES = {"rb": "k_rb<float> level-1 red-black SOR half sweep",
+                "sweep": "set_sc1 in-place scalar sweep (one launch per step)"}
 # other workloads (--workload): the plain channel of the reference's own
 # CPU-runnable case, and the large stretched channel
 WORKLOADS = {
@@ -96,8 +105,11 @@ class Ranks:
         self.rank, self.world, self.local = dist_env()
         self.dist = None
         if self.world > 1:
+            import datetime
             import torch.distributed as dist
-            dist.init_process_group("gloo")
+            # a rank that fails inside a timed region releases the others
+            # within minutes, not after gloo's default 30
+            dist.init_process_group("gloo", timeout=datetime.timedelta(minutes=2))
             self.dist = dist
 
     def barrier(self):
@@ -114,11 +126,32 @@ class Ranks:
 
     def close(self):
         if self.dist is not None:
-            self.dist.destroy_process_group()
-            self.dist = None
+            try:
+                self.dist.destroy_process_group()
+            finally:
+                self.dist = None
 
 
 RANKS = None  # set by main(); run_gpu's callers outside main get one process
+GPU_INDEX = 0  # physical index of this process's GPU (nvidia-smi -i)
+
+
+def pick_gpu(local: int, world: int) -> int:
+    """The physical GPU of this rank: the local-rank entry of an existing
+    CUDA_VISIBLE_DEVICES list (the launcher's choice), else the local rank;
+    CUDA_VISIBLE_DEVICES is then narrowed to that one GPU."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if vis:
+        ids = [v.strip() for v in vis.split(",") if v.strip()]
+        phys = ids[local % len(ids)] if world > 1 else ids[0]
+    else:
+        phys = str(local)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = phys
+    try:
+        return int(phys)
+    except ValueError:  # a UUID: nvidia-smi -i accepts it too
+        return phys
 
 
 def _ranks() -> Ranks:
@@ -311,7 +344,7 @@ def run_gpu(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         L.gpu_prof(True)
-        with ClockSampler(0) as clk:
+        with ClockSampler(GPU_INDEX) as clk:
             torch.cuda.synchronize()
             _ranks().barrier()
             e0.record(stream)
@@ -330,11 +363,13 @@ def run_gpu(args):
         L.gpu_prof(False)
         tuned = L.gpu_tuned(32 if mode == "mixed" else 64)
         ms = _ranks().max(e0.elapsed_time(e1))
-        kms, kl = L.gpu_prof_read()
+        kms, kl = L.gpu_prof_read(L.PROF_RB)
+        sms, sl = L.gpu_prof_read(L.PROF_SWEEP)
         res[mode] = {"ms_per_step": ms / args.steps, "cycles": float(np.mean(cyc)),
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
                      "launches": L.gpu_launch_count() - launches0, "rb_ms": kms,
-                     "rb_launches": kl, "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
+                     "rb_launches": kl, "sweep_ms": sms, "sweep_launches": sl,
+                     "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
         del g
         if args.step_graph and not WORKLOADS[wl].get("inflow"):
             res[mode]["graph"] = run_graph_leg(args, case, ctrl, wl)
@@ -367,7 +402,7 @@ def run_graph_leg(args, case, ctrl, wl):
     launches0 = L.gpu_launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with ClockSampler(GPU_INDEX) as clk:
         torch.cuda.synchronize()
         _ranks().barrier()
         e0.record(stream)
@@ -510,17 +545,18 @@ def run_poisson(args):
 
 
 def reference_line(args, rank):
-    """--impl reference: the oracle (the reference's algorithm on the CPU)."""
+    """--impl reference: the oracle (the reference's algorithm on the CPU),
+    the same --steps and --warmup as the GPU arm."""
     if rank != 0:
         return
     case = make_case()
-    n = max(1, min(args.steps, 2))
-    sps, nmg = run_cpu_steps(case, n, warmup=min(args.warmup, 1))
+    n, w = max(1, args.steps), max(0, args.warmup)
+    sps, nmg = run_cpu_steps(case, n, warmup=w)
     val = case.cells() / sps / 1e6
-    sample = (f"{n} full steps of the 256x192x128 workload after {min(args.warmup, 1)} warm-up, "
+    sample = (f"{n} full steps of the 256x192x128 workload after {w} warm-up, "
               f"reference solver settings ({nmg} V-cycles per step)")
     line = {"metric": METRIC, "value": val, "unit": "Mcell-steps/s", "impl": "reference",
-            "n_gpus": args.gpus, "steps": n, "warmup": min(args.warmup, 1),
+            "n_gpus": args.gpus, "steps": n, "warmup": w,
             "ms_per_step": 1e3 * sps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy default_rng)",
             "config": {"workload": WORKLOAD, "cells": case.cells()},
@@ -565,9 +601,9 @@ def main():
     if args.shape is None:
         args.shape = list(WORKLOADS[args.workload]["shape"])
     rank, world, local = dist_env()
-    if world > 1:
-        # the path runs on one GPU; extra ranks are independent replicas
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    # the path runs on one GPU; extra ranks are independent replicas
+    global GPU_INDEX
+    GPU_INDEX = pick_gpu(local, world)
     if args.impl == "reference":
         reference_line(args, rank)
         return
@@ -577,6 +613,13 @@ def main():
         return
     global RANKS
     RANKS = Ranks()
+    try:
+        report(args, rank, world)
+    finally:
+        RANKS.close()
+
+
+def report(args, rank, world):
     case, res = run_gpu(args)
     ncell = case.cells()
     wl = args.workload
@@ -603,10 +646,24 @@ def main():
     peak = peaks.get("hbm_gbs")
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    # dominant kernel: the level-1 FP32 red-black smoother, one colour per
-    # launch: 12 B/cell per sweep (read f, b; write f) / 2 = 6 B x cells
-    rb_avg_ms = mx["rb_ms"] / max(mx["rb_launches"], 1)
-    achieved = 6.0 * ncell / (rb_avg_ms * 1e-3) / 1e9
+    # roofline of the two timed kernels (CUDA events around every launch in
+    # the launched leg's timed region): algorithmic bytes per launch over the
+    # average launch time; the headline entry is the one with more time
+    kern = {}
+    for key, ms_k, n_k in (("rb", mx["rb_ms"], mx["rb_launches"]),
+                           ("sweep", mx["sweep_ms"], mx["sweep_launches"])):
+        if n_k <= 0:
+            continue
+        avg = ms_k / n_k
+        ach = ALG_BYTES[key] * ncell / (avg * 1e-3) / 1e9
+        kern[key] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": TRAFFIC[key] if wl == "mixing" else None,
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                                        "on this workload" if TRAFFIC[key] and wl == "mixing" else None),
+                     "peak_source": peak_src, "kernel": KERNEL_NAMES[key], "avg_launch_ms": avg,
+                     "launches": n_k, "total_ms": ms_k,
+                     "share_of_timed_steps": ms_k / (mx["ms_per_step"] * args.steps)}
+    dominant = max(kern, key=lambda k: kern[k]["total_ms"])
     sweeps = mx["tuned"]["rb_sweeps"] if mx["tuned"]["done"] else mx["ctrl"].rb_sweeps
     # outer iterations counted as defect correction unless flexible CG ran
     kry = 1 if args.outer == "fcg" else 0
@@ -649,13 +706,8 @@ def main():
                  "relres_max": fp["relres_max"]},
         "speedup_mixed_vs_fp64": fp_ms / mx_ms,
         "solve_speedup_mixed_vs_fp64": fp["solve_ms"] / mx["solve_ms"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": RB_TRAFFIC if wl == "mixing" else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one level-1 "
-                                       "launch, profiles/k_rb_float_level1_256x192x128.md",
-                     "peak_source": peak_src,
-                     "kernel": "k_rb<float> level-1 red-black SOR half sweep",
-                     "avg_launch_ms": rb_avg_ms},
+        "roofline": kern[dominant],
+        "roofline_kernels": kern,
         "step_roofline": {"mixed_gbs": step_gbs["mixed"], "fp64_gbs": step_gbs["fp64"],
                           "mixed_frac": step_gbs["mixed"] / peak,
                           "fp64_frac": step_gbs["fp64"] / peak},
@@ -669,7 +721,6 @@ def main():
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line), flush=True)
-    RANKS.close()
 
 
 if __name__ == "__main__":

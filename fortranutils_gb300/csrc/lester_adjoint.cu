@@ -400,7 +400,7 @@ void zero_wall_ghosts(Ctx &c, double *a)
     }
     unsigned gx = (unsigned)((m + 255) / 256);
     k_zero_wall_ghosts<<<dim3(gx, c.g.numbl, 6), 256, 0, c.stream>>>(L.d_blk, a);
-    c.prof_launches++;
+    count_launch(1);
 }
 
 constexpr int kSlotsU = 19, kSlotsW = 19;  // inputs of the u/v and w predictors (k_adjoint.cu)
@@ -508,7 +508,7 @@ int adjoint_step(Ctx &c, const lester_fields &W, const lester_fields &B, Adj &A,
             launch_sgs_lin(L.d_blk, nb, L.maxcell, 1, q, base, none, bar, A.gamb, nullptr, m[M_DIP], m[M_DJP],
                            W.dkp, m[M_HIJP], m[M_HJIP], A.S.vdd, k.csles, c.stream);
         k_zero_interior<<<dim3((unsigned)((L.maxcell + 255) / 256), nb), 256, 0, c.stream>>>(L.d_blk, A.gamb);
-        c.prof_launches++;
+        count_launch(1);
         zero_wall_ghosts(c, A.gamb);
         vbc_lin(c, B, 1, A.ub, A.wb);
     }

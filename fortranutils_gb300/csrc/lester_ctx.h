@@ -114,12 +114,14 @@ struct Ctx {
     std::vector<void *> stage_buf;
     std::vector<size_t> stage_cap;
     // kernel timing inside a timed region (lester_gpu_prof): CUDA events
-    // around every launch of the level-1 smoother of the fast solvers
+    // around every launch of the timed kernels (LES_PROF_*): pairs in
+    // ev_pool, the kernel of pair q in ev_tag[q]
     bool prof = false;
     std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_tag;
     size_t ev_used = 0;
-    long prof_launches = 0;
-    double prof_ms_acc = 0;
+    long prof_launches[2] = {0, 0};
+    double prof_ms_acc[2] = {0, 0};
     // graphs of the fast solvers: [FP64, mixed][defect correction, flexible CG]
     CycleGraph cg[2][2];
     cudaStream_t cap_stream = nullptr;
@@ -208,6 +210,13 @@ int fast_sgs_tabs(Ctx &c, const double *dip, const double *djp, const double *rp
                   const double *dkw, SgsFast &F);
 // the exact (bitwise) or fast build of the physics launchers
 #define LES_PHYS(c, fn) ((c).c.exact ? les_exact::fn : (c).c.phys32 ? les_f32::fn : les_fast::fn)
+
+// a pair of timing events for one launch of kernel `tag` (LES_PROF_*),
+// used when c.prof is on and nothing is being captured
+void prof_pair(Ctx &c, int tag, cudaEvent_t *e0, cudaEvent_t *e1);
+
+// polls a bounded device wait makes before it gives up (ctrl.wait_limit)
+inline long wait_polls(const Ctx &c) { return c.c.wait_limit > 0 ? (long)c.c.wait_limit : (1L << 24); }
 
 #define LES_CUDA(call)                                                                             \
     do {                                                                                           \

@@ -696,14 +696,19 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
     return 0;
 }
 
-static cudaEvent_t prof_event(Ctx &c)
+// a pair of timing events for one launch of kernel `tag` (LES_PROF_*)
+void prof_pair(Ctx &c, int tag, cudaEvent_t *e0, cudaEvent_t *e1)
 {
-    if (c.ev_used == c.ev_pool.size()) {
+    while (c.ev_used + 2 > c.ev_pool.size()) {
         cudaEvent_t e;
         cudaEventCreate(&e);
         c.ev_pool.push_back(e);
     }
-    return c.ev_pool[c.ev_used++];
+    c.ev_tag.resize(c.ev_pool.size() / 2);
+    c.ev_tag[c.ev_used / 2] = tag;
+    *e0 = c.ev_pool[c.ev_used++];
+    *e1 = c.ev_pool[c.ev_used++];
+    c.prof_launches[tag]++;
 }
 
 template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
@@ -733,9 +738,7 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
                 c.cap_ev->push_back(e0);
                 c.cap_ev->push_back(e1);
             } else if (prof) {
-                e0 = prof_event(c);
-                e1 = prof_event(c);
-                c.prof_launches++;
+                prof_pair(c, LES_PROF_RB, &e0, &e1);
             }
             // inside a capture only an external record becomes an event
             // node whose timestamps can be read after each replay
@@ -1065,8 +1068,8 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
             for (size_t q = 0; q + 1 < G.ev.size(); q += 2) {
                 float ms = 0;
                 LES_CUDA(cudaEventElapsedTime(&ms, G.ev[q], G.ev[q + 1]));
-                c.prof_ms_acc += ms;
-                c.prof_launches++;
+                c.prof_ms_acc[LES_PROF_RB] += ms;
+                c.prof_launches[LES_PROF_RB]++;
             }
         r2 = c.h_small[0];
         rel = std::sqrt(r2 / b2);
@@ -1262,11 +1265,20 @@ int lester_gpu_finalize(void)
     return 0;
 }
 
+// controls refused by lester_gpu_init and lester_gpu_set_ctrl
+static int check_ctrl(const lester_ctrl *c)
+{
+    if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
+    if (c->sc1_sweep < 0 || c->sc1_sweep > 3) return set_err(LES_ERR_ARG, "sc1_sweep %d out of 0..3", c->sc1_sweep);
+    if (c->wait_limit < 0) return set_err(LES_ERR_ARG, "wait_limit %d < 0", c->wait_limit);
+    return 0;
+}
+
 int lester_gpu_init(const lester_geom *g, const lester_ctrl *c)
 {
     lester_gpu_finalize();
     if (!g || !c) return set_err(LES_ERR_ARG, "null geometry or control");
-    if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
+    if (int rc = check_ctrl(c)) return rc;
     if (g->numbl < 1 || g->numbl > LES_MAXBL) return set_err(LES_ERR_GEOM, "numbl %d out of 1..%d", g->numbl, LES_MAXBL);
     Ctx *ctx = new Ctx();
     ctx->g = *g;
@@ -1292,7 +1304,7 @@ int lester_gpu_set_ctrl(const lester_ctrl *c)
 {
     LES_NEED_CTX();
     if (!c) return set_err(LES_ERR_ARG, "null control");
-    if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
+    if (int rc = check_ctrl(c)) return rc;
     g_ctx->c = *c;
     return 0;
 }
@@ -1348,33 +1360,43 @@ int lester_gpu_set_stream(void *s)
 }
 
 // Kernel timing over a timed region: lester_gpu_prof(1) clears and starts,
-// lester_gpu_prof(0) stops; lester_gpu_prof_read sums the event pairs.
+// lester_gpu_prof(0) stops; lester_gpu_prof_kernel sums the event pairs of
+// one kernel.
 int lester_gpu_prof(int enable)
 {
     LES_NEED_CTX();
     g_ctx->prof = enable != 0;
     if (enable) {
         g_ctx->ev_used = 0;
-        g_ctx->prof_launches = 0;
-        g_ctx->prof_ms_acc = 0;
+        for (int q = 0; q < 2; q++) {
+            g_ctx->prof_launches[q] = 0;
+            g_ctx->prof_ms_acc[q] = 0;
+        }
     }
     return 0;
 }
 
-int lester_gpu_prof_read(double *ms_total, long *launches)
+int lester_gpu_prof_kernel(int which, double *ms_total, long *launches)
 {
     LES_NEED_CTX();
+    if (which < 0 || which > 1) return set_err(LES_ERR_ARG, "prof kernel %d out of 0..1", which);
     Ctx &c = *g_ctx;
     LES_CUDA(cudaStreamSynchronize(c.stream));
-    double tot = c.prof_ms_acc;  // graph replays, summed after each replay
+    double tot = c.prof_ms_acc[which];  // graph replays, summed after each replay
     for (size_t q = 0; q + 1 < c.ev_used; q += 2) {
+        if (c.ev_tag[q / 2] != which) continue;
         float ms = 0;
         LES_CUDA(cudaEventElapsedTime(&ms, c.ev_pool[q], c.ev_pool[q + 1]));
         tot += ms;
     }
     *ms_total = tot;
-    *launches = c.prof_launches;
+    *launches = c.prof_launches[which];
     return 0;
+}
+
+int lester_gpu_prof_read(double *ms_total, long *launches)
+{
+    return lester_gpu_prof_kernel(LES_PROF_RB, ms_total, launches);
 }
 
 int lester_gpu_xfer_bytes(long *h2d, long *d2h)

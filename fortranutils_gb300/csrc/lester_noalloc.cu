@@ -1,13 +1,13 @@
 // lester_noalloc.cu -- lester_norms_noalloc: the residual and norms of one
 // block of the pressure system with no device allocation at all.
 //
-// Who needs it: a host that must not allocate device memory at the point
-// of the call -- code running inside a CUDA stream capture (cudaMalloc and
-// cudaFree are not permitted there), a real-time loop with a fixed memory
-// budget, or a host that owns all device memory through its own pool and
-// forbids allocations by libraries.  lester_norms needs lester_gpu_init,
-// which allocates the library's tables and its reduction scratch; this
-// variant needs neither.
+// Who needs it: a host that must not allocate device memory when it calls
+// this routine -- a solver embedded in a larger code that runs under a
+// fixed device-memory budget, or one that owns all device memory through
+// its own pool and forbids libraries to allocate behind its back, or a
+// host that wants the norms of a block before (or without) setting up the
+// library.  lester_norms needs lester_gpu_init, which allocates the
+// library's tables and its reduction scratch; this variant needs neither.
 //
 // Its scratch is a file-scope static device array of fixed size: one slot
 // of 4 partial sums per 256-point CTA plus 8 result slots.  The largest
@@ -18,14 +18,19 @@
 // a device: calls whose work overlaps on the GPU (two streams, or two host
 // threads) race on it and must be serialised by the caller.
 //
-// The device address of the scratch is looked up once per device with
-// cudaGetSymbolAddress, with that device current, on the first call made
-// while it is current.  That first call should come before any stream
-// capture is begun.
+// The call returns the four norms in host scalars: it queues its two
+// kernels on `stream`, copies the 4 results back and waits for the stream.
+//
+// The device address of the scratch is looked up with cudaGetSymbolAddress,
+// with the device current, on the first call in each CUDA context of a
+// device (a cudaDeviceReset makes a new context, so the next call looks it
+// up again).  That first call should come before any stream capture is
+// begun.  Every array must be device memory of the current device.
 //
 // The arithmetic is that of k_norms / k_norms_final (FP64, no FMA
 // contraction, same reduction order), so the results equal lester_norms on
-// the same single-block input.
+// the same single-block input bit for bit.
+#include <cuda.h>
 #include <mutex>
 
 #include "k_common.cuh"
@@ -88,31 +93,63 @@ __global__ void k_norms_noalloc_final(const double *__restrict__ partial, long n
 
 constexpr int kMaxDev = 64;
 std::mutex g_setup_mu;
-double *g_scratch_dev[kMaxDev] = {};
+// per device: the context the address was looked up in, and the address
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double *ptr;
+};
+ScratchSlot g_scratch_dev[kMaxDev] = {};
 
-// device address of the scratch on the current device (first call per
-// device looks it up)
-int scratch_address(double **out)
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+// unique id of the current CUDA context (ids are never reused, so a
+// context made by cudaDeviceReset has a new one); driver entry points are
+// fetched through the runtime, so the library needs no libcuda link
+int current_context_id(unsigned long long *id)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return les::set_err(LES_ERR_CUDA, "lester_norms_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            cudaGetLastError();
+            return les::set_err(LES_ERR_CUDA, "lester_norms_noalloc: driver context queries unavailable");
+        }
+        g_ctx_get_current = (PfnCtxGetCurrent)f1;
+        g_ctx_get_id = (PfnCtxGetId)f2;
     }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx || g_ctx_get_id(ctx, id) != CUDA_SUCCESS)
+        return les::set_err(LES_ERR_CUDA, "lester_norms_noalloc: no current CUDA context");
+    return 0;
+}
+
+// device address of the scratch on the current device and context (the
+// first call in each context looks it up)
+int scratch_address(int dev, double **out)
+{
     if (dev < 0 || dev >= kMaxDev) return les::set_err(LES_ERR_ARG, "lester_norms_noalloc: device %d out of range", dev);
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_dev[dev]) {
+    unsigned long long id = 0;
+    int r = current_context_id(&id);
+    if (r) return r;
+    ScratchSlot &s = g_scratch_dev[dev];
+    if (!s.ptr || s.ctx_id != id) {
         double *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
         if (e != cudaSuccess) {
             cudaGetLastError();
             return les::set_err(LES_ERR_CUDA, "lester_norms_noalloc: cudaGetSymbolAddress: %s",
                                 cudaGetErrorString(e));
         }
-        g_scratch_dev[dev] = p;
+        s.ptr = p;
+        s.ctx_id = id;
     }
-    *out = g_scratch_dev[dev];
+    *out = s.ptr;
     return 0;
 }
 
@@ -140,6 +177,12 @@ extern "C" int lester_norms_noalloc(const int *nijkp1, const double *ap, const d
         if (!p) return set_err(LES_ERR_ARG, "lester_norms_noalloc: NULL array");
     if (!res_norm || !rhs_norm || !err_norm || !var_norm)
         return set_err(LES_ERR_ARG, "lester_norms_noalloc: NULL norm output");
+    int dev = 0;
+    cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(LES_ERR_CUDA, "lester_norms_noalloc: cudaGetDevice: %s", cudaGetErrorString(de));
+    }
     for (const double *p : ptr) {
         cudaPointerAttributes at;
         cudaError_t e = cudaPointerGetAttributes(&at, p);
@@ -147,9 +190,12 @@ extern "C" int lester_norms_noalloc(const int *nijkp1, const double *ap, const d
             cudaGetLastError();
             return set_err(LES_ERR_ARG, "lester_norms_noalloc: arrays must be device memory");
         }
+        if (at.type == cudaMemoryTypeDevice && at.device != dev)
+            return set_err(LES_ERR_ARG, "lester_norms_noalloc: an array lives on device %d, the current device is %d",
+                           at.device, dev);
     }
     double *scratch = nullptr;
-    int r = scratch_address(&scratch);
+    int r = scratch_address(dev, &scratch);
     if (r) return r;
     cudaStream_t st = (cudaStream_t)stream;
     BlkDev blk{};

@@ -517,8 +517,14 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
     int maxctas = smem <= 48 * 1024 ? LES_PHYS(c, sc1_sweep_max_ctas)(smem) : 0;
     if (maxctas > 0) {
         LES_CUDA(cudaMemsetAsync(c.d_wave, 0, sizeof(WaveSync), c.stream));
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (c.prof && !c.capturing) {
+            prof_pair(c, LES_PROF_SWEEP, &e0, &e1);
+            cudaEventRecord(e0, c.stream);
+        }
         LES_CUDA(LES_PHYS(c, launch_sc1_sweep)(L.d_blk, c.d_wcum, c.d_wslice, c.nslice, maxctas, smin, smax, A,
-                                               c.c.dtime, c.d_wave, 1L << 24, c.stream));
+                                               c.c.dtime, c.d_wave, wait_polls(c), c.stream));
+        if (e1) cudaEventRecord(e1, c.stream);
         if (c.capturing) {
             // a replayed step reads the barrier's flag with its other status
             launch_copy_flag(&c.d_wave->err, c.d_loop + 6, c.stream);

@@ -61,6 +61,7 @@ class Ctrl(C.Structure):
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
         ("rb_line", C.c_int), ("autotune", C.c_int), ("phys32", C.c_int), ("step_graph", C.c_int),
+        ("sc1_sweep", C.c_int), ("wait_limit", C.c_int),
     ]
 
 
@@ -339,10 +340,16 @@ def gpu_prof(enable: bool) -> None:
     _check(lib().lester_gpu_prof(1 if enable else 0))
 
 
-def gpu_prof_read():
+PROF_RB, PROF_SWEEP = 0, 1
+
+
+def gpu_prof_read(which: int = PROF_RB):
+    """(summed device ms, timed launches) of one timed kernel since
+    gpu_prof(True): PROF_RB the level-1 red-black smoother, PROF_SWEEP the
+    scalar sweep."""
     ms = C.c_double()
     n = C.c_long()
-    _check(lib().lester_gpu_prof_read(C.byref(ms), C.byref(n)))
+    _check(lib().lester_gpu_prof_kernel(int(which), C.byref(ms), C.byref(n)))
     return ms.value, n.value
 
 

@@ -8,7 +8,7 @@
  * calling convention (scalars as pointers, arrays as FP64 arena slices in
  * Fortran order), so a Fortran build binds them with
  *     interface; subroutine ... bind(C, name="lester_<routine>") ...
- * and keeps its own subroutine names (see INTEGRATION.md).
+ * and keeps its own subroutine names.
  *
  * What the reference keeps in COMMON blocks (block sizes and links, boundary
  * types, time step, model and multigrid controls) is passed once to
@@ -152,6 +152,18 @@ typedef struct lester_ctrl {
                           set and controls (istep > 1, fast psolve, device
                           fields, no inflow/outflow sides, autotuning
                           finished); otherwise the step runs as launched */
+    int sc1_sweep;     /* in-place scalar sweep of set_sc1: 0 = automatic
+                          (the tile pipeline where its tiles fit, else the
+                          hyperplane sweep); 1 = hyperplane sweep, one
+                          cooperative launch with a grid barrier per
+                          i+j+k plane; 2 = tile pipeline, one CTA per
+                          (block, k, row range) tile walking the planes
+                          i+j with point-to-point progress flags; 3 = one
+                          launch per i+j+k plane.  All give the same
+                          result for a given physics build. */
+    int wait_limit;    /* bounded device waits (grid barrier, progress
+                          flags): polls before a wait gives up and the call
+                          returns LES_ERR_TIMEOUT; 0 = the default (2^24) */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */
@@ -213,10 +225,15 @@ int lester_gpu_solve_time(double *ms);
  * y-line relaxation won; *done = 0 while it has not run */
 int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *omega, int *tail, int *line);
 /* kernel timing inside a timed region: CUDA events around each launch of
- * the level-1 red-black smoother of the fast solvers.  prof(1) clears and
- * starts, prof(0) stops; prof_read returns the summed milliseconds and the
- * number of timed launches. */
+ * the timed kernels -- LES_PROF_RB: the level-1 red-black smoother of the
+ * fast solvers; LES_PROF_SWEEP: the in-place scalar sweep of set_sc1.
+ * prof(1) clears and starts, prof(0) stops; prof_kernel returns one
+ * kernel's summed milliseconds and number of timed launches; prof_read is
+ * prof_kernel(LES_PROF_RB). */
+#define LES_PROF_RB 0
+#define LES_PROF_SWEEP 1
 int lester_gpu_prof(int enable);
+int lester_gpu_prof_kernel(int which, double *ms_total, long *launches);
 int lester_gpu_prof_read(double *ms_total, long *launches);
 /* bytes copied host->device and device->host by calls with host arrays */
 int lester_gpu_xfer_bytes(long *h2d, long *d2h);
@@ -288,18 +305,20 @@ int lester_norms(const int *ilev, const int *mg_or_sg, const double *ap,
                  double *res_norm, double *rhs_norm, double *err_norm,
                  double *var_norm);
 /* No counterpart in the reference.  lester_norms for one block, for hosts
- * that cannot allocate device memory at the call (inside a stream capture,
- * under a fixed memory budget, or with their own device pool): it needs no
+ * that must not allocate device memory when they call it (a code that runs
+ * under a fixed device-memory budget, or owns all device memory through
+ * its own pool and forbids libraries to allocate): it needs no
  * lester_gpu_init and allocates nothing.  Its scratch is a static device
  * array of 4 * LES_NOALLOC_MAX_POINTS / 256 + 8 doubles (512 KB); blocks
  * with more than LES_NOALLOC_MAX_POINTS interior points are rejected with
  * LES_ERR_SIZE.  nijkp1 = points per axis incl. ghosts; every array is
- * device memory in the reference's Fortran order; the norms are written to
- * host scalars after the work on `stream` (a cudaStream_t, NULL for the
- * default stream) completes.  Nothing in the scratch has to start at
- * zero.  Calls that overlap on the GPU race on the one scratch.  The first
- * call on each device looks up the scratch address (cudaGetSymbolAddress)
- * and should come before any stream capture. */
+ * device memory of the current device, in the reference's Fortran order;
+ * the call queues its work on `stream` (a cudaStream_t, NULL for the
+ * default stream), waits for it and writes the norms to host scalars.
+ * Nothing in the scratch has to start at zero.  Calls that overlap on the
+ * GPU race on the one scratch.  The first call in each CUDA context of a
+ * device (again after a cudaDeviceReset) looks up the scratch address
+ * (cudaGetSymbolAddress) and should come before any stream capture. */
 #define LES_NOALLOC_MAX_POINTS 4194304L
 int lester_norms_noalloc(const int *nijkp1, const double *ap, const double *aw,
                          const double *ae, const double *as, const double *an,

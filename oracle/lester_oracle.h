@@ -65,6 +65,11 @@ typedef struct {
     double tolf;      /* enorm/vnorm stop tolerance */
     double relax_pmg; /* SOR omega                */
     double relax_pmgc;/* SOR omega, coarsest grid */
+    int compat;       /* orc_step only, not in the reference: 1 = solve for
+                         the pressure source minus its interior mean over all
+                         blocks (one connected component), the compatible part
+                         of a singular system, as the GPU fast solvers do; 0 =
+                         the source as sour_p leaves it (the reference) */
 } orc_mgctrl;
 
 /* ---- geometry ---------------------------------------------------------- */

@@ -14,6 +14,10 @@
  *   (428), conv_exitbc(2, u..w) (433-441), swap_rhos (450)
  * conv_exitbc is a no-op without convective sides; conv_exitbc(1, p) and
  * (1, sc1) change nothing; cflest only prints.
+ * With mg->compat (not in the reference) the pressure source loses its
+ * interior mean before lmg_solve: the compatible system of a singular
+ * (all-Neumann/periodic) pressure equation, solved to tolf, is the FP64
+ * reference for the GPU fast solvers on variable-density cases.
  */
 #include <stdlib.h>
 #include "orc_internal.h"
@@ -81,6 +85,27 @@ void orc_step(orc_ctx *c, const orc_mgctrl *mg, const orc_phys *k, int istep, in
     orc_sour_p(c, k->dtime, MET(M_DIU), MET(M_DJV), MET(M_RDIV), MET(M_RDJU), MET(M_DIDJP),
                F->dkp, MET(M_RDIDJP), F->dkw, F->u_int, F->v_int, F->w_int, F->rho, F->rhonp1,
                F->drhonp1dt, F->s, F->srhot, F->srhoux);
+    if (mg->compat) {
+        /* interior mean, summed block by block in k, j, i order */
+        double sum = 0.0, cnt = 0.0;
+        for (int b = 1; b <= c->numbl; b++) {
+            const int *n = c->mg_nijkp1[1][b];
+            for (int k = 2; k <= n[2] - 1; k++)
+                for (int j = 2; j <= n[1] - 1; j++)
+                    for (int i = 2; i <= n[0] - 1; i++) {
+                        sum += F->s[c->off3[1][b] + (i - 1) + (long)n[0] * ((j - 1) + (long)n[1] * (k - 1))];
+                        cnt += 1.0;
+                    }
+        }
+        const double mean = sum / cnt;
+        for (int b = 1; b <= c->numbl; b++) {
+            const int *n = c->mg_nijkp1[1][b];
+            for (int k = 2; k <= n[2] - 1; k++)
+                for (int j = 2; j <= n[1] - 1; j++)
+                    for (int i = 2; i <= n[0] - 1; i++)
+                        F->s[c->off3[1][b] + (i - 1) + (long)n[0] * ((j - 1) + (long)n[1] * (k - 1))] -= mean;
+        }
+    }
     orc_set_loop_bound(c, ORC_SV_P);
     double nrm[5];
     orc_lmg_solve(c, mg, F->ap, F->aw, F->ae, F->as, F->an, F->al, F->ar, F->p, F->s, F->res, nrm);

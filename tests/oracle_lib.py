@@ -46,7 +46,7 @@ class MgCtrl(C.Structure):
     _fields_ = [("nummgits", C.c_int), ("numpre", C.c_int), ("numpost", C.c_int),
                 ("numcits", C.c_int), ("meth_cycle", C.c_int), ("meth_smooth", C.c_int),
                 ("meth_csolve", C.c_int), ("tolf", C.c_double), ("relax_pmg", C.c_double),
-                ("relax_pmgc", C.c_double)]
+                ("relax_pmgc", C.c_double), ("compat", C.c_int)]
 
 
 class Oracle:
@@ -165,8 +165,10 @@ class Oracle:
                                    m["hkip"], m["hkjp"], m["rp"])))
 
 
-def mgctrl(nummgits=5, numpre=1, numpost=1, numcits=20, meth_cycle=1, tolf=5e-13, relax=1.6):
+def mgctrl(nummgits=5, numpre=1, numpost=1, numcits=20, meth_cycle=1, tolf=5e-13, relax=1.6,
+           compat=0):
     c = MgCtrl()
+    c.compat = compat
     c.nummgits, c.numpre, c.numpost, c.numcits = nummgits, numpre, numpost, numcits
     c.meth_cycle, c.meth_smooth, c.meth_csolve = meth_cycle, 1, 0
     c.tolf, c.relax_pmg, c.relax_pmgc = tolf, relax, relax
