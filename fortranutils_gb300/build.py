@@ -50,6 +50,9 @@ UNITS = {
     "k_outflow": ("k_outflow.cu", ["-fmad=false"]),
     "lester_outflow": ("lester_outflow.cu", []),
     "k_graph": ("k_graph.cu", []),
+    # the tiled scalar sweep: exact FP64 (no FMA); fast FP64 and FP32
+    "k_sweep": ("k_sweep.cu", ["-fmad=false", "-DLES_SWEEP_EXACT"]),
+    "k_sweep_fast": ("k_sweep.cu", []),
     # the FP32-arithmetic physics build (namespace les_f32), generated from
     # k_phys.cu and k_sgs.cu by gen_f32.py into the build directory
     "k_phys_f32": ("@k_phys_f32.cu", []),

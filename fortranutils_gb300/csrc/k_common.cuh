@@ -176,3 +176,52 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *out)
         }
     }
 }
+
+// ----------------------------------------------------- tiled scalar sweep
+// (k_sweep.cu).  Skewed layout of a block: element (i, j, k) (1-based) of a
+// 3-D field at sk3 + (k-1) layer + (i+j-2) vp + (j-1), of a 2-D table at
+// sk2 + (i+j-2) vp + (j-1): plane t = i + j of a layer is one vector over j.
+struct SkewBlk {
+    int n[3];      // nip1, njp1, nkp1
+    int vp;        // elements per plane vector: njp1 rounded up to 4
+    int bc[6];
+    long off3;     // FP64 3-D field offset of the block (level 1)
+    long off2;     // FP64 2-D metric offset
+    long off1k;    // 1-D k metric offset
+    long sk3;      // skewed 3-D offset
+    long sk2;      // skewed 2-D offset
+    long layer;    // elements per skewed layer: (nip1 + njp1 - 1) vp
+};
+
+// one tile: block, layer k (2..nkp1-1), own rows j0..j1-1, and the tiles
+// whose progress it waits for: (block, k-1, same rows) and (block, k,
+// rows below), -1 where there is none
+struct SweepTile {
+    int blk, k, j0, j1, up_k, up_j;
+};
+
+constexpr int kSweepThreads = 256;  // rows per tile at most (one thread per row)
+constexpr int kSweepDepth = 2;      // planes staged ahead
+
+// sources (FP64, reference layout) and skewed destinations of one k_skew
+// launch: up to 10 fields or tables
+template <typename S> struct SkewPtrs {
+    const double *src[10];
+    S *dst[10];
+};
+
+template <typename S> struct SweepArgs {
+    const SkewBlk *sb;
+    const SweepTile *tiles;
+    int ntile, sw;           // tiles; ring row width (elements)
+    S *f3[8];                // skewed sc1 hsc1 u v w rho gamsc1 gamlam (sc1, hsc1 updated)
+    const S *f2[10];         // skewed diu djv rdju rdiv rp didjp rdidjp (+ 1/diu 1/djv 1/rp)
+    const double *dkp, *dkw, *rdkp;
+    const double *grad;      // interface gradients (set_gamsc1_bc planes)
+    long gstride;
+    int gm;
+    const int *link;         // bl2bl, 0-based, 6 per block
+    int *flags;              // per tile: last plane done (released)
+    int *ticket;             // next tile to take
+    int *err;                // a bounded wait gave up
+};

@@ -20,13 +20,14 @@ __global__ void k_loop_init(cudaGraphConditionalHandle h, const double *__restri
                             double *__restrict__ loop, double rtol)
 {
     const double r2 = small[0], b2 = small[1];
+    const bool fin = isfinite(r2) && isfinite(b2);
     const double rel = b2 > 0 ? sqrt(r2 / b2) : 0.;
-    const int go = b2 > 0 && rel > rtol;
+    const int go = fin && b2 > 0 && rel > rtol;
     loop[0] = b2;
     loop[1] = rel;
     loop[2] = rel;
     loop[3] = 0;
-    loop[4] = go ? 0 : 1;
+    loop[4] = !fin ? 4 : go ? 0 : 1;
     cudaGraphSetConditional(h, go);
 }
 

@@ -1,0 +1,565 @@
+// k_sweep.cu -- the in-place scalar update of set_sc1_block
+// (code/set_sc1_block.F:104-502) as a pipeline of tiles.
+//
+// The update of sc1 at (i, j, k) reads sc1 at +-1 and +-2 along each axis
+// only, new values on the minus side and old ones on the plus side (the
+// reference's in-place loop).  Within one k layer the points of a plane
+// t = i + j are independent given planes t-1, t-2 of the layer and plane t
+// of the layers k-1, k-2 (new) and k+1, k+2 (old).  So:
+//
+//  * a tile is (block, layer k, rows j0..j1-1); one CTA walks its planes t
+//    in order, one thread per row, a __syncthreads between planes;
+//  * tile (k, J) may compute plane t once tile (k-1, J) has finished plane t
+//    and tile (k, J-1) plane t-1: point-to-point progress flags (acquire /
+//    release, bounded waits) replace grid-wide barriers, and the tiles run
+//    as a wavefront: the chain is one tile per layer and row range;
+//  * every field is first copied into a skewed layout (k_skew), in which
+//    plane t of a layer is one contiguous vector over j, so a tile stages
+//    the vectors of the planes it will need with coalesced 16-byte cp.async
+//    copies into a shared-memory ring, D planes ahead; the new values go
+//    back into the skewed scalar array (read by the next layer) and are
+//    copied to the FP64 fields at the end (k_unskew).
+//
+// The arithmetic per point is that of sc1_cell in k_phys.cu, operand for
+// operand, so the exact build (FP64, -fmad=false) equals the hyperplane
+// sweep and the oracle bit for bit; the fast build uses the reciprocal
+// metric tables (x * (1/d)) as k_phys.cu's fast build does; the FP32 build
+// is the same template with R = S = float (FP64 fields in HBM, FP32 skewed
+// copies).
+#include "k_common.cuh"
+#include "kernels.h"
+
+#if defined(LES_SWEEP_EXACT)
+#define SWEEP_NS les_exact
+#else
+#define SWEEP_NS les_fast
+#endif
+
+namespace les_sweep {
+namespace {  // internal to each build of this unit
+
+// vectors staged per plane: own layer (3-D fields 0..7), the layers k-1,
+// k-2, k+1, k+2, and the 2-D metric tables (reciprocals last: fast only)
+enum {
+    V_SC, V_H, V_U, V_V, V_W, V_RHO, V_GS, V_GL,
+    V_SCM1, V_RHOM1, V_GSM1, V_GLM1, V_SCM2,
+    V_SCP1, V_RHOP1, V_GSP1, V_GLP1, V_WP1, V_SCP2,
+    V_DIU, V_DJV, V_RDJU, V_RDIV, V_RP, V_DIDJP, V_RDIDJP,
+    V_RDIU, V_RDJV, V_RRP,
+    V_N
+};
+
+// per vector: source (0..7 a 3-D field: sc1 hsc1 u v w rho gamsc1 gamlam;
+// 8 + q the 2-D table q), layer offset, and the plane window [t+lo, t+hi]
+// a point of plane t reads
+struct VecDesc {
+    int src, dk, lo, hi;
+};
+__host__ __device__ constexpr VecDesc vdesc(int v)
+{
+    constexpr VecDesc d[V_N] = {
+        {0, 0, -2, 2}, {1, 0, 0, 0}, {2, 0, 0, 1}, {3, 0, 0, 1}, {4, 0, 0, 0}, {5, 0, -1, 1}, {6, 0, -1, 1},
+        {7, 0, -1, 1},
+        {0, -1, 0, 0}, {5, -1, 0, 0}, {6, -1, 0, 0}, {7, -1, 0, 0}, {0, -2, 0, 0},
+        {0, 1, 0, 0}, {5, 1, 0, 0}, {6, 1, 0, 0}, {7, 1, 0, 0}, {4, 1, 0, 0}, {0, 2, 0, 0},
+        {8, 0, -1, 2}, {9, 0, -1, 2}, {10, 0, 0, 1}, {11, 0, 0, 1}, {12, 0, 0, 0}, {13, 0, 0, 0},
+        {14, 0, 0, 0},
+        {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0}};
+    return d[v];
+}
+// ring slots of vector v for prefetch distance D: planes t+lo .. t+hi+D
+__host__ __device__ constexpr int vslots(int v, int D) { return vdesc(v).hi - vdesc(v).lo + D + 1; }
+__host__ __device__ constexpr int nvec(bool fast) { return fast ? V_N : V_RDIU; }
+__host__ __device__ constexpr int ring_slots(bool fast, int D)
+{
+    int s = 0;
+    for (int v = 0; v < nvec(fast); v++) s += vslots(v, D);
+    return s;
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p)
+{
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Wait until *flag >= need (thread 0 of the CTA); bounded: after `limit`
+// polls, or once another CTA has set *err, give up (returns false).
+__device__ bool wait_flag(const int *flag, int need, int &seen, int *err, long limit)
+{
+    long it = 0;
+    while (seen < need) {
+        seen = ld_acquire(flag);
+        if (seen >= need) break;
+        if (*(volatile int *)err) return false;
+        if (++it > limit) {
+            atomicExch(err, 1);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
+
+// ------------------------------------------------------------------ skew
+// Copy a 3-D field (or a 2-D table: n2 = 1) from the reference layout into
+// the skewed layout through a 32 x 32 (plane, row) shared tile: coalesced
+// reads along i, coalesced writes along j.  Element (i, j, k) goes to
+// sk + (k-1) layer + (i+j-2) vp + (j-1); entries of a plane vector whose i
+// falls outside 1..nip1 are not written.
+template <typename S>
+__global__ void __launch_bounds__(256) k_skew(const SkewBlk *__restrict__ sb, int nfield, SkewPtrs<S> P,
+                                              int two_d, int ntp)
+{
+    __shared__ double tile[32][33];
+    const SkewBlk b = sb[blockIdx.z / nfield];
+    const int f = blockIdx.z % nfield;
+    const int n0 = b.n[0], n1 = b.n[1];
+    const int nlay = two_d ? 1 : b.n[2];
+    const int k = blockIdx.y + 1;
+    if (k > nlay) return;
+    const int tt = blockIdx.x % ntp, jt = blockIdx.x / ntp;
+    if (jt * 32 >= n1 || 32 * tt > n0 + n1 - 2) return;
+    const int t0 = 2 + 32 * tt, jb = 1 + 32 * jt;
+    const double *s = P.src[f] + (two_d ? b.off2 : b.off3 + (long)n0 * n1 * (k - 1));
+    S *d = P.dst[f] + (two_d ? b.sk2 : b.sk3 + b.layer * (k - 1));
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int r = ty; r < 32; r += 8) {
+        const int j = jb + r, i = t0 + tx - j;
+        double v = 0.0;
+        if (j <= n1 && i >= 1 && i <= n0) v = s[(i - 1) + (long)n0 * (j - 1)];
+        tile[r][tx] = v;
+    }
+    __syncthreads();
+    for (int q = ty; q < 32; q += 8) {
+        const int t = t0 + q, j = jb + tx, i = t - j;
+        if (j <= n1 && i >= 1 && i <= n0) d[(long)(t - 2) * b.vp + (j - 1)] = (S)tile[tx][q];
+    }
+}
+
+// The reverse for the swept scalar and its history, interior points only:
+// the same (plane, row) tiles, read along j, written along i
+template <typename S>
+__global__ void __launch_bounds__(256) k_unskew(const SkewBlk *__restrict__ sb, const S *__restrict__ sks,
+                                                const S *__restrict__ skh, double *__restrict__ sc1,
+                                                double *__restrict__ hsc1, int ntp)
+{
+    __shared__ double tile[2][32][33];
+    const SkewBlk b = sb[blockIdx.z];
+    const int n0 = b.n[0], n1 = b.n[1];
+    const int k = blockIdx.y + 2;
+    if (k > b.n[2] - 1) return;
+    const int tt = blockIdx.x % ntp, jt = blockIdx.x / ntp;
+    if (jt * 32 >= n1 || 32 * tt > n0 + n1 - 2) return;
+    const int t0 = 2 + 32 * tt, jb = 1 + 32 * jt;
+    const long lay = b.sk3 + b.layer * (k - 1);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int q = ty; q < 32; q += 8) {
+        const int t = t0 + q, j = jb + tx, i = t - j;
+        double a = 0.0, h = 0.0;
+        if (j >= 2 && j <= n1 - 1 && i >= 2 && i <= n0 - 1) {
+            const long e = lay + (long)(t - 2) * b.vp + (j - 1);
+            a = (double)sks[e];
+            h = (double)skh[e];
+        }
+        tile[0][tx][q] = a;
+        tile[1][tx][q] = h;
+    }
+    __syncthreads();
+    const long base = b.off3 + (long)n0 * n1 * (k - 1);
+    for (int r = ty; r < 32; r += 8) {
+        const int j = jb + r, i = t0 + tx - j;
+        if (j >= 2 && j <= n1 - 1 && i >= 2 && i <= n0 - 1) {
+            const long p = base + (i - 1) + (long)n0 * (j - 1);
+            sc1[p] = tile[0][r][tx];
+            hsc1[p] = tile[1][r][tx];
+        }
+    }
+}
+
+// ----------------------------------------------------------- the pipeline
+// R: arithmetic type; S: storage type of the skewed copies; FAST: the
+// reciprocal tables of the fast builds; D: planes staged ahead.
+template <typename R, typename S, bool FAST, int D>
+__global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    S *ring = (S *)smem_raw;
+    __shared__ int s_tile, s_ok[2];  // s_ok by plane parity: thread 0 may write the next before all read this
+    constexpr int NV = nvec(FAST);
+    constexpr int E = 16 / sizeof(S);  // elements per 16-byte chunk
+    const R lambda = (R)4.0, small = (R)1.e-30, half = (R)0.5, one = (R)1.0, zero = (R)0.0;
+    const R dtime = (R)dtime_d;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) {
+            int tk = -1;
+            if (!*(volatile int *)A.err) tk = atomicAdd(A.ticket, 1);
+            s_tile = tk;
+        }
+        __syncthreads();
+        const int tix = s_tile;
+        if (tix < 0 || tix >= A.ntile) return;
+        const SweepTile T = A.tiles[tix];
+        const SkewBlk b = A.sb[T.blk];
+        const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+        const int k = T.k, j0 = T.j0, j1 = T.j1;
+        const int ni = n0 - 1, nj = n1 - 1, nk = n2 - 1;
+        // staged rows: j0-2 .. j1+1 (0-based jr), chunk aligned
+        const int sbase = (max(0, j0 - 3) / E) * E;
+        const int jr_lo = max(0, j0 - 3), jr_hi = min(n1, j1 + 1);  // [lo, hi)
+        const int SW = A.sw;
+        // own row and the plane range
+        const int j = j0 + tid;
+        const bool row = j < j1;
+        const int t0 = 2 + j0, t1 = ni + (j1 - 1);
+        // 1-D metrics of this layer
+        const double *dkp = A.dkp + b.off1k, *dkw = A.dkw + b.off1k;
+        const R dkw_k = (R)dkw[k - 1];
+        const R dkp_m3 = k > 2 ? (R)dkp[k - 3] : zero, dkp_m2 = (R)dkp[k - 2], dkp_m1 = (R)dkp[k - 1];
+        const R dkp_0 = k < nk ? (R)dkp[k] : zero;
+        R rdkp_m3 = zero, rdkp_m2 = zero, rdkp_m1 = zero, rdkp_0 = zero;
+        if (FAST) {
+            const double *rdkp = A.rdkp + b.off1k;
+            rdkp_m3 = k > 2 ? (R)rdkp[k - 3] : zero;
+            rdkp_m2 = (R)rdkp[k - 2];
+            rdkp_m1 = (R)rdkp[k - 1];
+            rdkp_0 = k < nk ? (R)rdkp[k] : zero;
+        }
+        int seen_k = 0, seen_j = 0;
+        // ring offsets (compile-time slot counts)
+        auto voff = [&](int v) {
+            int o = 0;
+#pragma unroll
+            for (int u = 0; u < NV; u++)
+                if (u < v) o += vslots(u, D);
+            return o * SW;
+        };
+        auto at = [&](int v, int p, int jj) -> R {
+            return (R)ring[voff(v) + (p % vslots(v, D)) * SW + (jj - 1 - sbase)];
+        };
+        // issue the copies of group t: plane t + D + hi of every vector
+        auto issue = [&](int t) {
+#pragma unroll
+            for (int v = 0; v < NV; v++) {
+                const VecDesc vd = vdesc(v);
+                const int p = t + D + vd.hi;
+                if (p < t0 + vd.lo || p > t1 + vd.hi || p < 2 || p > n0 + n1) continue;
+                const int kv = k + vd.dk;
+                if (kv < 1 || kv > n2) continue;
+                const bool cross = vd.dk != 0;
+                // rows: valid i = p - j in 1..n0; cross-layer vectors own rows only
+                int lo = max(cross ? j0 - 1 : jr_lo, p - n0 - 1), hi = min(cross ? j1 - 1 : jr_hi, p - 1);
+                if (lo >= hi) continue;
+                const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
+                const S *g;
+                if (vd.src < 8)
+                    g = A.f3[vd.src] + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
+                else
+                    g = A.f2[vd.src - 8] + b.sk2 + (long)(p - 2) * b.vp;
+                S *dst = ring + voff(v) + (p % vslots(v, D)) * SW - sbase;
+                for (int c = c_lo + tid; c < c_hi; c += blockDim.x) cp_async16(dst + c * E, g + c * E);
+            }
+        };
+        const int ts = t0 - D - 4;
+        bool ok = true;
+        for (int t = ts; t <= t1; t++) {
+            // progress needed before group t: cross planes t + D of layer k-1
+            // (and k-2 through it), own planes t + D + 2 of rows j0-2, j0-1
+            if (tid == 0) {
+                bool g = true;
+                if (T.up_k >= 0 && t + D >= t0) g = wait_flag(A.flags + T.up_k, t + D, seen_k, A.err, limit);
+                if (g && T.up_j >= 0) g = wait_flag(A.flags + T.up_j, t + D + 2, seen_j, A.err, limit);
+                s_ok[t & 1] = g;
+            }
+            if (t >= t0) cp_async_wait<D - 1>();
+            __syncthreads();
+            if (!s_ok[t & 1]) {
+                ok = false;
+                break;
+            }
+            if (tid == 0 && t - 1 >= 2) {
+                __threadfence();
+                st_release(A.flags + tix, t - 1);
+            }
+            issue(t);
+            cp_async_commit();
+            if (t < t0 || !row) continue;
+            const int i = t - j;
+            if (i < 2 || i > ni) continue;
+            // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands)
+            const R rho0 = at(V_RHO, t, j);
+            const R rhowf = half * (rho0 + at(V_RHO, t - 1, j));
+            const R rhoef = half * (rho0 + at(V_RHO, t + 1, j));
+            const R rhosf = half * (rho0 + at(V_RHO, t - 1, j - 1));
+            const R rhonf = half * (rho0 + at(V_RHO, t + 1, j + 1));
+            const R rholf = half * (rho0 + at(V_RHOM1, t, j));
+            const R rhorf = half * (rho0 + at(V_RHOP1, t, j));
+            const R rhop = rho0;
+            const R gs0 = at(V_GS, t, j), gl0 = at(V_GL, t, j);
+            const R gamwf = half * (gs0 + at(V_GS, t - 1, j)) * rhowf + half * (gl0 + at(V_GL, t - 1, j));
+            const R gamef = half * (gs0 + at(V_GS, t + 1, j)) * rhoef + half * (gl0 + at(V_GL, t + 1, j));
+            const R gamsf = half * (gs0 + at(V_GS, t - 1, j - 1)) * rhosf + half * (gl0 + at(V_GL, t - 1, j - 1));
+            const R gamnf = half * (gs0 + at(V_GS, t + 1, j + 1)) * rhonf + half * (gl0 + at(V_GL, t + 1, j + 1));
+            const R gamlf = half * (gs0 + at(V_GSM1, t, j)) * rholf + half * (gl0 + at(V_GLM1, t, j));
+            const R gamrf = half * (gs0 + at(V_GSP1, t, j)) * rhorf + half * (gl0 + at(V_GLP1, t, j));
+            const R uwf = at(V_U, t, j), uef = at(V_U, t + 1, j);
+            const R vsf = at(V_V, t, j), vnf = at(V_V, t + 1, j + 1);
+            const R wlf = at(V_W, t, j), wrf = at(V_WP1, t, j);
+            const R s0 = at(V_SC, t, j);
+            const R sw = at(V_SC, t - 1, j), se = at(V_SC, t + 1, j);
+            const R ss = at(V_SC, t - 1, j - 1), sn = at(V_SC, t + 1, j + 1);
+            const R sl = at(V_SCM1, t, j), sr = at(V_SCP1, t, j);
+#define QD(x, v, pp, jj) (FAST ? (x) * at(v##_R, pp, jj) : (x) / at(v, pp, jj))
+#define V_DIU_R V_RDIU
+#define V_DJV_R V_RDJV
+            const R dfdxwf = QD(s0 - sw, V_DIU, t, j);
+            const R dfdxef = QD(se - s0, V_DIU, t + 1, j);
+            const long gst = A.gstride;
+            const int gm = A.gm;
+            const double *GR = A.grad;
+            const int bi = T.blk;
+            R dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
+            if (i == 2)
+                dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D)
+                              ? dfdxwf
+                              : (R)GR[(long)(A.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
+            else
+                dfdxwwf = QD(sw - at(V_SC, t - 2, j), V_DIU, t - 1, j);
+            if (i == ni)
+                dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D)
+                              ? dfdxef
+                              : (R)GR[(long)(A.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
+            else
+                dfdxeef = QD(at(V_SC, t + 2, j) - se, V_DIU, t + 2, j);
+            const R dfdysf = QD(s0 - ss, V_DJV, t, j);
+            const R dfdynf = QD(sn - s0, V_DJV, t + 1, j + 1);
+            if (j == 2)
+                dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D)
+                              ? dfdysf
+                              : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
+            else
+                dfdyssf = QD(ss - at(V_SC, t - 2, j - 2), V_DJV, t - 1, j - 1);
+            if (j == nj)
+                dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D)
+                              ? dfdynf
+                              : (R)GR[(long)(A.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
+            else
+                dfdynnf = QD(at(V_SC, t + 2, j + 2) - sn, V_DJV, t + 2, j + 2);
+#undef QD
+#undef V_DIU_R
+#undef V_DJV_R
+            const R rpij = at(V_RP, t, j);
+            const R rrpij = FAST ? at(V_RRP, t, j) : zero;
+#define QZ(x, dk_, rdk_) (FAST ? (x) * (rrpij * (rdk_)) : (x) / (rpij * (dk_)))
+            const R dfdzlf = QZ(s0 - sl, dkp_m2, rdkp_m2);
+            const R dfdzrf = QZ(sr - s0, dkp_m1, rdkp_m1);
+            if (k == 2)
+                dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D)
+                              ? dfdzlf
+                              : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
+            else
+                dfdzllf = QZ(sl - at(V_SCM2, t, j), dkp_m3, rdkp_m3);
+            if (k == nk)
+                dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D)
+                              ? dfdzrf
+                              : (R)GR[(long)(A.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
+            else
+                dfdzrrf = QZ(at(V_SCP2, t, j) - sr, dkp_0, rdkp_0);
+#undef QZ
+            const R rwst = (uwf >= zero) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
+            const R rest = (uef > zero) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
+            const R rsth = (vsf >= zero) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
+            const R rnth = (vnf > zero) ? (dfdysf + small) / (dfdynf + small) : (dfdynnf + small) / (dfdynf + small);
+            const R rlft = (wlf >= zero) ? (dfdzllf + small) / (dfdzlf + small) : (dfdzrf + small) / (dfdzlf + small);
+            const R rrht = (wrf > zero) ? (dfdzlf + small) / (dfdzrf + small) : (dfdzrrf + small) / (dfdzrf + small);
+            const R limw = fmax(zero, fmin(lambda * rwst, one));
+            const R lime = fmax(zero, fmin(lambda * rest, one));
+            const R lims = fmax(zero, fmin(lambda * rsth, one));
+            const R limn = fmax(zero, fmin(lambda * rnth, one));
+            const R liml = fmax(zero, fmin(lambda * rlft, one));
+            const R limr = fmax(zero, fmin(lambda * rrht, one));
+            R fwf, fef, fsf, fnf, flf, frf;
+            if (uwf > zero) fwf = sw + half * limw * (s0 - sw);
+            else if (uwf < zero) fwf = s0 + half * limw * (sw - s0);
+            else fwf = half * (s0 + sw);
+            if (uef > zero) fef = s0 + half * lime * (se - s0);
+            else if (uef < zero) fef = se + half * lime * (s0 - se);
+            else fef = half * (s0 + se);
+            if (vsf > zero) fsf = ss + half * lims * (s0 - ss);
+            else if (vsf < zero) fsf = s0 + half * lims * (ss - s0);
+            else fsf = half * (s0 + ss);
+            if (vnf > zero) fnf = s0 + half * limn * (sn - s0);
+            else if (vnf < zero) fnf = sn + half * limn * (s0 - sn);
+            else fnf = half * (s0 + sn);
+            if (wlf > zero) flf = sl + half * liml * (s0 - sl);
+            else if (wlf < zero) flf = s0 + half * liml * (sl - s0);
+            else flf = half * (s0 + sl);
+            if (wrf > zero) frf = s0 + half * limr * (sr - s0);
+            else if (wrf < zero) frf = sr + half * limr * (s0 - sr);
+            else frf = half * (s0 + sr);
+            const R areawf = at(V_RDJU, t, j) * dkw_k;
+            const R areaef = at(V_RDJU, t + 1, j) * dkw_k;
+            const R areasf = at(V_RDIV, t, j) * dkw_k;
+            const R areanf = at(V_RDIV, t + 1, j + 1) * dkw_k;
+            const R areak = at(V_DIDJP, t, j);
+            const R vol = at(V_RDIDJP, t, j) * dkw_k;
+            const R gwf = rhowf * uwf * fwf * areawf;
+            const R gef = rhoef * uef * fef * areaef;
+            const R gsf = rhosf * vsf * fsf * areasf;
+            const R gnf = rhonf * vnf * fnf * areanf;
+            const R glf = rholf * wlf * flf * areak;
+            const R grf = rhorf * wrf * frf * areak;
+            const R convf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
+            const R twf = gamwf * areawf * dfdxwf;
+            const R tef = gamef * areaef * dfdxef;
+            const R tsf = gamsf * areasf * dfdysf;
+            const R tnf = gamnf * areanf * dfdynf;
+            const R tlf = gamlf * areak * dfdzlf;
+            const R trf = gamrf * areak * dfdzrf;
+            const R difff = (tef - twf) + (tnf - tsf) + (trf - tlf);
+            const R h = convf + difff;
+            R tmp = s0 + dtime / (vol * rhop) * ((R)1.5 * h - half * at(V_H, t, j));
+            if (tmp < zero) tmp = zero;
+            if (tmp > one) tmp = one;
+            // in place: the ring slot of plane t (read as new by later
+            // planes), the skewed scalar (read by layer k+1) and history
+            ring[voff(V_SC) + (t % vslots(V_SC, D)) * SW + (j - 1 - sbase)] = (S)tmp;
+            const long e = b.sk3 + b.layer * (k - 1) + (long)(t - 2) * b.vp + (j - 1);
+            A.f3[0][e] = (S)tmp;
+            A.f3[1][e] = (S)h;
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        if (!ok) return;
+        if (tid == 0) {
+            __threadfence();
+            st_release(A.flags + tix, 0x7fffffff);  // every plane of this tile done
+        }
+    }
+}
+
+} // namespace
+} // namespace les_sweep
+
+namespace SWEEP_NS {
+
+using namespace les_sweep;
+
+template <typename S>
+void launch_skew_t(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, int nfield,
+                   const SkewPtrs<S> &P, int two_d, cudaStream_t st)
+{
+    const int ntp = (maxn0 + maxn1 - 1 + 31) / 32, njt = (maxn1 + 31) / 32;
+    k_skew<S><<<dim3(ntp * njt, two_d ? 1 : maxn2, nb * nfield), 256, 0, st>>>(sb, nfield, P, two_d, ntp);
+    les::count_launch(1);
+}
+
+template <typename S>
+void launch_unskew_t(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, const S *sks, const S *skh,
+                     double *sc1, double *hsc1, cudaStream_t st)
+{
+    const int ntp = (maxn0 + maxn1 - 1 + 31) / 32, njt = (maxn1 + 31) / 32;
+    k_unskew<S><<<dim3(ntp * njt, maxn2 > 2 ? maxn2 - 2 : 1, nb), 256, 0, st>>>(sb, sks, skh, sc1, hsc1, ntp);
+    les::count_launch(1);
+}
+
+template <typename R, typename S, bool FAST, int D>
+int tiles_smem(int sw)
+{
+    return ring_slots(FAST, D) * sw * (int)sizeof(S);
+}
+
+template <typename R, typename S, bool FAST, int D>
+cudaError_t launch_tiles_t(const SweepArgs<S> &a, double dtime, long limit, int nctas, cudaStream_t st)
+{
+    const int smem = tiles_smem<R, S, FAST, D>(a.sw);
+    auto kern = k_sc1_tiles<R, S, FAST, D>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<nctas, kSweepThreads, smem, st>>>(a, dtime, limit);
+    les::count_launch(1);
+    return cudaGetLastError();
+}
+
+template <typename R, typename S, bool FAST, int D>
+int tiles_max_ctas(int sw)
+{
+    const int smem = tiles_smem<R, S, FAST, D>(sw);
+    auto kern = k_sc1_tiles<R, S, FAST, D>;
+    int dev = 0, nsm = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kSweepThreads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return nsm * per;
+}
+
+#if defined(LES_SWEEP_EXACT)
+// FP64, the reference's operation order (this unit is built with -fmad=false)
+using RT = double;
+using ST = double;
+constexpr bool kFast = false;
+#else
+// fast FP64 build: reciprocal tables and FMA contraction
+using RT = double;
+using ST = double;
+constexpr bool kFast = true;
+#endif
+
+void launch_sweep_skew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, int nfield,
+                       const SkewPtrs<double> &P, int two_d, cudaStream_t st)
+{
+    launch_skew_t<ST>(sb, nb, maxn0, maxn1, maxn2, nfield, P, two_d, st);
+}
+void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, const double *sks,
+                         const double *skh, double *sc1, double *hsc1, cudaStream_t st)
+{
+    launch_unskew_t<ST>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
+}
+int sweep_tiles_smem(int sw) { return tiles_smem<RT, ST, kFast, kSweepDepth>(sw); }
+int sweep_tiles_max_ctas(int sw) { return tiles_max_ctas<RT, ST, kFast, kSweepDepth>(sw); }
+cudaError_t launch_sweep_tiles(const SweepArgs<double> &a, double dtime, long limit, int nctas, cudaStream_t st)
+{
+    return launch_tiles_t<RT, ST, kFast, kSweepDepth>(a, dtime, limit, nctas, st);
+}
+
+} // namespace SWEEP_NS
+
+#if !defined(LES_SWEEP_EXACT)
+// the FP32 build: FP32 arithmetic on FP32 skewed copies
+namespace les_f32 {
+using namespace les_sweep;
+void launch_sweep_skew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, int nfield,
+                       const SkewPtrs<float> &P, int two_d, cudaStream_t st)
+{
+    les_fast::launch_skew_t<float>(sb, nb, maxn0, maxn1, maxn2, nfield, P, two_d, st);
+}
+void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, const float *sks,
+                         const float *skh, double *sc1, double *hsc1, cudaStream_t st)
+{
+    les_fast::launch_unskew_t<float>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
+}
+int sweep_tiles_smem(int sw) { return les_fast::tiles_smem<float, float, true, kSweepDepth>(sw); }
+int sweep_tiles_max_ctas(int sw) { return les_fast::tiles_max_ctas<float, float, true, kSweepDepth>(sw); }
+cudaError_t launch_sweep_tiles(const SweepArgs<float> &a, double dtime, long limit, int nctas, cudaStream_t st)
+{
+    return les_fast::launch_tiles_t<float, float, true, kSweepDepth>(a, dtime, limit, nctas, st);
+}
+} // namespace les_f32
+#endif

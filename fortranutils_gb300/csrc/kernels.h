@@ -237,3 +237,26 @@ LES_PHYS_LAUNCHERS
 namespace les_f32 {
 LES_PHYS_LAUNCHERS
 }
+
+// k_sweep.cu: the tiled scalar sweep, built per physics variant (FP64
+// exact and fast on FP64 skewed copies, FP32 on FP32 copies)
+#define LES_SWEEP_LAUNCHERS(S)                                                                      \
+    void launch_sweep_skew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2, int nfield, \
+                           const SkewPtrs<S> &P, int two_d, cudaStream_t st);                      \
+    void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2,           \
+                             const S *sks, const S *skh, double *sc1, double *hsc1,                \
+                             cudaStream_t st);                                                      \
+    int sweep_tiles_smem(int sw);                                                                   \
+    int sweep_tiles_max_ctas(int sw);                                                               \
+    cudaError_t launch_sweep_tiles(const SweepArgs<S> &a, double dtime, long limit, int nctas,     \
+                                   cudaStream_t st);
+
+namespace les_exact {
+LES_SWEEP_LAUNCHERS(double)
+}
+namespace les_fast {
+LES_SWEEP_LAUNCHERS(double)
+}
+namespace les_f32 {
+LES_SWEEP_LAUNCHERS(float)
+}

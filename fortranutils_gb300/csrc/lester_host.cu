@@ -474,6 +474,11 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_vlev);
     cudaFree(c->d_wslice);
     cudaFree(c->d_wave);
+    cudaFree(c->sw.d_sb);
+    cudaFree(c->sw.d_tiles);
+    cudaFree(c->sw.d_sync);
+    cudaFree(c->sw.d_sk[0]);
+    cudaFree(c->sw.d_sk[1]);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -543,6 +548,16 @@ static int sporlx(Ctx &c, int ilev, const Coef &A, double *f, const double *b, d
     return 0;
 }
 
+// A NaN or Inf in the system or the iterate makes every norm comparison of
+// the reference's control flow false (smooth.F, lmg_solve.F:82), which would
+// end the solve silently: report it instead
+static int check_norms(const double *nrm, int ilev)
+{
+    for (int q = 0; q < 4; q++)
+        if (!std::isfinite(nrm[q])) return set_err(LES_ERR_NONFINITE, "non-finite norm at level %d", ilev);
+    return 0;
+}
+
 // code/smooth.F:5-105
 static int smooth(Ctx &c, int ilev, const Coef &A, double *f, const double *b, double *residu,
                   int nsmooth, double omega, double soltol, double *nrm)
@@ -550,6 +565,7 @@ static int smooth(Ctx &c, int ilev, const Coef &A, double *f, const double *b, d
     int r;
     if (ilev == 1 || ilev == c.nummgl) {
         if ((r = norms_level(c, ilev, A, f, b, residu, nrm))) return r;
+        if ((r = check_norms(nrm, ilev))) return r;
     } else {
         nrm[2] = 1.;
         nrm[3] = 1.;
@@ -558,8 +574,10 @@ static int smooth(Ctx &c, int ilev, const Coef &A, double *f, const double *b, d
     while (nrm[2] / nrm[3] > soltol && ismooth < nsmooth) {
         ismooth++;
         if ((r = sporlx(c, ilev, A, f, b, omega, soltol, nrm))) return r;
-        if (ismooth == nsmooth)
+        if (ismooth == nsmooth) {
             if ((r = norms_level(c, ilev, A, f, b, residu, nrm))) return r;
+            if ((r = check_norms(nrm, ilev))) return r;
+        }
     }
     return 0;
 }
@@ -578,6 +596,7 @@ static int lmg_reference(Ctx &c, const Coef &A, double *f, double *b, double *re
     if (!c.d_nrm3) LES_CUDA(cudaMalloc(&c.d_nrm3, sizeof(double) * 3 * c.tot3));
     int r;
     if ((r = norms_level(c, 1, A, f, b, residu, nrm[1]))) return r;
+    if ((r = check_norms(nrm[1], 1))) return r;
     nummg_l[1] = m.nummgits;
     int ilev = 1, cycles = 0;
     while (nummg_l[1] > 0 && nrm[1][2] / nrm[1][3] > m.tolf) {
@@ -1053,6 +1072,8 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
     STAGE_CHECK("initial residual");
     if ((r = sync_small(c, 2))) return r;
     double r2 = c.h_small[0], b2 = c.h_small[1];
+    if (!std::isfinite(r2) || !std::isfinite(b2))
+        return set_err(LES_ERR_NONFINITE, "non-finite initial residual or source");
     int it = 0;
     double rel = b2 > 0 ? std::sqrt(r2 / b2) : 0.;
     CycleGraph *Gs = c.cg[sizeof(T) == 4 ? 1 : 0];

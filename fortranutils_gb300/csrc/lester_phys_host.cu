@@ -72,6 +72,201 @@ static int ensure_phys_tables(Ctx &c)
     return 0;
 }
 
+// Tiles and skew geometry of the tiled scalar sweep (k_sweep.cu), built on
+// first use.  A block's interior rows are split into as few tiles of at
+// most kSweepThreads rows as possible; one tile per (block, interior layer
+// k, row range), in ticket order (k, row range, block): every tile comes
+// after the two it waits for, (k-1, same rows) and (k, rows below).
+static int ensure_sweep_tiles(Ctx &c)
+{
+    Ctx::SweepState &W = c.sw;
+    if (W.d_sb) return 0;
+    const int nb = c.g.numbl;
+    std::vector<SkewBlk> sb(nb);
+    long s3 = 0, s2 = 0;
+    int maxk = 0, maxnj = 0;
+    std::vector<int> nJ(nb);
+    for (int b = 1; b <= nb; b++) {
+        SkewBlk &q = sb[b - 1];
+        memset(&q, 0, sizeof q);
+        const int *n = c.lv[1].n[b];
+        for (int d = 0; d < 3; d++) {
+            q.n[d] = n[d];
+            W.maxn[d] = std::max(W.maxn[d], n[d]);
+        }
+        for (int s6 = 0; s6 < 6; s6++) q.bc[s6] = c.g.bl_bc[b - 1][s6];
+        q.vp = (n[1] + 3) & ~3;
+        q.off3 = c.lv[1].off3[b];
+        q.off2 = c.lv[1].off2[b];
+        q.off1k = c.lv[1].off1k[b];
+        q.layer = (long)(n[0] + n[1] - 1) * q.vp;
+        q.sk3 = s3;
+        s3 += q.layer * n[2];
+        q.sk2 = s2;
+        s2 += q.layer;
+        const int rows = n[1] - 2;
+        nJ[b - 1] = (rows + kSweepThreads - 1) / kSweepThreads;
+        maxk = std::max(maxk, n[2]);
+        maxnj = std::max(maxnj, nJ[b - 1]);
+    }
+    W.tot3 = s3;
+    W.tot2 = s2;
+    // tile index of (block, k, J), -1 where none
+    auto key = [&](int b, int k, int J) { return ((long)k * maxnj + J) * nb + b; };
+    std::vector<int> idx((size_t)(maxk + 1) * maxnj * nb, -1);
+    std::vector<SweepTile> tiles;
+    for (int k = 2; k < maxk; k++)
+        for (int J = 0; J < maxnj; J++)
+            for (int b = 0; b < nb; b++) {
+                const int *n = c.lv[1].n[b + 1];
+                if (k > n[2] - 1 || J >= nJ[b]) continue;
+                const int rows = n[1] - 2, NJ = nJ[b];
+                SweepTile T;
+                T.blk = b;
+                T.k = k;
+                T.j0 = 2 + (int)((long)rows * J / NJ);
+                T.j1 = 2 + (int)((long)rows * (J + 1) / NJ);
+                T.up_k = k - 1 >= 2 ? idx[key(b, k - 1, J)] : -1;
+                T.up_j = J > 0 ? idx[key(b, k, J - 1)] : -1;
+                idx[key(b, k, J)] = (int)tiles.size();
+                tiles.push_back(T);
+            }
+    W.ntile = (int)tiles.size();
+    // ring row width: rows j0-2 .. j1+1 from a chunk boundary (16 bytes:
+    // 2 doubles or 4 floats)
+    for (int q = 0; q < 2; q++) {
+        const int E = q == 0 ? 2 : 4;
+        int w = 0;
+        for (const SweepTile &T : tiles) {
+            const int n1 = c.lv[1].n[T.blk + 1][1];
+            const int sbase = (std::max(0, T.j0 - 3) / E) * E;
+            const int hi = (std::min(n1, T.j1 + 1) + E - 1) / E * E;
+            w = std::max(w, hi - sbase);
+        }
+        W.sw[q] = w;
+    }
+    LES_CUDA(cudaMalloc(&W.d_sb, sizeof(SkewBlk) * nb));
+    LES_CUDA(cudaMemcpy(W.d_sb, sb.data(), sizeof(SkewBlk) * nb, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMalloc(&W.d_tiles, sizeof(SweepTile) * std::max(1, W.ntile)));
+    LES_CUDA(cudaMemcpy(W.d_tiles, tiles.data(), sizeof(SweepTile) * W.ntile, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMalloc(&W.d_sync, sizeof(int) * (W.ntile + 2)));
+    return 0;
+}
+
+// Which scalar sweep runs (ctrl.sc1_sweep): 1 the hyperplane sweep, 2 the
+// tile pipeline, 3 one launch per plane; 0 the tile pipeline where its
+// shared-memory ring fits, else the hyperplane sweep.  Negative: an error.
+static int sweep_choice(Ctx &c)
+{
+    const int m = c.c.sc1_sweep;
+    if (m == 1 || m == 3) return m;
+    int r;
+    if ((r = ensure_sweep_tiles(c))) return r;
+    Ctx::SweepState &W = c.sw;
+    const int q = phys32_on(c) ? 1 : 0;
+    if (W.maxctas[q][c.c.exact ? 1 : 0] == 0) {
+        // occupancy with the ring of this build (first call, never inside a
+        // capture: the first step of a run is launched)
+        int n = phys32_on(c) ? les_f32::sweep_tiles_max_ctas(W.sw[1])
+                : c.c.exact ? les_exact::sweep_tiles_max_ctas(W.sw[0]) : les_fast::sweep_tiles_max_ctas(W.sw[0]);
+        W.maxctas[q][c.c.exact ? 1 : 0] = n > 0 ? n : -1;
+    }
+    const bool fits = W.maxctas[q][c.c.exact ? 1 : 0] > 0 && W.ntile > 0;
+    if (m == 2 && !fits)
+        return set_err(LES_ERR_SIZE, "set_sc1: the tile pipeline's shared-memory ring does not fit (%d rows)", W.sw[q]);
+    return fits ? 2 : 1;
+}
+
+// The tile pipeline on skewed copies of storage type S (q = 0 FP64, 1 FP32)
+template <typename S>
+static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, const double *rdkp, int q,
+                           void (*skew)(const SkewBlk *, int, int, int, int, int, const SkewPtrs<S> &, int,
+                                        cudaStream_t),
+                           void (*unskew)(const SkewBlk *, int, int, int, int, const S *, const S *, double *,
+                                          double *, cudaStream_t),
+                           cudaError_t (*launch)(const SweepArgs<S> &, double, long, int, cudaStream_t))
+{
+    Ctx::SweepState &W = c.sw;
+    const int nb = c.g.numbl;
+    const bool fast = !c.c.exact;
+    if (!W.d_sk[q]) {
+        const size_t bytes = sizeof(S) * (8 * W.tot3 + 10 * W.tot2);
+        if (cudaMalloc(&W.d_sk[q], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            W.d_sk[q] = nullptr;
+            return set_err(LES_ERR_NOMEM, "set_sc1: skewed copies (%zu bytes)", bytes);
+        }
+    }
+    S *base = (S *)W.d_sk[q];
+    SkewPtrs<S> P3, P2;
+    memset(&P3, 0, sizeof P3);
+    memset(&P2, 0, sizeof P2);
+    const double *f3[8] = {A.sc1, A.hsc1, A.u, A.v, A.w, A.rho, A.gamsc1, A.gamlam};
+    for (int f = 0; f < 8; f++) {
+        P3.src[f] = f3[f];
+        P3.dst[f] = base + f * W.tot3;
+    }
+    const double *f2[10] = {A.m[MW_DIU], A.m[MW_DJV], A.m[MW_RDJU], A.m[MW_RDIV], A.m[MW_RP],
+                            A.m[MW_DIDJP], A.m[MW_RDIDJP], rtab[0], rtab[1], rtab[2]};
+    const int n2 = fast ? 10 : 7;
+    for (int f = 0; f < n2; f++) {
+        P2.src[f] = f2[f];
+        P2.dst[f] = base + 8 * W.tot3 + f * W.tot2;
+    }
+    skew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], 8, P3, 0, c.stream);
+    skew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], n2, P2, 1, c.stream);
+    SweepArgs<S> a;
+    memset(&a, 0, sizeof a);
+    a.sb = W.d_sb;
+    a.tiles = W.d_tiles;
+    a.ntile = W.ntile;
+    a.sw = W.sw[q];
+    for (int f = 0; f < 8; f++) a.f3[f] = P3.dst[f];
+    for (int f = 0; f < n2; f++) a.f2[f] = P2.dst[f];
+    a.dkp = A.dkp;
+    a.dkw = A.dkw;
+    a.rdkp = rdkp;
+    a.grad = A.grad;
+    a.gstride = A.gstride;
+    a.gm = A.gm;
+    a.link = A.link;
+    a.flags = W.d_sync;
+    a.ticket = W.d_sync + W.ntile;
+    a.err = W.d_sync + W.ntile + 1;
+    LES_CUDA(cudaMemsetAsync(W.d_sync, 0, sizeof(int) * (W.ntile + 2), c.stream));
+    const int nctas = std::min(W.ntile, W.maxctas[q][c.c.exact ? 1 : 0]);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (c.prof && !c.capturing) {
+        prof_pair(c, LES_PROF_SWEEP, &e0, &e1);
+        cudaEventRecord(e0, c.stream);
+    }
+    LES_CUDA(launch(a, c.c.dtime, wait_polls(c), nctas, c.stream));
+    if (e1) cudaEventRecord(e1, c.stream);
+    unskew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], P3.dst[0], P3.dst[1], A.sc1, A.hsc1, c.stream);
+    if (c.capturing) {
+        // a replayed step reads the wait's flag with its other status
+        launch_copy_flag(a.err, c.d_loop + 6, c.stream);
+    } else {
+        int err = 0;
+        LES_CUDA(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+        LES_CUDA(cudaStreamSynchronize(c.stream));
+        if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: a tile of the scalar sweep timed out waiting for its neighbour");
+    }
+    return 0;
+}
+
+static int sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, const double *rdkp)
+{
+    if (phys32_on(c))
+        return run_sweep_tiles<float>(c, A, rtab, rdkp, 1, les_f32::launch_sweep_skew, les_f32::launch_sweep_unskew,
+                                      les_f32::launch_sweep_tiles);
+    if (c.c.exact)
+        return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_exact::launch_sweep_skew,
+                                       les_exact::launch_sweep_unskew, les_exact::launch_sweep_tiles);
+    return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_fast::launch_sweep_skew, les_fast::launch_sweep_unskew,
+                                   les_fast::launch_sweep_tiles);
+}
+
 static int wave_range(Ctx &c, int &smin, int &smax)
 {
     smin = 6;
@@ -491,6 +686,7 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
     LevelGeom &L = c.lv[1];
     int smin, smax;
     wave_range(c, smin, smax);
+    const double *rtab[3] = {nullptr, nullptr, nullptr}, *rdkp = nullptr;  // FP64 reciprocals (fast builds)
     if (!c.c.exact) {
         tab_reset(c);
         const double *src2[3] = {A.m[MW_DIU], A.m[MW_DJV], A.m[MW_RP]}, *o2[3], *o1[1];
@@ -500,6 +696,14 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
         A.r[MW_DJV] = o2[1];
         A.r[MW_RP] = o2[2];
         A.rdkp = o1[0];
+        for (int q = 0; q < 3; q++) rtab[q] = o2[q];
+        rdkp = o1[0];
+    }
+    if ((r = sweep_choice(c)) < 0) return r;
+    if (r == 2) {
+        if ((r = sweep_tiles(c, A, rtab, rdkp))) return r;
+        launch_halo(L.d_face, L.nface, L.maxface, A.sc1, c.d_work, c.stream);
+        return st.finish();
     }
     if (phys32_on(c)) {
         phys32_reset(c);
@@ -514,7 +718,9 @@ int lester_set_sc1(const double *u, const double *v, const double *w, const doub
     // the whole sweep as one cooperative launch with a grid barrier per
     // plane; per-plane launches where the device cannot co-schedule it
     int smem = (int)sizeof(int) * (c.nslice + 1);
-    int maxctas = smem <= 48 * 1024 ? LES_PHYS(c, sc1_sweep_max_ctas)(smem) : 0;
+    int maxctas = smem <= 48 * 1024 && c.c.sc1_sweep != 3 ? LES_PHYS(c, sc1_sweep_max_ctas)(smem) : 0;
+    if (c.c.sc1_sweep == 1 && maxctas <= 0)
+        return set_err(LES_ERR_SIZE, "set_sc1: the hyperplane sweep does not fit as one cooperative launch");
     if (maxctas > 0) {
         LES_CUDA(cudaMemsetAsync(c.d_wave, 0, sizeof(WaveSync), c.stream));
         cudaEvent_t e0 = nullptr, e1 = nullptr;

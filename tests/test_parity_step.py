@@ -10,9 +10,11 @@ reproduce it bitwise.
 import numpy as np
 import pytest
 
+from fortranutils_gb300 import grid
 from fortranutils_gb300 import lester as L
 
 import cases
+import oracle_lib as O
 
 pytestmark = pytest.mark.gpu
 
@@ -167,3 +169,73 @@ def test_set_sc1var(env):
     L.set_sc1var(None, None, None, dev(sc1), None, d, None, md["dip"], md["djp"], dev(s.dkp),
                  dev(s.dkw), md["rp"])
     close(host(d), ref, s.exact)
+
+
+def scalar_fields(case, rng):
+    n = case.n3_sg
+    sc1 = rng.uniform(0.0, 1.0, n)
+    gs1 = rng.uniform(0.0, 1e-3, n)
+    gl = np.full(n, 1e-4)
+    hs = rng.standard_normal(n) * 1e-3
+    u, v, w = (rng.standard_normal(n) * 0.5 for _ in range(3))
+    u[::7] = 0.0
+    rho = rng.uniform(0.8, 1.2, n)
+    return sc1, gs1, gl, hs, u, v, w, rho
+
+
+def run_sweep(case, m, dkp, dkw, f, ctrl):
+    """set_gamsc1_bc then set_sc1 with the given controls; (sc1, hsc1)."""
+    sc1, gs1, gl, hs, u, v, w, rho = f
+    L.gpu_init(case.geom(), ctrl)
+    try:
+        md = {k: dev(val) for k, val in m.items()}
+        gd, ld = dev(gs1), dev(gl)
+        L.set_gamsc1_bc(dev(sc1), gd, ld, md["diu"], md["djv"], dev(dkp), md["rp"])
+        scd, hsd = dev(sc1), dev(hs)
+        L.set_sc1(dev(u), dev(v), dev(w), None, scd, dev(rho), gd, ld, hsd, md, dev(dkp), dev(dkw))
+        return host(scd), host(hsd)
+    finally:
+        L.gpu_finalize()
+
+
+SWEEP_CASES = {
+    # the benchmarked layout at 1/16 of the cells: 30 layers of tiles
+    "mixing64": lambda: grid.box_case(64, 48, 32, lx=7.5, ly=7.5, lz=3.75, ybc=L.BCT_ZERO_GRAD, beta=2.0),
+    # more rows than one tile holds: two tiles per layer, chained in j
+    "rows300": lambda: grid.box_case(12, 300, 6, ybc=L.BCT_WALL),
+    # uneven blocks joined by interfaces (interface gradients at tile edges)
+    "two_block": lambda: grid.two_block_case(12, 8, 8, 6),
+}
+
+
+@pytest.mark.parametrize("build", ["exact", "fast", "f32"])
+@pytest.mark.parametrize("name", list(SWEEP_CASES))
+def test_scalar_sweep_variants(name, build, gpulib):
+    """The tile pipeline (ctrl.sc1_sweep 2), the hyperplane sweep (1) and
+    per-plane launches (3) give the same in-place update: bitwise in the
+    exact build and equal to the oracle; the fast and FP32 builds within
+    rounding of the hyperplane sweep of the same build."""
+    case = SWEEP_CASES[name]()
+    orc = O.Oracle(case)
+    x, y, z = case.coordinates()
+    met, dkp, dkw = orc.comp_metric(x, y, z)
+    m = cases.metrics_dict(met)
+    f = scalar_fields(case, np.random.default_rng(17))
+    kw = dict(dtime=0.01, **K)
+    kw.update(exact=1) if build == "exact" else kw.update(exact=0, phys32=int(build == "f32"))
+    got = {sw: run_sweep(case, m, dkp, dkw, f, L.default_ctrl(sc1_sweep=sw, **kw)) for sw in (1, 2, 3)}
+    for q in (0, 1):
+        assert np.array_equal(got[1][q], got[3][q])
+    if build == "exact":
+        sc1, gs1, gl, hs, u, v, w, rho = f
+        g_ref, l_ref = gs1.copy(), gl.copy()
+        orc.set_gamsc1_bc(K["visc"], sc1, g_ref, l_ref, m, dkp)
+        sc_ref, hs_ref = sc1.copy(), hs.copy()
+        orc.set_sc1(0.01, m, dkp, dkw, u, v, w, sc_ref, hs_ref, rho, g_ref, l_ref)
+        assert np.array_equal(got[1][0], sc_ref) and np.array_equal(got[1][1], hs_ref)
+        assert np.array_equal(got[2][0], sc_ref) and np.array_equal(got[2][1], hs_ref)
+        return
+    tol = 1e-12 if build == "fast" else 2e-6
+    for q in (0, 1):
+        a, b = got[2][q], got[1][q]
+        assert np.linalg.norm(a - b) <= tol * np.linalg.norm(b), (q, np.linalg.norm(a - b) / np.linalg.norm(b))
