@@ -194,8 +194,8 @@ struct SkewBlk {
 };
 
 // one tile: block, layer k (2..nkp1-1), own rows j0..j1-1, and the tiles
-// whose progress it waits for: (block, k-1, same rows) and (block, k,
-// rows below), -1 where there is none
+// whose new values it reads: (block, k-1, same rows) and (block, k, rows
+// below), -1 where there is none (they come before it in ticket order)
 struct SweepTile {
     int blk, k, j0, j1, up_k, up_j;
 };
@@ -214,14 +214,14 @@ template <typename S> struct SweepArgs {
     const SkewBlk *sb;
     const SweepTile *tiles;
     int ntile, sw;           // tiles; ring row width (elements)
-    S *f3[8];                // skewed sc1 hsc1 u v w rho gamsc1 gamlam (sc1, hsc1 updated)
+    S *f3[8];                // skewed sc1 hsc1 u v w rho gamsc1 gamlam (old values; hsc1 updated)
+    S *scnew;                // skewed new values of sc1 (interior: -1 until computed)
     const S *f2[10];         // skewed diu djv rdju rdiv rp didjp rdidjp (+ 1/diu 1/djv 1/rp)
     const double *dkp, *dkw, *rdkp;
     const double *grad;      // interface gradients (set_gamsc1_bc planes)
     long gstride;
     int gm;
     const int *link;         // bl2bl, 0-based, 6 per block
-    int *flags;              // per tile: last plane done (released)
     int *ticket;             // next tile to take
     int *err;                // a bounded wait gave up
 };

@@ -9,16 +9,21 @@
 //
 //  * a tile is (block, layer k, rows j0..j1-1); one CTA walks its planes t
 //    in order, one thread per row, a __syncthreads between planes;
-//  * tile (k, J) may compute plane t once tile (k-1, J) has finished plane t
-//    and tile (k, J-1) plane t-1: point-to-point progress flags (acquire /
-//    release, bounded waits) replace grid-wide barriers, and the tiles run
-//    as a wavefront: the chain is one tile per layer and row range;
+//  * tile (k, J) needs the new values of plane t of layers k-1 and k-2 and
+//    of planes t-1, t-2 of rows j0-1, j0-2 (tile (k, J-1)); every other
+//    value it reads is an old one.  Old values come from a read-only skewed
+//    copy of sc1; new values are written to a second skewed array whose
+//    interior starts as a sentinel (-1, below the scalar's clamp at 0), so
+//    a tile simply checks each new value it staged and re-reads it from L2
+//    until it is no longer the sentinel (bounded).  No flags, no fences, no
+//    anti-dependences: the tiles run as a wavefront one layer apart, in
+//    ticket order (every tile waits only on tiles with smaller tickets);
 //  * every field is first copied into a skewed layout (k_skew), in which
 //    plane t of a layer is one contiguous vector over j, so a tile stages
 //    the vectors of the planes it will need with coalesced 16-byte cp.async
 //    copies into a shared-memory ring, D planes ahead; the new values go
-//    back into the skewed scalar array (read by the next layer) and are
-//    copied to the FP64 fields at the end (k_unskew).
+//    to the new-value array and to the ring (read by later planes of the
+//    tile) and are copied to the FP64 fields at the end (k_unskew).
 //
 // The arithmetic per point is that of sc1_cell in k_phys.cu, operand for
 // operand, so the exact build (FP64, -fmad=false) equals the hyperplane
@@ -46,12 +51,14 @@ enum {
     V_SCP1, V_RHOP1, V_GSP1, V_GLP1, V_WP1, V_SCP2,
     V_DIU, V_DJV, V_RDJU, V_RDIV, V_RP, V_DIDJP, V_RDIDJP,
     V_RDIU, V_RDJV, V_RRP,
+    V_SCH,  // own layer, rows j0-2, j0-1 of the tile below (new values)
     V_N
 };
 
 // per vector: source (0..7 a 3-D field: sc1 hsc1 u v w rho gamsc1 gamlam;
-// 8 + q the 2-D table q), layer offset, and the plane window [t+lo, t+hi]
-// a point of plane t reads
+// 8 + q the 2-D table q; 18 the new-value array), layer offset, and the
+// plane window [t+lo, t+hi] a point of plane t reads.  SCM1 and SCM2 read
+// the new-value array where their layer is an interior one.
 struct VecDesc {
     int src, dk, lo, hi;
 };
@@ -64,28 +71,44 @@ __host__ __device__ constexpr VecDesc vdesc(int v)
         {0, 1, 0, 0}, {5, 1, 0, 0}, {6, 1, 0, 0}, {7, 1, 0, 0}, {4, 1, 0, 0}, {0, 2, 0, 0},
         {8, 0, -1, 2}, {9, 0, -1, 2}, {10, 0, 0, 1}, {11, 0, 0, 1}, {12, 0, 0, 0}, {13, 0, 0, 0},
         {14, 0, 0, 0},
-        {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0}};
+        {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0},
+        {18, 0, -2, -1}};
     return d[v];
 }
 // ring slots of vector v for prefetch distance D: planes t+lo .. t+hi+D
 __host__ __device__ constexpr int vslots(int v, int D) { return vdesc(v).hi - vdesc(v).lo + D + 1; }
-__host__ __device__ constexpr int nvec(bool fast) { return fast ? V_N : V_RDIU; }
+// vectors of a build: the exact build has no reciprocal tables
+__host__ __device__ constexpr bool has_vec(bool fast, int v) { return fast || v < V_RDIU || v > V_RRP; }
 __host__ __device__ constexpr int ring_slots(bool fast, int D)
 {
     int s = 0;
-    for (int v = 0; v < nvec(fast); v++) s += vslots(v, D);
+    for (int v = 0; v < V_N; v++)
+        if (has_vec(fast, v)) s += vslots(v, D);
     return s;
 }
 
-__device__ __forceinline__ int ld_acquire(const int *p)
+// the new-value array's initial value: the scalar is clamped to [0, 1]
+constexpr float kSentinel = -1.0f;
+
+__device__ __forceinline__ float ld_strong(const float *p)
 {
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    float v;
+    asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release(int *p, int v)
+__device__ __forceinline__ double ld_strong(const double *p)
 {
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_strong(float *p, float v)
+{
+    asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_strong(double *p, double v)
+{
+    asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
@@ -96,22 +119,24 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Wait until *flag >= need (thread 0 of the CTA); bounded: after `limit`
-// polls, or once another CTA has set *err, give up (returns false).
-__device__ bool wait_flag(const int *flag, int need, int &seen, int *err, long limit)
+// A new value staged from the new-value array: while it is still the
+// sentinel, re-read it from L2 (another CTA is computing it); bounded by
+// `limit` polls, or until another CTA has set *err (then *err is set and
+// the staged value returned: the call reports LES_ERR_TIMEOUT).
+template <typename S>
+__device__ S fresh(S v, const S *g, int *err, long limit)
 {
     long it = 0;
-    while (seen < need) {
-        seen = ld_acquire(flag);
-        if (seen >= need) break;
-        if (*(volatile int *)err) return false;
+    while (v == (S)kSentinel) {
+        if (*(volatile int *)err) return v;
         if (++it > limit) {
             atomicExch(err, 1);
-            return false;
+            return v;
         }
-        __nanosleep(64);
+        __nanosleep(32);
+        v = ld_strong(g);
     }
-    return true;
+    return v;
 }
 
 // ------------------------------------------------------------------ skew
@@ -190,6 +215,13 @@ __global__ void __launch_bounds__(256) k_unskew(const SkewBlk *__restrict__ sb, 
     }
 }
 
+// the new-value array's initial state
+template <typename S> __global__ void k_fill_sentinel(S *__restrict__ p, long n)
+{
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
+        p[e] = (S)kSentinel;
+}
+
 // ----------------------------------------------------------- the pipeline
 // R: arithmetic type; S: storage type of the skewed copies; FAST: the
 // reciprocal tables of the fast builds; D: planes staged ahead.
@@ -199,7 +231,6 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
     extern __shared__ __align__(16) unsigned char smem_raw[];
     S *ring = (S *)smem_raw;
     __shared__ int s_tile, s_ok[2];  // s_ok by plane parity: thread 0 may write the next before all read this
-    constexpr int NV = nvec(FAST);
     constexpr int E = 16 / sizeof(S);  // elements per 16-byte chunk
     const R lambda = (R)4.0, small = (R)1.e-30, half = (R)0.5, one = (R)1.0, zero = (R)0.0;
     const R dtime = (R)dtime_d;
@@ -218,6 +249,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
         const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
         const int k = T.k, j0 = T.j0, j1 = T.j1;
         const int ni = n0 - 1, nj = n1 - 1, nk = n2 - 1;
+        const bool jhalo = T.up_j >= 0;  // rows j0-2, j0-1 belong to another tile
         // staged rows: j0-2 .. j1+1 (0-based jr), chunk aligned
         const int sbase = (max(0, j0 - 3) / E) * E;
         const int jr_lo = max(0, j0 - 3), jr_hi = min(n1, j1 + 1);  // [lo, hi)
@@ -239,37 +271,56 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
             rdkp_m1 = (R)rdkp[k - 1];
             rdkp_0 = k < nk ? (R)rdkp[k] : zero;
         }
-        int seen_k = 0, seen_j = 0;
         // ring offsets (compile-time slot counts)
         auto voff = [&](int v) {
             int o = 0;
 #pragma unroll
-            for (int u = 0; u < NV; u++)
-                if (u < v) o += vslots(u, D);
+            for (int u = 0; u < V_N; u++)
+                if (u < v && has_vec(FAST, u)) o += vslots(u, D);
             return o * SW;
         };
-        auto at = [&](int v, int p, int jj) -> R {
-            return (R)ring[voff(v) + (p % vslots(v, D)) * SW + (jj - 1 - sbase)];
+        auto slot = [&](int v, int p, int jj) -> S & {
+            return ring[voff(v) + (p % vslots(v, D)) * SW + (jj - 1 - sbase)];
+        };
+        auto at = [&](int v, int p, int jj) -> R { return (R)slot(v, p, jj); };
+        // element (plane p, row jj) of layer kv in a skewed 3-D array
+        auto e3 = [&](int kv, int p, int jj) -> long {
+            return b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp + (jj - 1);
+        };
+        // a new value of layer kv at (p, jj), staged in vector v
+        auto newval = [&](int v, int kv, int p, int jj) -> R {
+            return (R)fresh<S>(slot(v, p, jj), A.scnew + e3(kv, p, jj), A.err, limit);
         };
         // issue the copies of group t: plane t + D + hi of every vector
         auto issue = [&](int t) {
 #pragma unroll
-            for (int v = 0; v < NV; v++) {
+            for (int v = 0; v < V_N; v++) {
+                if (!has_vec(FAST, v)) continue;
                 const VecDesc vd = vdesc(v);
                 const int p = t + D + vd.hi;
                 if (p < t0 + vd.lo || p > t1 + vd.hi || p < 2 || p > n0 + n1) continue;
                 const int kv = k + vd.dk;
                 if (kv < 1 || kv > n2) continue;
+                if (v == V_SCH && !jhalo) continue;
                 const bool cross = vd.dk != 0;
-                // rows: valid i = p - j in 1..n0; cross-layer vectors own rows only
-                int lo = max(cross ? j0 - 1 : jr_lo, p - n0 - 1), hi = min(cross ? j1 - 1 : jr_hi, p - 1);
+                // rows: valid i = p - j in 1..n0; cross-layer vectors own
+                // rows only, the halo vector rows j0-2, j0-1
+                int lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
+                int hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
+                lo = max(lo, p - n0 - 1);
+                hi = min(hi, p - 1);
                 if (lo >= hi) continue;
                 const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
                 const S *g;
-                if (vd.src < 8)
-                    g = A.f3[vd.src] + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
-                else
+                if (vd.src < 8) {
+                    // new values of an interior layer below from the new-value array
+                    const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
+                    g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
+                } else if (vd.src < 18) {
                     g = A.f2[vd.src - 8] + b.sk2 + (long)(p - 2) * b.vp;
+                } else {
+                    g = A.scnew + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
+                }
                 S *dst = ring + voff(v) + (p % vslots(v, D)) * SW - sbase;
                 for (int c = c_lo + tid; c < c_hi; c += blockDim.x) cp_async16(dst + c * E, g + c * E);
             }
@@ -277,23 +328,12 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
         const int ts = t0 - D - 4;
         bool ok = true;
         for (int t = ts; t <= t1; t++) {
-            // progress needed before group t: cross planes t + D of layer k-1
-            // (and k-2 through it), own planes t + D + 2 of rows j0-2, j0-1
-            if (tid == 0) {
-                bool g = true;
-                if (T.up_k >= 0 && t + D >= t0) g = wait_flag(A.flags + T.up_k, t + D, seen_k, A.err, limit);
-                if (g && T.up_j >= 0) g = wait_flag(A.flags + T.up_j, t + D + 2, seen_j, A.err, limit);
-                s_ok[t & 1] = g;
-            }
+            if (tid == 0) s_ok[t & 1] = !*(volatile int *)A.err;
             if (t >= t0) cp_async_wait<D - 1>();
             __syncthreads();
             if (!s_ok[t & 1]) {
                 ok = false;
                 break;
-            }
-            if (tid == 0 && t - 1 >= 2) {
-                __threadfence();
-                st_release(A.flags + tix, t - 1);
             }
             issue(t);
             cp_async_commit();
@@ -321,8 +361,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
             const R wlf = at(V_W, t, j), wrf = at(V_WP1, t, j);
             const R s0 = at(V_SC, t, j);
             const R sw = at(V_SC, t - 1, j), se = at(V_SC, t + 1, j);
-            const R ss = at(V_SC, t - 1, j - 1), sn = at(V_SC, t + 1, j + 1);
-            const R sl = at(V_SCM1, t, j), sr = at(V_SCP1, t, j);
+            const R ss = (jhalo && j == j0) ? newval(V_SCH, k, t - 1, j - 1) : at(V_SC, t - 1, j - 1);
+            const R sn = at(V_SC, t + 1, j + 1);
+            const R sl = k - 1 >= 2 ? newval(V_SCM1, k - 1, t, j) : at(V_SCM1, t, j);
+            const R sr = at(V_SCP1, t, j);
 #define QD(x, v, pp, jj) (FAST ? (x) * at(v##_R, pp, jj) : (x) / at(v, pp, jj))
 #define V_DIU_R V_RDIU
 #define V_DJV_R V_RDJV
@@ -352,7 +394,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
                               ? dfdysf
                               : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
             else
-                dfdyssf = QD(ss - at(V_SC, t - 2, j - 2), V_DJV, t - 1, j - 1);
+                dfdyssf = QD(ss - ((jhalo && j - 2 < j0) ? newval(V_SCH, k, t - 2, j - 2) : at(V_SC, t - 2, j - 2)),
+                             V_DJV, t - 1, j - 1);
             if (j == nj)
                 dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D)
                               ? dfdynf
@@ -372,7 +415,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
                               ? dfdzlf
                               : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
             else
-                dfdzllf = QZ(sl - at(V_SCM2, t, j), dkp_m3, rdkp_m3);
+                dfdzllf = QZ(sl - (k - 2 >= 2 ? newval(V_SCM2, k - 2, t, j) : at(V_SCM2, t, j)), dkp_m3, rdkp_m3);
             if (k == nk)
                 dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D)
                               ? dfdzrf
@@ -435,20 +478,17 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
             R tmp = s0 + dtime / (vol * rhop) * ((R)1.5 * h - half * at(V_H, t, j));
             if (tmp < zero) tmp = zero;
             if (tmp > one) tmp = one;
-            // in place: the ring slot of plane t (read as new by later
-            // planes), the skewed scalar (read by layer k+1) and history
-            ring[voff(V_SC) + (t % vslots(V_SC, D)) * SW + (j - 1 - sbase)] = (S)tmp;
-            const long e = b.sk3 + b.layer * (k - 1) + (long)(t - 2) * b.vp + (j - 1);
-            A.f3[0][e] = (S)tmp;
+            // the new value: in the ring slot of plane t (read by later
+            // planes of this tile) and in the new-value array (read by the
+            // layers above and the tile above); the history in place
+            slot(V_SC, t, j) = (S)tmp;
+            const long e = e3(k, t, j);
+            st_strong(A.scnew + e, (S)tmp);
             A.f3[1][e] = (S)h;
         }
         cp_async_wait_all();
         __syncthreads();
         if (!ok) return;
-        if (tid == 0) {
-            __threadfence();
-            st_release(A.flags + tix, 0x7fffffff);  // every plane of this tile done
-        }
     }
 }
 
@@ -474,6 +514,13 @@ void launch_unskew_t(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2,
 {
     const int ntp = (maxn0 + maxn1 - 1 + 31) / 32, njt = (maxn1 + 31) / 32;
     k_unskew<S><<<dim3(ntp * njt, maxn2 > 2 ? maxn2 - 2 : 1, nb), 256, 0, st>>>(sb, sks, skh, sc1, hsc1, ntp);
+    les::count_launch(1);
+}
+
+template <typename S> void launch_fill_t(S *p, long n, cudaStream_t st)
+{
+    long g = (n + 255) / 256;
+    k_fill_sentinel<S><<<(unsigned)(g > 8192 ? 8192 : g), 256, 0, st>>>(p, n);
     les::count_launch(1);
 }
 
@@ -532,6 +579,7 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 {
     launch_unskew_t<ST>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
 }
+void launch_sweep_fill(double *p, long n, cudaStream_t st) { launch_fill_t<ST>(p, n, st); }
 int sweep_tiles_smem(int sw) { return tiles_smem<RT, ST, kFast, kSweepDepth>(sw); }
 int sweep_tiles_max_ctas(int sw) { return tiles_max_ctas<RT, ST, kFast, kSweepDepth>(sw); }
 cudaError_t launch_sweep_tiles(const SweepArgs<double> &a, double dtime, long limit, int nctas, cudaStream_t st)
@@ -555,6 +603,7 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 {
     les_fast::launch_unskew_t<float>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
 }
+void launch_sweep_fill(float *p, long n, cudaStream_t st) { les_fast::launch_fill_t<float>(p, n, st); }
 int sweep_tiles_smem(int sw) { return les_fast::tiles_smem<float, float, true, kSweepDepth>(sw); }
 int sweep_tiles_max_ctas(int sw) { return les_fast::tiles_max_ctas<float, float, true, kSweepDepth>(sw); }
 cudaError_t launch_sweep_tiles(const SweepArgs<float> &a, double dtime, long limit, int nctas, cudaStream_t st)

@@ -151,8 +151,8 @@ struct Ctx {
     int nslice = 0;
     WaveSync *d_wave = nullptr;
     // tiled scalar sweep (k_sweep.cu): per-block skew geometry, the tiles in
-    // ticket order, progress flags + ticket + error, skewed copies per
-    // storage type (FP64 for the FP64 builds, FP32 for phys32)
+    // ticket order, ticket + error, skewed copies per storage type (FP64 for
+    // the FP64 builds, FP32 for phys32)
     struct SweepState {
         SkewBlk *d_sb = nullptr;
         SweepTile *d_tiles = nullptr;
@@ -161,8 +161,8 @@ struct Ctx {
         int sw[2] = {0, 0};           // ring width [FP64, FP32]
         int maxctas[2][2] = {{0, 0}, {0, 0}};  // resident CTAs [FP64, FP32][fast, exact]; -1 none
         long tot3 = 0, tot2 = 0;      // skewed elements per 3-D field / 2-D table
-        int *d_sync = nullptr;        // flags[ntile], ticket, err
-        void *d_sk[2] = {nullptr, nullptr};  // [FP64, FP32]: 8 fields then 10 tables
+        int *d_sync = nullptr;        // ticket, error
+        void *d_sk[2] = {nullptr, nullptr};  // [FP64, FP32]: 8 fields, the new values, 10 tables
     } sw;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)

@@ -149,7 +149,7 @@ static int ensure_sweep_tiles(Ctx &c)
     LES_CUDA(cudaMemcpy(W.d_sb, sb.data(), sizeof(SkewBlk) * nb, cudaMemcpyHostToDevice));
     LES_CUDA(cudaMalloc(&W.d_tiles, sizeof(SweepTile) * std::max(1, W.ntile)));
     LES_CUDA(cudaMemcpy(W.d_tiles, tiles.data(), sizeof(SweepTile) * W.ntile, cudaMemcpyHostToDevice));
-    LES_CUDA(cudaMalloc(&W.d_sync, sizeof(int) * (W.ntile + 2)));
+    LES_CUDA(cudaMalloc(&W.d_sync, sizeof(int) * 2));  // ticket, error
     return 0;
 }
 
@@ -184,13 +184,14 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
                                         cudaStream_t),
                            void (*unskew)(const SkewBlk *, int, int, int, int, const S *, const S *, double *,
                                           double *, cudaStream_t),
+                           void (*fill)(S *, long, cudaStream_t),
                            cudaError_t (*launch)(const SweepArgs<S> &, double, long, int, cudaStream_t))
 {
     Ctx::SweepState &W = c.sw;
     const int nb = c.g.numbl;
     const bool fast = !c.c.exact;
     if (!W.d_sk[q]) {
-        const size_t bytes = sizeof(S) * (8 * W.tot3 + 10 * W.tot2);
+        const size_t bytes = sizeof(S) * (9 * W.tot3 + 10 * W.tot2);
         if (cudaMalloc(&W.d_sk[q], bytes) != cudaSuccess) {
             cudaGetLastError();
             W.d_sk[q] = nullptr;
@@ -211,7 +212,7 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     const int n2 = fast ? 10 : 7;
     for (int f = 0; f < n2; f++) {
         P2.src[f] = f2[f];
-        P2.dst[f] = base + 8 * W.tot3 + f * W.tot2;
+        P2.dst[f] = base + 9 * W.tot3 + f * W.tot2;
     }
     skew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], 8, P3, 0, c.stream);
     skew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], n2, P2, 1, c.stream);
@@ -230,10 +231,11 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     a.gstride = A.gstride;
     a.gm = A.gm;
     a.link = A.link;
-    a.flags = W.d_sync;
-    a.ticket = W.d_sync + W.ntile;
-    a.err = W.d_sync + W.ntile + 1;
-    LES_CUDA(cudaMemsetAsync(W.d_sync, 0, sizeof(int) * (W.ntile + 2), c.stream));
+    a.scnew = base + 8 * W.tot3;
+    a.ticket = W.d_sync;
+    a.err = W.d_sync + 1;
+    fill(a.scnew, W.tot3, c.stream);
+    LES_CUDA(cudaMemsetAsync(W.d_sync, 0, sizeof(int) * 2, c.stream));
     const int nctas = std::min(W.ntile, W.maxctas[q][c.c.exact ? 1 : 0]);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (c.prof && !c.capturing) {
@@ -242,7 +244,7 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     }
     LES_CUDA(launch(a, c.c.dtime, wait_polls(c), nctas, c.stream));
     if (e1) cudaEventRecord(e1, c.stream);
-    unskew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], P3.dst[0], P3.dst[1], A.sc1, A.hsc1, c.stream);
+    unskew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], a.scnew, P3.dst[1], A.sc1, A.hsc1, c.stream);
     if (c.capturing) {
         // a replayed step reads the wait's flag with its other status
         launch_copy_flag(a.err, c.d_loop + 6, c.stream);
@@ -250,7 +252,7 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
         int err = 0;
         LES_CUDA(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         LES_CUDA(cudaStreamSynchronize(c.stream));
-        if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: a tile of the scalar sweep timed out waiting for its neighbour");
+        if (err) return set_err(LES_ERR_TIMEOUT, "set_sc1: a tile of the scalar sweep timed out waiting for a new value");
     }
     return 0;
 }
@@ -259,12 +261,13 @@ static int sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, cons
 {
     if (phys32_on(c))
         return run_sweep_tiles<float>(c, A, rtab, rdkp, 1, les_f32::launch_sweep_skew, les_f32::launch_sweep_unskew,
-                                      les_f32::launch_sweep_tiles);
+                                      les_f32::launch_sweep_fill, les_f32::launch_sweep_tiles);
     if (c.c.exact)
         return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_exact::launch_sweep_skew,
-                                       les_exact::launch_sweep_unskew, les_exact::launch_sweep_tiles);
+                                       les_exact::launch_sweep_unskew, les_exact::launch_sweep_fill,
+                                       les_exact::launch_sweep_tiles);
     return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_fast::launch_sweep_skew, les_fast::launch_sweep_unskew,
-                                   les_fast::launch_sweep_tiles);
+                                   les_fast::launch_sweep_fill, les_fast::launch_sweep_tiles);
 }
 
 static int wave_range(Ctx &c, int &smin, int &smax)

@@ -214,7 +214,7 @@ def test_scalar_sweep_variants(name, build, gpulib):
     """The tile pipeline (ctrl.sc1_sweep 2), the hyperplane sweep (1) and
     per-plane launches (3) give the same in-place update: bitwise in the
     exact build and equal to the oracle; the fast and FP32 builds within
-    rounding of the hyperplane sweep of the same build."""
+    rounding of the other two variants of the same build."""
     case = SWEEP_CASES[name]()
     orc = O.Oracle(case)
     x, y, z = case.coordinates()
@@ -224,9 +224,9 @@ def test_scalar_sweep_variants(name, build, gpulib):
     kw = dict(dtime=0.01, **K)
     kw.update(exact=1) if build == "exact" else kw.update(exact=0, phys32=int(build == "f32"))
     got = {sw: run_sweep(case, m, dkp, dkw, f, L.default_ctrl(sc1_sweep=sw, **kw)) for sw in (1, 2, 3)}
-    for q in (0, 1):
-        assert np.array_equal(got[1][q], got[3][q])
     if build == "exact":
+        for q in (0, 1):
+            assert np.array_equal(got[1][q], got[3][q])
         sc1, gs1, gl, hs, u, v, w, rho = f
         g_ref, l_ref = gs1.copy(), gl.copy()
         orc.set_gamsc1_bc(K["visc"], sc1, g_ref, l_ref, m, dkp)
@@ -235,7 +235,11 @@ def test_scalar_sweep_variants(name, build, gpulib):
         assert np.array_equal(got[1][0], sc_ref) and np.array_equal(got[1][1], hs_ref)
         assert np.array_equal(got[2][0], sc_ref) and np.array_equal(got[2][1], hs_ref)
         return
+    # the builds with FMA contraction: each variant's expression trees
+    # contract differently, so they agree to rounding, not bitwise
     tol = 1e-12 if build == "fast" else 2e-6
-    for q in (0, 1):
-        a, b = got[2][q], got[1][q]
-        assert np.linalg.norm(a - b) <= tol * np.linalg.norm(b), (q, np.linalg.norm(a - b) / np.linalg.norm(b))
+    for other in (1, 3):
+        for q in (0, 1):
+            a, b = got[2][q], got[other][q]
+            err = np.linalg.norm(a - b) / np.linalg.norm(b)
+            assert err <= tol, (other, q, err)
