@@ -75,8 +75,18 @@ __host__ __device__ constexpr VecDesc vdesc(int v)
         {18, 0, -2, -1}};
     return d[v];
 }
-// ring slots of vector v for prefetch distance D: planes t+lo .. t+hi+D
-__host__ __device__ constexpr int vslots(int v, int D) { return vdesc(v).hi - vdesc(v).lo + D + 1; }
+// ring slots of vector v for prefetch distance D: planes t+lo .. t+hi+D,
+// rounded up to a power of two so that a plane's slot is (p & (slots-1))
+__host__ __device__ constexpr int pow2_ceil(int n) { return n <= 1 ? 1 : 2 * pow2_ceil((n + 1) / 2); }
+__host__ __device__ constexpr int vslots(int v, int D) { return pow2_ceil(vdesc(v).hi - vdesc(v).lo + D + 1); }
+// ring slots before vector v (compile time)
+__host__ __device__ constexpr int vprefix(bool fast, int v, int D)
+{
+    int s = 0;
+    for (int u = 0; u < v; u++)
+        if (fast || u < V_RDIU || u > V_RRP) s += vslots(u, D);
+    return s;
+}
 // vectors of a build: the exact build has no reciprocal tables
 __host__ __device__ constexpr bool has_vec(bool fast, int v) { return fast || v < V_RDIU || v > V_RRP; }
 __host__ __device__ constexpr int ring_slots(bool fast, int D)
@@ -84,6 +94,26 @@ __host__ __device__ constexpr int ring_slots(bool fast, int D)
     int s = 0;
     for (int v = 0; v < V_N; v++)
         if (has_vec(fast, v)) s += vslots(v, D);
+    return s;
+}
+
+// the same table for lookups by a runtime vector index (the producer lane)
+__constant__ VecDesc c_vdesc[V_N] = {
+    {0, 0, -2, 2}, {1, 0, 0, 0}, {2, 0, 0, 1}, {3, 0, 0, 1}, {4, 0, 0, 0}, {5, 0, -1, 1}, {6, 0, -1, 1},
+    {7, 0, -1, 1},
+    {0, -1, 0, 0}, {5, -1, 0, 0}, {6, -1, 0, 0}, {7, -1, 0, 0}, {0, -2, 0, 0},
+    {0, 1, 0, 0}, {5, 1, 0, 0}, {6, 1, 0, 0}, {7, 1, 0, 0}, {4, 1, 0, 0}, {0, 2, 0, 0},
+    {8, 0, -1, 2}, {9, 0, -1, 2}, {10, 0, 0, 1}, {11, 0, 0, 1}, {12, 0, 0, 0}, {13, 0, 0, 0},
+    {14, 0, 0, 0},
+    {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0},
+    {18, 0, -2, -1}};
+
+template <bool FAST, int D> __device__ __forceinline__ int vprefix_rt(int v)
+{
+    int s = 0;
+#pragma unroll
+    for (int u = 0; u < V_N; u++)
+        if (u < v && has_vec(FAST, u)) s += vslots(u, D);
     return s;
 }
 
@@ -110,14 +140,59 @@ __device__ __forceinline__ void st_strong(double *p, double v)
 {
     asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *m, int count)
 {
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect(unsigned long long *m, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *m, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(m)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// one contiguous global -> shared copy by the TMA unit, completing
+// `bytes` of the mbarrier's transaction count (16-byte aligned, size a
+// multiple of 16)
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *m)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(m))
+                 : "memory");
+}
+// wait for the copies of a phase to land before the ring is reused or the
+// CTA exits, even after an error elsewhere (they depend on nothing);
+// bounded by `limit` tries
+__device__ __forceinline__ void mbar_drain(unsigned long long *m, unsigned parity, int *err, long limit)
+{
+    long it = 0;
+    while (!mbar_try(m, parity))
+        if (++it > limit) {
+            atomicExch(err, 1);
+            return;
+        }
+}
+// wait for a phase of an mbarrier; bounded: after `limit` tries, or once
+// another CTA has set *err, give up (sets *err)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, int *err, long limit)
+{
+    long it = 0;
+    while (!mbar_try(m, parity)) {
+        if (++it > limit || *(volatile int *)err) {
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+    return true;
+}
 
 // A new value staged from the new-value array: while it is still the
 // sentinel, re-read it from L2 (another CTA is computing it); bounded by
@@ -225,16 +300,30 @@ template <typename S> __global__ void k_fill_sentinel(S *__restrict__ p, long n)
 // ----------------------------------------------------------- the pipeline
 // R: arithmetic type; S: storage type of the skewed copies; FAST: the
 // reciprocal tables of the fast builds; D: planes staged ahead.
+// One CTA: compute warps (one thread per row of the tile) and, last, one
+// producer warp whose lane v issues the bulk copy of staged vector v for
+// each plane.  Plane group u (the copies issued at the u-th plane step of
+// the CTA) completes mbarrier u % (D+1); the compute threads wait for group
+// u - D before plane step u, so D groups are in flight.
 template <typename R, typename S, bool FAST, int D>
-__global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
+__global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     S *ring = (S *)smem_raw;
+    constexpr int G = D + 1;
+    __shared__ __align__(8) unsigned long long mbar[G];
     __shared__ int s_tile, s_ok[2];  // s_ok by plane parity: thread 0 may write the next before all read this
     constexpr int E = 16 / sizeof(S);  // elements per 16-byte chunk
     const R lambda = (R)4.0, small = (R)1.e-30, half = (R)0.5, one = (R)1.0, zero = (R)0.0;
     const R dtime = (R)dtime_d;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nwc = (int)(blockDim.x >> 5) - 1;  // compute warps
+    const bool producer = (tid >> 5) == nwc;
+    if (tid == 0)
+        for (int g = 0; g < G; g++) mbar_init(&mbar[g], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    long ubase = 0;  // plane steps of earlier tiles (mbarrier phases continue)
     for (;;) {
         if (tid == 0) {
             int tk = -1;
@@ -256,8 +345,36 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
         const int SW = A.sw;
         // own row and the plane range
         const int j = j0 + tid;
-        const bool row = j < j1;
+        const bool row = !producer && j < j1;
         const int t0 = 2 + j0, t1 = ni + (j1 - 1);
+        const int ts = t0 - D - 4;
+        // ---- producer lane v: vector v's fixed parts
+        int pv_lo = 0, pv_hi = 0, pv_slots = 1, pv_hi_off = 0, pv_lo_off = 0;
+        const S *pv_g = nullptr;
+        S *pv_ring = nullptr;
+        bool pv_on = false;
+        if (producer && lane < V_N && has_vec(FAST, lane)) {
+            const int v = lane;
+            const VecDesc vd = c_vdesc[v];
+            const int kv = k + vd.dk;
+            pv_on = kv >= 1 && kv <= n2 && (v != V_SCH || jhalo);
+            const bool cross = vd.dk != 0;
+            pv_lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
+            pv_hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
+            pv_slots = pow2_ceil(vd.hi - vd.lo + D + 1);
+            pv_hi_off = vd.hi;
+            pv_lo_off = vd.lo;
+            if (vd.src < 8) {
+                // new values of an interior layer below come from the new-value array
+                const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
+                pv_g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1);
+            } else if (vd.src < 18) {
+                pv_g = A.f2[vd.src - 8] + b.sk2;
+            } else {
+                pv_g = A.scnew + b.sk3 + b.layer * (kv - 1);
+            }
+            pv_ring = ring + vprefix_rt<FAST, D>(v) * SW - sbase;
+        }
         // 1-D metrics of this layer
         const double *dkp = A.dkp + b.off1k, *dkw = A.dkw + b.off1k;
         const R dkw_k = (R)dkw[k - 1];
@@ -271,16 +388,10 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
             rdkp_m1 = (R)rdkp[k - 1];
             rdkp_0 = k < nk ? (R)rdkp[k] : zero;
         }
-        // ring offsets (compile-time slot counts)
-        auto voff = [&](int v) {
-            int o = 0;
-#pragma unroll
-            for (int u = 0; u < V_N; u++)
-                if (u < v && has_vec(FAST, u)) o += vslots(u, D);
-            return o * SW;
-        };
+        // ring element of vector v, plane p, row jj
+        const int rowoff = j - 1 - sbase;
         auto slot = [&](int v, int p, int jj) -> S & {
-            return ring[voff(v) + (p % vslots(v, D)) * SW + (jj - 1 - sbase)];
+            return ring[(vprefix(FAST, v, D) + (p & (vslots(v, D) - 1))) * SW + rowoff + (jj - j)];
         };
         auto at = [&](int v, int p, int jj) -> R { return (R)slot(v, p, jj); };
         // element (plane p, row jj) of layer kv in a skewed 3-D array
@@ -291,52 +402,38 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
         auto newval = [&](int v, int kv, int p, int jj) -> R {
             return (R)fresh<S>(slot(v, p, jj), A.scnew + e3(kv, p, jj), A.err, limit);
         };
-        // issue the copies of group t: plane t + D + hi of every vector
-        auto issue = [&](int t) {
-#pragma unroll
-            for (int v = 0; v < V_N; v++) {
-                if (!has_vec(FAST, v)) continue;
-                const VecDesc vd = vdesc(v);
-                const int p = t + D + vd.hi;
-                if (p < t0 + vd.lo || p > t1 + vd.hi || p < 2 || p > n0 + n1) continue;
-                const int kv = k + vd.dk;
-                if (kv < 1 || kv > n2) continue;
-                if (v == V_SCH && !jhalo) continue;
-                const bool cross = vd.dk != 0;
-                // rows: valid i = p - j in 1..n0; cross-layer vectors own
-                // rows only, the halo vector rows j0-2, j0-1
-                int lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
-                int hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
-                lo = max(lo, p - n0 - 1);
-                hi = min(hi, p - 1);
-                if (lo >= hi) continue;
-                const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
-                const S *g;
-                if (vd.src < 8) {
-                    // new values of an interior layer below from the new-value array
-                    const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
-                    g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
-                } else if (vd.src < 18) {
-                    g = A.f2[vd.src - 8] + b.sk2 + (long)(p - 2) * b.vp;
-                } else {
-                    g = A.scnew + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
-                }
-                S *dst = ring + voff(v) + (p % vslots(v, D)) * SW - sbase;
-                for (int c = c_lo + tid; c < c_hi; c += blockDim.x) cp_async16(dst + c * E, g + c * E);
-            }
-        };
-        const int ts = t0 - D - 4;
         bool ok = true;
-        for (int t = ts; t <= t1; t++) {
+        int t = ts;
+        for (; t <= t1; t++) {
+            const long u = ubase + (t - ts);
             if (tid == 0) s_ok[t & 1] = !*(volatile int *)A.err;
-            if (t >= t0) cp_async_wait<D - 1>();
+            if (!producer && u >= D) mbar_wait(&mbar[(u - D) % G], (unsigned)(((u - D) / G) & 1), A.err, limit);
             __syncthreads();
             if (!s_ok[t & 1]) {
                 ok = false;
                 break;
             }
-            issue(t);
-            cp_async_commit();
+            if (producer) {
+                // group u: plane t + D + hi of every vector, its valid rows
+                unsigned bytes = 0;
+                const S *src = nullptr;
+                S *dst = nullptr;
+                const int p = t + D + pv_hi_off;
+                if (pv_on && p >= t0 + pv_lo_off && p <= t1 + pv_hi_off && p >= 2 && p <= n0 + n1) {
+                    const int lo = max(pv_lo, p - n0 - 1), hi = min(pv_hi, p - 1);
+                    if (lo < hi) {
+                        const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
+                        bytes = (unsigned)(c_hi - c_lo) * 16u;
+                        src = pv_g + (long)(p - 2) * b.vp + c_lo * E;
+                        dst = pv_ring + (p & (pv_slots - 1)) * SW + c_lo * E;
+                    }
+                }
+                const unsigned total = __reduce_add_sync(0xffffffffu, bytes);
+                if (lane == 0) mbar_expect(&mbar[u % G], total);
+                __syncwarp();
+                if (bytes) bulk_copy(dst, src, bytes, &mbar[u % G]);
+                continue;
+            }
             if (t < t0 || !row) continue;
             const int i = t - j;
             if (i < 2 || i > ni) continue;
@@ -486,8 +583,13 @@ __global__ void __launch_bounds__(kSweepThreads) k_sc1_tiles(SweepArgs<S> A, dou
             st_strong(A.scnew + e, (S)tmp);
             A.f3[1][e] = (S)h;
         }
-        cp_async_wait_all();
+        // the groups still in flight (issued, never waited for) land before
+        // the ring is reused or the CTA exits
+        const long uend = ubase + (t - ts);  // groups issued: ubase .. uend-1
+        if (producer && lane == 0)
+            for (long w = max(ubase, uend - D); w < uend; w++) mbar_drain(&mbar[w % G], (unsigned)((w / G) & 1), A.err, limit);
         __syncthreads();
+        ubase = uend;
         if (!ok) return;
     }
 }
@@ -531,26 +633,26 @@ int tiles_smem(int sw)
 }
 
 template <typename R, typename S, bool FAST, int D>
-cudaError_t launch_tiles_t(const SweepArgs<S> &a, double dtime, long limit, int nctas, cudaStream_t st)
+cudaError_t launch_tiles_t(const SweepArgs<S> &a, double dtime, long limit, int nctas, int nthr, cudaStream_t st)
 {
     const int smem = tiles_smem<R, S, FAST, D>(a.sw);
     auto kern = k_sc1_tiles<R, S, FAST, D>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    kern<<<nctas, kSweepThreads, smem, st>>>(a, dtime, limit);
+    kern<<<nctas, nthr, smem, st>>>(a, dtime, limit);
     les::count_launch(1);
     return cudaGetLastError();
 }
 
+// resident CTAs of nthr threads with the ring for row width sw (sets the
+// kernel's dynamic shared-memory limit; called before any launch)
 template <typename R, typename S, bool FAST, int D>
-int tiles_max_ctas(int sw)
+int tiles_max_ctas(int sw, int nthr)
 {
     const int smem = tiles_smem<R, S, FAST, D>(sw);
     auto kern = k_sc1_tiles<R, S, FAST, D>;
     int dev = 0, nsm = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kSweepThreads, smem) != cudaSuccess) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, nthr, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -581,10 +683,11 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 }
 void launch_sweep_fill(double *p, long n, cudaStream_t st) { launch_fill_t<ST>(p, n, st); }
 int sweep_tiles_smem(int sw) { return tiles_smem<RT, ST, kFast, kSweepDepth>(sw); }
-int sweep_tiles_max_ctas(int sw) { return tiles_max_ctas<RT, ST, kFast, kSweepDepth>(sw); }
-cudaError_t launch_sweep_tiles(const SweepArgs<double> &a, double dtime, long limit, int nctas, cudaStream_t st)
+int sweep_tiles_max_ctas(int sw, int nthr) { return tiles_max_ctas<RT, ST, kFast, kSweepDepth>(sw, nthr); }
+cudaError_t launch_sweep_tiles(const SweepArgs<double> &a, double dtime, long limit, int nctas, int nthr,
+                               cudaStream_t st)
 {
-    return launch_tiles_t<RT, ST, kFast, kSweepDepth>(a, dtime, limit, nctas, st);
+    return launch_tiles_t<RT, ST, kFast, kSweepDepth>(a, dtime, limit, nctas, nthr, st);
 }
 
 } // namespace SWEEP_NS
@@ -605,10 +708,11 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 }
 void launch_sweep_fill(float *p, long n, cudaStream_t st) { les_fast::launch_fill_t<float>(p, n, st); }
 int sweep_tiles_smem(int sw) { return les_fast::tiles_smem<float, float, true, kSweepDepth>(sw); }
-int sweep_tiles_max_ctas(int sw) { return les_fast::tiles_max_ctas<float, float, true, kSweepDepth>(sw); }
-cudaError_t launch_sweep_tiles(const SweepArgs<float> &a, double dtime, long limit, int nctas, cudaStream_t st)
+int sweep_tiles_max_ctas(int sw, int nthr) { return les_fast::tiles_max_ctas<float, float, true, kSweepDepth>(sw, nthr); }
+cudaError_t launch_sweep_tiles(const SweepArgs<float> &a, double dtime, long limit, int nctas, int nthr,
+                               cudaStream_t st)
 {
-    return les_fast::launch_tiles_t<float, float, true, kSweepDepth>(a, dtime, limit, nctas, st);
+    return les_fast::launch_tiles_t<float, float, true, kSweepDepth>(a, dtime, limit, nctas, nthr, st);
 }
 } // namespace les_f32
 #endif

@@ -248,9 +248,9 @@ LES_PHYS_LAUNCHERS
                              cudaStream_t st);                                                      \
     void launch_sweep_fill(S *p, long n, cudaStream_t st);                                          \
     int sweep_tiles_smem(int sw);                                                                   \
-    int sweep_tiles_max_ctas(int sw);                                                               \
+    int sweep_tiles_max_ctas(int sw, int nthr);                                                     \
     cudaError_t launch_sweep_tiles(const SweepArgs<S> &a, double dtime, long limit, int nctas,     \
-                                   cudaStream_t st);
+                                   int nthr, cudaStream_t st);
 
 namespace les_exact {
 LES_SWEEP_LAUNCHERS(double)

@@ -155,14 +155,17 @@ struct Ctx {
     // the FP64 builds, FP32 for phys32)
     struct SweepState {
         SkewBlk *d_sb = nullptr;
-        SweepTile *d_tiles = nullptr;
-        int ntile = 0;
         int maxn[3] = {0, 0, 0};
-        int sw[2] = {0, 0};           // ring width [FP64, FP32]
-        int maxctas[2][2] = {{0, 0}, {0, 0}};  // resident CTAs [FP64, FP32][fast, exact]; -1 none
         long tot3 = 0, tot2 = 0;      // skewed elements per 3-D field / 2-D table
         int *d_sync = nullptr;        // ticket, error
         void *d_sk[2] = {nullptr, nullptr};  // [FP64, FP32]: 8 fields, the new values, 10 tables
+        // per physics build [exact, fast, FP32]: rows per tile follow the
+        // build's shared-memory ring
+        SweepTile *d_tiles[3] = {nullptr, nullptr, nullptr};
+        int ntile[3] = {0, 0, 0};
+        int sw[3] = {0, 0, 0};        // ring row width (elements)
+        int nthr[3] = {0, 0, 0};      // threads per CTA: row warps + the producer warp
+        int maxctas[3] = {0, 0, 0};   // resident CTAs; -1 none
     } sw;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)

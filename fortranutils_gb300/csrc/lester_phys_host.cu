@@ -72,20 +72,17 @@ static int ensure_phys_tables(Ctx &c)
     return 0;
 }
 
-// Tiles and skew geometry of the tiled scalar sweep (k_sweep.cu), built on
-// first use.  A block's interior rows are split into as few tiles of at
-// most kSweepThreads rows as possible; one tile per (block, interior layer
-// k, row range), in ticket order (k, row range, block): every tile comes
-// after the two it waits for, (k-1, same rows) and (k, rows below).
-static int ensure_sweep_tiles(Ctx &c)
+// physics build of the current controls: 0 exact, 1 fast, 2 FP32
+static int sweep_variant(const Ctx &c) { return c.c.exact ? 0 : phys32_on(c) ? 2 : 1; }
+
+// Skew geometry of the tiled scalar sweep (k_sweep.cu), built on first use
+static int ensure_sweep_geom(Ctx &c)
 {
     Ctx::SweepState &W = c.sw;
     if (W.d_sb) return 0;
     const int nb = c.g.numbl;
     std::vector<SkewBlk> sb(nb);
     long s3 = 0, s2 = 0;
-    int maxk = 0, maxnj = 0;
-    std::vector<int> nJ(nb);
     for (int b = 1; b <= nb; b++) {
         SkewBlk &q = sb[b - 1];
         memset(&q, 0, sizeof q);
@@ -104,17 +101,51 @@ static int ensure_sweep_tiles(Ctx &c)
         s3 += q.layer * n[2];
         q.sk2 = s2;
         s2 += q.layer;
-        const int rows = n[1] - 2;
-        nJ[b - 1] = (rows + kSweepThreads - 1) / kSweepThreads;
-        maxk = std::max(maxk, n[2]);
-        maxnj = std::max(maxnj, nJ[b - 1]);
     }
     W.tot3 = s3;
     W.tot2 = s2;
-    // tile index of (block, k, J), -1 where none
+    LES_CUDA(cudaMalloc(&W.d_sb, sizeof(SkewBlk) * nb));
+    LES_CUDA(cudaMemcpy(W.d_sb, sb.data(), sizeof(SkewBlk) * nb, cudaMemcpyHostToDevice));
+    LES_CUDA(cudaMalloc(&W.d_sync, sizeof(int) * 2));  // ticket, error
+    return 0;
+}
+
+// Tiles of build `var` (0 exact, 1 fast, 2 FP32), built on first use.  A
+// block's interior rows are split into as few tiles as the build's ring
+// allows (its shared memory grows with the rows of a tile; at most
+// kSweepThreads rows); one tile per (block, interior layer k, row range),
+// in ticket order (k, row range, block): every tile comes after the two
+// whose new values it reads, (k-1, same rows) and (k, rows below).
+static int ensure_sweep_tiles(Ctx &c, int var)
+{
+    Ctx::SweepState &W = c.sw;
+    int r;
+    if ((r = ensure_sweep_geom(c))) return r;
+    if (W.d_tiles[var] || W.maxctas[var] < 0) return 0;
+    const int nb = c.g.numbl;
+    const int E = var == 2 ? 4 : 2;  // elements per 16-byte chunk
+    // shared memory per element of ring row width; rows such that the ring
+    // fits the 227 KB a CTA may have (with the ring's 12 rows of halo and
+    // chunk rounding)
+    const int per = var == 0 ? les_exact::sweep_tiles_smem(1) : var == 1 ? les_fast::sweep_tiles_smem(1)
+                                                                         : les_f32::sweep_tiles_smem(1);
+    const int rows_max = std::min(kSweepThreads, (227 * 1024 - 1024) / per - 12);
+    if (rows_max < 8) {
+        W.maxctas[var] = -1;
+        return 0;
+    }
+    int maxk = 0, maxnj = 0;
+    std::vector<int> nJ(nb);
+    for (int b = 1; b <= nb; b++) {
+        const int *n = c.lv[1].n[b];
+        nJ[b - 1] = (n[1] - 2 + rows_max - 1) / rows_max;
+        maxk = std::max(maxk, n[2]);
+        maxnj = std::max(maxnj, nJ[b - 1]);
+    }
     auto key = [&](int b, int k, int J) { return ((long)k * maxnj + J) * nb + b; };
     std::vector<int> idx((size_t)(maxk + 1) * maxnj * nb, -1);
     std::vector<SweepTile> tiles;
+    int rows_big = 0;
     for (int k = 2; k < maxk; k++)
         for (int J = 0; J < maxnj; J++)
             for (int b = 0; b < nb; b++) {
@@ -130,50 +161,46 @@ static int ensure_sweep_tiles(Ctx &c)
                 T.up_j = J > 0 ? idx[key(b, k, J - 1)] : -1;
                 idx[key(b, k, J)] = (int)tiles.size();
                 tiles.push_back(T);
+                rows_big = std::max(rows_big, T.j1 - T.j0);
             }
-    W.ntile = (int)tiles.size();
-    // ring row width: rows j0-2 .. j1+1 from a chunk boundary (16 bytes:
-    // 2 doubles or 4 floats)
-    for (int q = 0; q < 2; q++) {
-        const int E = q == 0 ? 2 : 4;
-        int w = 0;
-        for (const SweepTile &T : tiles) {
-            const int n1 = c.lv[1].n[T.blk + 1][1];
-            const int sbase = (std::max(0, T.j0 - 3) / E) * E;
-            const int hi = (std::min(n1, T.j1 + 1) + E - 1) / E * E;
-            w = std::max(w, hi - sbase);
-        }
-        W.sw[q] = w;
+    W.ntile[var] = (int)tiles.size();
+    // ring row width: rows j0-2 .. j1+1 from a chunk boundary
+    int w = 0;
+    for (const SweepTile &T : tiles) {
+        const int n1 = c.lv[1].n[T.blk + 1][1];
+        const int sbase = (std::max(0, T.j0 - 3) / E) * E;
+        const int hi = (std::min(n1, T.j1 + 1) + E - 1) / E * E;
+        w = std::max(w, hi - sbase);
     }
-    LES_CUDA(cudaMalloc(&W.d_sb, sizeof(SkewBlk) * nb));
-    LES_CUDA(cudaMemcpy(W.d_sb, sb.data(), sizeof(SkewBlk) * nb, cudaMemcpyHostToDevice));
-    LES_CUDA(cudaMalloc(&W.d_tiles, sizeof(SweepTile) * std::max(1, W.ntile)));
-    LES_CUDA(cudaMemcpy(W.d_tiles, tiles.data(), sizeof(SweepTile) * W.ntile, cudaMemcpyHostToDevice));
-    LES_CUDA(cudaMalloc(&W.d_sync, sizeof(int) * 2));  // ticket, error
+    W.sw[var] = w;
+    W.nthr[var] = 32 * ((rows_big + 31) / 32) + 32;  // row warps + the producer warp
+    if (W.ntile[var] == 0) {
+        W.maxctas[var] = -1;
+        return 0;
+    }
+    LES_CUDA(cudaMalloc(&W.d_tiles[var], sizeof(SweepTile) * W.ntile[var]));
+    LES_CUDA(cudaMemcpy(W.d_tiles[var], tiles.data(), sizeof(SweepTile) * W.ntile[var], cudaMemcpyHostToDevice));
+    // occupancy with this ring (first use: never inside a capture, the
+    // first step of a run is launched)
+    const int n = var == 0 ? les_exact::sweep_tiles_max_ctas(w, W.nthr[var])
+                  : var == 1 ? les_fast::sweep_tiles_max_ctas(w, W.nthr[var])
+                             : les_f32::sweep_tiles_max_ctas(w, W.nthr[var]);
+    W.maxctas[var] = n > 0 ? n : -1;
     return 0;
 }
 
 // Which scalar sweep runs (ctrl.sc1_sweep): 1 the hyperplane sweep, 2 the
 // tile pipeline, 3 one launch per plane; 0 the tile pipeline where its
-// shared-memory ring fits, else the hyperplane sweep.  Negative: an error.
+// ring fits, else the hyperplane sweep.  Negative: an error.
 static int sweep_choice(Ctx &c)
 {
     const int m = c.c.sc1_sweep;
     if (m == 1 || m == 3) return m;
+    const int var = sweep_variant(c);
     int r;
-    if ((r = ensure_sweep_tiles(c))) return r;
-    Ctx::SweepState &W = c.sw;
-    const int q = phys32_on(c) ? 1 : 0;
-    if (W.maxctas[q][c.c.exact ? 1 : 0] == 0) {
-        // occupancy with the ring of this build (first call, never inside a
-        // capture: the first step of a run is launched)
-        int n = phys32_on(c) ? les_f32::sweep_tiles_max_ctas(W.sw[1])
-                : c.c.exact ? les_exact::sweep_tiles_max_ctas(W.sw[0]) : les_fast::sweep_tiles_max_ctas(W.sw[0]);
-        W.maxctas[q][c.c.exact ? 1 : 0] = n > 0 ? n : -1;
-    }
-    const bool fits = W.maxctas[q][c.c.exact ? 1 : 0] > 0 && W.ntile > 0;
-    if (m == 2 && !fits)
-        return set_err(LES_ERR_SIZE, "set_sc1: the tile pipeline's shared-memory ring does not fit (%d rows)", W.sw[q]);
+    if ((r = ensure_sweep_tiles(c, var))) return r;
+    const bool fits = c.sw.maxctas[var] > 0;
+    if (m == 2 && !fits) return set_err(LES_ERR_SIZE, "set_sc1: the tile pipeline's shared-memory ring does not fit");
     return fits ? 2 : 1;
 }
 
@@ -185,11 +212,12 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
                            void (*unskew)(const SkewBlk *, int, int, int, int, const S *, const S *, double *,
                                           double *, cudaStream_t),
                            void (*fill)(S *, long, cudaStream_t),
-                           cudaError_t (*launch)(const SweepArgs<S> &, double, long, int, cudaStream_t))
+                           cudaError_t (*launch)(const SweepArgs<S> &, double, long, int, int, cudaStream_t))
 {
     Ctx::SweepState &W = c.sw;
     const int nb = c.g.numbl;
     const bool fast = !c.c.exact;
+    const int var = sweep_variant(c);
     if (!W.d_sk[q]) {
         const size_t bytes = sizeof(S) * (9 * W.tot3 + 10 * W.tot2);
         if (cudaMalloc(&W.d_sk[q], bytes) != cudaSuccess) {
@@ -219,9 +247,9 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     SweepArgs<S> a;
     memset(&a, 0, sizeof a);
     a.sb = W.d_sb;
-    a.tiles = W.d_tiles;
-    a.ntile = W.ntile;
-    a.sw = W.sw[q];
+    a.tiles = W.d_tiles[var];
+    a.ntile = W.ntile[var];
+    a.sw = W.sw[var];
     for (int f = 0; f < 8; f++) a.f3[f] = P3.dst[f];
     for (int f = 0; f < n2; f++) a.f2[f] = P2.dst[f];
     a.dkp = A.dkp;
@@ -236,13 +264,13 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     a.err = W.d_sync + 1;
     fill(a.scnew, W.tot3, c.stream);
     LES_CUDA(cudaMemsetAsync(W.d_sync, 0, sizeof(int) * 2, c.stream));
-    const int nctas = std::min(W.ntile, W.maxctas[q][c.c.exact ? 1 : 0]);
+    const int nctas = std::min(W.ntile[var], W.maxctas[var]);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (c.prof && !c.capturing) {
         prof_pair(c, LES_PROF_SWEEP, &e0, &e1);
         cudaEventRecord(e0, c.stream);
     }
-    LES_CUDA(launch(a, c.c.dtime, wait_polls(c), nctas, c.stream));
+    LES_CUDA(launch(a, c.c.dtime, wait_polls(c), nctas, W.nthr[var], c.stream));
     if (e1) cudaEventRecord(e1, c.stream);
     unskew(W.d_sb, nb, W.maxn[0], W.maxn[1], W.maxn[2], a.scnew, P3.dst[1], A.sc1, A.hsc1, c.stream);
     if (c.capturing) {
