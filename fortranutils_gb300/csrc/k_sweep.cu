@@ -404,9 +404,13 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
         };
         bool ok = true;
         int t = ts;
+        int err_seen = 0;  // thread 0: the error flag, re-read from L2 every 16 planes only
         for (; t <= t1; t++) {
             const long u = ubase + (t - ts);
-            if (tid == 0) s_ok[t & 1] = !*(volatile int *)A.err;
+            if (tid == 0) {
+                if (((t - ts) & 15) == 0) err_seen = *(volatile int *)A.err;
+                s_ok[t & 1] = !err_seen;
+            }
             if (!producer && u >= D) mbar_wait(&mbar[(u - D) % G], (unsigned)(((u - D) / G) & 1), A.err, limit);
             __syncthreads();
             if (!s_ok[t & 1]) {
