@@ -200,7 +200,8 @@ struct SweepTile {
     int blk, k, j0, j1, up_k, up_j;
 };
 
-constexpr int kSweepThreads = 256;  // rows per tile at most (one thread per row)
+constexpr int kSweepRows = 192;   // rows per tile at most (three compute threads per row)
+constexpr int kSweepThreadsMax = 3 * kSweepRows + 32;  // and one producer warp
 constexpr int kSweepDepth = 4;      // planes staged ahead
 
 // sources (FP64, reference layout) and skewed destinations of one k_skew

@@ -141,58 +141,13 @@ __device__ __forceinline__ void st_strong(double *p, double v)
     asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(unsigned long long *m, int count)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void mbar_expect(unsigned long long *m, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(unsigned long long *m, unsigned parity)
-{
-    unsigned ok;
-    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-                 : "=r"(ok)
-                 : "r"(smem_addr(m)), "r"(parity)
-                 : "memory");
-    return ok != 0;
-}
-// one contiguous global -> shared copy by the TMA unit, completing
-// `bytes` of the mbarrier's transaction count (16-byte aligned, size a
-// multiple of 16)
-__device__ __forceinline__ void bulk_copy(void *dst, const void *src, unsigned bytes, unsigned long long *m)
-{
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(m))
-                 : "memory");
-}
-// wait for the copies of a phase to land before the ring is reused or the
-// CTA exits, even after an error elsewhere (they depend on nothing);
-// bounded by `limit` tries
-__device__ __forceinline__ void mbar_drain(unsigned long long *m, unsigned parity, int *err, long limit)
-{
-    long it = 0;
-    while (!mbar_try(m, parity))
-        if (++it > limit) {
-            atomicExch(err, 1);
-            return;
-        }
-}
-// wait for a phase of an mbarrier; bounded: after `limit` tries, or once
-// another CTA has set *err, give up (sets *err)
-__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, int *err, long limit)
-{
-    long it = 0;
-    while (!mbar_try(m, parity)) {
-        if (++it > limit || *(volatile int *)err) {
-            atomicExch(err, 1);
-            return false;
-        }
-    }
-    return true;
-}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // A new value staged from the new-value array: while it is still the
 // sentinel, re-read it from L2 (another CTA is computing it); bounded by
@@ -300,30 +255,31 @@ template <typename S> __global__ void k_fill_sentinel(S *__restrict__ p, long n)
 // ----------------------------------------------------------- the pipeline
 // R: arithmetic type; S: storage type of the skewed copies; FAST: the
 // reciprocal tables of the fast builds; D: planes staged ahead.
-// One CTA: compute warps (one thread per row of the tile) and, last, one
-// producer warp whose lane v issues the bulk copy of staged vector v for
-// each plane.  Plane group u (the copies issued at the u-th plane step of
-// the CTA) completes mbarrier u % (D+1); the compute threads wait for group
-// u - D before plane step u, so D groups are in flight.
+//
+// One CTA: three compute threads per row of the tile -- thread (d, r)
+// computes the two faces of axis d of the row's point (gradients, limited
+// face values, convective and diffusive fluxes), the x thread then adds
+// the three axes' flux differences in the reference's order and updates
+// the point -- and, last, one producer warp whose lanes stage the vectors
+// of each plane with 16-byte cp.async copies, one cp.async group per plane
+// step.  At plane step u the producer waits for its group u - (D-1); the
+// __syncthreads that opens step u+1 then publishes it to the compute
+// threads, which read group u+1-D there: D groups are in flight.
 template <typename R, typename S, bool FAST, int D>
-__global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
+__global__ void __launch_bounds__(kSweepThreadsMax) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     S *ring = (S *)smem_raw;
-    constexpr int G = D + 1;
-    __shared__ __align__(8) unsigned long long mbar[G];
     __shared__ int s_tile, s_ok[2];  // s_ok by plane parity: thread 0 may write the next before all read this
+    __shared__ R part[4][kSweepRows];  // y and z flux differences of each row's point
     constexpr int E = 16 / sizeof(S);  // elements per 16-byte chunk
     const R lambda = (R)4.0, small = (R)1.e-30, half = (R)0.5, one = (R)1.0, zero = (R)0.0;
     const R dtime = (R)dtime_d;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int nwc = (int)(blockDim.x >> 5) - 1;  // compute warps
-    const bool producer = (tid >> 5) == nwc;
-    if (tid == 0)
-        for (int g = 0; g < G; g++) mbar_init(&mbar[g], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    __syncthreads();
-    long ubase = 0;  // plane steps of earlier tiles (mbarrier phases continue)
+    const int rpad = ((int)blockDim.x - 32) / 3;  // rows per axis group (a multiple of 32)
+    const int ncomp = 3 * rpad;                    // compute threads
+    const bool producer = tid >= ncomp;
+    const int axis = producer ? 0 : tid / rpad, r = producer ? 0 : tid - axis * rpad;
     for (;;) {
         if (tid == 0) {
             int tk = -1;
@@ -344,37 +300,10 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
         const int jr_lo = max(0, j0 - 3), jr_hi = min(n1, j1 + 1);  // [lo, hi)
         const int SW = A.sw;
         // own row and the plane range
-        const int j = j0 + tid;
+        const int j = j0 + r;
         const bool row = !producer && j < j1;
         const int t0 = 2 + j0, t1 = ni + (j1 - 1);
         const int ts = t0 - D - 4;
-        // ---- producer lane v: vector v's fixed parts
-        int pv_lo = 0, pv_hi = 0, pv_slots = 1, pv_hi_off = 0, pv_lo_off = 0;
-        const S *pv_g = nullptr;
-        S *pv_ring = nullptr;
-        bool pv_on = false;
-        if (producer && lane < V_N && has_vec(FAST, lane)) {
-            const int v = lane;
-            const VecDesc vd = c_vdesc[v];
-            const int kv = k + vd.dk;
-            pv_on = kv >= 1 && kv <= n2 && (v != V_SCH || jhalo);
-            const bool cross = vd.dk != 0;
-            pv_lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
-            pv_hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
-            pv_slots = pow2_ceil(vd.hi - vd.lo + D + 1);
-            pv_hi_off = vd.hi;
-            pv_lo_off = vd.lo;
-            if (vd.src < 8) {
-                // new values of an interior layer below come from the new-value array
-                const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
-                pv_g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1);
-            } else if (vd.src < 18) {
-                pv_g = A.f2[vd.src - 8] + b.sk2;
-            } else {
-                pv_g = A.scnew + b.sk3 + b.layer * (kv - 1);
-            }
-            pv_ring = ring + vprefix_rt<FAST, D>(v) * SW - sbase;
-        }
         // 1-D metrics of this layer
         const double *dkp = A.dkp + b.off1k, *dkw = A.dkw + b.off1k;
         const R dkw_k = (R)dkw[k - 1];
@@ -402,198 +331,199 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
         auto newval = [&](int v, int kv, int p, int jj) -> R {
             return (R)fresh<S>(slot(v, p, jj), A.scnew + e3(kv, p, jj), A.err, limit);
         };
+        // producer: the copies of group t, plane t + D + hi of every vector,
+        // chunks spread over the lanes
+        auto issue = [&](int t) {
+#pragma unroll
+            for (int v = 0; v < V_N; v++) {
+                if (!has_vec(FAST, v)) continue;
+                const VecDesc vd = vdesc(v);
+                const int p = t + D + vd.hi;
+                if (p < t0 + vd.lo || p > t1 + vd.hi || p < 2 || p > n0 + n1) continue;
+                const int kv = k + vd.dk;
+                if (kv < 1 || kv > n2) continue;
+                if (v == V_SCH && !jhalo) continue;
+                const bool cross = vd.dk != 0;
+                int lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
+                int hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
+                lo = max(lo, p - n0 - 1);
+                hi = min(hi, p - 1);
+                if (lo >= hi) continue;
+                const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
+                const S *g;
+                if (vd.src < 8) {
+                    // new values of an interior layer below from the new-value array
+                    const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
+                    g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
+                } else if (vd.src < 18) {
+                    g = A.f2[vd.src - 8] + b.sk2 + (long)(p - 2) * b.vp;
+                } else {
+                    g = A.scnew + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
+                }
+                S *dst = ring + (vprefix(FAST, v, D) + (p & (vslots(v, D) - 1))) * SW - sbase;
+                for (int c = c_lo + lane; c < c_hi; c += 32) cp_async16(dst + c * E, g + c * E);
+            }
+        };
         bool ok = true;
         int t = ts;
         int err_seen = 0;  // thread 0: the error flag, re-read from L2 every 16 planes only
         for (; t <= t1; t++) {
-            const long u = ubase + (t - ts);
             if (tid == 0) {
                 if (((t - ts) & 15) == 0) err_seen = *(volatile int *)A.err;
                 s_ok[t & 1] = !err_seen;
             }
-            if (!producer && u >= D) mbar_wait(&mbar[(u - D) % G], (unsigned)(((u - D) / G) & 1), A.err, limit);
             __syncthreads();
             if (!s_ok[t & 1]) {
                 ok = false;
                 break;
             }
             if (producer) {
-                // group u: plane t + D + hi of every vector, its valid rows
-                unsigned bytes = 0;
-                const S *src = nullptr;
-                S *dst = nullptr;
-                const int p = t + D + pv_hi_off;
-                if (pv_on && p >= t0 + pv_lo_off && p <= t1 + pv_hi_off && p >= 2 && p <= n0 + n1) {
-                    const int lo = max(pv_lo, p - n0 - 1), hi = min(pv_hi, p - 1);
-                    if (lo < hi) {
-                        const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
-                        bytes = (unsigned)(c_hi - c_lo) * 16u;
-                        src = pv_g + (long)(p - 2) * b.vp + c_lo * E;
-                        dst = pv_ring + (p & (pv_slots - 1)) * SW + c_lo * E;
-                    }
-                }
-                const unsigned total = __reduce_add_sync(0xffffffffu, bytes);
-                if (lane == 0) mbar_expect(&mbar[u % G], total);
-                __syncwarp();
-                if (bytes) bulk_copy(dst, src, bytes, &mbar[u % G]);
+                issue(t);
+                cp_async_commit();
+                cp_async_wait<D - 1>();
                 continue;
             }
-            if (t < t0 || !row) continue;
             const int i = t - j;
-            if (i < 2 || i > ni) continue;
-            // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands)
-            const R rho0 = at(V_RHO, t, j);
-            const R rhowf = half * (rho0 + at(V_RHO, t - 1, j));
-            const R rhoef = half * (rho0 + at(V_RHO, t + 1, j));
-            const R rhosf = half * (rho0 + at(V_RHO, t - 1, j - 1));
-            const R rhonf = half * (rho0 + at(V_RHO, t + 1, j + 1));
-            const R rholf = half * (rho0 + at(V_RHOM1, t, j));
-            const R rhorf = half * (rho0 + at(V_RHOP1, t, j));
-            const R rhop = rho0;
-            const R gs0 = at(V_GS, t, j), gl0 = at(V_GL, t, j);
-            const R gamwf = half * (gs0 + at(V_GS, t - 1, j)) * rhowf + half * (gl0 + at(V_GL, t - 1, j));
-            const R gamef = half * (gs0 + at(V_GS, t + 1, j)) * rhoef + half * (gl0 + at(V_GL, t + 1, j));
-            const R gamsf = half * (gs0 + at(V_GS, t - 1, j - 1)) * rhosf + half * (gl0 + at(V_GL, t - 1, j - 1));
-            const R gamnf = half * (gs0 + at(V_GS, t + 1, j + 1)) * rhonf + half * (gl0 + at(V_GL, t + 1, j + 1));
-            const R gamlf = half * (gs0 + at(V_GSM1, t, j)) * rholf + half * (gl0 + at(V_GLM1, t, j));
-            const R gamrf = half * (gs0 + at(V_GSP1, t, j)) * rhorf + half * (gl0 + at(V_GLP1, t, j));
-            const R uwf = at(V_U, t, j), uef = at(V_U, t + 1, j);
-            const R vsf = at(V_V, t, j), vnf = at(V_V, t + 1, j + 1);
-            const R wlf = at(V_W, t, j), wrf = at(V_WP1, t, j);
-            const R s0 = at(V_SC, t, j);
-            const R sw = at(V_SC, t - 1, j), se = at(V_SC, t + 1, j);
-            const R ss = (jhalo && j == j0) ? newval(V_SCH, k, t - 1, j - 1) : at(V_SC, t - 1, j - 1);
-            const R sn = at(V_SC, t + 1, j + 1);
-            const R sl = k - 1 >= 2 ? newval(V_SCM1, k - 1, t, j) : at(V_SCM1, t, j);
-            const R sr = at(V_SCP1, t, j);
-#define QD(x, v, pp, jj) (FAST ? (x) * at(v##_R, pp, jj) : (x) / at(v, pp, jj))
-#define V_DIU_R V_RDIU
-#define V_DJV_R V_RDJV
-            const R dfdxwf = QD(s0 - sw, V_DIU, t, j);
-            const R dfdxef = QD(se - s0, V_DIU, t + 1, j);
-            const long gst = A.gstride;
-            const int gm = A.gm;
-            const double *GR = A.grad;
-            const int bi = T.blk;
-            R dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
-            if (i == 2)
-                dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D)
-                              ? dfdxwf
-                              : (R)GR[(long)(A.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
-            else
-                dfdxwwf = QD(sw - at(V_SC, t - 2, j), V_DIU, t - 1, j);
-            if (i == ni)
-                dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D)
-                              ? dfdxef
-                              : (R)GR[(long)(A.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
-            else
-                dfdxeef = QD(at(V_SC, t + 2, j) - se, V_DIU, t + 2, j);
-            const R dfdysf = QD(s0 - ss, V_DJV, t, j);
-            const R dfdynf = QD(sn - s0, V_DJV, t + 1, j + 1);
-            if (j == 2)
-                dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D)
-                              ? dfdysf
-                              : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
-            else
-                dfdyssf = QD(ss - ((jhalo && j - 2 < j0) ? newval(V_SCH, k, t - 2, j - 2) : at(V_SC, t - 2, j - 2)),
-                             V_DJV, t - 1, j - 1);
-            if (j == nj)
-                dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D)
-                              ? dfdynf
-                              : (R)GR[(long)(A.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
-            else
-                dfdynnf = QD(at(V_SC, t + 2, j + 2) - sn, V_DJV, t + 2, j + 2);
+            const bool pt = t >= t0 && row && i >= 2 && i <= ni;
+            // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands),
+            // axis by axis
+            R c_d = zero, t_d = zero;  // this axis: g_hi - g_lo and t_hi - t_lo
+            if (pt) {
+                const R s0 = at(V_SC, t, j);
+                const R rho0 = at(V_RHO, t, j), gs0 = at(V_GS, t, j), gl0 = at(V_GL, t, j);
+                const long gst = A.gstride;
+                const int gm = A.gm;
+                const double *GR = A.grad;
+                const int bi = T.blk;
+                R rlo, rhi, gslo, gshi, gllo, glhi, vlo, vhi, slo, shi, dlo, dmid, dhi;  // faces' operands
+                R areal, areah, glo_m, ghi_p;  // face areas; gradient beyond each face
+                int s_lo, s_hi;                // sides of the two faces
+                bool first, last;              // the point is the first / last interior one along the axis
+                if (axis == 0) {
+                    rlo = at(V_RHO, t - 1, j); rhi = at(V_RHO, t + 1, j);
+                    gslo = at(V_GS, t - 1, j); gshi = at(V_GS, t + 1, j);
+                    gllo = at(V_GL, t - 1, j); glhi = at(V_GL, t + 1, j);
+                    vlo = at(V_U, t, j); vhi = at(V_U, t + 1, j);
+                    slo = at(V_SC, t - 1, j); shi = at(V_SC, t + 1, j);
+#define QD(x, v, vr, pp, jj) (FAST ? (x) * at(vr, pp, jj) : (x) / at(v, pp, jj))
+                    dlo = QD(s0 - slo, V_DIU, V_RDIU, t, j);
+                    dhi = QD(shi - s0, V_DIU, V_RDIU, t + 1, j);
+                    first = i == 2;
+                    last = i == ni;
+                    s_lo = 0;
+                    s_hi = 1;
+                    glo_m = first ? ((b.bc[0] != LES_BCT_INTERFACE_D) ? dlo
+                                     : (R)GR[(long)(A.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)])
+                                  : QD(slo - at(V_SC, t - 2, j), V_DIU, V_RDIU, t - 1, j);
+                    ghi_p = last ? ((b.bc[1] != LES_BCT_INTERFACE_D) ? dhi
+                                    : (R)GR[(long)(A.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)])
+                                 : QD(at(V_SC, t + 2, j) - shi, V_DIU, V_RDIU, t + 2, j);
+                    areal = at(V_RDJU, t, j) * dkw_k;
+                    areah = at(V_RDJU, t + 1, j) * dkw_k;
+                } else if (axis == 1) {
+                    rlo = at(V_RHO, t - 1, j - 1); rhi = at(V_RHO, t + 1, j + 1);
+                    gslo = at(V_GS, t - 1, j - 1); gshi = at(V_GS, t + 1, j + 1);
+                    gllo = at(V_GL, t - 1, j - 1); glhi = at(V_GL, t + 1, j + 1);
+                    vlo = at(V_V, t, j); vhi = at(V_V, t + 1, j + 1);
+                    slo = (jhalo && j == j0) ? newval(V_SCH, k, t - 1, j - 1) : at(V_SC, t - 1, j - 1);
+                    shi = at(V_SC, t + 1, j + 1);
+                    dlo = QD(s0 - slo, V_DJV, V_RDJV, t, j);
+                    dhi = QD(shi - s0, V_DJV, V_RDJV, t + 1, j + 1);
+                    first = j == 2;
+                    last = j == nj;
+                    glo_m = first ? ((b.bc[2] != LES_BCT_INTERFACE_D) ? dlo
+                                     : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)])
+                                  : QD(slo - ((jhalo && j - 2 < j0) ? newval(V_SCH, k, t - 2, j - 2) : at(V_SC, t - 2, j - 2)),
+                                       V_DJV, V_RDJV, t - 1, j - 1);
+                    ghi_p = last ? ((b.bc[3] != LES_BCT_INTERFACE_D) ? dhi
+                                    : (R)GR[(long)(A.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)])
+                                 : QD(at(V_SC, t + 2, j + 2) - shi, V_DJV, V_RDJV, t + 2, j + 2);
 #undef QD
-#undef V_DIU_R
-#undef V_DJV_R
-            const R rpij = at(V_RP, t, j);
-            const R rrpij = FAST ? at(V_RRP, t, j) : zero;
+                    areal = at(V_RDIV, t, j) * dkw_k;
+                    areah = at(V_RDIV, t + 1, j + 1) * dkw_k;
+                    s_lo = 2;
+                    s_hi = 3;
+                } else {
+                    rlo = at(V_RHOM1, t, j); rhi = at(V_RHOP1, t, j);
+                    gslo = at(V_GSM1, t, j); gshi = at(V_GSP1, t, j);
+                    gllo = at(V_GLM1, t, j); glhi = at(V_GLP1, t, j);
+                    vlo = at(V_W, t, j); vhi = at(V_WP1, t, j);
+                    slo = k - 1 >= 2 ? newval(V_SCM1, k - 1, t, j) : at(V_SCM1, t, j);
+                    shi = at(V_SCP1, t, j);
+                    const R rpij = at(V_RP, t, j);
+                    const R rrpij = FAST ? at(V_RRP, t, j) : zero;
 #define QZ(x, dk_, rdk_) (FAST ? (x) * (rrpij * (rdk_)) : (x) / (rpij * (dk_)))
-            const R dfdzlf = QZ(s0 - sl, dkp_m2, rdkp_m2);
-            const R dfdzrf = QZ(sr - s0, dkp_m1, rdkp_m1);
-            if (k == 2)
-                dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D)
-                              ? dfdzlf
-                              : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
-            else
-                dfdzllf = QZ(sl - (k - 2 >= 2 ? newval(V_SCM2, k - 2, t, j) : at(V_SCM2, t, j)), dkp_m3, rdkp_m3);
-            if (k == nk)
-                dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D)
-                              ? dfdzrf
-                              : (R)GR[(long)(A.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
-            else
-                dfdzrrf = QZ(at(V_SCP2, t, j) - sr, dkp_0, rdkp_0);
+                    dlo = QZ(s0 - slo, dkp_m2, rdkp_m2);
+                    dhi = QZ(shi - s0, dkp_m1, rdkp_m1);
+                    first = k == 2;
+                    last = k == nk;
+                    glo_m = first ? ((b.bc[4] != LES_BCT_INTERFACE_D) ? dlo
+                                     : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)])
+                                  : QZ(slo - (k - 2 >= 2 ? newval(V_SCM2, k - 2, t, j) : at(V_SCM2, t, j)), dkp_m3, rdkp_m3);
+                    ghi_p = last ? ((b.bc[5] != LES_BCT_INTERFACE_D) ? dhi
+                                    : (R)GR[(long)(A.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)])
+                                 : QZ(at(V_SCP2, t, j) - shi, dkp_0, rdkp_0);
 #undef QZ
-            const R rwst = (uwf >= zero) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
-            const R rest = (uef > zero) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
-            const R rsth = (vsf >= zero) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
-            const R rnth = (vnf > zero) ? (dfdysf + small) / (dfdynf + small) : (dfdynnf + small) / (dfdynf + small);
-            const R rlft = (wlf >= zero) ? (dfdzllf + small) / (dfdzlf + small) : (dfdzrf + small) / (dfdzlf + small);
-            const R rrht = (wrf > zero) ? (dfdzlf + small) / (dfdzrf + small) : (dfdzrrf + small) / (dfdzrf + small);
-            const R limw = fmax(zero, fmin(lambda * rwst, one));
-            const R lime = fmax(zero, fmin(lambda * rest, one));
-            const R lims = fmax(zero, fmin(lambda * rsth, one));
-            const R limn = fmax(zero, fmin(lambda * rnth, one));
-            const R liml = fmax(zero, fmin(lambda * rlft, one));
-            const R limr = fmax(zero, fmin(lambda * rrht, one));
-            R fwf, fef, fsf, fnf, flf, frf;
-            if (uwf > zero) fwf = sw + half * limw * (s0 - sw);
-            else if (uwf < zero) fwf = s0 + half * limw * (sw - s0);
-            else fwf = half * (s0 + sw);
-            if (uef > zero) fef = s0 + half * lime * (se - s0);
-            else if (uef < zero) fef = se + half * lime * (s0 - se);
-            else fef = half * (s0 + se);
-            if (vsf > zero) fsf = ss + half * lims * (s0 - ss);
-            else if (vsf < zero) fsf = s0 + half * lims * (ss - s0);
-            else fsf = half * (s0 + ss);
-            if (vnf > zero) fnf = s0 + half * limn * (sn - s0);
-            else if (vnf < zero) fnf = sn + half * limn * (s0 - sn);
-            else fnf = half * (s0 + sn);
-            if (wlf > zero) flf = sl + half * liml * (s0 - sl);
-            else if (wlf < zero) flf = s0 + half * liml * (sl - s0);
-            else flf = half * (s0 + sl);
-            if (wrf > zero) frf = s0 + half * limr * (sr - s0);
-            else if (wrf < zero) frf = sr + half * limr * (s0 - sr);
-            else frf = half * (s0 + sr);
-            const R areawf = at(V_RDJU, t, j) * dkw_k;
-            const R areaef = at(V_RDJU, t + 1, j) * dkw_k;
-            const R areasf = at(V_RDIV, t, j) * dkw_k;
-            const R areanf = at(V_RDIV, t + 1, j + 1) * dkw_k;
-            const R areak = at(V_DIDJP, t, j);
-            const R vol = at(V_RDIDJP, t, j) * dkw_k;
-            const R gwf = rhowf * uwf * fwf * areawf;
-            const R gef = rhoef * uef * fef * areaef;
-            const R gsf = rhosf * vsf * fsf * areasf;
-            const R gnf = rhonf * vnf * fnf * areanf;
-            const R glf = rholf * wlf * flf * areak;
-            const R grf = rhorf * wrf * frf * areak;
-            const R convf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
-            const R twf = gamwf * areawf * dfdxwf;
-            const R tef = gamef * areaef * dfdxef;
-            const R tsf = gamsf * areasf * dfdysf;
-            const R tnf = gamnf * areanf * dfdynf;
-            const R tlf = gamlf * areak * dfdzlf;
-            const R trf = gamrf * areak * dfdzrf;
-            const R difff = (tef - twf) + (tnf - tsf) + (trf - tlf);
-            const R h = convf + difff;
-            R tmp = s0 + dtime / (vol * rhop) * ((R)1.5 * h - half * at(V_H, t, j));
-            if (tmp < zero) tmp = zero;
-            if (tmp > one) tmp = one;
-            // the new value: in the ring slot of plane t (read by later
-            // planes of this tile) and in the new-value array (read by the
-            // layers above and the tile above); the history in place
-            slot(V_SC, t, j) = (S)tmp;
-            const long e = e3(k, t, j);
-            st_strong(A.scnew + e, (S)tmp);
-            A.f3[1][e] = (S)h;
+                    areal = at(V_DIDJP, t, j);
+                    areah = areal;
+                    s_lo = 4;
+                    s_hi = 5;
+                }
+                (void)s_lo;
+                (void)s_hi;
+                (void)dmid;
+                const R rholf = half * (rho0 + rlo);
+                const R rhohf = half * (rho0 + rhi);
+                const R gamlf = half * (gs0 + gslo) * rholf + half * (gl0 + gllo);
+                const R gamhf = half * (gs0 + gshi) * rhohf + half * (gl0 + glhi);
+                // low face tests v >= 0, high face v > 0 (rwst / rest of the reference)
+                const R rl = (vlo >= zero) ? (glo_m + small) / (dlo + small) : (dhi + small) / (dlo + small);
+                const R rh = (vhi > zero) ? (dlo + small) / (dhi + small) : (ghi_p + small) / (dhi + small);
+                const R liml = fmax(zero, fmin(lambda * rl, one));
+                const R limh = fmax(zero, fmin(lambda * rh, one));
+                R fl, fh;
+                if (vlo > zero) fl = slo + half * liml * (s0 - slo);
+                else if (vlo < zero) fl = s0 + half * liml * (slo - s0);
+                else fl = half * (s0 + slo);
+                if (vhi > zero) fh = s0 + half * limh * (shi - s0);
+                else if (vhi < zero) fh = shi + half * limh * (s0 - shi);
+                else fh = half * (s0 + shi);
+                const R gl_ = rholf * vlo * fl * areal;
+                const R gh_ = rhohf * vhi * fh * areah;
+                const R tl_ = gamlf * areal * dlo;
+                const R th_ = gamhf * areah * dhi;
+                c_d = gh_ - gl_;
+                t_d = th_ - tl_;
+                if (axis > 0) {
+                    part[2 * (axis - 1)][r] = c_d;
+                    part[2 * (axis - 1) + 1][r] = t_d;
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(ncomp) : "memory");  // the compute threads
+            if (pt && axis == 0) {
+                // combine in the reference's order:
+                // convf = -(gef - gwf) - (gnf - gsf) - (grf - glf), difff likewise
+                const R convf = -c_d - part[0][r] - part[2][r];
+                const R difff = (t_d + part[1][r]) + part[3][r];
+                const R h = convf + difff;
+                const R s0 = at(V_SC, t, j);
+                const R vol = at(V_RDIDJP, t, j) * dkw_k;
+                R tmp = s0 + dtime / (vol * at(V_RHO, t, j)) * ((R)1.5 * h - half * at(V_H, t, j));
+                if (tmp < zero) tmp = zero;
+                if (tmp > one) tmp = one;
+                // the new value: in the ring slot of plane t (read by later
+                // planes of this tile) and in the new-value array (read by the
+                // layers above and the tile above); the history in place
+                slot(V_SC, t, j) = (S)tmp;
+                const long e = e3(k, t, j);
+                st_strong(A.scnew + e, (S)tmp);
+                A.f3[1][e] = (S)h;
+            }
         }
-        // the groups still in flight (issued, never waited for) land before
-        // the ring is reused or the CTA exits
-        const long uend = ubase + (t - ts);  // groups issued: ubase .. uend-1
-        if (producer && lane == 0)
-            for (long w = max(ubase, uend - D); w < uend; w++) mbar_drain(&mbar[w % G], (unsigned)((w / G) & 1), A.err, limit);
+        // the copies still in flight land before the ring is reused or the
+        // CTA exits
+        if (producer) cp_async_wait_all();
         __syncthreads();
-        ubase = uend;
         if (!ok) return;
     }
 }

@@ -113,7 +113,7 @@ static int ensure_sweep_geom(Ctx &c)
 // Tiles of build `var` (0 exact, 1 fast, 2 FP32), built on first use.  A
 // block's interior rows are split into as few tiles as the build's ring
 // allows (its shared memory grows with the rows of a tile; at most
-// kSweepThreads rows); one tile per (block, interior layer k, row range),
+// kSweepRows rows); one tile per (block, interior layer k, row range),
 // in ticket order (k, row range, block): every tile comes after the two
 // whose new values it reads, (k-1, same rows) and (k, rows below).
 static int ensure_sweep_tiles(Ctx &c, int var)
@@ -129,7 +129,7 @@ static int ensure_sweep_tiles(Ctx &c, int var)
     // chunk rounding)
     const int per = var == 0 ? les_exact::sweep_tiles_smem(1) : var == 1 ? les_fast::sweep_tiles_smem(1)
                                                                          : les_f32::sweep_tiles_smem(1);
-    const int rows_max = std::min(kSweepThreads, (227 * 1024 - 1024) / per - 12);
+    const int rows_max = std::min(kSweepRows, (227 * 1024 - 8192) / per - 12);  // static: partials
     if (rows_max < 8) {
         W.maxctas[var] = -1;
         return 0;
@@ -173,7 +173,7 @@ static int ensure_sweep_tiles(Ctx &c, int var)
         w = std::max(w, hi - sbase);
     }
     W.sw[var] = w;
-    W.nthr[var] = 32 * ((rows_big + 31) / 32) + 32;  // row warps + the producer warp
+    W.nthr[var] = 3 * 32 * ((rows_big + 31) / 32) + 32;  // three row groups + the producer warp
     if (W.ntile[var] == 0) {
         W.maxctas[var] = -1;
         return 0;
