@@ -200,9 +200,8 @@ struct SweepTile {
     int blk, k, j0, j1, up_k, up_j;
 };
 
-constexpr int kSweepRows = 192;   // rows per tile at most (three compute threads per row)
-constexpr int kSweepThreadsMax = 3 * kSweepRows + 32;  // and one producer warp
-constexpr int kSweepDepth = 4;      // planes staged ahead
+constexpr int kSweepThreads = 256;  // rows per tile at most (one thread per row)
+constexpr int kSweepDepth = 2;      // planes staged ahead
 
 // sources (FP64, reference layout) and skewed destinations of one k_skew
 // launch: up to 10 fields or tables
@@ -216,13 +215,15 @@ template <typename S> struct SweepArgs {
     const SweepTile *tiles;
     int ntile, sw;           // tiles; ring row width (elements)
     S *f3[8];                // skewed sc1 hsc1 u v w rho gamsc1 gamlam (old values; hsc1 updated)
-    S *scnew;                // skewed new values of sc1 (interior: -1 until computed)
+    S *scnew;                // skewed new values of sc1 (field 8: interior -1 until computed, ghosts old)
     const S *f2[10];         // skewed diu djv rdju rdiv rp didjp rdidjp (+ 1/diu 1/djv 1/rp)
     const double *dkp, *dkw, *rdkp;
     const double *grad;      // interface gradients (set_gamsc1_bc planes)
     long gstride;
     int gm;
     const int *link;         // bl2bl, 0-based, 6 per block
+    const void *tmaps;       // per block 4 TMA tensor maps (CUtensorMap, global memory): 3-D fields
+                             // in boxes of 8, 4, 1 fields, the 2-D tables
     int *ticket;             // next tile to take
     int *err;                // a bounded wait gave up
 };

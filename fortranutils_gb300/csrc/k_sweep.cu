@@ -19,11 +19,15 @@
 //    anti-dependences: the tiles run as a wavefront one layer apart, in
 //    ticket order (every tile waits only on tiles with smaller tickets);
 //  * every field is first copied into a skewed layout (k_skew), in which
-//    plane t of a layer is one contiguous vector over j, so a tile stages
-//    the vectors of the planes it will need with coalesced 16-byte cp.async
-//    copies into a shared-memory ring, D planes ahead; the new values go
-//    to the new-value array and to the ring (read by later planes of the
-//    tile) and are copied to the FP64 fields at the end (k_unskew).
+//    plane t of a layer is one contiguous vector over j and the fields of a
+//    block follow one another at a fixed stride, so (rows, planes, fields)
+//    is a 3-D tensor: one TMA tensor copy stages the plane vectors of
+//    several fields of a layer into a shared-memory ring, D planes ahead
+//    (eight copies per plane: the layer's own fields, those of the layers
+//    k-1, k-2, k+1, k+2 it reads, the 2-D metric tables, the new values of
+//    the tile below); the new values go to the new-value array and to the
+//    ring (read by later planes of the tile) and are copied to the FP64
+//    fields at the end (k_unskew).
 //
 // The arithmetic per point is that of sc1_cell in k_phys.cu, operand for
 // operand, so the exact build (FP64, -fmad=false) equals the hyperplane
@@ -31,6 +35,8 @@
 // metric tables (x * (1/d)) as k_phys.cu's fast build does; the FP32 build
 // is the same template with R = S = float (FP64 fields in HBM, FP32 skewed
 // copies).
+#include <cuda.h>
+
 #include "k_common.cuh"
 #include "kernels.h"
 
@@ -43,81 +49,53 @@
 namespace les_sweep {
 namespace {  // internal to each build of this unit
 
-// vectors staged per plane: own layer (3-D fields 0..7), the layers k-1,
-// k-2, k+1, k+2, and the 2-D metric tables (reciprocals last: fast only)
-enum {
-    V_SC, V_H, V_U, V_V, V_W, V_RHO, V_GS, V_GL,
-    V_SCM1, V_RHOM1, V_GSM1, V_GLM1, V_SCM2,
-    V_SCP1, V_RHOP1, V_GSP1, V_GLP1, V_WP1, V_SCP2,
-    V_DIU, V_DJV, V_RDJU, V_RDIV, V_RP, V_DIDJP, V_RDIDJP,
-    V_RDIU, V_RDJV, V_RRP,
-    V_SCH,  // own layer, rows j0-2, j0-1 of the tile below (new values)
-    V_N
+// Copy groups staged per plane.  Fields of the skewed 3-D tensor: 0 sc1
+// (old values), 1 hsc1, 2 u, 3 v, 4 w, 5 rho, 6 gamsc1, 7 gamlam, 8 the new
+// values of sc1 (sentinel until computed; old values on ghost points).
+// Per group: layer offset, first field, fields, the plane window
+// [t+lo, t+hi] a point of plane t reads, and the tensor map it copies with
+// (0: 8 fields, 1: 4 fields, 2: 1 field, 3: the 2-D tables).
+enum { GR_OWN, GR_M1, GR_M2, GR_P1A, GR_P1B, GR_P2, GR_SCH, GR_2D, GR_N };
+struct GroupDesc {
+    int dk, f0, nf, lo, hi, map;
 };
-
-// per vector: source (0..7 a 3-D field: sc1 hsc1 u v w rho gamsc1 gamlam;
-// 8 + q the 2-D table q; 18 the new-value array), layer offset, and the
-// plane window [t+lo, t+hi] a point of plane t reads.  SCM1 and SCM2 read
-// the new-value array where their layer is an interior one.
-struct VecDesc {
-    int src, dk, lo, hi;
-};
-__host__ __device__ constexpr VecDesc vdesc(int v)
+__host__ __device__ constexpr GroupDesc gdesc(int g, bool fast)
 {
-    constexpr VecDesc d[V_N] = {
-        {0, 0, -2, 2}, {1, 0, 0, 0}, {2, 0, 0, 1}, {3, 0, 0, 1}, {4, 0, 0, 0}, {5, 0, -1, 1}, {6, 0, -1, 1},
-        {7, 0, -1, 1},
-        {0, -1, 0, 0}, {5, -1, 0, 0}, {6, -1, 0, 0}, {7, -1, 0, 0}, {0, -2, 0, 0},
-        {0, 1, 0, 0}, {5, 1, 0, 0}, {6, 1, 0, 0}, {7, 1, 0, 0}, {4, 1, 0, 0}, {0, 2, 0, 0},
-        {8, 0, -1, 2}, {9, 0, -1, 2}, {10, 0, 0, 1}, {11, 0, 0, 1}, {12, 0, 0, 0}, {13, 0, 0, 0},
-        {14, 0, 0, 0},
-        {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0},
-        {18, 0, -2, -1}};
-    return d[v];
+    return g == GR_OWN ? GroupDesc{0, 0, 8, -2, 2, 0}
+           : g == GR_M1 ? GroupDesc{-1, 5, 4, 0, 0, 1}   // rho gamsc1 gamlam new sc1 of k-1
+           : g == GR_M2 ? GroupDesc{-2, 8, 1, 0, 0, 2}   // new sc1 of k-2
+           : g == GR_P1A ? GroupDesc{1, 4, 4, 0, 0, 1}   // w rho gamsc1 gamlam of k+1
+           : g == GR_P1B ? GroupDesc{1, 0, 1, 0, 0, 2}   // old sc1 of k+1
+           : g == GR_P2 ? GroupDesc{2, 0, 1, 0, 0, 2}    // old sc1 of k+2
+           : g == GR_SCH ? GroupDesc{0, 8, 1, -2, -1, 2} // new sc1, rows of the tile below
+                         : GroupDesc{0, 0, fast ? 10 : 7, -1, 2, 3};
 }
-// ring slots of vector v for prefetch distance D: planes t+lo .. t+hi+D,
-// rounded up to a power of two so that a plane's slot is (p & (slots-1))
+// 2-D tables: diu djv rdju rdiv rp didjp rdidjp (1/diu 1/djv 1/rp)
+enum { T_DIU, T_DJV, T_RDJU, T_RDIV, T_RP, T_DIDJP, T_RDIDJP, T_RDIU, T_RDJV, T_RRP };
+
 __host__ __device__ constexpr int pow2_ceil(int n) { return n <= 1 ? 1 : 2 * pow2_ceil((n + 1) / 2); }
-__host__ __device__ constexpr int vslots(int v, int D) { return pow2_ceil(vdesc(v).hi - vdesc(v).lo + D + 1); }
-// ring slots before vector v (compile time)
-__host__ __device__ constexpr int vprefix(bool fast, int v, int D)
+// ring slots of group g: planes t+lo .. t+hi+D, a power of two (slot of
+// plane p = p & (slots-1))
+__host__ __device__ constexpr int gslots(int g, bool fast, int D)
 {
-    int s = 0;
-    for (int u = 0; u < v; u++)
-        if (fast || u < V_RDIU || u > V_RRP) s += vslots(u, D);
-    return s;
+    return pow2_ceil(gdesc(g, fast).hi - gdesc(g, fast).lo + D + 1);
 }
-// vectors of a build: the exact build has no reciprocal tables
-__host__ __device__ constexpr bool has_vec(bool fast, int v) { return fast || v < V_RDIU || v > V_RRP; }
-__host__ __device__ constexpr int ring_slots(bool fast, int D)
+// elements of one slot of group g for ring row width sw, rounded up to 128
+// bytes (the alignment of a tensor copy's destination)
+__host__ __device__ constexpr int gslot_elems(int g, bool fast, int sw, int esz)
 {
-    int s = 0;
-    for (int v = 0; v < V_N; v++)
-        if (has_vec(fast, v)) s += vslots(v, D);
-    return s;
+    return (gdesc(g, fast).nf * sw * esz + 127) / 128 * 128 / esz;
 }
-
-// the same table for lookups by a runtime vector index (the producer lane)
-__constant__ VecDesc c_vdesc[V_N] = {
-    {0, 0, -2, 2}, {1, 0, 0, 0}, {2, 0, 0, 1}, {3, 0, 0, 1}, {4, 0, 0, 0}, {5, 0, -1, 1}, {6, 0, -1, 1},
-    {7, 0, -1, 1},
-    {0, -1, 0, 0}, {5, -1, 0, 0}, {6, -1, 0, 0}, {7, -1, 0, 0}, {0, -2, 0, 0},
-    {0, 1, 0, 0}, {5, 1, 0, 0}, {6, 1, 0, 0}, {7, 1, 0, 0}, {4, 1, 0, 0}, {0, 2, 0, 0},
-    {8, 0, -1, 2}, {9, 0, -1, 2}, {10, 0, 0, 1}, {11, 0, 0, 1}, {12, 0, 0, 0}, {13, 0, 0, 0},
-    {14, 0, 0, 0},
-    {15, 0, -1, 2}, {16, 0, -1, 2}, {17, 0, 0, 0},
-    {18, 0, -2, -1}};
-
-template <bool FAST, int D> __device__ __forceinline__ int vprefix_rt(int v)
+// ring elements before group g
+__host__ __device__ constexpr int gbase(int g, bool fast, int D, int sw, int esz)
 {
     int s = 0;
-#pragma unroll
-    for (int u = 0; u < V_N; u++)
-        if (u < v && has_vec(FAST, u)) s += vslots(u, D);
+    for (int q = 0; q < g; q++) s += gslots(q, fast, D) * gslot_elems(q, fast, sw, esz);
     return s;
 }
 
-// the new-value array's initial value: the scalar is clamped to [0, 1]
+// the new-value array's initial value on interior points: the scalar is
+// clamped to [0, 1]
 constexpr float kSentinel = -1.0f;
 
 __device__ __forceinline__ float ld_strong(const float *p)
@@ -141,13 +119,57 @@ __device__ __forceinline__ void st_strong(double *p, double v)
     asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
 }
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+__device__ __forceinline__ void mbar_init(unsigned long long *m, int count)
 {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem)), "l"(gmem) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(count) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect(unsigned long long *m, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(m)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *m, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(smem_addr(m)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// one box of a 3-D tensor map (global memory) into shared memory by the TMA
+// unit, completing its bytes on the mbarrier
+__device__ __forceinline__ void tensor_copy(void *dst, const void *map, int x, int y, int z, unsigned long long *m)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_addr(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(m))
+        : "memory");
+}
+// wait for a phase of an mbarrier; bounded: after `limit` tries, or once
+// another CTA has set *err, give up (sets *err)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, int *err, long limit)
+{
+    long it = 0;
+    while (!mbar_try(m, parity)) {
+        if (++it > limit || *(volatile int *)err) {
+            atomicExch(err, 1);
+            return false;
+        }
+    }
+    return true;
+}
+// the same for the copies in flight when a tile ends, even after an error
+// elsewhere (they depend on nothing); bounded
+__device__ __forceinline__ void mbar_drain(unsigned long long *m, unsigned parity, int *err, long limit)
+{
+    long it = 0;
+    while (!mbar_try(m, parity))
+        if (++it > limit) {
+            atomicExch(err, 1);
+            return;
+        }
+}
 
 // A new value staged from the new-value array: while it is still the
 // sentinel, re-read it from L2 (another CTA is computing it); bounded by
@@ -245,41 +267,53 @@ __global__ void __launch_bounds__(256) k_unskew(const SkewBlk *__restrict__ sb, 
     }
 }
 
-// the new-value array's initial state
-template <typename S> __global__ void k_fill_sentinel(S *__restrict__ p, long n)
+// The new-value array's initial state: the sentinel on interior points,
+// the old scalar (field 0) on ghost points, which no tile changes
+template <typename S>
+__global__ void __launch_bounds__(256) k_init_new(const SkewBlk *__restrict__ sb, const S *__restrict__ old,
+                                                  S *__restrict__ nw)
 {
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
-        p[e] = (S)kSentinel;
+    const SkewBlk b = sb[blockIdx.y];
+    const long n = b.layer * b.n[2];
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+        const long kv = e / b.layer, rem = e - kv * b.layer;
+        const int p = (int)(rem / b.vp) + 2, jr = (int)(rem - (long)(p - 2) * b.vp);
+        const int i = p - (jr + 1), j = jr + 1, k = (int)kv + 1;
+        const bool inner = i >= 2 && i <= b.n[0] - 1 && j >= 2 && j <= b.n[1] - 1 && k >= 2 && k <= b.n[2] - 1;
+        nw[b.sk3 + e] = inner ? (S)kSentinel : old[b.sk3 + e];
+    }
 }
 
 // ----------------------------------------------------------- the pipeline
 // R: arithmetic type; S: storage type of the skewed copies; FAST: the
 // reciprocal tables of the fast builds; D: planes staged ahead.
-//
-// One CTA: three compute threads per row of the tile -- thread (d, r)
-// computes the two faces of axis d of the row's point (gradients, limited
-// face values, convective and diffusive fluxes), the x thread then adds
-// the three axes' flux differences in the reference's order and updates
-// the point -- and, last, one producer warp whose lanes stage the vectors
-// of each plane with 16-byte cp.async copies, one cp.async group per plane
-// step.  At plane step u the producer waits for its group u - (D-1); the
-// __syncthreads that opens step u+1 then publishes it to the compute
-// threads, which read group u+1-D there: D groups are in flight.
+// One CTA: compute warps (one thread per row of the tile) and, last, one
+// producer warp whose lane g issues the tensor copy of group g for each
+// plane.  Plane group u (the copies issued at the u-th plane step of the
+// CTA) completes mbarrier u % (D+1); warp 0 waits for group u - D before
+// plane step u and the __syncthreads that follows publishes it, so D
+// groups are in flight.
 template <typename R, typename S, bool FAST, int D>
-__global__ void __launch_bounds__(kSweepThreadsMax) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
+__global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A, double dtime_d, long limit)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     S *ring = (S *)smem_raw;
+    constexpr int G = D + 1;
+    __shared__ __align__(8) unsigned long long mbar[G];
     __shared__ int s_tile, s_ok[2];  // s_ok by plane parity: thread 0 may write the next before all read this
-    __shared__ R part[4][kSweepRows];  // y and z flux differences of each row's point
     constexpr int E = 16 / sizeof(S);  // elements per 16-byte chunk
+    constexpr int ESZ = sizeof(S);
     const R lambda = (R)4.0, small = (R)1.e-30, half = (R)0.5, one = (R)1.0, zero = (R)0.0;
     const R dtime = (R)dtime_d;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int rpad = ((int)blockDim.x - 32) / 3;  // rows per axis group (a multiple of 32)
-    const int ncomp = 3 * rpad;                    // compute threads
-    const bool producer = tid >= ncomp;
-    const int axis = producer ? 0 : tid / rpad, r = producer ? 0 : tid - axis * rpad;
+    const int nwc = (int)(blockDim.x >> 5) - 1;  // compute warps
+    const bool producer = (tid >> 5) == nwc;
+    const int SW = A.sw;
+    if (tid == 0)
+        for (int g = 0; g < G; g++) mbar_init(&mbar[g], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+    long ubase = 0;  // plane steps of earlier tiles (mbarrier phases continue)
     for (;;) {
         if (tid == 0) {
             int tk = -1;
@@ -294,16 +328,32 @@ __global__ void __launch_bounds__(kSweepThreadsMax) k_sc1_tiles(SweepArgs<S> A, 
         const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
         const int k = T.k, j0 = T.j0, j1 = T.j1;
         const int ni = n0 - 1, nj = n1 - 1, nk = n2 - 1;
+        const int np = n0 + n1 - 1;      // planes of a layer
         const bool jhalo = T.up_j >= 0;  // rows j0-2, j0-1 belong to another tile
-        // staged rows: j0-2 .. j1+1 (0-based jr), chunk aligned
-        const int sbase = (max(0, j0 - 3) / E) * E;
-        const int jr_lo = max(0, j0 - 3), jr_hi = min(n1, j1 + 1);  // [lo, hi)
-        const int SW = A.sw;
-        // own row and the plane range
-        const int j = j0 + r;
+        const int sbase = (max(0, j0 - 3) / E) * E;  // first staged row (0-based), 16-byte aligned
+        const int j = j0 + tid;
         const bool row = !producer && j < j1;
         const int t0 = 2 + j0, t1 = ni + (j1 - 1);
         const int ts = t0 - D - 4;
+        // producer lane g: group g's fixed parts
+        GroupDesc pg{0, 0, 0, 0, 0, 0};
+        bool pg_on = false;
+        const CUtensorMap *pg_map = nullptr;
+        unsigned pg_bytes = 0;
+        S *pg_ring = nullptr;
+        int pg_slots = 1, pg_slot_elems = 0;
+        if (producer && lane < GR_N) {
+            pg = gdesc(lane, FAST);
+            const int kv = k + pg.dk;
+            pg_on = kv >= 1 && kv <= n2 && (lane != GR_SCH || jhalo);
+            pg_map = (const CUtensorMap *)A.tmaps + 4 * T.blk + pg.map;
+            pg_bytes = (unsigned)(pg.nf * SW * ESZ);
+            pg_slots = pow2_ceil(pg.hi - pg.lo + D + 1);
+            pg_slot_elems = (pg.nf * SW * ESZ + 127) / 128 * 128 / ESZ;
+            int base = 0;
+            for (int q = 0; q < lane; q++) base += gslots(q, FAST, D) * gslot_elems(q, FAST, SW, ESZ);
+            pg_ring = ring + base;
+        }
         // 1-D metrics of this layer
         const double *dkp = A.dkp + b.off1k, *dkw = A.dkw + b.off1k;
         const R dkw_k = (R)dkw[k - 1];
@@ -317,215 +367,208 @@ __global__ void __launch_bounds__(kSweepThreadsMax) k_sc1_tiles(SweepArgs<S> A, 
             rdkp_m1 = (R)rdkp[k - 1];
             rdkp_0 = k < nk ? (R)rdkp[k] : zero;
         }
-        // ring element of vector v, plane p, row jj
+        // ring element of group g, field fl, plane p, row jj
         const int rowoff = j - 1 - sbase;
-        auto slot = [&](int v, int p, int jj) -> S & {
-            return ring[(vprefix(FAST, v, D) + (p & (vslots(v, D) - 1))) * SW + rowoff + (jj - j)];
+        auto slot = [&](int g, int fl, int p, int jj) -> S & {
+            return ring[gbase(g, FAST, D, SW, ESZ) + (p & (gslots(g, FAST, D) - 1)) * gslot_elems(g, FAST, SW, ESZ) +
+                        fl * SW + rowoff + (jj - j)];
         };
-        auto at = [&](int v, int p, int jj) -> R { return (R)slot(v, p, jj); };
+        auto at = [&](int g, int fl, int p, int jj) -> R { return (R)slot(g, fl, p, jj); };
         // element (plane p, row jj) of layer kv in a skewed 3-D array
         auto e3 = [&](int kv, int p, int jj) -> long {
             return b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp + (jj - 1);
         };
-        // a new value of layer kv at (p, jj), staged in vector v
-        auto newval = [&](int v, int kv, int p, int jj) -> R {
-            return (R)fresh<S>(slot(v, p, jj), A.scnew + e3(kv, p, jj), A.err, limit);
+        // a new value of layer kv at (p, jj), staged in group g, field fl
+        auto newval = [&](int g, int fl, int kv, int p, int jj) -> R {
+            return (R)fresh<S>(slot(g, fl, p, jj), A.scnew + e3(kv, p, jj), A.err, limit);
         };
-        // producer: the copies of group t, plane t + D + hi of every vector,
-        // chunks spread over the lanes
-        auto issue = [&](int t) {
-#pragma unroll
-            for (int v = 0; v < V_N; v++) {
-                if (!has_vec(FAST, v)) continue;
-                const VecDesc vd = vdesc(v);
-                const int p = t + D + vd.hi;
-                if (p < t0 + vd.lo || p > t1 + vd.hi || p < 2 || p > n0 + n1) continue;
-                const int kv = k + vd.dk;
-                if (kv < 1 || kv > n2) continue;
-                if (v == V_SCH && !jhalo) continue;
-                const bool cross = vd.dk != 0;
-                int lo = cross ? j0 - 1 : v == V_SCH ? max(0, j0 - 3) : jr_lo;
-                int hi = cross ? j1 - 1 : v == V_SCH ? j0 - 1 : jr_hi;
-                lo = max(lo, p - n0 - 1);
-                hi = min(hi, p - 1);
-                if (lo >= hi) continue;
-                const int c_lo = lo / E, c_hi = (hi + E - 1) / E;
-                const S *g;
-                if (vd.src < 8) {
-                    // new values of an interior layer below from the new-value array
-                    const bool nw = vd.src == 0 && vd.dk < 0 && kv >= 2 && kv <= n2 - 1;
-                    g = (nw ? A.scnew : A.f3[vd.src]) + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
-                } else if (vd.src < 18) {
-                    g = A.f2[vd.src - 8] + b.sk2 + (long)(p - 2) * b.vp;
-                } else {
-                    g = A.scnew + b.sk3 + b.layer * (kv - 1) + (long)(p - 2) * b.vp;
-                }
-                S *dst = ring + (vprefix(FAST, v, D) + (p & (vslots(v, D) - 1))) * SW - sbase;
-                for (int c = c_lo + lane; c < c_hi; c += 32) cp_async16(dst + c * E, g + c * E);
-            }
-        };
+#define SC(p, jj) at(GR_OWN, 0, p, jj)
+#define TB(tb, p, jj) at(GR_2D, tb, p, jj)
         bool ok = true;
         int t = ts;
         int err_seen = 0;  // thread 0: the error flag, re-read from L2 every 16 planes only
         for (; t <= t1; t++) {
+            const long u = ubase + (t - ts);
             if (tid == 0) {
                 if (((t - ts) & 15) == 0) err_seen = *(volatile int *)A.err;
                 s_ok[t & 1] = !err_seen;
             }
+            if (tid < 32 && u >= D) mbar_wait(&mbar[(u - D) % G], (unsigned)(((u - D) / G) & 1), A.err, limit);
             __syncthreads();
             if (!s_ok[t & 1]) {
                 ok = false;
                 break;
             }
             if (producer) {
-                issue(t);
-                cp_async_commit();
-                cp_async_wait<D - 1>();
+                // group u: plane t + D + hi of every copy group
+                const int p = t + D + pg.hi;
+                const bool go = pg_on && p >= t0 + pg.lo && p <= t1 + pg.hi && p >= 2 && p <= n0 + n1;
+                const unsigned total = __reduce_add_sync(0xffffffffu, go ? pg_bytes : 0u);
+                if (lane == 0) mbar_expect(&mbar[u % G], total);
+                __syncwarp();
+                if (go) {
+                    const int y = pg.map == 3 ? p - 2 : (k + pg.dk - 1) * np + (p - 2);
+                    tensor_copy(pg_ring + (p & (pg_slots - 1)) * pg_slot_elems, pg_map, sbase, y, pg.f0, &mbar[u % G]);
+                }
                 continue;
             }
+            if (t < t0 || !row) continue;
             const int i = t - j;
-            const bool pt = t >= t0 && row && i >= 2 && i <= ni;
-            // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands),
-            // axis by axis
-            R c_d = zero, t_d = zero;  // this axis: g_hi - g_lo and t_hi - t_lo
-            if (pt) {
-                const R s0 = at(V_SC, t, j);
-                const R rho0 = at(V_RHO, t, j), gs0 = at(V_GS, t, j), gl0 = at(V_GL, t, j);
-                const long gst = A.gstride;
-                const int gm = A.gm;
-                const double *GR = A.grad;
-                const int bi = T.blk;
-                R rlo, rhi, gslo, gshi, gllo, glhi, vlo, vhi, slo, shi, dlo, dmid, dhi;  // faces' operands
-                R areal, areah, glo_m, ghi_p;  // face areas; gradient beyond each face
-                int s_lo, s_hi;                // sides of the two faces
-                bool first, last;              // the point is the first / last interior one along the axis
-                if (axis == 0) {
-                    rlo = at(V_RHO, t - 1, j); rhi = at(V_RHO, t + 1, j);
-                    gslo = at(V_GS, t - 1, j); gshi = at(V_GS, t + 1, j);
-                    gllo = at(V_GL, t - 1, j); glhi = at(V_GL, t + 1, j);
-                    vlo = at(V_U, t, j); vhi = at(V_U, t + 1, j);
-                    slo = at(V_SC, t - 1, j); shi = at(V_SC, t + 1, j);
-#define QD(x, v, vr, pp, jj) (FAST ? (x) * at(vr, pp, jj) : (x) / at(v, pp, jj))
-                    dlo = QD(s0 - slo, V_DIU, V_RDIU, t, j);
-                    dhi = QD(shi - s0, V_DIU, V_RDIU, t + 1, j);
-                    first = i == 2;
-                    last = i == ni;
-                    s_lo = 0;
-                    s_hi = 1;
-                    glo_m = first ? ((b.bc[0] != LES_BCT_INTERFACE_D) ? dlo
-                                     : (R)GR[(long)(A.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)])
-                                  : QD(slo - at(V_SC, t - 2, j), V_DIU, V_RDIU, t - 1, j);
-                    ghi_p = last ? ((b.bc[1] != LES_BCT_INTERFACE_D) ? dhi
-                                    : (R)GR[(long)(A.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)])
-                                 : QD(at(V_SC, t + 2, j) - shi, V_DIU, V_RDIU, t + 2, j);
-                    areal = at(V_RDJU, t, j) * dkw_k;
-                    areah = at(V_RDJU, t + 1, j) * dkw_k;
-                } else if (axis == 1) {
-                    rlo = at(V_RHO, t - 1, j - 1); rhi = at(V_RHO, t + 1, j + 1);
-                    gslo = at(V_GS, t - 1, j - 1); gshi = at(V_GS, t + 1, j + 1);
-                    gllo = at(V_GL, t - 1, j - 1); glhi = at(V_GL, t + 1, j + 1);
-                    vlo = at(V_V, t, j); vhi = at(V_V, t + 1, j + 1);
-                    slo = (jhalo && j == j0) ? newval(V_SCH, k, t - 1, j - 1) : at(V_SC, t - 1, j - 1);
-                    shi = at(V_SC, t + 1, j + 1);
-                    dlo = QD(s0 - slo, V_DJV, V_RDJV, t, j);
-                    dhi = QD(shi - s0, V_DJV, V_RDJV, t + 1, j + 1);
-                    first = j == 2;
-                    last = j == nj;
-                    glo_m = first ? ((b.bc[2] != LES_BCT_INTERFACE_D) ? dlo
-                                     : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)])
-                                  : QD(slo - ((jhalo && j - 2 < j0) ? newval(V_SCH, k, t - 2, j - 2) : at(V_SC, t - 2, j - 2)),
-                                       V_DJV, V_RDJV, t - 1, j - 1);
-                    ghi_p = last ? ((b.bc[3] != LES_BCT_INTERFACE_D) ? dhi
-                                    : (R)GR[(long)(A.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)])
-                                 : QD(at(V_SC, t + 2, j + 2) - shi, V_DJV, V_RDJV, t + 2, j + 2);
+            if (i < 2 || i > ni) continue;
+            // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands)
+            const R rho0 = at(GR_OWN, 5, t, j);
+            const R rhowf = half * (rho0 + at(GR_OWN, 5, t - 1, j));
+            const R rhoef = half * (rho0 + at(GR_OWN, 5, t + 1, j));
+            const R rhosf = half * (rho0 + at(GR_OWN, 5, t - 1, j - 1));
+            const R rhonf = half * (rho0 + at(GR_OWN, 5, t + 1, j + 1));
+            const R rholf = half * (rho0 + at(GR_M1, 0, t, j));
+            const R rhorf = half * (rho0 + at(GR_P1A, 1, t, j));
+            const R rhop = rho0;
+            const R gs0 = at(GR_OWN, 6, t, j), gl0 = at(GR_OWN, 7, t, j);
+            const R gamwf = half * (gs0 + at(GR_OWN, 6, t - 1, j)) * rhowf + half * (gl0 + at(GR_OWN, 7, t - 1, j));
+            const R gamef = half * (gs0 + at(GR_OWN, 6, t + 1, j)) * rhoef + half * (gl0 + at(GR_OWN, 7, t + 1, j));
+            const R gamsf = half * (gs0 + at(GR_OWN, 6, t - 1, j - 1)) * rhosf + half * (gl0 + at(GR_OWN, 7, t - 1, j - 1));
+            const R gamnf = half * (gs0 + at(GR_OWN, 6, t + 1, j + 1)) * rhonf + half * (gl0 + at(GR_OWN, 7, t + 1, j + 1));
+            const R gamlf = half * (gs0 + at(GR_M1, 1, t, j)) * rholf + half * (gl0 + at(GR_M1, 2, t, j));
+            const R gamrf = half * (gs0 + at(GR_P1A, 2, t, j)) * rhorf + half * (gl0 + at(GR_P1A, 3, t, j));
+            const R uwf = at(GR_OWN, 2, t, j), uef = at(GR_OWN, 2, t + 1, j);
+            const R vsf = at(GR_OWN, 3, t, j), vnf = at(GR_OWN, 3, t + 1, j + 1);
+            const R wlf = at(GR_OWN, 4, t, j), wrf = at(GR_P1A, 0, t, j);
+            const R s0 = SC(t, j);
+            const R sw = SC(t - 1, j), se = SC(t + 1, j);
+            const R ss = (jhalo && j == j0) ? newval(GR_SCH, 0, k, t - 1, j - 1) : SC(t - 1, j - 1);
+            const R sn = SC(t + 1, j + 1);
+            // the layer below: new values (interior), old ones on its ghost layer
+            const R sl = newval(GR_M1, 3, k - 1, t, j);
+            const R sr = at(GR_P1B, 0, t, j);
+#define QD(x, tb, rtb, pp, jj) (FAST ? (x) * TB(rtb, pp, jj) : (x) / TB(tb, pp, jj))
+            const R dfdxwf = QD(s0 - sw, T_DIU, T_RDIU, t, j);
+            const R dfdxef = QD(se - s0, T_DIU, T_RDIU, t + 1, j);
+            const long gst = A.gstride;
+            const int gm = A.gm;
+            const double *GR = A.grad;
+            const int bi = T.blk;
+            R dfdxwwf, dfdxeef, dfdyssf, dfdynnf, dfdzllf, dfdzrrf;
+            if (i == 2)
+                dfdxwwf = (b.bc[0] != LES_BCT_INTERFACE_D)
+                              ? dfdxwf
+                              : (R)GR[(long)(A.link[bi * 6 + 0]) * 6 * gst + 1 * gst + (j - 1) + (long)gm * (k - 1)];
+            else
+                dfdxwwf = QD(sw - SC(t - 2, j), T_DIU, T_RDIU, t - 1, j);
+            if (i == ni)
+                dfdxeef = (b.bc[1] != LES_BCT_INTERFACE_D)
+                              ? dfdxef
+                              : (R)GR[(long)(A.link[bi * 6 + 1]) * 6 * gst + 0 * gst + (j - 1) + (long)gm * (k - 1)];
+            else
+                dfdxeef = QD(SC(t + 2, j) - se, T_DIU, T_RDIU, t + 2, j);
+            const R dfdysf = QD(s0 - ss, T_DJV, T_RDJV, t, j);
+            const R dfdynf = QD(sn - s0, T_DJV, T_RDJV, t + 1, j + 1);
+            if (j == 2)
+                dfdyssf = (b.bc[2] != LES_BCT_INTERFACE_D)
+                              ? dfdysf
+                              : (R)GR[(long)(A.link[bi * 6 + 2]) * 6 * gst + 3 * gst + (i - 1) + (long)gm * (k - 1)];
+            else
+                dfdyssf = QD(ss - ((jhalo && j - 2 < j0) ? newval(GR_SCH, 0, k, t - 2, j - 2) : SC(t - 2, j - 2)),
+                             T_DJV, T_RDJV, t - 1, j - 1);
+            if (j == nj)
+                dfdynnf = (b.bc[3] != LES_BCT_INTERFACE_D)
+                              ? dfdynf
+                              : (R)GR[(long)(A.link[bi * 6 + 3]) * 6 * gst + 2 * gst + (i - 1) + (long)gm * (k - 1)];
+            else
+                dfdynnf = QD(SC(t + 2, j + 2) - sn, T_DJV, T_RDJV, t + 2, j + 2);
 #undef QD
-                    areal = at(V_RDIV, t, j) * dkw_k;
-                    areah = at(V_RDIV, t + 1, j + 1) * dkw_k;
-                    s_lo = 2;
-                    s_hi = 3;
-                } else {
-                    rlo = at(V_RHOM1, t, j); rhi = at(V_RHOP1, t, j);
-                    gslo = at(V_GSM1, t, j); gshi = at(V_GSP1, t, j);
-                    gllo = at(V_GLM1, t, j); glhi = at(V_GLP1, t, j);
-                    vlo = at(V_W, t, j); vhi = at(V_WP1, t, j);
-                    slo = k - 1 >= 2 ? newval(V_SCM1, k - 1, t, j) : at(V_SCM1, t, j);
-                    shi = at(V_SCP1, t, j);
-                    const R rpij = at(V_RP, t, j);
-                    const R rrpij = FAST ? at(V_RRP, t, j) : zero;
+            const R rpij = TB(T_RP, t, j);
+            const R rrpij = FAST ? TB(T_RRP, t, j) : zero;
 #define QZ(x, dk_, rdk_) (FAST ? (x) * (rrpij * (rdk_)) : (x) / (rpij * (dk_)))
-                    dlo = QZ(s0 - slo, dkp_m2, rdkp_m2);
-                    dhi = QZ(shi - s0, dkp_m1, rdkp_m1);
-                    first = k == 2;
-                    last = k == nk;
-                    glo_m = first ? ((b.bc[4] != LES_BCT_INTERFACE_D) ? dlo
-                                     : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)])
-                                  : QZ(slo - (k - 2 >= 2 ? newval(V_SCM2, k - 2, t, j) : at(V_SCM2, t, j)), dkp_m3, rdkp_m3);
-                    ghi_p = last ? ((b.bc[5] != LES_BCT_INTERFACE_D) ? dhi
-                                    : (R)GR[(long)(A.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)])
-                                 : QZ(at(V_SCP2, t, j) - shi, dkp_0, rdkp_0);
+            const R dfdzlf = QZ(s0 - sl, dkp_m2, rdkp_m2);
+            const R dfdzrf = QZ(sr - s0, dkp_m1, rdkp_m1);
+            if (k == 2)
+                dfdzllf = (b.bc[4] != LES_BCT_INTERFACE_D)
+                              ? dfdzlf
+                              : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
+            else
+                dfdzllf = QZ(sl - newval(GR_M2, 0, k - 2, t, j), dkp_m3, rdkp_m3);
+            if (k == nk)
+                dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D)
+                              ? dfdzrf
+                              : (R)GR[(long)(A.link[bi * 6 + 5]) * 6 * gst + 4 * gst + (i - 1) + (long)gm * (j - 1)];
+            else
+                dfdzrrf = QZ(at(GR_P2, 0, t, j) - sr, dkp_0, rdkp_0);
 #undef QZ
-                    areal = at(V_DIDJP, t, j);
-                    areah = areal;
-                    s_lo = 4;
-                    s_hi = 5;
-                }
-                (void)s_lo;
-                (void)s_hi;
-                (void)dmid;
-                const R rholf = half * (rho0 + rlo);
-                const R rhohf = half * (rho0 + rhi);
-                const R gamlf = half * (gs0 + gslo) * rholf + half * (gl0 + gllo);
-                const R gamhf = half * (gs0 + gshi) * rhohf + half * (gl0 + glhi);
-                // low face tests v >= 0, high face v > 0 (rwst / rest of the reference)
-                const R rl = (vlo >= zero) ? (glo_m + small) / (dlo + small) : (dhi + small) / (dlo + small);
-                const R rh = (vhi > zero) ? (dlo + small) / (dhi + small) : (ghi_p + small) / (dhi + small);
-                const R liml = fmax(zero, fmin(lambda * rl, one));
-                const R limh = fmax(zero, fmin(lambda * rh, one));
-                R fl, fh;
-                if (vlo > zero) fl = slo + half * liml * (s0 - slo);
-                else if (vlo < zero) fl = s0 + half * liml * (slo - s0);
-                else fl = half * (s0 + slo);
-                if (vhi > zero) fh = s0 + half * limh * (shi - s0);
-                else if (vhi < zero) fh = shi + half * limh * (s0 - shi);
-                else fh = half * (s0 + shi);
-                const R gl_ = rholf * vlo * fl * areal;
-                const R gh_ = rhohf * vhi * fh * areah;
-                const R tl_ = gamlf * areal * dlo;
-                const R th_ = gamhf * areah * dhi;
-                c_d = gh_ - gl_;
-                t_d = th_ - tl_;
-                if (axis > 0) {
-                    part[2 * (axis - 1)][r] = c_d;
-                    part[2 * (axis - 1) + 1][r] = t_d;
-                }
-            }
-            asm volatile("bar.sync 1, %0;" ::"r"(ncomp) : "memory");  // the compute threads
-            if (pt && axis == 0) {
-                // combine in the reference's order:
-                // convf = -(gef - gwf) - (gnf - gsf) - (grf - glf), difff likewise
-                const R convf = -c_d - part[0][r] - part[2][r];
-                const R difff = (t_d + part[1][r]) + part[3][r];
-                const R h = convf + difff;
-                const R s0 = at(V_SC, t, j);
-                const R vol = at(V_RDIDJP, t, j) * dkw_k;
-                R tmp = s0 + dtime / (vol * at(V_RHO, t, j)) * ((R)1.5 * h - half * at(V_H, t, j));
-                if (tmp < zero) tmp = zero;
-                if (tmp > one) tmp = one;
-                // the new value: in the ring slot of plane t (read by later
-                // planes of this tile) and in the new-value array (read by the
-                // layers above and the tile above); the history in place
-                slot(V_SC, t, j) = (S)tmp;
-                const long e = e3(k, t, j);
-                st_strong(A.scnew + e, (S)tmp);
-                A.f3[1][e] = (S)h;
-            }
+            const R rwst = (uwf >= zero) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
+            const R rest = (uef > zero) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
+            const R rsth = (vsf >= zero) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
+            const R rnth = (vnf > zero) ? (dfdysf + small) / (dfdynf + small) : (dfdynnf + small) / (dfdynf + small);
+            const R rlft = (wlf >= zero) ? (dfdzllf + small) / (dfdzlf + small) : (dfdzrf + small) / (dfdzlf + small);
+            const R rrht = (wrf > zero) ? (dfdzlf + small) / (dfdzrf + small) : (dfdzrrf + small) / (dfdzrf + small);
+            const R limw = fmax(zero, fmin(lambda * rwst, one));
+            const R lime = fmax(zero, fmin(lambda * rest, one));
+            const R lims = fmax(zero, fmin(lambda * rsth, one));
+            const R limn = fmax(zero, fmin(lambda * rnth, one));
+            const R liml = fmax(zero, fmin(lambda * rlft, one));
+            const R limr = fmax(zero, fmin(lambda * rrht, one));
+            R fwf, fef, fsf, fnf, flf, frf;
+            if (uwf > zero) fwf = sw + half * limw * (s0 - sw);
+            else if (uwf < zero) fwf = s0 + half * limw * (sw - s0);
+            else fwf = half * (s0 + sw);
+            if (uef > zero) fef = s0 + half * lime * (se - s0);
+            else if (uef < zero) fef = se + half * lime * (s0 - se);
+            else fef = half * (s0 + se);
+            if (vsf > zero) fsf = ss + half * lims * (s0 - ss);
+            else if (vsf < zero) fsf = s0 + half * lims * (ss - s0);
+            else fsf = half * (s0 + ss);
+            if (vnf > zero) fnf = s0 + half * limn * (sn - s0);
+            else if (vnf < zero) fnf = sn + half * limn * (s0 - sn);
+            else fnf = half * (s0 + sn);
+            if (wlf > zero) flf = sl + half * liml * (s0 - sl);
+            else if (wlf < zero) flf = s0 + half * liml * (sl - s0);
+            else flf = half * (s0 + sl);
+            if (wrf > zero) frf = s0 + half * limr * (sr - s0);
+            else if (wrf < zero) frf = sr + half * limr * (s0 - sr);
+            else frf = half * (s0 + sr);
+            const R areawf = TB(T_RDJU, t, j) * dkw_k;
+            const R areaef = TB(T_RDJU, t + 1, j) * dkw_k;
+            const R areasf = TB(T_RDIV, t, j) * dkw_k;
+            const R areanf = TB(T_RDIV, t + 1, j + 1) * dkw_k;
+            const R areak = TB(T_DIDJP, t, j);
+            const R vol = TB(T_RDIDJP, t, j) * dkw_k;
+            const R gwf = rhowf * uwf * fwf * areawf;
+            const R gef = rhoef * uef * fef * areaef;
+            const R gsf = rhosf * vsf * fsf * areasf;
+            const R gnf = rhonf * vnf * fnf * areanf;
+            const R glf = rholf * wlf * flf * areak;
+            const R grf = rhorf * wrf * frf * areak;
+            const R convf = -(gef - gwf) - (gnf - gsf) - (grf - glf);
+            const R twf = gamwf * areawf * dfdxwf;
+            const R tef = gamef * areaef * dfdxef;
+            const R tsf = gamsf * areasf * dfdysf;
+            const R tnf = gamnf * areanf * dfdynf;
+            const R tlf = gamlf * areak * dfdzlf;
+            const R trf = gamrf * areak * dfdzrf;
+            const R difff = (tef - twf) + (tnf - tsf) + (trf - tlf);
+            const R h = convf + difff;
+            R tmp = s0 + dtime / (vol * rhop) * ((R)1.5 * h - half * at(GR_OWN, 1, t, j));
+            if (tmp < zero) tmp = zero;
+            if (tmp > one) tmp = one;
+            // the new value: in the ring slot of plane t (read by later
+            // planes of this tile) and in the new-value array (read by the
+            // layers above and the tile above); the history in place
+            slot(GR_OWN, 0, t, j) = (S)tmp;
+            const long e = e3(k, t, j);
+            st_strong(A.scnew + e, (S)tmp);
+            A.f3[1][e] = (S)h;
         }
-        // the copies still in flight land before the ring is reused or the
-        // CTA exits
-        if (producer) cp_async_wait_all();
+        // the copies still in flight (issued, never waited for) land before
+        // the ring is reused or the CTA exits
+        const long uend = ubase + (t - ts);  // groups issued: ubase .. uend-1
+        if (producer && lane == 0)
+            for (long w = max(ubase, uend - D); w < uend; w++) mbar_drain(&mbar[w % G], (unsigned)((w / G) & 1), A.err, limit);
         __syncthreads();
+        ubase = uend;
         if (!ok) return;
     }
+#undef SC
+#undef TB
 }
 
 } // namespace
@@ -553,17 +596,18 @@ void launch_unskew_t(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2,
     les::count_launch(1);
 }
 
-template <typename S> void launch_fill_t(S *p, long n, cudaStream_t st)
+template <typename S>
+void launch_init_new_t(const SkewBlk *sb, int nb, const S *old, S *nw, cudaStream_t st)
 {
-    long g = (n + 255) / 256;
-    k_fill_sentinel<S><<<(unsigned)(g > 8192 ? 8192 : g), 256, 0, st>>>(p, n);
+    k_init_new<S><<<dim3(2048, nb), 256, 0, st>>>(sb, old, nw);
     les::count_launch(1);
 }
 
+// dynamic shared memory of the ring for row width sw
 template <typename R, typename S, bool FAST, int D>
 int tiles_smem(int sw)
 {
-    return ring_slots(FAST, D) * sw * (int)sizeof(S);
+    return gbase(GR_N, FAST, D, sw, (int)sizeof(S)) * (int)sizeof(S);
 }
 
 template <typename R, typename S, bool FAST, int D>
@@ -615,7 +659,10 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 {
     launch_unskew_t<ST>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
 }
-void launch_sweep_fill(double *p, long n, cudaStream_t st) { launch_fill_t<ST>(p, n, st); }
+void launch_sweep_init_new(const SkewBlk *sb, int nb, const double *old, double *nw, cudaStream_t st)
+{
+    launch_init_new_t<ST>(sb, nb, old, nw, st);
+}
 int sweep_tiles_smem(int sw) { return tiles_smem<RT, ST, kFast, kSweepDepth>(sw); }
 int sweep_tiles_max_ctas(int sw, int nthr) { return tiles_max_ctas<RT, ST, kFast, kSweepDepth>(sw, nthr); }
 cudaError_t launch_sweep_tiles(const SweepArgs<double> &a, double dtime, long limit, int nctas, int nthr,
@@ -640,7 +687,10 @@ void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int ma
 {
     les_fast::launch_unskew_t<float>(sb, nb, maxn0, maxn1, maxn2, sks, skh, sc1, hsc1, st);
 }
-void launch_sweep_fill(float *p, long n, cudaStream_t st) { les_fast::launch_fill_t<float>(p, n, st); }
+void launch_sweep_init_new(const SkewBlk *sb, int nb, const float *old, float *nw, cudaStream_t st)
+{
+    les_fast::launch_init_new_t<float>(sb, nb, old, nw, st);
+}
 int sweep_tiles_smem(int sw) { return les_fast::tiles_smem<float, float, true, kSweepDepth>(sw); }
 int sweep_tiles_max_ctas(int sw, int nthr) { return les_fast::tiles_max_ctas<float, float, true, kSweepDepth>(sw, nthr); }
 cudaError_t launch_sweep_tiles(const SweepArgs<float> &a, double dtime, long limit, int nctas, int nthr,

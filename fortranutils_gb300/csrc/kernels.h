@@ -246,7 +246,7 @@ LES_PHYS_LAUNCHERS
     void launch_sweep_unskew(const SkewBlk *sb, int nb, int maxn0, int maxn1, int maxn2,           \
                              const S *sks, const S *skh, double *sc1, double *hsc1,                \
                              cudaStream_t st);                                                      \
-    void launch_sweep_fill(S *p, long n, cudaStream_t st);                                          \
+    void launch_sweep_init_new(const SkewBlk *sb, int nb, const S *old, S *nw, cudaStream_t st);    \
     int sweep_tiles_smem(int sw);                                                                   \
     int sweep_tiles_max_ctas(int sw, int nthr);                                                     \
     cudaError_t launch_sweep_tiles(const SweepArgs<S> &a, double dtime, long limit, int nctas,     \

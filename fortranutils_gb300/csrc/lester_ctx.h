@@ -166,6 +166,7 @@ struct Ctx {
         int sw[3] = {0, 0, 0};        // ring row width (elements)
         int nthr[3] = {0, 0, 0};      // threads per CTA: row warps + the producer warp
         int maxctas[3] = {0, 0, 0};   // resident CTAs; -1 none
+        void *d_tmaps[3] = {nullptr, nullptr, nullptr};  // TMA tensor maps over d_sk (k_sweep.cu)
     } sw;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)

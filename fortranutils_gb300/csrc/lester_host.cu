@@ -475,7 +475,10 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_wslice);
     cudaFree(c->d_wave);
     cudaFree(c->sw.d_sb);
-    for (int q = 0; q < 3; q++) cudaFree(c->sw.d_tiles[q]);
+    for (int q = 0; q < 3; q++) {
+        cudaFree(c->sw.d_tiles[q]);
+        cudaFree(c->sw.d_tmaps[q]);
+    }
     cudaFree(c->sw.d_sync);
     cudaFree(c->sw.d_sk[0]);
     cudaFree(c->sw.d_sk[1]);

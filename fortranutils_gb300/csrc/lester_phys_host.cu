@@ -1,6 +1,7 @@
 // lester_phys_host.cu -- C ABI entry points of the momentum predictor and
 // the scalar transport (include/lester_gpu.h).
 #include <cstring>
+#include <cuda.h>
 #include <vector>
 #include "kernels.h"
 #include "lester_ctx.h"
@@ -113,7 +114,7 @@ static int ensure_sweep_geom(Ctx &c)
 // Tiles of build `var` (0 exact, 1 fast, 2 FP32), built on first use.  A
 // block's interior rows are split into as few tiles as the build's ring
 // allows (its shared memory grows with the rows of a tile; at most
-// kSweepRows rows); one tile per (block, interior layer k, row range),
+// kSweepThreads rows); one tile per (block, interior layer k, row range),
 // in ticket order (k, row range, block): every tile comes after the two
 // whose new values it reads, (k-1, same rows) and (k, rows below).
 static int ensure_sweep_tiles(Ctx &c, int var)
@@ -124,12 +125,15 @@ static int ensure_sweep_tiles(Ctx &c, int var)
     if (W.d_tiles[var] || W.maxctas[var] < 0) return 0;
     const int nb = c.g.numbl;
     const int E = var == 2 ? 4 : 2;  // elements per 16-byte chunk
-    // shared memory per element of ring row width; rows such that the ring
-    // fits the 227 KB a CTA may have (with the ring's 12 rows of halo and
-    // chunk rounding)
-    const int per = var == 0 ? les_exact::sweep_tiles_smem(1) : var == 1 ? les_fast::sweep_tiles_smem(1)
-                                                                         : les_f32::sweep_tiles_smem(1);
-    const int rows_max = std::min(kSweepRows, (227 * 1024 - 8192) / per - 12);  // static: partials
+    // rows per tile: as many as kSweepThreads, with the ring for them (row
+    // width rows + 4 halo rows + chunk rounding) within the 227 KB a CTA
+    // may have
+    auto smem_of = [&](int sw) {
+        return var == 0 ? les_exact::sweep_tiles_smem(sw) : var == 1 ? les_fast::sweep_tiles_smem(sw)
+                                                                     : les_f32::sweep_tiles_smem(sw);
+    };
+    int rows_max = kSweepThreads;
+    while (rows_max >= 8 && smem_of(rows_max + 4 + 2 * E) > 227 * 1024 - 1024) rows_max--;
     if (rows_max < 8) {
         W.maxctas[var] = -1;
         return 0;
@@ -173,7 +177,7 @@ static int ensure_sweep_tiles(Ctx &c, int var)
         w = std::max(w, hi - sbase);
     }
     W.sw[var] = w;
-    W.nthr[var] = 3 * 32 * ((rows_big + 31) / 32) + 32;  // three row groups + the producer warp
+    W.nthr[var] = 32 * ((rows_big + 31) / 32) + 32;  // row warps + the producer warp
     if (W.ntile[var] == 0) {
         W.maxctas[var] = -1;
         return 0;
@@ -186,6 +190,71 @@ static int ensure_sweep_tiles(Ctx &c, int var)
                   : var == 1 ? les_fast::sweep_tiles_max_ctas(w, W.nthr[var])
                              : les_f32::sweep_tiles_max_ctas(w, W.nthr[var]);
     W.maxctas[var] = n > 0 ? n : -1;
+    return 0;
+}
+
+// TMA tensor maps of build `var` over the skewed copies of storage q (0
+// FP64, 1 FP32), built once the copies exist: per block, the 3-D fields as
+// (rows, planes of all layers, fields) in boxes of 8, 4 and 1 fields of
+// one plane, and the ntab 2-D tables as (rows, planes, tables).  The map
+// encoder is the driver's, reached through the runtime.
+typedef CUresult (*PfnEncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int ensure_tensor_maps(Ctx &c, int var, int q, int ntab)
+{
+    Ctx::SweepState &W = c.sw;
+    if (W.d_tmaps[var]) return 0;
+    static PfnEncodeTiled encode = nullptr;
+    if (!encode) {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+            qr != cudaDriverEntryPointSuccess || !f) {
+            cudaGetLastError();
+            return set_err(LES_ERR_CUDA, "set_sc1: cuTensorMapEncodeTiled unavailable");
+        }
+        encode = (PfnEncodeTiled)f;
+    }
+    const int nb = c.g.numbl;
+    const size_t es = q == 1 ? sizeof(float) : sizeof(double);
+    const CUtensorMapDataType dt = q == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+    char *base = (char *)W.d_sk[q];
+    const cuuint32_t sw = (cuuint32_t)W.sw[var];
+    std::vector<CUtensorMap> maps(4 * nb);
+    for (int b = 1; b <= nb; b++) {
+        const int *n = c.lv[1].n[b];
+        const cuuint64_t vp = (cuuint64_t)((n[1] + 3) & ~3), np = (cuuint64_t)(n[0] + n[1] - 1);
+        // the block's offsets in the skewed arrays (as ensure_sweep_geom lays them out)
+        long sk3 = 0, sk2 = 0;
+        for (int q2 = 1; q2 < b; q2++) {
+            const int *m = c.lv[1].n[q2];
+            const long lay = (long)(m[0] + m[1] - 1) * ((m[1] + 3) & ~3);
+            sk3 += lay * m[2];
+            sk2 += lay;
+        }
+        const cuuint64_t dim3[3] = {vp, np * (cuuint64_t)n[2], 9};
+        const cuuint64_t str3[2] = {vp * es, (cuuint64_t)W.tot3 * es};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        const cuuint32_t nf[3] = {8, 4, 1};
+        for (int m = 0; m < 3; m++) {
+            const cuuint32_t box[3] = {sw, 1, nf[m]};
+            CUresult e = encode(&maps[4 * (b - 1) + m], dt, 3, base + es * sk3, dim3, str3, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (e != CUDA_SUCCESS) return set_err(LES_ERR_CUDA, "set_sc1: tensor map (block %d): error %d", b, (int)e);
+        }
+        const cuuint64_t dim2[3] = {vp, np, (cuuint64_t)ntab};
+        const cuuint64_t str2[2] = {vp * es, (cuuint64_t)W.tot2 * es};
+        const cuuint32_t box2[3] = {sw, 1, (cuuint32_t)ntab};
+        CUresult e = encode(&maps[4 * (b - 1) + 3], dt, 3, base + es * (9 * W.tot3 + sk2), dim2, str2, box2, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (e != CUDA_SUCCESS) return set_err(LES_ERR_CUDA, "set_sc1: tensor map of the tables (block %d): error %d", b, (int)e);
+    }
+    LES_CUDA(cudaMalloc(&W.d_tmaps[var], sizeof(CUtensorMap) * maps.size()));
+    LES_CUDA(cudaMemcpy(W.d_tmaps[var], maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -211,13 +280,14 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
                                         cudaStream_t),
                            void (*unskew)(const SkewBlk *, int, int, int, int, const S *, const S *, double *,
                                           double *, cudaStream_t),
-                           void (*fill)(S *, long, cudaStream_t),
+                           void (*init_new)(const SkewBlk *, int, const S *, S *, cudaStream_t),
                            cudaError_t (*launch)(const SweepArgs<S> &, double, long, int, int, cudaStream_t))
 {
     Ctx::SweepState &W = c.sw;
     const int nb = c.g.numbl;
     const bool fast = !c.c.exact;
     const int var = sweep_variant(c);
+    int r;
     if (!W.d_sk[q]) {
         const size_t bytes = sizeof(S) * (9 * W.tot3 + 10 * W.tot2);
         if (cudaMalloc(&W.d_sk[q], bytes) != cudaSuccess) {
@@ -262,7 +332,9 @@ static int run_sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, 
     a.scnew = base + 8 * W.tot3;
     a.ticket = W.d_sync;
     a.err = W.d_sync + 1;
-    fill(a.scnew, W.tot3, c.stream);
+    if ((r = ensure_tensor_maps(c, var, q, fast ? 10 : 7))) return r;
+    a.tmaps = W.d_tmaps[var];
+    init_new(W.d_sb, nb, P3.dst[0], a.scnew, c.stream);
     LES_CUDA(cudaMemsetAsync(W.d_sync, 0, sizeof(int) * 2, c.stream));
     const int nctas = std::min(W.ntile[var], W.maxctas[var]);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -289,13 +361,13 @@ static int sweep_tiles(Ctx &c, const Sc1Args &A, const double *const *rtab, cons
 {
     if (phys32_on(c))
         return run_sweep_tiles<float>(c, A, rtab, rdkp, 1, les_f32::launch_sweep_skew, les_f32::launch_sweep_unskew,
-                                      les_f32::launch_sweep_fill, les_f32::launch_sweep_tiles);
+                                      les_f32::launch_sweep_init_new, les_f32::launch_sweep_tiles);
     if (c.c.exact)
         return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_exact::launch_sweep_skew,
-                                       les_exact::launch_sweep_unskew, les_exact::launch_sweep_fill,
+                                       les_exact::launch_sweep_unskew, les_exact::launch_sweep_init_new,
                                        les_exact::launch_sweep_tiles);
     return run_sweep_tiles<double>(c, A, rtab, rdkp, 0, les_fast::launch_sweep_skew, les_fast::launch_sweep_unskew,
-                                   les_fast::launch_sweep_fill, les_fast::launch_sweep_tiles);
+                                   les_fast::launch_sweep_init_new, les_fast::launch_sweep_tiles);
 }
 
 static int wave_range(Ctx &c, int &smin, int &smax)
