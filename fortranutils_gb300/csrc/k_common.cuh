@@ -201,7 +201,7 @@ struct SweepTile {
 };
 
 constexpr int kSweepThreads = 256;  // rows per tile at most (one thread per row)
-constexpr int kSweepDepth = 2;      // planes staged ahead
+constexpr int kSweepDepth = 1;      // planes staged ahead
 
 // sources (FP64, reference layout) and skewed destinations of one k_skew
 // launch: up to 10 fields or tables

@@ -259,12 +259,16 @@ static int ensure_tensor_maps(Ctx &c, int var, int q, int ntab)
 }
 
 // Which scalar sweep runs (ctrl.sc1_sweep): 1 the hyperplane sweep, 2 the
-// tile pipeline, 3 one launch per plane; 0 the tile pipeline where its
-// ring fits, else the hyperplane sweep.  Negative: an error.
+// tile pipeline, 3 one launch per plane; 0 the tile pipeline for the FP32
+// physics build where its ring fits, else the hyperplane sweep (with FP64
+// arithmetic the hyperplane sweep, which spreads each plane over every SM,
+// is the faster: GB300's FP64 rate bounds both, 8.0 against 10.0 ms on the
+// 256x192x128 mixing layer).  Negative: an error.
 static int sweep_choice(Ctx &c)
 {
     const int m = c.c.sc1_sweep;
     if (m == 1 || m == 3) return m;
+    if (m == 0 && !phys32_on(c)) return 1;
     const int var = sweep_variant(c);
     int r;
     if ((r = ensure_sweep_tiles(c, var))) return r;

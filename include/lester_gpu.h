@@ -153,14 +153,15 @@ typedef struct lester_ctrl {
                           fields, no inflow/outflow sides, autotuning
                           finished); otherwise the step runs as launched */
     int sc1_sweep;     /* in-place scalar sweep of set_sc1: 0 = automatic
-                          (the tile pipeline where its tiles fit, else the
-                          hyperplane sweep); 1 = hyperplane sweep, one
-                          cooperative launch with a grid barrier per
-                          i+j+k plane; 2 = tile pipeline, one CTA per
-                          (block, k, row range) tile walking the planes
-                          i+j with point-to-point progress flags; 3 = one
-                          launch per i+j+k plane.  All give the same
-                          result for a given physics build. */
+                          (the tile pipeline with FP32 physics where its
+                          shared-memory ring fits, else the hyperplane
+                          sweep); 1 = hyperplane sweep, one cooperative
+                          launch with a grid barrier per i+j+k plane; 2 =
+                          tile pipeline, one CTA per (block, k, row range)
+                          tile walking the planes i+j, the layers a
+                          wavefront apart; 3 = one launch per i+j+k plane.
+                          The exact build gives the same result bit for bit
+                          with each; the builds with FMA agree to rounding. */
     int wait_limit;    /* bounded device waits (grid barrier, progress
                           flags): polls before a wait gives up and the call
                           returns LES_ERR_TIMEOUT; 0 = the default (2^24) */
