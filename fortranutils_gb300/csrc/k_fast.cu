@@ -539,13 +539,39 @@ __device__ void tail_smooth(const VLev &L, int nb, int nsweep, T omega, const T 
         }
 }
 
+// With `span` > 0 the tail's slice of the multigrid arrays (levels l0..L,
+// elements [start, start + span)) is first copied into shared memory --
+// x and b, and E, N, R, D unless the couplings are matrix-free -- and the
+// same phases run there, each a __syncthreads apart instead of an L2
+// round trip; x of the slice is copied back at the end (level l0's is
+// what the prolongation to level l0-1 reads).
 template <typename T>
 __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int l0, int L, int nb,
                                                 int pre, int crs, T omega, int singular,
                                                 const T *__restrict__ E, const T *__restrict__ N,
                                                 const T *__restrict__ R, const T *__restrict__ D,
-                                                T *__restrict__ x, T *__restrict__ bb, MfTab<T> mf)
+                                                T *__restrict__ x, T *__restrict__ bb, MfTab<T> mf,
+                                                long start, long span)
 {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    T *const xg = x;
+    if (span > 0) {
+        T *s = (T *)tail_smem;
+        const int na = mf.E2 ? 2 : 6;
+        const T *src[6] = {x, bb, E, N, R, D};
+        for (int a = 0; a < na; a++)
+            for (long q = threadIdx.x; q < span; q += blockDim.x) s[a * span + q] = src[a][start + q];
+        __syncthreads();
+        // the same indices (off3 of the levels) address the shared copies
+        x = s - start;
+        bb = s + span - start;
+        if (!mf.E2) {
+            E = s + 2 * span - start;
+            N = s + 3 * span - start;
+            R = s + 4 * span - start;
+            D = s + 5 * span - start;
+        }
+    }
     for (int lev = l0; lev < L; lev++) {
         tail_smooth(lv[lev], nb, pre, omega, E, N, R, D, x, bb, mf);
         for (int bi = 0; bi < nb; bi++) {
@@ -571,6 +597,10 @@ __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int 
         }
         __syncthreads();
         tail_smooth(lv[lev], nb, pre, omega, E, N, R, D, x, bb, mf);
+    }
+    if (span > 0) {
+        __syncthreads();
+        for (long q = threadIdx.x; q < span; q += blockDim.x) xg[start + q] = x[start + q];
     }
 }
 
@@ -932,10 +962,31 @@ void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int m
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
-                  cudaStream_t st)
+                  long start, long span, cudaStream_t st)
 {
-    k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf);
+    // the slice in shared memory where it fits (kVtailSmem, the limit
+    // prepare_vtail set)
+    const size_t smem = span > 0 ? (size_t)span * (mf.E2 ? 2 : 6) * sizeof(T) : 0;
+    if (smem == 0 || smem > kVtailSmem) {
+        k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, 0, 0);
+    } else {
+        k_vtail<T><<<1, 512, smem, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, start,
+                                         span);
+    }
     count_launch(1);
+}
+
+// the tail kernels' shared-memory limit, set once per context (outside any
+// stream capture); false where the device refuses it (the tail then runs in
+// global memory... only if the caller checks: launch_vtail uses the limit)
+bool prepare_vtail()
+{
+    bool ok = cudaFuncSetAttribute(k_vtail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVtailSmem) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_vtail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVtailSmem) ==
+                  cudaSuccess;
+    if (!ok) cudaGetLastError();
+    return ok;
 }
 
 #define INST(T)                                                                                    \
@@ -953,7 +1004,7 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
                                            T *, const MfTab<T> &, cudaStream_t);                  \
     template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
-                                  cudaStream_t);                                                  \
+                                  long, long, cudaStream_t);                                      \
     template void launch_mf_tables<T>(const BlkDev *, int, long, long, int, const T *, const T *, \
                                       const T *, const T *, const MfTab<T> &, double, int *,      \
                                       cudaStream_t);                                              \

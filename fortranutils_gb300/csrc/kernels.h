@@ -81,7 +81,10 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxc
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
-                  cudaStream_t st);
+                  long start, long span, cudaStream_t st);
+// shared memory the coarse tail may use for its slice of the multigrid arrays
+constexpr size_t kVtailSmem = 200 * 1024;
+bool prepare_vtail();
 template <typename T>
 void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const T *E,
                       const T *N, const T *R, const T *D, const MfTab<T> &t, double tol, int *bad,

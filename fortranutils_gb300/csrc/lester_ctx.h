@@ -136,7 +136,12 @@ struct Ctx {
     int gm = 0;
     int iststep = 2;  // step.F:180 increments it once before the first step
     int init_vdd[LES_MAXBL][6] = {};
-    std::vector<double *> scratch;  // step fields the caller left NULL  // set_virt_bc's init_vdd (set by the u call)
+    std::vector<double *> scratch;  // step fields the caller left NULL, or host work arrays lester_step keeps on the device
+    // lester_step with host arrays: device mirrors of the pressure
+    // coefficients (written at istep 1 by coeff_p, then only read), keyed
+    // by the host array they mirror
+    double *coef_mirror[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    const double *coef_host[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // last solve statistics
     double last_norms[4] = {0, 0, 0, 0};
     int last_cycles = 0;
@@ -169,6 +174,7 @@ struct Ctx {
         void *d_tmaps[3] = {nullptr, nullptr, nullptr};  // TMA tensor maps over d_sk (k_sweep.cu)
     } sw;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
+    bool vtail_smem = false; // k_vtail may stage its slice in shared memory
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)
     long tabcap = 0, tab_next = 0;
     float *d_pool32 = nullptr;      // FP32 copies of the tables (phys32), reset per call
@@ -271,21 +277,28 @@ class Staging {
     // pending on entry is reported as such rather than blamed on this call
     explicit Staging(Ctx *c, const char *who = "?") : c_(c), who_(who), pre_(cudaGetLastError()) {}
     ~Staging();
-    // in: read only; io: read and written
+    // in: read only; io: read and written; out: written only (a host
+    // array is not copied in); io_part: a device array of n elements of
+    // which only the first ncopy cross to and from a host array
     int in(const double *user, long n, const double **dev);
     int io(double *user, long n, double **dev);
+    int out(double *user, long n, double **dev);
+    int io_part(double *user, long n, long ncopy, double **dev);
+    // a host array written through a library-held device array `dev` of n
+    // elements: copied back by finish()
+    void out_from(double *user, double *dev, long n);
     int finish();  // copies outputs back and synchronises if anything was staged
     bool any_host() const { return any_host_; }
 
   private:
-    int map(const double *user, long n, bool out, double **dev);
+    int map(const double *user, long n, bool out, double **dev, bool copy_in = true, long ncopy = -1);
     Ctx *c_;
     const char *who_;
     cudaError_t pre_;
     struct Ent {
         const double *user;
         double *dev;
-        long n;
+        long n;       // elements copied back (out)
         bool out;
         bool host;
     };

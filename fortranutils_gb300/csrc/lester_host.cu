@@ -40,8 +40,9 @@ int set_err(int code, const char *fmt, ...)
 // ------------------------------------------------------------------ staging
 Staging::~Staging() {}
 
-int Staging::map(const double *user, long n, bool out, double **dev)
+int Staging::map(const double *user, long n, bool out, double **dev, bool copy_in, long ncopy)
 {
+    if (ncopy < 0) ncopy = n;
     if (!user) {
         *dev = nullptr;
         return 0;
@@ -59,7 +60,7 @@ int Staging::map(const double *user, long n, bool out, double **dev)
         cudaGetLastError();
         at.type = cudaMemoryTypeUnregistered;
     }
-    Ent e{user, nullptr, n, out, false};
+    Ent e{user, nullptr, ncopy, out, false};
     if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
         e.dev = const_cast<double *>(user);
     } else {
@@ -82,8 +83,11 @@ int Staging::map(const double *user, long n, bool out, double **dev)
             c_->stage_cap[s] = bytes;
         }
         e.dev = (double *)c_->stage_buf[s];
-        LES_CUDA(cudaMemcpyAsync(e.dev, user, bytes, cudaMemcpyHostToDevice, c_->stream));
-        c_->h2d_bytes += (long)bytes;
+        if (copy_in) {
+            LES_CUDA(cudaMemcpyAsync(e.dev, user, (size_t)ncopy * sizeof(double), cudaMemcpyHostToDevice,
+                                     c_->stream));
+            c_->h2d_bytes += ncopy * (long)sizeof(double);
+        }
     }
     ent_.push_back(e);
     *dev = e.dev;
@@ -99,6 +103,14 @@ int Staging::in(const double *user, long n, const double **dev)
 }
 
 int Staging::io(double *user, long n, double **dev) { return map(user, n, true, dev); }
+int Staging::out(double *user, long n, double **dev) { return map(user, n, true, dev, false); }
+int Staging::io_part(double *user, long n, long ncopy, double **dev) { return map(user, n, true, dev, true, ncopy); }
+
+void Staging::out_from(double *user, double *dev, long n)
+{
+    ent_.push_back(Ent{user, dev, n, true, true});
+    any_host_ = true;
+}
 
 int Staging::finish()
 {
@@ -458,6 +470,7 @@ static void free_ctx(Ctx *c)
             for (cudaEvent_t e : G.ev) cudaEventDestroy(e);
         }
     for (double *p : c->scratch) cudaFree(p);
+    for (double *p : c->coef_mirror) cudaFree(p);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->sg.exec) cudaGraphExecDestroy(c->sg.exec);
     if (c->graph_stream) cudaStreamDestroy(c->graph_stream);
@@ -812,8 +825,10 @@ template <typename T> static void fast_vcycle(Ctx &c)
                                  F.b, F.b, mf, c.stream);
     }
     if (l0) {
+        // levels l0..L are one contiguous slice of the multigrid arrays
+        const long start = c.lv[l0].start3, span = c.vtail_smem ? c.lv[L].start3 + c.lv[L].len3 - start : 0;
         launch_vtail<T>(c.d_vlev, l0, L, c.g.numbl, pre, crs, c.c.rb_omega, c.singular ? 1 : 0, F.E, F.N,
-                        F.R, F.D, F.x, F.b, mf, c.stream);
+                        F.R, F.D, F.x, F.b, mf, start, span, c.stream);
     } else {
         if (c.singular) launch_coarse_mean<T>(c.lv[L].d_blk, c.g.numbl, F.b, c.stream);
         fast_smooth<T>(c, L, L == 1 ? pre : crs);
@@ -1266,6 +1281,7 @@ static int ensure_scratch(Ctx &c)
     LES_CUDA(cudaMalloc(&c.d_small, sizeof(double) * 64));
     LES_CUDA(cudaMallocHost(&c.h_small, sizeof(double) * 64));
     LES_CUDA(cudaMalloc(&c.d_flag, sizeof(int) * 4));
+    c.vtail_smem = prepare_vtail();
     return 0;
 }
 

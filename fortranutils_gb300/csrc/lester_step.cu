@@ -338,46 +338,98 @@ int lester_step(lester_fields *F, const int *istep)
     if ((r0 = ensure_sides(c))) return r0;
     if (has_inlet(c) && (!c.d_uprof || !c.d_vprof))
         return set_err(LES_ERR_ARG, "inlet blocks set without profiles (lester_gpu_set_inlet)");
-    // whole-state staging: host arrays are mirrored once for the step
+    // Host arrays are mirrored once for the step.  What crosses: the
+    // fields a step reads before it writes them (the carried state) are
+    // copied in, the fields the caller reads afterwards (the state and the
+    // outputs of the eddy viscosity, scalar and density) are copied back;
+    // only level 1 of p crosses; the predictor's and the solver's work
+    // arrays (u_int, v_int, w_int, s, res, the sour_p diagnostics)
+    // stay in library-held device arrays; the metrics only come in; the
+    // pressure coefficients, which coeff_p writes at istep 1 and no later
+    // step changes (as in the reference), cross back at istep 1 and are
+    // kept on the device for the host arrays they mirror.
     Staging st(&c, __func__);
     lester_fields D = *F;
     long n3 = c.tot_sg3, nm = c.tot3;
-    double **f3[] = {&D.u, &D.v, &D.w, &D.sc1, &D.rho, &D.rhonp1, &D.rhonm1, &D.u_int, &D.v_int, &D.w_int,
-                     &D.hn_u, &D.hn_v, &D.hn_w, &D.hn_sc1, &D.gam, &D.gamsc1, &D.gamlam, &D.sc1var, &D.sc1dis,
-                     &D.vd_damping, &D.temperature, &D.drhonp1dt, &D.srhot, &D.srhoux};
+    enum { IO, OUT, WORK };
+    struct F3 {
+        double **pp;
+        int role;
+    } f3[] = {{&D.u, IO},      {&D.v, IO},           {&D.w, IO},         {&D.sc1, IO},         {&D.rho, IO},
+              {&D.rhonp1, IO}, {&D.rhonm1, OUT},     {&D.u_int, WORK},   {&D.v_int, WORK},     {&D.w_int, WORK},
+              {&D.hn_u, IO},   {&D.hn_v, IO},        {&D.hn_w, IO},      {&D.hn_sc1, IO},      {&D.gam, IO},
+              {&D.gamsc1, IO}, {&D.gamlam, OUT},    {&D.sc1var, IO},    {&D.sc1dis, OUT},     {&D.vd_damping, OUT},
+              {&D.temperature, IO}, {&D.drhonp1dt, WORK}, {&D.srhot, WORK}, {&D.srhoux, WORK}};
     int r;
     int nscr = 0;
-    for (double **pp : f3) {
-        if (*pp) RET(st.io(*pp, n3, pp));
-        else {
-            // library-held scratch field
-            if ((int)c.scratch.size() <= nscr) {
-                double *d = nullptr;
-                if (cudaMalloc(&d, sizeof(double) * n3) != cudaSuccess) {
-                    cudaGetLastError();
-                    return set_err(LES_ERR_NOMEM, "step scratch allocation failed");
-                }
-                cudaMemsetAsync(d, 0, sizeof(double) * n3, c.stream);
-                c.scratch.push_back(d);
+    // a library-held device array of n elements (zeroed at first use)
+    auto scratch = [&](long n, double **pp) -> int {
+        if ((int)c.scratch.size() <= nscr) {
+            double *d = nullptr;
+            if (cudaMalloc(&d, sizeof(double) * nm) != cudaSuccess) {
+                cudaGetLastError();
+                return set_err(LES_ERR_NOMEM, "step scratch allocation failed");
             }
-            *pp = c.scratch[nscr++];
+            cudaMemsetAsync(d, 0, sizeof(double) * nm, c.stream);
+            c.scratch.push_back(d);
         }
+        (void)n;
+        *pp = c.scratch[nscr++];
+        return 0;
+    };
+    auto is_host = [](const double *p) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+            cudaGetLastError();
+            return true;
+        }
+        return at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged;
+    };
+    for (const F3 &f : f3) {
+        double **pp = f.pp;
+        if (!*pp || (f.role == WORK && is_host(*pp))) RET(scratch(n3, pp));  // NULL, or a host work array
+        else if (f.role == OUT) RET(st.out(*pp, n3, pp));
+        else RET(st.io(*pp, n3, pp));
     }
-    double **fm[] = {&D.p, &D.s, &D.res, &D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
-    for (int q = 0; q < 10; q++) {
-        double **pp = fm[q];
+    if (!D.p || !D.s || !D.res) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
+    RET(st.io_part(D.p, nm, n3, &D.p));  // level 1 crosses; the coarser levels are solver work
+    if (is_host(D.s)) RET(scratch(nm, &D.s));
+    if (is_host(D.res)) RET(scratch(nm, &D.res));
+    double **fc[] = {&D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
+    for (int q = 0; q < 7; q++) {
+        double **pp = fc[q];
         if (!*pp) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
-        // the coefficients are written only by coeff_p at the first step:
-        // host arrays are not copied back after the others
-        if (q >= 3 && *istep != 1) RET(st.in(*pp, nm, (const double **)pp));
-        else RET(st.io(*pp, nm, pp));
+        if (!is_host(*pp)) continue;
+        const double *h = *pp;
+        if (!c.coef_mirror[q]) {
+            if (cudaMalloc(&c.coef_mirror[q], sizeof(double) * nm) != cudaSuccess) {
+                cudaGetLastError();
+                c.coef_mirror[q] = nullptr;
+                return set_err(LES_ERR_NOMEM, "coefficient mirror allocation failed");
+            }
+            c.coef_host[q] = nullptr;
+        }
+        if (*istep == 1) {
+            // written by coeff_p in this step into the mirror, copied back
+            // to the host array by finish()
+            st.out_from(const_cast<double *>(h), c.coef_mirror[q], nm);
+            c.coef_host[q] = h;
+            *pp = c.coef_mirror[q];
+        } else if (c.coef_host[q] != h) {
+            LES_CUDA(cudaMemcpyAsync(c.coef_mirror[q], h, sizeof(double) * nm, cudaMemcpyHostToDevice, c.stream));
+            c.h2d_bytes += nm * (long)sizeof(double);
+            c.coef_host[q] = h;
+            *pp = c.coef_mirror[q];
+        } else {
+            *pp = c.coef_mirror[q];
+        }
     }
     for (int q = 0; q < 35; q++) {
         if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
-        RET(st.io(D.metric[q], c.tot2, &D.metric[q]));
+        RET(st.in(D.metric[q], c.tot2, (const double **)&D.metric[q]));
     }
-    RET(st.io(D.dkp, c.tot1k, &D.dkp));
-    RET(st.io(D.dkw, c.tot1k, &D.dkw));
+    RET(st.in(D.dkp, c.tot1k, (const double **)&D.dkp));
+    RET(st.in(D.dkw, c.tot1k, (const double **)&D.dkw));
     {
         long tl[12] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1, c.totjk, c.totjk, c.tot2_l1, c.tot2_l1,
                        c.totjk, c.totjk, c.totki, c.totki};
@@ -392,10 +444,16 @@ int lester_step(lester_fields *F, const int *istep)
             RET(st.io(D.tw[q], tl[q], &D.tw[q]));
         }
     }
-    if (c.c.step_graph && !st.any_host()) {
+    if (c.c.step_graph) {
+        // device pointers are stable from call to call (staging buffers by
+        // call order, library arrays): the graph keyed on them replays
         bool done = false;
         const int rg = step_graph(c, D, istep, &done);
-        if (done) return rg;
+        if (done) {
+            if (rg && rg != LES_ERR_NOT_CONVERGED) return rg;
+            const int rf = st.finish();
+            return rf ? rf : rg;
+        }
     }
     RET(step_pre(c, D, istep));
     c.want_norms = false;

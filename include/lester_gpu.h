@@ -243,7 +243,18 @@ int lester_gpu_xfer_bytes(long *h2d, long *d2h);
  * inlet blocks of lester_gpu_set_inlet, set_virt_bc x3, subgrid, scalar
  * transport and density, momentum predictor with conv_exitbc task 1 after
  * each component, coeff_p at istep 1, sour_p, solvers, extrap_p,
- * p_ref_subtract, uvw_adv x3, slipbc, conv_exitbc task 2, swap_rhos).  Host arrays are copied in once and back once per call.
+ * p_ref_subtract, uvw_adv x3, slipbc, conv_exitbc task 2, swap_rhos).
+ * Host arrays: the fields a step reads before writing them (u v w sc1 rho
+ * rhonp1 hn_* gam gamsc1 sc1var temperature, level 1 of p, metrics, dkp,
+ * dkw, the wall arrays) are copied in once per call; the fields the caller
+ * reads after the step (those, rhonm1, gamlam, sc1dis, vd_damping, the wall
+ * arrays, level 1 of p) are copied back once.  The work arrays (u_int v_int
+ * w_int drhonp1dt srhot srhoux s res, p below level 1) are library-held
+ * device arrays when host arrays are passed and are not written back.  The
+ * pressure coefficients, which coeff_p writes at istep 1 and no later step
+ * changes, are written back at istep 1 and kept on the device for the host
+ * arrays passed then; a later call with other host coefficient arrays
+ * copies those in once.
  * Returns LES_ERR_NOT_CONVERGED (after completing the step) if a fast
  * pressure solver stopped at max_outer above rtol. */
 int lester_step(lester_fields *fields, const int *istep);

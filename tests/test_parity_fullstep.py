@@ -84,14 +84,54 @@ def test_steps_reference_solver(name, exact, gpulib):
     assert rel(got["u"], s["u"]) > 1e-6
 
 
+def host_state_equal(hst, dev, st):
+    """The fields lester_step returns to host arrays equal the device run's:
+    the carried state, p on level 1 (the coarser levels are solver work)."""
+    n3 = st.case.n3_sg
+    for n in S.STATE:
+        a, b = (hst[n][:n3], dev[n][:n3]) if n == "p" else (hst[n], dev[n])
+        np.testing.assert_array_equal(a, b, err_msg=n)
+
+
 def test_steps_host_arrays_match_device(gpulib):
     """Host (numpy) fields through the same entry point: copied in and out
     once per call, same numbers as device-resident fields."""
     st, ctrl, s = make("box_wall")
     dev, _ = gpu_steps(st, ctrl, s, 2, "torch")
     hst, _ = gpu_steps(st, ctrl, s, 2, "numpy")
-    for n in S.STATE:
-        np.testing.assert_array_equal(hst[n], dev[n], err_msg=n)
+    host_state_equal(hst, dev, st)
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_host_arrays_fast_path(graph, gpulib):
+    """The benchmarked path (mixed solver, FP32 physics) with host arrays,
+    steps 2.. replayed from the whole-step graph or launched: the state the
+    host gets back equals the device-resident run bit for bit, and the
+    pressure coefficients cross to the device once after the first step."""
+    st, ctrl, s = make("box_slip_stretched", psolve=L.PSOLVE_MIXED, rtol=1e-9, exact=0, phys32=1,
+                       step_graph=graph)
+    dev, rd = gpu_steps(st, ctrl, s, 4, "torch")
+    g = s.to("pinned")
+    L.gpu_init(st.case.geom(), ctrl)
+    try:
+        rh = [S.step(g, 1), S.step(g, 2)]
+        b0 = L.gpu_xfer_bytes()
+        rh += [S.step(g, it) for it in (3, 4)]
+        b1 = L.gpu_xfer_bytes()
+        info = L.gpu_step_graph_info()
+        hst = g.to("numpy")
+    finally:
+        L.gpu_finalize()
+    assert rh == rd
+    if graph:
+        assert info["replays"] == 3 and not info["failed"], info
+    host_state_equal(hst, dev, st)
+    # per step in: the carried state, p on level 1, metrics and wall
+    # arrays; no coefficient or work array
+    carried = "u v w sc1 rho rhonp1 hn_u hn_v hn_w hn_sc1 gam gamsc1 sc1var temperature".split()
+    want_in = (sum(g[n].size for n in carried + S.TW) + st.case.n3_sg + g["dkp"].size + g["dkw"].size
+               + sum(a.size for a in g["metric"].values()))
+    assert (b1[0] - b0[0]) == 2 * 8 * want_in, (b1[0] - b0[0], want_in)
 
 
 @pytest.mark.parametrize("psolve", [L.PSOLVE_FP64, L.PSOLVE_MIXED])
