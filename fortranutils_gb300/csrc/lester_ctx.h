@@ -113,6 +113,10 @@ struct Ctx {
     // staging buffers for host arguments
     std::vector<void *> stage_buf;
     std::vector<size_t> stage_cap;
+    // copy streams and events of lester_step's deferred host copies
+    cudaStream_t xs_in = nullptr, xs_out = nullptr;
+    std::vector<cudaEvent_t> xev;
+    class Staging *xfer = nullptr;  // the running lester_step's host copies
     // kernel timing inside a timed region (lester_gpu_prof): CUDA events
     // around every launch of the timed kernels (LES_PROF_*): pairs in
     // ev_pool, the kernel of pair q in ev_tag[q]
@@ -183,7 +187,8 @@ struct Ctx {
     // whole-step graph (ctrl.step_graph, lester_step.cu)
     struct StepGraph {
         cudaGraphExec_t exec = nullptr;
-        lester_fields key{};  // the fields it was captured with
+        lester_fields key{};  // the fields it was captured with (device)
+        lester_fields hkey{}; // and as the caller passed them (host copies)
         lester_ctrl ctrl{};   // and the controls
         long coef_gen = -1;
         long launches = 0;    // kernels captured (the cycle loop's body once)
@@ -289,9 +294,36 @@ class Staging {
     void out_from(double *user, double *dev, long n);
     int finish();  // copies outputs back and synchronises if anything was staged
     bool any_host() const { return any_host_; }
+    bool pageable() const { return pageable_; }  // a host array is not page-locked
+
+    // Deferred copies (lester_step).  After defer(), host arrays are mapped
+    // without copying.  issue_in() copies the inputs, in map order, on a
+    // copy stream; need(dev) makes the compute stream wait for that array's
+    // copy (and so for every one mapped before it); put(dev) copies an
+    // output back on a second copy stream once the compute stream has
+    // written it for the last time; finish() puts the outputs not yet put,
+    // joins both copy streams and synchronises.  Issued inside a stream
+    // capture the copies become nodes of the graph: in_graph() then leaves
+    // finish() only the synchronisation, and copy_out_all() copies every
+    // output again on the compute stream (the host finished the step).
+    void defer() { defer_ = true; }
+    bool deferred() const { return defer_; }
+    int issue_in();
+    int need(const void *dev);
+    int put(const void *dev);
+    // put() of the output mapped to `dst` from the device array `src`,
+    // which holds its final values already (the step copies src to dst
+    // later without changing src)
+    int put_as(const void *src, const void *dst);
+    int put_rest();  // put() of every output not yet put
+    int join();
+    void clear_marks();
+    void in_graph() { in_graph_ = true; }
+    int copy_out_all();
 
   private:
     int map(const double *user, long n, bool out, double **dev, bool copy_in = true, long ncopy = -1);
+    int event(int i, cudaEvent_t *e);
     Ctx *c_;
     const char *who_;
     cudaError_t pre_;
@@ -301,10 +333,16 @@ class Staging {
         long n;       // elements copied back (out)
         bool out;
         bool host;
+        long nin = 0;     // elements copied in (deferred)
+        int ev = -1;      // event of its deferred in-copy
+        bool put = false; // deferred out-copy issued
     };
     std::vector<Ent> ent_;
     int slot_ = 0;
     bool any_host_ = false;
+    bool pageable_ = false;
+    bool defer_ = false, in_graph_ = false, forked_out_ = false, finished_ = false;
+    int nev_ = 0;
 };
 
 } // namespace les

@@ -38,7 +38,15 @@ int set_err(int code, const char *fmt, ...)
 }
 
 // ------------------------------------------------------------------ staging
-Staging::~Staging() {}
+Staging::~Staging()
+{
+    // an error return between the deferred copies and finish(): no copy
+    // may touch the caller's arrays after the call returns
+    if (defer_ && any_host_ && !finished_) {
+        if (c_->xs_in) cudaStreamSynchronize(c_->xs_in);
+        if (c_->xs_out) cudaStreamSynchronize(c_->xs_out);
+    }
+}
 
 int Staging::map(const double *user, long n, bool out, double **dev, bool copy_in, long ncopy)
 {
@@ -66,6 +74,7 @@ int Staging::map(const double *user, long n, bool out, double **dev, bool copy_i
     } else {
         e.host = true;
         any_host_ = true;
+        if (at.type != cudaMemoryTypeHost) pageable_ = true;
         int s = slot_++;
         if ((int)c_->stage_buf.size() <= s) {
             c_->stage_buf.push_back(nullptr);
@@ -83,7 +92,10 @@ int Staging::map(const double *user, long n, bool out, double **dev, bool copy_i
             c_->stage_cap[s] = bytes;
         }
         e.dev = (double *)c_->stage_buf[s];
-        if (copy_in) {
+        if (copy_in && defer_) {
+            e.nin = ncopy;
+            c_->h2d_bytes += ncopy * (long)sizeof(double);
+        } else if (copy_in) {
             LES_CUDA(cudaMemcpyAsync(e.dev, user, (size_t)ncopy * sizeof(double), cudaMemcpyHostToDevice,
                                      c_->stream));
             c_->h2d_bytes += ncopy * (long)sizeof(double);
@@ -112,8 +124,116 @@ void Staging::out_from(double *user, double *dev, long n)
     any_host_ = true;
 }
 
+int Staging::event(int i, cudaEvent_t *e)
+{
+    while ((int)c_->xev.size() <= i) {
+        cudaEvent_t ev;
+        LES_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        c_->xev.push_back(ev);
+    }
+    *e = c_->xev[i];
+    return 0;
+}
+
+int Staging::issue_in()
+{
+    if (!any_host_) return 0;
+    if (!c_->xs_in) LES_CUDA(cudaStreamCreateWithFlags(&c_->xs_in, cudaStreamNonBlocking));
+    cudaEvent_t fork;
+    nev_ = 0;
+    if (int r = event(nev_++, &fork)) return r;
+    // the copy stream starts after the compute stream's earlier work
+    LES_CUDA(cudaEventRecord(fork, c_->stream));
+    LES_CUDA(cudaStreamWaitEvent(c_->xs_in, fork, 0));
+    for (auto &e : ent_) {
+        if (!e.host || e.nin <= 0) continue;
+        LES_CUDA(cudaMemcpyAsync(e.dev, e.user, (size_t)e.nin * sizeof(double), cudaMemcpyHostToDevice,
+                                 c_->xs_in));
+        e.ev = nev_;
+        cudaEvent_t ev;
+        if (int r = event(nev_++, &ev)) return r;
+        LES_CUDA(cudaEventRecord(ev, c_->xs_in));
+    }
+    return 0;
+}
+
+int Staging::need(const void *dev)
+{
+    for (auto &e : ent_)
+        if (e.dev == dev && e.ev >= 0) {
+            LES_CUDA(cudaStreamWaitEvent(c_->stream, c_->xev[e.ev], 0));
+            return 0;
+        }
+    return 0;
+}
+
+int Staging::put(const void *dev) { return put_as(dev, dev); }
+
+int Staging::put_as(const void *src, const void *dst)
+{
+    if (!src || !dst) return 0;
+    for (auto &e : ent_) {
+        if (e.dev != dst || !e.host || !e.out || e.put) continue;
+        if (!c_->xs_out) LES_CUDA(cudaStreamCreateWithFlags(&c_->xs_out, cudaStreamNonBlocking));
+        cudaEvent_t ev;
+        if (int r = event(nev_++, &ev)) return r;
+        LES_CUDA(cudaEventRecord(ev, c_->stream));
+        LES_CUDA(cudaStreamWaitEvent(c_->xs_out, ev, 0));
+        LES_CUDA(cudaMemcpyAsync(const_cast<double *>(e.user), src, (size_t)e.n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c_->xs_out));
+        e.put = true;
+        forked_out_ = true;
+    }
+    return 0;
+}
+
+int Staging::put_rest()
+{
+    for (auto &e : ent_)
+        if (e.host && e.out && !e.put)
+            if (int r = put(e.dev)) return r;
+    return 0;
+}
+
+int Staging::join()
+{
+    cudaEvent_t ev;
+    if (nev_ > 0 && c_->xs_in) {
+        if (int r = event(nev_++, &ev)) return r;
+        LES_CUDA(cudaEventRecord(ev, c_->xs_in));
+        LES_CUDA(cudaStreamWaitEvent(c_->stream, ev, 0));
+    }
+    if (forked_out_) {
+        if (int r = event(nev_++, &ev)) return r;
+        LES_CUDA(cudaEventRecord(ev, c_->xs_out));
+        LES_CUDA(cudaStreamWaitEvent(c_->stream, ev, 0));
+        forked_out_ = false;
+    }
+    return 0;
+}
+
+void Staging::clear_marks()
+{
+    for (auto &e : ent_) {
+        e.ev = -1;
+        e.put = false;
+    }
+    nev_ = 0;
+    forked_out_ = false;
+}
+
+int Staging::copy_out_all()
+{
+    for (auto &e : ent_)
+        if (e.host && e.out)
+            LES_CUDA(cudaMemcpyAsync(const_cast<double *>(e.user), e.dev, (size_t)e.n * sizeof(double),
+                                     cudaMemcpyDeviceToHost, c_->stream));
+    return 0;
+}
+
 int Staging::finish()
 {
+    finished_ = true;
     if (pre_ != cudaSuccess)
         return set_err(LES_ERR_CUDA, "CUDA error pending before %s: %s", who_, cudaGetErrorString(pre_));
     if (!any_host_) {
@@ -123,10 +243,17 @@ int Staging::finish()
     }
     for (auto &e : ent_)
         if (e.host && e.out) {
+            c_->d2h_bytes += e.n * (long)sizeof(double);
+            if (defer_) continue;  // put() below, or the graph copied it
             LES_CUDA(cudaMemcpyAsync(const_cast<double *>(e.user), e.dev, (size_t)e.n * sizeof(double),
                                      cudaMemcpyDeviceToHost, c_->stream));
-            c_->d2h_bytes += e.n * (long)sizeof(double);
         }
+    if (defer_ && !in_graph_) {
+        finished_ = false;  // until the copy streams have joined
+        if (int r = put_rest()) return r;
+        if (int r = join()) return r;
+        finished_ = true;
+    }
     LES_CUDA(cudaStreamSynchronize(c_->stream));
     return 0;
 }
@@ -471,6 +598,9 @@ static void free_ctx(Ctx *c)
         }
     for (double *p : c->scratch) cudaFree(p);
     for (double *p : c->coef_mirror) cudaFree(p);
+    for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
+    if (c->xs_in) cudaStreamDestroy(c->xs_in);
+    if (c->xs_out) cudaStreamDestroy(c->xs_out);
     if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->sg.exec) cudaGraphExecDestroy(c->sg.exec);
     if (c->graph_stream) cudaStreamDestroy(c->graph_stream);

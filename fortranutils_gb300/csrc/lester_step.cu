@@ -6,10 +6,12 @@
 // sides this library does not support (FIXED inlet, CONVECTIVE outflow)
 // are not part of it; a block with such a side is refused.
 //
-// Field pointers may be host or device arrays.  Host arrays are copied to
-// device mirrors before the step and back after it (one copy each way per
-// call).  Scratch fields passed as NULL are kept on the device by the
-// library.
+// Field pointers may be host or device arrays.  Host arrays cross once each
+// way per call at most, on two copy streams beside the compute stream: an
+// input's copy is waited for just before the first routine that reads it,
+// an output is copied back as soon as the step has written it for the last
+// time, so that most of the traffic overlaps the step's kernels.  Scratch
+// fields passed as NULL are kept on the device by the library.
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -101,6 +103,22 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
         return exit_task(c, task, iva, D.rho, D.rhonp1, D.u, D.v, D.w, D.u_int, D.v_int, D.w_int, D.hn_u, D.hn_v,
                          D.hn_w, mx, D.dkp, D.dkw, m[M_RDIDJP]);
     };
+    // deferred host copies: wait for inputs, copy outputs back early
+    auto need = [&](std::initializer_list<const double *> l) {
+        if (c.xfer)
+            for (const double *q : l) RET(c.xfer->need(q));
+        return 0;
+    };
+    auto put = [&](std::initializer_list<const double *> l) {
+        if (c.xfer)
+            for (const double *q : l) RET(c.xfer->put(q));
+        return 0;
+    };
+    if (has_inlet(c))
+        RET(need({D.u, D.v, D.w, D.sc1, D.rho}));
+    RET(need({D.dkp, D.dkw, D.u, D.rho, D.gam, D.vd_damping}));
+    for (int q = 0; q < 35; q++) RET(need({m[q]}));
+    for (int q = 0; q < 12; q++) RET(need({tw[q]}));
     // ---- ivar = u: the inlet planes (step.F:226)
     if (has_inlet(c))
         RET(inlet_task(c, c.d_uprof, c.d_vprof, c.inlet_seed, *istep, D.u, D.v, D.w, D.sc1, D.rho, D.u_int,
@@ -108,32 +126,45 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
     // ---- ivar = u: boundary ghosts, eddy viscosity, scalar, u predictor
     for (int iv = 1; iv <= 3; iv++) {
         double *fld = iv == 1 ? D.u : iv == 2 ? D.v : D.w;
+        RET(need({fld}));
         RET(lester_set_virt_bc(&iv, &one, fld, nullptr, D.rho, D.gam, D.vd_damping, nullptr, &zero, tw[0], tw[1],
                                tw[2], tw[3], tw[4], tw[5], tw[6], tw[7], tw[8], tw[9], tw[10], tw[11], m[M_DIP],
                                m[M_DIU], m[M_DIV], m[M_DIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RU],
                                m[M_RV], D.dkp, D.dkw));
     }
+    RET(need({D.sc1, D.sc1var, D.gamsc1, D.sc1dis}));
     RET(lester_subgrid(D.gam, D.gamsc1, D.u, D.v, D.w, D.sc1, D.rho, D.sc1var, D.sc1dis, D.vd_damping, m[M_DIP],
                        m[M_DIU], m[M_DJP], m[M_DJV], D.dkp, D.dkw, m[M_HIJP], m[M_HJIP], m[M_HKIP], m[M_HKJP],
                        m[M_RP], nullptr, nullptr));
     RET(lester_set_gamsc1_bc(D.sc1, D.gamsc1, D.gamlam, m[M_DIU], m[M_DJV], D.dkp, m[M_RP]));
+    RET(need({D.p, D.hn_sc1}));
     RET(lester_set_sc1(D.u, D.v, D.w, D.p, D.sc1, D.rho, D.gamsc1, D.gamlam, D.hn_sc1, m[M_DIP], m[M_DIU],
                        m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
                        m[M_HKIU], m[M_HKJV], m[M_RP], D.dkp, D.dkw, nullptr, nullptr));
     RET(lester_set_sc1_bc(D.sc1));
     RET(lester_set_sc1var(D.u, D.v, D.w, D.sc1, D.rho, D.sc1var, D.sc1dis, m[M_DIP], m[M_DJP], D.dkp, D.dkw,
                           m[M_RP], nullptr, nullptr));
+    RET(need({D.rhonp1, D.temperature}));
     RET(lester_search_lib(D.sc1, D.sc1var, D.rhonp1, D.temperature, nullptr, nullptr, istep, &k.alpha, D.rho,
                           &k.rholo, &k.rhohi));
     RET(lester_set_sc1_bc(D.sc1));
     RET(lester_set_sc1_bc(D.rhonp1));
     RET(lester_set_sc1_bc(D.temperature));
+    // final for this step: the eddy viscosities, the wall damping, the
+    // scalar's right-hand side, variance and dissipation, the temperature
+    RET(put({D.gam, D.gamsc1, D.gamlam, D.vd_damping, D.sc1dis, D.sc1var, D.temperature, D.hn_sc1}));
+    // rhonp1 is final too, and swap_rhos ends the step with rho = rhonp1:
+    // the caller's rho is copied back from rhonp1 now
+    RET(put({D.rhonp1}));
+    if (c.xfer) RET(c.xfer->put_as(D.rhonp1, D.rho));
+    RET(need({D.hn_u}));
     RET(lester_set_uv_int(&iU, D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.u_int, D.hn_u, m[M_DIP], m[M_DIU],
                           m[M_DIX], m[M_RDIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RDJP], m[M_RDJU],
                           m[M_DIDJP], m[M_DIDJU], m[M_RDIDJU], m[M_HIJP], m[M_HIJU], m[M_HJIU], m[M_HKIU],
                           m[M_HKJU], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[0], tw[1], tw[2], tw[3], nullptr,
                           nullptr));
     RET(exitbc(1, 1));
+    RET(need({D.hn_v}));
     // ---- ivar = v (step.F:319-326: the v arrays in the u roles)
     RET(lester_set_uv_int(&iV, D.v, D.u, D.w, D.p, D.rho, D.rhonp1, D.gam, D.v_int, D.hn_v, m[M_DJP], m[M_DJV],
                           m[M_DJX], m[M_RDJX], m[M_DIP], m[M_DIV], m[M_DIU], m[M_DIX], m[M_RDIP], m[M_RDIV],
@@ -141,12 +172,18 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
                           m[M_HKIV], m[M_RP], m[M_RV], D.dkp, D.dkw, tw[4], tw[5], tw[6], tw[7], nullptr,
                           nullptr));
     RET(exitbc(1, 2));
+    RET(need({D.hn_w}));
     // ---- ivar = w
     RET(lester_set_w_int(D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.w_int, D.hn_w, m[M_DIP], m[M_DIU],
                          m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
                          m[M_HKIU], m[M_HKJV], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[10], tw[11], tw[8], tw[9],
                          nullptr, nullptr));
     RET(exitbc(1, 3));
+    // the wall arrays (set_virt_bc, then the predictors) are final; the
+    // predictors' right-hand sides too unless an outflow side updates them
+    // after the projection (conv_exitbc task 2)
+    for (int q = 0; q < 12; q++) RET(put({tw[q]}));
+    if (!has_convective(c)) RET(put({D.hn_u, D.hn_v, D.hn_w}));
     // ---- ivar = p
     if (*istep == 1)
         RET(lester_coeff_p(m[M_DIU], m[M_DJV], m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], D.dkp, D.dkw, D.ap, D.aw,
@@ -215,6 +252,7 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
     if (cudaMemcpyAsync(c.d_step, c.h_step, sizeof(int), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
         cudaMemsetAsync(c.d_loop, 0, 8 * sizeof(double), c.stream) != cudaSuccess)
         r = set_err(LES_ERR_CUDA, "step graph: status copies");
+    if (!r && c.xfer) r = c.xfer->issue_in();  // host inputs: copy nodes
     if (!r) r = step_pre(c, D, istep);
     if (!r) {
         c.want_norms = false;
@@ -234,6 +272,10 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
     }
     if (!r && cudaMemcpyAsync(c.h_loop, c.d_loop, 8 * sizeof(double), cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
         r = set_err(LES_ERR_CUDA, "step graph: status copy");
+    // host outputs not copied during the step, then both copy branches
+    // rejoin the capture's stream
+    if (!r && c.xfer) r = c.xfer->put_rest();
+    if (!r && c.xfer) r = c.xfer->join();
     c.capturing = false;
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c.stream, &g);
@@ -261,7 +303,7 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
 // value is the step's.
 static int step_graph_run(Ctx &c, lester_fields &D, const int *istep);
 
-static int step_graph(Ctx &c, lester_fields &D, const int *istep, bool *done)
+static int step_graph(Ctx &c, lester_fields &D, const lester_fields &H, const int *istep, bool *done)
 {
     *done = false;
     const int ps = c.c.psolve;
@@ -275,11 +317,12 @@ static int step_graph(Ctx &c, lester_fields &D, const int *istep, bool *done)
     bool ready = c.coef_prec == prec && c.coef_gen_seen == c.coef_gen;
     for (int q = 0; q < 7; q++) ready = ready && c.coef_key[q] == coef[q];
     if (!ready || (c.c.krylov == 1 && !c.d_fr) || (c.singular && !c.d_bmean)) return 0;
-    const bool same = !memcmp(&c.sg.key, &D, sizeof D) && !memcmp(&c.sg.ctrl, &c.c, sizeof c.c) &&
-                      c.sg.coef_gen == c.coef_gen;
+    const bool same = !memcmp(&c.sg.key, &D, sizeof D) && !memcmp(&c.sg.hkey, &H, sizeof H) &&
+                      !memcmp(&c.sg.ctrl, &c.c, sizeof c.c) && c.sg.coef_gen == c.coef_gen;
     if (same && c.sg.failed) return 0;
     if (!same || !c.sg.exec) {
         c.sg.key = D;
+        c.sg.hkey = H;
         c.sg.coef_gen = c.coef_gen;
         c.sg.failed = step_capture(c, D, istep) != 0;
         c.sg.ctrl = c.c;  // as the capture left it (with any autotuned settings)
@@ -290,6 +333,7 @@ static int step_graph(Ctx &c, lester_fields &D, const int *istep, bool *done)
         }
     }
     *done = true;
+    if (c.xfer) c.xfer->in_graph();  // its copies are the graph's
     return step_graph_run(c, D, istep);
 }
 
@@ -320,6 +364,7 @@ static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
         c.last_cycles += cycles;
         if (rs && rs != LES_ERR_NOT_CONVERGED) return rs;
         RET(step_post(c, D, istep));
+        if (c.xfer) RET(c.xfer->copy_out_all());  // the graph copied the outputs before this
         c.iststep += 1;
         return rs;
     }
@@ -347,20 +392,46 @@ int lester_step(lester_fields *F, const int *istep)
     // stay in library-held device arrays; the metrics only come in; the
     // pressure coefficients, which coeff_p writes at istep 1 and no later
     // step changes (as in the reference), cross back at istep 1 and are
-    // kept on the device for the host arrays they mirror.
+    // kept on the device for the host arrays they mirror.  Inputs are
+    // mapped in the order the step first reads them, the order of their
+    // copies.
     Staging st(&c, __func__);
+    st.defer();
     lester_fields D = *F;
     long n3 = c.tot_sg3, nm = c.tot3;
-    enum { IO, OUT, WORK };
+    int r;
+    for (int q = 0; q < 35; q++) {
+        if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
+        RET(st.in(D.metric[q], c.tot2, (const double **)&D.metric[q]));
+    }
+    RET(st.in(D.dkp, c.tot1k, (const double **)&D.dkp));
+    RET(st.in(D.dkw, c.tot1k, (const double **)&D.dkw));
+    {
+        long tl[12] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1, c.totjk, c.totjk, c.tot2_l1, c.tot2_l1,
+                       c.totjk, c.totjk, c.totki, c.totki};
+        // tot2_l1 is known once the tables exist
+        if (!c.d_offki) {
+            long l1 = 0;
+            for (int b = 1; b <= c.g.numbl; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
+            for (int q : {2, 3, 6, 7}) tl[q] = l1;
+        }
+        for (int q = 0; q < 12; q++) {
+            if (!D.tw[q]) return set_err(LES_ERR_ARG, "wall array %d missing", q);
+            RET(st.io(D.tw[q], tl[q], &D.tw[q]));
+        }
+    }
+    if (!D.p || !D.s || !D.res) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
+    enum { IO, OUT, WORK, P };
     struct F3 {
         double **pp;
         int role;
-    } f3[] = {{&D.u, IO},      {&D.v, IO},           {&D.w, IO},         {&D.sc1, IO},         {&D.rho, IO},
-              {&D.rhonp1, IO}, {&D.rhonm1, OUT},     {&D.u_int, WORK},   {&D.v_int, WORK},     {&D.w_int, WORK},
-              {&D.hn_u, IO},   {&D.hn_v, IO},        {&D.hn_w, IO},      {&D.hn_sc1, IO},      {&D.gam, IO},
-              {&D.gamsc1, IO}, {&D.gamlam, OUT},    {&D.sc1var, IO},    {&D.sc1dis, OUT},     {&D.vd_damping, OUT},
-              {&D.temperature, IO}, {&D.drhonp1dt, WORK}, {&D.srhot, WORK}, {&D.srhoux, WORK}};
-    int r;
+    } f3[] = {{&D.u, IO},         {&D.rho, IO},         {&D.gam, IO},        {&D.vd_damping, IO},
+              {&D.v, IO},         {&D.w, IO},           {&D.sc1, IO},        {&D.sc1var, IO},
+              {&D.gamsc1, IO},    {&D.sc1dis, IO},      {&D.gamlam, OUT},    {&D.p, P},
+              {&D.hn_sc1, IO},    {&D.rhonp1, IO},      {&D.temperature, IO}, {&D.hn_u, IO},
+              {&D.hn_v, IO},      {&D.hn_w, IO},        {&D.rhonm1, OUT},    {&D.u_int, WORK},
+              {&D.v_int, WORK},   {&D.w_int, WORK},     {&D.drhonp1dt, WORK}, {&D.srhot, WORK},
+              {&D.srhoux, WORK}};
     int nscr = 0;
     // a library-held device array of n elements (zeroed at first use)
     auto scratch = [&](long n, double **pp) -> int {
@@ -387,12 +458,11 @@ int lester_step(lester_fields *F, const int *istep)
     };
     for (const F3 &f : f3) {
         double **pp = f.pp;
-        if (!*pp || (f.role == WORK && is_host(*pp))) RET(scratch(n3, pp));  // NULL, or a host work array
+        if (f.role == P) RET(st.io_part(D.p, nm, n3, &D.p));  // level 1 crosses; the coarser levels are solver work
+        else if (!*pp || (f.role == WORK && is_host(*pp))) RET(scratch(n3, pp));  // NULL, or a host work array
         else if (f.role == OUT) RET(st.out(*pp, n3, pp));
         else RET(st.io(*pp, n3, pp));
     }
-    if (!D.p || !D.s || !D.res) return set_err(LES_ERR_ARG, "p, s, res and the coefficient arrays are required");
-    RET(st.io_part(D.p, nm, n3, &D.p));  // level 1 crosses; the coarser levels are solver work
     if (is_host(D.s)) RET(scratch(nm, &D.s));
     if (is_host(D.res)) RET(scratch(nm, &D.res));
     double **fc[] = {&D.ap, &D.aw, &D.ae, &D.as, &D.an, &D.al, &D.ar};
@@ -424,37 +494,26 @@ int lester_step(lester_fields *F, const int *istep)
             *pp = c.coef_mirror[q];
         }
     }
-    for (int q = 0; q < 35; q++) {
-        if (!D.metric[q]) return set_err(LES_ERR_ARG, "metric %d missing", q);
-        RET(st.in(D.metric[q], c.tot2, (const double **)&D.metric[q]));
-    }
-    RET(st.in(D.dkp, c.tot1k, (const double **)&D.dkp));
-    RET(st.in(D.dkw, c.tot1k, (const double **)&D.dkw));
-    {
-        long tl[12] = {c.totki, c.totki, c.tot2_l1, c.tot2_l1, c.totjk, c.totjk, c.tot2_l1, c.tot2_l1,
-                       c.totjk, c.totjk, c.totki, c.totki};
-        // tot2_l1 is known once the tables exist
-        if (!c.d_offki) {
-            long l1 = 0;
-            for (int b = 1; b <= c.g.numbl; b++) l1 += (long)c.lv[1].n[b][0] * c.lv[1].n[b][1];
-            for (int q : {2, 3, 6, 7}) tl[q] = l1;
-        }
-        for (int q = 0; q < 12; q++) {
-            if (!D.tw[q]) return set_err(LES_ERR_ARG, "wall array %d missing", q);
-            RET(st.io(D.tw[q], tl[q], &D.tw[q]));
-        }
-    }
-    if (c.c.step_graph) {
+    // the deferred copies of this call (step_pre's waits and early puts)
+    struct XferScope {
+        Ctx &c;
+        XferScope(Ctx &cc, Staging *s) : c(cc) { c.xfer = s; }
+        ~XferScope() { c.xfer = nullptr; }
+    } xscope(c, st.any_host() ? &st : nullptr);
+    if (c.c.step_graph && !st.pageable()) {
         // device pointers are stable from call to call (staging buffers by
-        // call order, library arrays): the graph keyed on them replays
+        // call order, library arrays): the graph keyed on them and on the
+        // host arrays it copies replays, the host copies as its nodes
         bool done = false;
-        const int rg = step_graph(c, D, istep, &done);
+        const int rg = step_graph(c, D, *F, istep, &done);
         if (done) {
             if (rg && rg != LES_ERR_NOT_CONVERGED) return rg;
             const int rf = st.finish();
             return rf ? rf : rg;
         }
+        st.clear_marks();
     }
+    RET(st.issue_in());
     RET(step_pre(c, D, istep));
     c.want_norms = false;
     int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);

@@ -93,10 +93,12 @@ def host_state_equal(hst, dev, st):
         np.testing.assert_array_equal(a, b, err_msg=n)
 
 
-def test_steps_host_arrays_match_device(gpulib):
-    """Host (numpy) fields through the same entry point: copied in and out
-    once per call, same numbers as device-resident fields."""
-    st, ctrl, s = make("box_wall")
+@pytest.mark.parametrize("name,kw", [("box_wall", {}), ("box_slip_stretched", {"model": 1})])
+def test_steps_host_arrays_match_device(name, kw, gpulib):
+    """Host (numpy, pageable) fields through the same entry point: copied
+    in and out once per call, same numbers as device-resident fields.  The
+    slip-wall Smagorinsky case reads vd_damping where no wall writes it."""
+    st, ctrl, s = make(name, **kw)
     dev, _ = gpu_steps(st, ctrl, s, 2, "torch")
     hst, _ = gpu_steps(st, ctrl, s, 2, "numpy")
     host_state_equal(hst, dev, st)
@@ -128,7 +130,8 @@ def test_host_arrays_fast_path(graph, gpulib):
     host_state_equal(hst, dev, st)
     # per step in: the carried state, p on level 1, metrics and wall
     # arrays; no coefficient or work array
-    carried = "u v w sc1 rho rhonp1 hn_u hn_v hn_w hn_sc1 gam gamsc1 sc1var temperature".split()
+    carried = ("u v w sc1 rho rhonp1 hn_u hn_v hn_w hn_sc1 gam gamsc1 sc1var sc1dis vd_damping "
+               "temperature").split()
     want_in = (sum(g[n].size for n in carried + S.TW) + st.case.n3_sg + g["dkp"].size + g["dkw"].size
                + sum(a.size for a in g["metric"].values()))
     assert (b1[0] - b0[0]) == 2 * 8 * want_in, (b1[0] - b0[0], want_in)
