@@ -441,6 +441,13 @@ def run_e2e(args, case, ctrl, wl="mixing"):
     h = g.to("pinned")
     del g
     torch.cuda.empty_cache()
+    # the same way of running the step as the headline: the whole-step
+    # graph (with the host copies as its nodes) unless --step-graph 0
+    graph = int(bool(args.step_graph) and not WORKLOADS[wl].get("inflow"))
+    ctrl.step_graph = graph
+    L.gpu_set_ctrl(ctrl)
+    L.gpu_set_iststep(2)  # a run's first step
+    info0 = L.gpu_step_graph_info()
     S.step(h, 1)  # coeff_p at istep 1, as the first step of a run
     S.step(h, 2)  # untimed: the first step that can be captured as a graph
     L.gpu_sync()
@@ -454,8 +461,14 @@ def run_e2e(args, case, ctrl, wl="mixing"):
     dt = _ranks().max(time.perf_counter() - t0) / k
     _ranks().barrier()
     b1 = L.gpu_xfer_bytes()
+    info = L.gpu_step_graph_info()
+    ctrl.step_graph = 0
+    L.gpu_set_ctrl(ctrl)
+    if graph and (info["failed"] or info["replays"] - info0["replays"] != k + 1):
+        raise RuntimeError(f"e2e: whole-step graph not replayed: {info}")
     return {"s_per_step": dt, "steps": k, "h2d_bytes_per_step": (b1[0] - b0[0]) // k,
-            "d2h_bytes_per_step": (b1[1] - b0[1]) // k}
+            "d2h_bytes_per_step": (b1[1] - b0[1]) // k,
+            "step_launch": "whole-step CUDA graph" if graph else "launched"}
 
 
 # ------------------------------------------------------------- CPU arm

@@ -50,6 +50,7 @@ UNITS = {
     "k_outflow": ("k_outflow.cu", ["-fmad=false"]),
     "lester_outflow": ("lester_outflow.cu", []),
     "k_graph": ("k_graph.cu", []),
+    "k_dfloat": ("k_dfloat.cu", ["-fmad=false"]),
     # the tiled scalar sweep: exact FP64 (no FMA); fast FP64 and FP32
     "k_sweep": ("k_sweep.cu", ["-fmad=false", "-DLES_SWEEP_EXACT"]),
     "k_sweep_fast": ("k_sweep.cu", []),

@@ -416,6 +416,37 @@ __global__ void k_uvw_adv(const BlkDev *__restrict__ blk, int ivar, double dtime
     u[ijk] = u_int[ijk] - ddtime * dpdi / rhou;
 }
 
+// The projection with FP32 arithmetic (the mixed path with FP32 physics):
+// the pressure difference is taken in FP64 and rounded once, the correction
+// dt grad p / rho is formed in FP32 and subtracted from the FP64 u_int in
+// FP64, so u keeps u_int's precision and the correction carries FP32's
+// (GB300 issues FP64 divisions slowly; this kernel has none).
+__global__ void k_uvw_adv_f32(const BlkDev *__restrict__ blk, int ivar, float dtime,
+                              const double *__restrict__ dg, const double *__restrict__ rp,
+                              const double *__restrict__ dkw, double *__restrict__ u,
+                              const double *__restrict__ u_int, const double *__restrict__ rho,
+                              const double *__restrict__ p)
+{
+    const BlkDev b = blk[blockIdx.y];
+    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    long ijk = decode_interior(b, q, i, j, k);
+    int istr = (ivar == 1 && !is_per_or_int(b.bc[0])) ? 3 : 2;
+    int jstr = (ivar == 2 && !is_per_or_int(b.bc[2])) ? 3 : 2;
+    int kstr = (ivar == 3 && !is_per_or_int(b.bc[4])) ? 3 : 2;
+    if (ivar == 3) istr = jstr;
+    if (i < istr || j < jstr || k < kstr) return;
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long nb = ijk - (ivar == 1 ? 1 : ivar == 2 ? jo : ko);
+    const float dp = (float)(p[ijk] - p[nb]);
+    const float h = ivar != 3 ? (float)dg[IDX2(b, i, j)]
+                              : (float)rp[IDX2(b, i, j)] * (float)dkw[b.off1k + k - 1];
+    const float rhou = 0.5f * (float)(rho[ijk] + rho[nb]);
+    const float corr = 1.5f * dtime * (dp / h) / rhou;
+    u[ijk] = u_int[ijk] - (double)corr;
+}
+
 // ------------------------------------------------- density and slip faces
 // code/swap_rhos_block.F:438-451
 __global__ void k_swap_rhos(double *__restrict__ rho, const double *__restrict__ rhonp1,
@@ -443,6 +474,28 @@ __global__ void k_search_lib(double *__restrict__ sc1, double *__restrict__ rhon
         f = (f * rho[q]) / rn;
         if (f > 1.0) f = 1.0;
         sc1[q] = f;
+    }
+}
+
+// search_lib with FP32 arithmetic (the mixed path with FP32 physics): the
+// mixing law and the conservative scalar rescaling of k_search_lib, FP64
+// fields rounded once on load and once on store.
+__global__ void k_search_lib_f32(double *__restrict__ sc1, double *__restrict__ rhonp1,
+                                 const double *__restrict__ rho, float alpha, float rholo, float rhohi,
+                                 long n)
+{
+    const float irhohi = 1.0f / rhohi, irholo = 1.0f / rholo;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        float f = (float)sc1[q];
+        const float r = (float)rho[q];
+        float rho_mix = 1.0f / (f * irhohi + (1.0f - f) * irholo);
+        if (f > 1.0f) rho_mix = rhohi;
+        if (f < 0.0f) rho_mix = rholo;
+        const float rn = alpha * r + (1.0f - alpha) * rho_mix;
+        rhonp1[q] = (double)rn;
+        f = (f * r) / rn;
+        if (f > 1.0f) f = 1.0f;
+        sc1[q] = (double)f;
     }
 }
 
@@ -602,10 +655,14 @@ void launch_pref(const BlkDev *blk, double *p, long n, double *scratch, cudaStre
 
 void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dtime,
                     const double *dg, const double *rp, const double *dkw, double *u,
-                    const double *u_int, const double *rho, const double *p, cudaStream_t st)
+                    const double *u_int, const double *rho, const double *p, bool f32, cudaStream_t st)
 {
-    k_uvw_adv<<<dim3(nblk(maxcell, 128), nb), 128, 0, st>>>(blk, ivar, dtime, dg, rp, dkw, u, u_int,
-                                                          rho, p);
+    if (f32)
+        k_uvw_adv_f32<<<dim3(nblk(maxcell, 256), nb), 256, 0, st>>>(blk, ivar, (float)dtime, dg, rp, dkw, u,
+                                                                  u_int, rho, p);
+    else
+        k_uvw_adv<<<dim3(nblk(maxcell, 128), nb), 128, 0, st>>>(blk, ivar, dtime, dg, rp, dkw, u, u_int,
+                                                              rho, p);
     count_launch(1);
 }
 
@@ -617,10 +674,14 @@ void launch_swap_rhos(double *rho, const double *rhonp1, double *rhonm1, long n,
 }
 
 void launch_search_lib(double *sc1, double *rhonp1, const double *rho, double alpha, double rholo,
-                       double rhohi, long n, cudaStream_t st)
+                       double rhohi, long n, bool f32, cudaStream_t st)
 {
     unsigned g = nblk(n, 256);
-    k_search_lib<<<g > 4096 ? 4096 : g, 256, 0, st>>>(sc1, rhonp1, rho, alpha, rholo, rhohi, n);
+    if (f32)
+        k_search_lib_f32<<<g > 4096 ? 4096 : g, 256, 0, st>>>(sc1, rhonp1, rho, (float)alpha, (float)rholo,
+                                                             (float)rhohi, n);
+    else
+        k_search_lib<<<g > 4096 ? 4096 : g, 256, 0, st>>>(sc1, rhonp1, rho, alpha, rholo, rhohi, n);
     count_launch(1);
 }
 

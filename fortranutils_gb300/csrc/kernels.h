@@ -39,10 +39,22 @@ void launch_extrap_p(const BlkDev *blk, int nb, double *p, cudaStream_t st);
 void launch_pref(const BlkDev *blk, double *p, long n, double *scratch, cudaStream_t st);
 void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dtime,
                     const double *dg, const double *rp, const double *dkw, double *u,
-                    const double *u_int, const double *rho, const double *p, cudaStream_t st);
+                    const double *u_int, const double *rho, const double *p, bool f32, cudaStream_t st);
 void launch_swap_rhos(double *rho, const double *rhonp1, double *rhonm1, long n, cudaStream_t st);
+// double-float outer iteration of the mixed solver (k_dfloat.cu)
+void launch_df_split(const double *src, float2 *dst, long n, cudaStream_t st);
+void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b, const double *shift, float2 *dst,
+                       cudaStream_t st);
+// cycles (nullable, device): skipped when *cycles == 0
+void launch_df_join(const float2 *src, double *dst, long n, const double *cycles, cudaStream_t st);
+void launch_df_update(const BlkDev *blk, int nb, long maxcell, float2 *p, const float *e, const PushDev *push,
+                      cudaStream_t st);
+void launch_df_resid(const BlkDev *blk, int nb, long maxcell, const float2 *E, const float2 *N, const float2 *R,
+                     const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
+                     cudaStream_t st);
+// f32: FP32 arithmetic on the FP64 fields (the mixed path with FP32 physics)
 void launch_search_lib(double *sc1, double *rhonp1, const double *rho, double alpha, double rholo,
-                       double rhohi, long n, cudaStream_t st);
+                       double rhohi, long n, bool f32, cudaStream_t st);
 void launch_slipbc(const BlkDev *blk, int nb, long maxik, double dtime, const double *djp,
                    double *u, double *v, const double *v_int, double *w, double *sc1,
                    double *rho, const double *p, cudaStream_t st);

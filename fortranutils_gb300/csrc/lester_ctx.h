@@ -89,6 +89,9 @@ struct Ctx {
     FastSet<float> f32;
     FastSet<double> f64;
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
+    // the mixed solver's outer iteration in double-float (k_dfloat.cu): the
+    // level-1 coefficients, p and b - shift as FP32 pairs
+    float2 *df_E = nullptr, *df_N = nullptr, *df_R = nullptr, *df_P = nullptr, *df_p = nullptr, *df_b = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
     // convective outflow / fixed inflow sides (lester_outflow.cu)
     bool sides_built = false;
@@ -127,7 +130,7 @@ struct Ctx {
     long prof_launches[2] = {0, 0};
     double prof_ms_acc[2] = {0, 0};
     // graphs of the fast solvers: [FP64, mixed][defect correction, flexible CG]
-    CycleGraph cg[2][2];
+    CycleGraph cg[2][3];  // [FP64, mixed][defect correction, flexible CG, double-float defect correction]
     cudaStream_t cap_stream = nullptr;
     std::vector<cudaEvent_t> *cap_ev = nullptr;  // set while capturing
     // bytes copied between host and device by staged (host-array) calls

@@ -598,6 +598,7 @@ static void free_ctx(Ctx *c)
         }
     for (double *p : c->scratch) cudaFree(p);
     for (double *p : c->coef_mirror) cudaFree(p);
+    for (float2 *p : {c->df_E, c->df_N, c->df_R, c->df_P, c->df_p, c->df_b}) cudaFree(p);
     for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
     if (c->xs_in) cudaStreamDestroy(c->xs_in);
     if (c->xs_out) cudaStreamDestroy(c->xs_out);
@@ -809,6 +810,20 @@ template <typename T> static int alloc_fast(Ctx &c)
     return 0;
 }
 
+static int alloc_df(Ctx &c)
+{
+    if (c.df_E) return 0;
+    float2 **arr[6] = {&c.df_E, &c.df_N, &c.df_R, &c.df_P, &c.df_p, &c.df_b};
+    for (float2 **a : arr) {
+        if (cudaMalloc((void **)a, sizeof(float2) * (size_t)c.tot_sg3) != cudaSuccess) {
+            cudaGetLastError();
+            return set_err(LES_ERR_NOMEM, "fast-solver allocation failed");
+        }
+        LES_CUDA(cudaMemset(*a, 0, sizeof(float2) * (size_t)c.tot_sg3));
+    }
+    return 0;
+}
+
 template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
 {
     bool same = (c.coef_prec == prec) && (c.coef_gen_seen == c.coef_gen);
@@ -854,6 +869,13 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
         LES_CUDA(cudaMemcpyAsync(&mbad, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
         LES_CUDA(cudaStreamSynchronize(c.stream));
         F.mf = (mbad == 0);
+    }
+    // mixed solver: double-float copies of the level-1 FP64 coefficients
+    if (sizeof(T) == 4) {
+        if ((r = alloc_df(c))) return r;
+        const double *src[4] = {c.E64, c.N64, c.R64, c.P64};
+        float2 *dst[4] = {c.df_E, c.df_N, c.df_R, c.df_P};
+        for (int q = 0; q < 4; q++) launch_df_split(src[q], dst[q], c.tot_sg3, c.stream);
     }
     for (int q = 0; q < 7; q++) c.coef_key[q] = A.a[q];
     c.coef_gen_seen = c.coef_gen;
@@ -978,18 +1000,38 @@ static void drop_graph(CycleGraph &G)
     G.ev.clear();
 }
 
+// The mixed solver's defect correction in double-float: p += e, then
+// r = b - A p (k_dfloat.cu) into the cycle's FP32 right-hand side and
+// ||r||^2 into d_small[0]
+static void df_cycle_tail(Ctx &c, float *e, float *rT)
+{
+    LevelGeom &L1 = c.lv[1];
+    const int nb = c.g.numbl;
+    launch_df_update(L1.d_blk, nb, L1.maxcell, c.df_p, e, L1.d_push, c.stream);
+    launch_df_resid(L1.d_blk, nb, L1.maxcell, c.df_E, c.df_N, c.df_R, c.df_P, c.df_p, c.df_b, rT, c.d_partial,
+                    c.d_small, c.stream);
+}
+
+// p and b - shift of level 1 as double-float pairs, from the FP64 arrays
+static void df_enter(Ctx &c, const double *f, const double *b)
+{
+    LevelGeom &L1 = c.lv[1];
+    launch_df_split(f, c.df_p, c.tot_sg3, c.stream);
+    launch_df_split_b(L1.d_blk, c.g.numbl, L1.maxcell, b, c.singular ? c.d_bmean : nullptr, c.df_b, c.stream);
+}
+
 // Capture one outer iteration as a CUDA graph, so the ~10^2 small launches
 // of the coarse levels cost one graph launch: defect correction (V-cycle,
 // p += e, FP64 residual) or flexible CG (V-cycle, direction and step),
 // then the read-back of the residual sums.  Re-captured when the arrays or
 // the solver settings change.
 template <typename T>
-static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b, bool kry)
+static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b, bool kry, bool df = false)
 {
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
-        G.krylov == (int)kry && G.threads == c.rb_threads && G.line == k.rb_line)
+        G.krylov == (kry ? 1 : df ? 2 : 0) && G.threads == c.rb_threads && G.line == k.rb_line)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -1010,6 +1052,8 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
         if (kry) {
             launch_fcg<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, F.x, f, c.d_fp, c.d_fq,
                           c.d_fr, F.b, L1.d_push, c.d_partial, c.d_small + 16, c.d_small, c.stream);
+        } else if (df) {
+            df_cycle_tail(c, (float *)F.x, (float *)F.b);
         } else {
             launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
@@ -1038,7 +1082,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.singular = c.singular;
     G.mf = fset<T>(c).mf;
     G.tail = k.mg_tail;
-    G.krylov = (int)kry;
+    G.krylov = kry ? 1 : df ? 2 : 0;
     G.threads = c.rb_threads;
     G.line = k.rb_line;
     return 0;
@@ -1140,6 +1184,8 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     cudaGraphConditionalHandle hw;
     if ((r = graph_cond_handle(c, &hw)) || (r = graph_cond_handle(c, &c.sg_post))) return r;
     launch_loop_init(hw, c.d_small, c.d_loop, rtol, c.stream);
+    const bool df = sizeof(T) == 4 && !kry;  // mixed defect correction: double-float cycles
+    if (df) df_enter(c, f, b);
     cudaGraph_t body;
     cudaStream_t saved;
     if ((r = graph_add_conditional(c, hw, cudaGraphCondTypeWhile, &body)) || (r = graph_begin_body(c, body, &saved)))
@@ -1149,6 +1195,8 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     if (kry) {
         launch_fcg<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, F.x, f, c.d_fp, c.d_fq, c.d_fr, F.b,
                       L1.d_push, c.d_partial, c.d_small + 16, c.d_small, c.stream);
+    } else if (df) {
+        df_cycle_tail(c, (float *)F.x, (float *)F.b);
     } else {
         launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
         launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
@@ -1157,11 +1205,15 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     launch_loop_step(hw, c.d_small, c.d_loop, rtol, maxit, c.c.krylov == 2 && !kry, c.stream);
     c.sg.body_launches = launch_count() - l0;
     if ((r = graph_end_body(c, saved))) return r;
-    // flexible CG: its recursive residual confirmed against b - A p
-    if (kry)
+    // double-float cycles: p back to FP64 (when a cycle ran)
+    if (df) launch_df_join(c.df_p, f, c.tot_sg3, c.d_loop + 3, c.stream);
+    // flexible CG's recursive residual, or the double-float one, confirmed
+    // against b - A p in FP64
+    if (kry || df)
         launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
-                              c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small, c.stream);
-    launch_loop_gate(c.sg_post, c.d_small, c.d_loop, rtol, kry, c.stream);
+                              c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial, c.d_small,
+                              c.stream);
+    launch_loop_gate(c.sg_post, c.d_small, c.d_loop, rtol, kry || df, c.stream);
     c.sg.kry = kry;
     return 0;
 }
@@ -1225,9 +1277,29 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
     int it = 0;
     double rel = b2 > 0 ? std::sqrt(r2 / b2) : 0.;
     CycleGraph *Gs = c.cg[sizeof(T) == 4 ? 1 : 0];
+    // mixed defect correction: the cycles in double-float, p in c.df_p
+    // until df_leave() puts it back into f and checks the residual in FP64
+    bool df = false;
+    auto df_leave = [&]() -> int {
+        if (!df) return 0;
+        df = false;
+        launch_df_join(c.df_p, f, c.tot_sg3, nullptr, c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+                              c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial, c.d_small, c.stream);
+        int rr = sync_small(c, 2);
+        if (rr) return rr;
+        r2 = c.h_small[0];
+        rel = std::sqrt(r2 / b2);
+        return 0;
+    };
+    bool df_done = false;  // one double-float pass per solve; FP64 cycles after it
     while (b2 > 0 && rel > rtol && it < maxit) {
-        CycleGraph &G = Gs[kry ? 1 : 0];
-        if ((r = ensure_cycle_graph<T>(c, G, f, b, kry))) return r;
+        if (sizeof(T) == 4 && !kry && !df && !df_done) {
+            df_enter(c, f, b);
+            df = df_done = true;
+        }
+        CycleGraph &G = Gs[kry ? 1 : df ? 2 : 0];
+        if ((r = ensure_cycle_graph<T>(c, G, f, b, kry, df))) return r;
         STAGE_CHECK("graph");
         const double rel_prev = rel;
         LES_CUDA(cudaGraphLaunch(G.exec, c.stream));
@@ -1244,8 +1316,16 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
         rel = std::sqrt(r2 / b2);
         it++;
         if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+        // converged in double-float, or out of cycles: confirm in FP64 (and
+        // carry on with FP64 cycles if the double-float residual was short)
+        if (df && (rel <= rtol || it >= maxit)) {
+            if ((r = df_leave())) return r;
+            if (!std::isfinite(rel)) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", it);
+            continue;
+        }
         if (may_switch && !kry && rel > rtol && rel > 0.5 * rel_prev) {
             // the plain cycle has stalled or diverges: flexible CG from here
+            if ((r = df_leave())) return r;
             kry = true;
             if ((r = fcg_reset(c))) return r;
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
@@ -1267,6 +1347,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
             if (rel > rtol) LES_CUDA(cudaMemsetAsync(c.d_small + 18, 0, sizeof(double), c.stream));
         }
     }
+    if ((r = df_leave())) return r;
     {
         cudaError_t ee = cudaGetLastError();
         if (ee != cudaSuccess) return set_err(LES_ERR_CUDA, "fast solve, %d cycles: %s", it, cudaGetErrorString(ee));
@@ -1919,7 +2000,8 @@ int lester_uvw_adv(const int *ivar1, const double *diu, const double *rp, const 
         (r = st.in(rho, c.tot_sg3, &drho)) || (r = st.in(p, c.tot_sg3, &dpp)))
         return r;
     LevelGeom &L = c.lv[1];
-    launch_uvw_adv(L.d_blk, c.g.numbl, L.maxcell, iv, c.c.dtime, dd, drp, ddkw, du, dui, drho, dpp, c.stream);
+    launch_uvw_adv(L.d_blk, c.g.numbl, L.maxcell, iv, c.c.dtime, dd, drp, ddkw, du, dui, drho, dpp, phys32_on(c),
+                   c.stream);
     halo(c, 1, du);
     return st.finish();
 }
@@ -1954,7 +2036,7 @@ int lester_search_lib(double *sc1, double *sc1var, double *rhonp1, double *tempe
     if ((r = st.io(sc1, c.tot_sg3, &ds)) || (r = st.io(rhonp1, c.tot_sg3, &dr)) || (r = st.in(rho, c.tot_sg3, &drho)))
         return r;
     if (temperature && (r = st.io(temperature, c.tot_sg3, &dt))) return r;
-    launch_search_lib(ds, dr, drho, *alpha, *rholo, *rhohi, c.tot_sg3, c.stream);
+    launch_search_lib(ds, dr, drho, *alpha, *rholo, *rhohi, c.tot_sg3, phys32_on(c), c.stream);
     halo(c, 1, ds);
     halo(c, 1, dr);
     if (dt) halo(c, 1, dt);
