@@ -45,6 +45,15 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b)
     return fast_sum(s.x, __fadd_rn(s.y, t.y));
 }
 
+// a + b, both double-float, with the lo parts added in FP32: the error is
+// about 2^-24 of |a.lo + b.lo|, i.e. about 2^-48 of |a| + |b|, the order of
+// the format itself; cheaper than df_add by nine operations
+__device__ __forceinline__ float2 df_add_lo(float2 a, float2 b)
+{
+    const float2 s = two_sum(a.x, b.x);
+    return fast_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+
 // a + b, b an FP32 value
 __device__ __forceinline__ float2 df_add_f(float2 a, float b)
 {
@@ -117,7 +126,7 @@ __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__
 // r = b - A p in double-float (E, N, R, P as in k_resid_outer): r rounded
 // to FP32 as the next cycle's right-hand side, per-CTA partial sums of r^2
 // in FP64 (an FP32 square overflows above 1.8e19, which a diverging cycle
-// reaches)
+// reaches).  One CTA per (j, k) row at a time, its threads along i.
 __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk, const float2 *__restrict__ E,
                                                   const float2 *__restrict__ N, const float2 *__restrict__ R,
                                                   const float2 *__restrict__ P, const float2 *__restrict__ x,
@@ -125,21 +134,25 @@ __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk
                                                   double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
-    double acc = 0.;
+    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < b.ncell; q += (long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        const long p = decode_interior(b, q, i, j, k);
-        float2 r = df_add(bb[p], df_neg(df_mul(P[p], x[p])));
-        r = df_add(r, df_mul(E[p - 1], x[p - 1]));
-        r = df_add(r, df_mul(E[p], x[p + 1]));
-        r = df_add(r, df_mul(N[p - jo], x[p - jo]));
-        r = df_add(r, df_mul(N[p], x[p + jo]));
-        r = df_add(r, df_mul(R[p - ko], x[p - ko]));
-        r = df_add(r, df_mul(R[p], x[p + ko]));
-        const float rf = __fadd_rn(r.x, r.y);
-        rT[p] = rf;
-        acc = __fma_rn((double)rf, (double)rf, acc);
+    double acc = 0.;
+    for (int row = blockIdx.x; row < nj * nk; row += gridDim.x) {
+        const int k = row / nj, j = row - k * nj;
+        const long base = b.off3 + jo * (j + 1) + ko * (k + 1);  // (i = 1, j + 2, k + 2)
+        for (int i = 1 + threadIdx.x; i <= ni; i += blockDim.x) {
+            const long p = base + i;
+            float2 r = df_add_lo(bb[p], df_neg(df_mul(P[p], x[p])));
+            r = df_add_lo(r, df_mul(E[p - 1], x[p - 1]));
+            r = df_add_lo(r, df_mul(E[p], x[p + 1]));
+            r = df_add_lo(r, df_mul(N[p - jo], x[p - jo]));
+            r = df_add_lo(r, df_mul(N[p], x[p + jo]));
+            r = df_add_lo(r, df_mul(R[p - ko], x[p - ko]));
+            r = df_add_lo(r, df_mul(R[p], x[p + ko]));
+            const float rf = __fadd_rn(r.x, r.y);
+            rT[p] = rf;
+            acc = __fma_rn((double)rf, (double)rf, acc);
+        }
     }
     double v[1] = {acc};
     block_reduce_store<1>(v, partial + (blockIdx.y * (long)gridDim.x + blockIdx.x));
@@ -196,8 +209,10 @@ void launch_df_resid(const BlkDev *blk, int nb, long maxcell, const float2 *E, c
                      const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
                      cudaStream_t st)
 {
-    // grid-stride: a few CTAs per SM, so the final sum reads few partials
-    unsigned gx = cap_grid(maxcell, 256, (unsigned)((1216 + nb - 1) / nb));
+    // rows of a block over a few CTAs per SM, so the final sum reads few
+    // partials (maxcell / 32 bounds the rows of any block: ni >= 32 is not
+    // assumed, only that a CTA per row is enough)
+    unsigned gx = cap_grid(maxcell, 32, (unsigned)((1216 + nb - 1) / nb));
     k_df_resid<<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, rT, partial);
     k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
     count_launch(2);

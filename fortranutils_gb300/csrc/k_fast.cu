@@ -17,6 +17,8 @@
 // prolongation of code/prol_block.F, whose "coarse ghost := interior
 // neighbour" rule (prol_block.F:325-357) is applied by clamping the coarse
 // index instead of writing the ghosts.
+#include <algorithm>
+
 #include "k_common.cuh"
 #include "kernels.h"
 
@@ -226,6 +228,13 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 }
 
 // ---- red-black SOR half sweep, all blocks of a level ----------------------
+// Grid-stride over the points of one colour, kRbU points per thread and
+// iteration: the operands of all kRbU points are loaded before any is
+// updated (the points share no operand: one colour is written, the other
+// read), so each thread has kRbU points' loads in flight, and the grid is a
+// few CTAs per SM rather than one short-lived thread per point.
+constexpr int kRbU = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
@@ -234,9 +243,44 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
                                             const PushDev *__restrict__ push, MfTab<T> mf)
 {
     const BlkDev b = blk[blockIdx.y];
-    int i, j, k;
-    if (!rb_decode(b, blockIdx.x * blockDim.x + threadIdx.x, color, i, j, k)) return;
-    rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const unsigned stride = gridDim.x * blockDim.x;
+    const unsigned total = (unsigned)((b.n[0] - 1) >> 1) * (unsigned)(b.n[1] - 2) * (unsigned)(b.n[2] - 2);
+    for (unsigned q0 = blockIdx.x * blockDim.x + threadIdx.x; q0 < total; q0 += kRbU * stride) {
+        bool ok[kRbU];
+        int ii[kRbU], jj[kRbU], kk[kRbU];
+        long pp[kRbU];
+        T c[kRbU][6], dinv[kRbU], s[kRbU], xo[kRbU];
+#pragma unroll
+        for (int u = 0; u < kRbU; u++) {
+            const unsigned q = q0 + u * stride;
+            ok[u] = q >= q0 && rb_decode(b, q, color, ii[u], jj[u], kk[u]);
+            if (!ok[u]) continue;
+            const long p = b.off3 + (ii[u] - 1) + jo * (jj[u] - 1) + ko * (kk[u] - 1);
+            pp[u] = p;
+            if (mf.E2) {
+                coefs_mf(b, mf, ii[u], jj[u], kk[u], c[u], dinv[u]);
+            } else {
+                c[u][0] = E[p - 1];
+                c[u][1] = E[p];
+                c[u][2] = N[p - jo];
+                c[u][3] = N[p];
+                c[u][4] = R[p - ko];
+                c[u][5] = R[p];
+                dinv[u] = D[p];
+            }
+            s[u] = bb[p] + c[u][0] * x[p - 1] + c[u][1] * x[p + 1] + c[u][2] * x[p - jo] + c[u][3] * x[p + jo] +
+                   c[u][4] * x[p - ko] + c[u][5] * x[p + ko];
+            xo[u] = x[p];
+        }
+#pragma unroll
+        for (int u = 0; u < kRbU; u++) {
+            if (!ok[u]) continue;
+            const T xn = xo[u] + omega * (s[u] * dinv[u] - xo[u]);
+            x[pp[u]] = xn;
+            if (push) push_ghosts(push + 6 * blockIdx.y, b, ii[u], jj[u], kk[u], xn, x);
+        }
+    }
 }
 
 // ---- y-line zebra relaxation ---------------------------------------------
@@ -796,13 +840,48 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 }
 
 // maxhalf = max over blocks of ((ni + 1) / 2) * nj * nk
+// the L2 persisting window (set_l2_window), applied per launch so that it
+// is kept when the launch is captured into a graph
+static cudaAccessPolicyWindow g_l2win = {};
+
+void set_l2_window(void *base, size_t bytes, float hit_ratio)
+{
+    g_l2win.base_ptr = base;
+    g_l2win.num_bytes = bytes;
+    g_l2win.hitRatio = hit_ratio;
+    g_l2win.hitProp = cudaAccessPropertyPersisting;
+    g_l2win.missProp = cudaAccessPropertyStreaming;
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_l2(void (*kern)(KArgs...), dim3 grid, int threads, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(threads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    if (g_l2win.num_bytes) {
+        at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        at[0].val.accessPolicyWindow = g_l2win;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
                const MfTab<T> &mf, int threads, cudaStream_t st)
 {
     const int t = (threads == 128 || threads == 512) ? threads : 256;
-    k_rb<T><<<dim3(nb_(maxhalf, t), nb), t, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
+    // enough threads for kRbU points each, at most about 16 CTA-slots of
+    // 128 threads per SM over all blocks
+    unsigned gx = nb_(maxhalf, t * kRbU);
+    const unsigned cap = (unsigned)std::max(1, (152 * 16 * 128 / t + nb - 1) / nb);
+    if (gx > cap) gx = cap;
+    launch_l2(k_rb<T>, dim3(gx, nb), t, st, blk, color, (T)omega, E, N, R, D, x, b, push, mf);
     count_launch(1);
 }
 
@@ -819,8 +898,7 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxc
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
                            const MfTab<T> &mf, cudaStream_t st)
 {
-    k_resid_restrict<T><<<dim3(nb_(maxcell_c, 256), nb), 256, 0, st>>>(bc, bf, E, N, R, D, x, b,
-                                                                     bcoarse, mf);
+    launch_l2(k_resid_restrict<T>, dim3(nb_(maxcell_c, 256), nb), 256, st, bc, bf, E, N, R, D, x, b, bcoarse, mf);
     count_launch(1);
 }
 
@@ -828,7 +906,7 @@ template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
                          T *xf, const PushDev *push, cudaStream_t st)
 {
-    k_prolong<T><<<dim3(nb_(maxcell_f, 256), nb), 256, 0, st>>>(bc, bf, xc, xf, push);
+    launch_l2(k_prolong<T>, dim3(nb_(maxcell_f, 256), nb), 256, st, bc, bf, xc, xf, push);
     count_launch(1);
 }
 

@@ -175,17 +175,21 @@ __device__ __forceinline__ void mbar_drain(unsigned long long *m, unsigned parit
 // sentinel, re-read it from L2 (another CTA is computing it); bounded by
 // `limit` polls, or until another CTA has set *err (then *err is set and
 // the staged value returned: the call reports LES_ERR_TIMEOUT).
+// The error flag is read every 64 polls only (each read is an L2 round
+// trip of its own).
 template <typename S>
 __device__ S fresh(S v, const S *g, int *err, long limit)
 {
     long it = 0;
     while (v == (S)kSentinel) {
-        if (*(volatile int *)err) return v;
-        if (++it > limit) {
-            atomicExch(err, 1);
-            return v;
+        if ((++it & 63) == 0) {
+            if (*(volatile int *)err) return v;
+            if (it > limit) {
+                atomicExch(err, 1);
+                return v;
+            }
         }
-        __nanosleep(32);
+        if (it > 4) __nanosleep(32);
         v = ld_strong(g);
     }
     return v;
@@ -386,7 +390,8 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
 #define TB(tb, p, jj) at(GR_2D, tb, p, jj)
         bool ok = true;
         int t = ts;
-        int err_seen = 0;  // thread 0: the error flag, re-read from L2 every 16 planes only
+        int err_seen = 0;
+  // thread 0: the error flag, re-read from L2 every 16 planes only
         for (; t <= t1; t++) {
             const long u = ubase + (t - ts);
             if (tid == 0) {
@@ -415,6 +420,12 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
             if (t < t0 || !row) continue;
             const int i = t - j;
             if (i < 2 || i > ni) continue;
+            // the new values of the two layers below: staged, or still the
+            // sentinel when staged; then their L2 re-reads are issued here,
+            // first, and overlap the rest of the point's work
+            S m1 = slot(GR_M1, 3, t, j), m2 = k != 2 ? slot(GR_M2, 0, t, j) : (S)0;
+            if (m1 == (S)kSentinel) m1 = ld_strong(A.scnew + e3(k - 1, t, j));
+            if (m2 == (S)kSentinel) m2 = ld_strong(A.scnew + e3(k - 2, t, j));
             // ---- one point of set_sc1_block.F:104-502 (sc1_cell's operands)
             const R rho0 = at(GR_OWN, 5, t, j);
             const R rhowf = half * (rho0 + at(GR_OWN, 5, t - 1, j));
@@ -439,7 +450,7 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
             const R ss = (jhalo && j == j0) ? newval(GR_SCH, 0, k, t - 1, j - 1) : SC(t - 1, j - 1);
             const R sn = SC(t + 1, j + 1);
             // the layer below: new values (interior), old ones on its ghost layer
-            const R sl = newval(GR_M1, 3, k - 1, t, j);
+            const R sl = (R)fresh<S>(m1, A.scnew + e3(k - 1, t, j), A.err, limit);
             const R sr = at(GR_P1B, 0, t, j);
 #define QD(x, tb, rtb, pp, jj) (FAST ? (x) * TB(rtb, pp, jj) : (x) / TB(tb, pp, jj))
             const R dfdxwf = QD(s0 - sw, T_DIU, T_RDIU, t, j);
@@ -487,7 +498,7 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
                               ? dfdzlf
                               : (R)GR[(long)(A.link[bi * 6 + 4]) * 6 * gst + 5 * gst + (i - 1) + (long)gm * (j - 1)];
             else
-                dfdzllf = QZ(sl - newval(GR_M2, 0, k - 2, t, j), dkp_m3, rdkp_m3);
+                dfdzllf = QZ(sl - (R)fresh<S>(m2, A.scnew + e3(k - 2, t, j), A.err, limit), dkp_m3, rdkp_m3);
             if (k == nk)
                 dfdzrrf = (b.bc[5] != LES_BCT_INTERFACE_D)
                               ? dfdzrf

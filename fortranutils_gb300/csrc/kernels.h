@@ -41,6 +41,9 @@ void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dt
                     const double *dg, const double *rp, const double *dkw, double *u,
                     const double *u_int, const double *rho, const double *p, bool f32, cudaStream_t st);
 void launch_swap_rhos(double *rho, const double *rhonp1, double *rhonm1, long n, cudaStream_t st);
+// L2 persisting window of the fast solvers' smoother, restriction and
+// prolongation launches (k_fast.cu): bytes 0 removes it
+void set_l2_window(void *base, size_t bytes, float hit_ratio);
 // double-float outer iteration of the mixed solver (k_dfloat.cu)
 void launch_df_split(const double *src, float2 *dst, long n, cudaStream_t st);
 void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b, const double *shift, float2 *dst,

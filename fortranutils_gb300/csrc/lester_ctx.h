@@ -1,6 +1,7 @@
 // lester_ctx.h -- host-side state of the library (what the reference keeps
 // in COMMON blocks) and helpers shared by the host translation units.
 #pragma once
+#include <cstdio>
 #include <cuda_runtime.h>
 #include <string>
 #include <vector>
@@ -91,6 +92,8 @@ struct Ctx {
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
     // the mixed solver's outer iteration in double-float (k_dfloat.cu): the
     // level-1 coefficients, p and b - shift as FP32 pairs
+    std::FILE *step_log = nullptr;  // lester_gpu_step_log's file (one JSON line per lester_step)
+    bool l2_window = false;  // the smoother's L2 persisting window is set (alloc_fast)
     float2 *df_E = nullptr, *df_N = nullptr, *df_R = nullptr, *df_P = nullptr, *df_p = nullptr, *df_b = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
     // convective outflow / fixed inflow sides (lester_outflow.cu)

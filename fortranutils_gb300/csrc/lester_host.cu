@@ -577,8 +577,14 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_nrm3);
     cudaFree(c->d_metbuf);
     cudaFree(c->d_flag);
-    void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.b, c->f32.cp, c->f32.dp,
-                  c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.b, c->f64.cp, c->f64.dp,
+    // (f32.b and f64.b lie in the allocations of f32.x and f64.x)
+    if (c->l2_window) {
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+        set_l2_window(nullptr, 0, 0.f);
+    }
+    void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.cp, c->f32.dp,
+                  c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.cp, c->f64.dp,
                   c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
                   c->d_exit, c->d_sideout, c->d_uprof, c->d_vprof};
     for (void *p : fp) cudaFree(p);
@@ -599,6 +605,7 @@ static void free_ctx(Ctx *c)
     for (double *p : c->scratch) cudaFree(p);
     for (double *p : c->coef_mirror) cudaFree(p);
     for (float2 *p : {c->df_E, c->df_N, c->df_R, c->df_P, c->df_p, c->df_b}) cudaFree(p);
+    if (c->step_log) std::fclose(c->step_log);
     for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
     if (c->xs_in) cudaStreamDestroy(c->xs_in);
     if (c->xs_out) cudaStreamDestroy(c->xs_out);
@@ -788,13 +795,38 @@ template <typename T> static int alloc_fast(Ctx &c)
     FastSet<T> &F = fset<T>(c);
     if (F.E) return 0;
     size_t nb = sizeof(T) * (size_t)c.tot3;
-    T **arr[6] = {&F.E, &F.N, &F.R, &F.D, &F.x, &F.b};
+    T **arr[5] = {&F.E, &F.N, &F.R, &F.D, &F.x};
+    // x and b in one allocation (x, then b at a 256-byte boundary): the
+    // level-1 part of both is one address range for the L2 window below
+    const long xspan = (c.tot3 + 63) / 64 * 64;
     for (T **a : arr) {
-        if (cudaMalloc((void **)a, nb) != cudaSuccess) {
+        const size_t bytes = a == &F.x ? sizeof(T) * (size_t)(xspan + c.tot3) : nb;
+        if (cudaMalloc((void **)a, bytes) != cudaSuccess) {
             cudaGetLastError();
             return set_err(LES_ERR_NOMEM, "fast-solver allocation failed");
         }
-        LES_CUDA(cudaMemset(*a, 0, nb));
+        LES_CUDA(cudaMemset(*a, 0, bytes));
+    }
+    F.b = F.x + xspan;
+    // The mixed solver's smoother re-reads x and b of level 1 from DRAM at
+    // every half sweep (they are not kept in L2 between launches): its
+    // launches mark them persisting in L2 (a per-launch access-policy
+    // window over x .. b's level 1, within the context's persisting
+    // set-aside, released at finalize).
+    if (sizeof(T) == 4 && !c.l2_window) {
+        int maxp = 0, maxw = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev);
+        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev);
+        const size_t span = sizeof(T) * (size_t)(xspan + c.tot_sg3);
+        if (maxp > 0 && maxw > 0 && span <= (size_t)maxw &&
+            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min((size_t)maxp, span)) == cudaSuccess) {
+            size_t got = 0;
+            cudaDeviceGetLimit(&got, cudaLimitPersistingL2CacheSize);
+            set_l2_window(F.x, span, got >= span ? 1.0f : (float)got / (float)span);
+            c.l2_window = true;
+        }
+        cudaGetLastError();
     }
     if (!c.E64) {
         size_t n1 = sizeof(double) * (size_t)c.tot_sg3;

@@ -13,6 +13,8 @@
 // time, so that most of the traffic overlaps the step's kernels.  Scratch
 // fields passed as NULL are kept on the device by the library.
 #include <algorithm>
+#include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 
@@ -349,6 +351,12 @@ static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
     c.last_cycles = cycles;
     c.last_relres = h[1];
     c.last_solve_ms = -1;  // not timed inside the graph
+    {
+        const double rn = 1.0 / c.lv[1].npts_all, bn = std::sqrt(h[0] * rn);
+        c.last_norms[0] = h[1] * bn;  // rnorm from ||r|| / ||b|| and ||b||^2
+        c.last_norms[1] = bn;
+        c.last_norms[2] = c.last_norms[3] = 0.;
+    }
     if (h[6] != 0) return set_err(LES_ERR_TIMEOUT, "set_sc1: grid barrier of the scalar sweep timed out");
     if (status == 4) return set_err(LES_ERR_NONFINITE, "non-finite residual after %d cycles", cycles);
     if (status == 3 || status == 5) {
@@ -374,10 +382,44 @@ static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
     return 0;
 }
 
+static int step_body(Ctx &c, lester_fields *F, const int *istep);
+
+// the step, and its JSON line when a step log is open (lester_gpu_step_log)
 int lester_step(lester_fields *F, const int *istep)
 {
     LES_NEED_CTX();
     Ctx &c = *g_ctx;
+    if (!c.step_log) return step_body(c, F, istep);
+    const long h0 = c.h2d_bytes, d0 = c.d2h_bytes, rep0 = c.sg.replays;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = step_body(c, F, istep);
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    // the discrete divergence of the projected velocity is the pressure
+    // equation's residual: resid_rms (rnorm of code/norms.F) measures it
+    std::fprintf(c.step_log,
+                 "{\"istep\": %d, \"rc\": %d, \"ms\": %.4f, \"vcycles\": %d, \"relres\": %.6e, "
+                 "\"resid_rms\": %.6e, \"rhs_rms\": %.6e, \"graph\": %s, \"h2d_bytes\": %ld, "
+                 "\"d2h_bytes\": %ld}\n",
+                 istep ? *istep : -1, rc, ms, c.last_cycles, c.last_relres, c.last_norms[0], c.last_norms[1],
+                 c.sg.replays != rep0 ? "true" : "false", c.h2d_bytes - h0, c.d2h_bytes - d0);
+    std::fflush(c.step_log);
+    return rc;
+}
+
+int lester_gpu_step_log(const char *path)
+{
+    LES_NEED_CTX();
+    Ctx &c = *g_ctx;
+    if (c.step_log) std::fclose(c.step_log);
+    c.step_log = nullptr;
+    if (!path || !*path) return 0;
+    c.step_log = std::fopen(path, "a");
+    if (!c.step_log) return set_err(LES_ERR_ARG, "step log: cannot open %s", path);
+    return 0;
+}
+
+static int step_body(Ctx &c, lester_fields *F, const int *istep)
+{
     if (!F || !istep) return set_err(LES_ERR_ARG, "null fields / istep");
     int r0;
     if ((r0 = ensure_sides(c))) return r0;

@@ -227,6 +227,11 @@ def gpu_step_graph_info() -> dict:
     return {"replays": n.value, "handovers": h.value, "failed": bool(f.value), "why": why.value.decode()}
 
 
+def gpu_step_log(path) -> None:
+    """Append one JSON line per lester_step to `path` (None closes)."""
+    _check(lib().lester_gpu_step_log(None if path is None else str(path).encode()))
+
+
 def gpu_tuned(prec: int) -> dict:
     """Settings the autotuner chose for prec 64 (FP64) or 32 (mixed)."""
     d, t, s, tl, ln = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()

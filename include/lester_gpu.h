@@ -262,6 +262,14 @@ int lester_gpu_xfer_bytes(long *h2d, long *d2h);
  * Returns LES_ERR_NOT_CONVERGED (after completing the step) if a fast
  * pressure solver stopped at max_outer above rtol. */
 int lester_step(lester_fields *fields, const int *istep);
+/* No counterpart in the reference (its step.F prints wall times only): with
+ * a path, every later lester_step appends one JSON line to that file --
+ * istep, return code, host wall ms of the call, V-cycles, relative
+ * residual, the RMS residual and right-hand side of the pressure equation
+ * (code/norms.F rnorm, fnorm; the projected velocity's discrete divergence
+ * is that residual), whether the step was replayed from the whole-step
+ * graph, bytes copied each way.  NULL or "" closes the log. */
+int lester_gpu_step_log(const char *path);
 
 /* ---- halo exchange ---------------------------------------------------- */
 /* code/swap_sc0.F:6 swap_sc(ivar1, igrid, var, work, mg_or_sg) */

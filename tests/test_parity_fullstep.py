@@ -291,3 +291,28 @@ def test_step_graph_recaptures_on_new_fields_and_controls(gpulib):
     assert not info["failed"] and info["replays"] == 5, info
     for f in S.STATE:
         assert np.array_equal(got[f], plain[f]), f
+
+
+def test_step_log_lines(tmp_path, gpulib):
+    """lester_gpu_step_log: one JSON line per step with the solve's cycles,
+    residual norms, the replay flag and the bytes copied; closing the log
+    stops the lines."""
+    import json
+    st, ctrl, s = make("box_wall", psolve=L.PSOLVE_MIXED, rtol=1e-9, exact=0, phys32=1, step_graph=1)
+    log = tmp_path / "steps.jsonl"
+    g = s.to("pinned")
+    L.gpu_init(st.case.geom(), ctrl)
+    try:
+        L.gpu_step_log(log)
+        rcs = [S.step(g, it) for it in (1, 2, 3)]
+        L.gpu_step_log(None)
+        S.step(g, 4)
+    finally:
+        L.gpu_finalize()
+    lines = [json.loads(x) for x in log.read_text().splitlines()]
+    assert [d["istep"] for d in lines] == [1, 2, 3] and [d["rc"] for d in lines] == rcs == [0, 0, 0]
+    assert [d["graph"] for d in lines] == [False, True, True]
+    for d in lines:
+        assert d["vcycles"] > 0 and 0 < d["relres"] <= 1e-9 and d["ms"] > 0
+        assert d["resid_rms"] == pytest.approx(d["relres"] * d["rhs_rms"], rel=1e-6)
+        assert d["h2d_bytes"] > 0 and d["d2h_bytes"] > 0
