@@ -49,15 +49,18 @@ EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per launch
-# of the timed kernels on the mixing-layer workload, from one capture each:
-# the level-1 k_rb<float> half sweep (52.0 MB read + 0.27 MB written,
-# against 37.7 MB algorithmic) and the scalar sweep (not captured: None)
-TRAFFIC = {"rb": 52.28e6, "sweep": None}
+# of the timed kernels on the mixing-layer workload: the level-1 k_rb<float>
+# half sweep from one capture at full size (52.0 MB read + 0.27 MB written,
+# against 37.7 MB algorithmic); the tile-pipeline scalar sweep from one
+# capture at 128x96x64 (53.1 MB read + 0.08 MB written for 0.786 M cells)
+# scaled by cells to 256x192x128
+TRAFFIC = {"rb": 52.28e6, "sweep": 53.22e6 * 6291456 / 786432}
 # algorithmic bytes per interior cell of one launch: the red-black half
 # sweep reads x and b and writes x in FP32, one colour per launch (12 / 2);
-# the scalar sweep reads sc1, hsc1, u, v, w, rho, gamsc1, gamlam and writes
-# sc1, hsc1 (10 FP64 arrays)
-ALG_BYTES = {"rb": 6.0, "sweep": 80.0}
+# the tile-pipeline scalar sweep reads the FP32 skewed copies of sc1, hsc1,
+# u, v, w, rho, gamsc1, gamlam and writes the new sc1 and hsc1 (10 FP32
+# arrays)
+ALG_BYTES = {"rb": 6.0, "sweep": 40.0}
 KERNEL_NAMES = {"rb": "k_rb<float> level-1 red-black SOR half sweep",
                 "sweep": "set_sc1 in-place scalar sweep (one launch per step)"}
 # other workloads (--workload): the plain channel of the reference's own
@@ -677,8 +680,11 @@ def report(args, rank, world):
         ach = ALG_BYTES[key] * ncell / (avg * 1e-3) / 1e9
         kern[key] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                      "traffic": TRAFFIC[key] if wl == "mixing" else None,
-                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
-                                        "on this workload" if TRAFFIC[key] and wl == "mixing" else None),
+                     "traffic_source": ({"rb": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                               "launch on this workload",
+                                        "sweep": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                                 "launch at 128x96x64, scaled by cells"}[key]
+                                        if TRAFFIC[key] and wl == "mixing" else None),
                      "peak_source": peak_src, "kernel": KERNEL_NAMES[key], "avg_launch_ms": avg,
                      "launches": n_k, "total_ms": ms_k,
                      "share_of_timed_steps": ms_k / (mx["ms_per_step"] * args.steps)}

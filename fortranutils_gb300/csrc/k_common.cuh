@@ -112,6 +112,16 @@ __device__ __forceinline__ void push_ghosts(const PushDev *__restrict__ pd, cons
     }
 }
 
+// The dense inverse of the V-cycle's bottom level (the fast solvers'
+// coarse direct solve): n interior points in block-then-interior order,
+// mt[h * n + g] = (A^-1)[g][h] (column-major, so that threads g read a
+// column coalesced); n = 0 when the bottom level is smoothed instead.
+constexpr int kDirectMax = 512;
+template <typename T> struct CoarseDirect {
+    const T *mt = nullptr;
+    int n = 0;
+};
+
 // one multigrid level of the fast solvers, for kernels that walk levels
 struct VLev {
     const BlkDev *blk;     // block table of the level (device)

@@ -126,7 +126,7 @@ __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__
 // r = b - A p in double-float (E, N, R, P as in k_resid_outer): r rounded
 // to FP32 as the next cycle's right-hand side, per-CTA partial sums of r^2
 // in FP64 (an FP32 square overflows above 1.8e19, which a diverging cycle
-// reaches).  One CTA per (j, k) row at a time, its threads along i.
+// reaches).  Grid-stride over the block's interior points, i fastest.
 __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk, const float2 *__restrict__ E,
                                                   const float2 *__restrict__ N, const float2 *__restrict__ R,
                                                   const float2 *__restrict__ P, const float2 *__restrict__ x,
@@ -134,14 +134,14 @@ __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk
                                                   double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
-    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
+    const unsigned ni = (unsigned)(b.n[0] - 2), nj = (unsigned)(b.n[1] - 2);
+    const unsigned npt = (unsigned)b.ncell;
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
     double acc = 0.;
-    for (int row = blockIdx.x; row < nj * nk; row += gridDim.x) {
-        const int k = row / nj, j = row - k * nj;
-        const long base = b.off3 + jo * (j + 1) + ko * (k + 1);  // (i = 1, j + 2, k + 2)
-        for (int i = 1 + threadIdx.x; i <= ni; i += blockDim.x) {
-            const long p = base + i;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < npt; q += gridDim.x * blockDim.x) {
+        const unsigned row = q / ni, k = row / nj;
+        {
+            const long p = b.off3 + (long)(q - row * ni + 1) + jo * (long)(row - k * nj + 1) + ko * (long)(k + 1);
             float2 r = df_add_lo(bb[p], df_neg(df_mul(P[p], x[p])));
             r = df_add_lo(r, df_mul(E[p - 1], x[p - 1]));
             r = df_add_lo(r, df_mul(E[p], x[p + 1]));
@@ -209,10 +209,8 @@ void launch_df_resid(const BlkDev *blk, int nb, long maxcell, const float2 *E, c
                      const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
                      cudaStream_t st)
 {
-    // rows of a block over a few CTAs per SM, so the final sum reads few
-    // partials (maxcell / 32 bounds the rows of any block: ni >= 32 is not
-    // assumed, only that a CTA per row is enough)
-    unsigned gx = cap_grid(maxcell, 32, (unsigned)((1216 + nb - 1) / nb));
+    // a few CTAs per SM, so that the final sum reads few partials
+    unsigned gx = cap_grid(maxcell, 256, (unsigned)((1216 + nb - 1) / nb));
     k_df_resid<<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, rT, partial);
     k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
     count_launch(2);

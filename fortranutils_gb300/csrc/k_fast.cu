@@ -228,13 +228,6 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 }
 
 // ---- red-black SOR half sweep, all blocks of a level ----------------------
-// Grid-stride over the points of one colour, kRbU points per thread and
-// iteration: the operands of all kRbU points are loaded before any is
-// updated (the points share no operand: one colour is written, the other
-// read), so each thread has kRbU points' loads in flight, and the grid is a
-// few CTAs per SM rather than one short-lived thread per point.
-constexpr int kRbU = 4;
-
 template <typename T>
 __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
@@ -243,44 +236,9 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
                                             const PushDev *__restrict__ push, MfTab<T> mf)
 {
     const BlkDev b = blk[blockIdx.y];
-    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    const unsigned stride = gridDim.x * blockDim.x;
-    const unsigned total = (unsigned)((b.n[0] - 1) >> 1) * (unsigned)(b.n[1] - 2) * (unsigned)(b.n[2] - 2);
-    for (unsigned q0 = blockIdx.x * blockDim.x + threadIdx.x; q0 < total; q0 += kRbU * stride) {
-        bool ok[kRbU];
-        int ii[kRbU], jj[kRbU], kk[kRbU];
-        long pp[kRbU];
-        T c[kRbU][6], dinv[kRbU], s[kRbU], xo[kRbU];
-#pragma unroll
-        for (int u = 0; u < kRbU; u++) {
-            const unsigned q = q0 + u * stride;
-            ok[u] = q >= q0 && rb_decode(b, q, color, ii[u], jj[u], kk[u]);
-            if (!ok[u]) continue;
-            const long p = b.off3 + (ii[u] - 1) + jo * (jj[u] - 1) + ko * (kk[u] - 1);
-            pp[u] = p;
-            if (mf.E2) {
-                coefs_mf(b, mf, ii[u], jj[u], kk[u], c[u], dinv[u]);
-            } else {
-                c[u][0] = E[p - 1];
-                c[u][1] = E[p];
-                c[u][2] = N[p - jo];
-                c[u][3] = N[p];
-                c[u][4] = R[p - ko];
-                c[u][5] = R[p];
-                dinv[u] = D[p];
-            }
-            s[u] = bb[p] + c[u][0] * x[p - 1] + c[u][1] * x[p + 1] + c[u][2] * x[p - jo] + c[u][3] * x[p + jo] +
-                   c[u][4] * x[p - ko] + c[u][5] * x[p + ko];
-            xo[u] = x[p];
-        }
-#pragma unroll
-        for (int u = 0; u < kRbU; u++) {
-            if (!ok[u]) continue;
-            const T xn = xo[u] + omega * (s[u] * dinv[u] - xo[u]);
-            x[pp[u]] = xn;
-            if (push) push_ghosts(push + 6 * blockIdx.y, b, ii[u], jj[u], kk[u], xn, x);
-        }
-    }
+    int i, j, k;
+    if (!rb_decode(b, blockIdx.x * blockDim.x + threadIdx.x, color, i, j, k)) return;
+    rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
 }
 
 // ---- y-line zebra relaxation ---------------------------------------------
@@ -583,6 +541,118 @@ __device__ void tail_smooth(const VLev &L, int nb, int nsweep, T omega, const T 
         }
 }
 
+// The bottom level solved exactly: b of its interior points gathered, x =
+// A^-1 b by one dense product (cd.mt, built on the host from the level's
+// couplings, ghosts folded into the columns of the points they mirror),
+// written to the interior and pushed to the ghosts as a sweep would.
+template <typename T>
+__device__ void tail_direct(const VLev &L, int nb, const CoarseDirect<T> &cd, T *x, const T *bb)
+{
+    __shared__ T sb[kDirectMax];
+    long g0 = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const BlkDev b = L.blk[bi];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            sb[g0 + q] = bb[decode_interior(b, q, i, j, k)];
+        }
+        g0 += b.ncell;
+    }
+    __syncthreads();
+    g0 = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const BlkDev b = L.blk[bi];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            const long g = g0 + q;
+            T acc = 0;
+            for (int h = 0; h < cd.n; h++) acc += cd.mt[(long)h * cd.n + g] * sb[h];
+            int i, j, k;
+            const long p = decode_interior(b, q, i, j, k);
+            x[p] = acc;
+            if (L.rb_push) push_ghosts(L.push + 6 * bi, b, i, j, k, acc, x);
+        }
+        g0 += b.ncell;
+    }
+    __syncthreads();
+    if (!L.rb_push && L.nface) {
+        for (int fi = 0; fi < L.nface; fi++) {
+            const FaceDev f = L.face[fi];
+            const long nj = f.nj - 2, n = nj * (f.nk - 2);
+            for (long q = threadIdx.x; q < n; q += blockDim.x) {
+                long kk = q / nj + 1, jj = q - (kk - 1) * nj + 1;
+                x[f.gh + f.jo * jj + f.ko * kk] = x[f.ppk + f.pjo * jj + f.pko * kk];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// The bottom level's operator for the host's dense inverse (one CTA): per
+// interior point g (the order of tail_direct) its element index, the six
+// couplings and 1/ap as the smoother forms them, and in `tag` (the level's
+// elements) g at the point and at every ghost the sweeps fill from it (-1
+// elsewhere).
+template <typename T>
+__global__ void __launch_bounds__(512) k_coarse_ops(const VLev *__restrict__ lvp, int lev, int nb, long base,
+                                                    long len, const T *__restrict__ E, const T *__restrict__ N,
+                                                    const T *__restrict__ R, const T *__restrict__ D, MfTab<T> mf,
+                                                    float *__restrict__ tag, float *__restrict__ ops,
+                                                    long *__restrict__ elem)
+{
+    const VLev L = lvp[lev];
+    for (long q = threadIdx.x; q < len; q += blockDim.x) tag[q] = -1.f;
+    __syncthreads();
+    float *tg = tag - base;  // indexed by element
+    long g0 = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const BlkDev b = L.blk[bi];
+        const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            const long p = decode_interior(b, q, i, j, k), g = g0 + q;
+            T c[6], dinv;
+            if (mf.E2) {
+                coefs_mf(b, mf, i, j, k, c, dinv);
+            } else {
+                c[0] = E[p - 1];
+                c[1] = E[p];
+                c[2] = N[p - jo];
+                c[3] = N[p];
+                c[4] = R[p - ko];
+                c[5] = R[p];
+                dinv = D[p];
+            }
+            for (int m = 0; m < 6; m++) ops[g * 7 + m] = (float)c[m];
+            ops[g * 7 + 6] = (float)dinv;
+            elem[g] = p;
+            tg[p] = (float)g;
+        }
+        g0 += b.ncell;
+    }
+    __syncthreads();
+    g0 = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const BlkDev b = L.blk[bi];
+        for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
+            int i, j, k;
+            decode_interior(b, q, i, j, k);
+            if (L.rb_push) push_ghosts(L.push + 6 * bi, b, i, j, k, (float)(g0 + q), tg);
+        }
+        g0 += b.ncell;
+    }
+    __syncthreads();
+    if (!L.rb_push)
+        for (int fi = 0; fi < L.nface; fi++) {
+            const FaceDev f = L.face[fi];
+            const long nj = f.nj - 2, n = nj * (f.nk - 2);
+            for (long q = threadIdx.x; q < n; q += blockDim.x) {
+                long kk = q / nj + 1, jj = q - (kk - 1) * nj + 1;
+                tg[f.gh + f.jo * jj + f.ko * kk] = tg[f.ppk + f.pjo * jj + f.pko * kk];
+            }
+            __syncthreads();
+        }
+}
+
 // With `span` > 0 the tail's slice of the multigrid arrays (levels l0..L,
 // elements [start, start + span)) is first copied into shared memory --
 // x and b, and E, N, R, D unless the couplings are matrix-free -- and the
@@ -595,7 +665,7 @@ __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int 
                                                 const T *__restrict__ E, const T *__restrict__ N,
                                                 const T *__restrict__ R, const T *__restrict__ D,
                                                 T *__restrict__ x, T *__restrict__ bb, MfTab<T> mf,
-                                                long start, long span)
+                                                long start, long span, CoarseDirect<T> cd)
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     T *const xg = x;
@@ -629,7 +699,10 @@ __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int 
         __syncthreads();
     }
     if (singular) remove_comp_means<T>(lv[L].blk, nb, bb);
-    tail_smooth(lv[L], nb, L == 1 ? pre : crs, omega, E, N, R, D, x, bb, mf);
+    if (cd.n > 0)
+        tail_direct(lv[L], nb, cd, x, bb);
+    else
+        tail_smooth(lv[L], nb, L == 1 ? pre : crs, omega, E, N, R, D, x, bb, mf);
     for (int lev = L - 1; lev >= l0; lev--) {
         for (int bi = 0; bi < nb; bi++) {
             const BlkDev c = lv[lev + 1].blk[bi], f = lv[lev].blk[bi];
@@ -840,48 +913,13 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 }
 
 // maxhalf = max over blocks of ((ni + 1) / 2) * nj * nk
-// the L2 persisting window (set_l2_window), applied per launch so that it
-// is kept when the launch is captured into a graph
-static cudaAccessPolicyWindow g_l2win = {};
-
-void set_l2_window(void *base, size_t bytes, float hit_ratio)
-{
-    g_l2win.base_ptr = base;
-    g_l2win.num_bytes = bytes;
-    g_l2win.hitRatio = hit_ratio;
-    g_l2win.hitProp = cudaAccessPropertyPersisting;
-    g_l2win.missProp = cudaAccessPropertyStreaming;
-}
-
-template <typename... KArgs, typename... Args>
-static void launch_l2(void (*kern)(KArgs...), dim3 grid, int threads, cudaStream_t st, Args... args)
-{
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = dim3(threads);
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    if (g_l2win.num_bytes) {
-        at[0].id = cudaLaunchAttributeAccessPolicyWindow;
-        at[0].val.accessPolicyWindow = g_l2win;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-    }
-    cudaLaunchKernelEx(&cfg, kern, args...);
-}
-
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
                const MfTab<T> &mf, int threads, cudaStream_t st)
 {
     const int t = (threads == 128 || threads == 512) ? threads : 256;
-    // enough threads for kRbU points each, at most about 16 CTA-slots of
-    // 128 threads per SM over all blocks
-    unsigned gx = nb_(maxhalf, t * kRbU);
-    const unsigned cap = (unsigned)std::max(1, (152 * 16 * 128 / t + nb - 1) / nb);
-    if (gx > cap) gx = cap;
-    launch_l2(k_rb<T>, dim3(gx, nb), t, st, blk, color, (T)omega, E, N, R, D, x, b, push, mf);
+    k_rb<T><<<dim3(nb_(maxhalf, t), nb), t, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
     count_launch(1);
 }
 
@@ -898,7 +936,7 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxc
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
                            const MfTab<T> &mf, cudaStream_t st)
 {
-    launch_l2(k_resid_restrict<T>, dim3(nb_(maxcell_c, 256), nb), 256, st, bc, bf, E, N, R, D, x, b, bcoarse, mf);
+    k_resid_restrict<T><<<dim3(nb_(maxcell_c, 256), nb), 256, 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf);
     count_launch(1);
 }
 
@@ -906,7 +944,7 @@ template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
                          T *xf, const PushDev *push, cudaStream_t st)
 {
-    launch_l2(k_prolong<T>, dim3(nb_(maxcell_f, 256), nb), 256, st, bc, bf, xc, xf, push);
+    k_prolong<T><<<dim3(nb_(maxcell_f, 256), nb), 256, 0, st>>>(bc, bf, xc, xf, push);
     count_launch(1);
 }
 
@@ -1040,17 +1078,25 @@ void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int m
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
-                  long start, long span, cudaStream_t st)
+                  long start, long span, const CoarseDirect<T> &cd, cudaStream_t st)
 {
     // the slice in shared memory where it fits (kVtailSmem, the limit
     // prepare_vtail set)
     const size_t smem = span > 0 ? (size_t)span * (mf.E2 ? 2 : 6) * sizeof(T) : 0;
     if (smem == 0 || smem > kVtailSmem) {
-        k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, 0, 0);
+        k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, 0, 0, cd);
     } else {
         k_vtail<T><<<1, 512, smem, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, start,
-                                         span);
+                                         span, cd);
     }
+    count_launch(1);
+}
+
+template <typename T>
+void launch_coarse_ops(const VLev *lv, int lev, int nb, long base, long len, const T *E, const T *N, const T *R,
+                       const T *D, const MfTab<T> &mf, float *tag, float *ops, long *elem, cudaStream_t st)
+{
+    k_coarse_ops<T><<<1, 512, 0, st>>>(lv, lev, nb, base, len, E, N, R, D, mf, tag, ops, elem);
     count_launch(1);
 }
 
@@ -1082,7 +1128,10 @@ bool prepare_vtail()
                                            T *, const MfTab<T> &, cudaStream_t);                  \
     template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
-                                  long, long, cudaStream_t);                                      \
+                                  long, long, const CoarseDirect<T> &, cudaStream_t);             \
+    template void launch_coarse_ops<T>(const VLev *, int, int, long, long, const T *, const T *,  \
+                                       const T *, const T *, const MfTab<T> &, float *, float *,  \
+                                       long *, cudaStream_t);                                     \
     template void launch_mf_tables<T>(const BlkDev *, int, long, long, int, const T *, const T *, \
                                       const T *, const T *, const MfTab<T> &, double, int *,      \
                                       cudaStream_t);                                              \

@@ -41,9 +41,6 @@ void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dt
                     const double *dg, const double *rp, const double *dkw, double *u,
                     const double *u_int, const double *rho, const double *p, bool f32, cudaStream_t st);
 void launch_swap_rhos(double *rho, const double *rhonp1, double *rhonm1, long n, cudaStream_t st);
-// L2 persisting window of the fast solvers' smoother, restriction and
-// prolongation launches (k_fast.cu): bytes 0 removes it
-void set_l2_window(void *base, size_t bytes, float hit_ratio);
 // double-float outer iteration of the mixed solver (k_dfloat.cu)
 void launch_df_split(const double *src, float2 *dst, long n, cudaStream_t st);
 void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b, const double *shift, float2 *dst,
@@ -96,7 +93,11 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxc
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
-                  long start, long span, cudaStream_t st);
+                  long start, long span, const CoarseDirect<T> &cd, cudaStream_t st);
+// the bottom level's couplings, point elements and ghost sources (k_coarse_ops)
+template <typename T>
+void launch_coarse_ops(const VLev *lv, int lev, int nb, long base, long len, const T *E, const T *N, const T *R,
+                       const T *D, const MfTab<T> &mf, float *tag, float *ops, long *elem, cudaStream_t st);
 // shared memory the coarse tail may use for its slice of the multigrid arrays
 constexpr size_t kVtailSmem = 200 * 1024;
 bool prepare_vtail();

@@ -54,6 +54,7 @@ struct CycleGraph {
     int krylov = 0;
     int threads = 0;                // red-black CTA size
     int line = 0;                   // y-line relaxation
+    int direct = 0;                 // points of the bottom level's direct solve (0: smoothed)
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };
@@ -64,6 +65,9 @@ template <typename T> struct FastSet {
     T *cp = nullptr, *dp = nullptr;  // y-line Thomas scratch (all levels), at first use
     MfTab<T> tab;       // separable factors (FP32 solver)
     bool mf = false;    // tab checked against every coefficient: used
+    T *cmt = nullptr;   // dense inverse of the bottom level (CoarseDirect), kDirectMax^2
+    int cn = 0;         // its points (0: the bottom level is smoothed)
+    int clev = 0;       // its level
 };
 
 struct Ctx {
@@ -93,7 +97,6 @@ struct Ctx {
     // the mixed solver's outer iteration in double-float (k_dfloat.cu): the
     // level-1 coefficients, p and b - shift as FP32 pairs
     std::FILE *step_log = nullptr;  // lester_gpu_step_log's file (one JSON line per lester_step)
-    bool l2_window = false;  // the smoother's L2 persisting window is set (alloc_fast)
     float2 *df_E = nullptr, *df_N = nullptr, *df_R = nullptr, *df_P = nullptr, *df_p = nullptr, *df_b = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
     // convective outflow / fixed inflow sides (lester_outflow.cu)

@@ -578,11 +578,8 @@ static void free_ctx(Ctx *c)
     cudaFree(c->d_metbuf);
     cudaFree(c->d_flag);
     // (f32.b and f64.b lie in the allocations of f32.x and f64.x)
-    if (c->l2_window) {
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-        set_l2_window(nullptr, 0, 0.f);
-    }
+    cudaFree(c->f32.cmt);
+    cudaFree(c->f64.cmt);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.cp, c->f32.dp,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.cp, c->f64.dp,
                   c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
@@ -796,8 +793,7 @@ template <typename T> static int alloc_fast(Ctx &c)
     if (F.E) return 0;
     size_t nb = sizeof(T) * (size_t)c.tot3;
     T **arr[5] = {&F.E, &F.N, &F.R, &F.D, &F.x};
-    // x and b in one allocation (x, then b at a 256-byte boundary): the
-    // level-1 part of both is one address range for the L2 window below
+    // x and b in one allocation (x, then b at a 256-byte boundary)
     const long xspan = (c.tot3 + 63) / 64 * 64;
     for (T **a : arr) {
         const size_t bytes = a == &F.x ? sizeof(T) * (size_t)(xspan + c.tot3) : nb;
@@ -808,26 +804,6 @@ template <typename T> static int alloc_fast(Ctx &c)
         LES_CUDA(cudaMemset(*a, 0, bytes));
     }
     F.b = F.x + xspan;
-    // The mixed solver's smoother re-reads x and b of level 1 from DRAM at
-    // every half sweep (they are not kept in L2 between launches): its
-    // launches mark them persisting in L2 (a per-launch access-policy
-    // window over x .. b's level 1, within the context's persisting
-    // set-aside, released at finalize).
-    if (sizeof(T) == 4 && !c.l2_window) {
-        int maxp = 0, maxw = 0, dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&maxp, cudaDevAttrMaxPersistingL2CacheSize, dev);
-        cudaDeviceGetAttribute(&maxw, cudaDevAttrMaxAccessPolicyWindowSize, dev);
-        const size_t span = sizeof(T) * (size_t)(xspan + c.tot_sg3);
-        if (maxp > 0 && maxw > 0 && span <= (size_t)maxw &&
-            cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min((size_t)maxp, span)) == cudaSuccess) {
-            size_t got = 0;
-            cudaDeviceGetLimit(&got, cudaLimitPersistingL2CacheSize);
-            set_l2_window(F.x, span, got >= span ? 1.0f : (float)got / (float)span);
-            c.l2_window = true;
-        }
-        cudaGetLastError();
-    }
     if (!c.E64) {
         size_t n1 = sizeof(double) * (size_t)c.tot_sg3;
         double **a64[4] = {&c.E64, &c.N64, &c.R64, &c.P64};
@@ -839,6 +815,129 @@ template <typename T> static int alloc_fast(Ctx &c)
             LES_CUDA(cudaMemset(*a, 0, n1));
         }
     }
+    return 0;
+}
+
+// The bottom of the V-cycle solved exactly: the finest level with at most
+// kDirectMax interior points gets a dense inverse of its operator as the
+// smoother sees it (couplings and 1/ap from k_coarse_ops, each ghost's
+// coupling folded onto the point that fills it), built here in FP64 by
+// Gauss-Jordan elimination with partial pivoting.  A singular operator (no
+// Dirichlet side) gets alpha 1 1^T added per connected component: for a
+// right-hand side of zero mean per component, which the cycle provides, the
+// result is the solution of zero mean.  Replaces the bottom level's
+// smoothing sweeps (20 red-black sweeps, two block-wide barriers each) by
+// one product.  Not built (cn = 0) where the level is not reached by the
+// single-CTA tail or the elimination breaks down.
+template <typename T> static int build_direct(Ctx &c, const MfTab<T> &mf)
+{
+    FastSet<T> &F = fset<T>(c);
+    F.cn = 0;
+    const int nb = c.g.numbl;
+    int Le = 0;
+    long n = 0;
+    for (int lev = 2; lev <= c.nummgl && !Le; lev++) {
+        long m = 0;
+        for (int b = 1; b <= nb; b++)
+            m += (long)(c.lv[lev].n[b][0] - 2) * (c.lv[lev].n[b][1] - 2) * (c.lv[lev].n[b][2] - 2);
+        if (m <= kDirectMax) {
+            Le = lev;
+            n = m;
+        }
+    }
+    if (!Le || !c.d_vlev || n <= 0) return 0;
+    const LevelGeom &L = c.lv[Le];
+    const long base = L.start3, len = L.len3;
+    float *d_tag = nullptr, *d_ops = nullptr;
+    long *d_elem = nullptr;
+    if (cudaMalloc(&d_tag, sizeof(float) * len) != cudaSuccess || cudaMalloc(&d_ops, sizeof(float) * 7 * n) != cudaSuccess ||
+        cudaMalloc(&d_elem, sizeof(long) * n) != cudaSuccess) {
+        cudaFree(d_tag);
+        cudaFree(d_ops);
+        cudaGetLastError();
+        return set_err(LES_ERR_NOMEM, "coarse direct solve: scratch");
+    }
+    launch_coarse_ops<T>(c.d_vlev, Le, nb, base, len, F.E, F.N, F.R, F.D, mf, d_tag, d_ops, d_elem, c.stream);
+    std::vector<float> tag(len), ops(7 * n);
+    std::vector<long> elem(n);
+    std::vector<BlkDev> hb(nb);
+    cudaMemcpyAsync(tag.data(), d_tag, sizeof(float) * len, cudaMemcpyDeviceToHost, c.stream);
+    cudaMemcpyAsync(ops.data(), d_ops, sizeof(float) * 7 * n, cudaMemcpyDeviceToHost, c.stream);
+    cudaMemcpyAsync(elem.data(), d_elem, sizeof(long) * n, cudaMemcpyDeviceToHost, c.stream);
+    cudaMemcpyAsync(hb.data(), L.d_blk, sizeof(BlkDev) * nb, cudaMemcpyDeviceToHost, c.stream);
+    const cudaError_t e = cudaStreamSynchronize(c.stream);
+    cudaFree(d_tag);
+    cudaFree(d_ops);
+    cudaFree(d_elem);
+    if (e != cudaSuccess) return set_err(LES_ERR_CUDA, "coarse direct solve: %s", cudaGetErrorString(e));
+    std::vector<double> A((size_t)n * n, 0.0);
+    std::vector<int> comp(n);
+    double diag = 0.;
+    long g = 0;
+    for (int bi = 0; bi < nb; bi++) {
+        const long jo = hb[bi].n[0], ko = jo * hb[bi].n[1];
+        for (long q = 0; q < hb[bi].ncell; q++, g++) {
+            const long p = elem[g];
+            const double ap = 1.0 / (double)ops[7 * g + 6];
+            A[g * n + g] += ap;
+            diag += ap;
+            comp[g] = hb[bi].comp;
+            const long nbr[6] = {p - 1, p + 1, p - jo, p + jo, p - ko, p + ko};
+            for (int m = 0; m < 6; m++) {
+                const double cm = ops[7 * g + m];
+                const long el = nbr[m] - base;
+                if (cm == 0. || el < 0 || el >= len || tag[el] < 0.f) continue;  // a fixed (zero) ghost
+                A[g * n + (long)tag[el]] -= cm;
+            }
+        }
+    }
+    if (c.singular) {
+        const double alpha = diag / (double)n;
+        for (long a = 0; a < n; a++)
+            for (long b = 0; b < n; b++)
+                if (comp[a] == comp[b]) A[a * n + b] += alpha;
+    }
+    // Gauss-Jordan on [A | I]
+    std::vector<double> I((size_t)n * n, 0.0);
+    for (long a = 0; a < n; a++) I[a * n + a] = 1.0;
+    double amax = 0.;
+    for (double v : A) amax = std::max(amax, std::fabs(v));
+    for (long col = 0; col < n; col++) {
+        long piv = col;
+        for (long r = col + 1; r < n; r++)
+            if (std::fabs(A[r * n + col]) > std::fabs(A[piv * n + col])) piv = r;
+        if (!(std::fabs(A[piv * n + col]) > 1e-12 * amax)) return 0;  // breaks down: keep the sweeps
+        if (piv != col)
+            for (long k = 0; k < n; k++) {
+                std::swap(A[piv * n + k], A[col * n + k]);
+                std::swap(I[piv * n + k], I[col * n + k]);
+            }
+        const double inv = 1.0 / A[col * n + col];
+        for (long k = 0; k < n; k++) {
+            A[col * n + k] *= inv;
+            I[col * n + k] *= inv;
+        }
+        for (long r = 0; r < n; r++) {
+            if (r == col) continue;
+            const double f = A[r * n + col];
+            if (f == 0.) continue;
+            for (long k = 0; k < n; k++) {
+                A[r * n + k] -= f * A[col * n + k];
+                I[r * n + k] -= f * I[col * n + k];
+            }
+        }
+    }
+    std::vector<T> mt((size_t)n * n);
+    for (long a = 0; a < n; a++)
+        for (long b = 0; b < n; b++) mt[b * n + a] = (T)I[a * n + b];
+    if (!F.cmt && cudaMalloc(&F.cmt, sizeof(T) * kDirectMax * kDirectMax) != cudaSuccess) {
+        cudaGetLastError();
+        F.cmt = nullptr;
+        return set_err(LES_ERR_NOMEM, "coarse direct solve: matrix");
+    }
+    LES_CUDA(cudaMemcpy(F.cmt, mt.data(), sizeof(T) * n * n, cudaMemcpyHostToDevice));
+    F.cn = (int)n;
+    F.clev = Le;
     return 0;
 }
 
@@ -902,6 +1001,7 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
         LES_CUDA(cudaStreamSynchronize(c.stream));
         F.mf = (mbad == 0);
     }
+    if ((r = build_direct<T>(c, F.mf ? F.tab : MfTab<T>()))) return r;
     // mixed solver: double-float copies of the level-1 FP64 coefficients
     if (sizeof(T) == 4) {
         if ((r = alloc_df(c))) return r;
@@ -991,6 +1091,16 @@ template <typename T> static void fast_vcycle(Ctx &c)
 {
     FastSet<T> &F = fset<T>(c);
     int L = c.nummgl;
+    // the bottom solved exactly inside the tail (build_direct)
+    CoarseDirect<T> cd;
+    {
+        const int l0 = tail_level(c);
+        if (F.cn > 0 && l0 && l0 <= F.clev) {
+            L = F.clev;
+            cd.mt = F.cmt;
+            cd.n = F.cn;
+        }
+    }
     int pre = c.c.rb_sweeps > 0 ? c.c.rb_sweeps : 1;
     int crs = c.c.rb_coarse > 0 ? c.c.rb_coarse : 20;
     // the coarsest level needs O(n) SOR sweeps for its n points per axis:
@@ -1012,7 +1122,7 @@ template <typename T> static void fast_vcycle(Ctx &c)
         // levels l0..L are one contiguous slice of the multigrid arrays
         const long start = c.lv[l0].start3, span = c.vtail_smem ? c.lv[L].start3 + c.lv[L].len3 - start : 0;
         launch_vtail<T>(c.d_vlev, l0, L, c.g.numbl, pre, crs, c.c.rb_omega, c.singular ? 1 : 0, F.E, F.N,
-                        F.R, F.D, F.x, F.b, mf, start, span, c.stream);
+                        F.R, F.D, F.x, F.b, mf, start, span, cd, c.stream);
     } else {
         if (c.singular) launch_coarse_mean<T>(c.lv[L].d_blk, c.g.numbl, F.b, c.stream);
         fast_smooth<T>(c, L, L == 1 ? pre : crs);
@@ -1063,7 +1173,8 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     const lester_ctrl &k = c.c;
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
-        G.krylov == (kry ? 1 : df ? 2 : 0) && G.threads == c.rb_threads && G.line == k.rb_line)
+        G.krylov == (kry ? 1 : df ? 2 : 0) && G.threads == c.rb_threads && G.line == k.rb_line &&
+        G.direct == fset<T>(c).cn)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -1115,6 +1226,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.mf = fset<T>(c).mf;
     G.tail = k.mg_tail;
     G.krylov = kry ? 1 : df ? 2 : 0;
+    G.direct = fset<T>(c).cn;
     G.threads = c.rb_threads;
     G.line = k.rb_line;
     return 0;
