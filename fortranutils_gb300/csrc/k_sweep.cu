@@ -506,12 +506,19 @@ __global__ void __launch_bounds__(kSweepThreads + 32) k_sc1_tiles(SweepArgs<S> A
             else
                 dfdzrrf = QZ(at(GR_P2, 0, t, j) - sr, dkp_0, rdkp_0);
 #undef QZ
-            const R rwst = (uwf >= zero) ? (dfdxwwf + small) / (dfdxwf + small) : (dfdxef + small) / (dfdxwf + small);
-            const R rest = (uef > zero) ? (dfdxwf + small) / (dfdxef + small) : (dfdxeef + small) / (dfdxef + small);
-            const R rsth = (vsf >= zero) ? (dfdyssf + small) / (dfdysf + small) : (dfdynf + small) / (dfdysf + small);
-            const R rnth = (vnf > zero) ? (dfdysf + small) / (dfdynf + small) : (dfdynnf + small) / (dfdynf + small);
-            const R rlft = (wlf >= zero) ? (dfdzllf + small) / (dfdzlf + small) : (dfdzrf + small) / (dfdzlf + small);
-            const R rrht = (wrf > zero) ? (dfdzlf + small) / (dfdzrf + small) : (dfdzrrf + small) / (dfdzrf + small);
+            // the limiters' slope ratios: an FP32 build divides with
+            // __fdividef (2 ulp; the ratio only enters min(4 r, 1)), the
+            // FP64 builds as the reference does
+            auto ratio = [](R a, R b) -> R {
+                if constexpr (sizeof(R) == 4 && FAST) return __fdividef(a, b);
+                else return a / b;
+            };
+            const R rwst = (uwf >= zero) ? ratio(dfdxwwf + small, dfdxwf + small) : ratio(dfdxef + small, dfdxwf + small);
+            const R rest = (uef > zero) ? ratio(dfdxwf + small, dfdxef + small) : ratio(dfdxeef + small, dfdxef + small);
+            const R rsth = (vsf >= zero) ? ratio(dfdyssf + small, dfdysf + small) : ratio(dfdynf + small, dfdysf + small);
+            const R rnth = (vnf > zero) ? ratio(dfdysf + small, dfdynf + small) : ratio(dfdynnf + small, dfdynf + small);
+            const R rlft = (wlf >= zero) ? ratio(dfdzllf + small, dfdzlf + small) : ratio(dfdzrf + small, dfdzlf + small);
+            const R rrht = (wrf > zero) ? ratio(dfdzlf + small, dfdzrf + small) : ratio(dfdzrrf + small, dfdzrf + small);
             const R limw = fmax(zero, fmin(lambda * rwst, one));
             const R lime = fmax(zero, fmin(lambda * rest, one));
             const R lims = fmax(zero, fmin(lambda * rsth, one));

@@ -192,6 +192,17 @@ struct Ctx {
     long tabcap = 0, tab_next = 0;
     float *d_pool32 = nullptr;      // FP32 copies of the tables (phys32), reset per call
     long cap32 = 0, next32 = 0;
+    // lester_step's three predictor calls share their FP32 copies of the
+    // caller's arrays (none of them changes between the calls): while
+    // f32_scope is set the pool is not rewound and a copy is reused for the
+    // same array and length (not for the per-call tables of d_tabpool)
+    bool f32_scope = false;
+    struct F32Copy {
+        const double *src;
+        long len;
+        float *dst;
+    };
+    std::vector<F32Copy> f32_cache;
     cudaEvent_t ev_solve[2] = {nullptr, nullptr};
     // whole-step graph (ctrl.step_graph, lester_step.cu)
     struct StepGraph {

@@ -2253,8 +2253,10 @@ int lester_subgrid(double *gam, double *gamsc1, const double *u, const double *v
                                        &F.r_dip, &F.r_djp, &F.r_rp};
         const double **const t2b[1] = {&F.delta2d};
         const double **const t1[5] = {&m[4], &m[5], &F.r_dkp, &F.r_dkw, &F.delta1d};
+        // the fields each point reads at ~19 neighbours, as FP32 copies
+        const double **const t3[4] = {&du, &dv, &dw, &dsc};
         if ((r = phys32_tables(c, 12, t2, c.tot2)) || (r = phys32_tables(c, 1, t2b, c.tot2)) ||
-            (r = phys32_tables(c, 5, t1, c.tot1k)))
+            (r = phys32_tables(c, 5, t1, c.tot1k)) || (r = phys32_tables(c, 4, t3, c.tot_sg3)))
             return r;
     }
     LES_PHYS(c, launch_subgrid)(L.d_blk, c.g.numbl, L.maxcell, c.c.model, c.c.csles, c.g.gotrad, c.c.alpha, dg,

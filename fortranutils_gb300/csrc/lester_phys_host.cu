@@ -388,12 +388,25 @@ namespace les {
 
 void tab_reset(Ctx &c) { c.tab_next = 0; }
 
-void phys32_reset(Ctx &c) { c.next32 = 0; }
+void phys32_reset(Ctx &c)
+{
+    // in a scope the pool keeps its copies while one entry point's worth of
+    // room is left (the predictor's: 28 + 8 2-D tables, 4 1-D, 7 fields);
+    // otherwise it starts again and forgets them
+    const long reserve = 40 * c.tot2 + 8 * c.tot1k + 7 * (c.tot_sg3 + 4) + 64;
+    if (!c.f32_scope || c.cap32 - c.next32 < reserve) {
+        c.next32 = 0;
+        c.f32_cache.clear();
+    }
+}
 
 int phys32_tables(Ctx &c, int n, const double **const *pp, long len)
 {
     if (!c.d_pool32) {
-        const long cap = 48 * c.tot2 + 24 * c.tot1k + 7 * (c.tot_sg3 + 4) + 256;
+        // room for the three predictor calls of one step (f32_scope): the
+        // metric tables they read, their per-call reciprocal tables, the
+        // seven fields once
+        const long cap = 96 * c.tot2 + 48 * c.tot1k + 7 * (c.tot_sg3 + 4) + 256;
         if (cudaMalloc(&c.d_pool32, sizeof(float) * cap) != cudaSuccess) {
             cudaGetLastError();
             return set_err(LES_ERR_NOMEM, "FP32 physics tables: %ld floats", cap);
@@ -407,6 +420,19 @@ int phys32_tables(Ctx &c, int n, const double **const *pp, long len)
     for (int t = 0; t < n; t++) {
         const double *q = *pp[t];
         if (!q || ((unsigned long long)q & 1ull)) continue;  // absent, or already a copy
+        // tables made per call (the reciprocal and delta tables of the
+        // fast builds) reuse their pool from call to call with other
+        // contents: never taken from, or put in, the cache
+        const bool pooled = c.d_tabpool && q >= c.d_tabpool && q < c.d_tabpool + c.tabcap;
+        if (c.f32_scope && !pooled) {
+            const float *hit = nullptr;
+            for (const Ctx::F32Copy &e : c.f32_cache)
+                if (e.src == q && e.len == len) hit = e.dst;
+            if (hit) {
+                *pp[t] = (const double *)((unsigned long long)hit | 1ull);
+                continue;
+            }
+        }
         const long step = (len + 3) & ~3L;                   // 16-byte aligned copies
         if (c.next32 + step > c.cap32) return set_err(LES_ERR_SIZE, "FP32 physics tables exhausted");
         float *d = c.d_pool32 + c.next32;
@@ -414,6 +440,7 @@ int phys32_tables(Ctx &c, int n, const double **const *pp, long len)
         src[m] = q;
         dst[m] = d;
         m++;
+        if (c.f32_scope && !pooled) c.f32_cache.push_back({q, len, d});
         *pp[t] = (const double *)((unsigned long long)d | 1ull);
     }
     if (m) launch_to_f32(src, dst, m, len, c.stream);

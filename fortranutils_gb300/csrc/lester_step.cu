@@ -134,6 +134,24 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
                                m[M_DIU], m[M_DIV], m[M_DIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RU],
                                m[M_RV], D.dkp, D.dkw));
     }
+    // the eddy viscosity and the three predictors convert the same fields
+    // (u, v, w, and p, rho, rhonp1, gam) and tables to FP32 once: none of
+    // them changes from the eddy viscosity to the last predictor
+    struct F32Scope {
+        Ctx &c;
+        explicit F32Scope(Ctx &cc) : c(cc)
+        {
+            c.next32 = 0;
+            c.f32_cache.clear();
+            c.f32_scope = true;
+        }
+        ~F32Scope()
+        {
+            c.f32_scope = false;
+            c.f32_cache.clear();
+        }
+    };
+    F32Scope f32s(c);
     RET(need({D.sc1, D.sc1var, D.gamsc1, D.sc1dis}));
     RET(lester_subgrid(D.gam, D.gamsc1, D.u, D.v, D.w, D.sc1, D.rho, D.sc1var, D.sc1dis, D.vd_damping, m[M_DIP],
                        m[M_DIU], m[M_DJP], m[M_DJV], D.dkp, D.dkw, m[M_HIJP], m[M_HJIP], m[M_HKIP], m[M_HKJP],
@@ -160,32 +178,34 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
     RET(put({D.rhonp1}));
     if (c.xfer) RET(c.xfer->put_as(D.rhonp1, D.rho));
     RET(need({D.hn_u}));
-    RET(lester_set_uv_int(&iU, D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.u_int, D.hn_u, m[M_DIP], m[M_DIU],
-                          m[M_DIX], m[M_RDIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RDJP], m[M_RDJU],
-                          m[M_DIDJP], m[M_DIDJU], m[M_RDIDJU], m[M_HIJP], m[M_HIJU], m[M_HJIU], m[M_HKIU],
-                          m[M_HKJU], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[0], tw[1], tw[2], tw[3], nullptr,
-                          nullptr));
-    RET(exitbc(1, 1));
-    RET(need({D.hn_v}));
-    // ---- ivar = v (step.F:319-326: the v arrays in the u roles)
-    RET(lester_set_uv_int(&iV, D.v, D.u, D.w, D.p, D.rho, D.rhonp1, D.gam, D.v_int, D.hn_v, m[M_DJP], m[M_DJV],
-                          m[M_DJX], m[M_RDJX], m[M_DIP], m[M_DIV], m[M_DIU], m[M_DIX], m[M_RDIP], m[M_RDIV],
-                          m[M_DIDJP], m[M_DJDIV], m[M_RDJDIV], m[M_HJIP], m[M_HJIV], m[M_HIJV], m[M_HKJV],
-                          m[M_HKIV], m[M_RP], m[M_RV], D.dkp, D.dkw, tw[4], tw[5], tw[6], tw[7], nullptr,
-                          nullptr));
-    RET(exitbc(1, 2));
-    RET(need({D.hn_w}));
-    // ---- ivar = w
-    RET(lester_set_w_int(D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.w_int, D.hn_w, m[M_DIP], m[M_DIU],
-                         m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
-                         m[M_HKIU], m[M_HKJV], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[10], tw[11], tw[8], tw[9],
-                         nullptr, nullptr));
-    RET(exitbc(1, 3));
-    // the wall arrays (set_virt_bc, then the predictors) are final; the
-    // predictors' right-hand sides too unless an outflow side updates them
-    // after the projection (conv_exitbc task 2)
-    for (int q = 0; q < 12; q++) RET(put({tw[q]}));
-    if (!has_convective(c)) RET(put({D.hn_u, D.hn_v, D.hn_w}));
+    {
+        RET(lester_set_uv_int(&iU, D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.u_int, D.hn_u, m[M_DIP], m[M_DIU],
+                              m[M_DIX], m[M_RDIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RDJP], m[M_RDJU],
+                              m[M_DIDJP], m[M_DIDJU], m[M_RDIDJU], m[M_HIJP], m[M_HIJU], m[M_HJIU], m[M_HKIU],
+                              m[M_HKJU], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[0], tw[1], tw[2], tw[3], nullptr,
+                              nullptr));
+        RET(exitbc(1, 1));
+        RET(need({D.hn_v}));
+        // ---- ivar = v (step.F:319-326: the v arrays in the u roles)
+        RET(lester_set_uv_int(&iV, D.v, D.u, D.w, D.p, D.rho, D.rhonp1, D.gam, D.v_int, D.hn_v, m[M_DJP], m[M_DJV],
+                              m[M_DJX], m[M_RDJX], m[M_DIP], m[M_DIV], m[M_DIU], m[M_DIX], m[M_RDIP], m[M_RDIV],
+                              m[M_DIDJP], m[M_DJDIV], m[M_RDJDIV], m[M_HJIP], m[M_HJIV], m[M_HIJV], m[M_HKJV],
+                              m[M_HKIV], m[M_RP], m[M_RV], D.dkp, D.dkw, tw[4], tw[5], tw[6], tw[7], nullptr,
+                              nullptr));
+        RET(exitbc(1, 2));
+        RET(need({D.hn_w}));
+        // ---- ivar = w
+        RET(lester_set_w_int(D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.w_int, D.hn_w, m[M_DIP], m[M_DIU],
+                             m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
+                             m[M_HKIU], m[M_HKJV], m[M_RP], m[M_RU], D.dkp, D.dkw, tw[10], tw[11], tw[8], tw[9],
+                             nullptr, nullptr));
+        RET(exitbc(1, 3));
+        // the wall arrays (set_virt_bc, then the predictors) are final; the
+        // predictors' right-hand sides too unless an outflow side updates them
+        // after the projection (conv_exitbc task 2)
+        for (int q = 0; q < 12; q++) RET(put({tw[q]}));
+        if (!has_convective(c)) RET(put({D.hn_u, D.hn_v, D.hn_w}));
+    }
     // ---- ivar = p
     if (*istep == 1)
         RET(lester_coeff_p(m[M_DIU], m[M_DJV], m[M_RDIV], m[M_RDJU], m[M_DIDJP], m[M_RP], D.dkp, D.dkw, D.ap, D.aw,

@@ -45,7 +45,8 @@ _METRICS = {"dip", "diu", "div", "dix", "djp", "dju", "djv", "djx", "rdip", "rdi
 # fields that particular kernels read as FP32 copies too (the host converts
 # them once per call: each is read by ~7 neighbouring points)
 _FIELDS32 = {"k_set_u_int": {"u", "v", "w", "p", "rho", "rhonp1", "gam"},
-             "k_set_w_int": {"u", "v", "w", "p", "rho", "rhonp1", "gam"}}
+             "k_set_w_int": {"u", "v", "w", "p", "rho", "rhonp1", "gam"},
+             "k_subgrid": {"u", "v", "w", "sc1"}}
 _func = ""
 
 
