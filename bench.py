@@ -63,6 +63,10 @@ TRAFFIC = {"rb": 52.28e6, "sweep": 53.22e6 * 6291456 / 786432}
 ALG_BYTES = {"rb": 6.0, "sweep": 40.0}
 KERNEL_NAMES = {"rb": "k_rb<float> level-1 red-black SOR half sweep",
                 "sweep": "set_sc1 in-place scalar sweep (one launch per step)"}
+# the level-1 smoother as shared-memory tiles (k_rb_tile, when the level
+# allows it): one launch is a full sweep, both colours (12 B per cell)
+ALG_BYTES_TILE = 12.0
+KERNEL_NAME_TILE = "k_rb_tile<float> level-1 red-black SOR sweep (both colours, shared-memory tiles)"
 # other workloads (--workload): the plain channel of the reference's own
 # CPU-runnable case, and the large stretched channel
 WORKLOADS = {
@@ -369,10 +373,11 @@ def run_gpu(args):
         tuned = L.gpu_tuned(32 if mode == "mixed" else 64)
         ms = _ranks().max(e0.elapsed_time(e1))
         kms, kl = L.gpu_prof_read(L.PROF_RB)
+        rb_tile = bool(L.gpu_rb_tiles() & 2)  # level 1 smoothed by k_rb_tile
         sms, sl = L.gpu_prof_read(L.PROF_SWEEP)
         res[mode] = {"ms_per_step": ms / args.steps, "cycles": float(np.mean(cyc)),
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
-                     "launches": L.gpu_launch_count() - launches0, "rb_ms": kms,
+                     "launches": L.gpu_launch_count() - launches0, "rb_ms": kms, "rb_tile": rb_tile,
                      "rb_launches": kl, "sweep_ms": sms, "sweep_launches": sl,
                      "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
         del g
@@ -677,15 +682,17 @@ def report(args, rank, world):
         if n_k <= 0:
             continue
         avg = ms_k / n_k
-        ach = ALG_BYTES[key] * ncell / (avg * 1e-3) / 1e9
+        tile = key == "rb" and mx.get("rb_tile")
+        ach = (ALG_BYTES_TILE if tile else ALG_BYTES[key]) * ncell / (avg * 1e-3) / 1e9
         kern[key] = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                     "traffic": TRAFFIC[key] if wl == "mixing" else None,
+                     "traffic": TRAFFIC[key] if wl == "mixing" and not tile else None,
                      "traffic_source": ({"rb": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                                "launch on this workload",
                                         "sweep": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                                  "launch at 128x96x64, scaled by cells"}[key]
-                                        if TRAFFIC[key] and wl == "mixing" else None),
-                     "peak_source": peak_src, "kernel": KERNEL_NAMES[key], "avg_launch_ms": avg,
+                                        if TRAFFIC[key] and wl == "mixing" and not tile else None),
+                     "peak_source": peak_src, "kernel": KERNEL_NAME_TILE if tile else KERNEL_NAMES[key],
+                     "avg_launch_ms": avg,
                      "launches": n_k, "total_ms": ms_k,
                      "share_of_timed_steps": ms_k / (mx["ms_per_step"] * args.steps)}
     dominant = max(kern, key=lambda k: kern[k]["total_ms"])

@@ -241,6 +241,120 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
     rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
 }
 
+// ---- red-black SOR, one full sweep per launch, shared-memory tiles --------
+// For a level of one block whose faces are periodic onto itself with even
+// extents, or walls (no coupling through them): each CTA stages a tile of
+// kTI x kTJ x kTK points of x with a two-point halo and of b with a
+// one-point halo (periodic axes wrapped, the wall sides clamped: their
+// couplings are zero), updates colour 0 on the tile and its one-point halo,
+// then colour 1 on the tile, in shared memory, and writes the tile to the
+// other buffer (with the ghosts its boundary points mirror).  The halo's
+// colour-0 values are recomputed from the same staged values the
+// neighbouring tile uses, so the sweep is the two half sweeps of k_rb, per
+// point the same operations; x is read once per sweep instead of twice and
+// one launch replaces two.
+constexpr int kTI = 32, kTJ = 16, kTK = 8;
+constexpr int kXI = kTI + 4, kXJ = kTJ + 4, kXK = kTK + 4;
+constexpr int kBI = kTI + 2, kBJ = kTJ + 2, kBK = kTK + 2;
+template <typename T> constexpr size_t kRbTileSmem = sizeof(T) * (kXK * kXJ * kXI + kBK * kBJ * kBI);
+
+// the source of unwrapped coordinate c on an axis with interior 2..n+1:
+// wrapped on a periodic axis, clamped to the ghosts 1..n+2 otherwise
+__device__ __forceinline__ int rbt_src(int c, int n, bool per)
+{
+    if (per) return c < 2 ? c + n : c > n + 1 ? c - n : c;
+    return c < 1 ? 1 : c > n + 2 ? n + 2 : c;
+}
+
+template <typename T>
+__device__ __forceinline__ void rbt_coefs(const BlkDev &b, int i, int j, int k, const T *__restrict__ E,
+                                          const T *__restrict__ N, const T *__restrict__ R,
+                                          const T *__restrict__ D, const MfTab<T> &mf, T c[6], T &dinv)
+{
+    if (mf.E2) {
+        coefs_mf(b, mf, i, j, k, c, dinv);
+        return;
+    }
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long p = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    c[0] = E[p - 1];
+    c[1] = E[p];
+    c[2] = N[p - jo];
+    c[3] = N[p];
+    c[4] = R[p - ko];
+    c[5] = R[p];
+    dinv = D[p];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rb_tile(const BlkDev *__restrict__ blk, T omega, const T *__restrict__ E,
+                                                 const T *__restrict__ N, const T *__restrict__ R,
+                                                 const T *__restrict__ D, const T *__restrict__ xin,
+                                                 T *__restrict__ xout, const T *__restrict__ bb,
+                                                 const PushDev *__restrict__ push, MfTab<T> mf)
+{
+    extern __shared__ __align__(16) unsigned char rbt_smem[];
+    T *const X = (T *)rbt_smem;
+    T *const Bs = X + kXK * kXJ * kXI;
+    const BlkDev b = blk[0];
+    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
+    const bool pi = b.bc[0] == LES_BCT_PERIODIC_D, pj = b.bc[2] == LES_BCT_PERIODIC_D,
+               pk = b.bc[4] == LES_BCT_PERIODIC_D;
+    const int ntx = (ni + kTI - 1) / kTI, nty = (nj + kTJ - 1) / kTJ;
+    const int t = blockIdx.x, tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
+    const int i0 = 2 + kTI * tx, j0 = 2 + kTJ * ty, k0 = 2 + kTK * tz;
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    auto gidx = [&](int i, int j, int k) { return b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1); };
+    for (int e = threadIdx.x; e < kXK * kXJ * kXI; e += blockDim.x) {
+        const int a = e % kXI, r = e / kXI, bq = r % kXJ, cq = r / kXJ;
+        X[e] = xin[gidx(rbt_src(i0 - 2 + a, ni, pi), rbt_src(j0 - 2 + bq, nj, pj), rbt_src(k0 - 2 + cq, nk, pk))];
+    }
+    for (int e = threadIdx.x; e < kBK * kBJ * kBI; e += blockDim.x) {
+        const int a = e % kBI, r = e / kBI, bq = r % kBJ, cq = r / kBJ;
+        Bs[e] = bb[gidx(rbt_src(i0 - 1 + a, ni, pi), rbt_src(j0 - 1 + bq, nj, pj), rbt_src(k0 - 1 + cq, nk, pk))];
+    }
+    __syncthreads();
+    constexpr int sJ = kXI, sK = kXI * kXJ;
+    // one update of the staged point at X index xe (b at Bs index be) with
+    // the couplings of the point it is, (iw, jw, kw)
+    auto update = [&](int xe, int be, int iw, int jw, int kw) {
+        T c[6], dinv;
+        rbt_coefs(b, iw, jw, kw, E, N, R, D, mf, c, dinv);
+        const T s = Bs[be] + c[0] * X[xe - 1] + c[1] * X[xe + 1] + c[2] * X[xe - sJ] + c[3] * X[xe + sJ] +
+                    c[4] * X[xe - sK] + c[5] * X[xe + sK];
+        const T xo = X[xe];
+        X[xe] = xo + omega * (s * dinv - xo);
+    };
+    // colour 0 on the tile and its one-point halo, where that is a point of
+    // the level (wrapped on periodic axes)
+    for (int e = threadIdx.x; e < kBK * kBJ * kBI; e += blockDim.x) {
+        const int a = e % kBI, r = e / kBI, bq = r % kBJ, cq = r / kBJ;
+        const int i = i0 - 1 + a, j = j0 - 1 + bq, k = k0 - 1 + cq;
+        if (((i + j + k) & 1) != 0) continue;
+        if ((!pi && (i < 2 || i > ni + 1)) || (!pj && (j < 2 || j > nj + 1)) || (!pk && (k < 2 || k > nk + 1)))
+            continue;
+        update(((cq + 1) * kXJ + bq + 1) * kXI + a + 1, e, rbt_src(i, ni, pi), rbt_src(j, nj, pj),
+               rbt_src(k, nk, pk));
+    }
+    __syncthreads();
+    // colour 1 on the tile's points of the level
+    for (int e = threadIdx.x; e < kTK * kTJ * kTI; e += blockDim.x) {
+        const int a = e % kTI, r = e / kTI, bq = r % kTJ, cq = r / kTJ;
+        const int i = i0 + a, j = j0 + bq, k = k0 + cq;
+        if (((i + j + k) & 1) != 1 || i > ni + 1 || j > nj + 1 || k > nk + 1) continue;
+        update(((cq + 2) * kXJ + bq + 2) * kXI + a + 2, ((cq + 1) * kBJ + bq + 1) * kBI + a + 1, i, j, k);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < kTK * kTJ * kTI; e += blockDim.x) {
+        const int a = e % kTI, r = e / kTI, bq = r % kTJ, cq = r / kTJ;
+        const int i = i0 + a, j = j0 + bq, k = k0 + cq;
+        if (i > ni + 1 || j > nj + 1 || k > nk + 1) continue;
+        const T v = X[((cq + 2) * kXJ + bq + 2) * kXI + a + 2];
+        xout[gidx(i, j, k)] = v;
+        if (push) push_ghosts(push, b, i, j, k, v, xout);
+    }
+}
+
 // ---- y-line zebra relaxation ---------------------------------------------
 // One thread per (i, k) column with (i + k) % 2 == color: the column's
 // tridiagonal system in j (couplings N to j -/+ 1, the i and k neighbours
@@ -923,6 +1037,28 @@ void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega,
     count_launch(1);
 }
 
+template <typename T> __global__ void k_copy_range(const T *__restrict__ src, T *__restrict__ dst, long n)
+{
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
+        dst[q] = src[q];
+}
+
+template <typename T> void launch_copy_range(const T *src, T *dst, long n, cudaStream_t st)
+{
+    unsigned g = nb_(n, 256);
+    k_copy_range<T><<<g > 2432 ? 2432 : g, 256, 0, st>>>(src, dst, n);
+    count_launch(1);
+}
+
+template <typename T>
+void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *E, const T *N, const T *R, const T *D,
+                    const T *xin, T *xout, const T *b, const PushDev *push, const MfTab<T> &mf, cudaStream_t st)
+{
+    const int ntile = ((n[0] - 2 + kTI - 1) / kTI) * ((n[1] - 2 + kTJ - 1) / kTJ) * ((n[2] - 2 + kTK - 1) / kTK);
+    k_rb_tile<T><<<ntile, 256, kRbTileSmem<T>, st>>>(blk, (T)omega, E, N, R, D, xin, xout, b, push, mf);
+    count_launch(1);
+}
+
 template <typename T>
 void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double omega, const T *E, const T *N,
                   const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, cudaStream_t st)
@@ -1113,6 +1249,17 @@ bool prepare_vtail()
     return ok;
 }
 
+// the shared-memory red-black tiles' shared memory limit, once per context
+bool prepare_rb_tile()
+{
+    const bool ok = cudaFuncSetAttribute(k_rb_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kRbTileSmem<float>) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_rb_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kRbTileSmem<double>) == cudaSuccess;
+    if (!ok) cudaGetLastError();
+    return ok;
+}
+
 #define INST(T)                                                                                    \
     template int launch_conv_coef<T>(const BlkDev *, int, long, const double *const *, T *, T *,   \
                                      T *, T *, double *, double *, double *, double *, int *,     \
@@ -1129,6 +1276,10 @@ bool prepare_vtail()
     template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
                                   long, long, const CoarseDirect<T> &, cudaStream_t);             \
+    template void launch_copy_range<T>(const T *, T *, long, cudaStream_t);                        \
+    template void launch_rb_tile<T>(const BlkDev *, const int *, double, const T *, const T *,     \
+                                    const T *, const T *, const T *, T *, const T *, const PushDev *, \
+                                    const MfTab<T> &, cudaStream_t);                              \
     template void launch_coarse_ops<T>(const VLev *, int, int, long, long, const T *, const T *,  \
                                        const T *, const T *, const MfTab<T> &, float *, float *,  \
                                        long *, cudaStream_t);                                     \

@@ -94,6 +94,13 @@ template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
                   long start, long span, const CoarseDirect<T> &cd, cudaStream_t st);
+// dst[0..n) = src[0..n) (device arrays)
+template <typename T> void launch_copy_range(const T *src, T *dst, long n, cudaStream_t st);
+// one red-black sweep (both colours) of a one-block level through shared-memory
+// tiles, xin -> xout (k_rb_tile); n: the block's points incl. ghosts
+template <typename T>
+void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *E, const T *N, const T *R, const T *D,
+                    const T *xin, T *xout, const T *b, const PushDev *push, const MfTab<T> &mf, cudaStream_t st);
 // the bottom level's couplings, point elements and ghost sources (k_coarse_ops)
 template <typename T>
 void launch_coarse_ops(const VLev *lv, int lev, int nb, long base, long len, const T *E, const T *N, const T *R,
@@ -101,6 +108,7 @@ void launch_coarse_ops(const VLev *lv, int lev, int nb, long base, long len, con
 // shared memory the coarse tail may use for its slice of the multigrid arrays
 constexpr size_t kVtailSmem = 200 * 1024;
 bool prepare_vtail();
+bool prepare_rb_tile();  // k_rb_tile's shared memory (false: not usable)
 template <typename T>
 void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const T *E,
                       const T *N, const T *R, const T *D, const MfTab<T> &t, double tol, int *bad,

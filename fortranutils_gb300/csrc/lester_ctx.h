@@ -65,6 +65,7 @@ template <typename T> struct FastSet {
     T *cp = nullptr, *dp = nullptr;  // y-line Thomas scratch (all levels), at first use
     MfTab<T> tab;       // separable factors (FP32 solver)
     bool mf = false;    // tab checked against every coefficient: used
+    T *x2 = nullptr;    // the other buffer of the shared-memory red-black sweeps (k_rb_tile)
     T *cmt = nullptr;   // dense inverse of the bottom level (CoarseDirect), kDirectMax^2
     int cn = 0;         // its points (0: the bottom level is smoothed)
     int clev = 0;       // its level
@@ -188,6 +189,8 @@ struct Ctx {
     } sw;
     VLev *d_vlev = nullptr;  // per-level descriptors (index = level) for k_vtail
     bool vtail_smem = false; // k_vtail may stage its slice in shared memory
+    bool rb_tile_ok = false; // k_rb_tile's shared memory granted
+    int rb_tile_mask = 0;    // levels (bit lev) the last cycle smoothed with k_rb_tile
     const double *fb[3] = {nullptr, nullptr, nullptr};  // body force u, v, w (device)
     long tabcap = 0, tab_next = 0;
     float *d_pool32 = nullptr;      // FP32 copies of the tables (phys32), reset per call

@@ -580,6 +580,8 @@ static void free_ctx(Ctx *c)
     // (f32.b and f64.b lie in the allocations of f32.x and f64.x)
     cudaFree(c->f32.cmt);
     cudaFree(c->f64.cmt);
+    cudaFree(c->f32.x2);
+    cudaFree(c->f64.x2);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.cp, c->f32.dp,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.cp, c->f64.dp,
                   c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
@@ -1030,10 +1032,65 @@ void prof_pair(Ctx &c, int tag, cudaEvent_t *e0, cudaEvent_t *e1)
     c.prof_launches[tag]++;
 }
 
+// Whether level lev is smoothed by k_rb_tile: one block, point red-black
+// (not y-line) relaxation, no interface face, periodic faces that push
+// (even extents), and the other buffer allocated.
+template <typename T> static bool rb_tile_level(Ctx &c, int lev)
+{
+    if (!c.rb_tile_ok || c.g.numbl != 1 || c.c.rb_line) return false;
+    const LevelGeom &L = c.lv[lev];
+    if (!L.rb_push) return false;
+    for (int s = 0; s < 6; s++) {
+        const int bc = c.g.bl_bc[0][s];
+        if (bc == LES_BCT_INTERFACE) return false;
+        // a periodic axis is periodic on both of its sides
+        if ((bc == LES_BCT_PERIODIC) != (c.g.bl_bc[0][s ^ 1] == LES_BCT_PERIODIC)) return false;
+    }
+    FastSet<T> &F = fset<T>(c);
+    if (!F.x2) {
+        if (cudaMalloc(&F.x2, sizeof(T) * (size_t)c.tot3) != cudaSuccess) {
+            cudaGetLastError();
+            F.x2 = nullptr;
+            c.rb_tile_ok = false;
+            return false;
+        }
+        cudaMemset(F.x2, 0, sizeof(T) * (size_t)c.tot3);
+    }
+    return true;
+}
+
 template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
 {
     FastSet<T> &F = fset<T>(c);
     LevelGeom &L = c.lv[lev];
+    if (rb_tile_level<T>(c, lev)) {
+        // one launch per sweep, x and x2 in turn; an odd count ends with a
+        // copy of the level back into x
+        c.rb_tile_mask |= 1 << lev;
+        bool cap = c.cap_ev && lev == 1;
+        bool prof = !c.cap_ev && c.prof && lev == 1;
+        T *in = F.x, *out = F.x2;
+        for (int s = 0; s < nsweep; s++) {
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (cap) {
+                cudaEventCreate(&e0);
+                cudaEventCreate(&e1);
+                c.cap_ev->push_back(e0);
+                c.cap_ev->push_back(e1);
+            } else if (prof) {
+                prof_pair(c, LES_PROF_RB, &e0, &e1);
+            }
+            unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
+            if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
+            launch_rb_tile<T>(L.d_blk, L.n[1], c.c.rb_omega, F.E, F.N, F.R, F.D, in, out, F.b, L.d_push,
+                              F.mf ? F.tab : MfTab<T>(), c.stream);
+            if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
+            std::swap(in, out);
+        }
+        if (in != F.x) launch_copy_range<T>(in + L.start3, F.x + L.start3, L.len3, c.stream);
+        return;
+    }
+    c.rb_tile_mask &= ~(1 << lev);
     if (c.c.rb_line && F.cp) {
         // y-line zebra relaxation; halos exchanged after each colour
         for (int s = 0; s < nsweep; s++)
@@ -1637,6 +1694,7 @@ static int ensure_scratch(Ctx &c)
     LES_CUDA(cudaMallocHost(&c.h_small, sizeof(double) * 64));
     LES_CUDA(cudaMalloc(&c.d_flag, sizeof(int) * 4));
     c.vtail_smem = prepare_vtail();
+    c.rb_tile_ok = prepare_rb_tile();
     return 0;
 }
 
@@ -1792,6 +1850,14 @@ int lester_gpu_prof_kernel(int which, double *ms_total, long *launches)
 int lester_gpu_prof_read(double *ms_total, long *launches)
 {
     return lester_gpu_prof_kernel(LES_PROF_RB, ms_total, launches);
+}
+
+int lester_gpu_rb_tiles(int *level_mask)
+{
+    LES_NEED_CTX();
+    if (!level_mask) return set_err(LES_ERR_ARG, "NULL level_mask");
+    *level_mask = g_ctx->rb_tile_mask;
+    return 0;
 }
 
 int lester_gpu_xfer_bytes(long *h2d, long *d2h)

@@ -227,6 +227,13 @@ def gpu_step_graph_info() -> dict:
     return {"replays": n.value, "handovers": h.value, "failed": bool(f.value), "why": why.value.decode()}
 
 
+def gpu_rb_tiles() -> int:
+    """Bit l set: level l was smoothed by the shared-memory red-black tiles."""
+    m = C.c_int()
+    _check(lib().lester_gpu_rb_tiles(C.byref(m)))
+    return m.value
+
+
 def gpu_step_log(path) -> None:
     """Append one JSON line per lester_step to `path` (None closes)."""
     _check(lib().lester_gpu_step_log(None if path is None else str(path).encode()))

@@ -234,6 +234,10 @@ int lester_gpu_tuned(int prec, int *done, int *threads, int *sweeps, double *ome
 #define LES_PROF_RB 0
 #define LES_PROF_SWEEP 1
 int lester_gpu_prof(int enable);
+/* levels (bit l for level l) the fast solvers' last V-cycle smoothed with
+ * one shared-memory red-black sweep per launch (k_rb_tile) instead of one
+ * launch per colour; LES_PROF_RB then times those launches */
+int lester_gpu_rb_tiles(int *level_mask);
 int lester_gpu_prof_kernel(int which, double *ms_total, long *launches);
 int lester_gpu_prof_read(double *ms_total, long *launches);
 /* bytes copied host->device and device->host by calls with host arrays */
