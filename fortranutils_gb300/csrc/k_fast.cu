@@ -256,7 +256,11 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
 constexpr int kTI = 32, kTJ = 16, kTK = 8;
 constexpr int kXI = kTI + 4, kXJ = kTJ + 4, kXK = kTK + 4;
 constexpr int kBI = kTI + 2, kBJ = kTJ + 2, kBK = kTK + 2;
-template <typename T> constexpr size_t kRbTileSmem = sizeof(T) * (kXK * kXJ * kXI + kBK * kBJ * kBI);
+// separable couplings of the tile and its one-point halo (coefs_mf's
+// operands, per (i, j) column and per k)
+constexpr int kMf2 = 5 * kBJ * kBI, kMf1 = 4 * kBK;
+template <typename T>
+constexpr size_t kRbTileSmem = sizeof(T) * (kXK * kXJ * kXI + kBK * kBJ * kBI + kMf2 + kMf1);
 
 // the source of unwrapped coordinate c on an axis with interior 2..n+1:
 // wrapped on a periodic axis, clamped to the ghosts 1..n+2 otherwise
@@ -266,36 +270,27 @@ __device__ __forceinline__ int rbt_src(int c, int n, bool per)
     return c < 1 ? 1 : c > n + 2 ? n + 2 : c;
 }
 
-template <typename T>
-__device__ __forceinline__ void rbt_coefs(const BlkDev &b, int i, int j, int k, const T *__restrict__ E,
-                                          const T *__restrict__ N, const T *__restrict__ R,
-                                          const T *__restrict__ D, const MfTab<T> &mf, T c[6], T &dinv)
+// one element, global -> shared, asynchronously (cp.async; completes at
+// the CTA's wait_group)
+template <typename T> __device__ __forceinline__ void rbt_async(T *dst, const T *src)
 {
-    if (mf.E2) {
-        coefs_mf(b, mf, i, j, k, c, dinv);
-        return;
-    }
-    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    const long p = b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
-    c[0] = E[p - 1];
-    c[1] = E[p];
-    c[2] = N[p - jo];
-    c[3] = N[p];
-    c[4] = R[p - ko];
-    c[5] = R[p];
-    dinv = D[p];
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    if (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_rb_tile(const BlkDev *__restrict__ blk, T omega, const T *__restrict__ E,
-                                                 const T *__restrict__ N, const T *__restrict__ R,
-                                                 const T *__restrict__ D, const T *__restrict__ xin,
+__global__ void __launch_bounds__(256) k_rb_tile(const BlkDev *__restrict__ blk, T omega, const T *__restrict__ xin,
                                                  T *__restrict__ xout, const T *__restrict__ bb,
                                                  const PushDev *__restrict__ push, MfTab<T> mf)
 {
     extern __shared__ __align__(16) unsigned char rbt_smem[];
     T *const X = (T *)rbt_smem;
     T *const Bs = X + kXK * kXJ * kXI;
+    T *const M2 = Bs + kBK * kBJ * kBI;  // [5][kBJ][kBI]: E2 west, E2, N2 south, N2, R2
+    T *const M1 = M2 + kMf2;             // [4][kBK]: Ez, Nz, Rz below, Rz
     const BlkDev b = blk[0];
     const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
     const bool pi = b.bc[0] == LES_BCT_PERIODIC_D, pj = b.bc[2] == LES_BCT_PERIODIC_D,
@@ -304,53 +299,92 @@ __global__ void __launch_bounds__(256) k_rb_tile(const BlkDev *__restrict__ blk,
     const int t = blockIdx.x, tx = t % ntx, ty = (t / ntx) % nty, tz = t / (ntx * nty);
     const int i0 = 2 + kTI * tx, j0 = 2 + kTJ * ty, k0 = 2 + kTK * tz;
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    auto gidx = [&](int i, int j, int k) { return b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1); };
-    for (int e = threadIdx.x; e < kXK * kXJ * kXI; e += blockDim.x) {
-        const int a = e % kXI, r = e / kXI, bq = r % kXJ, cq = r / kXJ;
-        X[e] = xin[gidx(rbt_src(i0 - 2 + a, ni, pi), rbt_src(j0 - 2 + bq, nj, pj), rbt_src(k0 - 2 + cq, nk, pk))];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    // staging, a warp per row (lanes along i), as asynchronous copies
+    // (cp.async) all in flight at once, then one wait
+    for (int r = warp; r < kXJ * kXK; r += nwarp) {
+        const int bq = r % kXJ, cq = r / kXJ;
+        const long row = b.off3 - 1 + jo * (rbt_src(j0 - 2 + bq, nj, pj) - 1) + ko * (rbt_src(k0 - 2 + cq, nk, pk) - 1);
+        for (int a = lane; a < kXI; a += 32) rbt_async(&X[r * kXI + a], xin + row + rbt_src(i0 - 2 + a, ni, pi));
     }
-    for (int e = threadIdx.x; e < kBK * kBJ * kBI; e += blockDim.x) {
-        const int a = e % kBI, r = e / kBI, bq = r % kBJ, cq = r / kBJ;
-        Bs[e] = bb[gidx(rbt_src(i0 - 1 + a, ni, pi), rbt_src(j0 - 1 + bq, nj, pj), rbt_src(k0 - 1 + cq, nk, pk))];
+    for (int r = warp; r < kBJ * kBK; r += nwarp) {
+        const int bq = r % kBJ, cq = r / kBJ;
+        const long row = b.off3 - 1 + jo * (rbt_src(j0 - 1 + bq, nj, pj) - 1) + ko * (rbt_src(k0 - 1 + cq, nk, pk) - 1);
+        for (int a = lane; a < kBI; a += 32) rbt_async(&Bs[r * kBI + a], bb + row + rbt_src(i0 - 1 + a, ni, pi));
     }
+    {
+        const long n0 = b.n[0];
+        // positions outside the level (clamped on a physical side) are
+        // never updated: zeros there, and no read outside the tables
+        for (int e = threadIdx.x; e < kBJ * kBI; e += blockDim.x) {
+            const int a = e % kBI, bq = e / kBI;
+            const int iw = rbt_src(i0 - 1 + a, ni, pi), jw = rbt_src(j0 - 1 + bq, nj, pj);
+            if (iw < 2 || iw > ni + 1 || jw < 2 || jw > nj + 1) {
+                for (int f = 0; f < 5; f++) M2[f * kBJ * kBI + e] = (T)0;
+                continue;
+            }
+            const long ij = b.off2 + (iw - 1) + n0 * (jw - 1);
+            rbt_async(&M2[e], mf.E2 + ij - 1);
+            rbt_async(&M2[kBJ * kBI + e], mf.E2 + ij);
+            rbt_async(&M2[2 * kBJ * kBI + e], mf.N2 + ij - n0);
+            rbt_async(&M2[3 * kBJ * kBI + e], mf.N2 + ij);
+            rbt_async(&M2[4 * kBJ * kBI + e], mf.R2 + ij);
+        }
+        for (int e = threadIdx.x; e < kBK; e += blockDim.x) {
+            const int kw = rbt_src(k0 - 1 + e, nk, pk);
+            if (kw < 2 || kw > nk + 1) {
+                for (int f = 0; f < 4; f++) M1[f * kBK + e] = (T)0;
+                continue;
+            }
+            const long kk = b.off1k + (kw - 1);
+            rbt_async(&M1[e], mf.Ez + kk);
+            rbt_async(&M1[kBK + e], mf.Nz + kk);
+            rbt_async(&M1[2 * kBK + e], mf.Rz + kk - 1);
+            rbt_async(&M1[3 * kBK + e], mf.Rz + kk);
+        }
+    }
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-    constexpr int sJ = kXI, sK = kXI * kXJ;
-    // one update of the staged point at X index xe (b at Bs index be) with
-    // the couplings of the point it is, (iw, jw, kw)
-    auto update = [&](int xe, int be, int iw, int jw, int kw) {
-        T c[6], dinv;
-        rbt_coefs(b, iw, jw, kw, E, N, R, D, mf, c, dinv);
-        const T s = Bs[be] + c[0] * X[xe - 1] + c[1] * X[xe + 1] + c[2] * X[xe - sJ] + c[3] * X[xe + sJ] +
-                    c[4] * X[xe - sK] + c[5] * X[xe + sK];
+    constexpr int sJ = kXI, sK = kXI * kXJ, sM = kBJ * kBI;
+    // one update of the staged point at X index xe, b at Bs index be, the
+    // couplings from the staged separable factors of column bc and layer
+    // bk: coefs_mf's and rb_point's operations
+    auto update = [&](int xe, int be, int bc, int bk) {
+        const T ez = M1[bk], nz = M1[kBK + bk], r2 = M2[4 * sM + bc];
+        const T c0 = M2[bc] * ez, c1 = M2[sM + bc] * ez, c2 = M2[2 * sM + bc] * nz, c3 = M2[3 * sM + bc] * nz;
+        const T c4 = r2 * M1[2 * kBK + bk], c5 = r2 * M1[3 * kBK + bk];
+        const T dinv = (T)1 / (((c0 + c1) + (c2 + c3)) + (c4 + c5));
+        const T s = Bs[be] + c0 * X[xe - 1] + c1 * X[xe + 1] + c2 * X[xe - sJ] + c3 * X[xe + sJ] + c4 * X[xe - sK] +
+                    c5 * X[xe + sK];
         const T xo = X[xe];
         X[xe] = xo + omega * (s * dinv - xo);
     };
     // colour 0 on the tile and its one-point halo, where that is a point of
-    // the level (wrapped on periodic axes)
-    for (int e = threadIdx.x; e < kBK * kBJ * kBI; e += blockDim.x) {
-        const int a = e % kBI, r = e / kBI, bq = r % kBJ, cq = r / kBJ;
-        const int i = i0 - 1 + a, j = j0 - 1 + bq, k = k0 - 1 + cq;
-        if (((i + j + k) & 1) != 0) continue;
-        if ((!pi && (i < 2 || i > ni + 1)) || (!pj && (j < 2 || j > nj + 1)) || (!pk && (k < 2 || k > nk + 1)))
-            continue;
-        update(((cq + 1) * kXJ + bq + 1) * kXI + a + 1, e, rbt_src(i, ni, pi), rbt_src(j, nj, pj),
-               rbt_src(k, nk, pk));
+    // the level (wrapped on periodic axes): a warp per row of the halo box,
+    // lane m on its m-th colour-0 point
+    for (int r = warp; r < kBJ * kBK; r += nwarp) {
+        const int bq = r % kBJ, cq = r / kBJ, j = j0 - 1 + bq, k = k0 - 1 + cq;
+        if ((!pj && (j < 2 || j > nj + 1)) || (!pk && (k < 2 || k > nk + 1))) continue;
+        const int a = ((i0 - 1 + j + k) & 1) + 2 * lane, i = i0 - 1 + a;
+        if (a >= kBI || (!pi && (i < 2 || i > ni + 1))) continue;
+        update(((cq + 1) * kXJ + bq + 1) * kXI + a + 1, r * kBI + a, bq * kBI + a, cq);
     }
     __syncthreads();
-    // colour 1 on the tile's points of the level
-    for (int e = threadIdx.x; e < kTK * kTJ * kTI; e += blockDim.x) {
-        const int a = e % kTI, r = e / kTI, bq = r % kTJ, cq = r / kTJ;
-        const int i = i0 + a, j = j0 + bq, k = k0 + cq;
-        if (((i + j + k) & 1) != 1 || i > ni + 1 || j > nj + 1 || k > nk + 1) continue;
-        update(((cq + 2) * kXJ + bq + 2) * kXI + a + 2, ((cq + 1) * kBJ + bq + 1) * kBI + a + 1, i, j, k);
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < kTK * kTJ * kTI; e += blockDim.x) {
-        const int a = e % kTI, r = e / kTI, bq = r % kTJ, cq = r / kTJ;
-        const int i = i0 + a, j = j0 + bq, k = k0 + cq;
+    // colour 1 on the tile's points of the level: a half warp per tile row
+    for (int r = 2 * warp + (lane >> 4); r < kTJ * kTK; r += 2 * nwarp) {
+        const int bq = r % kTJ, cq = r / kTJ, j = j0 + bq, k = k0 + cq;
+        const int a = ((i0 + j + k + 1) & 1) + 2 * (lane & 15), i = i0 + a;
         if (i > ni + 1 || j > nj + 1 || k > nk + 1) continue;
-        const T v = X[((cq + 2) * kXJ + bq + 2) * kXI + a + 2];
-        xout[gidx(i, j, k)] = v;
+        update(((cq + 2) * kXJ + bq + 2) * kXI + a + 2, ((cq + 1) * kBJ + bq + 1) * kBI + a + 1,
+               (bq + 1) * kBI + a + 1, cq + 1);
+    }
+    __syncthreads();
+    // the tile out, a warp per row, and the ghosts its boundary points mirror
+    for (int r = warp; r < kTJ * kTK; r += nwarp) {
+        const int bq = r % kTJ, cq = r / kTJ, j = j0 + bq, k = k0 + cq, i = i0 + lane;
+        if (i > ni + 1 || j > nj + 1 || k > nk + 1) continue;
+        const T v = X[((cq + 2) * kXJ + bq + 2) * kXI + lane + 2];
+        xout[b.off3 + (i - 1) + jo * (j - 1) + ko * (k - 1)] = v;
         if (push) push_ghosts(push, b, i, j, k, v, xout);
     }
 }
@@ -1051,11 +1085,11 @@ template <typename T> void launch_copy_range(const T *src, T *dst, long n, cudaS
 }
 
 template <typename T>
-void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *E, const T *N, const T *R, const T *D,
-                    const T *xin, T *xout, const T *b, const PushDev *push, const MfTab<T> &mf, cudaStream_t st)
+void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *xin, T *xout, const T *b,
+                    const PushDev *push, const MfTab<T> &mf, cudaStream_t st)
 {
     const int ntile = ((n[0] - 2 + kTI - 1) / kTI) * ((n[1] - 2 + kTJ - 1) / kTJ) * ((n[2] - 2 + kTK - 1) / kTK);
-    k_rb_tile<T><<<ntile, 256, kRbTileSmem<T>, st>>>(blk, (T)omega, E, N, R, D, xin, xout, b, push, mf);
+    k_rb_tile<T><<<ntile, 256, kRbTileSmem<T>, st>>>(blk, (T)omega, xin, xout, b, push, mf);
     count_launch(1);
 }
 
@@ -1252,10 +1286,15 @@ bool prepare_vtail()
 // the shared-memory red-black tiles' shared memory limit, once per context
 bool prepare_rb_tile()
 {
+    // the largest shared-memory carveout, so that several tiles share an SM
     const bool ok = cudaFuncSetAttribute(k_rb_tile<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kRbTileSmem<float>) == cudaSuccess &&
                     cudaFuncSetAttribute(k_rb_tile<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kRbTileSmem<double>) == cudaSuccess;
+                                         (int)kRbTileSmem<double>) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_rb_tile<float>, cudaFuncAttributePreferredSharedMemoryCarveout, 100) ==
+                        cudaSuccess &&
+                    cudaFuncSetAttribute(k_rb_tile<double>, cudaFuncAttributePreferredSharedMemoryCarveout, 100) ==
+                        cudaSuccess;
     if (!ok) cudaGetLastError();
     return ok;
 }
@@ -1277,9 +1316,8 @@ bool prepare_rb_tile()
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
                                   long, long, const CoarseDirect<T> &, cudaStream_t);             \
     template void launch_copy_range<T>(const T *, T *, long, cudaStream_t);                        \
-    template void launch_rb_tile<T>(const BlkDev *, const int *, double, const T *, const T *,     \
-                                    const T *, const T *, const T *, T *, const T *, const PushDev *, \
-                                    const MfTab<T> &, cudaStream_t);                              \
+    template void launch_rb_tile<T>(const BlkDev *, const int *, double, const T *, T *, const T *, \
+                                    const PushDev *, const MfTab<T> &, cudaStream_t);             \
     template void launch_coarse_ops<T>(const VLev *, int, int, long, long, const T *, const T *,  \
                                        const T *, const T *, const MfTab<T> &, float *, float *,  \
                                        long *, cudaStream_t);                                     \

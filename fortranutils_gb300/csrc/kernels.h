@@ -97,10 +97,10 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
 // dst[0..n) = src[0..n) (device arrays)
 template <typename T> void launch_copy_range(const T *src, T *dst, long n, cudaStream_t st);
 // one red-black sweep (both colours) of a one-block level through shared-memory
-// tiles, xin -> xout (k_rb_tile); n: the block's points incl. ghosts
+// tiles, xin -> xout, separable couplings (k_rb_tile); n: the block's points incl. ghosts
 template <typename T>
-void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *E, const T *N, const T *R, const T *D,
-                    const T *xin, T *xout, const T *b, const PushDev *push, const MfTab<T> &mf, cudaStream_t st);
+void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *xin, T *xout, const T *b,
+                    const PushDev *push, const MfTab<T> &mf, cudaStream_t st);
 // the bottom level's couplings, point elements and ghost sources (k_coarse_ops)
 template <typename T>
 void launch_coarse_ops(const VLev *lv, int lev, int nb, long base, long len, const T *E, const T *N, const T *R,

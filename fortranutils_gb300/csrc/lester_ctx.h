@@ -55,6 +55,7 @@ struct CycleGraph {
     int threads = 0;                // red-black CTA size
     int line = 0;                   // y-line relaxation
     int direct = 0;                 // points of the bottom level's direct solve (0: smoothed)
+    int tile = 0;                   // ctrl.rb_tile
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
 };

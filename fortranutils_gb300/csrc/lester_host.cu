@@ -806,6 +806,16 @@ template <typename T> static int alloc_fast(Ctx &c)
         LES_CUDA(cudaMemset(*a, 0, bytes));
     }
     F.b = F.x + xspan;
+    // the other buffer of the shared-memory red-black sweeps (one-block
+    // grids); without it those levels keep the per-colour launches
+    if (c.rb_tile_ok && c.g.numbl == 1) {
+        if (cudaMalloc((void **)&F.x2, sizeof(T) * (size_t)c.tot3) != cudaSuccess) {
+            cudaGetLastError();
+            F.x2 = nullptr;
+        } else {
+            LES_CUDA(cudaMemset(F.x2, 0, sizeof(T) * (size_t)c.tot3));
+        }
+    }
     if (!c.E64) {
         size_t n1 = sizeof(double) * (size_t)c.tot_sg3;
         double **a64[4] = {&c.E64, &c.N64, &c.R64, &c.P64};
@@ -1032,12 +1042,13 @@ void prof_pair(Ctx &c, int tag, cudaEvent_t *e0, cudaEvent_t *e1)
     c.prof_launches[tag]++;
 }
 
-// Whether level lev is smoothed by k_rb_tile: one block, point red-black
-// (not y-line) relaxation, no interface face, periodic faces that push
-// (even extents), and the other buffer allocated.
+// Whether level lev is smoothed by k_rb_tile (ctrl.rb_tile): one block, point red-black
+// (not y-line) relaxation with separable couplings (the FP32 solver), no
+// interface face, periodic faces that push (even extents), and the other
+// buffer allocated.
 template <typename T> static bool rb_tile_level(Ctx &c, int lev)
 {
-    if (!c.rb_tile_ok || c.g.numbl != 1 || c.c.rb_line) return false;
+    if (!c.c.rb_tile || !c.rb_tile_ok || c.g.numbl != 1 || c.c.rb_line || !fset<T>(c).mf) return false;
     const LevelGeom &L = c.lv[lev];
     if (!L.rb_push) return false;
     for (int s = 0; s < 6; s++) {
@@ -1046,17 +1057,7 @@ template <typename T> static bool rb_tile_level(Ctx &c, int lev)
         // a periodic axis is periodic on both of its sides
         if ((bc == LES_BCT_PERIODIC) != (c.g.bl_bc[0][s ^ 1] == LES_BCT_PERIODIC)) return false;
     }
-    FastSet<T> &F = fset<T>(c);
-    if (!F.x2) {
-        if (cudaMalloc(&F.x2, sizeof(T) * (size_t)c.tot3) != cudaSuccess) {
-            cudaGetLastError();
-            F.x2 = nullptr;
-            c.rb_tile_ok = false;
-            return false;
-        }
-        cudaMemset(F.x2, 0, sizeof(T) * (size_t)c.tot3);
-    }
-    return true;
+    return fset<T>(c).x2 != nullptr;  // allocated with the solver's arrays (alloc_fast)
 }
 
 template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
@@ -1082,8 +1083,7 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             }
             unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
-            launch_rb_tile<T>(L.d_blk, L.n[1], c.c.rb_omega, F.E, F.N, F.R, F.D, in, out, F.b, L.d_push,
-                              F.mf ? F.tab : MfTab<T>(), c.stream);
+            launch_rb_tile<T>(L.d_blk, L.n[1], c.c.rb_omega, in, out, F.b, L.d_push, F.tab, c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             std::swap(in, out);
         }
@@ -1231,7 +1231,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
         G.krylov == (kry ? 1 : df ? 2 : 0) && G.threads == c.rb_threads && G.line == k.rb_line &&
-        G.direct == fset<T>(c).cn)
+        G.direct == fset<T>(c).cn && G.tile == k.rb_tile)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -1284,6 +1284,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.tail = k.mg_tail;
     G.krylov = kry ? 1 : df ? 2 : 0;
     G.direct = fset<T>(c).cn;
+    G.tile = k.rb_tile;
     G.threads = c.rb_threads;
     G.line = k.rb_line;
     return 0;
@@ -1724,6 +1725,7 @@ static int check_ctrl(const lester_ctrl *c)
     if (c->phys32 && c->exact) return set_err(LES_ERR_ARG, "phys32 needs exact = 0 (FP32 physics is not the exact build)");
     if (c->sc1_sweep < 0 || c->sc1_sweep > 3) return set_err(LES_ERR_ARG, "sc1_sweep %d out of 0..3", c->sc1_sweep);
     if (c->wait_limit < 0) return set_err(LES_ERR_ARG, "wait_limit %d < 0", c->wait_limit);
+    if (c->rb_tile < 0 || c->rb_tile > 1) return set_err(LES_ERR_ARG, "rb_tile %d not 0 or 1", c->rb_tile);
     return 0;
 }
 

@@ -165,6 +165,11 @@ typedef struct lester_ctrl {
     int wait_limit;    /* bounded device waits (grid barrier, progress
                           flags): polls before a wait gives up and the call
                           returns LES_ERR_TIMEOUT; 0 = the default (2^24) */
+    int rb_tile;       /* 1: the FP32 solver's point red-black sweeps on a
+                          one-block level run as one launch per sweep through
+                          shared-memory tiles (both colours, a recomputed
+                          halo); 0 (default): one launch per colour, which
+                          measured faster on GB300 */
 } lester_ctrl;
 
 /* Arena slice lengths (elements) implied by the geometry. */
