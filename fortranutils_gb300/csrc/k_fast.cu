@@ -457,6 +457,169 @@ __global__ void __launch_bounds__(256) k_yline(const BlkDev *__restrict__ blk, i
     }
 }
 
+// ---- y-line zebra relaxation, a warp per line -----------------------------
+// The same relaxation as k_yline with the tridiagonal solve spread over the
+// 32 lanes of a warp: lane L holds rows [L m, L m + m) of the line (m =
+// ceil(nj / 32) <= kLineM), solves all but its last row by the Thomas
+// algorithm with three right-hand sides -- the line's own, and unit
+// couplings to the last row of lane L-1 and to its own last row -- so every
+// row is y + u X(L-1) + w X(L) in the lanes' last-row values X; the last
+// rows' equations then form a tridiagonal system of 32 unknowns, one per
+// lane, solved by parallel cyclic reduction over warp shuffles (5 steps),
+// and each lane substitutes back.  No scratch arrays; 32 lanes per line
+// instead of one thread: used where a level has few lines (launch_yline).
+// The elimination order differs from k_yline's, so results agree to
+// rounding.
+constexpr int kLineM = 16;  // rows per lane: lines of up to 512 points
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_yline_warp(const BlkDev *__restrict__ blk, int color, T omega,
+                                                    const T *__restrict__ E, const T *__restrict__ N,
+                                                    const T *__restrict__ R, const T *__restrict__ D,
+                                                    T *__restrict__ x, const T *__restrict__ bb, MfTab<T> mf)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int ni = b.n[0] - 2, nj = b.n[1] - 2, nk = b.n[2] - 2;
+    const unsigned nh = (unsigned)(ni + 1) >> 1;
+    const unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // the warp's line
+    const int lane = threadIdx.x & 31;
+    if (q >= nh * (unsigned)nk) return;  // whole warps leave together
+    const unsigned kq = q / nh;
+    const int k = (int)kq + 2;
+    const int i = 2 + 2 * (int)(q - kq * nh) + ((2 + k + color) & 1);
+    if (i > ni + 1) return;
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long p0 = b.off3 + (i - 1) + ko * (k - 1);
+    const int m = (nj + 31) / 32;
+    const int s = lane * m, e = min(s + m, nj), cnt = max(e - s, 0);
+    // row r of the line (j = r + 2) as a x(r-1) + bd x(r) + c x(r+1) = d
+    auto row = [&](int r, T &a, T &bd, T &c, T &d) {
+        const int j = r + 2;
+        const long p = p0 + jo * (j - 1);
+        T cf[6], dinv;
+        if (mf.E2) {
+            coefs_mf(b, mf, i, j, k, cf, dinv);
+        } else {
+            cf[0] = E[p - 1];
+            cf[1] = E[p];
+            cf[2] = N[p - jo];
+            cf[3] = N[p];
+            cf[4] = R[p - ko];
+            cf[5] = R[p];
+            dinv = D[p];
+        }
+        T rhs = bb[p] + cf[0] * x[p - 1] + cf[1] * x[p + 1] + cf[4] * x[p - ko] + cf[5] * x[p + ko];
+        T lo = cf[2], up = cf[3];
+        if (j == 2) {
+            rhs += lo * x[p - jo];
+            lo = 0;
+        }
+        if (j == nj + 1) {
+            rhs += up * x[p + jo];
+            up = 0;
+        }
+        a = -lo;
+        bd = (T)1 / dinv;
+        c = -up;
+        d = rhs;
+    };
+    // local Thomas on rows s .. e-2 with three right-hand sides
+    T cp[kLineM], vy[kLineM], vu[kLineM], vw[kLineM];
+    const int nl = cnt - 1;  // rows of the local system
+#pragma unroll
+    for (int t = 0; t < kLineM; t++) {
+        if (t < nl) {
+            T a, bd, c, d;
+            row(s + t, a, bd, c, d);
+            const T at = t > 0 ? a : (T)0;
+            const T den = bd - (t > 0 ? at * cp[t - 1] : (T)0);
+            const T ct = t < nl - 1 ? c : (T)0;
+            const T ru = t == 0 ? -a : (T)0, rw = t == nl - 1 ? -c : (T)0;
+            cp[t] = ct / den;
+            vy[t] = (d - (t > 0 ? at * vy[t - 1] : (T)0)) / den;
+            vu[t] = (ru - (t > 0 ? at * vu[t - 1] : (T)0)) / den;
+            vw[t] = (rw - (t > 0 ? at * vw[t - 1] : (T)0)) / den;
+        }
+    }
+#pragma unroll
+    for (int t = kLineM - 2; t >= 0; t--) {
+        if (t < nl - 1) {
+            vy[t] -= cp[t] * vy[t + 1];
+            vu[t] -= cp[t] * vu[t + 1];
+            vw[t] -= cp[t] * vw[t + 1];
+        }
+    }
+    // x(s) = F and x(e-2) = G in (X(L-1), X(L)); a one-row lane is X itself
+    T fy = 0, fu = 0, fw = 1, gy = 0, gu = 1, gw = 0;
+    if (nl > 0) {
+        fy = vy[0];
+        fu = vu[0];
+        fw = vw[0];
+#pragma unroll
+        for (int t = 0; t < kLineM; t++)
+            if (t == nl - 1) {
+                gy = vy[t];
+                gu = vu[t];
+                gw = vw[t];
+            }
+    }
+    const T ny = __shfl_down_sync(0xffffffffu, fy, 1), nu = __shfl_down_sync(0xffffffffu, fu, 1),
+            nw = __shfl_down_sync(0xffffffffu, fw, 1);
+    const int ncnt = __shfl_down_sync(0xffffffffu, cnt, 1);
+    // the reduced equation of the lane's last row
+    T A = 0, B = 1, C = 0, Dr = 0;
+    if (cnt > 0) {
+        T a, bd, c, d;
+        row(e - 1, a, bd, c, d);
+        const bool nxt = lane < 31 && ncnt > 0;
+        const T fyn = nxt ? ny : (T)0, fun = nxt ? nu : (T)0, fwn = nxt ? nw : (T)0;
+        A = a * gu;
+        B = a * gw + bd + c * fun;
+        C = c * fwn;
+        Dr = d - a * gy - c * fyn;
+    }
+    // parallel cyclic reduction over the lanes
+#pragma unroll
+    for (int st = 1; st < 32; st <<= 1) {
+        T am = __shfl_up_sync(0xffffffffu, A, st), bm = __shfl_up_sync(0xffffffffu, B, st),
+          cm = __shfl_up_sync(0xffffffffu, C, st), dm = __shfl_up_sync(0xffffffffu, Dr, st);
+        T ap = __shfl_down_sync(0xffffffffu, A, st), bp = __shfl_down_sync(0xffffffffu, B, st),
+          cq = __shfl_down_sync(0xffffffffu, C, st), dp = __shfl_down_sync(0xffffffffu, Dr, st);
+        if (lane < st) {
+            am = 0;
+            bm = 1;
+            cm = 0;
+            dm = 0;
+        }
+        if (lane + st > 31) {
+            ap = 0;
+            bp = 1;
+            cq = 0;
+            dp = 0;
+        }
+        const T k1 = A / bm, k2 = C / bp;
+        const T An = -am * k1, Cn = -cq * k2;
+        const T Bn = B - cm * k1 - ap * k2, Dn = Dr - dm * k1 - dp * k2;
+        A = An;
+        B = Bn;
+        C = Cn;
+        Dr = Dn;
+    }
+    const T X = Dr / B;
+    T Xm = __shfl_up_sync(0xffffffffu, X, 1);
+    if (lane == 0) Xm = 0;
+    // back substitution and the relaxation of the lane's rows
+#pragma unroll
+    for (int t = 0; t < kLineM; t++) {
+        if (t < cnt) {
+            const T xl = t < nl ? vy[t] + vu[t] * Xm + vw[t] * X : X;
+            const long p = p0 + jo * (s + t + 1);
+            const T xo = x[p];
+            x[p] = xo + omega * (xl - xo);
+        }
+    }
+}
+
 // ---- residual + restriction ------------------------------------------------
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
 // children are summed into the coarse right-hand side.
@@ -1095,9 +1258,18 @@ void launch_rb_tile(const BlkDev *blk, const int n[3], double omega, const T *xi
 
 template <typename T>
 void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double omega, const T *E, const T *N,
-                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, cudaStream_t st)
+                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, int maxnj,
+                  cudaStream_t st)
 {
-    k_yline<T><<<dim3(nb_(maxik_half, 128), nb), 128, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, mf, cp, dp);
+    // a warp per line (4 per CTA of 128 threads) where the lines are few:
+    // with tens of thousands of lines a thread per line already fills the
+    // GPU and does less work in all (measured on the 512x384x256 channel's
+    // level 1, 65536 lines a colour: the warps were slower)
+    if (maxnj <= 32 * kLineM && maxik_half * nb <= 8192)
+        k_yline_warp<T><<<dim3(nb_(maxik_half, 4), nb), 128, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, mf);
+    else
+        k_yline<T><<<dim3(nb_(maxik_half, 128), nb), 128, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, mf, cp,
+                                                                   dp);
     count_launch(1);
 }
 
@@ -1308,7 +1480,7 @@ bool prepare_rb_tile()
                                const MfTab<T> &, int, cudaStream_t);                              \
     template void launch_yline<T>(const BlkDev *, int, long, int, double, const T *, const T *,   \
                                   const T *, const T *, T *, const T *, const MfTab<T> &, T *, T *, \
-                                  cudaStream_t);                                                  \
+                                  int, cudaStream_t);                                             \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
                                            const T *, const T *, const T *, const T *, const T *, \
                                            T *, const MfTab<T> &, cudaStream_t);                  \

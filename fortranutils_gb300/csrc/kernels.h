@@ -85,7 +85,8 @@ void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega,
 // most columns of one colour in a block)
 template <typename T>
 void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double omega, const T *E, const T *N,
-                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, cudaStream_t st);
+                  const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, int maxnj,
+                  cudaStream_t st);
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,

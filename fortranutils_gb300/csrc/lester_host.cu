@@ -1092,11 +1092,14 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
     }
     c.rb_tile_mask &= ~(1 << lev);
     if (c.c.rb_line && F.cp) {
-        // y-line zebra relaxation; halos exchanged after each colour
+        // y-line zebra relaxation; halos exchanged after each colour.  A
+        // warp per line where every block's lines fit kLineM rows a lane
+        int maxnj = 0;
+        for (int bl = 1; bl <= c.g.numbl; bl++) maxnj = std::max(maxnj, L.n[bl][1] - 2);
         for (int s = 0; s < nsweep; s++)
             for (int color = 0; color < 2; color++) {
                 launch_yline<T>(L.d_blk, c.g.numbl, L.maxik, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x, F.b,
-                                F.mf ? F.tab : MfTab<T>(), F.cp, F.dp, c.stream);
+                                F.mf ? F.tab : MfTab<T>(), F.cp, F.dp, maxnj, c.stream);
                 launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
             }
         return;
