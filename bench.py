@@ -385,7 +385,7 @@ def run_gpu(args):
                      "rb_launches": kl, "sweep_ms": sms, "sweep_launches": sl,
                      "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
         del g
-        if args.step_graph and not WORKLOADS[wl].get("inflow"):
+        if args.step_graph:
             res[mode]["graph"] = run_graph_leg(args, case, ctrl, wl)
         if mode == "mixed" and not args.no_e2e:
             res[mode]["e2e"] = run_e2e(args, case, ctrl, wl)
@@ -455,7 +455,7 @@ def run_e2e(args, case, ctrl, wl="mixing"):
     torch.cuda.empty_cache()
     # the same way of running the step as the headline: the whole-step
     # graph (with the host copies as its nodes) unless --step-graph 0
-    graph = int(bool(args.step_graph) and not WORKLOADS[wl].get("inflow"))
+    graph = int(bool(args.step_graph))
     ctrl.step_graph = graph
     L.gpu_set_ctrl(ctrl)
     L.gpu_set_iststep(2)  # a run's first step

@@ -248,13 +248,17 @@ __device__ __forceinline__ double inlet_uniform(unsigned long long seed, int ste
 
 // fixed_inlet (code/fixed_inlet.F:61-176) on one inlet block: the i = 2
 // face and the i = 1 ghost cells, all j, k including ghosts
+// step_dev (nullable): the step number read from device memory instead of
+// step (a replayed graph: the host writes it before each launch)
 __global__ void k_fixed_inlet(const BlkDev *__restrict__ blk, int iblk, int which, const double *__restrict__ uprof,
                               const double *__restrict__ vprof, unsigned long long seed, int step,
-                              double rholo, double rhohi, double *__restrict__ u, double *__restrict__ v,
+                              const int *__restrict__ step_dev, double rholo, double rhohi,
+                              double *__restrict__ u, double *__restrict__ v,
                               double *__restrict__ w, double *__restrict__ sc1, double *__restrict__ rho,
                               double *__restrict__ u_int, double *__restrict__ v_int,
                               double *__restrict__ w_int)
 {
+    if (step_dev) step = *step_dev;
     const BlkDev b = blk[iblk];
     const int njp1 = b.n[1], nkp1 = b.n[2], nj = njp1 - 1;
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
@@ -526,13 +530,13 @@ void launch_mass_change(const BlkDev *blk, int nb, long maxcell, double dtime, c
 }
 
 void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, const double *uprof,
-                        const double *vprof, unsigned long long seed, int step, double rholo, double rhohi,
-                        double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
+                        const double *vprof, unsigned long long seed, int step, const int *step_dev, double rholo,
+                        double rhohi, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                         double *v_int, double *w_int, cudaStream_t st)
 {
     unsigned g = (unsigned)((nplane + 255) / 256);
-    k_fixed_inlet<<<g, 256, 0, st>>>(blk, iblk, which, uprof, vprof, seed, step, rholo, rhohi, u, v, w, sc1, rho,
-                                     u_int, v_int, w_int);
+    k_fixed_inlet<<<g, 256, 0, st>>>(blk, iblk, which, uprof, vprof, seed, step, step_dev, rholo, rhohi, u, v, w,
+                                     sc1, rho, u_int, v_int, w_int);
     count_launch(1);
 }
 

@@ -204,8 +204,8 @@ void launch_mass_change(const BlkDev *blk, int nb, long maxcell, double dtime, c
                         const double *rhonp1, const double *rdidjp, const double *dkw, double *partial,
                         double *out, cudaStream_t st);
 void launch_fixed_inlet(const BlkDev *blk, int iblk, int which, int nplane, const double *uprof,
-                        const double *vprof, unsigned long long seed, int step, double rholo, double rhohi,
-                        double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
+                        const double *vprof, unsigned long long seed, int step, const int *step_dev, double rholo,
+                        double rhohi, double *u, double *v, double *w, double *sc1, double *rho, double *u_int,
                         double *v_int, double *w_int, cudaStream_t st);
 
 void launch_statistics(const BlkDev *blk, int nb, long maxpts, long maxij, int no_sam, const double *u,

@@ -150,7 +150,10 @@ int inlet_task(Ctx &c, const double *uprof, const double *vprof, unsigned long l
         if (std::max(need, need_amp) > c.nprof)
             return set_err(LES_ERR_ARG, "inlet block %d needs %ld profile values, %d given", b,
                            std::max(need, need_amp), c.nprof);
-        launch_fixed_inlet(c.lv[1].d_blk, b - 1, which, n[1] * n[2], uprof, vprof, seed, step, c.c.rholo,
+        // inside the whole-step graph's capture the step comes from device
+        // memory (d_step[1], written before each replay)
+        launch_fixed_inlet(c.lv[1].d_blk, b - 1, which, n[1] * n[2], uprof, vprof, seed, step,
+                           c.capturing ? c.d_step + 1 : nullptr, c.c.rholo,
                            c.c.rhohi, u, v, w, sc1, rho, u_int, v_int, w_int, c.stream);
     }
     LES_CUDA(cudaGetLastError());

@@ -252,9 +252,11 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
 {
     if (c.sg.exec) cudaGraphExecDestroy(c.sg.exec);
     c.sg.exec = nullptr;
-    if (!c.h_step) LES_CUDA(cudaMallocHost(&c.h_step, sizeof(int)));
+    // step counters of a replay: [0] iststep (the predictors' running
+    // means), [1] the caller's istep (the inlet perturbations)
+    if (!c.h_step) LES_CUDA(cudaMallocHost(&c.h_step, 2 * sizeof(int)));
     if (!c.h_loop) LES_CUDA(cudaMallocHost(&c.h_loop, 8 * sizeof(double)));
-    if (!c.d_step) LES_CUDA(cudaMalloc(&c.d_step, sizeof(int)));
+    if (!c.d_step) LES_CUDA(cudaMalloc(&c.d_step, 2 * sizeof(int)));
     if (!c.d_loop) LES_CUDA(cudaMalloc(&c.d_loop, 8 * sizeof(double)));
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
     if (!c.graph_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.graph_stream, cudaStreamNonBlocking));
@@ -271,7 +273,7 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
     }
     c.capturing = true;
     int r = 0;
-    if (cudaMemcpyAsync(c.d_step, c.h_step, sizeof(int), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
+    if (cudaMemcpyAsync(c.d_step, c.h_step, 2 * sizeof(int), cudaMemcpyHostToDevice, c.stream) != cudaSuccess ||
         cudaMemsetAsync(c.d_loop, 0, 8 * sizeof(double), c.stream) != cudaSuccess)
         r = set_err(LES_ERR_CUDA, "step graph: status copies");
     if (!r && c.xfer) r = c.xfer->issue_in();  // host inputs: copy nodes
@@ -329,9 +331,7 @@ static int step_graph(Ctx &c, lester_fields &D, const lester_fields &H, const in
 {
     *done = false;
     const int ps = c.c.psolve;
-    if (*istep == 1 || (ps != LES_PSOLVE_FP64 && ps != LES_PSOLVE_MIXED) || c.prof || has_inlet(c) ||
-        has_convective(c))
-        return 0;
+    if (*istep == 1 || (ps != LES_PSOLVE_FP64 && ps != LES_PSOLVE_MIXED) || c.prof) return 0;
     const int prec = ps == LES_PSOLVE_MIXED ? 32 : 64;
     if (c.c.autotune && !c.tuned[prec == 32 ? 1 : 0].done) return 0;
     // the coefficients converted by an earlier solve of this precision
@@ -361,7 +361,8 @@ static int step_graph(Ctx &c, lester_fields &D, const lester_fields &H, const in
 
 static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
 {
-    *c.h_step = c.iststep;
+    c.h_step[0] = c.iststep;
+    c.h_step[1] = *istep;
     LES_CUDA(cudaGraphLaunch(c.sg.exec, c.stream));
     c.sg.replays++;
     LES_CUDA(cudaStreamSynchronize(c.stream));

@@ -150,8 +150,8 @@ typedef struct lester_ctrl {
                           graph, the fast solve's cycle loop a device-side
                           conditional (WHILE) node; captured once per field
                           set and controls (istep > 1, fast psolve, device
-                          fields, no inflow/outflow sides, autotuning
-                          finished); otherwise the step runs as launched */
+                          or pinned host fields, autotuning finished);
+                          otherwise the step runs as launched */
     int sc1_sweep;     /* in-place scalar sweep of set_sc1: 0 = automatic
                           (the tile pipeline with FP32 physics where its
                           shared-memory ring fits, else the hyperplane

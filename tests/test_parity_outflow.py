@@ -245,3 +245,41 @@ def test_statistics_bitwise(gpulib):
     for n in L.STAT_NAMES:
         np.testing.assert_array_equal(got[n], ref[n], err_msg=n)
     assert not np.array_equal(ref["um"], outs0["um"])
+
+
+@pytest.mark.parametrize("psolve,phys32", [(L.PSOLVE_FP64, 0), (L.PSOLVE_MIXED, 1)])
+def test_six_blocks_step_graph(psolve, phys32, gpulib):
+    """The six-block boundary layer with its inflow and outflow sides,
+    steps 2..5 replayed from the whole-step graph (the inlet perturbation's
+    step number read from device memory in the replay): the same fields as
+    the steps launched call by call, bit for bit."""
+    case = grid.bl6_case(8)
+    cases.CASES["bl6"] = lambda: case
+    try:
+        st = cases.Setup("bl6", seed=3)
+    finally:
+        del cases.CASES["bl6"]
+    up, vp = grid.bl6_inflow(case)
+    inlet = [1, 0, 0, 4]
+    s = S.new_state(case, st.m, st.dkp, st.dkw)
+    S.init_bl6(s, rholo=1.0, rhohi=1.0)
+    out = {}
+    for graph in (0, 1):
+        ctrl = L.default_ctrl(dtime=2e-3, model=1, psolve=psolve, rtol=1e-9, max_outer=100, exact=0,
+                              phys32=phys32, step_graph=graph)
+        L.gpu_init(case.geom(), ctrl)
+        try:
+            L.gpu_set_inlet(inlet, up, vp, SEED)
+            g = s.to("torch")
+            rcs = [S.step(g, it) for it in range(1, 6)]
+            info = L.gpu_step_graph_info()
+            L.gpu_sync()
+            out[graph] = (g.to("numpy"), rcs, info)
+        finally:
+            L.gpu_finalize()
+    (a, ra, _), (b, rb, info) = out[0], out[1]
+    assert ra == rb == [0] * 5
+    assert not info["failed"] and info["replays"] == 4, info
+    for n in S.STATE:
+        assert np.array_equal(a[n], b[n]), n
+    assert rel(b["u"], s["u"]) > 1e-6
