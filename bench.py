@@ -249,6 +249,7 @@ def cfl_dt(case, s, cfl=0.3, dfs=0.2, visc=1.0 / 2800.0):
 
 SMOOTHER = "auto"
 RB_TILE = 0  # ctrl.rb_tile: red-black sweeps through shared-memory tiles (opt-in)
+P_GUESS = 0  # ctrl.p_guess: 0 the previous pressure, 1 extrapolated in time
 PHYS32 = 1
 
 
@@ -256,6 +257,7 @@ def make_ctrl(psolve, krylov=2, wl="mixing", dtime=None):
     from fortranutils_gb300 import lester as L
     sm = dict(autotune=3) if SMOOTHER == "auto" else dict(autotune=0)
     sm["rb_tile"] = RB_TILE
+    sm["p_guess"] = P_GUESS
     # the mixed path's physics in FP32 arithmetic (FP64 fields)
     sm["phys32"] = PHYS32 if psolve == L.PSOLVE_MIXED else 0
     if SMOOTHER == "line":
@@ -620,6 +622,8 @@ def main():
     ap.add_argument("--smoother", default="auto", choices=["auto", "point", "line"],
                     help="fast solvers' smoother: autotuned on the third solve (inside the warm-up "
                          "steps), point red-black, or y-line zebra relaxation")
+    ap.add_argument("--p-guess", type=int, default=0, choices=[0, 1],
+                    help="fast solves' initial pressure: 0 p(n), 1 2p(n)-p(n-1) (ctrl.p_guess)")
     ap.add_argument("--rb-tile", type=int, default=0, choices=[0, 1],
                     help="1: the FP32 solver's red-black sweeps through shared-memory tiles (ctrl.rb_tile)")
     ap.add_argument("--workload", default="mixing", choices=list(WORKLOADS),
@@ -628,9 +632,10 @@ def main():
     ap.add_argument("--shape", type=int, nargs=3, default=None,
                     help="cells per axis (other shapes than the workload's are for profiling only)")
     args = ap.parse_args()
-    global SMOOTHER, PHYS32, RB_TILE
+    global SMOOTHER, PHYS32, RB_TILE, P_GUESS
     SMOOTHER = args.smoother
     RB_TILE = args.rb_tile
+    P_GUESS = args.p_guess
     PHYS32 = args.phys32
     if args.shape is None:
         args.shape = list(WORKLOADS[args.workload]["shape"])

@@ -68,6 +68,29 @@ __global__ void k_loop_gate(cudaGraphConditionalHandle h, const double *__restri
 
 __global__ void k_copy_flag(const int *__restrict__ src, double *__restrict__ dst) { *dst = (double)*src; }
 
+// The fast solves' initial pressure in lester_step (ctrl.p_guess 1): when
+// pp holds the pressure the previous step started its solve from, and that
+// step was not the first (its p was a solution then),
+// p <- 2 p - pp (linear extrapolation in time); pp <- the p found here
+// either way.  The step number comes from istep_dev when given (a replayed
+// graph) and saved holds the step pp was taken at.
+__global__ void k_p_guess(double *__restrict__ p, double *__restrict__ pp, long n, int istep,
+                          const int *__restrict__ istep_dev, const int *__restrict__ saved)
+{
+    const int st = istep_dev ? *istep_dev : istep;
+    const bool extrap = *saved == st - 1 && st - 1 >= 2;
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const double t = p[q];
+        if (extrap) p[q] = 2.0 * t - pp[q];
+        pp[q] = t;
+    }
+}
+
+__global__ void k_p_guess_mark(int istep, const int *__restrict__ istep_dev, int *__restrict__ saved)
+{
+    *saved = istep_dev ? *istep_dev : istep;
+}
+
 } // namespace
 
 namespace les {
@@ -91,6 +114,14 @@ void launch_loop_gate(cudaGraphConditionalHandle h, const double *small, double 
 {
     k_loop_gate<<<1, 1, 0, st>>>(h, small, loop, rtol, confirm);
     count_launch(1);
+}
+
+void launch_p_guess(double *p, double *pp, long n, int istep, const int *istep_dev, int *saved, cudaStream_t st)
+{
+    unsigned g = (unsigned)((n + 255) / 256);
+    k_p_guess<<<g > 2432 ? 2432 : g, 256, 0, st>>>(p, pp, n, istep, istep_dev, saved);
+    k_p_guess_mark<<<1, 1, 0, st>>>(istep, istep_dev, saved);
+    count_launch(2);
 }
 
 void launch_copy_flag(const int *src, double *dst, cudaStream_t st)

@@ -224,6 +224,8 @@ void launch_loop_step(cudaGraphConditionalHandle h, const double *small, double 
                       int may_switch, cudaStream_t st);
 void launch_loop_gate(cudaGraphConditionalHandle h, const double *small, double *loop, double rtol, int confirm,
                       cudaStream_t st);
+// lester_step's initial pressure for the fast solves (k_graph.cu: k_p_guess)
+void launch_p_guess(double *p, double *pp, long n, int istep, const int *istep_dev, int *saved, cudaStream_t st);
 void launch_copy_flag(const int *src, double *dst, cudaStream_t st);
 
 } // namespace les

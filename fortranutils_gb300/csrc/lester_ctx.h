@@ -98,6 +98,8 @@ struct Ctx {
     double *E64 = nullptr, *N64 = nullptr, *R64 = nullptr, *P64 = nullptr;
     // the mixed solver's outer iteration in double-float (k_dfloat.cu): the
     // level-1 coefficients, p and b - shift as FP32 pairs
+    double *p_prev = nullptr;  // level-1 p at the start of the previous step's fast solve (ctrl.p_guess)
+    int *d_pguess = nullptr;   // the istep p_prev was taken at (device; -1: none)
     std::FILE *step_log = nullptr;  // lester_gpu_step_log's file (one JSON line per lester_step)
     float2 *df_E = nullptr, *df_N = nullptr, *df_R = nullptr, *df_P = nullptr, *df_p = nullptr, *df_b = nullptr;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)

@@ -582,6 +582,8 @@ static void free_ctx(Ctx *c)
     cudaFree(c->f64.cmt);
     cudaFree(c->f32.x2);
     cudaFree(c->f64.x2);
+    cudaFree(c->p_prev);
+    cudaFree(c->d_pguess);
     void *fp[] = {c->f32.E, c->f32.N, c->f32.R, c->f32.D, c->f32.x, c->f32.cp, c->f32.dp,
                   c->f64.E, c->f64.N, c->f64.R, c->f64.D, c->f64.x, c->f64.cp, c->f64.dp,
                   c->E64,   c->N64,   c->R64,   c->P64,   c->d_fr,  c->d_fp,  c->d_fq,  c->d_bmean,
@@ -1729,6 +1731,7 @@ static int check_ctrl(const lester_ctrl *c)
     if (c->sc1_sweep < 0 || c->sc1_sweep > 3) return set_err(LES_ERR_ARG, "sc1_sweep %d out of 0..3", c->sc1_sweep);
     if (c->wait_limit < 0) return set_err(LES_ERR_ARG, "wait_limit %d < 0", c->wait_limit);
     if (c->rb_tile < 0 || c->rb_tile > 1) return set_err(LES_ERR_ARG, "rb_tile %d not 0 or 1", c->rb_tile);
+    if (c->p_guess < 0 || c->p_guess > 1) return set_err(LES_ERR_ARG, "p_guess %d not 0 or 1", c->p_guess);
     return 0;
 }
 

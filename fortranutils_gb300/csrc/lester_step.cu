@@ -248,6 +248,8 @@ static int step_post(Ctx &c, lester_fields &D, const int *istep)
 // the end; the step counter of the predictors' running means is copied in
 // at the start.  Nothing runs while capturing, so a capture that fails
 // leaves the state as it was and the step runs as launched.
+static int p_guess(Ctx &c, lester_fields &D, const int *istep);
+
 static int step_capture(Ctx &c, lester_fields &D, const int *istep)
 {
     if (c.sg.exec) cudaGraphExecDestroy(c.sg.exec);
@@ -278,6 +280,7 @@ static int step_capture(Ctx &c, lester_fields &D, const int *istep)
         r = set_err(LES_ERR_CUDA, "step graph: status copies");
     if (!r && c.xfer) r = c.xfer->issue_in();  // host inputs: copy nodes
     if (!r) r = step_pre(c, D, istep);
+    if (!r) r = p_guess(c, D, istep);
     if (!r) {
         c.want_norms = false;
         r = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
@@ -404,6 +407,28 @@ static int step_graph_run(Ctx &c, lester_fields &D, const int *istep)
 }
 
 static int step_body(Ctx &c, lester_fields *F, const int *istep);
+
+// The initial pressure of a fast solve with ctrl.p_guess 1: 2 p(n) - p(n-1)
+// once the previous step's solve started from a solution (k_p_guess); the
+// arrays are allocated on a launched step, never while capturing.
+static int p_guess(Ctx &c, lester_fields &D, const int *istep)
+{
+    const int ps = c.c.psolve;
+    if (c.c.p_guess != 1 || (ps != LES_PSOLVE_FP64 && ps != LES_PSOLVE_MIXED)) return 0;
+    if (!c.p_prev) {
+        if (c.capturing) return 0;
+        if (cudaMalloc(&c.p_prev, sizeof(double) * (size_t)c.tot_sg3) != cudaSuccess ||
+            cudaMalloc(&c.d_pguess, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(c.p_prev);
+            c.p_prev = nullptr;
+            return set_err(LES_ERR_NOMEM, "p_guess: previous pressure");
+        }
+        LES_CUDA(cudaMemsetAsync(c.d_pguess, 0xff, sizeof(int), c.stream));  // -1: none
+    }
+    launch_p_guess(D.p, c.p_prev, c.tot_sg3, *istep, c.capturing ? c.d_step + 1 : nullptr, c.d_pguess, c.stream);
+    return 0;
+}
 
 // the step, and its JSON line when a step log is open (lester_gpu_step_log)
 int lester_step(lester_fields *F, const int *istep)
@@ -578,6 +603,7 @@ static int step_body(Ctx &c, lester_fields *F, const int *istep)
     }
     RET(st.issue_in());
     RET(step_pre(c, D, istep));
+    RET(p_guess(c, D, istep));
     c.want_norms = false;
     int rs = lester_lmg_solve(D.ap, D.aw, D.ae, D.as, D.an, D.al, D.ar, D.p, D.s, D.res, nullptr, nullptr);
     c.want_norms = true;

@@ -61,7 +61,7 @@ class Ctrl(C.Structure):
         ("rb_sweeps", C.c_int), ("rb_coarse", C.c_int), ("rb_omega", C.c_double),
         ("exact", C.c_int), ("rb_matfree", C.c_int), ("mg_tail", C.c_int), ("krylov", C.c_int),
         ("rb_line", C.c_int), ("autotune", C.c_int), ("phys32", C.c_int), ("step_graph", C.c_int),
-        ("sc1_sweep", C.c_int), ("wait_limit", C.c_int), ("rb_tile", C.c_int),
+        ("sc1_sweep", C.c_int), ("wait_limit", C.c_int), ("p_guess", C.c_int), ("rb_tile", C.c_int),
     ]
 
 

@@ -165,6 +165,13 @@ typedef struct lester_ctrl {
     int wait_limit;    /* bounded device waits (grid barrier, progress
                           flags): polls before a wait gives up and the call
                           returns LES_ERR_TIMEOUT; 0 = the default (2^24) */
+    int p_guess;       /* initial pressure of lester_step's fast solves:
+                          0 (default) = p(n), as the reference's lmg_solve
+                          starts; 1 = linear extrapolation in time,
+                          2 p(n) - p(n-1), from the second solved step on.
+                          The fast solvers iterate to rtol either way (on
+                          the mixing layer the extrapolated start took 8.15
+                          V-cycles a step against 8.0). */
     int rb_tile;       /* 1: the FP32 solver's point red-black sweeps on a
                           one-block level run as one launch per sweep through
                           shared-memory tiles (both colours, a recomputed

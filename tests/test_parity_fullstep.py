@@ -344,3 +344,30 @@ def test_rb_tile_smoother(graph, gpulib):
     assert mask & 2, mask  # level 1 smoothed by the tiles
     for n in ("u", "v", "w", "p", "sc1"):
         assert rel(got[n], ref[n]) <= 1e-7, (n, rel(got[n], ref[n]))
+
+
+def test_p_guess_extrapolation(gpulib):
+    """ctrl.p_guess: the fast solves starting from 2 p(n) - p(n-1) (1) or
+    from p(n) (0, the default) reach the same fields to the solver's
+    tolerance."""
+    st, ctrl, s = make("box_slip_stretched", psolve=L.PSOLVE_MIXED, rtol=1e-10, exact=0, phys32=1)
+    res = {}
+    for guess in (1, 0):
+        ctrl.p_guess = guess
+        g = s.to("torch")
+        L.gpu_init(st.case.geom(), ctrl)
+        try:
+            cyc = 0
+            for it in range(1, 7):
+                assert S.step(g, it) == 0
+                cyc += L.gpu_solve_stats()["cycles"]
+            L.gpu_sync()
+            res[guess] = (g.to("numpy"), cyc)
+        finally:
+            L.gpu_finalize()
+    (a, ca), (b, cb) = res[1], res[0]
+    # a residual of 1e-10 bounds p's error only up to the operator's
+    # condition number: p within 1e-5, as the FP32 physics' stated bound
+    for n, tol in (("u", 1e-7), ("v", 1e-7), ("w", 1e-7), ("sc1", 1e-7), ("p", 1e-5)):
+        assert rel(a[n], b[n]) <= tol, (n, rel(a[n], b[n]))
+    print(f"\nV-cycles over 6 steps: extrapolated start {ca}, previous p {cb}")
