@@ -343,25 +343,23 @@ __global__ void k_prol_fine(const BlkDev *__restrict__ bc_, const BlkDev *__rest
 // ----------------------------------------------------------------- extrap_p
 // code/extrap_p_block.F:335-366: ghost plane := adjacent interior plane on
 // every side that is neither periodic nor interface, sides 1..6 in turn.
-__global__ void k_extrap_p(const BlkDev *__restrict__ blk, double *__restrict__ p)
+// side s of every block (one launch per side, the sides in the reference's
+// order: an edge point two sides share takes the later side's value)
+__global__ void k_extrap_p(const BlkDev *__restrict__ blk, int s, double *__restrict__ p)
 {
-    const BlkDev b = blk[blockIdx.x];
+    const BlkDev b = blk[blockIdx.y];
+    if (is_per_or_int(b.bc[s - 1])) return;
     const int co[2][4] = {{0, 2, 1, 1}, {0, 3, 3, 2}};
     long st[4] = {0, 1, b.n[0], (long)b.n[0] * b.n[1]};
     int nn[4] = {0, b.n[0], b.n[1], b.n[2]};
-    for (int s = 1; s <= 6; s++) {
-        if (!is_per_or_int(b.bc[s - 1])) {
-            int d1 = (s + 1) / 2, d2 = co[0][d1], d3 = co[1][d1];
-            long base = (s % 2 == 1) ? 0 : st[d1] * (nn[d1] - 1);
-            long io1 = (s % 2 == 0) ? -st[d1] : st[d1];
-            long n = (long)nn[d2] * nn[d3];
-            for (long q = threadIdx.x; q < n; q += blockDim.x) {
-                long kk = q / nn[d2], jj = q - kk * nn[d2];
-                long ijk = b.off3 + base + st[d2] * jj + st[d3] * kk;
-                p[ijk] = p[ijk + io1];
-            }
-        }
-        __syncthreads();
+    int d1 = (s + 1) / 2, d2 = co[0][d1], d3 = co[1][d1];
+    long base = (s % 2 == 1) ? 0 : st[d1] * (nn[d1] - 1);
+    long io1 = (s % 2 == 0) ? -st[d1] : st[d1];
+    long n = (long)nn[d2] * nn[d3];
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        long kk = q / nn[d2], jj = q - kk * nn[d2];
+        long ijk = b.off3 + base + st[d2] * jj + st[d3] * kk;
+        p[ijk] = p[ijk + io1];
     }
 }
 
@@ -642,8 +640,10 @@ void launch_prolong(const BlkDev *bc, const BlkDev *bf, int nb, long maxfine, do
 
 void launch_extrap_p(const BlkDev *blk, int nb, double *p, cudaStream_t st)
 {
-    k_extrap_p<<<nb, 512, 0, st>>>(blk, p);
-    count_launch(1);
+    // a side of a block holds at most 64 k points in these grids; 64 CTAs of
+    // 256 threads per block and side, grid-stride beyond
+    for (int s = 1; s <= 6; s++) k_extrap_p<<<dim3(64, nb), 256, 0, st>>>(blk, s, p);
+    count_launch(6);
 }
 
 void launch_pref(const BlkDev *blk, double *p, long n, double *scratch, cudaStream_t st)

@@ -118,7 +118,7 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
     };
     if (has_inlet(c))
         RET(need({D.u, D.v, D.w, D.sc1, D.rho}));
-    RET(need({D.dkp, D.dkw, D.u, D.rho, D.gam, D.vd_damping}));
+    RET(need({D.dkp, D.dkw, D.u, D.rho, D.vd_damping}));
     for (int q = 0; q < 35; q++) RET(need({m[q]}));
     for (int q = 0; q < 12; q++) RET(need({tw[q]}));
     // ---- ivar = u: the inlet planes (step.F:226)
@@ -152,19 +152,19 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
         }
     };
     F32Scope f32s(c);
-    RET(need({D.sc1, D.sc1var, D.gamsc1, D.sc1dis}));
+    RET(need({D.gam, D.sc1, D.sc1var, D.gamsc1, D.sc1dis}));
     RET(lester_subgrid(D.gam, D.gamsc1, D.u, D.v, D.w, D.sc1, D.rho, D.sc1var, D.sc1dis, D.vd_damping, m[M_DIP],
                        m[M_DIU], m[M_DJP], m[M_DJV], D.dkp, D.dkw, m[M_HIJP], m[M_HJIP], m[M_HKIP], m[M_HKJP],
                        m[M_RP], nullptr, nullptr));
     RET(lester_set_gamsc1_bc(D.sc1, D.gamsc1, D.gamlam, m[M_DIU], m[M_DJV], D.dkp, m[M_RP]));
-    RET(need({D.p, D.hn_sc1}));
+    RET(need({D.hn_sc1}));  // set_sc1 does not read p
     RET(lester_set_sc1(D.u, D.v, D.w, D.p, D.sc1, D.rho, D.gamsc1, D.gamlam, D.hn_sc1, m[M_DIP], m[M_DIU],
                        m[M_RDIV], m[M_DJP], m[M_DJV], m[M_RDJU], m[M_DIDJP], m[M_RDIDJP], m[M_HKIP], m[M_HKJP],
                        m[M_HKIU], m[M_HKJV], m[M_RP], D.dkp, D.dkw, nullptr, nullptr));
     RET(lester_set_sc1_bc(D.sc1));
     RET(lester_set_sc1var(D.u, D.v, D.w, D.sc1, D.rho, D.sc1var, D.sc1dis, m[M_DIP], m[M_DJP], D.dkp, D.dkw,
                           m[M_RP], nullptr, nullptr));
-    RET(need({D.rhonp1, D.temperature}));
+    RET(need({D.temperature}));  // rhonp1: written whole by search_lib, not copied in
     RET(lester_search_lib(D.sc1, D.sc1var, D.rhonp1, D.temperature, nullptr, nullptr, istep, &k.alpha, D.rho,
                           &k.rholo, &k.rhohi));
     RET(lester_set_sc1_bc(D.sc1));
@@ -177,7 +177,7 @@ static int step_pre(Ctx &c, lester_fields &D, const int *istep)
     // the caller's rho is copied back from rhonp1 now
     RET(put({D.rhonp1}));
     if (c.xfer) RET(c.xfer->put_as(D.rhonp1, D.rho));
-    RET(need({D.hn_u}));
+    RET(need({D.p, D.hn_u}));
     {
         RET(lester_set_uv_int(&iU, D.u, D.v, D.w, D.p, D.rho, D.rhonp1, D.gam, D.u_int, D.hn_u, m[M_DIP], m[M_DIU],
                               m[M_DIX], m[M_RDIX], m[M_DJP], m[M_DJU], m[M_DJV], m[M_DJX], m[M_RDJP], m[M_RDJU],
@@ -513,10 +513,10 @@ static int step_body(Ctx &c, lester_fields *F, const int *istep)
     struct F3 {
         double **pp;
         int role;
-    } f3[] = {{&D.u, IO},         {&D.rho, IO},         {&D.gam, IO},        {&D.vd_damping, IO},
-              {&D.v, IO},         {&D.w, IO},           {&D.sc1, IO},        {&D.sc1var, IO},
-              {&D.gamsc1, IO},    {&D.sc1dis, IO},      {&D.gamlam, OUT},    {&D.p, P},
-              {&D.hn_sc1, IO},    {&D.rhonp1, IO},      {&D.temperature, IO}, {&D.hn_u, IO},
+    } f3[] = {{&D.u, IO},         {&D.rho, IO},         {&D.vd_damping, IO}, {&D.v, IO},
+              {&D.w, IO},         {&D.gam, IO},         {&D.sc1, IO},        {&D.sc1var, IO},
+              {&D.gamsc1, IO},    {&D.sc1dis, IO},      {&D.gamlam, OUT},    {&D.hn_sc1, IO},
+              {&D.rhonp1, OUT},   {&D.temperature, IO}, {&D.p, P},           {&D.hn_u, IO},
               {&D.hn_v, IO},      {&D.hn_w, IO},        {&D.rhonm1, OUT},    {&D.u_int, WORK},
               {&D.v_int, WORK},   {&D.w_int, WORK},     {&D.drhonp1dt, WORK}, {&D.srhot, WORK},
               {&D.srhoux, WORK}};

@@ -261,9 +261,9 @@ int lester_gpu_xfer_bytes(long *h2d, long *d2h);
  * each component, coeff_p at istep 1, sour_p, solvers, extrap_p,
  * p_ref_subtract, uvw_adv x3, slipbc, conv_exitbc task 2, swap_rhos).
  * Host arrays: the fields a step reads, or writes only in part (u v w sc1
- * rho rhonp1 hn_* gam gamsc1 sc1var sc1dis vd_damping temperature, level 1
- * of p, metrics, dkp, dkw, the wall arrays), are copied in once per call;
- * the fields the caller reads after the step (those, rhonm1 and gamlam,
+ * rho hn_* gam gamsc1 sc1var sc1dis vd_damping temperature, level 1 of p,
+ * metrics, dkp, dkw, the wall arrays), are copied in once per call; the
+ * fields the caller reads after the step (those, rhonp1, rhonm1 and gamlam,
  * without the metrics) are copied back once.  The copies run on two copy
  * streams beside the step's kernels: each input is waited for just before
  * the first routine that touches it, each output is copied back once the

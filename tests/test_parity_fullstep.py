@@ -130,7 +130,7 @@ def test_host_arrays_fast_path(graph, gpulib):
     host_state_equal(hst, dev, st)
     # per step in: the carried state, p on level 1, metrics and wall
     # arrays; no coefficient or work array
-    carried = ("u v w sc1 rho rhonp1 hn_u hn_v hn_w hn_sc1 gam gamsc1 sc1var sc1dis vd_damping "
+    carried = ("u v w sc1 rho hn_u hn_v hn_w hn_sc1 gam gamsc1 sc1var sc1dis vd_damping "
                "temperature").split()
     want_in = (sum(g[n].size for n in carried + S.TW) + st.case.n3_sg + g["dkp"].size + g["dkw"].size
                + sum(a.size for a in g["metric"].values()))
