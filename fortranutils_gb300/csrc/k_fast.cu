@@ -105,6 +105,11 @@ __global__ void k_delta_tables(const double *__restrict__ dip, const double *__r
     }
 }
 
+// 1 / v correctly rounded, the value of (T)1 / v (IEEE division), from the
+// reciprocal intrinsic without the division's numerator scaling
+__device__ __forceinline__ float rcp_rn(float v) { return __frcp_rn(v); }
+__device__ __forceinline__ double rcp_rn(double v) { return __drcp_rn(v); }
+
 // ---- separable (matrix-free) coefficients ---------------------------------
 // coeff_p's couplings factor into a 2-D (i, j) part and a 1-D k part
 // (code/coeff_p_block.F: ae = rdju/diu * dkp(k), an = rdiv/djv * dkp(k),
@@ -126,7 +131,7 @@ __device__ __forceinline__ void coefs_mf(const BlkDev &b, const MfTab<T> &t, int
     c[3] = t.N2[ij] * nz;
     c[4] = r2 * t.Rz[kk - 1];
     c[5] = r2 * t.Rz[kk];
-    dinv = (T)1 / (((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5]));
+    dinv = rcp_rn((((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5])));
 }
 
 // 2-D factors at k = kr, 1-D factors along the reference column (i0, j0)
@@ -228,17 +233,53 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 }
 
 // ---- red-black SOR half sweep, all blocks of a level ----------------------
-template <typename T>
+// Thread (x, y) of CTA (bx, by, bz): point 2 + 2 (32 bx + x) (+1 by colour)
+// of row j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
+// bi0 + bz / maxnk; no per-thread division.  Ix: the offset type, int when every
+// offset of the multigrid arrays is below 2^31.  Per point the operations
+// of rb_point.
+template <typename T, bool MF, typename Ix>
 __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
                                             const T *__restrict__ E, const T *__restrict__ N,
                                             const T *__restrict__ R, const T *__restrict__ D,
                                             T *__restrict__ x, const T *__restrict__ bb,
-                                            const PushDev *__restrict__ push, MfTab<T> mf)
+                                            const PushDev *__restrict__ push, MfTab<T> mf, int maxnk, int bi0)
 {
-    const BlkDev b = blk[blockIdx.y];
-    int i, j, k;
-    if (!rb_decode(b, blockIdx.x * blockDim.x + threadIdx.x, color, i, j, k)) return;
-    rb_point(b, blockIdx.y, i, j, k, omega, E, N, R, D, x, bb, push, mf);
+    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > n2 - 1 || j > n1 - 1) return;
+    const int i = 2 + 2 * (int)(blockIdx.x * 32 + threadIdx.x) + ((j + k + color) & 1);
+    if (i > n0 - 1) return;
+    const Ix jo = n0, ko = (Ix)n0 * n1;
+    const Ix p = (Ix)blk[bi].off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    T c[6], dinv;
+    if (MF) {
+        const Ix ij = (Ix)blk[bi].off2 + (i - 1) + jo * (j - 1), kk = (Ix)blk[bi].off1k + (k - 1);
+        const T ez = mf.Ez[kk], nz = mf.Nz[kk], r2 = mf.R2[ij];
+        c[0] = mf.E2[ij - 1] * ez;
+        c[1] = mf.E2[ij] * ez;
+        c[2] = mf.N2[ij - jo] * nz;
+        c[3] = mf.N2[ij] * nz;
+        c[4] = r2 * mf.Rz[kk - 1];
+        c[5] = r2 * mf.Rz[kk];
+        dinv = rcp_rn((((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5])));
+    } else {
+        c[0] = E[p - 1];
+        c[1] = E[p];
+        c[2] = N[p - jo];
+        c[3] = N[p];
+        c[4] = R[p - ko];
+        c[5] = R[p];
+        dinv = D[p];
+    }
+    const T *xp = x + p;
+    T s = bb[p] + c[0] * xp[-1] + c[1] * xp[1] + c[2] * xp[-jo] + c[3] * xp[jo] + c[4] * xp[-ko] + c[5] * xp[ko];
+    T xo = xp[0];
+    T xn = xo + omega * (s * dinv - xo);
+    x[p] = xn;
+    if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
+        push_ghosts(push + 6 * bi, blk[bi], i, j, k, xn, x);
 }
 
 // ---- red-black SOR, one full sweep per launch, shared-memory tiles --------
@@ -353,7 +394,7 @@ __global__ void __launch_bounds__(256) k_rb_tile(const BlkDev *__restrict__ blk,
         const T ez = M1[bk], nz = M1[kBK + bk], r2 = M2[4 * sM + bc];
         const T c0 = M2[bc] * ez, c1 = M2[sM + bc] * ez, c2 = M2[2 * sM + bc] * nz, c3 = M2[3 * sM + bc] * nz;
         const T c4 = r2 * M1[2 * kBK + bk], c5 = r2 * M1[3 * kBK + bk];
-        const T dinv = (T)1 / (((c0 + c1) + (c2 + c3)) + (c4 + c5));
+        const T dinv = rcp_rn((((c0 + c1) + (c2 + c3)) + (c4 + c5)));
         const T s = Bs[be] + c0 * X[xe - 1] + c1 * X[xe + 1] + c2 * X[xe - sJ] + c3 * X[xe + sJ] + c4 * X[xe - sK] +
                     c5 * X[xe + sK];
         const T xo = X[xe];
@@ -623,15 +664,17 @@ __global__ void __launch_bounds__(128) k_yline_warp(const BlkDev *__restrict__ b
 // ---- residual + restriction ------------------------------------------------
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
 // children are summed into the coarse right-hand side.
-// residual of the 8 fine children of coarse point (i, j, k), summed
-template <typename T>
+// residual of the 8 fine children of coarse point (i, j, k), summed.  With
+// separable couplings the diagonal is their sum (the value whose
+// reciprocal the smoother takes), so no division; Ix the offset type.
+template <typename T, typename Ix = long>
 __device__ __forceinline__ T rr_point(const BlkDev &f, int i, int j, int k, const T *__restrict__ E,
                                       const T *__restrict__ N, const T *__restrict__ R,
                                       const T *__restrict__ D, const T *__restrict__ x,
                                       const T *__restrict__ bb, const MfTab<T> &mf)
 {
-    long jo = f.n[0], ko = (long)f.n[0] * f.n[1];
-    long p0 = f.off3 + (2 * i - 3) + jo * (2 * j - 3) + ko * (2 * k - 3);
+    const Ix jo = f.n[0], ko = (Ix)f.n[0] * f.n[1];
+    const Ix p0 = (Ix)f.off3 + (2 * i - 3) + jo * (2 * j - 3) + ko * (2 * k - 3);
     T sum = 0;
 #pragma unroll
     for (int dz = 0; dz < 2; dz++)
@@ -639,10 +682,23 @@ __device__ __forceinline__ T rr_point(const BlkDev &f, int i, int j, int k, cons
         for (int dy = 0; dy < 2; dy++)
 #pragma unroll
             for (int dx = 0; dx < 2; dx++) {
-                long p = p0 + dx + jo * dy + ko * dz;
+                const Ix p = p0 + dx + jo * dy + ko * dz;
                 T cf[6], dinv;
                 if (mf.E2) {
-                    coefs_mf(f, mf, 2 * i - 2 + dx, 2 * j - 2 + dy, 2 * k - 2 + dz, cf, dinv);
+                    const Ix ij = (Ix)f.off2 + (2 * i - 3 + dx) + jo * (2 * j - 3 + dy);
+                    const Ix kk = (Ix)f.off1k + (2 * k - 3 + dz);
+                    const T ez = mf.Ez[kk], nz = mf.Nz[kk], r2 = mf.R2[ij];
+                    cf[0] = mf.E2[ij - 1] * ez;
+                    cf[1] = mf.E2[ij] * ez;
+                    cf[2] = mf.N2[ij - jo] * nz;
+                    cf[3] = mf.N2[ij] * nz;
+                    cf[4] = r2 * mf.Rz[kk - 1];
+                    cf[5] = r2 * mf.Rz[kk];
+                    const T ap = ((cf[0] + cf[1]) + (cf[2] + cf[3])) + (cf[4] + cf[5]);
+                    const T ax = cf[0] * x[p - 1] + cf[1] * x[p + 1] + cf[2] * x[p - jo] + cf[3] * x[p + jo] +
+                                 cf[4] * x[p - ko] + cf[5] * x[p + ko];
+                    sum += bb[p] - x[p] * ap + ax;
+                    continue;
                 } else {
                     cf[0] = E[p - 1];
                     cf[1] = E[p];
@@ -660,19 +716,22 @@ __device__ __forceinline__ T rr_point(const BlkDev &f, int i, int j, int k, cons
 }
 
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
-// children are summed into the coarse right-hand side.
-template <typename T>
+// children are summed into the coarse right-hand side.  Thread (x, y) of
+// CTA (bx, by, bz): coarse point i = 2 + 32 bx + x of row j = 2 +
+// blockDim.y by + y of plane k = 2 + bz % maxnk of block bi0 + bz / maxnk.
+template <typename T, typename Ix>
 __global__ void __launch_bounds__(256) k_resid_restrict(
     const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_, const T *__restrict__ E,
     const T *__restrict__ N, const T *__restrict__ R, const T *__restrict__ D,
-    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse, MfTab<T> mf)
+    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse, MfTab<T> mf, int maxnk, int bi0)
 {
-    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= c.ncell) return;
-    int i, j, k;
-    long pc = decode_interior(c, q, i, j, k);
-    bcoarse[pc] = rr_point(f, i, j, k, E, N, R, D, x, bb, mf);
+    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const BlkDev &c = bc_[bi];
+    const int n0 = c.n[0], n1 = c.n[1];
+    const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > c.n[2] - 1 || j > n1 - 1 || i > n0 - 1) return;
+    const Ix pc = (Ix)c.off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
+    bcoarse[pc] = rr_point<T, Ix>(bf_[bi], i, j, k, E, N, R, D, x, bb, mf);
 }
 
 // ---- prolongation + correction --------------------------------------------
@@ -684,20 +743,25 @@ __device__ __forceinline__ int clamp_c(int ic, int n, int lo_int, int hi_int)
     return ic;
 }
 
-// trilinear correction of fine interior point (i, j, k) at pf
-template <typename T>
+// trilinear correction of fine interior point (i, j, k) at pf; Ix the
+// offset type (int when every offset of the arrays is below 2^31)
+template <typename T, typename Ix = long>
 __device__ __forceinline__ void prolong_point(const BlkDev &c, const BlkDev &f, int bi, int i, int j,
-                                              int k, long pf, const T *__restrict__ xc,
+                                              int k, Ix pf, const T *__restrict__ xc,
                                               T *__restrict__ xf, const PushDev *__restrict__ push)
 {
     int ic = (i + 1) >> 1, a = (i + 1) & 1;
     int jc = (j + 1) >> 1, bq = (j + 1) & 1;
     int kc = (k + 1) >> 1, cq = (k + 1) & 1;
-    const T w[4] = {(T)0.421875, (T)0.140625, (T)0.046875, (T)0.015625};
+    // trilinear weights by the number h of axes on which the coarse point
+    // is the far one: (3/4)^(3-h) (1/4)^h
+    auto w = [](int h) -> T {
+        return h == 0 ? (T)0.421875 : h == 1 ? (T)0.140625 : h == 2 ? (T)0.046875 : (T)0.015625;
+    };
     bool iw = c.bc[0] == LES_BCT_INTERFACE_D, ie = c.bc[1] == LES_BCT_INTERFACE_D;
     bool js = c.bc[2] == LES_BCT_INTERFACE_D, jn = c.bc[3] == LES_BCT_INTERFACE_D;
     bool kl = c.bc[4] == LES_BCT_INTERFACE_D, kr = c.bc[5] == LES_BCT_INTERFACE_D;
-    long joc = c.n[0], koc = (long)c.n[0] * c.n[1];
+    const Ix joc = c.n[0], koc = (Ix)c.n[0] * c.n[1], oc = (Ix)c.off3;
     T cr = 0;
 #pragma unroll
     for (int sz = 0; sz < 2; sz++)
@@ -709,25 +773,30 @@ __device__ __forceinline__ void prolong_point(const BlkDev &c, const BlkDev &f, 
                 int ii = clamp_c<T>(ic + sx, c.n[0], iw, ie);
                 int jj = clamp_c<T>(jc + sy, c.n[1], js, jn);
                 int kk = clamp_c<T>(kc + sz, c.n[2], kl, kr);
-                cr += w[h] * xc[c.off3 + (ii - 1) + joc * (jj - 1) + koc * (kk - 1)];
+                cr += w(h) * xc[oc + (ii - 1) + joc * (jj - 1) + koc * (kk - 1)];
             }
     T v = xf[pf] + cr;
     xf[pf] = v;
-    if (push) push_ghosts(push + 6 * bi, f, i, j, k, v, xf);
+    if (push && (i == 2 || i == f.n[0] - 1 || j == 2 || j == f.n[1] - 1 || k == 2 || k == f.n[2] - 1))
+        push_ghosts(push + 6 * bi, f, i, j, k, v, xf);
 }
 
-template <typename T>
+// Thread (x, y) of CTA (bx, by, bz): fine point i = 2 + 32 bx + x of row
+// j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
+// bi0 + bz / maxnk (no per-thread division)
+template <typename T, typename Ix>
 __global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
                                                  const BlkDev *__restrict__ bf_,
                                                  const T *__restrict__ xc, T *__restrict__ xf,
-                                                 const PushDev *__restrict__ push)
+                                                 const PushDev *__restrict__ push, int maxnk, int bi0)
 {
-    const BlkDev c = bc_[blockIdx.y], f = bf_[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= f.ncell) return;
-    int i, j, k;
-    long pf = decode_interior(f, q, i, j, k);
-    prolong_point(c, f, blockIdx.y, i, j, k, pf, xc, xf, push);
+    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const BlkDev &f = bf_[bi];
+    const int n0 = f.n[0], n1 = f.n[1];
+    const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > f.n[2] - 1 || j > n1 - 1 || i > n0 - 1) return;
+    const Ix pf = (Ix)f.off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
+    prolong_point<T, Ix>(bc_[bi], f, bi, i, j, k, pf, xc, xf, push);
 }
 
 // ---- halo for the fast solvers ---------------------------------------------
@@ -1223,15 +1292,33 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
     return 0;
 }
 
-// maxhalf = max over blocks of ((ni + 1) / 2) * nj * nk
+// maxn: the most points (ghosts included) of a block along i, j, k;
+// threads per CTA 128, 256 or 512 (4, 8 or 16 rows of 32); wide: 64-bit
+// offsets (the multigrid arrays hold 2^31 points or more)
 template <typename T>
-void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
+void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, cudaStream_t st)
+               const MfTab<T> &mf, int threads, bool wide, cudaStream_t st)
 {
-    const int t = (threads == 128 || threads == 512) ? threads : 256;
-    k_rb<T><<<dim3(nb_(maxhalf, t), nb), t, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf);
-    count_launch(1);
+    const int rows = (threads == 128 || threads == 512) ? threads / 32 : 8;
+    const int maxnk = maxn[2] - 2;
+    // gridDim.z <= 65535: blocks in groups of at most 65535 / maxnk
+    const int per = std::max(1, 65535 / maxnk);
+    for (int bi0 = 0; bi0 < nb; bi0 += per) {
+        const int nbl = std::min(per, nb - bi0);
+        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)(maxnk * nbl));
+        const dim3 cta(32, rows);
+        if (!wide && mf.E2)
+            k_rb<T, true, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+        else if (!wide)
+            k_rb<T, false, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+        else if (mf.E2)
+            k_rb<T, true, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+        else
+            k_rb<T, false, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk,
+                                                       bi0);
+        count_launch(1);
+    }
 }
 
 template <typename T> __global__ void k_copy_range(const T *__restrict__ src, T *__restrict__ dst, long n)
@@ -1274,20 +1361,36 @@ void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double 
 }
 
 template <typename T>
-void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
+void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_c[3], const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           const MfTab<T> &mf, cudaStream_t st)
+                           const MfTab<T> &mf, bool wide, cudaStream_t st)
 {
-    k_resid_restrict<T><<<dim3(nb_(maxcell_c, 256), nb), 256, 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf);
-    count_launch(1);
+    const int maxnk = maxn_c[2] - 2, per = std::max(1, 65535 / maxnk);
+    for (int bi0 = 0; bi0 < nb; bi0 += per) {
+        const dim3 grid(nb_(maxn_c[0] - 2, 32), nb_(maxn_c[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+        if (wide)
+            k_resid_restrict<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, maxnk,
+                                                                    bi0);
+        else
+            k_resid_restrict<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, maxnk,
+                                                                   bi0);
+        count_launch(1);
+    }
 }
 
 template <typename T>
-void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
-                         T *xf, const PushDev *push, cudaStream_t st)
+void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_f[3], const T *xc,
+                         T *xf, const PushDev *push, bool wide, cudaStream_t st)
 {
-    k_prolong<T><<<dim3(nb_(maxcell_f, 256), nb), 256, 0, st>>>(bc, bf, xc, xf, push);
-    count_launch(1);
+    const int maxnk = maxn_f[2] - 2, per = std::max(1, 65535 / maxnk);
+    for (int bi0 = 0; bi0 < nb; bi0 += per) {
+        const dim3 grid(nb_(maxn_f[0] - 2, 32), nb_(maxn_f[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+        if (wide)
+            k_prolong<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+        else
+            k_prolong<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+        count_launch(1);
+    }
 }
 
 template <typename T>
@@ -1475,15 +1578,15 @@ bool prepare_rb_tile()
     template int launch_conv_coef<T>(const BlkDev *, int, long, const double *const *, T *, T *,   \
                                      T *, T *, double *, double *, double *, double *, int *,     \
                                      cudaStream_t);                                                \
-    template void launch_rb<T>(const BlkDev *, int, long, int, double, const T *, const T *,      \
+    template void launch_rb<T>(const BlkDev *, int, const int *, int, double, const T *, const T *, \
                                const T *, const T *, T *, const T *, const PushDev *,             \
-                               const MfTab<T> &, int, cudaStream_t);                              \
+                               const MfTab<T> &, int, bool, cudaStream_t);                        \
     template void launch_yline<T>(const BlkDev *, int, long, int, double, const T *, const T *,   \
                                   const T *, const T *, T *, const T *, const MfTab<T> &, T *, T *, \
                                   int, cudaStream_t);                                             \
-    template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, long, const T *,  \
+    template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, const int *, const T *, \
                                            const T *, const T *, const T *, const T *, const T *, \
-                                           T *, const MfTab<T> &, cudaStream_t);                  \
+                                           T *, const MfTab<T> &, bool, cudaStream_t);            \
     template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
                                   long, long, const CoarseDirect<T> &, cudaStream_t);             \
@@ -1496,8 +1599,8 @@ bool prepare_rb_tile()
     template void launch_mf_tables<T>(const BlkDev *, int, long, long, int, const T *, const T *, \
                                       const T *, const T *, const MfTab<T> &, double, int *,      \
                                       cudaStream_t);                                              \
-    template void launch_prolong_fast<T>(const BlkDev *, const BlkDev *, int, long, const T *,    \
-                                         T *, const PushDev *, cudaStream_t);                     \
+    template void launch_prolong_fast<T>(const BlkDev *, const BlkDev *, int, const int *, const T *, \
+                                         T *, const PushDev *, bool, cudaStream_t);               \
     template void launch_halo_fast<T>(const FaceDev *, int, long, T *, cudaStream_t);             \
     template void launch_resid_outer<T>(const BlkDev *, int, long, const double *,                \
                                         const double *, const double *, const double *,           \

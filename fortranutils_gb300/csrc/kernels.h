@@ -77,10 +77,13 @@ template <typename T>
 int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *const *a, T *E, T *N,
                      T *R, T *D, double *E64, double *N64, double *R64, double *P64, int *bad,
                      cudaStream_t st);
+// red-black half sweep: CTAs of `threads` (128, 256, 512) = 32 points of a
+// row x 4, 8 or 16 rows; maxn: the most points of a block along i, j, k
+// (ghosts included); wide: 64-bit offsets (arrays of 2^31 points or more)
 template <typename T>
-void launch_rb(const BlkDev *blk, int nb, long maxhalf, int color, double omega, const T *E,
+void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, cudaStream_t st);
+               const MfTab<T> &mf, int threads, bool wide, cudaStream_t st);
 // y-line zebra relaxation of one colour of (i, k) columns (maxik_half: the
 // most columns of one colour in a block)
 template <typename T>
@@ -88,9 +91,9 @@ void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double 
                   const T *R, const T *D, T *x, const T *b, const MfTab<T> &mf, T *cp, T *dp, int maxnj,
                   cudaStream_t st);
 template <typename T>
-void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_c, const T *E,
+void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_c[3], const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           const MfTab<T> &mf, cudaStream_t st);
+                           const MfTab<T> &mf, bool wide, cudaStream_t st);
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
@@ -115,8 +118,8 @@ void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int m
                       const T *N, const T *R, const T *D, const MfTab<T> &t, double tol, int *bad,
                       cudaStream_t st);
 template <typename T>
-void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, long maxcell_f, const T *xc,
-                         T *xf, const PushDev *push, cudaStream_t st);
+void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_f[3], const T *xc,
+                         T *xf, const PushDev *push, bool wide, cudaStream_t st);
 template <typename T>
 void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
 template <typename T>

@@ -18,6 +18,7 @@ struct LevelGeom {
     long off3[LES_MAXBL + 1], off2[LES_MAXBL + 1], off1k[LES_MAXBL + 1];
     long offxy[LES_MAXBL + 1], offz[LES_MAXBL + 1];
     long maxcell, maxjk, maxhalf, maxfine, maxik, maxface, maxij, maxk;
+    int maxn[3];  // the most points of a block along i, j, k (ghosts included)
     long start3, len3;     // contiguous range of this level in a 3-D mg field
     double npts_all;       // interior points, pressure loop bounds (set_loop_bound.F:364)
     BlkDev *d_blk = nullptr;

@@ -308,6 +308,7 @@ static int build_levels(Ctx &c)
         LevelGeom &L = c.lv[lev];
         L.start3 = o3;
         L.maxcell = L.maxjk = L.maxhalf = L.maxfine = L.maxik = L.maxij = L.maxk = 0;
+        L.maxn[0] = L.maxn[1] = L.maxn[2] = 0;
         double npts = 0;
         for (int b = 1; b <= nb; b++) {
             int *n = L.n[b];
@@ -333,6 +334,7 @@ static int build_levels(Ctx &c)
             L.maxik = std::max(L.maxik, (long)n[0] * (n[2] - 2));
             L.maxij = std::max(L.maxij, (long)n[0] * n[1]);
             L.maxk = std::max(L.maxk, (long)n[2]);
+            for (int d = 0; d < 3; d++) L.maxn[d] = std::max(L.maxn[d], n[d]);
             npts += (double)(n[0] - 2) * (double)(n[1] - 2) * (double)(n[2] - 2);
         }
         L.npts_all = npts;
@@ -1125,9 +1127,9 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             // node whose timestamps can be read after each replay
             unsigned fl = cap ? cudaEventRecordExternal : cudaEventRecordDefault;
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
-            launch_rb<T>(L.d_blk, c.g.numbl, L.maxhalf, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
+            launch_rb<T>(L.d_blk, c.g.numbl, L.maxn, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
                          F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.rb_threads,
-                         c.stream);
+                         c.tot3 >= (1L << 31), c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
@@ -1177,8 +1179,8 @@ template <typename T> static void fast_vcycle(Ctx &c)
     for (int lev = 1; lev < Lr; lev++) {
         fast_smooth<T>(c, lev, pre);
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
-        launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxcell, F.E, F.N, F.R, F.D, F.x,
-                                 F.b, F.b, mf, c.stream);
+        launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxn, F.E, F.N, F.R, F.D, F.x,
+                                 F.b, F.b, mf, c.tot3 >= (1L << 31), c.stream);
     }
     if (l0) {
         // levels l0..L are one contiguous slice of the multigrid arrays
@@ -1191,7 +1193,8 @@ template <typename T> static void fast_vcycle(Ctx &c)
     }
     for (int lev = Lr - 1; lev >= 1; lev--) {
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
-        launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxcell, F.x, F.x, Lf.d_push, c.stream);
+        launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxn, F.x, F.x, Lf.d_push, c.tot3 >= (1L << 31),
+                               c.stream);
         fast_smooth<T>(c, lev, pre);
     }
 }
