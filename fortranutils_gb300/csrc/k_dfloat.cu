@@ -17,6 +17,8 @@
 // takes it, and the converged p is converted back to FP64 and confirmed by
 // one FP64 residual (k_resid_outer), so the tolerance is met in FP64.
 // Compiled without FMA contraction: every FMA below is written out.
+#include <algorithm>
+
 #include "k_common.cuh"
 #include "kernels.h"
 
@@ -109,18 +111,23 @@ __global__ void k_df_join(const float2 *__restrict__ src, double *__restrict__ d
     }
 }
 
-// p += e on the interior of level 1, ghosts pushed as k_update does
+// p += e on the interior of level 1, ghosts pushed as k_update does.
+// Thread (x, y) of CTA (bx, by, bz): point i = 2 + 32 bx + x of row
+// j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
+// bi0 + bz / maxnk.
+template <typename Ix>
 __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__ p, const float *__restrict__ e,
-                            const PushDev *__restrict__ push)
+                            const PushDev *__restrict__ push, int maxnk, int bi0)
 {
-    const BlkDev b = blk[blockIdx.y];
-    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= b.ncell) return;
-    int i, j, k;
-    const long pp = decode_interior(b, q, i, j, k);
+    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
+    const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > n2 - 1 || j > n1 - 1 || i > n0 - 1) return;
+    const Ix pp = (Ix)blk[bi].off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
     const float2 v = df_add_f(p[pp], e[pp]);
     p[pp] = v;
-    if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, v, p);
+    if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
+        push_ghosts(push + 6 * bi, blk[bi], i, j, k, v, p);
 }
 
 // r = b - A p in double-float (E, N, R, P as in k_resid_outer): r rounded
@@ -128,7 +135,8 @@ __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__
 // in FP64 (an FP32 square overflows above 1.8e19, which a diverging cycle
 // reaches; summing in FP32 within [2^-60, 2^60] and in FP64 outside
 // measured slower, 119 against 88 us on the mixing layer's level 1).
-// Grid-stride over the block's interior points, i fastest.
+// A warp per (j, k) row of the block's interior, grid-stride over rows,
+// lanes along i.
 __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk, const float2 *__restrict__ E,
                                                   const float2 *__restrict__ N, const float2 *__restrict__ R,
                                                   const float2 *__restrict__ P, const float2 *__restrict__ x,
@@ -136,14 +144,16 @@ __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk
                                                   double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
-    const unsigned ni = (unsigned)(b.n[0] - 2), nj = (unsigned)(b.n[1] - 2);
-    const unsigned npt = (unsigned)b.ncell;
+    const int ni = b.n[0] - 2;
+    const unsigned nj = (unsigned)(b.n[1] - 2), nrow = nj * (unsigned)(b.n[2] - 2);
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const unsigned wpb = blockDim.x >> 5;
     double acc = 0.;
-    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < npt; q += gridDim.x * blockDim.x) {
-        const unsigned row = q / ni, k = row / nj;
-        {
-            const long p = b.off3 + (long)(q - row * ni + 1) + jo * (long)(row - k * nj + 1) + ko * (long)(k + 1);
+    for (unsigned row = blockIdx.x * wpb + (threadIdx.x >> 5); row < nrow; row += gridDim.x * wpb) {
+        const unsigned k = row / nj;
+        const long base = b.off3 + 1 + jo * (long)(row - k * nj + 1) + ko * (long)(k + 1);
+        for (int iq = threadIdx.x & 31; iq < ni; iq += 32) {
+            const long p = base + iq;
             float2 r = df_add_lo(bb[p], df_neg(df_mul(P[p], x[p])));
             r = df_add_lo(r, df_mul(E[p - 1], x[p - 1]));
             r = df_add_lo(r, df_mul(E[p], x[p + 1]));
@@ -200,19 +210,29 @@ void launch_df_join(const float2 *src, double *dst, long n, const double *cycles
     count_launch(1);
 }
 
-void launch_df_update(const BlkDev *blk, int nb, long maxcell, float2 *p, const float *e, const PushDev *push,
-                      cudaStream_t st)
+void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, const float *e, const PushDev *push,
+                      bool wide, cudaStream_t st)
 {
-    k_df_update<<<dim3((unsigned)((maxcell + 255) / 256), nb), 256, 0, st>>>(blk, p, e, push);
-    count_launch(1);
+    const int maxnk = maxn[2] - 2, per = std::max(1, 65535 / maxnk);
+    for (int bi0 = 0; bi0 < nb; bi0 += per) {
+        const dim3 grid((unsigned)(maxn[0] + 29) / 32, (unsigned)(maxn[1] + 5) / 8,
+                        (unsigned)(maxnk * std::min(per, nb - bi0)));
+        if (wide)
+            k_df_update<long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+        else
+            k_df_update<int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+        count_launch(1);
+    }
 }
 
-void launch_df_resid(const BlkDev *blk, int nb, long maxcell, const float2 *E, const float2 *N, const float2 *R,
+void launch_df_resid(const BlkDev *blk, int nb, long maxrow, const float2 *E, const float2 *N, const float2 *R,
                      const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
                      cudaStream_t st)
 {
-    // a few CTAs per SM, so that the final sum reads few partials
-    unsigned gx = cap_grid(maxcell, 256, (unsigned)((1216 + nb - 1) / nb));
+    // a few CTAs per SM (so that the final sum reads few partials), every
+    // warp the same number of rows
+    const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
+    const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
     k_df_resid<<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, rT, partial);
     k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
     count_launch(2);

@@ -97,7 +97,10 @@ __global__ void k_coeff_p(const BlkDev *__restrict__ blk, const double *__restri
 // ------------------------------------------------------------------- sour_p
 // code/sour_p_block.F:161-241; every face flux of the running-flux loops is
 // recomputed from the same operands, so the values are identical.
-__global__ void k_sour_p(const BlkDev *__restrict__ blk, double dtime,
+// ddtime = 2 / (3 dtime) * 0.5, cdtime = 2 / (3 dtime), rdtime = 1 / dtime,
+// formed once on the host (the same IEEE operations): GB300's FP64 pipe
+// made the three divisions per point the larger part of the kernel
+__global__ void k_sour_p(const BlkDev *__restrict__ blk, double ddtime, double cdtime, double rdtime,
                          const double *__restrict__ rdiv, const double *__restrict__ rdju,
                          const double *__restrict__ didjp, const double *__restrict__ dkp,
                          const double *__restrict__ rdidjp, const double *__restrict__ dkw,
@@ -113,9 +116,6 @@ __global__ void k_sour_p(const BlkDev *__restrict__ blk, double dtime,
     int i, j, k;
     long p = decode_interior(b, q, i, j, k);
     long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-    double ddtime = 2.0 / (3.0 * dtime) * 0.5;
-    double cdtime = 2.0 / (3.0 * dtime);
-    double rdtime = 1.0 / dtime;
     double dkpk = dkp[b.off1k + k - 1];
     double gwf = rdju[IDX2(b, i, j)] * dkpk * (rhonp1[p] + rhonp1[p - 1]) * u[p];
     double gef = rdju[IDX2(b, i + 1, j)] * dkpk * (rhonp1[p] + rhonp1[p + 1]) * u[p + 1];
@@ -584,8 +584,9 @@ void launch_sour_p(const BlkDev *blk, int nb, long maxcell, double dtime, const 
                    const double *w, const double *rho, const double *rhonp1, double *drhodt,
                    double *s, double *srhot, double *srhoux, cudaStream_t st)
 {
-    k_sour_p<<<dim3(nblk(maxcell, 128), nb), 128, 0, st>>>(blk, dtime, rdiv, rdju, didjp, dkp, rdidjp,
-                                                         dkw, u, v, w, rho, rhonp1, drhodt, s, srhot,
+    const double cdtime = 2.0 / (3.0 * dtime), ddtime = cdtime * 0.5, rdtime = 1.0 / dtime;
+    k_sour_p<<<dim3(nblk(maxcell, 128), nb), 128, 0, st>>>(blk, ddtime, cdtime, rdtime, rdiv, rdju, didjp, dkp,
+                                                         rdidjp, dkw, u, v, w, rho, rhonp1, drhodt, s, srhot,
                                                          srhoux);
     count_launch(1);
 }

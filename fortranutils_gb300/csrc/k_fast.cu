@@ -1114,21 +1114,25 @@ __global__ void __launch_bounds__(256) k_resid_outer(
     double *__restrict__ r64, double *__restrict__ partial)
 {
     const BlkDev b = blk[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     double v[2] = {0., 0.};
     const double s0 = shift ? shift[blockIdx.y] : 0.;
-    for (; q < b.ncell; q += (long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        long p = decode_interior(b, q, i, j, k);
-        long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
-        const double bp = bb[p] - s0;
-        double r = bp - P[p] * x[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] +
-                   N[p - jo] * x[p - jo] + N[p] * x[p + jo] + R[p - ko] * x[p - ko] +
-                   R[p] * x[p + ko];
-        rT[p] = (T)r;
-        if (r64) r64[p] = r;
-        v[0] += r * r;
-        v[1] += bp * bp;
+    // a warp per (j, k) row of the interior, grid-stride over rows
+    const int ni = b.n[0] - 2;
+    const unsigned nj = (unsigned)(b.n[1] - 2), nrow = nj * (unsigned)(b.n[2] - 2), wpb = blockDim.x >> 5;
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    for (unsigned row = blockIdx.x * wpb + (threadIdx.x >> 5); row < nrow; row += gridDim.x * wpb) {
+        const unsigned kq = row / nj;
+        const long base = b.off3 + 1 + jo * (long)(row - kq * nj + 1) + ko * (long)(kq + 1);
+        for (int iq = threadIdx.x & 31; iq < ni; iq += 32) {
+            const long p = base + iq;
+            const double bp = bb[p] - s0;
+            double r = bp - P[p] * x[p] + E[p - 1] * x[p - 1] + E[p] * x[p + 1] + N[p - jo] * x[p - jo] +
+                       N[p] * x[p + jo] + R[p - ko] * x[p - ko] + R[p] * x[p + ko];
+            rT[p] = (T)r;
+            if (r64) r64[p] = r;
+            v[0] += r * r;
+            v[1] += bp * bp;
+        }
     }
     block_reduce_store<2>(v, partial + 2 * (blockIdx.y * (long)gridDim.x + blockIdx.x));
 }
@@ -1178,19 +1182,22 @@ __global__ void k_coarse_mean(const BlkDev *__restrict__ blk, int nb, T *__restr
     remove_comp_means<T>(blk, nb, bb);
 }
 
-// p += e on the interior of level 1
-template <typename T>
+// p += e on the interior of level 1.  Thread (x, y) of CTA (bx, by, bz):
+// point i = 2 + 32 bx + x of row j = 2 + blockDim.y by + y of plane
+// k = 2 + bz % maxnk of block bi0 + bz / maxnk.
+template <typename T, typename Ix>
 __global__ void k_update(const BlkDev *__restrict__ blk, double *__restrict__ p,
-                         const T *__restrict__ e, const PushDev *__restrict__ push)
+                         const T *__restrict__ e, const PushDev *__restrict__ push, int maxnk, int bi0)
 {
-    const BlkDev b = blk[blockIdx.y];
-    long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (q >= b.ncell) return;
-    int i, j, k;
-    long pp = decode_interior(b, q, i, j, k);
+    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
+    const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > n2 - 1 || j > n1 - 1 || i > n0 - 1) return;
+    const Ix pp = (Ix)blk[bi].off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
     double v = p[pp] + (double)e[pp];
     p[pp] = v;
-    if (push) push_ghosts(push + 6 * blockIdx.y, b, i, j, k, v, p);
+    if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
+        push_ghosts(push + 6 * bi, blk[bi], i, j, k, v, p);
 }
 
 // ---- flexible conjugate gradients around the V-cycle ----------------------
@@ -1404,15 +1411,15 @@ void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaS
 }
 
 template <typename T>
-void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
+void launch_resid_outer(const BlkDev *blk, int nb, long maxrow, const double *E, const double *N,
                         const double *R, const double *P, const double *x, const double *b,
                         const double *shift, T *rT, double *r64, double *partial, double *out2,
                         cudaStream_t st)
 {
-    // grid-stride: a few CTAs per SM, so the final sum reads few partials
-    unsigned gx = nb_(maxcell, 256);
-    unsigned cap = (unsigned)((1216 + nb - 1) / nb);
-    if (gx > cap) gx = cap;
+    // grid-stride over rows: a few CTAs per SM (so that the final sum reads
+    // few partials), every warp the same number of rows
+    const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
+    const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
     k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, r64, partial);
     k_sum2_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out2);
     count_launch(2);
@@ -1502,11 +1509,18 @@ void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st)
 }
 
 template <typename T>
-void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, const PushDev *push,
-                   cudaStream_t st)
+void launch_update(const BlkDev *blk, int nb, const int maxn[3], double *p, const T *e, const PushDev *push,
+                   bool wide, cudaStream_t st)
 {
-    k_update<T><<<dim3(nb_(maxcell, 256), nb), 256, 0, st>>>(blk, p, e, push);
-    count_launch(1);
+    const int maxnk = maxn[2] - 2, per = std::max(1, 65535 / maxnk);
+    for (int bi0 = 0; bi0 < nb; bi0 += per) {
+        const dim3 grid(nb_(maxn[0] - 2, 32), nb_(maxn[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+        if (wide)
+            k_update<T, long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+        else
+            k_update<T, int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+        count_launch(1);
+    }
 }
 
 template <typename T>
@@ -1610,7 +1624,7 @@ bool prepare_rb_tile()
                                 const double *, const double *, const T *, double *, double *,   \
                                 double *, double *, T *, const PushDev *, double *, double *,    \
                                 double *, cudaStream_t);                                         \
-    template void launch_update<T>(const BlkDev *, int, long, double *, const T *, const PushDev *, \
+    template void launch_update<T>(const BlkDev *, int, const int *, double *, const T *, const PushDev *, bool, \
                                    cudaStream_t);                                                \
     template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);
 INST(float)

@@ -47,9 +47,9 @@ void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b,
                        cudaStream_t st);
 // cycles (nullable, device): skipped when *cycles == 0
 void launch_df_join(const float2 *src, double *dst, long n, const double *cycles, cudaStream_t st);
-void launch_df_update(const BlkDev *blk, int nb, long maxcell, float2 *p, const float *e, const PushDev *push,
-                      cudaStream_t st);
-void launch_df_resid(const BlkDev *blk, int nb, long maxcell, const float2 *E, const float2 *N, const float2 *R,
+void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, const float *e, const PushDev *push,
+                      bool wide, cudaStream_t st);
+void launch_df_resid(const BlkDev *blk, int nb, long maxrow, const float2 *E, const float2 *N, const float2 *R,
                      const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
                      cudaStream_t st);
 // f32: FP32 arithmetic on the FP64 fields (the mixed path with FP32 physics)
@@ -123,7 +123,7 @@ void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int m
 template <typename T>
 void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
 template <typename T>
-void launch_resid_outer(const BlkDev *blk, int nb, long maxcell, const double *E, const double *N,
+void launch_resid_outer(const BlkDev *blk, int nb, long maxrow, const double *E, const double *N,
                         const double *R, const double *P, const double *x, const double *b,
                         const double *shift, T *rT, double *r64, double *partial, double *out2,
                         cudaStream_t st);
@@ -138,8 +138,8 @@ void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const 
 void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double *b, double *partial,
                           double *out, cudaStream_t st);
 template <typename T>
-void launch_update(const BlkDev *blk, int nb, long maxcell, double *p, const T *e, const PushDev *push,
-                   cudaStream_t st);
+void launch_update(const BlkDev *blk, int nb, const int maxn[3], double *p, const T *e, const PushDev *push,
+                   bool wide, cudaStream_t st);
 template <typename T>
 void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st);
 

@@ -1214,8 +1214,8 @@ static void df_cycle_tail(Ctx &c, float *e, float *rT)
 {
     LevelGeom &L1 = c.lv[1];
     const int nb = c.g.numbl;
-    launch_df_update(L1.d_blk, nb, L1.maxcell, c.df_p, e, L1.d_push, c.stream);
-    launch_df_resid(L1.d_blk, nb, L1.maxcell, c.df_E, c.df_N, c.df_R, c.df_P, c.df_p, c.df_b, rT, c.d_partial,
+    launch_df_update(L1.d_blk, nb, L1.maxn, c.df_p, e, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+    launch_df_resid(L1.d_blk, nb, L1.maxjk, c.df_E, c.df_N, c.df_R, c.df_P, c.df_p, c.df_b, rT, c.d_partial,
                     c.d_small, c.stream);
 }
 
@@ -1263,8 +1263,8 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
         } else if (df) {
             df_cycle_tail(c, (float *)F.x, (float *)F.b);
         } else {
-            launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
-            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+            launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                                   c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial,
                                   c.d_small, c.stream);
         }
@@ -1388,7 +1388,7 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     launch_halo_fast<double>(L1.d_face, L1.nface, L1.maxface, f, c.stream);
     if (c.singular) launch_interior_mean(L1.d_blk, nb, L1.maxcell, b, c.d_partial, c.d_bmean, c.stream);
     if (kry && (r = fcg_reset(c))) return r;
-    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+    launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                           c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial, c.d_small,
                           c.stream);
     cudaGraphConditionalHandle hw;
@@ -1408,8 +1408,8 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     } else if (df) {
         df_cycle_tail(c, (float *)F.x, (float *)F.b);
     } else {
-        launch_update<T>(L1.d_blk, nb, L1.maxcell, f, F.x, L1.d_push, c.stream);
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+        launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                               c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial, c.d_small, c.stream);
     }
     launch_loop_step(hw, c.d_small, c.d_loop, rtol, maxit, c.c.krylov == 2 && !kry, c.stream);
@@ -1420,7 +1420,7 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     // flexible CG's recursive residual, or the double-float one, confirmed
     // against b - A p in FP64
     if (kry || df)
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                               c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial, c.d_small,
                               c.stream);
     launch_loop_gate(c.sg_post, c.d_small, c.d_loop, rtol, kry || df, c.stream);
@@ -1476,7 +1476,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
     bool kry = c.c.krylov == 1 || forced;
     const bool may_switch = c.c.krylov == 2;
     if (kry && (r = fcg_reset(c))) return r;
-    launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+    launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                           c.singular ? c.d_bmean : nullptr, F.b, kry ? c.d_fr : nullptr, c.d_partial,
                           c.d_small, c.stream);
     STAGE_CHECK("initial residual");
@@ -1494,7 +1494,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
         if (!df) return 0;
         df = false;
         launch_df_join(c.df_p, f, c.tot_sg3, nullptr, c.stream);
-        launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+        launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                               c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial, c.d_small, c.stream);
         int rr = sync_small(c, 2);
         if (rr) return rr;
@@ -1538,7 +1538,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
             if ((r = df_leave())) return r;
             kry = true;
             if ((r = fcg_reset(c))) return r;
-            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                                   c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
                                   c.stream);
             if ((r = sync_small(c, 2))) return r;
@@ -1548,7 +1548,7 @@ template <typename T> static int fast_solve_run(Ctx &c, const Coef &A, double *f
         if (kry && rel <= rtol) {
             // the CG residual is updated recursively: confirm with b - A p,
             // and restart from it (beta = 0) if rounding has drifted
-            launch_resid_outer<T>(L1.d_blk, nb, L1.maxcell, c.E64, c.N64, c.R64, c.P64, f, b,
+            launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                                   c.singular ? c.d_bmean : nullptr, F.b, c.d_fr, c.d_partial, c.d_small,
                                   c.stream);
             if ((r = sync_small(c, 2))) return r;
