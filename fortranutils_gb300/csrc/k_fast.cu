@@ -781,22 +781,65 @@ __device__ __forceinline__ void prolong_point(const BlkDev &c, const BlkDev &f, 
         push_ghosts(push + 6 * bi, f, i, j, k, v, xf);
 }
 
-// Thread (x, y) of CTA (bx, by, bz): fine point i = 2 + 32 bx + x of row
-// j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
-// bi0 + bz / maxnk (no per-thread division)
+// Thread (x, y) of CTA (bx, by, bz): the fine points 2c - 1 and 2c along
+// each axis (c = 1 + 32 bx + x, 1 + blockDim.y by + y, 1 + bz % maxnk of
+// block bi0 + bz / maxnk; coarse c up to n - 1), i.e. the fine points whose
+// coarse stencil is the 2 x 2 x 2 coarse points c..c+1 (clamped as
+// prolong_point clamps).  The eight coarse values are loaded once for up to
+// eight fine points; each fine point sums them in prolong_point's order.
 template <typename T, typename Ix>
-__global__ void __launch_bounds__(256) k_prolong(const BlkDev *__restrict__ bc_,
-                                                 const BlkDev *__restrict__ bf_,
-                                                 const T *__restrict__ xc, T *__restrict__ xf,
-                                                 const PushDev *__restrict__ push, int maxnk, int bi0)
+__global__ void __launch_bounds__(256) k_prolong8(const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_,
+                                                  const T *__restrict__ xc, T *__restrict__ xf,
+                                                  const PushDev *__restrict__ push, int maxnk, int bi0)
 {
-    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
-    const BlkDev &f = bf_[bi];
-    const int n0 = f.n[0], n1 = f.n[1];
-    const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
-    if (k > f.n[2] - 1 || j > n1 - 1 || i > n0 - 1) return;
-    const Ix pf = (Ix)f.off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
-    prolong_point<T, Ix>(bc_[bi], f, bi, i, j, k, pf, xc, xf, push);
+    const int bz = (int)blockIdx.z / maxnk, cz = (int)blockIdx.z - bz * maxnk + 1, bi = bi0 + bz;
+    const BlkDev &c = bc_[bi], &f = bf_[bi];
+    const int cx = (int)(blockIdx.x * 32 + threadIdx.x) + 1, cy = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 1;
+    if (cx > c.n[0] - 1 || cy > c.n[1] - 1 || cz > c.n[2] - 1) return;
+    const bool iw = c.bc[0] == LES_BCT_INTERFACE_D, ie = c.bc[1] == LES_BCT_INTERFACE_D;
+    const bool js = c.bc[2] == LES_BCT_INTERFACE_D, jn = c.bc[3] == LES_BCT_INTERFACE_D;
+    const bool kl = c.bc[4] == LES_BCT_INTERFACE_D, kr = c.bc[5] == LES_BCT_INTERFACE_D;
+    const Ix joc = c.n[0], koc = (Ix)c.n[0] * c.n[1], oc = (Ix)c.off3;
+    T v[2][2][2];
+#pragma unroll
+    for (int sz = 0; sz < 2; sz++)
+#pragma unroll
+        for (int sy = 0; sy < 2; sy++)
+#pragma unroll
+            for (int sx = 0; sx < 2; sx++) {
+                const int ii = clamp_c<T>(cx + sx, c.n[0], iw, ie);
+                const int jj = clamp_c<T>(cy + sy, c.n[1], js, jn);
+                const int kk = clamp_c<T>(cz + sz, c.n[2], kl, kr);
+                v[sz][sy][sx] = xc[oc + (ii - 1) + joc * (jj - 1) + koc * (kk - 1)];
+            }
+    auto w = [](int h) -> T {
+        return h == 0 ? (T)0.421875 : h == 1 ? (T)0.140625 : h == 2 ? (T)0.046875 : (T)0.015625;
+    };
+    const int n0 = f.n[0], n1 = f.n[1], n2 = f.n[2];
+    const Ix jo = n0, ko = (Ix)n0 * n1, of = (Ix)f.off3;
+#pragma unroll
+    for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+        for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+            for (int dx = 0; dx < 2; dx++) {
+                // fine point (2c - 1 + d): its coarse index is c and (i + 1) & 1 = d
+                const int i = 2 * cx - 1 + dx, j = 2 * cy - 1 + dy, k = 2 * cz - 1 + dz;
+                if (i < 2 || i > n0 - 1 || j < 2 || j > n1 - 1 || k < 2 || k > n2 - 1) continue;
+                T cr = 0;
+#pragma unroll
+                for (int sz = 0; sz < 2; sz++)
+#pragma unroll
+                    for (int sy = 0; sy < 2; sy++)
+#pragma unroll
+                        for (int sx = 0; sx < 2; sx++)
+                            cr += w((sx != dx) + (sy != dy) + (sz != dz)) * v[sz][sy][sx];
+                const Ix pf = of + (i - 1) + jo * (j - 1) + ko * (k - 1);
+                const T val = xf[pf] + cr;
+                xf[pf] = val;
+                if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
+                    push_ghosts(push + 6 * bi, f, i, j, k, val, xf);
+            }
 }
 
 // ---- halo for the fast solvers ---------------------------------------------
@@ -1389,13 +1432,16 @@ template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_f[3], const T *xc,
                          T *xf, const PushDev *push, bool wide, cudaStream_t st)
 {
-    const int maxnk = maxn_f[2] - 2, per = std::max(1, 65535 / maxnk);
+    // a thread per coarse c = 1 .. n_coarse - 1 along each axis: the fine
+    // level has n_fine = 2 n_coarse - 2 points per axis, ghosts included
+    const int mc[3] = {maxn_f[0] / 2 + 1, maxn_f[1] / 2 + 1, maxn_f[2] / 2 + 1};
+    const int maxnk = mc[2] - 1, per = std::max(1, 65535 / maxnk);
     for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const dim3 grid(nb_(maxn_f[0] - 2, 32), nb_(maxn_f[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+        const dim3 grid(nb_(mc[0] - 1, 32), nb_(mc[1] - 1, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
         if (wide)
-            k_prolong<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+            k_prolong8<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
         else
-            k_prolong<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+            k_prolong8<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
         count_launch(1);
     }
 }
