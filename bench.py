@@ -54,7 +54,7 @@ WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch 
 # against 50.3 MB algorithmic); the tile-pipeline scalar sweep from one
 # capture at 128x96x64 (53.1 MB read + 0.08 MB written for 0.786 M cells)
 # scaled by cells to 256x192x128
-TRAFFIC = {"rb": 52.28e6, "sweep": 53.22e6 * 6291456 / 786432}
+TRAFFIC = {"rb": 52.18e6, "sweep": 53.22e6 * 6291456 / 786432}
 # algorithmic bytes per interior cell of one launch: a red-black half sweep
 # (one colour per launch, FP32) must read x of both colours (its own points
 # and their neighbours of the other colour: 4 B per cell), b of its colour
