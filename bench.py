@@ -377,6 +377,7 @@ def run_gpu(args):
             _ranks().barrier()
         L.gpu_prof(False)
         tuned = L.gpu_tuned(32 if mode == "mixed" else 64)
+        forms = L.gpu_solver_forms()
         ms = _ranks().max(e0.elapsed_time(e1))
         kms, kl = L.gpu_prof_read(L.PROF_RB)
         rb_tile = bool(L.gpu_rb_tiles() & 2)  # level 1 smoothed by k_rb_tile
@@ -385,7 +386,7 @@ def run_gpu(args):
                      "relres_max": float(np.max(rel)), "solve_ms": float(np.mean(solve_ms)),
                      "launches": L.gpu_launch_count() - launches0, "rb_ms": kms, "rb_tile": rb_tile,
                      "rb_launches": kl, "sweep_ms": sms, "sweep_launches": sl,
-                     "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned}
+                     "clocks": clk.summary(), "ctrl": ctrl, "tuned": tuned, "forms": forms}
         del g
         if args.step_graph:
             res[mode]["graph"] = run_graph_leg(args, case, ctrl, wl)
@@ -740,7 +741,7 @@ def report(args, rank, world):
                   "graph_vcycles_per_step": mx["graph"]["cycles"] if "graph" in mx else None,
                   "vcycles_per_step": mx["cycles"], "solve_ms": mx["solve_ms"], "tuned": mx["tuned"],
                   "vcycle_ms": mx["solve_ms"] / max(mx["cycles"], 1),
-                  "relres_max": mx["relres_max"]},
+                  "relres_max": mx["relres_max"], "solver_forms": mx["forms"]},
         "fp64": {"value": ncell / (fp_ms * 1e-3) / 1e6 * world, "step_launch": fp_how,
                  "ms_per_step": fp_ms, "launched_ms_per_step": fp["ms_per_step"],
                  "graph_ms_per_step": fp["graph"]["ms_per_step"] if "graph" in fp else None,

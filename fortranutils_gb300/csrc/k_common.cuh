@@ -82,6 +82,8 @@ struct FaceDev {
 template <typename T> struct MfTab {
     T *E2 = nullptr, *N2 = nullptr, *R2 = nullptr, *Ez = nullptr, *Nz = nullptr, *Rz = nullptr;
 };
+// the same factorisation of the level-1 FP64 couplings as double-float pairs
+using DfTab = MfTab<float2>;
 
 // Push-style halo of the fast solvers: for side s of a block whose first
 // interior plane feeds a ghost plane (periodic or interface link), the

@@ -170,6 +170,112 @@ __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk
     block_reduce_store<1>(v, partial + (blockIdx.y * (long)gridDim.x + blockIdx.x));
 }
 
+// Separable double-float factors of the level-1 FP64 couplings, the
+// factorisation the FP32 solver's tables use (k_mf_extract): E(i, j, k) =
+// E2(i, j) Ez(k) with E2 the couplings of plane kr and Ez(k) their ratio
+// along the reference column (i0, j0); the same for N and R.  The factors
+// are formed in FP64 and stored as double-float pairs.  bit 16: a zero
+// coupling on the reference column.
+__global__ void k_df_mf_extract(const BlkDev *__restrict__ blk, const double *__restrict__ E,
+                                const double *__restrict__ N, const double *__restrict__ R, DfTab t,
+                                int *__restrict__ bad)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+    const long jo = n0, ko = (long)n0 * n1;
+    const int i0 = (n0 + 1) / 2, j0 = (n1 + 1) / 2, kr = (n2 + 1) / 2;
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q < (long)n0 * n1) {
+        const long p = b.off3 + q + ko * (kr - 1);
+        t.E2[b.off2 + q] = split(E[p]);
+        t.N2[b.off2 + q] = split(N[p]);
+        t.R2[b.off2 + q] = split(R[p]);
+    }
+    if (q < n2) {
+        const long pc = b.off3 + (i0 - 1) + jo * (j0 - 1);
+        const double e0 = E[pc + ko * (kr - 1)], nn0 = N[pc + ko * (kr - 1)], r0 = R[pc + ko * (kr - 1)];
+        if (e0 == 0. || nn0 == 0. || r0 == 0.) {
+            atomicOr(bad, 16);
+            return;
+        }
+        t.Ez[b.off1k + q] = split(E[pc + ko * q] / e0);
+        t.Nz[b.off1k + q] = split(N[pc + ko * q] / nn0);
+        t.Rz[b.off1k + q] = split(R[pc + ko * q] / r0);
+    }
+}
+
+__device__ __forceinline__ double df_val(float2 a) { return (double)a.x + (double)a.y; }
+
+// Every interior point's six couplings from the factors within tol * ap of
+// the FP64 arrays (else bit 1), and ap within tol * ap of their sum (else
+// bit 2: the diagonal is then read from its array)
+__global__ void k_df_mf_check(const BlkDev *__restrict__ blk, const double *__restrict__ E,
+                              const double *__restrict__ N, const double *__restrict__ R,
+                              const double *__restrict__ P, DfTab t, double tol, int *__restrict__ bad)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (q >= b.ncell) return;
+    int i, j, k;
+    const long p = decode_interior(b, q, i, j, k);
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const long ij = b.off2 + (i - 1) + jo * (j - 1), kk = b.off1k + (k - 1);
+    const double ez = df_val(t.Ez[kk]), nz = df_val(t.Nz[kk]), r2 = df_val(t.R2[ij]);
+    const double m[6] = {df_val(t.E2[ij - 1]) * ez, df_val(t.E2[ij]) * ez, df_val(t.N2[ij - jo]) * nz,
+                         df_val(t.N2[ij]) * nz,     r2 * df_val(t.Rz[kk - 1]), r2 * df_val(t.Rz[kk])};
+    const double ref[6] = {E[p - 1], E[p], N[p - jo], N[p], R[p - ko], R[p]};
+    const double ap = fabs(P[p]);
+    int f = 0;
+    for (int c = 0; c < 6; c++)
+        if (!(fabs(m[c] - ref[c]) <= tol * ap)) f |= 1;
+    const double sum = ((m[0] + m[1]) + (m[2] + m[3])) + (m[4] + m[5]);
+    if (!(fabs(sum - P[p]) <= tol * ap)) f |= 2;
+    if (f) atomicOr(bad, f);
+}
+
+// k_df_resid with the couplings from the separable factors (df_mul of a
+// 2-D and a 1-D pair) and, where P is NULL, the diagonal as their sum:
+// the residual reads x, b and writes rT only (20 of k_df_resid's 52 B per
+// point); the factors stay in L2.
+__global__ void __launch_bounds__(256) k_df_resid_mf(const BlkDev *__restrict__ blk, DfTab t,
+                                                     const float2 *__restrict__ P, const float2 *__restrict__ x,
+                                                     const float2 *__restrict__ bb, float *__restrict__ rT,
+                                                     double *__restrict__ partial)
+{
+    const BlkDev b = blk[blockIdx.y];
+    const int ni = b.n[0] - 2;
+    const unsigned nj = (unsigned)(b.n[1] - 2), nrow = nj * (unsigned)(b.n[2] - 2);
+    const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
+    const unsigned wpb = blockDim.x >> 5;
+    double acc = 0.;
+    for (unsigned row = blockIdx.x * wpb + (threadIdx.x >> 5); row < nrow; row += gridDim.x * wpb) {
+        const unsigned k = row / nj, jr = row - k * nj;
+        const long base = b.off3 + 1 + jo * (long)(jr + 1) + ko * (long)(k + 1);
+        const long ijb = b.off2 + 1 + jo * (long)(jr + 1), kk = b.off1k + k + 1;
+        const float2 ez = t.Ez[kk], nz = t.Nz[kk], rzl = t.Rz[kk - 1], rzr = t.Rz[kk];
+        for (int iq = threadIdx.x & 31; iq < ni; iq += 32) {
+            const long p = base + iq, ij = ijb + iq;
+            const float2 r2 = t.R2[ij];
+            const float2 cw = df_mul(t.E2[ij - 1], ez), ce = df_mul(t.E2[ij], ez);
+            const float2 cs = df_mul(t.N2[ij - jo], nz), cn = df_mul(t.N2[ij], nz);
+            const float2 cl = df_mul(r2, rzl), cr = df_mul(r2, rzr);
+            const float2 ap = P ? P[p] : df_add(df_add(df_add(cw, ce), df_add(cs, cn)), df_add(cl, cr));
+            float2 r = df_add_lo(bb[p], df_neg(df_mul(ap, x[p])));
+            r = df_add_lo(r, df_mul(cw, x[p - 1]));
+            r = df_add_lo(r, df_mul(ce, x[p + 1]));
+            r = df_add_lo(r, df_mul(cs, x[p - jo]));
+            r = df_add_lo(r, df_mul(cn, x[p + jo]));
+            r = df_add_lo(r, df_mul(cl, x[p - ko]));
+            r = df_add_lo(r, df_mul(cr, x[p + ko]));
+            const float rf = __fadd_rn(r.x, r.y);
+            rT[p] = rf;
+            acc = __fma_rn((double)rf, (double)rf, acc);
+        }
+    }
+    double v[1] = {acc};
+    block_reduce_store<1>(v, partial + (blockIdx.y * (long)gridDim.x + blockIdx.x));
+}
+
 // out[0] = the sum of the partials (out[1], ||b||^2, is left as it is)
 __global__ void k_df_sum_final(const double *__restrict__ partial, long nparts, double *__restrict__ out)
 {
@@ -223,6 +329,26 @@ void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, c
             k_df_update<int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
         count_launch(1);
     }
+}
+
+int launch_df_mf(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const double *E, const double *N,
+                 const double *R, const double *P, const DfTab &t, double tol, int *bad, cudaStream_t st)
+{
+    const long m = std::max(max2d, (long)maxn2);
+    k_df_mf_extract<<<dim3((unsigned)((m + 255) / 256), nb), 256, 0, st>>>(blk, E, N, R, t, bad);
+    k_df_mf_check<<<dim3((unsigned)((maxcell + 255) / 256), nb), 256, 0, st>>>(blk, E, N, R, P, t, tol, bad);
+    count_launch(2);
+    return 0;
+}
+
+void launch_df_resid_mf(const BlkDev *blk, int nb, long maxrow, const DfTab &t, const float2 *P, const float2 *x,
+                        const float2 *b, float *rT, double *partial, double *out, cudaStream_t st)
+{
+    const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
+    const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
+    k_df_resid_mf<<<dim3(gx, nb), 256, 0, st>>>(blk, t, P, x, b, rT, partial);
+    k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
+    count_launch(2);
 }
 
 void launch_df_resid(const BlkDev *blk, int nb, long maxrow, const float2 *E, const float2 *N, const float2 *R,

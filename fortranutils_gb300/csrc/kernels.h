@@ -49,6 +49,16 @@ void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b,
 void launch_df_join(const float2 *src, double *dst, long n, const double *cycles, cudaStream_t st);
 void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, const float *e, const PushDev *push,
                       bool wide, cudaStream_t st);
+// separable double-float factors of the level-1 FP64 couplings (E, N, R,
+// P: the FP64 arrays) and their check against every interior point within
+// tol * ap: bad |= 1 (couplings), 2 (diagonal not their sum), 16 (a zero
+// reference coupling)
+int launch_df_mf(const BlkDev *blk, int nb, long maxcell, long max2d, int maxn2, const double *E, const double *N,
+                 const double *R, const double *P, const DfTab &t, double tol, int *bad, cudaStream_t st);
+// the double-float residual from those factors; P NULL: the diagonal as the
+// couplings' sum
+void launch_df_resid_mf(const BlkDev *blk, int nb, long maxrow, const DfTab &t, const float2 *P, const float2 *x,
+                        const float2 *b, float *rT, double *partial, double *out, cudaStream_t st);
 void launch_df_resid(const BlkDev *blk, int nb, long maxrow, const float2 *E, const float2 *N, const float2 *R,
                      const float2 *P, const float2 *x, const float2 *b, float *rT, double *partial, double *out,
                      cudaStream_t st);

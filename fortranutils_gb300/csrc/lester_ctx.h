@@ -56,6 +56,7 @@ struct CycleGraph {
     int threads = 0;                // red-black CTA size
     int line = 0;                   // y-line relaxation
     int direct = 0;                 // points of the bottom level's direct solve (0: smoothed)
+    int dfsep = 0;                  // Ctx::df_sep
     int tile = 0;                   // ctrl.rb_tile
     long launches = 0;              // kernels per replay
     std::vector<cudaEvent_t> ev;    // pairs around the level-1 smoother launches
@@ -103,6 +104,11 @@ struct Ctx {
     int *d_pguess = nullptr;   // the istep p_prev was taken at (device; -1: none)
     std::FILE *step_log = nullptr;  // lester_gpu_step_log's file (one JSON line per lester_step)
     float2 *df_E = nullptr, *df_N = nullptr, *df_R = nullptr, *df_P = nullptr, *df_p = nullptr, *df_b = nullptr;
+    // separable double-float factors of the level-1 couplings; df_sep: 0
+    // not in use (the arrays above), 1 couplings from the factors and the
+    // diagonal from df_P, 2 the diagonal as the couplings' sum too
+    DfTab df_tab;
+    int df_sep = 0;
     double *d_fr = nullptr, *d_fp = nullptr, *d_fq = nullptr;  // flexible CG: r, p, q (level 1)
     // convective outflow / fixed inflow sides (lester_outflow.cu)
     bool sides_built = false;

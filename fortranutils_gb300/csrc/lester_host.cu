@@ -608,6 +608,7 @@ static void free_ctx(Ctx *c)
     for (double *p : c->scratch) cudaFree(p);
     for (double *p : c->coef_mirror) cudaFree(p);
     for (float2 *p : {c->df_E, c->df_N, c->df_R, c->df_P, c->df_p, c->df_b}) cudaFree(p);
+    for (float2 *p : {c->df_tab.E2, c->df_tab.N2, c->df_tab.R2, c->df_tab.Ez, c->df_tab.Nz, c->df_tab.Rz}) cudaFree(p);
     if (c->step_log) std::fclose(c->step_log);
     for (cudaEvent_t e : c->xev) cudaEventDestroy(e);
     if (c->xs_in) cudaStreamDestroy(c->xs_in);
@@ -1018,12 +1019,38 @@ template <typename T> static int prepare_coef(Ctx &c, const Coef &A, int prec)
         F.mf = (mbad == 0);
     }
     if ((r = build_direct<T>(c, F.mf ? F.tab : MfTab<T>()))) return r;
-    // mixed solver: double-float copies of the level-1 FP64 coefficients
+    // mixed solver: double-float copies of the level-1 FP64 coefficients,
+    // and, where the FP32 tables are separable, double-float factors checked
+    // against every coupling to 1e-14 of ap (the outer residual then reads
+    // no coefficient arrays)
     if (sizeof(T) == 4) {
         if ((r = alloc_df(c))) return r;
         const double *src[4] = {c.E64, c.N64, c.R64, c.P64};
         float2 *dst[4] = {c.df_E, c.df_N, c.df_R, c.df_P};
         for (int q = 0; q < 4; q++) launch_df_split(src[q], dst[q], c.tot_sg3, c.stream);
+        c.df_sep = 0;
+        if (F.mf) {
+            if (!c.df_tab.E2) {
+                float2 **t2[3] = {&c.df_tab.E2, &c.df_tab.N2, &c.df_tab.R2};
+                float2 **t1[3] = {&c.df_tab.Ez, &c.df_tab.Nz, &c.df_tab.Rz};
+                for (float2 **a : t2) LES_CUDA(cudaMalloc((void **)a, sizeof(float2) * c.tot2));
+                for (float2 **a : t1) LES_CUDA(cudaMalloc((void **)a, sizeof(float2) * c.tot1k));
+            }
+            LevelGeom &L1 = c.lv[1];
+            long max2d = 0;
+            int maxn2 = 0;
+            for (int b = 1; b <= c.g.numbl; b++) {
+                max2d = std::max(max2d, (long)L1.n[b][0] * L1.n[b][1]);
+                maxn2 = std::max(maxn2, L1.n[b][2]);
+            }
+            LES_CUDA(cudaMemsetAsync(c.d_flag, 0, sizeof(int), c.stream));
+            launch_df_mf(L1.d_blk, c.g.numbl, L1.maxcell, max2d, maxn2, c.E64, c.N64, c.R64, c.P64, c.df_tab, 1e-14,
+                         c.d_flag, c.stream);
+            int dbad = 0;
+            LES_CUDA(cudaMemcpyAsync(&dbad, c.d_flag, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            LES_CUDA(cudaStreamSynchronize(c.stream));
+            c.df_sep = (dbad & 17) ? 0 : (dbad & 2) ? 1 : 2;
+        }
     }
     for (int q = 0; q < 7; q++) c.coef_key[q] = A.a[q];
     c.coef_gen_seen = c.coef_gen;
@@ -1215,8 +1242,12 @@ static void df_cycle_tail(Ctx &c, float *e, float *rT)
     LevelGeom &L1 = c.lv[1];
     const int nb = c.g.numbl;
     launch_df_update(L1.d_blk, nb, L1.maxn, c.df_p, e, L1.d_push, c.tot3 >= (1L << 31), c.stream);
-    launch_df_resid(L1.d_blk, nb, L1.maxjk, c.df_E, c.df_N, c.df_R, c.df_P, c.df_p, c.df_b, rT, c.d_partial,
-                    c.d_small, c.stream);
+    if (c.df_sep)
+        launch_df_resid_mf(L1.d_blk, nb, L1.maxjk, c.df_tab, c.df_sep == 2 ? nullptr : c.df_P, c.df_p, c.df_b, rT,
+                           c.d_partial, c.d_small, c.stream);
+    else
+        launch_df_resid(L1.d_blk, nb, L1.maxjk, c.df_E, c.df_N, c.df_R, c.df_P, c.df_p, c.df_b, rT, c.d_partial,
+                        c.d_small, c.stream);
 }
 
 // p and b - shift of level 1 as double-float pairs, from the FP64 arrays
@@ -1239,7 +1270,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     if (G.exec && G.f == f && G.b == b && G.sweeps == k.rb_sweeps && G.coarse == k.rb_coarse &&
         G.omega == k.rb_omega && G.singular == c.singular && G.mf == fset<T>(c).mf && G.tail == k.mg_tail &&
         G.krylov == (kry ? 1 : df ? 2 : 0) && G.threads == c.rb_threads && G.line == k.rb_line &&
-        G.direct == fset<T>(c).cn && G.tile == k.rb_tile)
+        G.direct == fset<T>(c).cn && G.tile == k.rb_tile && G.dfsep == c.df_sep)
         return 0;
     drop_graph(G);
     if (!c.cap_stream) LES_CUDA(cudaStreamCreateWithFlags(&c.cap_stream, cudaStreamNonBlocking));
@@ -1293,6 +1324,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
     G.krylov = kry ? 1 : df ? 2 : 0;
     G.direct = fset<T>(c).cn;
     G.tile = k.rb_tile;
+    G.dfsep = c.df_sep;
     G.threads = c.rb_threads;
     G.line = k.rb_line;
     return 0;
@@ -1868,6 +1900,16 @@ int lester_gpu_rb_tiles(int *level_mask)
     LES_NEED_CTX();
     if (!level_mask) return set_err(LES_ERR_ARG, "NULL level_mask");
     *level_mask = g_ctx->rb_tile_mask;
+    return 0;
+}
+
+int lester_gpu_solver_forms(int *flags)
+{
+    LES_NEED_CTX();
+    if (!flags) return set_err(LES_ERR_ARG, "NULL flags");
+    const Ctx &c = *g_ctx;
+    *flags = (c.f32.mf ? 1 : 0) | (c.df_sep ? 2 : 0) | (c.df_sep == 2 ? 4 : 0) | (c.f32.cn > 0 ? 8 : 0) |
+             (c.f64.cn > 0 ? 16 : 0);
     return 0;
 }
 

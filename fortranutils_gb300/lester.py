@@ -227,6 +227,15 @@ def gpu_step_graph_info() -> dict:
     return {"replays": n.value, "handovers": h.value, "failed": bool(f.value), "why": why.value.decode()}
 
 
+def gpu_solver_forms() -> dict:
+    """Forms the fast solvers took for the current coefficients."""
+    m = C.c_int()
+    _check(lib().lester_gpu_solver_forms(C.byref(m)))
+    v = m.value
+    return {"mf32": bool(v & 1), "df_separable": bool(v & 2), "df_diag_sum": bool(v & 4),
+            "direct32": bool(v & 8), "direct64": bool(v & 16)}
+
+
 def gpu_rb_tiles() -> int:
     """Bit l set: level l was smoothed by the shared-memory red-black tiles."""
     m = C.c_int()

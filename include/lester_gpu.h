@@ -254,6 +254,12 @@ int lester_gpu_prof_kernel(int which, double *ms_total, long *launches);
 int lester_gpu_prof_read(double *ms_total, long *launches);
 /* bytes copied host->device and device->host by calls with host arrays */
 int lester_gpu_xfer_bytes(long *h2d, long *d2h);
+/* forms the fast solvers took for the current coefficients: bit 0 the FP32
+ * solver's couplings from separable factors (no coefficient arrays); bit 1
+ * the mixed solver's double-float residual from separable double-float
+ * factors, bit 2 its diagonal as their sum; bit 3 / bit 4 the bottom level
+ * solved exactly by the FP32 / FP64 solver */
+int lester_gpu_solver_forms(int *flags);
 
 /* One time step: the ivar loop of code/step.F:214-454 (fixed_inlet on the
  * inlet blocks of lester_gpu_set_inlet, set_virt_bc x3, subgrid, scalar
