@@ -96,6 +96,20 @@ struct PushDev {
     int a2, a3, valid;
 };
 
+// A level of at most kGeoBlk blocks as a kernel parameter (constant
+// bank): per block its points with ghosts, its offsets in the 3-D, 2-D and
+// 1-D arrays, and its six ghost mirrors -- a half sweep then loads no
+// descriptor from memory, and a point on a mirrored face writes its ghost
+// without a dependent load.  Offsets fit 32 bits (the multigrid arrays
+// hold fewer than 2^31 points).
+constexpr int kGeoBlk = 4;
+struct LevGeo {
+    int nb;
+    int n[kGeoBlk][3];
+    int off3[kGeoBlk], off2[kGeoBlk], off1k[kGeoBlk];
+    PushDev push[kGeoBlk][6];
+};
+
 template <typename T>
 __device__ __forceinline__ void push_ghosts(const PushDev *__restrict__ pd, const BlkDev &b, int i,
                                             int j, int k, T val, T *__restrict__ x)

@@ -282,6 +282,65 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
         push_ghosts(push + 6 * bi, blk[bi], i, j, k, xn, x);
 }
 
+// The same half sweep with the level's geometry as a kernel parameter
+// (LevGeo): no descriptor loads, and for one block no division either.
+// PUSH: some face of the level mirrors its first interior plane.
+template <typename T, bool MF, bool ONE, bool PUSH>
+__global__ void __launch_bounds__(512) k_rb_geo(const __grid_constant__ LevGeo G, int color, T omega,
+                                                const T *__restrict__ E, const T *__restrict__ N,
+                                                const T *__restrict__ R, const T *__restrict__ D,
+                                                T *__restrict__ x, const T *__restrict__ bb, MfTab<T> mf, int maxnk)
+{
+    const int bi = ONE ? 0 : (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bi * maxnk + 2;
+    const int n0 = G.n[bi][0], n1 = G.n[bi][1], n2 = G.n[bi][2];
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > n2 - 1 || j > n1 - 1) return;
+    const int i = 2 + 2 * (int)(blockIdx.x * 32 + threadIdx.x) + ((j + k + color) & 1);
+    if (i > n0 - 1) return;
+    const int jo = n0, ko = n0 * n1;
+    const int p = G.off3[bi] + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    T c[6], dinv;
+    if (MF) {
+        const int ij = G.off2[bi] + (i - 1) + jo * (j - 1), kk = G.off1k[bi] + (k - 1);
+        const T ez = mf.Ez[kk], nz = mf.Nz[kk], r2 = mf.R2[ij];
+        c[0] = mf.E2[ij - 1] * ez;
+        c[1] = mf.E2[ij] * ez;
+        c[2] = mf.N2[ij - jo] * nz;
+        c[3] = mf.N2[ij] * nz;
+        c[4] = r2 * mf.Rz[kk - 1];
+        c[5] = r2 * mf.Rz[kk];
+        dinv = rcp_rn((((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5])));
+    } else {
+        c[0] = E[p - 1];
+        c[1] = E[p];
+        c[2] = N[p - jo];
+        c[3] = N[p];
+        c[4] = R[p - ko];
+        c[5] = R[p];
+        dinv = D[p];
+    }
+    const T *xp = x + p;
+    T s = bb[p] + c[0] * xp[-1] + c[1] * xp[1] + c[2] * xp[-jo] + c[3] * xp[jo] + c[4] * xp[-ko] + c[5] * xp[ko];
+    T xo = xp[0];
+    T xn = xo + omega * (s * dinv - xo);
+    x[p] = xn;
+    if (PUSH && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1)) {
+        // push_ghosts with the mirrors from the parameter
+        const int cc[3] = {i - 1, j - 1, k - 1}, nn[3] = {n0, n1, n2};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (cc[d] == 1 && G.push[bi][2 * d].valid) {
+                const PushDev &P = G.push[bi][2 * d];
+                x[P.gh + P.jo * cc[P.a2] + P.ko * cc[P.a3]] = xn;
+            }
+            if (cc[d] == nn[d] - 2 && G.push[bi][2 * d + 1].valid) {
+                const PushDev &P = G.push[bi][2 * d + 1];
+                x[P.gh + P.jo * cc[P.a2] + P.ko * cc[P.a3]] = xn;
+            }
+        }
+    }
+}
+
 // ---- red-black SOR, one full sweep per launch, shared-memory tiles --------
 // For a level of one block whose faces are periodic onto itself with even
 // extents, or walls (no coupling through them): each CTA stages a tile of
@@ -1348,10 +1407,28 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, bool wide, cudaStream_t st)
+               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, cudaStream_t st)
 {
     const int rows = (threads == 128 || threads == 512) ? threads / 32 : 8;
     const int maxnk = maxn[2] - 2;
+    if (geo && !wide && maxnk * geo->nb <= 65535) {
+        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)(maxnk * geo->nb));
+        const dim3 cta(32, rows);
+        const T om = (T)omega;
+#define LES_RB_GEO(MF, ONE, PUSH)                                                                            \
+    k_rb_geo<T, MF, ONE, PUSH><<<grid, cta, 0, st>>>(*geo, color, om, E, N, R, D, x, b, mf, maxnk)
+        const bool one = geo->nb == 1, pu = push != nullptr;
+        if (mf.E2) {
+            if (one) { if (pu) LES_RB_GEO(true, true, true); else LES_RB_GEO(true, true, false); }
+            else { if (pu) LES_RB_GEO(true, false, true); else LES_RB_GEO(true, false, false); }
+        } else {
+            if (one) { if (pu) LES_RB_GEO(false, true, true); else LES_RB_GEO(false, true, false); }
+            else { if (pu) LES_RB_GEO(false, false, true); else LES_RB_GEO(false, false, false); }
+        }
+#undef LES_RB_GEO
+        count_launch(1);
+        return;
+    }
     // gridDim.z <= 65535: blocks in groups of at most 65535 / maxnk
     const int per = std::max(1, 65535 / maxnk);
     for (int bi0 = 0; bi0 < nb; bi0 += per) {
@@ -1640,7 +1717,7 @@ bool prepare_rb_tile()
                                      cudaStream_t);                                                \
     template void launch_rb<T>(const BlkDev *, int, const int *, int, double, const T *, const T *, \
                                const T *, const T *, T *, const T *, const PushDev *,             \
-                               const MfTab<T> &, int, bool, cudaStream_t);                        \
+                               const MfTab<T> &, int, bool, const LevGeo *, cudaStream_t);        \
     template void launch_yline<T>(const BlkDev *, int, long, int, double, const T *, const T *,   \
                                   const T *, const T *, T *, const T *, const MfTab<T> &, T *, T *, \
                                   int, cudaStream_t);                                             \

@@ -89,11 +89,12 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
                      cudaStream_t st);
 // red-black half sweep: CTAs of `threads` (128, 256, 512) = 32 points of a
 // row x 4, 8 or 16 rows; maxn: the most points of a block along i, j, k
-// (ghosts included); wide: 64-bit offsets (arrays of 2^31 points or more)
+// (ghosts included); wide: 64-bit offsets (arrays of 2^31 points or more);
+// geo (nullable): the level as a kernel parameter (at most kGeoBlk blocks)
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, bool wide, cudaStream_t st);
+               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, cudaStream_t st);
 // y-line zebra relaxation of one colour of (i, k) columns (maxik_half: the
 // most columns of one colour in a block)
 template <typename T>

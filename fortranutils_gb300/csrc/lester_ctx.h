@@ -24,6 +24,8 @@ struct LevelGeom {
     BlkDev *d_blk = nullptr;
     FaceDev *d_face = nullptr;
     PushDev *d_push = nullptr;  // 6 per block: ghost mirrors of the interior planes
+    LevGeo geo;                 // the level as a kernel parameter (geo_ok: at most kGeoBlk blocks)
+    bool geo_ok = false;
     // red-black sweeps may push: on every face the point a ghost mirrors and
     // the point that reads that ghost have different colours
     bool rb_push = true;

@@ -448,6 +448,19 @@ static int build_faces(Ctx &c)
                 L.maxface = std::max(L.maxface, (long)f.nj * f.nk);
             }
         L.nface = (int)fv.size();
+        // the same as a kernel parameter where it fits
+        L.geo_ok = nb <= kGeoBlk;
+        if (L.geo_ok) {
+            L.geo = LevGeo{};
+            L.geo.nb = nb;
+            for (int b = 1; b <= nb; b++) {
+                for (int d = 0; d < 3; d++) L.geo.n[b - 1][d] = L.n[b][d];
+                L.geo.off3[b - 1] = (int)L.off3[b];
+                L.geo.off2[b - 1] = (int)L.off2[b];
+                L.geo.off1k[b - 1] = (int)L.off1k[b];
+                for (int s = 0; s < 6; s++) L.geo.push[b - 1][s] = pv[(b - 1) * 6 + s];
+            }
+        }
         LES_CUDA(cudaMalloc(&L.d_push, sizeof(PushDev) * pv.size()));
         LES_CUDA(cudaMemcpy(L.d_push, pv.data(), sizeof(PushDev) * pv.size(), cudaMemcpyHostToDevice));
         L.worklen = w;
@@ -1156,7 +1169,7 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxn, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
                          F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.rb_threads,
-                         c.tot3 >= (1L << 31), c.stream);
+                         c.tot3 >= (1L << 31), L.geo_ok ? &L.geo : nullptr, c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
