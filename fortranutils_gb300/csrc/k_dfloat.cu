@@ -259,7 +259,10 @@ __global__ void __launch_bounds__(256) k_df_resid_mf(const BlkDev *__restrict__ 
             const float2 cw = df_mul(t.E2[ij - 1], ez), ce = df_mul(t.E2[ij], ez);
             const float2 cs = df_mul(t.N2[ij - jo], nz), cn = df_mul(t.N2[ij], nz);
             const float2 cl = df_mul(r2, rzl), cr = df_mul(r2, rzr);
-            const float2 ap = P ? P[p] : df_add(df_add(df_add(cw, ce), df_add(cs, cn)), df_add(cl, cr));
+            // the couplings are positive: their sum has no cancellation, and
+            // the lo parts added in FP32 keep it to about 2^-48
+            const float2 ap =
+                P ? P[p] : df_add_lo(df_add_lo(df_add_lo(cw, ce), df_add_lo(cs, cn)), df_add_lo(cl, cr));
             float2 r = df_add_lo(bb[p], df_neg(df_mul(ap, x[p])));
             r = df_add_lo(r, df_mul(cw, x[p - 1]));
             r = df_add_lo(r, df_mul(ce, x[p + 1]));
