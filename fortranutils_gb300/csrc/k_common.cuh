@@ -96,6 +96,16 @@ struct PushDev {
     int a2, a3, valid;
 };
 
+// The (block, plane) pairs a 3-D launch walks along gridDim.z: entry z is
+// (0-based block, 1-based plane); n entries.  Built per level for its
+// interior planes (2 .. n[2] - 1) and for the planes 1 .. n[2] - 1 a
+// prolongation from it walks, so that blocks of different extents waste
+// no planes and no CTA divides by a plane count.
+struct ZMap {
+    const int2 *map = nullptr;
+    int n = 0;
+};
+
 // A level of at most kGeoBlk blocks as a kernel parameter (constant
 // bank): per block its points with ghosts, its offsets in the 3-D, 2-D and
 // 1-D arrays, and its six ghost mirrors -- a half sweep then loads no

@@ -113,13 +113,13 @@ __global__ void k_df_join(const float2 *__restrict__ src, double *__restrict__ d
 
 // p += e on the interior of level 1, ghosts pushed as k_update does.
 // Thread (x, y) of CTA (bx, by, bz): point i = 2 + 32 bx + x of row
-// j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
-// bi0 + bz / maxnk.
+// j = 2 + blockDim.y by + y of the (block, plane) zmap[z0 + bz].
 template <typename Ix>
 __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__ p, const float *__restrict__ e,
-                            const PushDev *__restrict__ push, int maxnk, int bi0)
+                            const PushDev *__restrict__ push, const int2 *__restrict__ zmap, int z0)
 {
-    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, k = bk.y;
     const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
     const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > n2 - 1 || j > n1 - 1 || i > n0 - 1) return;
@@ -320,16 +320,15 @@ void launch_df_join(const float2 *src, double *dst, long n, const double *cycles
 }
 
 void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, const float *e, const PushDev *push,
-                      bool wide, cudaStream_t st)
+                      bool wide, ZMap zm, cudaStream_t st)
 {
-    const int maxnk = maxn[2] - 2, per = std::max(1, 65535 / maxnk);
-    for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const dim3 grid((unsigned)(maxn[0] + 29) / 32, (unsigned)(maxn[1] + 5) / 8,
-                        (unsigned)(maxnk * std::min(per, nb - bi0)));
+    (void)nb;
+    for (int z0 = 0; z0 < zm.n; z0 += 65535) {
+        const dim3 grid((unsigned)(maxn[0] + 29) / 32, (unsigned)(maxn[1] + 5) / 8, (unsigned)std::min(65535, zm.n - z0));
         if (wide)
-            k_df_update<long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+            k_df_update<long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
         else
-            k_df_update<int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+            k_df_update<int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
         count_launch(1);
     }
 }

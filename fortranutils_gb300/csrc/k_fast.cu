@@ -234,8 +234,8 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 
 // ---- red-black SOR half sweep, all blocks of a level ----------------------
 // Thread (x, y) of CTA (bx, by, bz): point 2 + 2 (32 bx + x) (+1 by colour)
-// of row j = 2 + blockDim.y by + y of plane k = 2 + bz % maxnk of block
-// bi0 + bz / maxnk; no per-thread division.  Ix: the offset type, int when every
+// of row j = 2 + blockDim.y by + y of the (block, plane) zmap[z0 + bz]; no
+// per-thread division.  Ix: the offset type, int when every
 // offset of the multigrid arrays is below 2^31.  Per point the operations
 // of rb_point.
 template <typename T, bool MF, typename Ix>
@@ -243,9 +243,11 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
                                             const T *__restrict__ E, const T *__restrict__ N,
                                             const T *__restrict__ R, const T *__restrict__ D,
                                             T *__restrict__ x, const T *__restrict__ bb,
-                                            const PushDev *__restrict__ push, MfTab<T> mf, int maxnk, int bi0)
+                                            const PushDev *__restrict__ push, MfTab<T> mf,
+                                            const int2 *__restrict__ zmap, int z0)
 {
-    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, k = bk.y;
     const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > n2 - 1 || j > n1 - 1) return;
@@ -777,14 +779,16 @@ __device__ __forceinline__ T rr_point(const BlkDev &f, int i, int j, int k, cons
 // One coarse interior point per thread: the residuals of its 2x2x2 fine
 // children are summed into the coarse right-hand side.  Thread (x, y) of
 // CTA (bx, by, bz): coarse point i = 2 + 32 bx + x of row j = 2 +
-// blockDim.y by + y of plane k = 2 + bz % maxnk of block bi0 + bz / maxnk.
+// blockDim.y by + y of the coarse (block, plane) zmap[z0 + bz].
 template <typename T, typename Ix>
 __global__ void __launch_bounds__(256) k_resid_restrict(
     const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_, const T *__restrict__ E,
     const T *__restrict__ N, const T *__restrict__ R, const T *__restrict__ D,
-    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse, MfTab<T> mf, int maxnk, int bi0)
+    const T *__restrict__ x, const T *__restrict__ bb, T *__restrict__ bcoarse, MfTab<T> mf,
+    const int2 *__restrict__ zmap, int z0)
 {
-    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, k = bk.y;
     const BlkDev &c = bc_[bi];
     const int n0 = c.n[0], n1 = c.n[1];
     const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
@@ -841,17 +845,19 @@ __device__ __forceinline__ void prolong_point(const BlkDev &c, const BlkDev &f, 
 }
 
 // Thread (x, y) of CTA (bx, by, bz): the fine points 2c - 1 and 2c along
-// each axis (c = 1 + 32 bx + x, 1 + blockDim.y by + y, 1 + bz % maxnk of
-// block bi0 + bz / maxnk; coarse c up to n - 1), i.e. the fine points whose
+// each axis (c = 1 + 32 bx + x, 1 + blockDim.y by + y, and the coarse
+// (block, plane) zmap[z0 + bz]; coarse c up to n - 1), i.e. the fine points whose
 // coarse stencil is the 2 x 2 x 2 coarse points c..c+1 (clamped as
 // prolong_point clamps).  The eight coarse values are loaded once for up to
 // eight fine points; each fine point sums them in prolong_point's order.
 template <typename T, typename Ix>
 __global__ void __launch_bounds__(256) k_prolong8(const BlkDev *__restrict__ bc_, const BlkDev *__restrict__ bf_,
                                                   const T *__restrict__ xc, T *__restrict__ xf,
-                                                  const PushDev *__restrict__ push, int maxnk, int bi0)
+                                                  const PushDev *__restrict__ push, const int2 *__restrict__ zmap,
+                                                  int z0)
 {
-    const int bz = (int)blockIdx.z / maxnk, cz = (int)blockIdx.z - bz * maxnk + 1, bi = bi0 + bz;
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, cz = bk.y;
     const BlkDev &c = bc_[bi], &f = bf_[bi];
     const int cx = (int)(blockIdx.x * 32 + threadIdx.x) + 1, cy = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 1;
     if (cx > c.n[0] - 1 || cy > c.n[1] - 1 || cz > c.n[2] - 1) return;
@@ -1285,13 +1291,15 @@ __global__ void k_coarse_mean(const BlkDev *__restrict__ blk, int nb, T *__restr
 }
 
 // p += e on the interior of level 1.  Thread (x, y) of CTA (bx, by, bz):
-// point i = 2 + 32 bx + x of row j = 2 + blockDim.y by + y of plane
-// k = 2 + bz % maxnk of block bi0 + bz / maxnk.
+// point i = 2 + 32 bx + x of row j = 2 + blockDim.y by + y of the (block,
+// plane) zmap[z0 + bz].
 template <typename T, typename Ix>
 __global__ void k_update(const BlkDev *__restrict__ blk, double *__restrict__ p,
-                         const T *__restrict__ e, const PushDev *__restrict__ push, int maxnk, int bi0)
+                         const T *__restrict__ e, const PushDev *__restrict__ push, const int2 *__restrict__ zmap,
+                         int z0)
 {
-    const int bz = (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bz * maxnk + 2, bi = bi0 + bz;
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, k = bk.y;
     const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
     const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > n2 - 1 || j > n1 - 1 || i > n0 - 1) return;
@@ -1407,7 +1415,7 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, cudaStream_t st)
+               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, ZMap zm, cudaStream_t st)
 {
     const int rows = (threads == 128 || threads == 512) ? threads / 32 : 8;
     const int maxnk = maxn[2] - 2;
@@ -1429,21 +1437,18 @@ void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double o
         count_launch(1);
         return;
     }
-    // gridDim.z <= 65535: blocks in groups of at most 65535 / maxnk
-    const int per = std::max(1, 65535 / maxnk);
-    for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const int nbl = std::min(per, nb - bi0);
-        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)(maxnk * nbl));
+    // gridDim.z <= 65535: the (block, plane) pairs in groups
+    for (int z0 = 0; z0 < zm.n; z0 += 65535) {
+        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)std::min(65535, zm.n - z0));
         const dim3 cta(32, rows);
         if (!wide && mf.E2)
-            k_rb<T, true, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+            k_rb<T, true, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
         else if (!wide)
-            k_rb<T, false, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+            k_rb<T, false, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
         else if (mf.E2)
-            k_rb<T, true, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk, bi0);
+            k_rb<T, true, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
         else
-            k_rb<T, false, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, maxnk,
-                                                       bi0);
+            k_rb<T, false, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
         count_launch(1);
     }
 }
@@ -1490,35 +1495,34 @@ void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double 
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_c[3], const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           const MfTab<T> &mf, bool wide, cudaStream_t st)
+                           const MfTab<T> &mf, bool wide, ZMap zm_c, cudaStream_t st)
 {
-    const int maxnk = maxn_c[2] - 2, per = std::max(1, 65535 / maxnk);
-    for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const dim3 grid(nb_(maxn_c[0] - 2, 32), nb_(maxn_c[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+    for (int z0 = 0; z0 < zm_c.n; z0 += 65535) {
+        const dim3 grid(nb_(maxn_c[0] - 2, 32), nb_(maxn_c[1] - 2, 8), (unsigned)std::min(65535, zm_c.n - z0));
         if (wide)
-            k_resid_restrict<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, maxnk,
-                                                                    bi0);
+            k_resid_restrict<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, zm_c.map,
+                                                                    z0);
         else
-            k_resid_restrict<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, maxnk,
-                                                                   bi0);
+            k_resid_restrict<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, zm_c.map,
+                                                                   z0);
         count_launch(1);
     }
 }
 
 template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_f[3], const T *xc,
-                         T *xf, const PushDev *push, bool wide, cudaStream_t st)
+                         T *xf, const PushDev *push, bool wide, ZMap zm_c, cudaStream_t st)
 {
     // a thread per coarse c = 1 .. n_coarse - 1 along each axis: the fine
-    // level has n_fine = 2 n_coarse - 2 points per axis, ghosts included
-    const int mc[3] = {maxn_f[0] / 2 + 1, maxn_f[1] / 2 + 1, maxn_f[2] / 2 + 1};
-    const int maxnk = mc[2] - 1, per = std::max(1, 65535 / maxnk);
-    for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const dim3 grid(nb_(mc[0] - 1, 32), nb_(mc[1] - 1, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+    // level has n_fine = 2 n_coarse - 2 points per axis, ghosts included;
+    // zm_c: the coarse (block, plane) pairs, planes 1 .. n_coarse - 1
+    const int mc[2] = {maxn_f[0] / 2 + 1, maxn_f[1] / 2 + 1};
+    for (int z0 = 0; z0 < zm_c.n; z0 += 65535) {
+        const dim3 grid(nb_(mc[0] - 1, 32), nb_(mc[1] - 1, 8), (unsigned)std::min(65535, zm_c.n - z0));
         if (wide)
-            k_prolong8<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+            k_prolong8<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, zm_c.map, z0);
         else
-            k_prolong8<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, maxnk, bi0);
+            k_prolong8<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, zm_c.map, z0);
         count_launch(1);
     }
 }
@@ -1633,15 +1637,14 @@ void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st)
 
 template <typename T>
 void launch_update(const BlkDev *blk, int nb, const int maxn[3], double *p, const T *e, const PushDev *push,
-                   bool wide, cudaStream_t st)
+                   bool wide, ZMap zm, cudaStream_t st)
 {
-    const int maxnk = maxn[2] - 2, per = std::max(1, 65535 / maxnk);
-    for (int bi0 = 0; bi0 < nb; bi0 += per) {
-        const dim3 grid(nb_(maxn[0] - 2, 32), nb_(maxn[1] - 2, 8), (unsigned)(maxnk * std::min(per, nb - bi0)));
+    for (int z0 = 0; z0 < zm.n; z0 += 65535) {
+        const dim3 grid(nb_(maxn[0] - 2, 32), nb_(maxn[1] - 2, 8), (unsigned)std::min(65535, zm.n - z0));
         if (wide)
-            k_update<T, long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+            k_update<T, long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
         else
-            k_update<T, int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, maxnk, bi0);
+            k_update<T, int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
         count_launch(1);
     }
 }
@@ -1717,13 +1720,13 @@ bool prepare_rb_tile()
                                      cudaStream_t);                                                \
     template void launch_rb<T>(const BlkDev *, int, const int *, int, double, const T *, const T *, \
                                const T *, const T *, T *, const T *, const PushDev *,             \
-                               const MfTab<T> &, int, bool, const LevGeo *, cudaStream_t);        \
+                               const MfTab<T> &, int, bool, const LevGeo *, ZMap, cudaStream_t);  \
     template void launch_yline<T>(const BlkDev *, int, long, int, double, const T *, const T *,   \
                                   const T *, const T *, T *, const T *, const MfTab<T> &, T *, T *, \
                                   int, cudaStream_t);                                             \
     template void launch_resid_restrict<T>(const BlkDev *, const BlkDev *, int, const int *, const T *, \
                                            const T *, const T *, const T *, const T *, const T *, \
-                                           T *, const MfTab<T> &, bool, cudaStream_t);            \
+                                           T *, const MfTab<T> &, bool, ZMap, cudaStream_t);      \
     template void launch_vtail<T>(const VLev *, int, int, int, int, int, double, int, const T *,   \
                                   const T *, const T *, const T *, T *, T *, const MfTab<T> &,    \
                                   long, long, const CoarseDirect<T> &, cudaStream_t);             \
@@ -1737,7 +1740,7 @@ bool prepare_rb_tile()
                                       const T *, const T *, const MfTab<T> &, double, int *,      \
                                       cudaStream_t);                                              \
     template void launch_prolong_fast<T>(const BlkDev *, const BlkDev *, int, const int *, const T *, \
-                                         T *, const PushDev *, bool, cudaStream_t);               \
+                                         T *, const PushDev *, bool, ZMap, cudaStream_t);         \
     template void launch_halo_fast<T>(const FaceDev *, int, long, T *, cudaStream_t);             \
     template void launch_resid_outer<T>(const BlkDev *, int, long, const double *,                \
                                         const double *, const double *, const double *,           \
@@ -1748,7 +1751,7 @@ bool prepare_rb_tile()
                                 double *, double *, T *, const PushDev *, double *, double *,    \
                                 double *, cudaStream_t);                                         \
     template void launch_update<T>(const BlkDev *, int, const int *, double *, const T *, const PushDev *, bool, \
-                                   cudaStream_t);                                                \
+                                   ZMap, cudaStream_t);                                          \
     template void launch_coarse_mean<T>(const BlkDev *, int, T *, cudaStream_t);
 INST(float)
 INST(double)

@@ -48,7 +48,7 @@ void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b,
 // cycles (nullable, device): skipped when *cycles == 0
 void launch_df_join(const float2 *src, double *dst, long n, const double *cycles, cudaStream_t st);
 void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, const float *e, const PushDev *push,
-                      bool wide, cudaStream_t st);
+                      bool wide, ZMap zm, cudaStream_t st);
 // separable double-float factors of the level-1 FP64 couplings (E, N, R,
 // P: the FP64 arrays) and their check against every interior point within
 // tol * ap: bad |= 1 (couplings), 2 (diagonal not their sum), 16 (a zero
@@ -94,7 +94,7 @@ int launch_conv_coef(const BlkDev *blk, int nb, long maxcell, const double *cons
 template <typename T>
 void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double omega, const T *E,
                const T *N, const T *R, const T *D, T *x, const T *b, const PushDev *push,
-               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, cudaStream_t st);
+               const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, ZMap zm, cudaStream_t st);
 // y-line zebra relaxation of one colour of (i, k) columns (maxik_half: the
 // most columns of one colour in a block)
 template <typename T>
@@ -104,7 +104,7 @@ void launch_yline(const BlkDev *blk, int nb, long maxik_half, int color, double 
 template <typename T>
 void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_c[3], const T *E,
                            const T *N, const T *R, const T *D, const T *x, const T *b, T *bcoarse,
-                           const MfTab<T> &mf, bool wide, cudaStream_t st);
+                           const MfTab<T> &mf, bool wide, ZMap zm_c, cudaStream_t st);
 template <typename T>
 void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, double omega, int singular,
                   const T *E, const T *N, const T *R, const T *D, T *x, T *b, const MfTab<T> &mf,
@@ -130,7 +130,7 @@ void launch_mf_tables(const BlkDev *blk, int nb, long maxcell, long max2d, int m
                       cudaStream_t st);
 template <typename T>
 void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int maxn_f[3], const T *xc,
-                         T *xf, const PushDev *push, bool wide, cudaStream_t st);
+                         T *xf, const PushDev *push, bool wide, ZMap zm_c, cudaStream_t st);
 template <typename T>
 void launch_halo_fast(const FaceDev *faces, int nface, long maxface, T *x, cudaStream_t st);
 template <typename T>
@@ -150,7 +150,7 @@ void launch_interior_mean(const BlkDev *blk, int nb, long maxcell, const double 
                           double *out, cudaStream_t st);
 template <typename T>
 void launch_update(const BlkDev *blk, int nb, const int maxn[3], double *p, const T *e, const PushDev *push,
-                   bool wide, cudaStream_t st);
+                   bool wide, ZMap zm, cudaStream_t st);
 template <typename T>
 void launch_coarse_mean(const BlkDev *blk, int nb, T *b, cudaStream_t st);
 

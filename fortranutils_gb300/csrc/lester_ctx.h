@@ -25,6 +25,8 @@ struct LevelGeom {
     FaceDev *d_face = nullptr;
     PushDev *d_push = nullptr;  // 6 per block: ghost mirrors of the interior planes
     LevGeo geo;                 // the level as a kernel parameter (geo_ok: at most kGeoBlk blocks)
+    ZMap zint, zpro;            // (block, plane) maps: interior planes; planes 1 .. n[2] - 1
+    int2 *d_zmaps = nullptr;    // both maps in one allocation
     bool geo_ok = false;
     // red-black sweeps may push: on every face the point a ghost mirrors and
     // the point that reads that ghost have different colours

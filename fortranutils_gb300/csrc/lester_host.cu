@@ -509,6 +509,18 @@ static int build_faces(Ctx &c)
         }
         LES_CUDA(cudaMalloc(&L.d_blk, sizeof(BlkDev) * nb));
         LES_CUDA(cudaMemcpy(L.d_blk, bv.data(), sizeof(BlkDev) * nb, cudaMemcpyHostToDevice));
+        {
+            std::vector<int2> zm;
+            for (int b = 1; b <= nb; b++)
+                for (int k = 2; k <= L.n[b][2] - 1; k++) zm.push_back(make_int2(b - 1, k));
+            const int nint = (int)zm.size();
+            for (int b = 1; b <= nb; b++)
+                for (int k = 1; k <= L.n[b][2] - 1; k++) zm.push_back(make_int2(b - 1, k));
+            LES_CUDA(cudaMalloc(&L.d_zmaps, sizeof(int2) * zm.size()));
+            LES_CUDA(cudaMemcpy(L.d_zmaps, zm.data(), sizeof(int2) * zm.size(), cudaMemcpyHostToDevice));
+            L.zint = ZMap{L.d_zmaps, nint};
+            L.zpro = ZMap{L.d_zmaps + nint, (int)zm.size() - nint};
+        }
         // metric tables (code/comp_metric.F, metric_swap1/2.F)
         std::vector<char> mb(metblk_size() * nb);
         for (int b = 1; b <= nb; b++)
@@ -582,6 +594,7 @@ static void free_ctx(Ctx *c)
         cudaFree(L.d_blk);
         cudaFree(L.d_face);
         cudaFree(L.d_push);
+        cudaFree(L.d_zmaps);
         cudaFree(L.d_metblk);
         for (int s = 0; s < 6; s++) cudaFree(L.d_metface[s]);
     }
@@ -1169,7 +1182,7 @@ template <typename T> static void fast_smooth(Ctx &c, int lev, int nsweep)
             if (e0) cudaEventRecordWithFlags(e0, c.stream, fl);
             launch_rb<T>(L.d_blk, c.g.numbl, L.maxn, color, c.c.rb_omega, F.E, F.N, F.R, F.D, F.x,
                          F.b, L.rb_push ? L.d_push : nullptr, F.mf ? F.tab : MfTab<T>(), c.rb_threads,
-                         c.tot3 >= (1L << 31), L.geo_ok ? &L.geo : nullptr, c.stream);
+                         c.tot3 >= (1L << 31), L.geo_ok ? &L.geo : nullptr, L.zint, c.stream);
             if (e1) cudaEventRecordWithFlags(e1, c.stream, fl);
             if (!L.rb_push) launch_halo_fast<T>(L.d_face, L.nface, L.maxface, F.x, c.stream);
         }
@@ -1220,7 +1233,7 @@ template <typename T> static void fast_vcycle(Ctx &c)
         fast_smooth<T>(c, lev, pre);
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
         launch_resid_restrict<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lc.maxn, F.E, F.N, F.R, F.D, F.x,
-                                 F.b, F.b, mf, c.tot3 >= (1L << 31), c.stream);
+                                 F.b, F.b, mf, c.tot3 >= (1L << 31), Lc.zint, c.stream);
     }
     if (l0) {
         // levels l0..L are one contiguous slice of the multigrid arrays
@@ -1234,7 +1247,7 @@ template <typename T> static void fast_vcycle(Ctx &c)
     for (int lev = Lr - 1; lev >= 1; lev--) {
         LevelGeom &Lc = c.lv[lev + 1], &Lf = c.lv[lev];
         launch_prolong_fast<T>(Lc.d_blk, Lf.d_blk, c.g.numbl, Lf.maxn, F.x, F.x, Lf.d_push, c.tot3 >= (1L << 31),
-                               c.stream);
+                               Lc.zpro, c.stream);
         fast_smooth<T>(c, lev, pre);
     }
 }
@@ -1254,7 +1267,7 @@ static void df_cycle_tail(Ctx &c, float *e, float *rT)
 {
     LevelGeom &L1 = c.lv[1];
     const int nb = c.g.numbl;
-    launch_df_update(L1.d_blk, nb, L1.maxn, c.df_p, e, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+    launch_df_update(L1.d_blk, nb, L1.maxn, c.df_p, e, L1.d_push, c.tot3 >= (1L << 31), L1.zint, c.stream);
     if (c.df_sep)
         launch_df_resid_mf(L1.d_blk, nb, L1.maxjk, c.df_tab, c.df_sep == 2 ? nullptr : c.df_P, c.df_p, c.df_b, rT,
                            c.d_partial, c.d_small, c.stream);
@@ -1307,7 +1320,7 @@ static int ensure_cycle_graph(Ctx &c, CycleGraph &G, double *f, const double *b,
         } else if (df) {
             df_cycle_tail(c, (float *)F.x, (float *)F.b);
         } else {
-            launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+            launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), L1.zint, c.stream);
             launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                                   c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial,
                                   c.d_small, c.stream);
@@ -1453,7 +1466,7 @@ template <typename T> static int fast_solve_graph(Ctx &c, const Coef &A, double 
     } else if (df) {
         df_cycle_tail(c, (float *)F.x, (float *)F.b);
     } else {
-        launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), c.stream);
+        launch_update<T>(L1.d_blk, nb, L1.maxn, f, F.x, L1.d_push, c.tot3 >= (1L << 31), L1.zint, c.stream);
         launch_resid_outer<T>(L1.d_blk, nb, L1.maxjk, c.E64, c.N64, c.R64, c.P64, f, b,
                               c.singular ? c.d_bmean : nullptr, F.b, nullptr, c.d_partial, c.d_small, c.stream);
     }
