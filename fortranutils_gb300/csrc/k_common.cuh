@@ -10,6 +10,32 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+// Programmatic dependent launch (sm_90 and later): a kernel launched with
+// launch_pdl may start while the kernel before it on the stream drains; it
+// computes what depends on no earlier kernel of the chain (indices,
+// couplings set up long before), then pdl_wait() until the kernel before
+// it has finished and its writes are visible, then pdl_trigger() lets the
+// next one start.  Launched without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 #define LES_BCT_WALL_D 1
 #define LES_BCT_ZERO_GRAD_D 2
 #define LES_BCT_TRACTION_D 6

@@ -124,6 +124,8 @@ __global__ void k_df_update(const BlkDev *__restrict__ blk, float2 *__restrict__
     const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > n2 - 1 || j > n1 - 1 || i > n0 - 1) return;
     const Ix pp = (Ix)blk[bi].off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
+    pdl_wait();
+    pdl_trigger();
     const float2 v = df_add_f(p[pp], e[pp]);
     p[pp] = v;
     if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
@@ -149,6 +151,8 @@ __global__ void __launch_bounds__(256) k_df_resid(const BlkDev *__restrict__ blk
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
     const unsigned wpb = blockDim.x >> 5;
     double acc = 0.;
+    pdl_wait();
+    pdl_trigger();
     for (unsigned row = blockIdx.x * wpb + (threadIdx.x >> 5); row < nrow; row += gridDim.x * wpb) {
         const unsigned k = row / nj;
         const long base = b.off3 + 1 + jo * (long)(row - k * nj + 1) + ko * (long)(k + 1);
@@ -248,6 +252,8 @@ __global__ void __launch_bounds__(256) k_df_resid_mf(const BlkDev *__restrict__ 
     const long jo = b.n[0], ko = (long)b.n[0] * b.n[1];
     const unsigned wpb = blockDim.x >> 5;
     double acc = 0.;
+    pdl_wait();
+    pdl_trigger();
     for (unsigned row = blockIdx.x * wpb + (threadIdx.x >> 5); row < nrow; row += gridDim.x * wpb) {
         const unsigned k = row / nj, jr = row - k * nj;
         const long base = b.off3 + 1 + jo * (long)(jr + 1) + ko * (long)(k + 1);
@@ -282,6 +288,8 @@ __global__ void __launch_bounds__(256) k_df_resid_mf(const BlkDev *__restrict__ 
 // out[0] = the sum of the partials (out[1], ||b||^2, is left as it is)
 __global__ void k_df_sum_final(const double *__restrict__ partial, long nparts, double *__restrict__ out)
 {
+    pdl_wait();
+    pdl_trigger();
     double v[1] = {0.};
     for (long t = threadIdx.x; t < nparts; t += blockDim.x) v[0] += partial[t];
     __shared__ double r[1];
@@ -326,9 +334,9 @@ void launch_df_update(const BlkDev *blk, int nb, const int maxn[3], float2 *p, c
     for (int z0 = 0; z0 < zm.n; z0 += 65535) {
         const dim3 grid((unsigned)(maxn[0] + 29) / 32, (unsigned)(maxn[1] + 5) / 8, (unsigned)std::min(65535, zm.n - z0));
         if (wide)
-            k_df_update<long><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
+            launch_pdl(k_df_update<long>, grid, dim3(32, 8), 0, st, blk, p, e, push, zm.map, z0);
         else
-            k_df_update<int><<<grid, dim3(32, 8), 0, st>>>(blk, p, e, push, zm.map, z0);
+            launch_pdl(k_df_update<int>, grid, dim3(32, 8), 0, st, blk, p, e, push, zm.map, z0);
         count_launch(1);
     }
 }
@@ -348,8 +356,8 @@ void launch_df_resid_mf(const BlkDev *blk, int nb, long maxrow, const DfTab &t, 
 {
     const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
     const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
-    k_df_resid_mf<<<dim3(gx, nb), 256, 0, st>>>(blk, t, P, x, b, rT, partial);
-    k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
+    launch_pdl(k_df_resid_mf, dim3(gx, nb), dim3(256), 0, st, blk, t, P, x, b, rT, partial);
+    launch_pdl(k_df_sum_final, dim3(1), dim3(256), 0, st, (const double *)partial, (long)gx * nb, out);
     count_launch(2);
 }
 
@@ -361,8 +369,8 @@ void launch_df_resid(const BlkDev *blk, int nb, long maxrow, const float2 *E, co
     // warp the same number of rows
     const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
     const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
-    k_df_resid<<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, rT, partial);
-    k_df_sum_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out);
+    launch_pdl(k_df_resid, dim3(gx, nb), dim3(256), 0, st, blk, E, N, R, P, x, b, rT, partial);
+    launch_pdl(k_df_sum_final, dim3(1), dim3(256), 0, st, (const double *)partial, (long)gx * nb, out);
     count_launch(2);
 }
 

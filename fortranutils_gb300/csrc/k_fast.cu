@@ -275,6 +275,8 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
         c[5] = R[p];
         dinv = D[p];
     }
+    pdl_wait();
+    pdl_trigger();
     const T *xp = x + p;
     T s = bb[p] + c[0] * xp[-1] + c[1] * xp[1] + c[2] * xp[-jo] + c[3] * xp[jo] + c[4] * xp[-ko] + c[5] * xp[ko];
     T xo = xp[0];
@@ -321,6 +323,8 @@ __global__ void __launch_bounds__(512) k_rb_geo(const __grid_constant__ LevGeo G
         c[5] = R[p];
         dinv = D[p];
     }
+    pdl_wait();
+    pdl_trigger();
     const T *xp = x + p;
     T s = bb[p] + c[0] * xp[-1] + c[1] * xp[1] + c[2] * xp[-jo] + c[3] * xp[jo] + c[4] * xp[-ko] + c[5] * xp[ko];
     T xo = xp[0];
@@ -794,6 +798,8 @@ __global__ void __launch_bounds__(256) k_resid_restrict(
     const int i = (int)(blockIdx.x * 32 + threadIdx.x) + 2, j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > c.n[2] - 1 || j > n1 - 1 || i > n0 - 1) return;
     const Ix pc = (Ix)c.off3 + (i - 1) + (Ix)n0 * (j - 1) + (Ix)n0 * n1 * (k - 1);
+    pdl_wait();
+    pdl_trigger();
     bcoarse[pc] = rr_point<T, Ix>(bf_[bi], i, j, k, E, N, R, D, x, bb, mf);
 }
 
@@ -865,6 +871,8 @@ __global__ void __launch_bounds__(256) k_prolong8(const BlkDev *__restrict__ bc_
     const bool js = c.bc[2] == LES_BCT_INTERFACE_D, jn = c.bc[3] == LES_BCT_INTERFACE_D;
     const bool kl = c.bc[4] == LES_BCT_INTERFACE_D, kr = c.bc[5] == LES_BCT_INTERFACE_D;
     const Ix joc = c.n[0], koc = (Ix)c.n[0] * c.n[1], oc = (Ix)c.off3;
+    pdl_wait();
+    pdl_trigger();
     T v[2][2][2];
 #pragma unroll
     for (int sz = 0; sz < 2; sz++)
@@ -1157,6 +1165,8 @@ __global__ void __launch_bounds__(512) k_vtail(const VLev *__restrict__ lv, int 
 {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     T *const xg = x;
+    pdl_wait();
+    pdl_trigger();
     if (span > 0) {
         T *s = (T *)tail_smem;
         const int na = mf.E2 ? 2 : 6;
@@ -1424,7 +1434,7 @@ void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double o
         const dim3 cta(32, rows);
         const T om = (T)omega;
 #define LES_RB_GEO(MF, ONE, PUSH)                                                                            \
-    k_rb_geo<T, MF, ONE, PUSH><<<grid, cta, 0, st>>>(*geo, color, om, E, N, R, D, x, b, mf, maxnk)
+    launch_pdl(k_rb_geo<T, MF, ONE, PUSH>, grid, cta, 0, st, *geo, color, om, E, N, R, D, x, b, mf, maxnk)
         const bool one = geo->nb == 1, pu = push != nullptr;
         if (mf.E2) {
             if (one) { if (pu) LES_RB_GEO(true, true, true); else LES_RB_GEO(true, true, false); }
@@ -1441,14 +1451,16 @@ void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double o
     for (int z0 = 0; z0 < zm.n; z0 += 65535) {
         const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)std::min(65535, zm.n - z0));
         const dim3 cta(32, rows);
+        const T om = (T)omega;
         if (!wide && mf.E2)
-            k_rb<T, true, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
+            launch_pdl(k_rb<T, true, int>, grid, cta, 0, st, blk, color, om, E, N, R, D, x, b, push, mf, zm.map, z0);
         else if (!wide)
-            k_rb<T, false, int><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
+            launch_pdl(k_rb<T, false, int>, grid, cta, 0, st, blk, color, om, E, N, R, D, x, b, push, mf, zm.map, z0);
         else if (mf.E2)
-            k_rb<T, true, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
+            launch_pdl(k_rb<T, true, long>, grid, cta, 0, st, blk, color, om, E, N, R, D, x, b, push, mf, zm.map, z0);
         else
-            k_rb<T, false, long><<<grid, cta, 0, st>>>(blk, color, (T)omega, E, N, R, D, x, b, push, mf, zm.map, z0);
+            launch_pdl(k_rb<T, false, long>, grid, cta, 0, st, blk, color, om, E, N, R, D, x, b, push, mf, zm.map,
+                       z0);
         count_launch(1);
     }
 }
@@ -1500,11 +1512,11 @@ void launch_resid_restrict(const BlkDev *bc, const BlkDev *bf, int nb, const int
     for (int z0 = 0; z0 < zm_c.n; z0 += 65535) {
         const dim3 grid(nb_(maxn_c[0] - 2, 32), nb_(maxn_c[1] - 2, 8), (unsigned)std::min(65535, zm_c.n - z0));
         if (wide)
-            k_resid_restrict<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, zm_c.map,
-                                                                    z0);
+            launch_pdl(k_resid_restrict<T, long>, grid, dim3(32, 8), 0, st, bc, bf, E, N, R, D, x, b, bcoarse, mf,
+                       zm_c.map, z0);
         else
-            k_resid_restrict<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, E, N, R, D, x, b, bcoarse, mf, zm_c.map,
-                                                                   z0);
+            launch_pdl(k_resid_restrict<T, int>, grid, dim3(32, 8), 0, st, bc, bf, E, N, R, D, x, b, bcoarse, mf,
+                       zm_c.map, z0);
         count_launch(1);
     }
 }
@@ -1520,9 +1532,9 @@ void launch_prolong_fast(const BlkDev *bc, const BlkDev *bf, int nb, const int m
     for (int z0 = 0; z0 < zm_c.n; z0 += 65535) {
         const dim3 grid(nb_(mc[0] - 1, 32), nb_(mc[1] - 1, 8), (unsigned)std::min(65535, zm_c.n - z0));
         if (wide)
-            k_prolong8<T, long><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, zm_c.map, z0);
+            launch_pdl(k_prolong8<T, long>, grid, dim3(32, 8), 0, st, bc, bf, xc, xf, push, zm_c.map, z0);
         else
-            k_prolong8<T, int><<<grid, dim3(32, 8), 0, st>>>(bc, bf, xc, xf, push, zm_c.map, z0);
+            launch_pdl(k_prolong8<T, int>, grid, dim3(32, 8), 0, st, bc, bf, xc, xf, push, zm_c.map, z0);
         count_launch(1);
     }
 }
@@ -1668,12 +1680,13 @@ void launch_vtail(const VLev *lv, int l0, int L, int nb, int pre, int crs, doubl
     // the slice in shared memory where it fits (kVtailSmem, the limit
     // prepare_vtail set)
     const size_t smem = span > 0 ? (size_t)span * (mf.E2 ? 2 : 6) * sizeof(T) : 0;
-    if (smem == 0 || smem > kVtailSmem) {
-        k_vtail<T><<<1, 512, 0, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, 0, 0, cd);
-    } else {
-        k_vtail<T><<<1, 512, smem, st>>>(lv, l0, L, nb, pre, crs, (T)omega, singular, E, N, R, D, x, b, mf, start,
-                                         span, cd);
-    }
+    const T om = (T)omega;
+    if (smem == 0 || smem > kVtailSmem)
+        launch_pdl(k_vtail<T>, dim3(1), dim3(512), 0, st, lv, l0, L, nb, pre, crs, om, singular, E, N, R, D, x, b, mf,
+                   0L, 0L, cd);
+    else
+        launch_pdl(k_vtail<T>, dim3(1), dim3(512), smem, st, lv, l0, L, nb, pre, crs, om, singular, E, N, R, D, x, b,
+                   mf, start, span, cd);
     count_launch(1);
 }
 
