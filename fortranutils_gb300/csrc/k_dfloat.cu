@@ -83,6 +83,8 @@ __device__ __forceinline__ float2 split(double v)
 
 __global__ void k_df_split(const double *__restrict__ src, float2 *__restrict__ dst, long n)
 {
+    pdl_wait();
+    pdl_trigger();
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
         dst[q] = split(src[q]);
 }
@@ -91,6 +93,8 @@ __global__ void k_df_split(const double *__restrict__ src, float2 *__restrict__ 
 __global__ void k_df_split_b(const BlkDev *__restrict__ blk, const double *__restrict__ b,
                              const double *__restrict__ shift, float2 *__restrict__ dst)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev bk = blk[blockIdx.y];
     const double s0 = shift ? shift[blockIdx.y] : 0.;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < bk.ncell; q += (long)gridDim.x * blockDim.x) {
@@ -104,6 +108,8 @@ __global__ void k_df_split_b(const BlkDev *__restrict__ blk, const double *__res
 __global__ void k_df_join(const float2 *__restrict__ src, double *__restrict__ dst, long n,
                           const double *__restrict__ cycles)
 {
+    pdl_wait();
+    pdl_trigger();
     if (cycles && *cycles == 0.) return;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         const float2 v = src[q];
@@ -310,20 +316,20 @@ namespace les {
 
 void launch_df_split(const double *src, float2 *dst, long n, cudaStream_t st)
 {
-    k_df_split<<<cap_grid(n, 256, 4096), 256, 0, st>>>(src, dst, n);
+    launch_pdl(k_df_split, dim3(cap_grid(n, 256, 4096)), dim3(256), 0, st, src, dst, n);
     count_launch(1);
 }
 
 void launch_df_split_b(const BlkDev *blk, int nb, long maxcell, const double *b, const double *shift, float2 *dst,
                        cudaStream_t st)
 {
-    k_df_split_b<<<dim3(cap_grid(maxcell, 256, 2048), nb), 256, 0, st>>>(blk, b, shift, dst);
+    launch_pdl(k_df_split_b, dim3(cap_grid(maxcell, 256, 2048), nb), dim3(256), 0, st, blk, b, shift, dst);
     count_launch(1);
 }
 
 void launch_df_join(const float2 *src, double *dst, long n, const double *cycles, cudaStream_t st)
 {
-    k_df_join<<<cap_grid(n, 256, 4096), 256, 0, st>>>(src, dst, n, cycles);
+    launch_pdl(k_df_join, dim3(cap_grid(n, 256, 4096)), dim3(256), 0, st, src, dst, n, cycles);
     count_launch(1);
 }
 

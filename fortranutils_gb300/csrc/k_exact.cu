@@ -21,6 +21,8 @@
 __global__ void k_halo_pack(const FaceDev *__restrict__ fc, const double *__restrict__ var,
                             double *__restrict__ work)
 {
+    pdl_wait();
+    pdl_trigger();
     const FaceDev f = fc[blockIdx.y];
     long n = (long)f.nj * f.nk;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
@@ -32,6 +34,8 @@ __global__ void k_halo_pack(const FaceDev *__restrict__ fc, const double *__rest
 __global__ void k_halo_unpack(const FaceDev *__restrict__ fc, double *__restrict__ var,
                               const double *__restrict__ work)
 {
+    pdl_wait();
+    pdl_trigger();
     const FaceDev f = fc[blockIdx.y];
     long n = (long)f.nj * f.nk;
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
@@ -347,6 +351,8 @@ __global__ void k_prol_fine(const BlkDev *__restrict__ bc_, const BlkDev *__rest
 // order: an edge point two sides share takes the later side's value)
 __global__ void k_extrap_p(const BlkDev *__restrict__ blk, int s, double *__restrict__ p)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev b = blk[blockIdx.y];
     if (is_per_or_int(b.bc[s - 1])) return;
     const int co[2][4] = {{0, 2, 1, 1}, {0, 3, 3, 2}};
@@ -369,12 +375,16 @@ __global__ void k_extrap_p(const BlkDev *__restrict__ blk, int s, double *__rest
 __global__ void k_pref_get(const BlkDev *__restrict__ blk, const double *__restrict__ p,
                            double *__restrict__ pref)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev b = blk[0];
     pref[0] = p[IDX3(b, 2, 2, 2)];
 }
 
 __global__ void k_pref_sub(double *__restrict__ p, long n, const double *__restrict__ pref)
 {
+    pdl_wait();
+    pdl_trigger();
     double r = pref[0];
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x)
         p[q] = p[q] - r;
@@ -389,6 +399,8 @@ __global__ void k_uvw_adv(const BlkDev *__restrict__ blk, int ivar, double dtime
                           const double *__restrict__ u_int, const double *__restrict__ rho,
                           const double *__restrict__ p)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
@@ -425,6 +437,8 @@ __global__ void k_uvw_adv_f32(const BlkDev *__restrict__ blk, int ivar, float dt
                               const double *__restrict__ u_int, const double *__restrict__ rho,
                               const double *__restrict__ p)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev b = blk[blockIdx.y];
     long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
     if (q >= b.ncell) return;
@@ -563,8 +577,8 @@ void launch_halo(const FaceDev *faces, int nface, long maxface, double *var, dou
     if (nface == 0) return;
     unsigned gx = nblk(maxface, 256);
     if (gx > 64) gx = 64;
-    k_halo_pack<<<dim3(gx, nface), 256, 0, st>>>(faces, var, work);
-    k_halo_unpack<<<dim3(gx, nface), 256, 0, st>>>(faces, var, work);
+    launch_pdl(k_halo_pack, dim3(gx, nface), dim3(256), 0, st, faces, var, work);
+    launch_pdl(k_halo_unpack, dim3(gx, nface), dim3(256), 0, st, faces, var, work);
     count_launch(2);
 }
 
@@ -643,14 +657,15 @@ void launch_extrap_p(const BlkDev *blk, int nb, double *p, cudaStream_t st)
 {
     // a side of a block holds at most 64 k points in these grids; 64 CTAs of
     // 256 threads per block and side, grid-stride beyond
-    for (int s = 1; s <= 6; s++) k_extrap_p<<<dim3(64, nb), 256, 0, st>>>(blk, s, p);
+    for (int s = 1; s <= 6; s++) launch_pdl(k_extrap_p, dim3(64, nb), dim3(256), 0, st, blk, s, p);
     count_launch(6);
 }
 
 void launch_pref(const BlkDev *blk, double *p, long n, double *scratch, cudaStream_t st)
 {
-    k_pref_get<<<1, 1, 0, st>>>(blk, p, scratch);
-    k_pref_sub<<<nblk(n, 256) > 2048 ? 2048 : nblk(n, 256), 256, 0, st>>>(p, n, scratch);
+    launch_pdl(k_pref_get, dim3(1), dim3(1), 0, st, blk, p, scratch);
+    const unsigned g = nblk(n, 256) > 2048 ? 2048 : nblk(n, 256);
+    launch_pdl(k_pref_sub, dim3(g), dim3(256), 0, st, p, n, (const double *)scratch);
     count_launch(2);
 }
 
@@ -659,11 +674,11 @@ void launch_uvw_adv(const BlkDev *blk, int nb, long maxcell, int ivar, double dt
                     const double *u_int, const double *rho, const double *p, bool f32, cudaStream_t st)
 {
     if (f32)
-        k_uvw_adv_f32<<<dim3(nblk(maxcell, 256), nb), 256, 0, st>>>(blk, ivar, (float)dtime, dg, rp, dkw, u,
-                                                                  u_int, rho, p);
+        launch_pdl(k_uvw_adv_f32, dim3(nblk(maxcell, 256), nb), dim3(256), 0, st, blk, ivar, (float)dtime, dg, rp, dkw,
+                   u, u_int, rho, p);
     else
-        k_uvw_adv<<<dim3(nblk(maxcell, 128), nb), 128, 0, st>>>(blk, ivar, dtime, dg, rp, dkw, u, u_int,
-                                                              rho, p);
+        launch_pdl(k_uvw_adv, dim3(nblk(maxcell, 128), nb), dim3(128), 0, st, blk, ivar, dtime, dg, rp, dkw, u, u_int,
+                   rho, p);
     count_launch(1);
 }
 

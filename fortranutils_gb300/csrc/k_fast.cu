@@ -75,6 +75,8 @@ struct RecipJob {
 
 __global__ void k_recip(RecipJob J, long n)
 {
+    pdl_wait();
+    pdl_trigger();
     const double *s = J.src[blockIdx.y];
     double *d = J.dst[blockIdx.y];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
@@ -89,6 +91,8 @@ struct F32Job {
 
 __global__ void k_to_f32(F32Job J, long n)
 {
+    pdl_wait();
+    pdl_trigger();
     const double *s = J.src[blockIdx.y];
     float *d = J.dst[blockIdx.y];
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x)
@@ -1231,6 +1235,8 @@ __global__ void __launch_bounds__(256) k_resid_outer(
     const double *__restrict__ bb, const double *__restrict__ shift, T *__restrict__ rT,
     double *__restrict__ r64, double *__restrict__ partial)
 {
+    pdl_wait();
+    pdl_trigger();
     const BlkDev b = blk[blockIdx.y];
     double v[2] = {0., 0.};
     const double s0 = shift ? shift[blockIdx.y] : 0.;
@@ -1257,6 +1263,8 @@ __global__ void __launch_bounds__(256) k_resid_outer(
 
 __global__ void k_sum2_final(const double *__restrict__ partial, long nparts, double *__restrict__ out)
 {
+    pdl_wait();
+    pdl_trigger();
     double v[2] = {0., 0.};
     for (long t = threadIdx.x; t < nparts; t += blockDim.x) {
         v[0] += partial[2 * t];
@@ -1559,8 +1567,8 @@ void launch_resid_outer(const BlkDev *blk, int nb, long maxrow, const double *E,
     // few partials), every warp the same number of rows
     const long cap = (1216 + nb - 1) / nb, per = (maxrow + 8 * cap - 1) / (8 * cap);
     const unsigned gx = (unsigned)std::max(1L, (maxrow + 8 * per - 1) / (8 * per));
-    k_resid_outer<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, x, b, shift, rT, r64, partial);
-    k_sum2_final<<<1, 256, 0, st>>>(partial, (long)gx * nb, out2);
+    launch_pdl(k_resid_outer<T>, dim3(gx, nb), dim3(256), 0, st, blk, E, N, R, P, x, b, shift, rT, r64, partial);
+    launch_pdl(k_sum2_final, dim3(1), dim3(256), 0, st, partial, (long)gx * nb, out2);
     count_launch(2);
 }
 
@@ -1579,11 +1587,11 @@ void launch_fcg(const BlkDev *blk, int nb, long maxcell, const double *E, const 
     unsigned gx = reduce_grid(maxcell, nb);
     long np = (long)gx * nb;
     k_fcg_dot<T><<<dim3(gx, nb), 256, 0, st>>>(blk, z, q, r, partial);
-    k_sum2_final<<<1, 256, 0, st>>>(partial, np, sc);
+    launch_pdl(k_sum2_final, dim3(1), dim3(256), 0, st, partial, np, sc);
     k_fcg_dir<T><<<dim3(gx, nb), 256, 0, st>>>(blk, E, N, R, P, z, pd, q, r, sc, partial);
-    k_sum2_final<<<1, 256, 0, st>>>(partial, np, sc + 2);
+    launch_pdl(k_sum2_final, dim3(1), dim3(256), 0, st, partial, np, sc + 2);
     k_fcg_step<T><<<dim3(gx, nb), 256, 0, st>>>(blk, x, pd, q, r, rT, sc, push, partial);
-    k_sum2_final<<<1, 256, 0, st>>>(partial, np, out_rr);
+    launch_pdl(k_sum2_final, dim3(1), dim3(256), 0, st, partial, np, out_rr);
     count_launch(6);
 }
 
@@ -1609,7 +1617,7 @@ void launch_recip(const double *const *src, double *const *dst, int ntab, long n
         }
         unsigned gx = nb_(n, 256);
         if (gx > 256) gx = 256;
-        k_recip<<<dim3(gx, m), 256, 0, st>>>(J, n);
+        launch_pdl(k_recip, dim3(gx, m), dim3(256), 0, st, J, n);
         count_launch(1);
     }
 }
@@ -1625,7 +1633,7 @@ void launch_to_f32(const double *const *src, float *const *dst, int ntab, long n
         }
         unsigned gx = nb_(n, 256);
         if (gx > 256) gx = 256;
-        k_to_f32<<<dim3(gx, m), 256, 0, st>>>(J, n);
+        launch_pdl(k_to_f32, dim3(gx, m), dim3(256), 0, st, J, n);
         count_launch(1);
     }
 }
