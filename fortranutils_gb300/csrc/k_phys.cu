@@ -41,11 +41,13 @@ __global__ void __launch_bounds__(128) k_set_u_int(const BlkDev *__restrict__ bl
     int nip1 = iva == 1 ? b.n[0] : b.n[1], njp1 = iva == 1 ? b.n[1] : b.n[0], nkp1 = b.n[2];
     long io = iva == 1 ? 1 : b.n[0], jo = iva == 1 ? b.n[0] : 1, ko = (long)b.n[0] * b.n[1];
     long io_ij = io, jo_ij = jo;
-    int d1 = iva == 1 ? 0 : 2, d2 = iva == 1 ? 2 : 0;  // first side of each axis
-    int s0 = b.bc[d1];
+    // first side of the i axis and of the j axis (selects, not an index:
+    // a runtime index would put the descriptor copy in local memory)
+    int s0 = iva == 1 ? b.bc[0] : b.bc[2];
     int istart = (s0 != LES_BCT_PERIODIC_D && s0 != LES_BCT_INTERFACE_D) ? 3 : 2;
     if (i < istart) return;
-    bool wallsf = b.bc[d2] == LES_BCT_WALL_D, wallnf = b.bc[d2 + 1] == LES_BCT_WALL_D;
+    bool wallsf = (iva == 1 ? b.bc[2] : b.bc[0]) == LES_BCT_WALL_D;
+    bool wallnf = (iva == 1 ? b.bc[3] : b.bc[1]) == LES_BCT_WALL_D;
     bool walllf = b.bc[4] == LES_BCT_WALL_D, wallrf = b.bc[5] == LES_BCT_WALL_D;
     int nj = njp1 - 1, nk = nkp1 - 1;
     double st1 = iststep - 1, st2 = iststep - 2, stden = 1.0 / iststep;
