@@ -90,16 +90,23 @@ def _function_spans(text: str):
     return spans
 
 
+# kernels launched cooperatively (arguments passed by address as the FP64
+# build lays them out): their FP64 scalar parameters stay double
+_COOPERATIVE = {"k_sc1_sweep"}
+
+
 def _params(sig: str):
     """FP64 pointer parameters become converting views (one pointer, the
-    same layout).  FP64 scalars become float in device functions; in
-    kernels they stay double -- a cooperative launch passes arguments by
-    address, and an FP64 value read as an FP32 parameter is garbage -- under
-    a new name, and the body opens with a float copy under the old one.
-    Returns the signature and that opening."""
+    same layout).  FP64 scalars become float in device functions and in
+    kernels launched with <<<>>> (the launch converts the argument once on
+    the host; converting it in every thread would run on GB300's slow FP64
+    pipe); in a cooperative kernel they stay double -- the launch passes
+    arguments by address, and an FP64 value read as an FP32 parameter is
+    garbage -- under a new name, and the body opens with a float copy
+    under the old one.  Returns the signature and that opening."""
     sig = re.sub(r"const\s+double\s*\*\s*(?:__restrict__\s*)?(\w+)", lambda m: _view(m.group(1)) + " " + m.group(1),
                  sig)
-    if not sig.lstrip().startswith("__global__"):
+    if not sig.lstrip().startswith("__global__") or _func not in _COOPERATIVE:
         return re.sub(r"\bdouble\b(?!\s*\*)", "real", sig), ""
     names = re.findall(r"\bdouble\s+(\w+)\s*(?=[,)])", sig)
     sig = re.sub(r"\bdouble\s+(\w+)\s*(?=[,)])", r"double \1_fp64", sig)

@@ -50,7 +50,11 @@ void host(double d) { double e = d * 0.5; }
 """
     out = gen_f32.transform(src, "t.cu")
     assert "LdF a" in out and "double *__restrict__ o" in out
-    assert "double s_fp64" in out and "const real s = (real)s_fp64;" in out
+    # a <<<>>> kernel takes its FP64 scalars as float (converted at the launch)
+    assert "real s, int n" in out and "s_fp64" not in out
+    # a cooperative kernel keeps them double and converts once in its body
+    coop = gen_f32.transform(src.replace("void k(", "void k_sc1_sweep("), "t.cu")
+    assert "double s_fp64" in coop and "const real s = (real)s_fp64;" in coop
     assert "const LdF b = a + 1, c = a + 2;" in out
     assert "real t = 0.5f * (a[0] + b[1]) + s * c[2] + LdF(A_.x)[3] + LdF(F.y)[4];" in out
     assert "A_.z[n] = t;" in out and "1.e-30f + 2.0f * t" in out
