@@ -1065,6 +1065,9 @@ __device__ void tail_direct(const VLev &L, int nb, const CoarseDirect<T> &cd, T 
         for (long q = threadIdx.x; q < b.ncell; q += blockDim.x) {
             const long g = g0 + q;
             T acc = 0;
+            // the column reads are independent: many in flight (the inverse
+            // comes from L2), the sum in the order of h
+#pragma unroll 16
             for (int h = 0; h < cd.n; h++) acc += cd.mt[(long)h * cd.n + g] * sb[h];
             int i, j, k;
             const long p = decode_interior(b, q, i, j, k);
