@@ -242,26 +242,18 @@ __device__ __forceinline__ bool rb_decode(const BlkDev &b, unsigned q, int color
 // per-thread division.  Ix: the offset type, int when every
 // offset of the multigrid arrays is below 2^31.  Per point the operations
 // of rb_point.
+// One point of a half sweep at offset p (ij, kk: its 2-D and 1-D table
+// offsets; jo, ko: its block's strides): the couplings (separable factors
+// or arrays), then -- once the kernel before has finished -- the update
+// x[p] = x + omega (s / ap - x); returns the new value.  rb_point's
+// operations in the same order.
 template <typename T, bool MF, typename Ix>
-__global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
-                                            const T *__restrict__ E, const T *__restrict__ N,
-                                            const T *__restrict__ R, const T *__restrict__ D,
-                                            T *__restrict__ x, const T *__restrict__ bb,
-                                            const PushDev *__restrict__ push, MfTab<T> mf,
-                                            const int2 *__restrict__ zmap, int z0)
+__device__ __forceinline__ T rb_update(Ix p, Ix ij, Ix kk, Ix jo, Ix ko, T omega, const T *__restrict__ E,
+                                       const T *__restrict__ N, const T *__restrict__ R, const T *__restrict__ D,
+                                       T *__restrict__ x, const T *__restrict__ bb, const MfTab<T> &mf)
 {
-    const int2 bk = zmap[z0 + blockIdx.z];
-    const int bi = bk.x, k = bk.y;
-    const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
-    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
-    if (k > n2 - 1 || j > n1 - 1) return;
-    const int i = 2 + 2 * (int)(blockIdx.x * 32 + threadIdx.x) + ((j + k + color) & 1);
-    if (i > n0 - 1) return;
-    const Ix jo = n0, ko = (Ix)n0 * n1;
-    const Ix p = (Ix)blk[bi].off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
     T c[6], dinv;
     if (MF) {
-        const Ix ij = (Ix)blk[bi].off2 + (i - 1) + jo * (j - 1), kk = (Ix)blk[bi].off1k + (k - 1);
         const T ez = mf.Ez[kk], nz = mf.Nz[kk], r2 = mf.R2[ij];
         c[0] = mf.E2[ij - 1] * ez;
         c[1] = mf.E2[ij] * ez;
@@ -286,6 +278,28 @@ __global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int 
     T xo = xp[0];
     T xn = xo + omega * (s * dinv - xo);
     x[p] = xn;
+    return xn;
+}
+
+template <typename T, bool MF, typename Ix>
+__global__ void __launch_bounds__(512) k_rb(const BlkDev *__restrict__ blk, int color, T omega,
+                                            const T *__restrict__ E, const T *__restrict__ N,
+                                            const T *__restrict__ R, const T *__restrict__ D,
+                                            T *__restrict__ x, const T *__restrict__ bb,
+                                            const PushDev *__restrict__ push, MfTab<T> mf,
+                                            const int2 *__restrict__ zmap, int z0)
+{
+    const int2 bk = zmap[z0 + blockIdx.z];
+    const int bi = bk.x, k = bk.y;
+    const int n0 = blk[bi].n[0], n1 = blk[bi].n[1], n2 = blk[bi].n[2];
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
+    if (k > n2 - 1 || j > n1 - 1) return;
+    const int i = 2 + 2 * (int)(blockIdx.x * 32 + threadIdx.x) + ((j + k + color) & 1);
+    if (i > n0 - 1) return;
+    const Ix jo = n0, ko = (Ix)n0 * n1;
+    const Ix p = (Ix)blk[bi].off3 + (i - 1) + jo * (j - 1) + ko * (k - 1);
+    const Ix ij = (Ix)blk[bi].off2 + (i - 1) + jo * (j - 1), kk = (Ix)blk[bi].off1k + (k - 1);
+    const T xn = rb_update<T, MF, Ix>(p, ij, kk, jo, ko, omega, E, N, R, D, x, bb, mf);
     if (push && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1))
         push_ghosts(push + 6 * bi, blk[bi], i, j, k, xn, x);
 }
@@ -307,33 +321,8 @@ __global__ void __launch_bounds__(512) k_rb_geo(const __grid_constant__ LevGeo G
     if (i > n0 - 1) return;
     const int jo = n0, ko = n0 * n1;
     const int p = G.off3[bi] + (i - 1) + jo * (j - 1) + ko * (k - 1);
-    T c[6], dinv;
-    if (MF) {
-        const int ij = G.off2[bi] + (i - 1) + jo * (j - 1), kk = G.off1k[bi] + (k - 1);
-        const T ez = mf.Ez[kk], nz = mf.Nz[kk], r2 = mf.R2[ij];
-        c[0] = mf.E2[ij - 1] * ez;
-        c[1] = mf.E2[ij] * ez;
-        c[2] = mf.N2[ij - jo] * nz;
-        c[3] = mf.N2[ij] * nz;
-        c[4] = r2 * mf.Rz[kk - 1];
-        c[5] = r2 * mf.Rz[kk];
-        dinv = rcp_rn((((c[0] + c[1]) + (c[2] + c[3])) + (c[4] + c[5])));
-    } else {
-        c[0] = E[p - 1];
-        c[1] = E[p];
-        c[2] = N[p - jo];
-        c[3] = N[p];
-        c[4] = R[p - ko];
-        c[5] = R[p];
-        dinv = D[p];
-    }
-    pdl_wait();
-    pdl_trigger();
-    const T *xp = x + p;
-    T s = bb[p] + c[0] * xp[-1] + c[1] * xp[1] + c[2] * xp[-jo] + c[3] * xp[jo] + c[4] * xp[-ko] + c[5] * xp[ko];
-    T xo = xp[0];
-    T xn = xo + omega * (s * dinv - xo);
-    x[p] = xn;
+    const int ij = G.off2[bi] + (i - 1) + jo * (j - 1), kk = G.off1k[bi] + (k - 1);
+    const T xn = rb_update<T, MF, int>(p, ij, kk, jo, ko, omega, E, N, R, D, x, bb, mf);
     if (PUSH && (i == 2 || i == n0 - 1 || j == 2 || j == n1 - 1 || k == 2 || k == n2 - 1)) {
         // push_ghosts with the mirrors from the parameter
         const int cc[3] = {i - 1, j - 1, k - 1}, nn[3] = {n0, n1, n2};
