@@ -138,7 +138,7 @@ struct ZMap {
 // descriptor from memory, and a point on a mirrored face writes its ghost
 // without a dependent load.  Offsets fit 32 bits (the multigrid arrays
 // hold fewer than 2^31 points).
-constexpr int kGeoBlk = 4;
+constexpr int kGeoBlk = 8;
 struct LevGeo {
     int nb;
     int n[kGeoBlk][3];

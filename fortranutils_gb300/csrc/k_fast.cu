@@ -311,9 +311,16 @@ template <typename T, bool MF, bool ONE, bool PUSH>
 __global__ void __launch_bounds__(512) k_rb_geo(const __grid_constant__ LevGeo G, int color, T omega,
                                                 const T *__restrict__ E, const T *__restrict__ N,
                                                 const T *__restrict__ R, const T *__restrict__ D,
-                                                T *__restrict__ x, const T *__restrict__ bb, MfTab<T> mf, int maxnk)
+                                                T *__restrict__ x, const T *__restrict__ bb, MfTab<T> mf,
+                                                const int2 *__restrict__ zmap)
 {
-    const int bi = ONE ? 0 : (int)blockIdx.z / maxnk, k = (int)blockIdx.z - bi * maxnk + 2;
+    // one block: plane 2 + bz; several: the (block, plane) map
+    int bi = 0, k = (int)blockIdx.z + 2;
+    if (!ONE) {
+        const int2 bk = zmap[blockIdx.z];
+        bi = bk.x;
+        k = bk.y;
+    }
     const int n0 = G.n[bi][0], n1 = G.n[bi][1], n2 = G.n[bi][2];
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y) + 2;
     if (k > n2 - 1 || j > n1 - 1) return;
@@ -1428,13 +1435,12 @@ void launch_rb(const BlkDev *blk, int nb, const int maxn[3], int color, double o
                const MfTab<T> &mf, int threads, bool wide, const LevGeo *geo, ZMap zm, cudaStream_t st)
 {
     const int rows = (threads == 128 || threads == 512) ? threads / 32 : 8;
-    const int maxnk = maxn[2] - 2;
-    if (geo && !wide && maxnk * geo->nb <= 65535) {
-        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)(maxnk * geo->nb));
+    if (geo && !wide && zm.n <= 65535) {
+        const dim3 grid(nb_((maxn[0] - 1) / 2, 32), nb_(maxn[1] - 2, rows), (unsigned)zm.n);
         const dim3 cta(32, rows);
         const T om = (T)omega;
 #define LES_RB_GEO(MF, ONE, PUSH)                                                                            \
-    launch_pdl(k_rb_geo<T, MF, ONE, PUSH>, grid, cta, 0, st, *geo, color, om, E, N, R, D, x, b, mf, maxnk)
+    launch_pdl(k_rb_geo<T, MF, ONE, PUSH>, grid, cta, 0, st, *geo, color, om, E, N, R, D, x, b, mf, zm.map)
         const bool one = geo->nb == 1, pu = push != nullptr;
         if (mf.E2) {
             if (one) { if (pu) LES_RB_GEO(true, true, true); else LES_RB_GEO(true, true, false); }
