@@ -49,12 +49,12 @@ EXACT = 0
 WORKLOAD = ("variable-density temporal mixing layer 256x192x128, tanh y-stretch beta 2, slip y "
             "walls, WALE Cw 0.5, density ratio 2, full lester_step, Poisson to 1e-8")
 # DRAM bytes (ncu dram__bytes_read.sum + dram__bytes_write.sum) per launch
-# of the timed kernels on the mixing-layer workload: the level-1 k_rb<float>
-# half sweep from one capture at full size (52.0 MB read + 0.27 MB written,
-# against 50.3 MB algorithmic); the tile-pipeline scalar sweep from one
+# of the timed kernels on the mixing-layer workload: the level-1 half sweep
+# (k_rb_geo<float>) from one capture at full size (52.0 MB read + 0.16 MB
+# written, against 50.3 MB algorithmic); the tile-pipeline scalar sweep from one
 # capture at 128x96x64 (53.1 MB read + 0.08 MB written for 0.786 M cells)
 # scaled by cells to 256x192x128
-TRAFFIC = {"rb": 52.18e6, "sweep": 53.22e6 * 6291456 / 786432}
+TRAFFIC = {"rb": 52.17e6, "sweep": 53.22e6 * 6291456 / 786432}
 # algorithmic bytes per interior cell of one launch: a red-black half sweep
 # (one colour per launch, FP32) must read x of both colours (its own points
 # and their neighbours of the other colour: 4 B per cell), b of its colour
@@ -63,7 +63,7 @@ TRAFFIC = {"rb": 52.18e6, "sweep": 53.22e6 * 6291456 / 786432}
 # u, v, w, rho, gamsc1, gamlam and writes the new sc1 and hsc1 (10 FP32
 # arrays)
 ALG_BYTES = {"rb": 8.0, "sweep": 40.0}
-KERNEL_NAMES = {"rb": "k_rb<float> level-1 red-black SOR half sweep",
+KERNEL_NAMES = {"rb": "k_rb_geo<float> level-1 red-black SOR half sweep",
                 "sweep": "set_sc1 in-place scalar sweep (one launch per step)"}
 # the level-1 smoother as shared-memory tiles (k_rb_tile, when the level
 # allows it): one launch is a full sweep, both colours (12 B per cell)
